@@ -1,0 +1,177 @@
+/*
+ * psmma.h -- C ABI of the GB300 structured multiply library (libpsmma_gb300.so).
+ *
+ * The library computes the PSMMA structured products on one GPU:
+ *
+ *   psmma_cauchy   Q := alpha * A * H + beta * Q,  H(i,j) = U(i)*V(j) / (D(i) - F(j))
+ *   psmma_toeplitz Q := alpha * A * H + beta * Q,  H(i,j) = G(K + j - i)          (1-based)
+ *   psmma_hankel   Q := alpha * A * H + beta * Q,  H(i,j) = G(i + j - 1)          (1-based)
+ *   pzmdftl        C := alpha * F * B + beta * C,  F(j,k) = w^((j-1)(k-1)), w = exp(-2*pi*i/N)
+ *
+ * A and Q are N-by-K, H is K-by-K, F is N-by-N, B and C are N-by-K.  All matrices are
+ * column-major (Fortran order) with an explicit leading dimension, exactly as the
+ * reference's local arrays are.  H and F are never stored: every thread block rebuilds
+ * the tile it needs from the O(K) generators.
+ *
+ * Generators keep the reference's storage conventions:
+ *   Cauchy   gen is a (ldgen x 4) column-major array [D | F | U | V], ldgen >= K
+ *            (PSMMA_CAUCHY's B(LDB,4); psmma_cauchy.f90:22, Auxil_2p5D.f90:138-141).
+ *   Toeplitz gen has 2K-1 entries: gen[0..K-1] is the first column from bottom to top,
+ *            gen[K-1] the diagonal, gen[K..2K-2] the first row after the diagonal
+ *            (psmma_toeplitz.f90:27-32).
+ *   Hankel   gen has 2K-1 entries: gen[0..K-1] is the first row, gen[K..2K-2] the last
+ *            column below the anti-diagonal (psmma_hankel.f90:27-32).
+ *   DFT      the root of unity is implied by N, as in PZMDFTL (pzmdftL.f90:325-326).
+ *
+ * Entry points taking device pointers enqueue on `stream` (a cudaStream_t, NULL for the
+ * legacy default stream) and return without synchronising.  The *_host entry points take
+ * host pointers, copy to the device, run and copy back before returning; they are the
+ * drop-in for the reference's host-array calls.
+ *
+ * Return value: PSMMA_OK (0) or a negative status.  Argument errors return -INFO with the
+ * INFO numbering of the reference routine that performs the same check (PXERBLA codes of
+ * PSCAUCHY_COMPUTE, pscauchy_compute.f90:234-255, and PZMDFTL, pzmdftL.f90:182-205);
+ * the reference prints these and returns nothing, this library returns them.
+ */
+#ifndef PSMMA_GB300_H
+#define PSMMA_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------------------ */
+#define PSMMA_OK              0
+/* -2 (N<0), -3 (K<0), -9 (LDA), -14 (LDQ): PSCAUCHY_COMPUTE INFO numbering.            */
+/* -1 (N<0), -2 (K<0), -7 (LDB), -10 (LDC): PZMDFTL INFO numbering.                     */
+#define PSMMA_EGEN          -108  /* generator pointer NULL or ldgen too small            */
+#define PSMMA_ENULL         -109  /* matrix pointer NULL for a non-empty operand           */
+#define PSMMA_ENOMEM        -110  /* device or pinned-host allocation failed              */
+#define PSMMA_EDEVICE       -111  /* CUDA launch/runtime error                            */
+#define PSMMA_ETIMEDOUT     -112  /* a bounded device-side wait expired                   */
+#define PSMMA_ESINGULAR     -113  /* split path: a Cauchy denominator D(i)-F(j) is zero   */
+#define PSMMA_EUNSUPPORTED  -114  /* option combination not supported                     */
+#define PSMMA_EWORKSPACE    -115  /* caller workspace smaller than psmma_workspace_size   */
+#define PSMMA_ERANGE        -116  /* split path: non-finite input or exponent out of range */
+
+/* ---- options ------------------------------------------------------------------------ */
+#define PSMMA_PREC_FP64   0   /* plain path: FP64 tensor-core MMA, H tile generated in smem  */
+#define PSMMA_PREC_SPLIT  1   /* split path: exact modular slices on BF16 tensor cores (tcgen05),
+                                 FP64 scaling and recombination (Cauchy, Toeplitz, Hankel)    */
+
+typedef struct psmma_opts {
+  int    precision;   /* PSMMA_PREC_FP64 (default) or PSMMA_PREC_SPLIT                        */
+  int    n_moduli;    /* split path: number of moduli, 0 = default (14); 8..20                 */
+  void*  work;        /* optional caller-owned device workspace (NULL: library-owned pool)      */
+  size_t lwork;       /* size of `work` in bytes                                               */
+  int    reserved[8]; /* must be zero                                                          */
+} psmma_opts;
+
+/* Interleaved complex double, layout-compatible with cuDoubleComplex and COMPLEX*16. */
+typedef struct psmma_complex {
+  double re, im;
+} psmma_complex;
+
+/* Kinds for psmma_workspace_size. */
+#define PSMMA_KIND_CAUCHY   0
+#define PSMMA_KIND_TOEPLITZ 1
+#define PSMMA_KIND_HANKEL   2
+#define PSMMA_KIND_DFT      3
+
+/* ---- device-pointer entry points --------------------------------------------------- */
+
+/* Replaces PSMMA_CAUCHY(N,K,ALPHA,A,IA,JA,DESCA,B,LDB,BETA,Q,IQ,JQ,DESCQ,WORK,REDIST)
+ * (psmma_cauchy.f90:2-3) and its ring kernel PSCAUCHY_COMPUTE (pscauchy_compute.f90:2-3).
+ * DESCA/DESCQ become lda/ldq, B/LDB become gen/ldgen, WORK becomes opts->work. */
+int psmma_cauchy(int n, int k, double alpha, const double* A, int lda,
+                 const double* gen, int ldgen, double beta, double* Q, int ldq,
+                 const psmma_opts* opts, void* stream);
+
+/* Replaces PSMMA_TOEPLITZ(...) (psmma_toeplitz.f90:2-3) / PSTOEPLITZ_COMPUTE
+ * (pstoeplitz_compute.f90:2-3); gen has ldgen >= 2k-1 entries. */
+int psmma_toeplitz(int n, int k, double alpha, const double* A, int lda,
+                   const double* gen, int ldgen, double beta, double* Q, int ldq,
+                   const psmma_opts* opts, void* stream);
+
+/* Replaces PSMMA_HANKEL(...) (psmma_hankel.f90:2-3) / PSHANKEL_COMPUTE
+ * (pshankel_compute.f90:2-3); gen has ldgen >= 2k-1 entries. */
+int psmma_hankel(int n, int k, double alpha, const double* A, int lda,
+                 const double* gen, int ldgen, double beta, double* Q, int ldq,
+                 const psmma_opts* opts, void* stream);
+
+/* Replaces PZMDFTL(N,K,NB,KB,ALPHA,B,LDB,BETA,C,LDC,IMROW,IMCOL,WORK,RWORK)
+ * (pzmdftL.f90:1-2): C := alpha*F*B + beta*C with F the N-by-N DFT matrix on the left.
+ * The reference's ALPHA and BETA are real (DOUBLE PRECISION); so are these. */
+int pzmdftl(int n, int k, double alpha, const psmma_complex* B, int ldb,
+            double beta, psmma_complex* C, int ldc, const psmma_opts* opts, void* stream);
+
+/* Replaces PZMDFTL1 (pzmdftL1.f90:1-2), the RRQR variant of PZMDFTL.  Both reference
+ * routines compute the same product up to their 1e-13 truncation; on the GPU the DFT
+ * tile is generated exactly, so this is the same computation as pzmdftl. */
+int pzmdftl1(int n, int k, double alpha, const psmma_complex* B, int ldb,
+             double beta, psmma_complex* C, int ldc, const psmma_opts* opts, void* stream);
+
+/* ---- host-pointer entry points (copy in, compute, copy out, synchronise) ------------ */
+int psmma_cauchy_host(int n, int k, double alpha, const double* A, int lda,
+                      const double* gen, int ldgen, double beta, double* Q, int ldq,
+                      const psmma_opts* opts);
+int psmma_toeplitz_host(int n, int k, double alpha, const double* A, int lda,
+                        const double* gen, int ldgen, double beta, double* Q, int ldq,
+                        const psmma_opts* opts);
+int psmma_hankel_host(int n, int k, double alpha, const double* A, int lda,
+                      const double* gen, int ldgen, double beta, double* Q, int ldq,
+                      const psmma_opts* opts);
+int pzmdftl_host(int n, int k, double alpha, const psmma_complex* B, int ldb,
+                 double beta, psmma_complex* C, int ldc, const psmma_opts* opts);
+
+/* ---- Fortran-ABI entry points ------------------------------------------------------ */
+/* Same argument lists as the reference's Fortran subroutines, passed by reference with
+ * gfortran's trailing-underscore names, on host arrays.  The descriptors must describe a
+ * 1x1 process grid (the whole matrix is local): only DESC(9) (LLD) is read.  IA, JA, IQ,
+ * JQ must be 1, WORK is not touched and REDIST is ignored (there is nothing to
+ * redistribute on one device).  The INFO-style status of the last call is returned by
+ * psmma_last_status(). */
+void psmma_cauchy_(const int* n, const int* k, const double* alpha, const double* A,
+                   const int* ia, const int* ja, const int* desca, const double* B,
+                   const int* ldb, const double* beta, double* Q, const int* iq,
+                   const int* jq, const int* descq, double* work, const int* redist);
+void psmma_toeplitz_(const int* n, const int* k, const double* alpha, const double* A,
+                     const int* ia, const int* ja, const int* desca, const double* B,
+                     const int* ldb, const double* beta, double* Q, const int* iq,
+                     const int* jq, const int* descq, double* work, const int* redist);
+void psmma_hankel_(const int* n, const int* k, const double* alpha, const double* A,
+                   const int* ia, const int* ja, const int* desca, const double* B,
+                   const int* ldb, const double* beta, double* Q, const int* iq,
+                   const int* jq, const int* descq, double* work, const int* redist);
+void pzmdftl_(const int* n, const int* k, const int* nb, const int* kb, const double* alpha,
+              const psmma_complex* B, const int* ldb, const double* beta, psmma_complex* C,
+              const int* ldc, const int* imrow, const int* imcol, psmma_complex* work,
+              double* rwork);
+void pzmdftl1_(const int* n, const int* k, const int* nb, const int* kb, const double* alpha,
+               const psmma_complex* B, const int* ldb, const double* beta, psmma_complex* C,
+               const int* ldc, const int* imrow, const int* imcol, psmma_complex* work,
+               double* rwork);
+int psmma_last_status(void);
+
+/* ---- workspace and housekeeping ----------------------------------------------------- */
+
+/* Bytes of device workspace a call with these sizes and options needs (0 for the FP64
+ * path).  Pass a buffer at least this large in opts->work to avoid library allocation. */
+size_t psmma_workspace_size(int kind, int n, int k, const psmma_opts* opts);
+
+/* Frees the library-owned workspace pools of the current device. */
+void psmma_release_workspace(void);
+
+/* Text for a status code (static storage). */
+const char* psmma_status_string(int status);
+
+/* Library version string. */
+const char* psmma_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PSMMA_GB300_H */

@@ -1,0 +1,170 @@
+"""psmma_git_gb300 -- PSMMA's structured multiply on one GB300 (sm_103a).
+
+Python mirror of the reference's public routines, calling the C ABI of
+``libpsmma_gb300.so`` (include/psmma.h) through ctypes:
+
+* :func:`psmma_cauchy`   -- PSMMA_CAUCHY   (psmma_cauchy.f90:2-3):   Q := alpha*A*H + beta*Q,
+  H(i,j) = U(i)*V(j)/(D(i)-F(j)), generators ``[D|F|U|V]`` as a (ldgen x 4) array.
+* :func:`psmma_toeplitz` -- PSMMA_TOEPLITZ (psmma_toeplitz.f90:2-3): H(i,j) = G(K+j-i).
+* :func:`psmma_hankel`   -- PSMMA_HANKEL   (psmma_hankel.f90:2-3):   H(i,j) = G(i+j-1).
+* :func:`pzmdftl` / :func:`pzmdftl1` -- PZMDFTL / PZMDFTL1 (pzmdftL.f90:1-2):
+  C := alpha*F*B + beta*C with F the N-by-N DFT matrix, w = exp(-2*pi*i/N).
+
+Matrices are column-major.  Device operands are ``torch`` CUDA tensors with unit row
+stride (``t.stride(0) == 1``, leading dimension ``t.stride(1)``), as made by
+:func:`fortran_empty`; host operands are Fortran-ordered ``numpy`` arrays, which take the
+copy-in/compute/copy-out path.  Errors raise :class:`PsmmaError` carrying the status code
+(argument errors use the reference's PXERBLA INFO numbers, negated).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from ._lib import (KIND_CAUCHY, KIND_DFT, KIND_HANKEL, KIND_TOEPLITZ, PREC_FP64, PREC_SPLIT,
+                   PsmmaError, PsmmaOpts, load, status_string)
+
+__all__ = [
+    "psmma_cauchy", "psmma_toeplitz", "psmma_hankel", "pzmdftl", "pzmdftl1", "fortran_empty",
+    "workspace_size", "PsmmaError", "PREC_FP64", "PREC_SPLIT", "load", "status_string",
+    "make_opts",
+]
+
+_PREC = {"fp64": PREC_FP64, "split": PREC_SPLIT, PREC_FP64: PREC_FP64, PREC_SPLIT: PREC_SPLIT}
+
+
+def make_opts(precision="fp64", n_moduli: int = 0, work=None, lwork: int = 0) -> PsmmaOpts:
+    o = PsmmaOpts()
+    o.precision = _PREC[precision]
+    o.n_moduli = n_moduli
+    if work is not None:
+        o.work = C.c_void_p(work.data_ptr())
+        o.lwork = lwork or work.numel() * work.element_size()
+    return o
+
+
+def fortran_empty(n: int, k: int, dtype=None, device="cuda", ld: int | None = None):
+    """A column-major (n x k) torch tensor with leading dimension ``ld`` (default n)."""
+    import torch
+    ld = n if ld is None else ld
+    dtype = dtype or torch.float64
+    base = torch.empty((k, max(ld, 1)), dtype=dtype, device=device)
+    return base.t()[:n, :]
+
+
+def _is_torch(x) -> bool:
+    return type(x).__module__.startswith("torch")
+
+
+def _dev(x, name: str, dtype):
+    """(pointer, leading dimension) of a column-major CUDA tensor."""
+    import torch
+    if not x.is_cuda:
+        raise ValueError(f"{name}: expected a CUDA tensor")
+    if x.dtype != dtype:
+        raise TypeError(f"{name}: expected {dtype}, got {x.dtype}")
+    if x.dim() == 1:
+        return x.data_ptr(), x.numel()
+    if x.dim() != 2 or (x.stride(0) != 1 and x.shape[0] > 1):
+        raise ValueError(f"{name}: expected a column-major 2-D tensor (stride(0) == 1)")
+    ld = x.stride(1) if x.shape[1] > 1 else max(x.shape[0], 1)
+    return x.data_ptr(), ld
+
+
+def _host(x, name: str, dtype):
+    if not isinstance(x, np.ndarray) or x.dtype != dtype:
+        raise TypeError(f"{name}: expected a numpy {np.dtype(dtype)} array")
+    if x.ndim == 1:
+        return x.ctypes.data, x.size
+    if not x.flags.f_contiguous and x.shape[0] > 1 and x.shape[1] > 1:
+        # column-major with a leading dimension: a Fortran-ordered view of a larger array
+        if x.strides[0] != x.itemsize:
+            raise ValueError(f"{name}: expected a column-major (Fortran-ordered) array")
+    ld = x.strides[1] // x.itemsize if x.shape[1] > 1 else max(x.shape[0], 1)
+    return x.ctypes.data, ld
+
+
+def _stream_ptr(stream):
+    if stream is None:
+        import torch
+        return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    if isinstance(stream, int):
+        return C.c_void_p(stream)
+    return C.c_void_p(stream.cuda_stream)
+
+
+def _real(kind: int, name: str, n, k, alpha, A, gen, beta, Q, precision, n_moduli, stream, work):
+    lib = load()
+    opts = make_opts(precision, n_moduli, work)
+    if _is_torch(Q):
+        import torch
+        pa, lda = _dev(A, "A", torch.float64) if A is not None else (0, max(1, n))
+        pg, ldg = (0, 0) if gen is None else _dev(gen, "gen", torch.float64)
+        if gen is not None and kind == KIND_CAUCHY and gen.dim() == 1:
+            ldg = gen.numel() // 4
+        pq, ldq = _dev(Q, "Q", torch.float64)
+        fn = getattr(lib, name)
+        st = fn(n, k, float(alpha), C.c_void_p(pa), lda, C.c_void_p(pg), ldg, float(beta),
+                C.c_void_p(pq), ldq, C.byref(opts), _stream_ptr(stream))
+    else:
+        pa, lda = _host(A, "A", np.float64) if A is not None else (0, max(1, n))
+        pg, ldg = (0, 0) if gen is None else _host(gen, "gen", np.float64)
+        if gen is not None and kind == KIND_CAUCHY and gen.ndim == 1:
+            ldg = gen.size // 4
+        pq, ldq = _host(Q, "Q", np.float64)
+        fn = getattr(lib, name + "_host")
+        st = fn(n, k, float(alpha), C.c_void_p(pa), lda, C.c_void_p(pg), ldg, float(beta),
+                C.c_void_p(pq), ldq, C.byref(opts))
+    if st != 0:
+        raise PsmmaError(st, name)
+    return Q
+
+
+def psmma_cauchy(n, k, alpha, A, gen, beta, Q, *, precision="fp64", n_moduli=0, stream=None, work=None):
+    """Q := alpha*A*H + beta*Q with H(i,j) = U(i)*V(j)/(D(i)-F(j)), gen = [D|F|U|V]."""
+    return _real(KIND_CAUCHY, "psmma_cauchy", n, k, alpha, A, gen, beta, Q, precision, n_moduli, stream, work)
+
+
+def psmma_toeplitz(n, k, alpha, A, gen, beta, Q, *, precision="fp64", n_moduli=0, stream=None, work=None):
+    """Q := alpha*A*H + beta*Q with H(i,j) = G(K+j-i) (1-based), len(G) = 2K-1."""
+    return _real(KIND_TOEPLITZ, "psmma_toeplitz", n, k, alpha, A, gen, beta, Q, precision, n_moduli, stream, work)
+
+
+def psmma_hankel(n, k, alpha, A, gen, beta, Q, *, precision="fp64", n_moduli=0, stream=None, work=None):
+    """Q := alpha*A*H + beta*Q with H(i,j) = G(i+j-1) (1-based), len(G) = 2K-1."""
+    return _real(KIND_HANKEL, "psmma_hankel", n, k, alpha, A, gen, beta, Q, precision, n_moduli, stream, work)
+
+
+def _dft(name: str, n, k, alpha, B, beta, Cm, stream, work):
+    lib = load()
+    opts = make_opts("fp64", 0, work)
+    if _is_torch(Cm):
+        import torch
+        pb, ldb = _dev(B, "B", torch.complex128) if B is not None else (0, max(1, n))
+        pc, ldc = _dev(Cm, "C", torch.complex128)
+        st = getattr(lib, name)(n, k, float(alpha), C.c_void_p(pb), ldb, float(beta), C.c_void_p(pc),
+                                ldc, C.byref(opts), _stream_ptr(stream))
+    else:
+        pb, ldb = _host(B, "B", np.complex128) if B is not None else (0, max(1, n))
+        pc, ldc = _host(Cm, "C", np.complex128)
+        st = lib.pzmdftl_host(n, k, float(alpha), C.c_void_p(pb), ldb, float(beta), C.c_void_p(pc),
+                              ldc, C.byref(opts))
+    if st != 0:
+        raise PsmmaError(st, name)
+    return Cm
+
+
+def pzmdftl(n, k, alpha, B, beta, Cm, *, stream=None, work=None):
+    """C := alpha*F*B + beta*C, F(j,l) = exp(-2*pi*i*(j-1)*(l-1)/N), F on the left."""
+    return _dft("pzmdftl", n, k, alpha, B, beta, Cm, stream, work)
+
+
+def pzmdftl1(n, k, alpha, B, beta, Cm, *, stream=None, work=None):
+    """PZMDFTL1 (RRQR variant in the reference); the same exact product here."""
+    return _dft("pzmdftl1", n, k, alpha, B, beta, Cm, stream, work)
+
+
+def workspace_size(kind: int, n: int, k: int, precision="fp64", n_moduli: int = 0) -> int:
+    opts = make_opts(precision, n_moduli)
+    return int(load().psmma_workspace_size(kind, n, k, C.byref(opts)))

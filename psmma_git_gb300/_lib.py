@@ -1,0 +1,111 @@
+"""ctypes binding of libpsmma_gb300.so (the C ABI declared in include/psmma.h).
+
+The library is loaded from the package directory.  There is no fallback: if the shared
+library is missing or lacks a symbol, loading raises, so no computation can silently run
+anywhere but in the CUDA kernels.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import re
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "libpsmma_gb300.so"
+HEADER = PKG.parent / "include" / "psmma.h"
+
+PSMMA_OK = 0
+PSMMA_EGEN = -108
+PSMMA_ENULL = -109
+PSMMA_ENOMEM = -110
+PSMMA_EDEVICE = -111
+PSMMA_ETIMEDOUT = -112
+PSMMA_ESINGULAR = -113
+PSMMA_EUNSUPPORTED = -114
+PSMMA_EWORKSPACE = -115
+PSMMA_ERANGE = -116
+
+PREC_FP64 = 0
+PREC_SPLIT = 1
+
+KIND_CAUCHY, KIND_TOEPLITZ, KIND_HANKEL, KIND_DFT = 0, 1, 2, 3
+
+
+class PsmmaOpts(C.Structure):
+    _fields_ = [
+        ("precision", C.c_int),
+        ("n_moduli", C.c_int),
+        ("work", C.c_void_p),
+        ("lwork", C.c_size_t),
+        ("reserved", C.c_int * 8),
+    ]
+
+
+_p = C.c_void_p
+_i = C.c_int
+_d = C.c_double
+_ip = C.POINTER(C.c_int)
+_dp = C.POINTER(C.c_double)
+_op = C.POINTER(PsmmaOpts)
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "psmma_cauchy": (_i, [_i, _i, _d, _p, _i, _p, _i, _d, _p, _i, _op, _p]),
+    "psmma_toeplitz": (_i, [_i, _i, _d, _p, _i, _p, _i, _d, _p, _i, _op, _p]),
+    "psmma_hankel": (_i, [_i, _i, _d, _p, _i, _p, _i, _d, _p, _i, _op, _p]),
+    "pzmdftl": (_i, [_i, _i, _d, _p, _i, _d, _p, _i, _op, _p]),
+    "pzmdftl1": (_i, [_i, _i, _d, _p, _i, _d, _p, _i, _op, _p]),
+    "psmma_cauchy_host": (_i, [_i, _i, _d, _p, _i, _p, _i, _d, _p, _i, _op]),
+    "psmma_toeplitz_host": (_i, [_i, _i, _d, _p, _i, _p, _i, _d, _p, _i, _op]),
+    "psmma_hankel_host": (_i, [_i, _i, _d, _p, _i, _p, _i, _d, _p, _i, _op]),
+    "pzmdftl_host": (_i, [_i, _i, _d, _p, _i, _d, _p, _i, _op]),
+    "psmma_cauchy_": (None, [_ip, _ip, _dp, _p, _ip, _ip, _ip, _p, _ip, _dp, _p, _ip, _ip, _ip, _p, _ip]),
+    "psmma_toeplitz_": (None, [_ip, _ip, _dp, _p, _ip, _ip, _ip, _p, _ip, _dp, _p, _ip, _ip, _ip, _p, _ip]),
+    "psmma_hankel_": (None, [_ip, _ip, _dp, _p, _ip, _ip, _ip, _p, _ip, _dp, _p, _ip, _ip, _ip, _p, _ip]),
+    "pzmdftl_": (None, [_ip, _ip, _ip, _ip, _dp, _p, _ip, _dp, _p, _ip, _ip, _ip, _p, _p]),
+    "pzmdftl1_": (None, [_ip, _ip, _ip, _ip, _dp, _p, _ip, _dp, _p, _ip, _ip, _ip, _p, _p]),
+    "psmma_last_status": (_i, []),
+    "psmma_workspace_size": (C.c_size_t, [_i, _i, _i, _op]),
+    "psmma_release_workspace": (None, []),
+    "psmma_status_string": (C.c_char_p, [_i]),
+    "psmma_version": (C.c_char_p, []),
+}
+
+
+def header_symbols() -> list[str]:
+    """Function names declared in include/psmma.h (used by the export test)."""
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = re.findall(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b([a-z_][a-z0-9_]*)\s*\(", text, flags=re.M)
+    return sorted(set(n for n in names if n.startswith(("psmma", "pzmdft"))))
+
+
+_lib = None
+
+
+def load() -> C.CDLL:
+    """Loads the in-tree library and binds every C-ABI symbol; raises if anything is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise RuntimeError(
+            f"{LIB_PATH} is missing: build it with `python -m psmma_git_gb300.build` "
+            "(there is no CPU fallback)")
+    lib = C.CDLL(str(LIB_PATH))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)  # AttributeError if the symbol is not exported
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def status_string(st: int) -> str:
+    return load().psmma_status_string(st).decode()
+
+
+class PsmmaError(RuntimeError):
+    def __init__(self, status: int, where: str):
+        self.status = status
+        super().__init__(f"{where}: status {status} ({status_string(status)})")

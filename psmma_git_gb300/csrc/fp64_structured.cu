@@ -1,0 +1,311 @@
+// FP64 plain path: structured multiply on FP64 tensor-core MMA (mma.sync .f64) with the
+// structured operand generated tile by tile in shared memory, never read from HBM.
+//
+// Real kinds (Cauchy, Toeplitz, Hankel):  Q(n x k) = alpha * A(n x k) * H(k x k) + beta * Q
+//   A streams from HBM (column-major, lda); H's tile is rebuilt from the generators.
+//   Tile formulas follow the reference's tile builders:
+//     Cauchy   H(i,j) = U(i)*V(j) / (D(i)-F(j))     Cauchylowrank.f90:509-521 (Cauchylike),
+//              generator columns [D,F,U,V]          Auxil_2p5D.f90:138-141 (ConstCauchy)
+//     Toeplitz H(i,j) = G(K+j-i)                    Auxil_2p5D.f90:224-231 (ConstToeplitz)
+//     Hankel   H(i,j) = G(i+j-1)                    Auxil_2p5D.f90:309-316 (ConstHankel)
+//   The reference's ring over process columns (pscauchy_compute.f90:355-423) visits every
+//   k-block of A once; here the k-loop of one thread block does the same.
+//
+// DFT (pzmdftL.f90): C(n x k) = alpha * F(n x n) * B(n x k) + beta * C, F(j,l) = w^(j*l).
+//   Viewing interleaved complex B and C as real (2n x k) column-major arrays with twice the
+//   leading dimension, the product is the real GEMM C' = F' * B' where F' (2n x 2n) holds
+//   the 2x2 blocks [[Re F, -Im F], [Im F, Re F]].  F' tiles are generated from a table
+//   w^t, t = 0..n-1, indexed by the exact integer (j*l) mod n.
+#include "psmma_internal.h"
+
+namespace psmma {
+
+// ------------------------------------------------------------------------------------
+// Tile geometry.  256 threads = 8 warps as 2 (M) x 4 (N); warp tile 64 x 32.
+// ------------------------------------------------------------------------------------
+constexpr int F64_BM = 128;
+constexpr int F64_BN = 128;
+constexpr int F64_BK = 16;
+constexpr int F64_THREADS = 256;
+constexpr int F64_WM = 64;                  // warp tile rows
+constexpr int F64_WN = 32;                  // warp tile cols
+constexpr int F64_MT = F64_WM / 16;         // m16 fragments per warp
+constexpr int F64_NT = F64_WN / 8;          // n8 fragments per warp
+constexpr int F64_APAD = F64_BM + 8;        // smem row stride (doubles) of the A tile [k][i]
+constexpr int F64_BPAD = F64_BN + 8;        // smem row stride (doubles) of the B tile [k][j]
+constexpr int F64_SMEM_A = F64_BK * F64_APAD;
+constexpr int F64_SMEM_B = F64_BK * F64_BPAD;
+constexpr size_t F64_SMEM_BYTES = 2 * (F64_SMEM_A + F64_SMEM_B) * sizeof(double);
+
+struct F64Args {
+  int M, N, K;               // GEMM sizes of the real view
+  double alpha, beta;
+  const double* X; long ldx;  // streamed operand (A for real kinds, B' for DFT)
+  double* C; long ldc;        // output (Q or C')
+  // generator data
+  const double* gen; long ldgen;   // Cauchy [D|F|U|V] columns / Toeplitz-Hankel vector
+  int korder;                      // order K of H (real kinds) or n (DFT)
+  const double2* wtab;             // DFT: w^t table, t = 0..n-1
+};
+
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem, bool pred) {
+  unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  int sz = pred ? 8 : 0;
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(s), "l"(gmem), "r"(sz));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::); }
+
+// m16n8k16 FP64 MMA.  Fragment layout (g = lane/4, t = lane%4):
+//   a[r]: A[g + 8*(r&1)][t + 4*(r>>1)], r = 0..7
+//   b[r]: B[t + 4*r][g],                r = 0..3
+//   c[0..1]: C[g][2t + {0,1}], c[2..3]: C[g+8][2t + {0,1}]
+__device__ __forceinline__ void dmma16816(double (&c)[4], const double (&a)[8], const double (&b)[4]) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f64.f64.f64.f64 {%0,%1,%2,%3}, "
+      "{%4,%5,%6,%7,%8,%9,%10,%11}, {%12,%13,%14,%15}, {%0,%1,%2,%3};\n"
+      : "+d"(c[0]), "+d"(c[1]), "+d"(c[2]), "+d"(c[3])
+      : "d"(a[0]), "d"(a[1]), "d"(a[2]), "d"(a[3]), "d"(a[4]), "d"(a[5]), "d"(a[6]), "d"(a[7]),
+        "d"(b[0]), "d"(b[1]), "d"(b[2]), "d"(b[3]));
+}
+
+// One BK-deep step of the warp tile from smem tiles As[k][i] and Bs[k][j].
+__device__ __forceinline__ void warp_mma_step(double (&acc)[F64_MT][F64_NT][4], const double* As,
+                                              const double* Bs, int wm0, int wn0, int lane) {
+  const int g = lane >> 2, t = lane & 3;
+  double b[F64_NT][4];
+#pragma unroll
+  for (int nt = 0; nt < F64_NT; nt++)
+#pragma unroll
+    for (int r = 0; r < 4; r++) b[nt][r] = Bs[(t + 4 * r) * F64_BPAD + wn0 + nt * 8 + g];
+#pragma unroll
+  for (int mt = 0; mt < F64_MT; mt++) {
+    double a[8];
+#pragma unroll
+    for (int r = 0; r < 8; r++) a[r] = As[(t + 4 * (r >> 1)) * F64_APAD + wm0 + mt * 16 + g + 8 * (r & 1)];
+#pragma unroll
+    for (int nt = 0; nt < F64_NT; nt++) dmma16816(acc[mt][nt], a, b[nt]);
+  }
+}
+
+// ---- streamed-operand loaders -----------------------------------------------------------
+// A tile (real kinds): As[kk][ii] = A[(m0+ii) + (k0+kk)*lda], zero outside M x K.
+__device__ __forceinline__ void load_A_tile(double* As, const F64Args& p, int m0, int k0, int tid) {
+#pragma unroll
+  for (int e = tid; e < F64_BM * F64_BK; e += F64_THREADS) {
+    int ii = e % F64_BM, kk = e / F64_BM;
+    int gi = m0 + ii, gk = k0 + kk;
+    bool ok = gi < p.M && gk < p.K;
+    const double* src = ok ? p.X + (long)gi + (long)gk * p.ldx : p.X;
+    cp_async8(&As[kk * F64_APAD + ii], src, ok);
+  }
+}
+// B tile (DFT): Bs[kk][jj] = B'[(k0+kk) + (n0+jj)*ldb'], zero outside K x N.
+__device__ __forceinline__ void load_B_tile(double* Bs, const F64Args& p, int n0, int k0, int tid) {
+#pragma unroll
+  for (int e = tid; e < F64_BN * F64_BK; e += F64_THREADS) {
+    int kk = e % F64_BK, jj = e / F64_BK;
+    int gk = k0 + kk, gj = n0 + jj;
+    bool ok = gk < p.K && gj < p.N;
+    const double* src = ok ? p.X + (long)gk + (long)gj * p.ldx : p.X;
+    cp_async8(&Bs[kk * F64_BPAD + jj], src, ok);
+  }
+}
+
+// ---- generated-operand builders -----------------------------------------------------------
+// H tile (real kinds): Bs[kk][jj] = H(k0+kk, n0+jj) (0-based), zero outside K x K.
+// Each thread owns one column jj and BK/2 consecutive rows.
+template <int KIND>
+__device__ __forceinline__ void gen_H_tile(double* Bs, const F64Args& p, int n0, int k0, int tid,
+                                           double colF, double colV) {
+  const int jj = tid % F64_BN;
+  const int kh = tid / F64_BN;  // 0 or 1
+  const int gj = n0 + jj;
+  const int K = p.korder;
+#pragma unroll
+  for (int q = 0; q < F64_BK / 2; q++) {
+    int kk = kh * (F64_BK / 2) + q;
+    int gk = k0 + kk;
+    double h = 0.0;
+    if (gk < K && gj < K) {
+      if (KIND == KIND_CAUCHY) {
+        double d = __ldg(p.gen + gk);                 // D(i)
+        double u = __ldg(p.gen + 2 * p.ldgen + gk);   // U(i)
+        h = (u * colV) / (d - colF);                  // U(i)*V(j) / (D(i)-F(j))
+      } else if (KIND == KIND_TOEPLITZ) {
+        h = __ldg(p.gen + (K - 1) + gj - gk);         // G(K + j - i), 1-based
+      } else {
+        h = __ldg(p.gen + gk + gj);                   // G(i + j - 1), 1-based
+      }
+    }
+    Bs[kk * F64_BPAD + jj] = h;
+  }
+}
+
+// F' tile (DFT): As[kk][ii] = F'(m0+ii, k0+kk), F'(2r+a, 2l+b) = [[Re,-Im],[Im,Re]][a][b] of
+// w^(r*l mod n).  Each thread owns one row ii and BK/2 consecutive k columns (one complex l
+// per pair of columns).
+__device__ __forceinline__ void gen_F_tile(double* As, const F64Args& p, int m0, int k0, int tid) {
+  const int ii = tid % F64_BM;
+  const int kh = tid / F64_BM;  // 0 or 1
+  const int gi = m0 + ii;
+  const long n = p.korder;
+  const int r = gi >> 1, a = gi & 1;
+#pragma unroll
+  for (int q = 0; q < F64_BK / 4; q++) {
+    int kk = kh * (F64_BK / 2) + 2 * q;   // even column: b = 0, next: b = 1
+    int gk = k0 + kk;
+    int l = gk >> 1;
+    double v0 = 0.0, v1 = 0.0;
+    if (gi < p.M && gk < p.K) {
+      long t = ((long)r * (long)l) % n;
+      double2 w = __ldg(p.wtab + t);
+      // row 2r  : [ Re, -Im ];  row 2r+1: [ Im, Re ]
+      v0 = a ? w.y : w.x;
+      v1 = a ? w.x : -w.y;
+    }
+    As[kk * F64_APAD + ii] = v0;
+    As[(kk + 1) * F64_APAD + ii] = v1;
+  }
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(F64_THREADS, 1) k_struct_f64(F64Args p) {
+  extern __shared__ __align__(16) double smem[];
+  double* As0 = smem;
+  double* Bs0 = smem + F64_SMEM_A;
+  double* As1 = smem + F64_SMEM_A + F64_SMEM_B;
+  double* Bs1 = As1 + F64_SMEM_A;
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int m0 = blockIdx.x * F64_BM, n0 = blockIdx.y * F64_BN;
+  const int wm0 = (warp & 1) * F64_WM, wn0 = (warp >> 1) * F64_WN;
+
+  double colF = 0.0, colV = 0.0;
+  if (KIND == KIND_CAUCHY) {
+    int gj = n0 + (tid % F64_BN);
+    if (gj < p.korder) {
+      colF = __ldg(p.gen + p.ldgen + gj);       // F(j)
+      colV = __ldg(p.gen + 3 * p.ldgen + gj);   // V(j)
+    }
+  }
+
+  double acc[F64_MT][F64_NT][4];
+#pragma unroll
+  for (int i = 0; i < F64_MT; i++)
+#pragma unroll
+    for (int j = 0; j < F64_NT; j++)
+#pragma unroll
+      for (int r = 0; r < 4; r++) acc[i][j][r] = 0.0;
+
+  const int nk = (p.K + F64_BK - 1) / F64_BK;
+  auto stage = [&](int kt, double* As, double* Bs) {
+    int k0 = kt * F64_BK;
+    if (KIND == KIND_DFT) {
+      load_B_tile(Bs, p, n0, k0, tid);
+      cp_async_commit();
+      gen_F_tile(As, p, m0, k0, tid);
+    } else {
+      load_A_tile(As, p, m0, k0, tid);
+      cp_async_commit();
+      gen_H_tile<KIND>(Bs, p, n0, k0, tid, colF, colV);
+    }
+  };
+
+  stage(0, As0, Bs0);
+  cp_async_wait_all();
+  __syncthreads();
+  for (int kt = 0; kt < nk; kt++) {
+    double* As = (kt & 1) ? As1 : As0;
+    double* Bs = (kt & 1) ? Bs1 : Bs0;
+    if (kt + 1 < nk) stage(kt + 1, (kt & 1) ? As0 : As1, (kt & 1) ? Bs0 : Bs1);
+    warp_mma_step(acc, As, Bs, wm0, wn0, lane);
+    cp_async_wait_all();
+    __syncthreads();
+  }
+
+  // Epilogue: C = alpha*acc + beta*C (beta == 0: C is not read).
+  const int g = lane >> 2, t = lane & 3;
+#pragma unroll
+  for (int mt = 0; mt < F64_MT; mt++)
+#pragma unroll
+    for (int nt = 0; nt < F64_NT; nt++)
+#pragma unroll
+      for (int r = 0; r < 4; r++) {
+        int gi = m0 + wm0 + mt * 16 + g + 8 * (r >> 1);
+        int gj = n0 + wn0 + nt * 8 + 2 * t + (r & 1);
+        if (gi < p.M && gj < p.N) {
+          double* cp = p.C + (long)gi + (long)gj * p.ldc;
+          double v = p.alpha * acc[mt][nt][r];
+          if (p.beta != 0.0) v = fma(p.beta, *cp, v);
+          *cp = v;
+        }
+      }
+}
+
+// C := beta * C for an M x N column-major block (alpha == 0 path).
+__global__ void k_scale(double* C, long ldc, int M, int N, double beta) {
+  long total = (long)M * N;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x) {
+    long i = e % M, j = e / M;
+    double* cp = C + i + j * ldc;
+    *cp = (beta == 0.0) ? 0.0 : beta * *cp;
+  }
+}
+
+// w^t = exp(-2*pi*i*t/n), t = 0..n-1, from sincospi of the exact fraction 2t/n.
+__global__ void k_dft_table(double2* w, int n) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    double s, c;
+    sincospi(2.0 * (double)t / (double)n, &s, &c);
+    w[t] = make_double2(c, -s);
+  }
+}
+
+int launch_struct_f64(int kind, int M, int N, int K, double alpha, const double* X, long ldx,
+                      const double* gen, long ldgen, int korder, const double2* wtab, double beta,
+                      double* C, long ldc, cudaStream_t stream) {
+  if (M == 0 || N == 0) return PSMMA_OK;
+  if (alpha == 0.0 || K == 0) {
+    if (beta == 1.0) return PSMMA_OK;
+    int blocks = (int)std::min<long>(((long)M * N + 255) / 256, 152L * 16);
+    k_scale<<<blocks, 256, 0, stream>>>(C, ldc, M, N, beta);
+    return cudaGetLastError() == cudaSuccess ? PSMMA_OK : PSMMA_EDEVICE;
+  }
+  F64Args p;
+  p.M = M; p.N = N; p.K = K; p.alpha = alpha; p.beta = beta;
+  p.X = X; p.ldx = ldx; p.C = C; p.ldc = ldc;
+  p.gen = gen; p.ldgen = ldgen; p.korder = korder; p.wtab = wtab;
+  dim3 grid((M + F64_BM - 1) / F64_BM, (N + F64_BN - 1) / F64_BN);
+  if (grid.y > 65535) return PSMMA_EUNSUPPORTED;
+  switch (kind) {
+#define PSMMA_LAUNCH_F64(KD)                                                                  \
+  case KD: {                                                                                  \
+    static bool attr_set = false;                                                             \
+    if (!attr_set) {                                                                          \
+      if (cudaFuncSetAttribute(k_struct_f64<KD>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                               (int)F64_SMEM_BYTES) != cudaSuccess)                           \
+        return PSMMA_EDEVICE;                                                                 \
+      attr_set = true;                                                                        \
+    }                                                                                         \
+    k_struct_f64<KD><<<grid, F64_THREADS, F64_SMEM_BYTES, stream>>>(p);                       \
+    break;                                                                                    \
+  }
+    PSMMA_LAUNCH_F64(KIND_CAUCHY)
+    PSMMA_LAUNCH_F64(KIND_TOEPLITZ)
+    PSMMA_LAUNCH_F64(KIND_HANKEL)
+    PSMMA_LAUNCH_F64(KIND_DFT)
+#undef PSMMA_LAUNCH_F64
+    default:
+      return PSMMA_EUNSUPPORTED;
+  }
+  return cudaGetLastError() == cudaSuccess ? PSMMA_OK : PSMMA_EDEVICE;
+}
+
+int launch_dft_table(double2* w, int n, cudaStream_t stream) {
+  int blocks = std::max(1, std::min((n + 255) / 256, 1024));
+  k_dft_table<<<blocks, 256, 0, stream>>>(w, n);
+  return cudaGetLastError() == cudaSuccess ? PSMMA_OK : PSMMA_EDEVICE;
+}
+
+}  // namespace psmma

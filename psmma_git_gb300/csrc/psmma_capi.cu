@@ -1,0 +1,383 @@
+// C ABI of libpsmma_gb300: argument checks with the reference's INFO numbering, dispatch
+// to the FP64 and split kernels, host-pointer wrappers, Fortran-ABI shims and the
+// library-owned workspace pools.
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <utility>
+
+#include "psmma_internal.h"
+
+namespace psmma {
+
+// ------------------------------------------------------------------------------------
+// Workspace pools: grow-only device buffers, one per (device, stream).  A pool is only
+// reallocated after its stream has drained, so work in flight never loses its buffer.
+// ------------------------------------------------------------------------------------
+namespace {
+struct Pool {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+};
+std::mutex g_pool_mu;
+std::map<std::pair<int, cudaStream_t>, Pool> g_pools;
+}  // namespace
+
+void* pool_get(size_t bytes, cudaStream_t stream, int* status) {
+  *status = PSMMA_OK;
+  if (bytes == 0) return nullptr;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) { *status = PSMMA_EDEVICE; return nullptr; }
+  std::lock_guard<std::mutex> lk(g_pool_mu);
+  Pool& pl = g_pools[{dev, stream}];
+  if (pl.bytes >= bytes) return pl.ptr;
+  if (pl.ptr) {
+    if (cudaStreamSynchronize(stream) != cudaSuccess) { *status = PSMMA_EDEVICE; return nullptr; }
+    cudaFree(pl.ptr);
+    pl.ptr = nullptr;
+    pl.bytes = 0;
+  }
+  size_t want = (bytes + (1u << 20) - 1) & ~((size_t)(1u << 20) - 1);
+  if (cudaMalloc(&pl.ptr, want) != cudaSuccess) {
+    cudaGetLastError();
+    pl.ptr = nullptr;
+    *status = PSMMA_ENOMEM;
+    return nullptr;
+  }
+  pl.bytes = want;
+  return pl.ptr;
+}
+
+namespace {
+
+const psmma_opts kDefaultOpts = {PSMMA_PREC_FP64, 0, nullptr, 0, {0, 0, 0, 0, 0, 0, 0, 0}};
+
+int check_opts(const psmma_opts* o, int kind) {
+  if (o->precision != PSMMA_PREC_FP64 && o->precision != PSMMA_PREC_SPLIT) return PSMMA_EUNSUPPORTED;
+  if (o->precision == PSMMA_PREC_SPLIT && kind == KIND_DFT) return PSMMA_EUNSUPPORTED;
+  if (o->n_moduli != 0 && (o->n_moduli < 8 || o->n_moduli > 20)) return PSMMA_EUNSUPPORTED;
+  for (int i = 0; i < 8; i++)
+    if (o->reserved[i] != 0) return PSMMA_EUNSUPPORTED;
+  return PSMMA_OK;
+}
+
+// Argument checks of PSCAUCHY_COMPUTE / PSTOEPLITZ_COMPUTE / PSHANKEL_COMPUTE
+// (pscauchy_compute.f90:234-255, 298-311 on a 1x1 grid where MP = N).
+int check_real(int kind, int n, int k, double alpha, const double* A, int lda, const double* gen,
+               int ldgen, double beta, const double* Q, int ldq) {
+  if (n < 0) return -2;
+  if (k < 0) return -3;
+  if (lda < std::max(1, n)) return -9;
+  if (ldq < std::max(1, n)) return -14;
+  if (n == 0 || ((alpha == 0.0 || k == 0) && beta == 1.0)) return 1;  // quick return
+  if (k == 0) return 1;
+  if (!Q) return PSMMA_ENULL;
+  if (alpha != 0.0) {
+    if (!A) return PSMMA_ENULL;
+    if (!gen) return PSMMA_EGEN;
+    long need = (kind == KIND_CAUCHY) ? (long)k : 2L * k - 1;
+    if (ldgen < need) return PSMMA_EGEN;
+  }
+  return PSMMA_OK;
+}
+
+// Argument checks of PZMDFTL (pzmdftL.f90:182-205, 279-284 on a 1x1 grid).
+int check_dft(int n, int k, double alpha, const void* B, int ldb, double beta, const void* C, int ldc) {
+  if (n < 0) return -1;
+  if (k < 0) return -2;
+  if (ldb < std::max(1, n)) return -7;
+  if (ldc < std::max(1, n)) return -10;
+  if (n == 0 || k == 0 || (alpha == 0.0 && beta == 1.0)) return 1;  // quick return
+  if (!C) return PSMMA_ENULL;
+  if (alpha != 0.0 && !B) return PSMMA_ENULL;
+  return PSMMA_OK;
+}
+
+int run_real(int kind, int n, int k, double alpha, const double* A, int lda, const double* gen,
+             int ldgen, double beta, double* Q, int ldq, const psmma_opts* opts, void* stream) {
+  const psmma_opts* o = opts ? opts : &kDefaultOpts;
+  int st = check_opts(o, kind);
+  if (st) return st;
+  st = check_real(kind, n, k, alpha, A, lda, gen, ldgen, beta, Q, ldq);
+  if (st == 1) return PSMMA_OK;
+  if (st) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (o->precision == PSMMA_PREC_SPLIT && alpha != 0.0) {
+    size_t need = split_workspace_bytes(kind, n, k, o->n_moduli);
+    void* work = o->work;
+    if (work) {
+      if (o->lwork < need) return PSMMA_EWORKSPACE;
+    } else {
+      work = pool_get(need, s, &st);
+      if (st) return st;
+    }
+    return launch_split(kind, n, k, alpha, A, lda, gen, ldgen, beta, Q, ldq, o->n_moduli, work,
+                        need, s);
+  }
+  return launch_struct_f64(kind, n, k, k, alpha, A, lda, gen, ldgen, k, nullptr, beta, Q, ldq, s);
+}
+
+int run_dft(int n, int k, double alpha, const psmma_complex* B, int ldb, double beta,
+            psmma_complex* C, int ldc, const psmma_opts* opts, void* stream) {
+  const psmma_opts* o = opts ? opts : &kDefaultOpts;
+  int st = check_opts(o, KIND_DFT);
+  if (st) return st;
+  st = check_dft(n, k, alpha, B, ldb, beta, C, ldc);
+  if (st == 1) return PSMMA_OK;
+  if (st) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  double2* wtab = nullptr;
+  if (alpha != 0.0) {
+    size_t need = (size_t)n * sizeof(double2);
+    if (o->work) {
+      if (o->lwork < need) return PSMMA_EWORKSPACE;
+      wtab = (double2*)o->work;
+    } else {
+      wtab = (double2*)pool_get(need, s, &st);
+      if (st) return st;
+    }
+    st = launch_dft_table(wtab, n, s);
+    if (st) return st;
+  }
+  // Real view: C'(2n x k) = F'(2n x 2n) * B'(2n x k), ld doubled.
+  return launch_struct_f64(KIND_DFT, 2 * n, k, 2 * n, alpha, (const double*)B, 2L * ldb, nullptr,
+                           0, n, wtab, beta, (double*)C, 2L * ldc, s);
+}
+
+// ---- host-pointer wrappers -------------------------------------------------------------
+struct HostArena {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+  cudaStream_t stream = nullptr;
+};
+std::mutex g_host_mu;
+std::map<int, HostArena> g_host;
+
+// Returns a device buffer of >= bytes and the library stream of the current device.
+void* host_arena(size_t bytes, cudaStream_t* stream, int* status) {
+  *status = PSMMA_OK;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) { *status = PSMMA_EDEVICE; return nullptr; }
+  HostArena& a = g_host[dev];
+  if (!a.stream && cudaStreamCreateWithFlags(&a.stream, cudaStreamNonBlocking) != cudaSuccess) {
+    *status = PSMMA_EDEVICE;
+    return nullptr;
+  }
+  *stream = a.stream;
+  if (a.bytes < bytes) {
+    if (a.ptr) cudaFree(a.ptr);
+    a.ptr = nullptr;
+    a.bytes = 0;
+    size_t want = (bytes + (1u << 20) - 1) & ~((size_t)(1u << 20) - 1);
+    if (cudaMalloc(&a.ptr, want) != cudaSuccess) {
+      cudaGetLastError();
+      *status = PSMMA_ENOMEM;
+      return nullptr;
+    }
+    a.bytes = want;
+  }
+  return a.ptr;
+}
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+int host_real(int kind, int n, int k, double alpha, const double* A, int lda, const double* gen,
+              int ldgen, double beta, double* Q, int ldq, const psmma_opts* opts) {
+  const psmma_opts* o = opts ? opts : &kDefaultOpts;
+  int st = check_opts(o, kind);
+  if (st) return st;
+  st = check_real(kind, n, k, alpha, A, lda, gen, ldgen, beta, Q, ldq);
+  if (st == 1) return PSMMA_OK;
+  if (st) return st;
+  std::lock_guard<std::mutex> lk(g_host_mu);
+  long glen = (alpha == 0.0) ? 0 : ((kind == KIND_CAUCHY) ? 4L * k : 2L * k - 1);
+  size_t bA = align256((size_t)n * k * 8), bG = align256((size_t)glen * 8), bQ = align256((size_t)n * k * 8);
+  cudaStream_t s;
+  char* base = (char*)host_arena(bA + bG + bQ, &s, &st);
+  if (st) return st;
+  double* dA = (double*)base;
+  double* dG = (double*)(base + bA);
+  double* dQ = (double*)(base + bA + bG);
+  bool ok = true;
+  if (alpha != 0.0) {
+    ok &= cudaMemcpy2DAsync(dA, (size_t)n * 8, A, (size_t)lda * 8, (size_t)n * 8, k, cudaMemcpyHostToDevice, s) == cudaSuccess;
+    if (kind == KIND_CAUCHY)
+      ok &= cudaMemcpy2DAsync(dG, (size_t)k * 8, gen, (size_t)ldgen * 8, (size_t)k * 8, 4, cudaMemcpyHostToDevice, s) == cudaSuccess;
+    else
+      ok &= cudaMemcpyAsync(dG, gen, (size_t)glen * 8, cudaMemcpyHostToDevice, s) == cudaSuccess;
+  }
+  if (beta != 0.0)
+    ok &= cudaMemcpy2DAsync(dQ, (size_t)n * 8, Q, (size_t)ldq * 8, (size_t)n * 8, k, cudaMemcpyHostToDevice, s) == cudaSuccess;
+  if (!ok) return PSMMA_EDEVICE;
+  psmma_opts o2 = *o;
+  st = run_real(kind, n, k, alpha, dA, n, dG, (kind == KIND_CAUCHY) ? k : (int)glen, beta, dQ, n, &o2, s);
+  if (st) { cudaStreamSynchronize(s); return st; }
+  ok &= cudaMemcpy2DAsync(Q, (size_t)ldq * 8, dQ, (size_t)n * 8, (size_t)n * 8, k, cudaMemcpyDeviceToHost, s) == cudaSuccess;
+  ok &= cudaStreamSynchronize(s) == cudaSuccess;
+  return ok ? PSMMA_OK : PSMMA_EDEVICE;
+}
+
+int host_dft(int n, int k, double alpha, const psmma_complex* B, int ldb, double beta,
+             psmma_complex* C, int ldc, const psmma_opts* opts) {
+  const psmma_opts* o = opts ? opts : &kDefaultOpts;
+  int st = check_opts(o, KIND_DFT);
+  if (st) return st;
+  st = check_dft(n, k, alpha, B, ldb, beta, C, ldc);
+  if (st == 1) return PSMMA_OK;
+  if (st) return st;
+  std::lock_guard<std::mutex> lk(g_host_mu);
+  size_t bB = align256((size_t)n * k * 16), bC = bB;
+  cudaStream_t s;
+  char* base = (char*)host_arena(bB + bC, &s, &st);
+  if (st) return st;
+  psmma_complex* dB = (psmma_complex*)base;
+  psmma_complex* dC = (psmma_complex*)(base + bB);
+  bool ok = true;
+  if (alpha != 0.0)
+    ok &= cudaMemcpy2DAsync(dB, (size_t)n * 16, B, (size_t)ldb * 16, (size_t)n * 16, k, cudaMemcpyHostToDevice, s) == cudaSuccess;
+  if (beta != 0.0)
+    ok &= cudaMemcpy2DAsync(dC, (size_t)n * 16, C, (size_t)ldc * 16, (size_t)n * 16, k, cudaMemcpyHostToDevice, s) == cudaSuccess;
+  if (!ok) return PSMMA_EDEVICE;
+  st = run_dft(n, k, alpha, dB, n, beta, dC, n, o, s);
+  if (st) { cudaStreamSynchronize(s); return st; }
+  ok &= cudaMemcpy2DAsync(C, (size_t)ldc * 16, dC, (size_t)n * 16, (size_t)n * 16, k, cudaMemcpyDeviceToHost, s) == cudaSuccess;
+  ok &= cudaStreamSynchronize(s) == cudaSuccess;
+  return ok ? PSMMA_OK : PSMMA_EDEVICE;
+}
+
+thread_local int g_last_status = PSMMA_OK;
+
+}  // namespace
+}  // namespace psmma
+
+using namespace psmma;
+
+extern "C" {
+
+int psmma_cauchy(int n, int k, double alpha, const double* A, int lda, const double* gen, int ldgen,
+                 double beta, double* Q, int ldq, const psmma_opts* opts, void* stream) {
+  return run_real(KIND_CAUCHY, n, k, alpha, A, lda, gen, ldgen, beta, Q, ldq, opts, stream);
+}
+int psmma_toeplitz(int n, int k, double alpha, const double* A, int lda, const double* gen,
+                   int ldgen, double beta, double* Q, int ldq, const psmma_opts* opts, void* stream) {
+  return run_real(KIND_TOEPLITZ, n, k, alpha, A, lda, gen, ldgen, beta, Q, ldq, opts, stream);
+}
+int psmma_hankel(int n, int k, double alpha, const double* A, int lda, const double* gen, int ldgen,
+                 double beta, double* Q, int ldq, const psmma_opts* opts, void* stream) {
+  return run_real(KIND_HANKEL, n, k, alpha, A, lda, gen, ldgen, beta, Q, ldq, opts, stream);
+}
+int pzmdftl(int n, int k, double alpha, const psmma_complex* B, int ldb, double beta,
+            psmma_complex* C, int ldc, const psmma_opts* opts, void* stream) {
+  return run_dft(n, k, alpha, B, ldb, beta, C, ldc, opts, stream);
+}
+int pzmdftl1(int n, int k, double alpha, const psmma_complex* B, int ldb, double beta,
+             psmma_complex* C, int ldc, const psmma_opts* opts, void* stream) {
+  return run_dft(n, k, alpha, B, ldb, beta, C, ldc, opts, stream);
+}
+
+int psmma_cauchy_host(int n, int k, double alpha, const double* A, int lda, const double* gen,
+                      int ldgen, double beta, double* Q, int ldq, const psmma_opts* opts) {
+  return host_real(KIND_CAUCHY, n, k, alpha, A, lda, gen, ldgen, beta, Q, ldq, opts);
+}
+int psmma_toeplitz_host(int n, int k, double alpha, const double* A, int lda, const double* gen,
+                        int ldgen, double beta, double* Q, int ldq, const psmma_opts* opts) {
+  return host_real(KIND_TOEPLITZ, n, k, alpha, A, lda, gen, ldgen, beta, Q, ldq, opts);
+}
+int psmma_hankel_host(int n, int k, double alpha, const double* A, int lda, const double* gen,
+                      int ldgen, double beta, double* Q, int ldq, const psmma_opts* opts) {
+  return host_real(KIND_HANKEL, n, k, alpha, A, lda, gen, ldgen, beta, Q, ldq, opts);
+}
+int pzmdftl_host(int n, int k, double alpha, const psmma_complex* B, int ldb, double beta,
+                 psmma_complex* C, int ldc, const psmma_opts* opts) {
+  return host_dft(n, k, alpha, B, ldb, beta, C, ldc, opts);
+}
+
+// Fortran ABI: by-reference arguments, 1x1 grid descriptors (LLD = DESC(9)).
+void psmma_cauchy_(const int* n, const int* k, const double* alpha, const double* A, const int*,
+                   const int*, const int* desca, const double* B, const int* ldb, const double* beta,
+                   double* Q, const int*, const int*, const int* descq, double*, const int*) {
+  g_last_status = host_real(KIND_CAUCHY, *n, *k, *alpha, A, desca[8], B, *ldb, *beta, Q, descq[8], nullptr);
+}
+void psmma_toeplitz_(const int* n, const int* k, const double* alpha, const double* A, const int*,
+                     const int*, const int* desca, const double* B, const int* ldb, const double* beta,
+                     double* Q, const int*, const int*, const int* descq, double*, const int*) {
+  g_last_status = host_real(KIND_TOEPLITZ, *n, *k, *alpha, A, desca[8], B, *ldb, *beta, Q, descq[8], nullptr);
+}
+void psmma_hankel_(const int* n, const int* k, const double* alpha, const double* A, const int*,
+                   const int*, const int* desca, const double* B, const int* ldb, const double* beta,
+                   double* Q, const int*, const int*, const int* descq, double*, const int*) {
+  g_last_status = host_real(KIND_HANKEL, *n, *k, *alpha, A, desca[8], B, *ldb, *beta, Q, descq[8], nullptr);
+}
+void pzmdftl_(const int* n, const int* k, const int*, const int*, const double* alpha,
+              const psmma_complex* B, const int* ldb, const double* beta, psmma_complex* C,
+              const int* ldc, const int*, const int*, psmma_complex*, double*) {
+  g_last_status = host_dft(*n, *k, *alpha, B, *ldb, *beta, C, *ldc, nullptr);
+}
+void pzmdftl1_(const int* n, const int* k, const int*, const int*, const double* alpha,
+               const psmma_complex* B, const int* ldb, const double* beta, psmma_complex* C,
+               const int* ldc, const int*, const int*, psmma_complex*, double*) {
+  g_last_status = host_dft(*n, *k, *alpha, B, *ldb, *beta, C, *ldc, nullptr);
+}
+int psmma_last_status(void) { return g_last_status; }
+
+size_t psmma_workspace_size(int kind, int n, int k, const psmma_opts* opts) {
+  const psmma_opts* o = opts ? opts : &kDefaultOpts;
+  if (n <= 0 || k <= 0) return 0;
+  if (kind == KIND_DFT) return align256((size_t)n * sizeof(double2));
+  if (kind < KIND_CAUCHY || kind > KIND_HANKEL) return 0;
+  if (o->precision == PSMMA_PREC_SPLIT) return split_workspace_bytes(kind, n, k, o->n_moduli);
+  return 0;
+}
+
+void psmma_release_workspace(void) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return;
+  {
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    for (auto it = g_pools.begin(); it != g_pools.end();) {
+      if (it->first.first == dev) {
+        cudaStreamSynchronize(it->first.second);
+        cudaFree(it->second.ptr);
+        it = g_pools.erase(it);
+      } else {
+        ++it;
+      }
+    }
+  }
+  std::lock_guard<std::mutex> lk(g_host_mu);
+  auto it = g_host.find(dev);
+  if (it != g_host.end() && it->second.ptr) {
+    cudaStreamSynchronize(it->second.stream);
+    cudaFree(it->second.ptr);
+    it->second.ptr = nullptr;
+    it->second.bytes = 0;
+  }
+}
+
+const char* psmma_status_string(int status) {
+  switch (status) {
+    case PSMMA_OK: return "ok";
+    case -1: return "argument N < 0 (PZMDFTL INFO=1)";
+    case -2: return "argument N < 0 (PSCAUCHY_COMPUTE INFO=2) or K < 0 (PZMDFTL INFO=2)";
+    case -3: return "argument K < 0 (PSCAUCHY_COMPUTE INFO=3)";
+    case -7: return "LDB too small (PZMDFTL INFO=7)";
+    case -9: return "LDA too small (PSCAUCHY_COMPUTE INFO=9)";
+    case -10: return "LDC too small (PZMDFTL INFO=10)";
+    case -14: return "LDQ too small (PSCAUCHY_COMPUTE INFO=14)";
+    case PSMMA_EGEN: return "generator pointer NULL or generator length too small";
+    case PSMMA_ENULL: return "matrix pointer NULL for a non-empty operand";
+    case PSMMA_ENOMEM: return "device allocation failed";
+    case PSMMA_EDEVICE: return "CUDA runtime error";
+    case PSMMA_ETIMEDOUT: return "bounded device-side wait expired";
+    case PSMMA_ESINGULAR: return "Cauchy denominator D(i)-F(j) is zero";
+    case PSMMA_EUNSUPPORTED: return "unsupported option combination";
+    case PSMMA_EWORKSPACE: return "workspace too small";
+    case PSMMA_ERANGE: return "non-finite input or exponent out of range for the split path";
+    default: return "unknown status";
+  }
+}
+
+const char* psmma_version(void) { return "psmma-gb300 0.1.0 (sm_103a)"; }
+
+}  // extern "C"

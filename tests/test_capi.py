@@ -1,0 +1,82 @@
+"""CPU tests of the C ABI: the library builds, loads, exports every declared symbol, and
+its argument checks return the reference's INFO numbers (no GPU work is launched)."""
+import ctypes as C
+
+import numpy as np
+
+from psmma_git_gb300 import _lib
+
+
+def test_library_exports_every_header_symbol(lib):
+    names = _lib.header_symbols()
+    assert "psmma_cauchy" in names and "pzmdftl1_" in names and len(names) >= 19
+    for name in names:
+        assert hasattr(lib, name), f"libpsmma_gb300.so does not export {name}"
+    assert set(names) <= set(_lib.SIGNATURES), "binding table out of date"
+    assert lib.psmma_version().startswith(b"psmma-gb300")
+
+
+def _call_real(lib, name, n, k, lda, ldgen, ldq, gen=True, alpha=1.0, beta=0.0):
+    buf = np.zeros(16)
+    p = C.c_void_p(buf.ctypes.data)
+    return getattr(lib, name)(n, k, alpha, p, lda, p if gen else None, ldgen, beta, p, ldq, None, None)
+
+
+def test_argument_checks_use_reference_info_numbers(lib):
+    # PSCAUCHY_COMPUTE: N<0 -> 2, K<0 -> 3, LDA -> 9, LDC -> 14 (pscauchy_compute.f90:234-255)
+    for name in ["psmma_cauchy", "psmma_toeplitz", "psmma_hankel"]:
+        assert _call_real(lib, name, -1, 4, 4, 8, 4) == -2
+        assert _call_real(lib, name, 4, -1, 4, 8, 4) == -3
+        assert _call_real(lib, name, 4, 4, 3, 8, 4) == -9
+        assert _call_real(lib, name, 4, 4, 4, 8, 3) == -14
+        assert _call_real(lib, name, 4, 4, 4, 8, 4, gen=False) == _lib.PSMMA_EGEN
+    assert _call_real(lib, "psmma_cauchy", 4, 4, 4, 3, 4) == _lib.PSMMA_EGEN     # ldgen < k
+    assert _call_real(lib, "psmma_toeplitz", 4, 4, 4, 6, 4) == _lib.PSMMA_EGEN   # < 2k-1
+    # quick returns touch nothing (N == 0; alpha == 0 and beta == 1)
+    assert _call_real(lib, "psmma_cauchy", 0, 4, 1, 4, 1) == 0
+    assert _call_real(lib, "psmma_cauchy", 4, 4, 4, 4, 4, alpha=0.0, beta=1.0) == 0
+    # PZMDFTL: N<0 -> 1, K<0 -> 2, LDB -> 7, LDC -> 10 (pzmdftL.f90:182-205)
+    buf = np.zeros(16)
+    p = C.c_void_p(buf.ctypes.data)
+    assert lib.pzmdftl(-1, 2, 1.0, p, 2, 0.0, p, 2, None, None) == -1
+    assert lib.pzmdftl(2, -1, 1.0, p, 2, 0.0, p, 2, None, None) == -2
+    assert lib.pzmdftl(4, 2, 1.0, p, 3, 0.0, p, 4, None, None) == -7
+    assert lib.pzmdftl(4, 2, 1.0, p, 4, 0.0, p, 3, None, None) == -10
+    assert lib.pzmdftl_host(0, 2, 1.0, p, 1, 0.0, p, 1, None) == 0
+
+
+def test_options_are_validated(lib):
+    buf = np.zeros(16)
+    p = C.c_void_p(buf.ctypes.data)
+    o = _lib.PsmmaOpts()
+    o.precision = 7
+    assert lib.psmma_cauchy(2, 2, 1.0, p, 2, p, 2, 0.0, p, 2, C.byref(o), None) == _lib.PSMMA_EUNSUPPORTED
+    o.precision = _lib.PREC_SPLIT
+    assert lib.pzmdftl(2, 2, 1.0, p, 2, 0.0, p, 2, C.byref(o), None) == _lib.PSMMA_EUNSUPPORTED
+    o.precision = 0
+    o.reserved[3] = 1
+    assert lib.psmma_hankel(2, 2, 1.0, p, 2, p, 3, 0.0, p, 2, C.byref(o), None) == _lib.PSMMA_EUNSUPPORTED
+
+
+def test_fortran_abi_argument_check(lib):
+    # PSMMA_CAUCHY(N,K,ALPHA,A,IA,JA,DESCA,B,LDB,BETA,Q,IQ,JQ,DESCQ,WORK,REDIST) with N < 0
+    i = lambda v: C.byref(C.c_int(v))
+    d = lambda v: C.byref(C.c_double(v))
+    desc = (C.c_int * 9)(1, 0, 4, 4, 4, 4, 0, 0, 4)
+    buf = np.zeros(16)
+    p = C.c_void_p(buf.ctypes.data)
+    lib.psmma_cauchy_(i(-1), i(4), d(1.0), p, i(1), i(1), desc, p, i(4), d(0.0), p, i(1), i(1), desc, p, i(0))
+    assert lib.psmma_last_status() == -2
+    lib.pzmdftl_(i(4), i(4), i(2), i(2), d(1.0), p, i(3), d(0.0), p, i(4), i(0), i(0), p, p)
+    assert lib.psmma_last_status() == -7
+
+
+def test_status_strings(lib):
+    for st in [0, -2, -3, -9, -14, _lib.PSMMA_EGEN, _lib.PSMMA_ETIMEDOUT, _lib.PSMMA_ESINGULAR]:
+        assert _lib.status_string(st) != "unknown status"
+
+
+def test_workspace_size_queries(lib):
+    from psmma_git_gb300 import workspace_size
+    assert workspace_size(_lib.KIND_CAUCHY, 1024, 1024) == 0
+    assert workspace_size(_lib.KIND_DFT, 1000, 10) >= 1000 * 16
