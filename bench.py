@@ -1,0 +1,382 @@
+#!/usr/bin/env python
+"""Benchmark of the structured multiply on GB300: Cauchy A*C at n = 16384.
+
+Workload (one step = one pass of the hot path over one batch): psmma_cauchy on the split
+path, Q = A*H with H(i,j) = u_i v_j / (d_i - w_j), n = k = 16384, 10% of the poles within
+1e-10 of a neighbour, A ~ N(0,1) in FP64; inputs resident in HBM (A is 2 GiB, larger
+than L2, so no explicit flush is needed between steps).  Reported beside it:
+  * the FP64 plain path (FP64 tensor-core MMA, H generated in shared memory) on the same
+    inputs, and the relative Frobenius error of the split result against it and against
+    the CPU oracle on sampled rows;
+  * p50/p99 step latency, per-phase times (CUDA events on the launch stream);
+  * e2e: the same metric through the host-pointer entry point psmma_cauchy_host with
+    pinned host buffers, host<->device copies inside the timed region;
+  * roofline of the dominant kernel (the modular BF16 GEMM, tensor-bound);
+  * cpu_baseline: the oracle's restatement of the reference (ConstCauchy + DGEMM, which is
+    what PSCAUCHY_COMPUTE does on a 1x1 process grid) on the host cores, on a row sample.
+
+``python bench.py --impl reference`` times that CPU restatement alone (the reference is
+Fortran + MPI + ScaLAPACK and cannot be built on this machine or the GPU host).
+Multi-GPU (torchrun): each rank multiplies its own 16384-row panel of A by the same H
+(weak scaling, no collective on the data path); value = total FLOPs / max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Cauchy A·C eff. TFLOP/s n=16384, FP64 vs split-prec at ≤1e-12 err; p99 ms"
+N_DEFAULT = 16384
+CPU_COLS = 1024  # column-panel sample of the CPU baseline per step
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"bf16": d.get("bf16_tflops", 1900.0), "bf16_sustained": d.get("bf16_tflops_sustained", 1700.0),
+                "hbm": d.get("hbm_gbs", 6800.0), "source": "measured"}
+    return {"bf16": 1900.0, "bf16_sustained": 1700.0, "hbm": 6800.0, "source": "fallback"}
+
+
+def ncu_traffic(n: int):
+    """DRAM bytes per launch of the modular GEMM from the committed ncu summary, scaled to
+    this workload (its traffic grows with the tile count and k)."""
+    f = ROOT / "profiles" / "crt_gemm_ncu.md"
+    if not f.exists():
+        return None
+    m = re.search(r"traffic_bytes_per_launch_n(\d+):\s*([0-9.eE+]+)", f.read_text())
+    if not m:
+        return None
+    n0, b0 = int(m.group(1)), float(m.group(2))
+    return b0 * (n / n0) ** 3
+
+
+class Clocks:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = ROOT / "gpurun_out" / f"bench_clocks_{os.getpid()}.csv"
+
+    def start(self):
+        try:
+            self.path.parent.mkdir(exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        try:
+            self.path.unlink()
+        except Exception:
+            pass
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "samples": len(sm),
+                "reasons": sorted(reasons)}
+
+
+def dist_init(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if args.impl != "reference" else "gloo")
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x: float, ws: int, device=None) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_inputs(n: int, seed_gen: int = 0, seed_a: int = 1):
+    import numpy as np
+    from oracle import psmma_oracle as O
+    gen = O.cfg_cauchy_generators(n, seed=seed_gen, clustered=0.1)
+    rng = np.random.Generator(np.random.PCG64(seed_a))
+    A = np.asfortranarray(rng.standard_normal((n, n)))
+    return A, gen
+
+
+def cpu_sample(A, gen, cols: int):
+    """One bounded step of the CPU restatement: the column panel Q[:, 0:cols] = A * H[:, 0:cols]
+    -- ConstCauchy of that panel of H followed by one DGEMM, i.e. what PSCAUCHY_COMPUTE does
+    for the first ring step of one process column (every part of the work scales by
+    cols / n)."""
+    import numpy as np
+    from oracle import psmma_oracle as O
+    n, k = A.shape
+    t0 = time.perf_counter()
+    H = O.const_cauchy(gen, np.arange(1, k + 1), np.arange(1, cols + 1))
+    Qp = A @ H
+    return time.perf_counter() - t0, Qp
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return 0
+    n = args.n
+    cols = args.cpu_cols
+    A, gen = cpu_inputs(n)
+    for _ in range(args.warmup):
+        cpu_sample(A, gen, cols)
+    times = []
+    for _ in range(args.steps):
+        t, _ = cpu_sample(A, gen, cols)
+        times.append(t)
+    tot = sum(times)
+    flops = 2.0 * n * n * cols * args.steps
+    val = flops / tot / 1e12
+    line = {
+        "impl": "reference", "metric": METRIC, "value": val, "unit": "TFLOP/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"psmma_cauchy n={n} clustered poles, CPU restatement of PSCAUCHY_COMPUTE "
+                               f"(ConstCauchy + DGEMM), column panel {n} x {cols} of Q per step", "n": n, "k": n},
+        "cpu_baseline": {"value": val, "unit": "TFLOP/s", "cores": os.cpu_count(), "kind": "port",
+                         "sample": f"Q[:, 0:{cols}] of the {n}x{n} product per step (H panel generated each step)"},
+        "e2e": {"value": val, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "latency_ms": {"p50": 1e3 * statistics.median(times), "p99": 1e3 * max(times)},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gpu(args, ws, rank, local):
+    import numpy as np
+    import torch
+    import psmma_git_gb300 as P
+    from psmma_git_gb300 import _lib
+    from oracle import psmma_oracle as O
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    lib = _lib.load()
+    n = k = args.n
+    stream = torch.cuda.current_stream(dev)
+
+    gen_np = O.cfg_cauchy_generators(k, seed=0, clustered=0.1)
+    gen = torch.from_numpy(np.ascontiguousarray(gen_np.T)).to(dev).t()
+    g = torch.Generator(device=dev)
+    g.manual_seed(1 + rank)
+    A = P.fortran_empty(n, k, torch.float64, dev)
+    A.copy_(torch.randn(k, n, generator=g, device=dev, dtype=torch.float64).t())
+    Q = P.fortran_empty(n, k, torch.float64, dev)
+    Q.zero_()
+
+    def step():
+        P.psmma_cauchy(n, k, 1.0, A, gen, 0.0, Q, precision="split", n_moduli=args.n_moduli, stream=stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    # ---------------- timed region (split path) ----------------
+    lib.psmma_set_profiling(1)
+    clocks = Clocks(local)
+    clocks.start()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    phase_tot = {}
+    barrier(ws)
+    torch.cuda.synchronize()
+    ev[0].record(stream)
+    for s in range(args.steps):
+        step()
+        ev[s + 1].record(stream)
+        ms = (C_float * 16)()
+        names = (C_charp * 16)()
+        m = lib.psmma_profile_read(ms, names, 16)
+        for i in range(m):
+            phase_tot[names[i].decode()] = phase_tot.get(names[i].decode(), 0.0) + ms[i]
+    torch.cuda.synchronize()
+    barrier(ws)
+    cl = clocks.stop()
+    lib.psmma_set_profiling(0)
+    step_ms = [ev[s].elapsed_time(ev[s + 1]) for s in range(args.steps)]
+    total_ms = ev[0].elapsed_time(ev[args.steps])
+    total_ms = max_over_ranks(total_ms, ws, dev)
+    flops_rank = 2.0 * n * k * k
+    value = flops_rank * ws * args.steps / (total_ms * 1e-3) / 1e12
+    phases = {kname: v / args.steps for kname, v in phase_tot.items()}
+    launches_per_step = len(phases)
+
+    result = {"metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": ws, "steps": args.steps,
+              "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+              "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic"}
+    result["config"] = {
+        "workload": f"psmma_cauchy split-precision n={n} (10% of poles within 1e-10 of a neighbour, A ~ N(0,1) FP64)",
+        "n": n, "k": k, "kind": "cauchy", "precision": "split (CRT residues on BF16 tcgen05, FP64 recombination)",
+        "n_moduli": args.n_moduli, "l2": "inputs larger than L2 (A = 2 GiB), no flush",
+        "parallelism": f"{ws} replica(s), row panels, no collective"}
+    result["latency_ms"] = {"p50": statistics.median(step_ms),
+                            "p99": float(np.percentile(np.asarray(step_ms), 99))}
+    result["phases_ms"] = phases
+    result["gpu_launches"] = launches_per_step * args.steps
+
+    # ---------------- roofline of the modular GEMM ----------------
+    pk = peaks()
+    gemm_ms = phases.get("modular_gemm")
+    kp = (k + 63) // 64 * 64
+    if gemm_ms:
+        flops_gemm = 2.0 * args.n_moduli * n * k * kp
+        achieved = flops_gemm / (gemm_ms * 1e-3) / 1e12
+        traffic = ncu_traffic(n)
+        result["roofline"] = {"bound": "tensor", "achieved": achieved, "peak": pk["bf16_sustained"],
+                              "unit": "TFLOP/s", "frac": achieved / pk["bf16_sustained"], "traffic": traffic,
+                              "kernel": "k_crt_gemm", "flops_per_launch": flops_gemm,
+                              "peak_note": f"{pk['source']} cuBLAS bf16 sustained (kernel timed inside a "
+                                           f"multi-second loop); burst {pk['bf16']}",
+                              "frac_of_burst": achieved / pk["bf16"]}
+
+    if rank == 0:
+        # ---------------- FP64 plain path on the same inputs ----------------
+        if not args.no_fp64:
+            Q64 = P.fortran_empty(n, k, torch.float64, dev)
+            A_small = A[:2048, :2048]
+            P.psmma_cauchy(2048, 2048, 1.0, A_small, gen[:2048], 0.0, Q64[:2048, :2048], stream=stream)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            P.psmma_cauchy(n, k, 1.0, A, gen, 0.0, Q64, precision="fp64", stream=stream)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            t64 = e0.elapsed_time(e1)
+            # cuBLAS DGEMM rate on this GPU, the FP64 roofline denominator
+            a = torch.randn(8192, 8192, device=dev, dtype=torch.float64)
+            torch.matmul(a, a)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            torch.matmul(a, a)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            dgemm = 2 * 8192 ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12
+            del a
+            v64 = flops_rank / (t64 * 1e-3) / 1e12
+            rel = (torch.linalg.norm(Q - Q64) / torch.linalg.norm(Q64)).item()
+            result["fp64_plain"] = {"value": v64, "unit": "TFLOP/s", "ms_per_step": t64, "steps": 1,
+                                    "cublas_dgemm_tflops": dgemm, "frac_of_dgemm": v64 / dgemm,
+                                    "speedup_split_vs_fp64": value / ws / v64}
+            result["rel_err"] = {"split_vs_fp64_path": rel}
+            del Q64
+        # ---------------- CPU baseline + oracle panel ----------------
+        if not args.no_cpu:
+            Acpu = np.asfortranarray(A.t().contiguous().cpu().numpy().T)
+            t, Qcpu = cpu_sample(Acpu, gen_np, args.cpu_cols)
+            del Acpu
+            cpu_val = 2.0 * n * k * args.cpu_cols / t / 1e12
+            result["cpu_baseline"] = {"value": cpu_val, "unit": "TFLOP/s", "cores": os.cpu_count(),
+                                      "kind": "port",
+                                      "sample": f"Q[:, 0:{args.cpu_cols}] of the {n}x{n} product: ConstCauchy of "
+                                                f"that H panel + DGEMM (oracle restatement), {t:.1f} s"}
+            got = Q[:, :args.cpu_cols].t().contiguous().cpu().numpy().T
+            result.setdefault("rel_err", {})["split_vs_cpu_oracle_panel"] = O.rel_fro(got, Qcpu)
+        # ---------------- e2e through the host-pointer entry point ----------------
+        if not args.no_e2e:
+            hA = torch.empty((k, n), dtype=torch.float64, pin_memory=True)
+            hA.copy_(A.t())
+            hQ = torch.empty((k, n), dtype=torch.float64, pin_memory=True)
+            hG = torch.empty((4, k), dtype=torch.float64, pin_memory=True)
+            hG.copy_(gen.t())
+            nA, nQ, nG = hA.numpy().T, hQ.numpy().T, hG.numpy().T
+            del A, Q
+            torch.cuda.empty_cache()
+            P.psmma_cauchy(n, k, 1.0, nA, nG, 0.0, nQ, precision="split", n_moduli=args.n_moduli)
+            e2e_steps = max(1, min(args.steps, 5))
+            t0 = time.perf_counter()
+            for _ in range(e2e_steps):
+                P.psmma_cauchy(n, k, 1.0, nA, nG, 0.0, nQ, precision="split", n_moduli=args.n_moduli)
+            te = (time.perf_counter() - t0) / e2e_steps
+            result["e2e"] = {"value": flops_rank / te / 1e12, "unit": "TFLOP/s",
+                             "h2d_bytes_per_step": n * k * 8 + 4 * k * 8, "d2h_bytes_per_step": n * k * 8,
+                             "ms_per_step": te * 1e3, "steps": e2e_steps,
+                             "api": "psmma_cauchy_host (pinned host buffers)"}
+        if cl is not None:
+            result["clocks"] = cl
+        print(json.dumps(result), flush=True)
+    return 0
+
+
+import ctypes  # noqa: E402
+
+C_float = ctypes.c_float
+C_charp = ctypes.c_char_p
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="psmma", choices=["psmma", "reference"])
+    ap.add_argument("--n", type=int, default=N_DEFAULT)
+    ap.add_argument("--n-moduli", type=int, default=14)
+    ap.add_argument("--cpu-cols", type=int, default=CPU_COLS)
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    ws, rank, local = dist_init(args)
+    if args.impl == "reference":
+        return run_reference(args, ws, rank)
+    from psmma_git_gb300 import build as B
+    if rank == 0:
+        B.build()
+    barrier(ws)
+    return run_gpu(args, ws, rank, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -63,7 +63,7 @@ extern "C" {
 
 typedef struct psmma_opts {
   int    precision;   /* PSMMA_PREC_FP64 (default) or PSMMA_PREC_SPLIT                        */
-  int    n_moduli;    /* split path: number of moduli, 0 = default (14); 8..20                 */
+  int    n_moduli;    /* split path: number of moduli, 0 = default (14); 8..16                 */
   void*  work;        /* optional caller-owned device workspace (NULL: library-owned pool)      */
   size_t lwork;       /* size of `work` in bytes                                               */
   int    reserved[8]; /* must be zero                                                          */
@@ -163,6 +163,14 @@ size_t psmma_workspace_size(int kind, int n, int k, const psmma_opts* opts);
 
 /* Frees the library-owned workspace pools of the current device. */
 void psmma_release_workspace(void);
+
+/* Per-phase tracing.  While enabled, each call records a CUDA event on its stream after
+ * every phase (split path: row scales, H generation, parameters, A residues, H residues,
+ * modular GEMMs, CRT recombination; FP64 path: the structured GEMM).  psmma_profile_read
+ * waits for the last recorded call and returns its phase times in milliseconds and the
+ * phase names (static strings); the return value is the number of phases. */
+void psmma_set_profiling(int on);
+int psmma_profile_read(float* ms, const char** names, int max_phases);
 
 /* Text for a status code (static storage). */
 const char* psmma_status_string(int status);

@@ -31,6 +31,9 @@ __all__ = [
     "make_opts",
 ]
 
+# The split path (exact modular slices on the BF16 tensor cores) is built into the library.
+SPLIT_AVAILABLE = True
+
 _PREC = {"fp64": PREC_FP64, "split": PREC_SPLIT, PREC_FP64: PREC_FP64, PREC_SPLIT: PREC_SPLIT}
 
 

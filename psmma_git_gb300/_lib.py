@@ -68,6 +68,8 @@ SIGNATURES = {
     "psmma_workspace_size": (C.c_size_t, [_i, _i, _i, _op]),
     "psmma_release_workspace": (None, []),
     "psmma_status_string": (C.c_char_p, [_i]),
+    "psmma_set_profiling": (None, [_i]),
+    "psmma_profile_read": (_i, [C.POINTER(C.c_float), C.POINTER(C.c_char_p), _i]),
     "psmma_version": (C.c_char_p, []),
 }
 

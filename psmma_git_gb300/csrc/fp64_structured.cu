@@ -278,6 +278,7 @@ int launch_struct_f64(int kind, int M, int N, int K, double alpha, const double*
   p.gen = gen; p.ldgen = ldgen; p.korder = korder; p.wtab = wtab;
   dim3 grid((M + F64_BM - 1) / F64_BM, (N + F64_BN - 1) / F64_BN);
   if (grid.y > 65535) return PSMMA_EUNSUPPORTED;
+  prof_begin(stream);
   switch (kind) {
 #define PSMMA_LAUNCH_F64(KD)                                                                  \
   case KD: {                                                                                  \
@@ -299,6 +300,7 @@ int launch_struct_f64(int kind, int M, int N, int K, double alpha, const double*
     default:
       return PSMMA_EUNSUPPORTED;
   }
+  prof_mark(stream, "struct_gemm_f64");
   return cudaGetLastError() == cudaSuccess ? PSMMA_OK : PSMMA_EDEVICE;
 }
 

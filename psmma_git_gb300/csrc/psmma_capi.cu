@@ -49,6 +49,42 @@ void* pool_get(size_t bytes, cudaStream_t stream, int* status) {
   return pl.ptr;
 }
 
+// ------------------------------------------------------------------------------------
+// Per-phase tracing with CUDA events on the launch stream (single recording slot).
+// ------------------------------------------------------------------------------------
+namespace {
+std::mutex g_prof_mu;
+bool g_prof_on = false;
+int g_prof_n = 0;
+cudaEvent_t g_prof_ev[PROF_MAX_PHASES + 1];
+const char* g_prof_name[PROF_MAX_PHASES + 1];
+bool g_prof_created = false;
+}  // namespace
+
+bool prof_enabled() { return g_prof_on; }
+
+void prof_begin(cudaStream_t stream) {
+  if (!g_prof_on) return;
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  if (!g_prof_created) {
+    for (int i = 0; i <= PROF_MAX_PHASES; ++i) cudaEventCreate(&g_prof_ev[i]);
+    g_prof_created = true;
+  }
+  g_prof_n = 0;
+  cudaEventRecord(g_prof_ev[0], stream);
+  g_prof_name[0] = "begin";
+  g_prof_n = 1;
+}
+
+void prof_mark(cudaStream_t stream, const char* name) {
+  if (!g_prof_on) return;
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  if (g_prof_n > PROF_MAX_PHASES) return;
+  cudaEventRecord(g_prof_ev[g_prof_n], stream);
+  g_prof_name[g_prof_n] = name;
+  g_prof_n++;
+}
+
 namespace {
 
 const psmma_opts kDefaultOpts = {PSMMA_PREC_FP64, 0, nullptr, 0, {0, 0, 0, 0, 0, 0, 0, 0}};
@@ -56,7 +92,7 @@ const psmma_opts kDefaultOpts = {PSMMA_PREC_FP64, 0, nullptr, 0, {0, 0, 0, 0, 0,
 int check_opts(const psmma_opts* o, int kind) {
   if (o->precision != PSMMA_PREC_FP64 && o->precision != PSMMA_PREC_SPLIT) return PSMMA_EUNSUPPORTED;
   if (o->precision == PSMMA_PREC_SPLIT && kind == KIND_DFT) return PSMMA_EUNSUPPORTED;
-  if (o->n_moduli != 0 && (o->n_moduli < 8 || o->n_moduli > 20)) return PSMMA_EUNSUPPORTED;
+  if (o->n_moduli != 0 && (o->n_moduli < 8 || o->n_moduli > 16)) return PSMMA_EUNSUPPORTED;
   for (int i = 0; i < 8; i++)
     if (o->reserved[i] != 0) return PSMMA_EUNSUPPORTED;
   return PSMMA_OK;
@@ -376,6 +412,23 @@ const char* psmma_status_string(int status) {
     case PSMMA_ERANGE: return "non-finite input or exponent out of range for the split path";
     default: return "unknown status";
   }
+}
+
+void psmma_set_profiling(int on) { g_prof_on = on != 0; }
+
+int psmma_profile_read(float* ms, const char** names, int max_phases) {
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  int np = g_prof_n - 1;
+  if (np <= 0) return 0;
+  if (cudaEventSynchronize(g_prof_ev[g_prof_n - 1]) != cudaSuccess) return PSMMA_EDEVICE;
+  int m = std::min(np, max_phases);
+  for (int i = 0; i < m; ++i) {
+    float t = 0.0f;
+    cudaEventElapsedTime(&t, g_prof_ev[i], g_prof_ev[i + 1]);
+    if (ms) ms[i] = t;
+    if (names) names[i] = g_prof_name[i + 1];
+  }
+  return m;
 }
 
 const char* psmma_version(void) { return "psmma-gb300 0.1.0 (sm_103a)"; }

@@ -28,4 +28,11 @@ int launch_split(int kind, int n, int k, double alpha, const double* A, long lda
 // Library-owned device workspace (psmma_capi.cu): grow-only, one pool per (device, stream).
 void* pool_get(size_t bytes, cudaStream_t stream, int* status);
 
+// Per-phase tracing (psmma_capi.cu): when enabled, launchers record a CUDA event on the
+// launch stream after each phase; psmma_profile_read turns them into milliseconds.
+constexpr int PROF_MAX_PHASES = 16;
+bool prof_enabled();
+void prof_begin(cudaStream_t stream);
+void prof_mark(cudaStream_t stream, const char* name);
+
 }  // namespace psmma

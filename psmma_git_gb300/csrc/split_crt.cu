@@ -1,14 +1,665 @@
-// Split path (exact modular slices on BF16 tensor cores).  Under construction: reports
-// PSMMA_EUNSUPPORTED until the tcgen05 kernels land.
+// Split path: the structured multiply Q = alpha*A*H + beta*Q computed exactly in modular
+// integer arithmetic on the BF16 tensor cores (tcgen05), with FP64 scaling and
+// recombination.
+//
+// Scheme (Chinese-remainder slicing of an integer-scaled product):
+//   1. Each row i of A is scaled by a power of two 2^s_i and rounded to an integer with at
+//      most P bits, A' = rint(A * 2^s); each column j of H likewise, H' = rint(H * 2^f).
+//   2. For pairwise coprime moduli m_1..m_N <= 256 the residues A' mod m_l and H' mod m_l
+//      lie in [-128, 128] and are exact in BF16.
+//   3. One BF16 GEMM per modulus gives Z_l = A'H' mod m_l.  FP32 accumulation is exact
+//      because the tensor memory accumulator is drained every 512 k (|sum| <= 2^23) into a
+//      register-held residue.
+//   4. Z = A'H' is recovered exactly by CRT (128-bit integer arithmetic, |Z| < M/16 with
+//      M = prod m_l), scaled back by 2^-(s_i+f_j) and combined with alpha and beta in FP64.
+// P is chosen on the device from the product bound |Z_ij| <= 2^(2P) * max_j(sum_k|H_kj| /
+// max_k|H_kj|), so no host synchronisation is needed between the passes.
+//
+// H is generated on the device from the generators (formulas of Cauchylowrank.f90:509-521,
+// Auxil_2p5D.f90:224-231, 309-316) in one pass; the caller never supplies a dense H.
+#include <cuda_bf16.h>
+#include <cudaTypedefs.h>
+
+#include <cmath>
+#include <cstring>
+#include <mutex>
+
 #include "psmma_internal.h"
+#include "tcgen05_util.cuh"
 
 namespace psmma {
 
-size_t split_workspace_bytes(int, int, int, int) { return 0; }
+constexpr int SPL_MAX_MODULI = 16;
+constexpr int SPL_DEFAULT_MODULI = 14;
+// Pairwise coprime: 2^8, 3*5*17, 11*23, 13*19 and primes.
+static const int kModuli[SPL_MAX_MODULI] = {256, 255, 253, 251, 247, 241, 239, 233,
+                                            229, 227, 223, 211, 199, 197, 193, 191};
 
-int launch_split(int, int, int, double, const double*, long, const double*, long, double, double*,
-                 long, int, void*, size_t, cudaStream_t) {
-  return PSMMA_EUNSUPPORTED;
+struct CrtConsts {
+  int nmod;
+  int m[SPL_MAX_MODULI];
+  float inv_m[SPL_MAX_MODULI];
+  int c21[SPL_MAX_MODULI];  // 2^21 mod m
+  int c42[SPL_MAX_MODULI];  // 2^42 mod m
+  unsigned long long C_lo[SPL_MAX_MODULI], C_hi[SPL_MAX_MODULI];  // CRT basis C_l < M
+  float f[SPL_MAX_MODULI];                                        // C_l / M
+  unsigned long long M_lo, M_hi;
+  double log2M;
+};
+
+// Device-side parameters of one call (in the workspace).
+struct SplitDevParams {
+  unsigned status;
+  int P;
+  unsigned long long rho_bits;  // max_j sum_k |H_kj| / max_k |H_kj| (bits of a positive double)
+};
+
+// ------------------------------------------------------------------------------------------
+// Host: constants of the CRT for the first nmod moduli.
+// ------------------------------------------------------------------------------------------
+static long long inv_mod(long long a, long long m) {
+  long long t = 0, nt = 1, r = m, nr = ((a % m) + m) % m;
+  while (nr) {
+    long long q = r / nr, tmp;
+    tmp = t - q * nt; t = nt; nt = tmp;
+    tmp = r - q * nr; r = nr; nr = tmp;
+  }
+  return (t % m + m) % m;
+}
+
+static CrtConsts make_consts(int nmod) {
+  CrtConsts c;
+  memset(&c, 0, sizeof(c));
+  c.nmod = nmod;
+  typedef unsigned __int128 u128;
+  u128 M = 1;
+  double l2 = 0.0;
+  for (int l = 0; l < nmod; l++) {
+    M *= (u128)kModuli[l];
+    l2 += std::log2((double)kModuli[l]);
+  }
+  for (int l = 0; l < nmod; l++) {
+    int m = kModuli[l];
+    c.m[l] = m;
+    c.inv_m[l] = 1.0f / (float)m;
+    c.c21[l] = (int)((1LL << 21) % m);
+    c.c42[l] = (int)(((1ULL << 42) % (unsigned long long)m));
+    u128 Ml = M / (u128)m;
+    long long Ml_mod = (long long)(Ml % (u128)m);
+    long long y = inv_mod(Ml_mod, m);
+    u128 C = (Ml * (u128)y) % M;
+    c.C_lo[l] = (unsigned long long)C;
+    c.C_hi[l] = (unsigned long long)(C >> 64);
+    // C / M as float: C < M < 2^126, take the top bits of both
+    long double cf = (long double)C / (long double)M;
+    c.f[l] = (float)cf;
+  }
+  c.M_lo = (unsigned long long)M;
+  c.M_hi = (unsigned long long)(M >> 64);
+  c.log2M = l2 - 1e-9;
+  return c;
+}
+
+// ------------------------------------------------------------------------------------------
+// Workspace layout
+// ------------------------------------------------------------------------------------------
+static size_t al1k(size_t x) { return (x + 1023) & ~(size_t)1023; }
+
+struct SplitLayout {
+  int kp, kr;
+  size_t off_params, off_amax, off_hmax, off_hsum, off_ht, off_ra, off_rh, off_r, total;
+};
+
+static SplitLayout split_layout(int n, int k, int nmod) {
+  SplitLayout L;
+  L.kp = (k + 63) / 64 * 64;
+  L.kr = (k + 255) / 256 * 256;
+  size_t o = 0;
+  L.off_params = o; o += al1k(sizeof(SplitDevParams));
+  L.off_amax = o;   o += al1k((size_t)n * 8);
+  L.off_hmax = o;   o += al1k((size_t)k * 8);
+  L.off_hsum = o;   o += al1k((size_t)k * 8);
+  L.off_ht = o;     o += al1k((size_t)k * L.kp * 8);
+  L.off_ra = o;     o += al1k((size_t)nmod * n * L.kp * 2);
+  L.off_rh = o;     o += al1k((size_t)nmod * k * L.kp * 2);
+  L.off_r = o;      o += al1k((size_t)nmod * n * L.kr);
+  L.total = o;
+  return L;
+}
+
+static int resolve_nmod(int n_moduli) { return n_moduli == 0 ? SPL_DEFAULT_MODULI : n_moduli; }
+
+size_t split_workspace_bytes(int kind, int n, int k, int n_moduli) {
+  (void)kind;
+  if (n <= 0 || k <= 0) return 0;
+  return split_layout(n, k, resolve_nmod(n_moduli)).total;
+}
+
+// ------------------------------------------------------------------------------------------
+// Pass kernels
+// ------------------------------------------------------------------------------------------
+constexpr unsigned long long ABS_MASK = 0x7FFFFFFFFFFFFFFFull;
+constexpr unsigned long long INF_BITS = 0x7FF0000000000000ull;
+
+// Row max of |A| as the bits of a non-negative double (NaN/Inf compare above all finite).
+__global__ void k_row_absmax(const double* __restrict__ A, long lda, int n, int k, int kchunk,
+                             unsigned long long* __restrict__ amax_bits) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int k0 = blockIdx.y * kchunk, k1 = min(k, k0 + kchunk);
+  unsigned long long mb = 0;
+  for (int kk = k0; kk < k1; ++kk) {
+    unsigned long long b = (unsigned long long)__double_as_longlong(__ldg(A + i + (long)kk * lda)) & ABS_MASK;
+    mb = b > mb ? b : mb;
+  }
+  if (mb) atomicMax(amax_bits + i, mb);
+}
+
+// H pass 1: Ht[j][kk] = H(kk, j) in FP64, column max |H| and column sum |H|, and the global
+// ratio rho = max_j sum/max over finite columns.  One block per column j.
+template <int KIND>
+__global__ void k_h_pass1(const double* __restrict__ gen, long ldgen, int k, int kp, double* __restrict__ Ht,
+                          unsigned long long* __restrict__ hmax_bits, double* __restrict__ hsum,
+                          SplitDevParams* prm) {
+  const int j = blockIdx.x;
+  double w = 0.0, v = 0.0;
+  if (KIND == KIND_CAUCHY) {
+    w = __ldg(gen + ldgen + j);       // F(j)
+    v = __ldg(gen + 3 * ldgen + j);   // V(j)
+  }
+  unsigned long long mb = 0;
+  double s = 0.0;
+  double* row = Ht + (long)j * kp;
+  for (int kk = threadIdx.x; kk < kp; kk += blockDim.x) {
+    double h = 0.0;
+    if (kk < k) {
+      if (KIND == KIND_CAUCHY) {
+        double d = __ldg(gen + kk), u = __ldg(gen + 2 * ldgen + kk);
+        h = (u * v) / (d - w);        // U(i)*V(j) / (D(i)-F(j))
+      } else if (KIND == KIND_TOEPLITZ) {
+        h = __ldg(gen + (k - 1) + j - kk);
+      } else {
+        h = __ldg(gen + kk + j);
+      }
+    }
+    row[kk] = h;
+    unsigned long long b = (unsigned long long)__double_as_longlong(h) & ABS_MASK;
+    mb = b > mb ? b : mb;
+    s += fabs(h);
+  }
+  __shared__ unsigned long long smax[32];
+  __shared__ double ssum[32];
+  for (int o = 16; o > 0; o >>= 1) {
+    unsigned long long ob = __shfl_xor_sync(0xffffffffu, mb, o);
+    mb = ob > mb ? ob : mb;
+    s += __shfl_xor_sync(0xffffffffu, s, o);
+  }
+  int wid = threadIdx.x >> 5, ln = threadIdx.x & 31;
+  if (ln == 0) { smax[wid] = mb; ssum[wid] = s; }
+  __syncthreads();
+  if (wid == 0) {
+    int nw = blockDim.x >> 5;
+    mb = ln < nw ? smax[ln] : 0ull;
+    s = ln < nw ? ssum[ln] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) {
+      unsigned long long ob = __shfl_xor_sync(0xffffffffu, mb, o);
+      mb = ob > mb ? ob : mb;
+      s += __shfl_xor_sync(0xffffffffu, s, o);
+    }
+    if (ln == 0) {
+      hmax_bits[j] = mb;
+      hsum[j] = s;
+      if (mb > 0 && mb < INF_BITS && isfinite(s)) {
+        double rho = s / __longlong_as_double((long long)mb);
+        atomicMax(&prm->rho_bits, (unsigned long long)__double_as_longlong(rho));
+      }
+    }
+  }
+}
+
+// P from the bound |Z| <= 2^(2P) * (rho + 1) <= M / 16.
+__global__ void k_split_params(SplitDevParams* prm, double log2M) {
+  double rho = __longlong_as_double((long long)prm->rho_bits);
+  if (!(rho >= 1.0)) rho = 1.0;
+  int P = (int)floor((log2M - 4.0 - log2(rho + 1.0)) * 0.5);
+  prm->P = max(8, min(53, P));
+}
+
+// Exponent s such that |x * 2^s| < 2^P for all |x| <= amax (amax finite, > 0).
+__device__ __forceinline__ int scale_exp(unsigned long long amax_bits, int P) {
+  return P - 1 - ilogb(__longlong_as_double((long long)amax_bits));
+}
+
+// Symmetric residue of the integer x (|x| <= 2^53) modulo m, as an exact float.
+__device__ __forceinline__ float sym_residue(unsigned long long ux, bool neg, int m, float inv_m, int c21, int c42) {
+  int x0 = (int)(ux & 0x1FFFFFull);
+  int x1 = (int)((ux >> 21) & 0x1FFFFFull);
+  int x2 = (int)(ux >> 42);
+  int t = x2 * c42 + x1 * c21 + x0;  // < 2^30, t == x (mod m)
+  int q = __float2int_rn(__int2float_rn(t) * inv_m);
+  int r = t - q * m;
+  int half = m >> 1;
+  r = (r > half) ? r - m : r;
+  r = (r < -half) ? r + m : r;
+  return (float)(neg ? -r : r);
+}
+
+// Integer-scaled value rint(x * 2^e) as (|.|, sign); x finite.
+__device__ __forceinline__ unsigned long long scaled_int(double x, int e, bool* neg) {
+  double y = rint(ldexp(x, e));
+  *neg = y < 0.0;
+  return (unsigned long long)fabs(y);
+}
+
+// RA[l][i][kk] = residues of A' (bf16), rows i, K-major.  Block: 32 rows x 64 k.
+__global__ void k_residues_A(const double* __restrict__ A, long lda, int n, int k, int kp,
+                             const unsigned long long* __restrict__ amax_bits, const SplitDevParams* prm,
+                             CrtConsts cc, __nv_bfloat16* __restrict__ RA) {
+  __shared__ double tile[64][33];
+  const int i0 = blockIdx.y * 32, k0 = blockIdx.x * 64;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 256 threads: 8 x 32
+  for (int kk = ty; kk < 64; kk += 8) {
+    int gi = i0 + tx, gk = k0 + kk;
+    tile[kk][tx] = (gi < n && gk < k) ? __ldg(A + gi + (long)gk * lda) : 0.0;
+  }
+  __syncthreads();
+  const int P = prm->P;
+  const size_t plane = (size_t)n * kp;
+  for (int r = ty; r < 32; r += 8) {
+    int gi = i0 + r;
+    if (gi >= n) continue;
+    unsigned long long ab = amax_bits[gi];
+    bool ok = ab > 0 && ab < INF_BITS;
+    int e = ok ? scale_exp(ab, P) : 0;
+    int kk = 2 * tx;
+    bool n0, n1;
+    unsigned long long u0 = ok ? scaled_int(tile[kk][r], e, &n0) : 0ull;
+    unsigned long long u1 = ok ? scaled_int(tile[kk + 1][r], e, &n1) : 0ull;
+    if (!ok) { n0 = n1 = false; }
+    __nv_bfloat162* dst = (__nv_bfloat162*)(RA + (size_t)gi * kp + k0 + kk);
+#pragma unroll 4
+    for (int l = 0; l < cc.nmod; ++l) {
+      float r0 = sym_residue(u0, n0, cc.m[l], cc.inv_m[l], cc.c21[l], cc.c42[l]);
+      float r1 = sym_residue(u1, n1, cc.m[l], cc.inv_m[l], cc.c21[l], cc.c42[l]);
+      *(__nv_bfloat162*)((__nv_bfloat16*)dst + l * plane) = __floats2bfloat162_rn(r0, r1);
+    }
+  }
+}
+
+// RH[l][j][kk] = residues of H' (bf16) from Ht[j][kk]; one thread per 2 consecutive kk.
+__global__ void k_residues_H(const double* __restrict__ Ht, int k, int kp,
+                             const unsigned long long* __restrict__ hmax_bits, const SplitDevParams* prm,
+                             CrtConsts cc, __nv_bfloat16* __restrict__ RH) {
+  const int j = blockIdx.y;
+  const int kk = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+  if (kk >= kp) return;
+  const int P = prm->P;
+  unsigned long long hb = hmax_bits[j];
+  bool ok = hb > 0 && hb < INF_BITS;
+  int e = ok ? scale_exp(hb, P) : 0;
+  double2 h = *(const double2*)(Ht + (size_t)j * kp + kk);
+  bool n0 = false, n1 = false;
+  unsigned long long u0 = ok ? scaled_int(h.x, e, &n0) : 0ull;
+  unsigned long long u1 = ok ? scaled_int(h.y, e, &n1) : 0ull;
+  const size_t plane = (size_t)k * kp;
+  __nv_bfloat16* dst = RH + (size_t)j * kp + kk;
+#pragma unroll 4
+  for (int l = 0; l < cc.nmod; ++l) {
+    float r0 = sym_residue(u0, n0, cc.m[l], cc.inv_m[l], cc.c21[l], cc.c42[l]);
+    float r1 = sym_residue(u1, n1, cc.m[l], cc.inv_m[l], cc.c21[l], cc.c42[l]);
+    *(__nv_bfloat162*)(dst + l * plane) = __floats2bfloat162_rn(r0, r1);
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// The modular GEMM: for modulus l and a 128 x 256 output tile, R_l = (RA_l * RH_l^T) mod m_l.
+// Warp roles (320 threads): warps 0-7 drain the accumulator (quadrant = warp % 4, column
+// half = warp / 4), warp 8 issues TMA loads, warp 9 issues tcgen05.mma.  Two 256-column FP32
+// accumulators in tensor memory alternate between 512-deep k chunks.
+// ------------------------------------------------------------------------------------------
+constexpr int G_BM = 128, G_BN = 256, G_BK = 64;
+constexpr int G_STAGES = 4;
+constexpr int G_CHUNK_KB = 8;  // 8 x 64 = 512 k per exact FP32 chunk: |sum| <= 512*128*128 = 2^23
+constexpr int G_EPI_WARPS = 8;
+constexpr int G_THREADS = (G_EPI_WARPS + 2) * 32;
+constexpr uint32_t G_A_BYTES = G_BM * G_BK * 2;
+constexpr uint32_t G_B_BYTES = G_BN * G_BK * 2;
+constexpr size_t G_SMEM = 1024 + (size_t)G_STAGES * (G_A_BYTES + G_B_BYTES) + 256;
+
+struct GemmArgs {
+  int n, kr, nkb, tiles_m, tiles_n, group_m;
+  int8_t* R;
+  unsigned* status;
+  int m[SPL_MAX_MODULI];
+  float inv_m[SPL_MAX_MODULI];
+};
+
+__global__ void __launch_bounds__(G_THREADS, 1)
+    k_crt_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, GemmArgs g) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint8_t* sA = base;
+  uint8_t* sB = base + G_STAGES * G_A_BYTES;
+  uint64_t* bars = (uint64_t*)(sB + G_STAGES * G_B_BYTES);
+  uint64_t* full = bars;
+  uint64_t* empty = bars + G_STAGES;
+  uint64_t* acc_full = bars + 2 * G_STAGES;
+  uint64_t* acc_empty = acc_full + 2;
+  uint64_t* mma_done = acc_empty + 2;
+  uint32_t* tmem_slot = (uint32_t*)(mma_done + 1);
+  volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int l = blockIdx.y;
+  // grouped raster: group_m row tiles sweep all column tiles together (L2 reuse)
+  const int bid = blockIdx.x;
+  const int per_group = g.group_m * g.tiles_n;
+  const int grp = bid / per_group;
+  const int first_m = grp * g.group_m;
+  const int gm = min(g.group_m, g.tiles_m - first_m);
+  const int rr = bid - grp * per_group;
+  const int tm = first_m + rr % gm, tn = rr / gm;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < G_STAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&acc_full[b], 1);
+      mbar_init(&acc_empty[b], G_EPI_WARPS * 32);
+    }
+    mbar_init(mma_done, 1);
+    // a launch whose pipeline already timed out does no further work
+    *abort_flag = status_aborted(g.status) ? 1 : 0;
+    fence_barrier_init();
+  }
+  if (warp == 0) {
+    tmem_alloc(tmem_slot, 512);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem_base = *tmem_slot;
+  const int nkb = *abort_flag ? 0 : g.nkb;
+  const int nchunks = (nkb + G_CHUNK_KB - 1) / G_CHUNK_KB;
+
+  if (warp == G_EPI_WARPS) {
+    // ---------------- TMA producer ----------------
+    if (lane == 0) {
+      prefetch_tmap(&tmA);
+      prefetch_tmap(&tmB);
+      int issued = 0;
+      for (int kb = 0; kb < nkb; ++kb) {
+        const int s = kb % G_STAGES;
+        const uint32_t ph = (kb / G_STAGES) & 1;
+        if (!mbar_wait(&empty[s], ph ^ 1, g.status, abort_flag)) break;
+        mbar_arrive_expect_tx(&full[s], G_A_BYTES + G_B_BYTES);
+        tma_load_3d(sA + s * G_A_BYTES, &tmA, &full[s], kb * G_BK, tm * G_BM, l);
+        tma_load_3d(sB + s * G_B_BYTES, &tmB, &full[s], kb * G_BK, tn * G_BN, l);
+        issued = kb + 1;
+      }
+      // every issued copy must have landed before the CTA may exit
+      for (int kb = max(0, issued - G_STAGES); kb < issued; ++kb)
+        mbar_wait_drain(&full[kb % G_STAGES], (kb / G_STAGES) & 1, g.status);
+    }
+    __syncwarp();
+  } else if (warp == G_EPI_WARPS + 1) {
+    // ---------------- MMA issuer ----------------
+    if (lane == 0) {
+      const uint32_t idesc = idesc_bf16_f32(G_BM, G_BN);
+      int kb = 0;
+      bool ok = true;
+      for (int c = 0; c < nchunks && ok; ++c) {
+        const int buf = c & 1;
+        const uint32_t use = (uint32_t)(c >> 1);
+        if (!mbar_wait(&acc_empty[buf], (use & 1) ^ 1, g.status, abort_flag)) break;
+        tc_fence_after();
+        const uint32_t dt = tmem_base + (uint32_t)(buf * G_BN);
+        const int kend = min(nkb, kb + G_CHUNK_KB);
+        uint32_t acc = 0;
+        for (; kb < kend; ++kb) {
+          const int s = kb % G_STAGES;
+          if (!mbar_wait(&full[s], (kb / G_STAGES) & 1, g.status, abort_flag)) { ok = false; break; }
+          tc_fence_after();
+          const uint32_t a0 = smem_u32(sA + s * G_A_BYTES), b0 = smem_u32(sB + s * G_B_BYTES);
+#pragma unroll
+          for (int kk = 0; kk < G_BK / 16; ++kk) {
+            tc_mma_bf16(dt, sdesc_sw128_kmajor(a0 + kk * 32), sdesc_sw128_kmajor(b0 + kk * 32), idesc, acc);
+            acc = 1;
+          }
+          tc_commit(&empty[s]);
+        }
+        if (ok) tc_commit(&acc_full[buf]);
+      }
+      // all tcgen05 work of this thread must complete before TMEM is released
+      tc_commit(mma_done);
+      mbar_wait_drain(mma_done, 0, g.status);
+    }
+    __syncwarp();
+  } else {
+    // ---------------- accumulator drain (epilogue) ----------------
+    const int q = warp & 3, h = warp >> 2;
+    const float m = (float)g.m[l], inv_m = g.inv_m[l];
+    float res[128];
+#pragma unroll
+    for (int e = 0; e < 128; ++e) res[e] = 0.0f;
+    bool ok = true;
+    for (int c = 0; c < nchunks; ++c) {
+      const int buf = c & 1;
+      const uint32_t use = (uint32_t)(c >> 1);
+      if (!mbar_wait(&acc_full[buf], use & 1, g.status, abort_flag)) { ok = false; break; }
+      tc_fence_after();
+#pragma unroll
+      for (int cb = 0; cb < 4; ++cb) {
+        uint32_t r[32];
+        tmem_ld32(tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * G_BN + h * 128 + cb * 32), r);
+        tmem_ld_wait();
+#pragma unroll
+        for (int e = 0; e < 32; ++e) {
+          float v = __uint_as_float(r[e]) + res[cb * 32 + e];  // exact: |v| < 2^24
+          float qq = rintf(v * inv_m);
+          float x = fmaf(-qq, m, v);
+          x = (x > 127.0f) ? x - m : x;
+          x = (x < -128.0f) ? x + m : x;
+          res[cb * 32 + e] = x;
+        }
+      }
+      tc_fence_before();
+      mbar_arrive(&acc_empty[buf]);
+    }
+    const int i = tm * G_BM + q * 32 + lane;
+    if (ok && !*abort_flag && i < g.n) {
+      int8_t* dst = g.R + ((size_t)l * g.n + i) * g.kr + (size_t)tn * G_BN + h * 128;
+#pragma unroll
+      for (int v = 0; v < 8; ++v) {
+        uint32_t w[4];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+          uint32_t b0 = (uint32_t)(uint8_t)(int8_t)__float2int_rn(res[v * 16 + t * 4 + 0]);
+          uint32_t b1 = (uint32_t)(uint8_t)(int8_t)__float2int_rn(res[v * 16 + t * 4 + 1]);
+          uint32_t b2 = (uint32_t)(uint8_t)(int8_t)__float2int_rn(res[v * 16 + t * 4 + 2]);
+          uint32_t b3 = (uint32_t)(uint8_t)(int8_t)__float2int_rn(res[v * 16 + t * 4 + 3]);
+          w[t] = b0 | (b1 << 8) | (b2 << 16) | (b3 << 24);
+        }
+        *(uint4*)(dst + v * 16) = make_uint4(w[0], w[1], w[2], w[3]);
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0) tmem_dealloc(tmem_base, 512);
+}
+
+// ------------------------------------------------------------------------------------------
+// CRT recombination + FP64 epilogue: Q(i,j) = alpha * Z_ij * 2^-(s_i+f_j) + beta * Q(i,j).
+// 32 x 32 output tile per block (32 x 8 threads), transposed through shared memory so that
+// both the residue reads (row-major) and the Q writes (column-major) are coalesced.
+// ------------------------------------------------------------------------------------------
+__global__ void k_crt_combine(const int8_t* __restrict__ R, int n, int k, int kr, CrtConsts cc,
+                              const unsigned long long* __restrict__ amax_bits,
+                              const unsigned long long* __restrict__ hmax_bits, const SplitDevParams* prm,
+                              double alpha, double beta, double* __restrict__ Q, long ldq) {
+  __shared__ double tile[32][33];
+  typedef unsigned __int128 u128;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int i0 = blockIdx.y * 32, j0 = blockIdx.x * 32;
+  const int P = prm->P;
+  const u128 M = ((u128)cc.M_hi << 64) | cc.M_lo;
+  const int j = j0 + tx;
+  unsigned long long hb = j < k ? hmax_bits[j] : 0ull;
+  for (int a = 0; a < 4; ++a) {
+    const int il = ty + 8 * a, i = i0 + il;
+    double val = 0.0;
+    if (i < n && j < k) {
+      unsigned long long ab = amax_bits[i];
+      if (ab >= INF_BITS || hb >= INF_BITS) {
+        val = __longlong_as_double(0x7FF8000000000000ll);  // NaN: non-finite input row/column
+      } else if (ab != 0 && hb != 0) {
+        float qf = 0.0f;
+        u128 S = 0;
+        const int8_t* src = R + (size_t)i * kr + j;
+        for (int l = 0; l < cc.nmod; ++l) {
+          int r = (int)src[(size_t)l * n * kr];
+          qf = fmaf((float)r, cc.f[l], qf);
+          u128 C = ((u128)cc.C_hi[l] << 64) | cc.C_lo[l];
+          S += (u128)(__int128)r * C;  // wraps modulo 2^128
+        }
+        long long qi = (long long)rintf(qf);
+        u128 Zu = S - (u128)(__int128)qi * M;
+        __int128 Z = (__int128)Zu;
+        long long zh = (long long)(Z >> 64);
+        unsigned long long zl = (unsigned long long)Z;
+        double z = fma((double)zh, 18446744073709551616.0, (double)zl);
+        int e = scale_exp(ab, P) + scale_exp(hb, P);
+        val = ldexp(z, -e);
+      }
+    }
+    tile[tx][il] = val;
+  }
+  __syncthreads();
+  for (int a = 0; a < 4; ++a) {
+    const int jl = ty + 8 * a, jj = j0 + jl, i = i0 + tx;
+    if (i < n && jj < k) {
+      double* qp = Q + i + (long)jj * ldq;
+      double v = alpha * tile[jl][tx];
+      if (beta != 0.0) v = fma(beta, *qp, v);
+      *qp = v;
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// Host orchestration
+// ------------------------------------------------------------------------------------------
+static PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+  });
+  return fn;
+}
+
+static bool make_tmap(CUtensorMap* map, void* ptr, int kp, int rows, int nmod, int box_rows) {
+  auto enc = get_encode();
+  if (!enc) return false;
+  cuuint64_t dims[3] = {(cuuint64_t)kp, (cuuint64_t)rows, (cuuint64_t)nmod};
+  cuuint64_t strides[2] = {(cuuint64_t)kp * 2, (cuuint64_t)rows * kp * 2};
+  cuuint32_t box[3] = {(cuuint32_t)G_BK, (cuuint32_t)box_rows, 1};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, ptr, dims, strides, box, estr,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+int launch_split(int kind, int n, int k, double alpha, const double* A, long lda, const double* gen, long ldgen,
+                 double beta, double* Q, long ldq, int n_moduli, void* work, size_t lwork, cudaStream_t stream) {
+  const int nmod = resolve_nmod(n_moduli);
+  if (nmod < 8 || nmod > SPL_MAX_MODULI) return PSMMA_EUNSUPPORTED;
+  if (k >= (1 << 24)) return PSMMA_EUNSUPPORTED;
+  SplitLayout L = split_layout(n, k, nmod);
+  if (lwork < L.total || !work) return PSMMA_EWORKSPACE;
+  char* w = (char*)work;
+  SplitDevParams* prm = (SplitDevParams*)(w + L.off_params);
+  unsigned long long* amax = (unsigned long long*)(w + L.off_amax);
+  unsigned long long* hmax = (unsigned long long*)(w + L.off_hmax);
+  double* hsum = (double*)(w + L.off_hsum);
+  double* Ht = (double*)(w + L.off_ht);
+  __nv_bfloat16* RA = (__nv_bfloat16*)(w + L.off_ra);
+  __nv_bfloat16* RH = (__nv_bfloat16*)(w + L.off_rh);
+  int8_t* R = (int8_t*)(w + L.off_r);
+
+  static std::mutex cmu;
+  static CrtConsts consts[SPL_MAX_MODULI + 1];
+  static bool have[SPL_MAX_MODULI + 1] = {false};
+  CrtConsts cc;
+  {
+    std::lock_guard<std::mutex> lk(cmu);
+    if (!have[nmod]) { consts[nmod] = make_consts(nmod); have[nmod] = true; }
+    cc = consts[nmod];
+  }
+
+  prof_begin(stream);
+  if (cudaMemsetAsync(w, 0, L.off_ht, stream) != cudaSuccess) return PSMMA_EDEVICE;
+
+  const int kchunk = 1024;
+  dim3 g1((n + 127) / 128, (k + kchunk - 1) / kchunk);
+  k_row_absmax<<<g1, 128, 0, stream>>>(A, lda, n, k, kchunk, amax);
+  prof_mark(stream, "row_scale");
+  switch (kind) {
+    case KIND_CAUCHY: k_h_pass1<KIND_CAUCHY><<<k, 256, 0, stream>>>(gen, ldgen, k, L.kp, Ht, hmax, hsum, prm); break;
+    case KIND_TOEPLITZ: k_h_pass1<KIND_TOEPLITZ><<<k, 256, 0, stream>>>(gen, ldgen, k, L.kp, Ht, hmax, hsum, prm); break;
+    case KIND_HANKEL: k_h_pass1<KIND_HANKEL><<<k, 256, 0, stream>>>(gen, ldgen, k, L.kp, Ht, hmax, hsum, prm); break;
+    default: return PSMMA_EUNSUPPORTED;
+  }
+  prof_mark(stream, "h_generate");
+  k_split_params<<<1, 1, 0, stream>>>(prm, cc.log2M);
+  prof_mark(stream, "params");
+  k_residues_A<<<dim3(L.kp / 64, (n + 31) / 32), 256, 0, stream>>>(A, lda, n, k, L.kp, amax, prm, cc, RA);
+  prof_mark(stream, "residues_A");
+  k_residues_H<<<dim3((L.kp / 2 + 127) / 128, k), 128, 0, stream>>>(Ht, k, L.kp, hmax, prm, cc, RH);
+  prof_mark(stream, "residues_H");
+
+  CUtensorMap tmA, tmB;
+  if (!make_tmap(&tmA, RA, L.kp, n, nmod, G_BM) || !make_tmap(&tmB, RH, L.kp, k, nmod, G_BN))
+    return PSMMA_EDEVICE;
+  GemmArgs ga;
+  memset(&ga, 0, sizeof(ga));
+  ga.n = n;
+  ga.kr = L.kr;
+  ga.nkb = L.kp / G_BK;
+  ga.tiles_m = (n + G_BM - 1) / G_BM;
+  ga.tiles_n = (k + G_BN - 1) / G_BN;
+  ga.group_m = 12;
+  ga.R = R;
+  ga.status = &prm->status;
+  for (int l = 0; l < nmod; ++l) { ga.m[l] = cc.m[l]; ga.inv_m[l] = cc.inv_m[l]; }
+  if (cudaFuncSetAttribute(k_crt_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G_SMEM) != cudaSuccess)
+    return PSMMA_EDEVICE;
+  dim3 gg(ga.tiles_m * ga.tiles_n, nmod);
+  k_crt_gemm<<<gg, G_THREADS, G_SMEM, stream>>>(tmA, tmB, ga);
+  prof_mark(stream, "modular_gemm");
+
+  dim3 gc((k + 31) / 32, (n + 31) / 32);
+  k_crt_combine<<<gc, dim3(32, 8), 0, stream>>>(R, n, k, L.kr, cc, amax, hmax, prm, alpha, beta, Q, ldq);
+  prof_mark(stream, "crt_combine");
+  if (cudaGetLastError() != cudaSuccess) return PSMMA_EDEVICE;
+
+  unsigned st = 0;
+  if (cudaMemcpyAsync(&st, &prm->status, sizeof(st), cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
+      cudaStreamSynchronize(stream) != cudaSuccess)
+    return PSMMA_EDEVICE;
+  if (st & DEV_ERR_TIMEOUT) return PSMMA_ETIMEDOUT;
+  return PSMMA_OK;
 }
 
 }  // namespace psmma

@@ -1,0 +1,155 @@
+"""GPU parity of the split path (modular BF16 tensor-core slices, FP64 recombination).
+
+Stated bound: relative Frobenius error <= 1e-12 against the FP64 oracle; integer fixtures
+whose products are exactly representable must match bit for bit."""
+import numpy as np
+import pytest
+
+from oracle import psmma_oracle as O
+from tests.conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12
+
+
+def _t(x, cuda):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(np.asarray(x).T)).to(cuda).t()
+
+
+def _np(t):
+    return t.t().contiguous().cpu().numpy().T
+
+
+def _split(kind, n, k, alpha, A, gen, beta, Q0, cuda, n_moduli=0, ld_pad=0):
+    import psmma_git_gb300 as P
+    import torch
+    dA = P.fortran_empty(n, k, torch.float64, cuda, ld=n + ld_pad)
+    dA.copy_(_t(A, cuda))
+    dQ = P.fortran_empty(n, k, torch.float64, cuda, ld=n + ld_pad)
+    dQ.copy_(_t(Q0, cuda))
+    dg = _t(gen, cuda) if kind == "cauchy" else torch.from_numpy(np.asarray(gen)).to(cuda)
+    getattr(P, "psmma_" + kind)(n, k, alpha, dA, dg, beta, dQ, precision="split", n_moduli=n_moduli)
+    torch.cuda.synchronize()
+    return _np(dQ)
+
+
+def _gen(kind, k, seed=3, clustered=0.0):
+    if kind == "cauchy":
+        return O.cfg_cauchy_generators(k, seed=seed, clustered=clustered)
+    return O.cfg_vector(2 * k - 1, seed=seed)
+
+
+def test_split_smoke_small(cuda):
+    n = k = 256
+    A = O.cfg_matrix(n, k, seed=1)
+    gen = _gen("cauchy", k)
+    got = _split("cauchy", n, k, 1.0, A, gen, 0.0, np.zeros((n, k)), cuda)
+    ref = O.dense_product("cauchy", 1.0, A, gen, 0.0, None, k)
+    assert O.rel_fro(got, ref) < TOL
+
+
+@pytest.mark.parametrize("kind", ["cauchy", "toeplitz", "hankel"])
+@pytest.mark.parametrize("n,k", [(1, 1), (5, 7), (256, 256), (300, 200), (129, 513), (1024, 1024)])
+def test_split_matches_dense_oracle(kind, n, k, cuda):
+    A = O.cfg_matrix(n, k, seed=n * 7 + k)
+    gen = _gen(kind, k)
+    Q0 = O.cfg_matrix(n, k, seed=2)
+    got = _split(kind, n, k, 0.75, A, gen, -1.5, Q0, cuda)
+    ref = O.dense_product(kind, 0.75, A, gen, -1.5, Q0, k)
+    assert O.rel_fro(got, ref) < TOL
+
+
+def test_split_clustered_cauchy(cuda):
+    # the split workload's distribution: 10% of the poles within 1e-10 of a neighbour, A ~ N(0,1)
+    n = k = 2048
+    A = O.cfg_matrix(n, k, seed=5, dist="normal")
+    gen = O.cfg_cauchy_generators(k, seed=6, clustered=0.1)
+    got = _split("cauchy", n, k, 1.0, A, gen, 0.0, np.zeros((n, k)), cuda)
+    ref = O.dense_product("cauchy", 1.0, A, gen, 0.0, None, k)
+    assert O.rel_fro(got, ref) < TOL
+
+
+def test_split_toeplitz_fixture_bit_exact(cuda):
+    z = np.load(GOLDEN / "toeplitz_kat.npz")
+    n = int(z["n"])
+    got = _split("toeplitz", n, n, 1.0, z["A"], z["g"], 0.0, np.zeros((n, n)), cuda)
+    np.testing.assert_array_equal(got, z["X"])
+
+
+def test_split_hankel_fixture_bit_exact(cuda):
+    z = np.load(GOLDEN / "hankel_exact.npz")
+    n = int(z["n"])
+    got = _split("hankel", n, n, 1.0, z["A"], z["g"], 0.0, np.zeros((n, n)), cuda)
+    np.testing.assert_array_equal(got, z["X"])
+
+
+def test_split_cauchy_reference_recipe(cuda):
+    z = np.load(GOLDEN / "cauchy_exact.npz")
+    n = int(z["n"])
+    got = _split("cauchy", n, n, 1.0, z["A"], z["gen"], 0.0, np.zeros((n, n)), cuda)
+    assert O.rel_fro(got, z["X"]) < TOL
+
+
+def test_split_beta_zero_ignores_q_and_ld(cuda):
+    n, k = 333, 270
+    A = O.cfg_matrix(n, k, seed=8)
+    gen = _gen("hankel", k)
+    got = _split("hankel", n, k, 2.0, A, gen, 0.0, np.full((n, k), np.nan), cuda, ld_pad=19)
+    assert np.isfinite(got).all()
+    assert O.rel_fro(got, O.dense_product("hankel", 2.0, A, gen, 0.0, None, k)) < TOL
+
+
+def test_split_nonfinite_row_gives_nan_row(cuda):
+    n = k = 64
+    A = O.cfg_matrix(n, k, seed=9)
+    A[5, 7] = np.inf
+    gen = _gen("toeplitz", k)
+    got = _split("toeplitz", n, k, 1.0, A, gen, 0.0, np.zeros((n, k)), cuda)
+    assert np.isnan(got[5]).all()
+    mask = np.ones(n, bool)
+    mask[5] = False
+    ref = O.dense_product("toeplitz", 1.0, A[mask], gen, 0.0, None, k)
+    assert O.rel_fro(got[mask], ref) < TOL
+
+
+def test_split_zero_rows_and_columns(cuda):
+    n = k = 96
+    A = O.cfg_matrix(n, k, seed=10)
+    A[3] = 0.0
+    g = _gen("hankel", k)
+    got = _split("hankel", n, k, 1.0, A, g, 0.0, np.zeros((n, k)), cuda)
+    assert (got[3] == 0.0).all()
+    assert O.rel_fro(got, O.dense_product("hankel", 1.0, A, g, 0.0, None, k)) < TOL
+
+
+@pytest.mark.parametrize("nmod", [10, 12, 16])
+def test_split_moduli_count_accuracy(nmod, cuda):
+    # fewer moduli -> fewer bits; the error must follow 2^-P and stay bounded
+    n = k = 512
+    A = O.cfg_matrix(n, k, seed=11)
+    gen = _gen("cauchy", k)
+    got = _split("cauchy", n, k, 1.0, A, gen, 0.0, np.zeros((n, k)), cuda, n_moduli=nmod)
+    err = O.rel_fro(got, O.dense_product("cauchy", 1.0, A, gen, 0.0, None, k))
+    bound = {10: 1e-6, 12: 1e-9, 16: 1e-14}[nmod]
+    assert err < bound
+
+
+def test_split_is_deterministic_and_matches_fp64_path(cuda):
+    import psmma_git_gb300 as P
+    import torch
+    n = k = 4096
+    A = O.cfg_matrix(n, k, seed=12)
+    gen = _gen("cauchy", k, seed=13)
+    dA = _t(A, cuda)
+    dg = _t(gen, cuda)
+    outs = []
+    for prec in ["split", "split", "fp64"]:
+        dQ = P.fortran_empty(n, k, torch.float64, cuda)
+        P.psmma_cauchy(n, k, 1.0, dA, dg, 0.0, dQ, precision=prec)
+        torch.cuda.synchronize()
+        outs.append(dQ)
+    assert torch.equal(outs[0], outs[1])
+    err = (torch.linalg.norm(outs[0] - outs[2]) / torch.linalg.norm(outs[2])).item()
+    assert err < TOL
