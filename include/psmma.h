@@ -55,6 +55,7 @@ extern "C" {
 #define PSMMA_EUNSUPPORTED  -114  /* option combination not supported                     */
 #define PSMMA_EWORKSPACE    -115  /* caller workspace smaller than psmma_workspace_size   */
 #define PSMMA_ERANGE        -116  /* split path: non-finite input or exponent out of range */
+#define PSMMA_ESCRATCH      -117  /* request exceeds the fixed scratch of psmma_cauchy_split_noalloc */
 
 /* ---- options ------------------------------------------------------------------------ */
 #define PSMMA_PREC_FP64   0   /* plain path: FP64 tensor-core MMA, H tile generated in smem  */
@@ -112,6 +113,20 @@ int pzmdftl(int n, int k, double alpha, const psmma_complex* B, int ldb,
  * tile is generated exactly, so this is the same computation as pzmdftl. */
 int pzmdftl1(int n, int k, double alpha, const psmma_complex* B, int ldb,
              double beta, psmma_complex* C, int ldc, const psmma_opts* opts, void* stream);
+
+/* No counterpart in the reference.  The split-path Cauchy multiply (same arguments and
+ * result as psmma_cauchy with opts->precision = PSMMA_PREC_SPLIT) for callers that cannot
+ * let a library allocate device memory -- they own all of it through their own pool, or
+ * run a latency-critical loop where cudaMalloc/cudaFree's device-wide synchronisation is
+ * not acceptable.  It allocates nothing: its workspace is a fixed 96 MiB device array of
+ * the library (held by every GPU that loads it until exit), so it accepts requests whose
+ * split workspace fits in it (n = k = 1024 with the default 14 moduli does) and returns
+ * PSMMA_ESCRATCH otherwise.  All calls share that array: calls that overlap on the GPU
+ * (other streams or threads) race and must be serialised by the caller.  The first call
+ * on a device looks up the array's address; make it before any stream capture. */
+int psmma_cauchy_split_noalloc(int n, int k, double alpha, const double* A, int lda,
+                               const double* gen, int ldgen, double beta, double* Q, int ldq,
+                               int n_moduli, void* stream);
 
 /* ---- host-pointer entry points (copy in, compute, copy out, synchronise) ------------ */
 int psmma_cauchy_host(int n, int k, double alpha, const double* A, int lda,

@@ -24,6 +24,7 @@ PSMMA_ESINGULAR = -113
 PSMMA_EUNSUPPORTED = -114
 PSMMA_EWORKSPACE = -115
 PSMMA_ERANGE = -116
+PSMMA_ESCRATCH = -117
 
 PREC_FP64 = 0
 PREC_SPLIT = 1
@@ -55,6 +56,7 @@ SIGNATURES = {
     "psmma_hankel": (_i, [_i, _i, _d, _p, _i, _p, _i, _d, _p, _i, _op, _p]),
     "pzmdftl": (_i, [_i, _i, _d, _p, _i, _d, _p, _i, _op, _p]),
     "pzmdftl1": (_i, [_i, _i, _d, _p, _i, _d, _p, _i, _op, _p]),
+    "psmma_cauchy_split_noalloc": (_i, [_i, _i, _d, _p, _i, _p, _i, _d, _p, _i, _i, _p]),
     "psmma_cauchy_host": (_i, [_i, _i, _d, _p, _i, _p, _i, _d, _p, _i, _op]),
     "psmma_toeplitz_host": (_i, [_i, _i, _d, _p, _i, _p, _i, _d, _p, _i, _op]),
     "psmma_hankel_host": (_i, [_i, _i, _d, _p, _i, _p, _i, _d, _p, _i, _op]),

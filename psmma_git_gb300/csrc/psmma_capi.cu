@@ -410,6 +410,7 @@ const char* psmma_status_string(int status) {
     case PSMMA_EUNSUPPORTED: return "unsupported option combination";
     case PSMMA_EWORKSPACE: return "workspace too small";
     case PSMMA_ERANGE: return "non-finite input or exponent out of range for the split path";
+    case PSMMA_ESCRATCH: return "request exceeds the 96 MiB fixed scratch of psmma_cauchy_split_noalloc";
     default: return "unknown status";
   }
 }
