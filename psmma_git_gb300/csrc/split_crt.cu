@@ -45,6 +45,12 @@ struct CrtConsts {
   float f[SPL_MAX_MODULI];                                        // C_l / M
   unsigned long long M_lo, M_hi;
   double log2M;
+  unsigned magic[SPL_MAX_MODULI];      // floor(2^32 / m): Barrett reduction of t < 2^30
+  unsigned climb[SPL_MAX_MODULI][4];   // C_l as four 32-bit limbs
+  unsigned bias[4];                    // 128 * sum_l C_l mod 2^128 (residues enter offset by 128)
+  int ffix[SPL_MAX_MODULI];            // round(2^19 * C_l / M): fixed-point quotient estimate
+  unsigned long long biasl[4];         // sum_l 128 * climb[l][t], per limb, unreduced
+  unsigned Mlimb[4];                   // M as four 32-bit limbs
 };
 
 // Device-side parameters of one call (in the workspace).
@@ -97,6 +103,24 @@ static CrtConsts make_consts(int nmod) {
   c.M_lo = (unsigned long long)M;
   c.M_hi = (unsigned long long)(M >> 64);
   c.log2M = l2 - 1e-9;
+  u128 bias = 0;
+  for (int l = 0; l < nmod; l++) {
+    c.magic[l] = (unsigned)((1ULL << 32) / (unsigned long long)kModuli[l]);
+    u128 C = ((u128)c.C_hi[l] << 64) | c.C_lo[l];
+    for (int t = 0; t < 4; t++) c.climb[l][t] = (unsigned)(C >> (32 * t));
+    bias += (u128)128 * C;  // wraps modulo 2^128
+  }
+  for (int t = 0; t < 4; t++) c.bias[t] = (unsigned)(bias >> (32 * t));
+  for (int t = 0; t < 4; t++) c.Mlimb[t] = (unsigned)(M >> (32 * t));
+  for (int t = 0; t < 4; t++) {
+    c.biasl[t] = 0;
+    for (int l = 0; l < nmod; l++) c.biasl[t] += 128ull * c.climb[l][t];
+  }
+  for (int l = 0; l < nmod; l++) {
+    u128 C = ((u128)c.C_hi[l] << 64) | c.C_lo[l];
+    long double cf = (long double)C / (long double)M;
+    c.ffix[l] = (int)std::llround((double)(cf * 524288.0L));  // |sum_l r_l ffix_l| < 16*128*2^19 = 2^30
+  }
   return c;
 }
 
@@ -230,25 +254,63 @@ __device__ __forceinline__ int scale_exp(unsigned long long amax_bits, int P) {
   return P - 1 - ilogb(__longlong_as_double((long long)amax_bits));
 }
 
-// Symmetric residue of the integer x (|x| <= 2^53) modulo m, as an exact float.
-__device__ __forceinline__ float sym_residue(unsigned long long ux, bool neg, int m, float inv_m, int c21, int c42) {
-  int x0 = (int)(ux & 0x1FFFFFull);
-  int x1 = (int)((ux >> 21) & 0x1FFFFFull);
-  int x2 = (int)(ux >> 42);
-  int t = x2 * c42 + x1 * c21 + x0;  // < 2^30, t == x (mod m)
-  int q = __float2int_rn(__int2float_rn(t) * inv_m);
-  int r = t - q * m;
-  int half = m >> 1;
-  r = (r > half) ? r - m : r;
-  r = (r < -half) ? r + m : r;
-  return (float)(neg ? -r : r);
+// rint(x * 2^e) (round half to even) for finite x with |x * 2^e| < 2^53, computed from the
+// bits of x with integer operations only; *neg receives the sign.
+__device__ __forceinline__ unsigned long long scaled_int(double x, int e, bool* neg) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  *neg = (b >> 63) != 0;
+  const int ex = (int)((b >> 52) & 0x7FF);
+  unsigned long long m = b & 0xFFFFFFFFFFFFFull;
+  int E = -1074;
+  if (ex != 0) {
+    m |= 1ull << 52;
+    E = ex - 1075;
+  }
+  if (m == 0) return 0;
+  const int sh = E + e;
+  if (sh >= 0) return m << sh;  // the caller's bound keeps the result below 2^53
+  const int k = -sh;
+  if (k > 63) return 0;  // below one half
+  unsigned long long q = m >> k;
+  const unsigned long long rem = m & ((1ull << k) - 1);
+  const unsigned long long half = 1ull << (k - 1);
+  if (rem > half || (rem == half && (q & 1))) ++q;
+  return q;
 }
 
-// Integer-scaled value rint(x * 2^e) as (|.|, sign); x finite.
-__device__ __forceinline__ unsigned long long scaled_int(double x, int e, bool* neg) {
-  double y = rint(ldexp(x, e));
-  *neg = y < 0.0;
-  return (unsigned long long)fabs(y);
+// Symmetric residue (|r| <= m/2) of the integer x = x2*2^42 + x1*2^21 + x0 (x < 2^53, chunks
+// of 21 bits) modulo m, negated when neg.  t = x mod-equivalent < 2^30, reduced by Barrett
+// division with magic = floor(2^32/m) (quotient exact or one too small).
+__device__ __forceinline__ int sym_residue(unsigned x0, unsigned x1, unsigned x2, bool neg, unsigned m,
+                                           unsigned magic, unsigned c21, unsigned c42) {
+  const unsigned t = x2 * c42 + x1 * c21 + x0;
+  const unsigned q = __umulhi(t, magic);
+  int r = (int)(t - q * m);
+  r = (r >= (int)m) ? r - (int)m : r;
+  r = (r > (int)(m >> 1)) ? r - (int)m : r;
+  return neg ? -r : r;
+}
+
+// BF16 bits of an integer with |r| <= 2^8 (exact): float via the 1.5*2^23 magic number, then
+// the top half of its bits.
+__device__ __forceinline__ unsigned bf16_small(int r) {
+  return __float_as_uint(__int_as_float(0x4B400000 + r) - 12582912.0f) >> 16;
+}
+
+// Residues of two neighbouring integers for every modulus, packed as bf16x2 into planes.
+__device__ __forceinline__ void write_residue_pair(unsigned long long u0, bool n0, unsigned long long u1, bool n1,
+                                                   const CrtConsts& cc, uint32_t* dst, size_t plane_words) {
+  const unsigned a0 = (unsigned)(u0 & 0x1FFFFFull), a1 = (unsigned)((u0 >> 21) & 0x1FFFFFull),
+                 a2 = (unsigned)(u0 >> 42);
+  const unsigned b0 = (unsigned)(u1 & 0x1FFFFFull), b1 = (unsigned)((u1 >> 21) & 0x1FFFFFull),
+                 b2 = (unsigned)(u1 >> 42);
+#pragma unroll 4
+  for (int l = 0; l < cc.nmod; ++l) {
+    const unsigned m = (unsigned)cc.m[l], mg = cc.magic[l], c21 = (unsigned)cc.c21[l], c42 = (unsigned)cc.c42[l];
+    const int r0 = sym_residue(a0, a1, a2, n0, m, mg, c21, c42);
+    const int r1 = sym_residue(b0, b1, b2, n1, m, mg, c21, c42);
+    dst[l * plane_words] = bf16_small(r0) | (bf16_small(r1) << 16);
+  }
 }
 
 // RA[l][i][kk] = residues of A' (bf16), rows i, K-major.  Block: 32 rows x 64 k.
@@ -272,17 +334,11 @@ __global__ void k_residues_A(const double* __restrict__ A, long lda, int n, int 
     bool ok = ab > 0 && ab < INF_BITS;
     int e = ok ? scale_exp(ab, P) : 0;
     int kk = 2 * tx;
-    bool n0, n1;
+    bool n0 = false, n1 = false;
     unsigned long long u0 = ok ? scaled_int(tile[kk][r], e, &n0) : 0ull;
     unsigned long long u1 = ok ? scaled_int(tile[kk + 1][r], e, &n1) : 0ull;
-    if (!ok) { n0 = n1 = false; }
-    __nv_bfloat162* dst = (__nv_bfloat162*)(RA + (size_t)gi * kp + k0 + kk);
-#pragma unroll 4
-    for (int l = 0; l < cc.nmod; ++l) {
-      float r0 = sym_residue(u0, n0, cc.m[l], cc.inv_m[l], cc.c21[l], cc.c42[l]);
-      float r1 = sym_residue(u1, n1, cc.m[l], cc.inv_m[l], cc.c21[l], cc.c42[l]);
-      *(__nv_bfloat162*)((__nv_bfloat16*)dst + l * plane) = __floats2bfloat162_rn(r0, r1);
-    }
+    uint32_t* dst = (uint32_t*)(RA + (size_t)gi * kp + k0 + kk);
+    write_residue_pair(u0, n0, u1, n1, cc, dst, plane / 2);
   }
 }
 
@@ -302,13 +358,8 @@ __global__ void k_residues_H(const double* __restrict__ Ht, int k, int kp,
   unsigned long long u0 = ok ? scaled_int(h.x, e, &n0) : 0ull;
   unsigned long long u1 = ok ? scaled_int(h.y, e, &n1) : 0ull;
   const size_t plane = (size_t)k * kp;
-  __nv_bfloat16* dst = RH + (size_t)j * kp + kk;
-#pragma unroll 4
-  for (int l = 0; l < cc.nmod; ++l) {
-    float r0 = sym_residue(u0, n0, cc.m[l], cc.inv_m[l], cc.c21[l], cc.c42[l]);
-    float r1 = sym_residue(u1, n1, cc.m[l], cc.inv_m[l], cc.c21[l], cc.c42[l]);
-    *(__nv_bfloat162*)(dst + l * plane) = __floats2bfloat162_rn(r0, r1);
-  }
+  uint32_t* dst = (uint32_t*)(RH + (size_t)j * kp + kk);
+  write_residue_pair(u0, n0, u1, n1, cc, dst, plane / 2);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -327,13 +378,31 @@ constexpr uint32_t G_B_BYTES = G_BN * G_BK * 2;
 constexpr size_t G_SMEM = 1024 + (size_t)G_STAGES * (G_A_BYTES + G_B_BYTES) + 256;
 
 struct GemmArgs {
-  int n, kr, nkb, tiles_m, tiles_n, group_m;
+  int n, kr, nkb, tiles_m, tiles_n, group_m, nmod;
   int8_t* R;
   unsigned* status;
   int m[SPL_MAX_MODULI];
   float inv_m[SPL_MAX_MODULI];
 };
 
+// Tile t of the launch -> (modulus, row tile, column tile).  Moduli are outermost; inside a
+// modulus group_m row tiles sweep all column tiles together (L2 reuse of both operands).
+__device__ __forceinline__ void gemm_tile(const GemmArgs& g, int t, int& l, int& tm, int& tn) {
+  const int per_mod = g.tiles_m * g.tiles_n;
+  l = t / per_mod;
+  const int b = t - l * per_mod;
+  const int per_group = g.group_m * g.tiles_n;
+  const int grp = b / per_group;
+  const int first_m = grp * g.group_m;
+  const int gm = min(g.group_m, g.tiles_m - first_m);
+  const int rr = b - grp * per_group;
+  tm = first_m + rr % gm;
+  tn = rr / gm;
+}
+
+// Persistent: one CTA per SM walks tiles t = blockIdx.x, blockIdx.x + gridDim.x, ...  The
+// stage ring and the two TMEM accumulators continue across tiles, so the loads and MMAs of
+// the next tile overlap the drain and residue store of the previous one.
 __global__ void __launch_bounds__(G_THREADS, 1)
     k_crt_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, GemmArgs g) {
   extern __shared__ uint8_t smem_raw[];
@@ -350,15 +419,6 @@ __global__ void __launch_bounds__(G_THREADS, 1)
   volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int l = blockIdx.y;
-  // grouped raster: group_m row tiles sweep all column tiles together (L2 reuse)
-  const int bid = blockIdx.x;
-  const int per_group = g.group_m * g.tiles_n;
-  const int grp = bid / per_group;
-  const int first_m = grp * g.group_m;
-  const int gm = min(g.group_m, g.tiles_m - first_m);
-  const int rr = bid - grp * per_group;
-  const int tm = first_m + rr % gm, tn = rr / gm;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < G_STAGES; ++s) {
@@ -382,56 +442,63 @@ __global__ void __launch_bounds__(G_THREADS, 1)
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem_base = *tmem_slot;
-  const int nkb = *abort_flag ? 0 : g.nkb;
-  const int nchunks = (nkb + G_CHUNK_KB - 1) / G_CHUNK_KB;
+  const int nkb = g.nkb;
+  const int cpt = (nkb + G_CHUNK_KB - 1) / G_CHUNK_KB;  // chunks per tile
+  const int total = *abort_flag ? 0 : g.tiles_m * g.tiles_n * g.nmod;
 
   if (warp == G_EPI_WARPS) {
     // ---------------- TMA producer ----------------
     if (lane == 0) {
       prefetch_tmap(&tmA);
       prefetch_tmap(&tmB);
-      int issued = 0;
-      for (int kb = 0; kb < nkb; ++kb) {
-        const int s = kb % G_STAGES;
-        const uint32_t ph = (kb / G_STAGES) & 1;
-        if (!mbar_wait(&empty[s], ph ^ 1, g.status, abort_flag)) break;
-        mbar_arrive_expect_tx(&full[s], G_A_BYTES + G_B_BYTES);
-        tma_load_3d(sA + s * G_A_BYTES, &tmA, &full[s], kb * G_BK, tm * G_BM, l);
-        tma_load_3d(sB + s * G_B_BYTES, &tmB, &full[s], kb * G_BK, tn * G_BN, l);
-        issued = kb + 1;
+      int it = 0, issued = 0;
+      bool ok = true;
+      for (int t = blockIdx.x; t < total && ok; t += gridDim.x) {
+        int l, tm, tn;
+        gemm_tile(g, t, l, tm, tn);
+        for (int kb = 0; kb < nkb; ++kb, ++it) {
+          const int s = it % G_STAGES;
+          if (!mbar_wait(&empty[s], ((it / G_STAGES) & 1) ^ 1, g.status, abort_flag)) { ok = false; break; }
+          mbar_arrive_expect_tx(&full[s], G_A_BYTES + G_B_BYTES);
+          tma_load_3d(sA + s * G_A_BYTES, &tmA, &full[s], kb * G_BK, tm * G_BM, l);
+          tma_load_3d(sB + s * G_B_BYTES, &tmB, &full[s], kb * G_BK, tn * G_BN, l);
+          issued = it + 1;
+        }
       }
       // every issued copy must have landed before the CTA may exit
-      for (int kb = max(0, issued - G_STAGES); kb < issued; ++kb)
-        mbar_wait_drain(&full[kb % G_STAGES], (kb / G_STAGES) & 1, g.status);
+      for (int q = max(0, issued - G_STAGES); q < issued; ++q)
+        mbar_wait_drain(&full[q % G_STAGES], (q / G_STAGES) & 1, g.status);
     }
     __syncwarp();
   } else if (warp == G_EPI_WARPS + 1) {
     // ---------------- MMA issuer ----------------
     if (lane == 0) {
       const uint32_t idesc = idesc_bf16_f32(G_BM, G_BN);
-      int kb = 0;
+      int it = 0, c = 0;
       bool ok = true;
-      for (int c = 0; c < nchunks && ok; ++c) {
-        const int buf = c & 1;
-        const uint32_t use = (uint32_t)(c >> 1);
-        if (!mbar_wait(&acc_empty[buf], (use & 1) ^ 1, g.status, abort_flag)) break;
-        tc_fence_after();
-        const uint32_t dt = tmem_base + (uint32_t)(buf * G_BN);
-        const int kend = min(nkb, kb + G_CHUNK_KB);
-        uint32_t acc = 0;
-        for (; kb < kend; ++kb) {
-          const int s = kb % G_STAGES;
-          if (!mbar_wait(&full[s], (kb / G_STAGES) & 1, g.status, abort_flag)) { ok = false; break; }
+      for (int t = blockIdx.x; t < total && ok; t += gridDim.x) {
+        for (int cc = 0; cc < cpt && ok; ++cc, ++c) {
+          const int buf = c & 1;
+          const uint32_t use = (uint32_t)(c >> 1);
+          if (!mbar_wait(&acc_empty[buf], (use & 1) ^ 1, g.status, abort_flag)) { ok = false; break; }
           tc_fence_after();
-          const uint32_t a0 = smem_u32(sA + s * G_A_BYTES), b0 = smem_u32(sB + s * G_B_BYTES);
+          const uint32_t dt = tmem_base + (uint32_t)(buf * G_BN);
+          const int kend = min(nkb, (cc + 1) * G_CHUNK_KB);
+          uint32_t acc = 0;
+          for (int kb = cc * G_CHUNK_KB; kb < kend; ++kb, ++it) {
+            const int s = it % G_STAGES;
+            if (!mbar_wait(&full[s], (it / G_STAGES) & 1, g.status, abort_flag)) { ok = false; break; }
+            tc_fence_after();
+            const uint32_t a0 = smem_u32(sA + s * G_A_BYTES), b0 = smem_u32(sB + s * G_B_BYTES);
 #pragma unroll
-          for (int kk = 0; kk < G_BK / 16; ++kk) {
-            tc_mma_bf16(dt, sdesc_sw128_kmajor(a0 + kk * 32), sdesc_sw128_kmajor(b0 + kk * 32), idesc, acc);
-            acc = 1;
+            for (int kk = 0; kk < G_BK / 16; ++kk) {
+              tc_mma_bf16(dt, sdesc_sw128_kmajor(a0 + kk * 32), sdesc_sw128_kmajor(b0 + kk * 32), idesc, acc);
+              acc = 1;
+            }
+            tc_commit(&empty[s]);
           }
-          tc_commit(&empty[s]);
+          if (ok) tc_commit(&acc_full[buf]);
         }
-        if (ok) tc_commit(&acc_full[buf]);
       }
       // all tcgen05 work of this thread must complete before TMEM is released
       tc_commit(mma_done);
@@ -441,49 +508,54 @@ __global__ void __launch_bounds__(G_THREADS, 1)
   } else {
     // ---------------- accumulator drain (epilogue) ----------------
     const int q = warp & 3, h = warp >> 2;
-    const float m = (float)g.m[l], inv_m = g.inv_m[l];
-    float res[128];
-#pragma unroll
-    for (int e = 0; e < 128; ++e) res[e] = 0.0f;
+    int c = 0;
     bool ok = true;
-    for (int c = 0; c < nchunks; ++c) {
-      const int buf = c & 1;
-      const uint32_t use = (uint32_t)(c >> 1);
-      if (!mbar_wait(&acc_full[buf], use & 1, g.status, abort_flag)) { ok = false; break; }
-      tc_fence_after();
+    for (int t = blockIdx.x; t < total && ok; t += gridDim.x) {
+      int l, tm, tn;
+      gemm_tile(g, t, l, tm, tn);
+      const float m = (float)g.m[l], inv_m = g.inv_m[l];
+      float res[128];
 #pragma unroll
-      for (int cb = 0; cb < 4; ++cb) {
-        uint32_t r[32];
-        tmem_ld32(tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * G_BN + h * 128 + cb * 32), r);
-        tmem_ld_wait();
+      for (int e = 0; e < 128; ++e) res[e] = 0.0f;
+      for (int cc = 0; cc < cpt; ++cc, ++c) {
+        const int buf = c & 1;
+        const uint32_t use = (uint32_t)(c >> 1);
+        if (!mbar_wait(&acc_full[buf], use & 1, g.status, abort_flag)) { ok = false; break; }
+        tc_fence_after();
 #pragma unroll
-        for (int e = 0; e < 32; ++e) {
-          float v = __uint_as_float(r[e]) + res[cb * 32 + e];  // exact: |v| < 2^24
-          float qq = rintf(v * inv_m);
-          float x = fmaf(-qq, m, v);
-          x = (x > 127.0f) ? x - m : x;
-          x = (x < -128.0f) ? x + m : x;
-          res[cb * 32 + e] = x;
+        for (int cb = 0; cb < 4; ++cb) {
+          uint32_t r[32];
+          tmem_ld32(tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * G_BN + h * 128 + cb * 32), r);
+          tmem_ld_wait();
+#pragma unroll
+          for (int e = 0; e < 32; ++e) {
+            float v = __uint_as_float(r[e]) + res[cb * 32 + e];  // exact: |v| < 2^24
+            float qq = rintf(v * inv_m);
+            float x = fmaf(-qq, m, v);
+            x = (x > 127.0f) ? x - m : x;
+            x = (x < -128.0f) ? x + m : x;
+            res[cb * 32 + e] = x;
+          }
         }
+        tc_fence_before();
+        mbar_arrive(&acc_empty[buf]);
       }
-      tc_fence_before();
-      mbar_arrive(&acc_empty[buf]);
-    }
-    const int i = tm * G_BM + q * 32 + lane;
-    if (ok && !*abort_flag && i < g.n) {
-      int8_t* dst = g.R + ((size_t)l * g.n + i) * g.kr + (size_t)tn * G_BN + h * 128;
+      const int i = tm * G_BM + q * 32 + lane;
+      if (ok && !*abort_flag && i < g.n) {
+        int8_t* dst = g.R + ((size_t)l * g.n + i) * g.kr + (size_t)tn * G_BN + h * 128;
 #pragma unroll
-      for (int v = 0; v < 8; ++v) {
-        uint32_t w[4];
+        for (int v = 0; v < 8; ++v) {
+          uint32_t w[4];
 #pragma unroll
-        for (int t = 0; t < 4; ++t) {
-          uint32_t b0 = (uint32_t)(uint8_t)(int8_t)__float2int_rn(res[v * 16 + t * 4 + 0]);
-          uint32_t b1 = (uint32_t)(uint8_t)(int8_t)__float2int_rn(res[v * 16 + t * 4 + 1]);
-          uint32_t b2 = (uint32_t)(uint8_t)(int8_t)__float2int_rn(res[v * 16 + t * 4 + 2]);
-          uint32_t b3 = (uint32_t)(uint8_t)(int8_t)__float2int_rn(res[v * 16 + t * 4 + 3]);
-          w[t] = b0 | (b1 << 8) | (b2 << 16) | (b3 << 24);
+          for (int t4 = 0; t4 < 4; ++t4) {
+            uint32_t b0 = (uint32_t)(uint8_t)(int8_t)__float2int_rn(res[v * 16 + t4 * 4 + 0]);
+            uint32_t b1 = (uint32_t)(uint8_t)(int8_t)__float2int_rn(res[v * 16 + t4 * 4 + 1]);
+            uint32_t b2 = (uint32_t)(uint8_t)(int8_t)__float2int_rn(res[v * 16 + t4 * 4 + 2]);
+            uint32_t b3 = (uint32_t)(uint8_t)(int8_t)__float2int_rn(res[v * 16 + t4 * 4 + 3]);
+            w[t4] = b0 | (b1 << 8) | (b2 << 16) | (b3 << 24);
+          }
+          *(uint4*)(dst + v * 16) = make_uint4(w[0], w[1], w[2], w[3]);
         }
-        *(uint4*)(dst + v * 16) = make_uint4(w[0], w[1], w[2], w[3]);
       }
     }
   }
@@ -498,53 +570,138 @@ __global__ void __launch_bounds__(G_THREADS, 1)
 // 32 x 32 output tile per block (32 x 8 threads), transposed through shared memory so that
 // both the residue reads (row-major) and the Q writes (column-major) are coalesced.
 // ------------------------------------------------------------------------------------------
-__global__ void k_crt_combine(const int8_t* __restrict__ R, int n, int k, int kr, CrtConsts cc,
-                              const unsigned long long* __restrict__ amax_bits,
-                              const unsigned long long* __restrict__ hmax_bits, const SplitDevParams* prm,
-                              double alpha, double beta, double* __restrict__ Q, long ldq) {
-  __shared__ double tile[32][33];
-  typedef unsigned __int128 u128;
+typedef unsigned __int128 u128;
+
+// (hi:lo) * 2^-e as a double, (hi:lo) a non-negative 128-bit integer in two words, rounded
+// to nearest even from the bits; results outside the normal range go through ldexp.
+__device__ __forceinline__ double u128w_scaled(unsigned long long hi, unsigned long long lo, bool neg, int e) {
+  if ((hi | lo) == 0) return 0.0;
+  // normalise so that the leading bit is bit 63 of `top`; `rest` keeps the bits below
+  int p;
+  unsigned long long top, rest;
+  if (hi) {
+    const int s = __clzll((long long)hi);
+    p = 127 - s;
+    top = s ? (hi << s) | (lo >> (64 - s)) : hi;
+    rest = s ? (lo << s) : lo;
+  } else {
+    const int s = __clzll((long long)lo);
+    p = 63 - s;
+    top = lo << s;
+    rest = 0;
+  }
+  unsigned long long m = top >> 11;  // 53 bits
+  const unsigned long long low11 = top & 0x7FFull;
+  const bool sticky = (low11 & 0x3FFull) != 0 || rest != 0;
+  if ((low11 & 0x400ull) && (sticky || (m & 1))) {
+    ++m;
+    if (m == (1ull << 53)) {
+      m >>= 1;
+      ++p;
+    }
+  }
+  const int field = p - e + 1023;
+  if (field >= 1 && field <= 2046) {
+    unsigned long long bits = ((unsigned long long)field << 52) | (m & 0xFFFFFFFFFFFFFull);
+    if (neg) bits |= 1ull << 63;
+    return __longlong_as_double((long long)bits);
+  }
+  const double v = ldexp((double)m, p - 52 - e);
+  return neg ? -v : v;
+}
+
+// One block: 32 rows x 128 columns (32 x 8 threads); a thread recombines 4 neighbouring
+// columns of one row per pass from 32-bit loads (4 residues) of each plane, so each warp
+// request moves 128 bytes.  Per modulus and element: four 32x32->64-bit multiply-adds for
+// the limbs of sum_l (r_l + 128) C_l and one for the fixed-point quotient estimate.
+constexpr int CRT_TI = 32, CRT_TJ = 128;
+
+__global__ void __launch_bounds__(256) k_crt_combine(const int8_t* __restrict__ R, int n, int k, int kr,
+                                                     CrtConsts cc, const unsigned long long* __restrict__ amax_bits,
+                                                     const unsigned long long* __restrict__ hmax_bits,
+                                                     const SplitDevParams* prm, double alpha, double beta,
+                                                     double* __restrict__ Q, long ldq) {
+  __shared__ double tile[CRT_TJ][CRT_TI + 1];
   const int tx = threadIdx.x, ty = threadIdx.y;
-  const int i0 = blockIdx.y * 32, j0 = blockIdx.x * 32;
+  const int i0 = blockIdx.y * CRT_TI, j0 = blockIdx.x * CRT_TJ;
   const int P = prm->P;
-  const u128 M = ((u128)cc.M_hi << 64) | cc.M_lo;
-  const int j = j0 + tx;
-  unsigned long long hb = j < k ? hmax_bits[j] : 0ull;
-  for (int a = 0; a < 4; ++a) {
+  const int jb = j0 + 4 * tx;
+  unsigned long long hb[4];
+  int fexp[4];
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    hb[c] = (jb + c < k) ? hmax_bits[jb + c] : 0ull;
+    fexp[c] = (hb[c] != 0 && hb[c] < INF_BITS) ? scale_exp(hb[c], P) : 0;
+  }
+  const size_t plane_w = (size_t)n * kr / 4;
+  for (int a = 0; a < CRT_TI / 8; ++a) {
     const int il = ty + 8 * a, i = i0 + il;
-    double val = 0.0;
-    if (i < n && j < k) {
-      unsigned long long ab = amax_bits[i];
-      if (ab >= INF_BITS || hb >= INF_BITS) {
-        val = __longlong_as_double(0x7FF8000000000000ll);  // NaN: non-finite input row/column
-      } else if (ab != 0 && hb != 0) {
-        float qf = 0.0f;
-        u128 S = 0;
-        const int8_t* src = R + (size_t)i * kr + j;
-        for (int l = 0; l < cc.nmod; ++l) {
-          int r = (int)src[(size_t)l * n * kr];
-          qf = fmaf((float)r, cc.f[l], qf);
-          u128 C = ((u128)cc.C_hi[l] << 64) | cc.C_lo[l];
-          S += (u128)(__int128)r * C;  // wraps modulo 2^128
+    double val[4] = {0.0, 0.0, 0.0, 0.0};
+    if (i < n && jb < k) {
+      const unsigned long long ab = amax_bits[i];
+      const int sexp = (ab != 0 && ab < INF_BITS) ? scale_exp(ab, P) : 0;
+      unsigned long long acc[4][4];
+      int qi[4];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        qi[c] = 0;
+#pragma unroll
+        for (int t = 0; t < 4; ++t) acc[c][t] = 0;
+      }
+      const uint32_t* src = (const uint32_t*)(R + (size_t)i * kr + jb);
+      for (int l = 0; l < cc.nmod; ++l) {
+        const uint32_t w4 = __ldg(src + (size_t)l * plane_w);
+        const int ff = cc.ffix[l];
+        const unsigned c0 = cc.climb[l][0], c1 = cc.climb[l][1], c2 = cc.climb[l][2], c3 = cc.climb[l][3];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          const int r = (int)(int8_t)(w4 >> (8 * c));
+          qi[c] += r * ff;
+          const unsigned ur = (unsigned)(r + 128);
+          acc[c][0] += (unsigned long long)ur * c0;
+          acc[c][1] += (unsigned long long)ur * c1;
+          acc[c][2] += (unsigned long long)ur * c2;
+          acc[c][3] += (unsigned long long)ur * c3;
         }
-        long long qi = (long long)rintf(qf);
-        u128 Zu = S - (u128)(__int128)qi * M;
-        __int128 Z = (__int128)Zu;
-        long long zh = (long long)(Z >> 64);
-        unsigned long long zl = (unsigned long long)Z;
-        double z = fma((double)zh, 18446744073709551616.0, (double)zl);
-        int e = scale_exp(ab, P) + scale_exp(hb, P);
-        val = ldexp(z, -e);
+      }
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        if (ab >= INF_BITS || hb[c] >= INF_BITS) {
+          val[c] = __longlong_as_double(0x7FF8000000000000ll);  // NaN: non-finite input row/column
+        } else if (ab != 0 && hb[c] != 0) {
+          // Z = sum_l r_l C_l - q*M in signed 64-bit limbs (|limb terms| < 2^46), then carries
+          const long long q = (long long)((qi[c] + (1 << 18)) >> 19);
+          long long z0 = (long long)acc[c][0] - (long long)cc.biasl[0] - q * (long long)cc.Mlimb[0];
+          long long z1 = (long long)acc[c][1] - (long long)cc.biasl[1] - q * (long long)cc.Mlimb[1];
+          long long z2 = (long long)acc[c][2] - (long long)cc.biasl[2] - q * (long long)cc.Mlimb[2];
+          long long z3 = (long long)acc[c][3] - (long long)cc.biasl[3] - q * (long long)cc.Mlimb[3];
+          z1 += z0 >> 32;
+          z2 += z1 >> 32;
+          z3 += z2 >> 32;  // exact: z3 holds the sign and top bits of Z (|Z| < 2^126)
+          const unsigned long long L0 = (unsigned long long)z0 & 0xFFFFFFFFull;
+          const unsigned long long L1 = (unsigned long long)z1 & 0xFFFFFFFFull;
+          const unsigned long long L2 = (unsigned long long)z2 & 0xFFFFFFFFull;
+          unsigned long long hi = ((unsigned long long)z3 << 32) | L2, lo = (L1 << 32) | L0;
+          const bool neg = z3 < 0;
+          if (neg) {  // two's-complement negate of the 128-bit value
+            lo = ~lo + 1;
+            hi = ~hi + (lo == 0 ? 1 : 0);
+          }
+          val[c] = u128w_scaled(hi, lo, neg, sexp + fexp[c]);
+        }
       }
     }
-    tile[tx][il] = val;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) tile[4 * tx + c][il] = val[c];
   }
   __syncthreads();
-  for (int a = 0; a < 4; ++a) {
-    const int jl = ty + 8 * a, jj = j0 + jl, i = i0 + tx;
+  const int i = i0 + tx;
+  for (int b = 0; b < CRT_TJ / 8; ++b) {
+    const int jl = ty + 8 * b, jj = j0 + jl;
     if (i < n && jj < k) {
       double* qp = Q + i + (long)jj * ldq;
-      double v = alpha * tile[jl][tx];
+      double v = tile[jl][tx];
+      if (alpha != 1.0) v *= alpha;
       if (beta != 0.0) v = fma(beta, *qp, v);
       *qp = v;
     }
@@ -645,11 +802,15 @@ int launch_split(int kind, int n, int k, double alpha, const double* A, long lda
   for (int l = 0; l < nmod; ++l) { ga.m[l] = cc.m[l]; ga.inv_m[l] = cc.inv_m[l]; }
   if (cudaFuncSetAttribute(k_crt_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G_SMEM) != cudaSuccess)
     return PSMMA_EDEVICE;
-  dim3 gg(ga.tiles_m * ga.tiles_n, nmod);
-  k_crt_gemm<<<gg, G_THREADS, G_SMEM, stream>>>(tmA, tmB, ga);
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return PSMMA_EDEVICE;
+  ga.nmod = nmod;
+  const int total_tiles = ga.tiles_m * ga.tiles_n * nmod;
+  k_crt_gemm<<<std::min(sms, total_tiles), G_THREADS, G_SMEM, stream>>>(tmA, tmB, ga);
   prof_mark(stream, "modular_gemm");
 
-  dim3 gc((k + 31) / 32, (n + 31) / 32);
+  dim3 gc((k + CRT_TJ - 1) / CRT_TJ, (n + CRT_TI - 1) / CRT_TI);
   k_crt_combine<<<gc, dim3(32, 8), 0, stream>>>(R, n, k, L.kr, cc, amax, hmax, prm, alpha, beta, Q, ldq);
   prof_mark(stream, "crt_combine");
   if (cudaGetLastError() != cudaSuccess) return PSMMA_EDEVICE;
