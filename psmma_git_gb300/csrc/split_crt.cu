@@ -56,7 +56,7 @@ struct CrtConsts {
 // Device-side parameters of one call (in the workspace).
 struct SplitDevParams {
   unsigned status;
-  int P;
+  int PA, PH;                   // bits of the integer-scaled A (per row) and H (per column)
   unsigned long long rho_bits;  // max_j sum_k |H_kj| / max_k |H_kj| (bits of a positive double)
 };
 
@@ -131,7 +131,7 @@ static size_t al1k(size_t x) { return (x + 1023) & ~(size_t)1023; }
 
 struct SplitLayout {
   int kp, kr;
-  size_t off_params, off_amax, off_hmax, off_hsum, off_ht, off_ra, off_rh, off_r, total;
+  size_t off_params, off_amax, off_hmax, off_hsum, off_asq, off_hsq, off_ht, off_ra, off_rh, off_r, total;
 };
 
 static SplitLayout split_layout(int n, int k, int nmod) {
@@ -143,6 +143,8 @@ static SplitLayout split_layout(int n, int k, int nmod) {
   L.off_amax = o;   o += al1k((size_t)n * 8);
   L.off_hmax = o;   o += al1k((size_t)k * 8);
   L.off_hsum = o;   o += al1k((size_t)k * 8);
+  L.off_asq = o;    o += al1k((size_t)n * 8);
+  L.off_hsq = o;    o += al1k((size_t)k * 8);
   L.off_ht = o;     o += al1k((size_t)k * L.kp * 8);
   L.off_ra = o;     o += al1k((size_t)nmod * n * L.kp * 2);
   L.off_rh = o;     o += al1k((size_t)nmod * k * L.kp * 2);
@@ -165,18 +167,23 @@ size_t split_workspace_bytes(int kind, int n, int k, int n_moduli) {
 constexpr unsigned long long ABS_MASK = 0x7FFFFFFFFFFFFFFFull;
 constexpr unsigned long long INF_BITS = 0x7FF0000000000000ull;
 
-// Row max of |A| as the bits of a non-negative double (NaN/Inf compare above all finite).
+// Row max of |A| as the bits of a non-negative double (NaN/Inf compare above all finite) and
+// row sums of squares (for the Cauchy-Schwarz bound of the integer product).
 __global__ void k_row_absmax(const double* __restrict__ A, long lda, int n, int k, int kchunk,
-                             unsigned long long* __restrict__ amax_bits) {
+                             unsigned long long* __restrict__ amax_bits, double* __restrict__ asq) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   int k0 = blockIdx.y * kchunk, k1 = min(k, k0 + kchunk);
   unsigned long long mb = 0;
+  double sq = 0.0;
   for (int kk = k0; kk < k1; ++kk) {
-    unsigned long long b = (unsigned long long)__double_as_longlong(__ldg(A + i + (long)kk * lda)) & ABS_MASK;
+    const double a = __ldg(A + i + (long)kk * lda);
+    unsigned long long b = (unsigned long long)__double_as_longlong(a) & ABS_MASK;
     mb = b > mb ? b : mb;
+    sq = fma(a, a, sq);
   }
   if (mb) atomicMax(amax_bits + i, mb);
+  if (sq != 0.0) atomicAdd(asq + i, sq);
 }
 
 // H pass 1: Ht[j][kk] = H(kk, j) in FP64, column max |H| and column sum |H|, and the global
@@ -184,7 +191,7 @@ __global__ void k_row_absmax(const double* __restrict__ A, long lda, int n, int 
 template <int KIND>
 __global__ void k_h_pass1(const double* __restrict__ gen, long ldgen, int k, int kp, double* __restrict__ Ht,
                           unsigned long long* __restrict__ hmax_bits, double* __restrict__ hsum,
-                          SplitDevParams* prm) {
+                          double* __restrict__ hsq, SplitDevParams* prm) {
   const int j = blockIdx.x;
   double w = 0.0, v = 0.0;
   if (KIND == KIND_CAUCHY) {
@@ -192,7 +199,7 @@ __global__ void k_h_pass1(const double* __restrict__ gen, long ldgen, int k, int
     v = __ldg(gen + 3 * ldgen + j);   // V(j)
   }
   unsigned long long mb = 0;
-  double s = 0.0;
+  double s = 0.0, s2 = 0.0;
   double* row = Ht + (long)j * kp;
   for (int kk = threadIdx.x; kk < kp; kk += blockDim.x) {
     double h = 0.0;
@@ -210,29 +217,34 @@ __global__ void k_h_pass1(const double* __restrict__ gen, long ldgen, int k, int
     unsigned long long b = (unsigned long long)__double_as_longlong(h) & ABS_MASK;
     mb = b > mb ? b : mb;
     s += fabs(h);
+    s2 = fma(h, h, s2);
   }
   __shared__ unsigned long long smax[32];
-  __shared__ double ssum[32];
+  __shared__ double ssum[32], ssq[32];
   for (int o = 16; o > 0; o >>= 1) {
     unsigned long long ob = __shfl_xor_sync(0xffffffffu, mb, o);
     mb = ob > mb ? ob : mb;
     s += __shfl_xor_sync(0xffffffffu, s, o);
+    s2 += __shfl_xor_sync(0xffffffffu, s2, o);
   }
   int wid = threadIdx.x >> 5, ln = threadIdx.x & 31;
-  if (ln == 0) { smax[wid] = mb; ssum[wid] = s; }
+  if (ln == 0) { smax[wid] = mb; ssum[wid] = s; ssq[wid] = s2; }
   __syncthreads();
   if (wid == 0) {
     int nw = blockDim.x >> 5;
     mb = ln < nw ? smax[ln] : 0ull;
     s = ln < nw ? ssum[ln] : 0.0;
+    s2 = ln < nw ? ssq[ln] : 0.0;
     for (int o = 16; o > 0; o >>= 1) {
       unsigned long long ob = __shfl_xor_sync(0xffffffffu, mb, o);
       mb = ob > mb ? ob : mb;
       s += __shfl_xor_sync(0xffffffffu, s, o);
+      s2 += __shfl_xor_sync(0xffffffffu, s2, o);
     }
     if (ln == 0) {
       hmax_bits[j] = mb;
       hsum[j] = s;
+      hsq[j] = s2;
       if (mb > 0 && mb < INF_BITS && isfinite(s)) {
         double rho = s / __longlong_as_double((long long)mb);
         atomicMax(&prm->rho_bits, (unsigned long long)__double_as_longlong(rho));
@@ -241,12 +253,73 @@ __global__ void k_h_pass1(const double* __restrict__ gen, long ldgen, int k, int
   }
 }
 
-// P from the bound |Z| <= 2^(2P) * (rho + 1) <= M / 16.
-__global__ void k_split_params(SplitDevParams* prm, double log2M) {
-  double rho = __longlong_as_double((long long)prm->rho_bits);
-  if (!(rho >= 1.0)) rho = 1.0;
-  int P = (int)floor((log2M - 4.0 - log2(rho + 1.0)) * 0.5);
-  prm->P = max(8, min(53, P));
+// Bits PA (rows of A) and PH (columns of H).  The integer product must satisfy
+// |Z_ij| <= M/16 for the CRT, with M = prod m_l.  Two rigorous bounds of |Z_ij| =
+// |sum_k A'_ik H'_kj| for |A'| <= 2^PA, |H'| <= 2^PH (rounding adds at most 1/2 per entry):
+//   L1: 2^(PA+PH) * (rho + k 2^-9),      rho = max_j sum_k|H_kj| / max_k|H_kj|
+//   CS: 2^(PA+PH) * (ra + sqrt(k)/512) * (rh + sqrt(k)/512),
+//       ra = max_i ||A_i:||_2 / max_k|A_ik|, rh = max_j ||H_:j||_2 / max_k|H_kj|  (PA, PH >= 8).
+// The budget PA + PH comes from the smaller bound.  It is split to balance the two rounding
+// errors, ~2^-PA * c_A and ~2^-PH * c_H with c_A ~ rms_i(max|A_i:|)/rms(A),
+// c_H ~ rms_j(max|H_:j|)/rms(H) (same constant factor): PH - PA = round(log2(c_H/c_A)).
+__global__ void k_split_params(SplitDevParams* prm, double log2M, int n, int k,
+                               const unsigned long long* __restrict__ amax_bits, const double* __restrict__ asq,
+                               const unsigned long long* __restrict__ hmax_bits, const double* __restrict__ hsq) {
+  double ra = 0.0, amx2 = 0.0, afro = 0.0, rh = 0.0, hmx2 = 0.0, hfro = 0.0;
+  const double rk = sqrt((double)k);
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const unsigned long long b = amax_bits[i];
+    if (b == 0 || b >= INF_BITS) continue;
+    const double m = __longlong_as_double((long long)b), q = asq[i];
+    const bool safe = m > 1e-140 && m < 1e140 && isfinite(q) && q > 0.0;
+    ra = fmax(ra, safe ? sqrt(q) / m : rk);
+    if (safe) { amx2 += m * m; afro += q; }
+  }
+  for (int j = threadIdx.x; j < k; j += blockDim.x) {
+    const unsigned long long b = hmax_bits[j];
+    if (b == 0 || b >= INF_BITS) continue;
+    const double m = __longlong_as_double((long long)b), q = hsq[j];
+    const bool safe = m > 1e-140 && m < 1e140 && isfinite(q) && q > 0.0;
+    rh = fmax(rh, safe ? sqrt(q) / m : rk);
+    if (safe) { hmx2 += m * m; hfro += q; }
+  }
+  double v[6] = {ra, amx2, afro, rh, hmx2, hfro};
+  // block reduction: max for ra/rh, sums otherwise
+  for (int o = 16; o > 0; o >>= 1)
+    for (int t = 0; t < 6; ++t) {
+      double w = __shfl_xor_sync(0xffffffffu, v[t], o);
+      v[t] = (t == 0 || t == 3) ? fmax(v[t], w) : v[t] + w;
+    }
+  __shared__ double sv[6][32];
+  const int wid = threadIdx.x >> 5, ln = threadIdx.x & 31;
+  if (ln == 0)
+    for (int t = 0; t < 6; ++t) sv[t][wid] = v[t];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int nw = blockDim.x >> 5;
+    for (int t = 0; t < 6; ++t) {
+      double acc = sv[t][0];
+      for (int w = 1; w < nw; ++w) acc = (t == 0 || t == 3) ? fmax(acc, sv[t][w]) : acc + sv[t][w];
+      v[t] = acc;
+    }
+    double rho = __longlong_as_double((long long)prm->rho_bits);
+    if (!(rho >= 1.0)) rho = rk * rk;
+    const double l1 = log2(rho * 1.01 + (double)k / 512.0);
+    const double cs = log2((v[0] * 1.01 + rk / 512.0) * (v[3] * 1.01 + rk / 512.0));
+    const double bound = fmin(l1, (v[0] > 0.0 && v[3] > 0.0) ? cs : l1);
+    int budget = (int)floor(log2M - 4.0 - bound);
+    int d = 0;
+    if (v[1] > 0.0 && v[2] > 0.0 && v[4] > 0.0 && v[5] > 0.0) {
+      const double cA = sqrt(v[1] / v[2]), cH = sqrt(v[4] / v[5]);
+      d = (int)lrint(log2(cH / cA));
+      d = max(-12, min(12, d));
+    }
+    int PA = (budget - d) >> 1, PH = budget - PA;
+    if (PH > 53) { PA += PH - 53; PH = 53; }
+    if (PA > 53) { PH += PA - 53; PA = 53; }
+    prm->PA = max(8, min(53, PA));
+    prm->PH = max(8, min(53, PH));
+  }
 }
 
 // Exponent s such that |x * 2^s| < 2^P for all |x| <= amax (amax finite, > 0).
@@ -325,7 +398,7 @@ __global__ void k_residues_A(const double* __restrict__ A, long lda, int n, int 
     tile[kk][tx] = (gi < n && gk < k) ? __ldg(A + gi + (long)gk * lda) : 0.0;
   }
   __syncthreads();
-  const int P = prm->P;
+  const int P = prm->PA;
   const size_t plane = (size_t)n * kp;
   for (int r = ty; r < 32; r += 8) {
     int gi = i0 + r;
@@ -349,7 +422,7 @@ __global__ void k_residues_H(const double* __restrict__ Ht, int k, int kp,
   const int j = blockIdx.y;
   const int kk = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
   if (kk >= kp) return;
-  const int P = prm->P;
+  const int P = prm->PH;
   unsigned long long hb = hmax_bits[j];
   bool ok = hb > 0 && hb < INF_BITS;
   int e = ok ? scale_exp(hb, P) : 0;
@@ -624,14 +697,14 @@ __global__ void __launch_bounds__(256) k_crt_combine(const int8_t* __restrict__ 
   __shared__ double tile[CRT_TJ][CRT_TI + 1];
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int i0 = blockIdx.y * CRT_TI, j0 = blockIdx.x * CRT_TJ;
-  const int P = prm->P;
+  const int PA = prm->PA, PH = prm->PH;
   const int jb = j0 + 4 * tx;
   unsigned long long hb[4];
   int fexp[4];
 #pragma unroll
   for (int c = 0; c < 4; ++c) {
     hb[c] = (jb + c < k) ? hmax_bits[jb + c] : 0ull;
-    fexp[c] = (hb[c] != 0 && hb[c] < INF_BITS) ? scale_exp(hb[c], P) : 0;
+    fexp[c] = (hb[c] != 0 && hb[c] < INF_BITS) ? scale_exp(hb[c], PH) : 0;
   }
   const size_t plane_w = (size_t)n * kr / 4;
   for (int a = 0; a < CRT_TI / 8; ++a) {
@@ -639,7 +712,7 @@ __global__ void __launch_bounds__(256) k_crt_combine(const int8_t* __restrict__ 
     double val[4] = {0.0, 0.0, 0.0, 0.0};
     if (i < n && jb < k) {
       const unsigned long long ab = amax_bits[i];
-      const int sexp = (ab != 0 && ab < INF_BITS) ? scale_exp(ab, P) : 0;
+      const int sexp = (ab != 0 && ab < INF_BITS) ? scale_exp(ab, PA) : 0;
       unsigned long long acc[4][4];
       int qi[4];
 #pragma unroll
@@ -696,13 +769,14 @@ __global__ void __launch_bounds__(256) k_crt_combine(const int8_t* __restrict__ 
   }
   __syncthreads();
   const int i = i0 + tx;
+  const bool scale = alpha != 1.0, accumulate = beta != 0.0;  // uniform: decided once
   for (int b = 0; b < CRT_TJ / 8; ++b) {
     const int jl = ty + 8 * b, jj = j0 + jl;
     if (i < n && jj < k) {
       double* qp = Q + i + (long)jj * ldq;
       double v = tile[jl][tx];
-      if (alpha != 1.0) v *= alpha;
-      if (beta != 0.0) v = fma(beta, *qp, v);
+      if (scale) v *= alpha;
+      if (accumulate) v = fma(beta, *qp, v);
       *qp = v;
     }
   }
@@ -750,6 +824,8 @@ int launch_split(int kind, int n, int k, double alpha, const double* A, long lda
   unsigned long long* amax = (unsigned long long*)(w + L.off_amax);
   unsigned long long* hmax = (unsigned long long*)(w + L.off_hmax);
   double* hsum = (double*)(w + L.off_hsum);
+  double* asq = (double*)(w + L.off_asq);
+  double* hsq = (double*)(w + L.off_hsq);
   double* Ht = (double*)(w + L.off_ht);
   __nv_bfloat16* RA = (__nv_bfloat16*)(w + L.off_ra);
   __nv_bfloat16* RH = (__nv_bfloat16*)(w + L.off_rh);
@@ -766,20 +842,20 @@ int launch_split(int kind, int n, int k, double alpha, const double* A, long lda
   }
 
   prof_begin(stream);
-  if (cudaMemsetAsync(w, 0, L.off_ht, stream) != cudaSuccess) return PSMMA_EDEVICE;
+  if (cudaMemsetAsync(w, 0, L.off_ht, stream) != cudaSuccess) return PSMMA_EDEVICE;  // params, maxima, sums
 
   const int kchunk = 1024;
   dim3 g1((n + 127) / 128, (k + kchunk - 1) / kchunk);
-  k_row_absmax<<<g1, 128, 0, stream>>>(A, lda, n, k, kchunk, amax);
+  k_row_absmax<<<g1, 128, 0, stream>>>(A, lda, n, k, kchunk, amax, asq);
   prof_mark(stream, "row_scale");
   switch (kind) {
-    case KIND_CAUCHY: k_h_pass1<KIND_CAUCHY><<<k, 256, 0, stream>>>(gen, ldgen, k, L.kp, Ht, hmax, hsum, prm); break;
-    case KIND_TOEPLITZ: k_h_pass1<KIND_TOEPLITZ><<<k, 256, 0, stream>>>(gen, ldgen, k, L.kp, Ht, hmax, hsum, prm); break;
-    case KIND_HANKEL: k_h_pass1<KIND_HANKEL><<<k, 256, 0, stream>>>(gen, ldgen, k, L.kp, Ht, hmax, hsum, prm); break;
+    case KIND_CAUCHY: k_h_pass1<KIND_CAUCHY><<<k, 256, 0, stream>>>(gen, ldgen, k, L.kp, Ht, hmax, hsum, hsq, prm); break;
+    case KIND_TOEPLITZ: k_h_pass1<KIND_TOEPLITZ><<<k, 256, 0, stream>>>(gen, ldgen, k, L.kp, Ht, hmax, hsum, hsq, prm); break;
+    case KIND_HANKEL: k_h_pass1<KIND_HANKEL><<<k, 256, 0, stream>>>(gen, ldgen, k, L.kp, Ht, hmax, hsum, hsq, prm); break;
     default: return PSMMA_EUNSUPPORTED;
   }
   prof_mark(stream, "h_generate");
-  k_split_params<<<1, 1, 0, stream>>>(prm, cc.log2M);
+  k_split_params<<<1, 1024, 0, stream>>>(prm, cc.log2M, n, k, amax, asq, hmax, hsq);
   prof_mark(stream, "params");
   k_residues_A<<<dim3(L.kp / 64, (n + 31) / 32), 256, 0, stream>>>(A, lda, n, k, L.kp, amax, prm, cc, RA);
   prof_mark(stream, "residues_A");

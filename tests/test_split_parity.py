@@ -153,3 +153,26 @@ def test_split_is_deterministic_and_matches_fp64_path(cuda):
     assert torch.equal(outs[0], outs[1])
     err = (torch.linalg.norm(outs[0] - outs[2]) / torch.linalg.norm(outs[2])).item()
     assert err < TOL
+
+
+def test_split_no_cancellation_hits_the_range_bound_exactly(cuda):
+    # all-positive operands: |A'H'| reaches the bound the moduli must cover; the exact
+    # answer (k in every entry) must come back bit for bit
+    n, k = 200, 1500
+    A = np.ones((n, k))
+    g = np.ones(2 * k - 1)
+    for kind in ["toeplitz", "hankel"]:
+        got = _split(kind, n, k, 1.0, A, g, 0.0, np.zeros((n, k)), cuda)
+        np.testing.assert_array_equal(got, np.full((n, k), float(k)))
+
+
+def test_split_wide_exponent_range_rows(cuda):
+    # rows scaled by 2^+-400: per-row exponents keep every row at full relative accuracy
+    n = k = 256
+    A = O.cfg_matrix(n, k, seed=14)
+    scale = np.where(np.arange(n) % 2 == 0, 2.0 ** 400, 2.0 ** -400)
+    gen = _gen("toeplitz", k, seed=15)
+    got = _split("toeplitz", n, k, 1.0, A * scale[:, None], gen, 0.0, np.zeros((n, k)), cuda)
+    ref = O.dense_product("toeplitz", 1.0, A, gen, 0.0, None, k) * scale[:, None]
+    for i in [0, 1, 100, 255]:
+        assert np.linalg.norm(got[i] - ref[i]) / np.linalg.norm(ref[i]) < TOL
