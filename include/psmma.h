@@ -60,7 +60,7 @@ extern "C" {
 /* ---- options ------------------------------------------------------------------------ */
 #define PSMMA_PREC_FP64   0   /* plain path: FP64 tensor-core MMA, H tile generated in smem  */
 #define PSMMA_PREC_SPLIT  1   /* split path: exact modular slices on BF16 tensor cores (tcgen05),
-                                 FP64 scaling and recombination (Cauchy, Toeplitz, Hankel)    */
+                                 FP64 scaling and recombination (all four kinds)              */
 
 typedef struct psmma_opts {
   int    precision;   /* PSMMA_PREC_FP64 (default) or PSMMA_PREC_SPLIT                        */
@@ -186,6 +186,13 @@ void psmma_release_workspace(void);
  * phase names (static strings); the return value is the number of phases. */
 void psmma_set_profiling(int on);
 int psmma_profile_read(float* ms, const char** names, int max_phases);
+
+/* No counterpart in the reference.  Self-test of the failure detection: launches a kernel
+ * that waits on a device barrier nothing ever releases, with a limit of limit_ns
+ * nanoseconds (at most 10 s), and returns PSMMA_ETIMEDOUT when the bounded wait gave up as
+ * designed (PSMMA_OK would mean the wait was released, which cannot happen).  The library's
+ * pipelined kernels use the same bounded waits with a 2 s limit. */
+int psmma_selftest_wait_timeout(unsigned long long limit_ns);
 
 /* Text for a status code (static storage). */
 const char* psmma_status_string(int status);

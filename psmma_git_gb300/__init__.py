@@ -139,9 +139,9 @@ def psmma_hankel(n, k, alpha, A, gen, beta, Q, *, precision="fp64", n_moduli=0, 
     return _real(KIND_HANKEL, "psmma_hankel", n, k, alpha, A, gen, beta, Q, precision, n_moduli, stream, work)
 
 
-def _dft(name: str, n, k, alpha, B, beta, Cm, stream, work):
+def _dft(name: str, n, k, alpha, B, beta, Cm, stream, work, precision="fp64", n_moduli=0):
     lib = load()
-    opts = make_opts("fp64", 0, work)
+    opts = make_opts(precision, n_moduli, work)
     if _is_torch(Cm):
         import torch
         pb, ldb = _dev(B, "B", torch.complex128) if B is not None else (0, max(1, n))
@@ -158,14 +158,14 @@ def _dft(name: str, n, k, alpha, B, beta, Cm, stream, work):
     return Cm
 
 
-def pzmdftl(n, k, alpha, B, beta, Cm, *, stream=None, work=None):
+def pzmdftl(n, k, alpha, B, beta, Cm, *, precision="fp64", n_moduli=0, stream=None, work=None):
     """C := alpha*F*B + beta*C, F(j,l) = exp(-2*pi*i*(j-1)*(l-1)/N), F on the left."""
-    return _dft("pzmdftl", n, k, alpha, B, beta, Cm, stream, work)
+    return _dft("pzmdftl", n, k, alpha, B, beta, Cm, stream, work, precision, n_moduli)
 
 
-def pzmdftl1(n, k, alpha, B, beta, Cm, *, stream=None, work=None):
+def pzmdftl1(n, k, alpha, B, beta, Cm, *, precision="fp64", n_moduli=0, stream=None, work=None):
     """PZMDFTL1 (RRQR variant in the reference); the same exact product here."""
-    return _dft("pzmdftl1", n, k, alpha, B, beta, Cm, stream, work)
+    return _dft("pzmdftl1", n, k, alpha, B, beta, Cm, stream, work, precision, n_moduli)
 
 
 def workspace_size(kind: int, n: int, k: int, precision="fp64", n_moduli: int = 0) -> int:

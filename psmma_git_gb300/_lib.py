@@ -73,6 +73,7 @@ SIGNATURES = {
     "psmma_set_profiling": (None, [_i]),
     "psmma_profile_read": (_i, [C.POINTER(C.c_float), C.POINTER(C.c_char_p), _i]),
     "psmma_version": (C.c_char_p, []),
+    "psmma_selftest_wait_timeout": (_i, [C.c_ulonglong]),
 }
 
 

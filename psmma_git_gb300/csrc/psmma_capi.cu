@@ -91,7 +91,6 @@ const psmma_opts kDefaultOpts = {PSMMA_PREC_FP64, 0, nullptr, 0, {0, 0, 0, 0, 0,
 
 int check_opts(const psmma_opts* o, int kind) {
   if (o->precision != PSMMA_PREC_FP64 && o->precision != PSMMA_PREC_SPLIT) return PSMMA_EUNSUPPORTED;
-  if (o->precision == PSMMA_PREC_SPLIT && kind == KIND_DFT) return PSMMA_EUNSUPPORTED;
   if (o->n_moduli != 0 && (o->n_moduli < 8 || o->n_moduli > 16)) return PSMMA_EUNSUPPORTED;
   for (int i = 0; i < 8; i++)
     if (o->reserved[i] != 0) return PSMMA_EUNSUPPORTED;
@@ -163,6 +162,18 @@ int run_dft(int n, int k, double alpha, const psmma_complex* B, int ldb, double 
   if (st == 1) return PSMMA_OK;
   if (st) return st;
   cudaStream_t s = (cudaStream_t)stream;
+  if (o->precision == PSMMA_PREC_SPLIT && alpha != 0.0) {
+    size_t need = split_workspace_bytes(KIND_DFT, n, k, o->n_moduli);
+    void* work = o->work;
+    if (work) {
+      if (o->lwork < need) return PSMMA_EWORKSPACE;
+    } else {
+      work = pool_get(need, s, &st);
+      if (st) return st;
+    }
+    return launch_split_any(KIND_DFT, n, k, alpha, (const double*)B, ldb, nullptr, 0, beta, (double*)C, ldc,
+                            o->n_moduli, work, need, s, nullptr);
+  }
   double2* wtab = nullptr;
   if (alpha != 0.0) {
     size_t need = (size_t)n * sizeof(double2);
@@ -360,9 +371,9 @@ int psmma_last_status(void) { return g_last_status; }
 size_t psmma_workspace_size(int kind, int n, int k, const psmma_opts* opts) {
   const psmma_opts* o = opts ? opts : &kDefaultOpts;
   if (n <= 0 || k <= 0) return 0;
-  if (kind == KIND_DFT) return align256((size_t)n * sizeof(double2));
-  if (kind < KIND_CAUCHY || kind > KIND_HANKEL) return 0;
+  if (kind < KIND_CAUCHY || kind > KIND_DFT) return 0;
   if (o->precision == PSMMA_PREC_SPLIT) return split_workspace_bytes(kind, n, k, o->n_moduli);
+  if (kind == KIND_DFT) return align256((size_t)n * sizeof(double2));
   return 0;
 }
 

@@ -24,6 +24,12 @@ size_t split_workspace_bytes(int kind, int n, int k, int n_moduli);
 int launch_split(int kind, int n, int k, double alpha, const double* A, long lda,
                  const double* gen, long ldgen, double beta, double* Q, long ldq, int n_moduli,
                  void* work, size_t lwork, cudaStream_t stream);
+// As launch_split, also for KIND_DFT (A = B and Q = C as interleaved complex, lda/ldq in
+// complex elements); with status_dev_out it does not synchronise (the device timeout flag
+// is copied there at the end of the stream's work).
+int launch_split_any(int kind, int n, int k, double alpha, const double* A, long lda,
+                     const double* gen, long ldgen, double beta, double* Q, long ldq, int n_moduli,
+                     void* work, size_t lwork, cudaStream_t stream, unsigned* status_dev_out);
 
 // Library-owned device workspace (psmma_capi.cu): grow-only, one pool per (device, stream).
 void* pool_get(size_t bytes, cudaStream_t stream, int* status);

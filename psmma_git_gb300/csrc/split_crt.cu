@@ -131,7 +131,8 @@ static size_t al1k(size_t x) { return (x + 1023) & ~(size_t)1023; }
 
 struct SplitLayout {
   int kp, kr;
-  size_t off_params, off_amax, off_hmax, off_hsum, off_asq, off_hsq, off_ht, off_ra, off_rh, off_r, total;
+  size_t off_params, off_amax, off_hmax, off_hsum, off_asq, off_hsq, off_wtab, off_ht, off_ra, off_rh, off_r,
+      total;
 };
 
 static SplitLayout split_layout(int n, int k, int nmod) {
@@ -145,6 +146,7 @@ static SplitLayout split_layout(int n, int k, int nmod) {
   L.off_hsum = o;   o += al1k((size_t)k * 8);
   L.off_asq = o;    o += al1k((size_t)n * 8);
   L.off_hsq = o;    o += al1k((size_t)k * 8);
+  L.off_wtab = o;   o += al1k((size_t)(k / 2 + 1) * 16);
   L.off_ht = o;     o += al1k((size_t)k * L.kp * 8);
   L.off_ra = o;     o += al1k((size_t)nmod * n * L.kp * 2);
   L.off_rh = o;     o += al1k((size_t)nmod * k * L.kp * 2);
@@ -156,8 +158,9 @@ static SplitLayout split_layout(int n, int k, int nmod) {
 static int resolve_nmod(int n_moduli) { return n_moduli == 0 ? SPL_DEFAULT_MODULI : n_moduli; }
 
 size_t split_workspace_bytes(int kind, int n, int k, int n_moduli) {
-  (void)kind;
   if (n <= 0 || k <= 0) return 0;
+  // DFT: the product runs as (B^T embedded, k x 2n) * (F embedded, 2n x 2n)
+  if (kind == KIND_DFT) return split_layout(k, 2 * n, resolve_nmod(n_moduli)).total;
   return split_layout(n, k, resolve_nmod(n_moduli)).total;
 }
 
@@ -209,8 +212,16 @@ __global__ void k_h_pass1(const double* __restrict__ gen, long ldgen, int k, int
         h = (u * v) / (d - w);        // U(i)*V(j) / (D(i)-F(j))
       } else if (KIND == KIND_TOEPLITZ) {
         h = __ldg(gen + (k - 1) + j - kk);
-      } else {
+      } else if (KIND == KIND_HANKEL) {
         h = __ldg(gen + kk + j);
+      } else {
+        // DFT embedding F' = [[Re F, Im F], [-Im F, Re F]] of order k = 2n; gen is the table
+        // w^t = (cos, -sin)(2 pi t / n), indexed by the exact (r c) mod n.
+        const int nn = k >> 1;
+        const bool rb = kk >= nn, cb = j >= nn;
+        const long rr = rb ? kk - nn : kk, cc2 = cb ? j - nn : j;
+        const double2 wv = __ldg((const double2*)gen + (rr * cc2) % nn);
+        h = (rb == cb) ? wv.x : (rb ? -wv.y : wv.y);
       }
     }
     row[kk] = h;
@@ -433,6 +444,65 @@ __global__ void k_residues_H(const double* __restrict__ Ht, int k, int kp,
   const size_t plane = (size_t)k * kp;
   uint32_t* dst = (uint32_t*)(RH + (size_t)j * kp + kk);
   write_residue_pair(u0, n0, u1, n1, cc, dst, plane / 2);
+}
+
+// DFT A side: row i of the embedded operand X' = [Re B^T | Im B^T] is column i of B, read
+// contiguously (Bre = B as interleaved doubles, ldb2 = 2*ldb).  One block per row.
+__global__ void k_row_absmax_dft(const double* __restrict__ Bre, long ldb2, int nn,
+                                 unsigned long long* __restrict__ amax_bits, double* __restrict__ asq) {
+  const int i = blockIdx.x;
+  const double* col = Bre + (long)i * ldb2;
+  unsigned long long mb = 0;
+  double sq = 0.0;
+  for (int t = threadIdx.x; t < 2 * nn; t += blockDim.x) {
+    const double a = __ldg(col + t);
+    unsigned long long b = (unsigned long long)__double_as_longlong(a) & ABS_MASK;
+    mb = b > mb ? b : mb;
+    sq = fma(a, a, sq);
+  }
+  __shared__ unsigned long long smax[32];
+  __shared__ double ssq[32];
+  for (int o = 16; o > 0; o >>= 1) {
+    unsigned long long ob = __shfl_xor_sync(0xffffffffu, mb, o);
+    mb = ob > mb ? ob : mb;
+    sq += __shfl_xor_sync(0xffffffffu, sq, o);
+  }
+  const int wid = threadIdx.x >> 5, ln = threadIdx.x & 31;
+  if (ln == 0) { smax[wid] = mb; ssq[wid] = sq; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
+      mb = smax[w] > mb ? smax[w] : mb;
+      sq += ssq[w];
+    }
+    amax_bits[i] = mb;
+    asq[i] = sq;
+  }
+}
+
+// X'(i, e) = Re B(e, i) for e < n, Im B(e - n, i) for n <= e < 2n, 0 beyond.
+__device__ __forceinline__ double dft_x(const double* col, int nn, int e) {
+  if (e < nn) return __ldg(col + 2 * e);
+  if (e < 2 * nn) return __ldg(col + 2 * (e - nn) + 1);
+  return 0.0;
+}
+
+__global__ void k_residues_A_dft(const double* __restrict__ Bre, long ldb2, int nn, int kp,
+                                 const unsigned long long* __restrict__ amax_bits, const SplitDevParams* prm,
+                                 CrtConsts cc, __nv_bfloat16* __restrict__ RA, int M) {
+  const int i = blockIdx.y;
+  const int kk = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+  if (kk >= kp) return;
+  const int P = prm->PA;
+  const unsigned long long ab = amax_bits[i];
+  const bool ok = ab > 0 && ab < INF_BITS;
+  const int e = ok ? scale_exp(ab, P) : 0;
+  const double* col = Bre + (long)i * ldb2;
+  bool n0 = false, n1 = false;
+  const unsigned long long u0 = ok ? scaled_int(dft_x(col, nn, kk), e, &n0) : 0ull;
+  const unsigned long long u1 = ok ? scaled_int(dft_x(col, nn, kk + 1), e, &n1) : 0ull;
+  uint32_t* dst = (uint32_t*)(RA + (size_t)i * kp + kk);
+  write_residue_pair(u0, n0, u1, n1, cc, dst, (size_t)M * kp / 2);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -689,6 +759,9 @@ __device__ __forceinline__ double u128w_scaled(unsigned long long hi, unsigned l
 // the limbs of sum_l (r_l + 128) C_l and one for the fixed-point quotient estimate.
 constexpr int CRT_TI = 32, CRT_TJ = 128;
 
+// DFT_OUT: the product is [Re C^T | Im C^T] (rows = columns of C); element (i, j) goes to the
+// interleaved complex C at 2*(j mod nn) + (j >= nn) + i*ldq (ldq in doubles).
+template <bool DFT_OUT>
 __global__ void __launch_bounds__(256) k_crt_combine(const int8_t* __restrict__ R, int n, int k, int kr,
                                                      CrtConsts cc, const unsigned long long* __restrict__ amax_bits,
                                                      const unsigned long long* __restrict__ hmax_bits,
@@ -768,16 +841,34 @@ __global__ void __launch_bounds__(256) k_crt_combine(const int8_t* __restrict__ 
     for (int c = 0; c < 4; ++c) tile[4 * tx + c][il] = val[c];
   }
   __syncthreads();
-  const int i = i0 + tx;
   const bool scale = alpha != 1.0, accumulate = beta != 0.0;  // uniform: decided once
-  for (int b = 0; b < CRT_TJ / 8; ++b) {
-    const int jl = ty + 8 * b, jj = j0 + jl;
-    if (i < n && jj < k) {
-      double* qp = Q + i + (long)jj * ldq;
-      double v = tile[jl][tx];
-      if (scale) v *= alpha;
-      if (accumulate) v = fma(beta, *qp, v);
-      *qp = v;
+  if (!DFT_OUT) {
+    const int i = i0 + tx;
+    for (int b = 0; b < CRT_TJ / 8; ++b) {
+      const int jl = ty + 8 * b, jj = j0 + jl;
+      if (i < n && jj < k) {
+        double* qp = Q + i + (long)jj * ldq;
+        double v = tile[jl][tx];
+        if (scale) v *= alpha;
+        if (accumulate) v = fma(beta, *qp, v);
+        *qp = v;
+      }
+    }
+  } else {
+    const int nn = k >> 1;
+    for (int a = 0; a < CRT_TI / 8; ++a) {
+      const int il = ty + 8 * a, i = i0 + il;
+      if (i >= n) continue;
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const int jj = jb + c;
+        if (jj >= k) continue;
+        double* qp = Q + (long)i * ldq + 2 * (jj < nn ? jj : jj - nn) + (jj >= nn ? 1 : 0);
+        double v = tile[4 * tx + c][il];
+        if (scale) v *= alpha;
+        if (accumulate) v = fma(beta, *qp, v);
+        *qp = v;
+      }
     }
   }
 }
@@ -812,69 +903,123 @@ static bool make_tmap(CUtensorMap* map, void* ptr, int kp, int rows, int nmod, i
   return r == CUDA_SUCCESS;
 }
 
-int launch_split(int kind, int n, int k, double alpha, const double* A, long lda, const double* gen, long ldgen,
-                 double beta, double* Q, long ldq, int n_moduli, void* work, size_t lwork, cudaStream_t stream) {
-  const int nmod = resolve_nmod(n_moduli);
-  if (nmod < 8 || nmod > SPL_MAX_MODULI) return PSMMA_EUNSUPPORTED;
-  if (k >= (1 << 24)) return PSMMA_EUNSUPPORTED;
-  SplitLayout L = split_layout(n, k, nmod);
-  if (lwork < L.total || !work) return PSMMA_EWORKSPACE;
-  char* w = (char*)work;
-  SplitDevParams* prm = (SplitDevParams*)(w + L.off_params);
-  unsigned long long* amax = (unsigned long long*)(w + L.off_amax);
-  unsigned long long* hmax = (unsigned long long*)(w + L.off_hmax);
-  double* hsum = (double*)(w + L.off_hsum);
-  double* asq = (double*)(w + L.off_asq);
-  double* hsq = (double*)(w + L.off_hsq);
-  double* Ht = (double*)(w + L.off_ht);
-  __nv_bfloat16* RA = (__nv_bfloat16*)(w + L.off_ra);
-  __nv_bfloat16* RH = (__nv_bfloat16*)(w + L.off_rh);
-  int8_t* R = (int8_t*)(w + L.off_r);
-
+static CrtConsts get_consts(int nmod) {
   static std::mutex cmu;
   static CrtConsts consts[SPL_MAX_MODULI + 1];
   static bool have[SPL_MAX_MODULI + 1] = {false};
-  CrtConsts cc;
-  {
-    std::lock_guard<std::mutex> lk(cmu);
-    if (!have[nmod]) { consts[nmod] = make_consts(nmod); have[nmod] = true; }
-    cc = consts[nmod];
+  std::lock_guard<std::mutex> lk(cmu);
+  if (!have[nmod]) {
+    consts[nmod] = make_consts(nmod);
+    have[nmod] = true;
   }
+  return consts[nmod];
+}
+
+struct SplitBuffers {
+  SplitDevParams* prm;
+  unsigned long long *amax, *hmax;
+  double *hsum, *asq, *hsq, *Ht;
+  double2* wtab;
+  __nv_bfloat16 *RA, *RH;
+  int8_t* R;
+};
+
+static SplitBuffers split_buffers(char* w, const SplitLayout& L) {
+  SplitBuffers b;
+  b.prm = (SplitDevParams*)(w + L.off_params);
+  b.amax = (unsigned long long*)(w + L.off_amax);
+  b.hmax = (unsigned long long*)(w + L.off_hmax);
+  b.hsum = (double*)(w + L.off_hsum);
+  b.asq = (double*)(w + L.off_asq);
+  b.hsq = (double*)(w + L.off_hsq);
+  b.wtab = (double2*)(w + L.off_wtab);
+  b.Ht = (double*)(w + L.off_ht);
+  b.RA = (__nv_bfloat16*)(w + L.off_ra);
+  b.RH = (__nv_bfloat16*)(w + L.off_rh);
+  b.R = (int8_t*)(w + L.off_r);
+  return b;
+}
+
+int launch_split_any(int kind, int n, int k, double alpha, const double* A, long lda, const double* gen,
+                     long ldgen, double beta, double* Q, long ldq, int n_moduli, void* work, size_t lwork,
+                     cudaStream_t stream, unsigned* status_dev_out);
+
+int launch_split(int kind, int n, int k, double alpha, const double* A, long lda, const double* gen, long ldgen,
+                 double beta, double* Q, long ldq, int n_moduli, void* work, size_t lwork, cudaStream_t stream) {
+  return launch_split_any(kind, n, k, alpha, A, lda, gen, ldgen, beta, Q, ldq, n_moduli, work, lwork, stream,
+                          nullptr);
+}
+
+// kind != DFT: Q (n x k) = alpha * A (n x k) * H (k x k) + beta * Q.
+// kind == DFT: C (n x k complex, ldq) = alpha * F (n x n) * B (n x k complex, lda) + beta * C,
+//   computed as [Re C^T | Im C^T] = [Re B^T | Im B^T] * [[Re F, Im F], [-Im F, Re F]].
+// With status_dev_out the call does not synchronise: the timeout flag is copied to that
+// device word at the end of the stream's work; otherwise it synchronises and returns it.
+int launch_split_any(int kind, int n, int k, double alpha, const double* A, long lda, const double* gen,
+                     long ldgen, double beta, double* Q, long ldq, int n_moduli, void* work, size_t lwork,
+                     cudaStream_t stream, unsigned* status_dev_out) {
+  const int nmod = resolve_nmod(n_moduli);
+  if (nmod < 8 || nmod > SPL_MAX_MODULI) return PSMMA_EUNSUPPORTED;
+  const bool dft = kind == KIND_DFT;
+  const int M = dft ? k : n;      // rows of the product
+  const int K = dft ? 2 * n : k;  // order of the structured operand
+  if (K >= (1 << 24) || M >= (1 << 30)) return PSMMA_EUNSUPPORTED;
+  SplitLayout L = split_layout(M, K, nmod);
+  if (lwork < L.total || !work) return PSMMA_EWORKSPACE;
+  char* w = (char*)work;
+  const SplitBuffers b = split_buffers(w, L);
+  const CrtConsts cc = get_consts(nmod);
 
   prof_begin(stream);
-  if (cudaMemsetAsync(w, 0, L.off_ht, stream) != cudaSuccess) return PSMMA_EDEVICE;  // params, maxima, sums
+  if (cudaMemsetAsync(w, 0, L.off_wtab, stream) != cudaSuccess) return PSMMA_EDEVICE;  // params, maxima, sums
 
-  const int kchunk = 1024;
-  dim3 g1((n + 127) / 128, (k + kchunk - 1) / kchunk);
-  k_row_absmax<<<g1, 128, 0, stream>>>(A, lda, n, k, kchunk, amax, asq);
+  // ---- A side: row maxima and norms
+  if (!dft) {
+    const int kchunk = 1024;
+    dim3 g1((M + 127) / 128, (K + kchunk - 1) / kchunk);
+    k_row_absmax<<<g1, 128, 0, stream>>>(A, lda, M, K, kchunk, b.amax, b.asq);
+  } else {
+    k_row_absmax_dft<<<M, 256, 0, stream>>>(A, 2 * lda, n, b.amax, b.asq);
+  }
   prof_mark(stream, "row_scale");
+  // ---- H side: generate, column maxima / sums / norms
   switch (kind) {
-    case KIND_CAUCHY: k_h_pass1<KIND_CAUCHY><<<k, 256, 0, stream>>>(gen, ldgen, k, L.kp, Ht, hmax, hsum, hsq, prm); break;
-    case KIND_TOEPLITZ: k_h_pass1<KIND_TOEPLITZ><<<k, 256, 0, stream>>>(gen, ldgen, k, L.kp, Ht, hmax, hsum, hsq, prm); break;
-    case KIND_HANKEL: k_h_pass1<KIND_HANKEL><<<k, 256, 0, stream>>>(gen, ldgen, k, L.kp, Ht, hmax, hsum, hsq, prm); break;
+    case KIND_CAUCHY: k_h_pass1<KIND_CAUCHY><<<K, 256, 0, stream>>>(gen, ldgen, K, L.kp, b.Ht, b.hmax, b.hsum, b.hsq, b.prm); break;
+    case KIND_TOEPLITZ: k_h_pass1<KIND_TOEPLITZ><<<K, 256, 0, stream>>>(gen, ldgen, K, L.kp, b.Ht, b.hmax, b.hsum, b.hsq, b.prm); break;
+    case KIND_HANKEL: k_h_pass1<KIND_HANKEL><<<K, 256, 0, stream>>>(gen, ldgen, K, L.kp, b.Ht, b.hmax, b.hsum, b.hsq, b.prm); break;
+    case KIND_DFT: {
+      int st = launch_dft_table(b.wtab, n, stream);
+      if (st) return st;
+      k_h_pass1<KIND_DFT><<<K, 256, 0, stream>>>((const double*)b.wtab, 0, K, L.kp, b.Ht, b.hmax, b.hsum, b.hsq, b.prm);
+      break;
+    }
     default: return PSMMA_EUNSUPPORTED;
   }
   prof_mark(stream, "h_generate");
-  k_split_params<<<1, 1024, 0, stream>>>(prm, cc.log2M, n, k, amax, asq, hmax, hsq);
+  k_split_params<<<1, 1024, 0, stream>>>(b.prm, cc.log2M, M, K, b.amax, b.asq, b.hmax, b.hsq);
   prof_mark(stream, "params");
-  k_residues_A<<<dim3(L.kp / 64, (n + 31) / 32), 256, 0, stream>>>(A, lda, n, k, L.kp, amax, prm, cc, RA);
+  if (!dft)
+    k_residues_A<<<dim3(L.kp / 64, (M + 31) / 32), 256, 0, stream>>>(A, lda, M, K, L.kp, b.amax, b.prm, cc, b.RA);
+  else
+    k_residues_A_dft<<<dim3((L.kp / 2 + 127) / 128, M), 128, 0, stream>>>(A, 2 * lda, n, L.kp, b.amax, b.prm, cc,
+                                                                           b.RA, M);
   prof_mark(stream, "residues_A");
-  k_residues_H<<<dim3((L.kp / 2 + 127) / 128, k), 128, 0, stream>>>(Ht, k, L.kp, hmax, prm, cc, RH);
+  k_residues_H<<<dim3((L.kp / 2 + 127) / 128, K), 128, 0, stream>>>(b.Ht, K, L.kp, b.hmax, b.prm, cc, b.RH);
   prof_mark(stream, "residues_H");
 
   CUtensorMap tmA, tmB;
-  if (!make_tmap(&tmA, RA, L.kp, n, nmod, G_BM) || !make_tmap(&tmB, RH, L.kp, k, nmod, G_BN))
+  if (!make_tmap(&tmA, b.RA, L.kp, M, nmod, G_BM) || !make_tmap(&tmB, b.RH, L.kp, K, nmod, G_BN))
     return PSMMA_EDEVICE;
   GemmArgs ga;
   memset(&ga, 0, sizeof(ga));
-  ga.n = n;
+  ga.n = M;
   ga.kr = L.kr;
   ga.nkb = L.kp / G_BK;
-  ga.tiles_m = (n + G_BM - 1) / G_BM;
-  ga.tiles_n = (k + G_BN - 1) / G_BN;
+  ga.tiles_m = (M + G_BM - 1) / G_BM;
+  ga.tiles_n = (K + G_BN - 1) / G_BN;
   ga.group_m = 12;
-  ga.R = R;
-  ga.status = &prm->status;
+  ga.R = b.R;
+  ga.status = &b.prm->status;
   for (int l = 0; l < nmod; ++l) { ga.m[l] = cc.m[l]; ga.inv_m[l] = cc.inv_m[l]; }
   if (cudaFuncSetAttribute(k_crt_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G_SMEM) != cudaSuccess)
     return PSMMA_EDEVICE;
@@ -886,13 +1031,23 @@ int launch_split(int kind, int n, int k, double alpha, const double* A, long lda
   k_crt_gemm<<<std::min(sms, total_tiles), G_THREADS, G_SMEM, stream>>>(tmA, tmB, ga);
   prof_mark(stream, "modular_gemm");
 
-  dim3 gc((k + CRT_TJ - 1) / CRT_TJ, (n + CRT_TI - 1) / CRT_TI);
-  k_crt_combine<<<gc, dim3(32, 8), 0, stream>>>(R, n, k, L.kr, cc, amax, hmax, prm, alpha, beta, Q, ldq);
+  dim3 gc((K + CRT_TJ - 1) / CRT_TJ, (M + CRT_TI - 1) / CRT_TI);
+  if (!dft)
+    k_crt_combine<false><<<gc, dim3(32, 8), 0, stream>>>(b.R, M, K, L.kr, cc, b.amax, b.hmax, b.prm, alpha, beta, Q, ldq);
+  else
+    k_crt_combine<true><<<gc, dim3(32, 8), 0, stream>>>(b.R, M, K, L.kr, cc, b.amax, b.hmax, b.prm, alpha, beta, Q,
+                                                        2 * ldq);
   prof_mark(stream, "crt_combine");
   if (cudaGetLastError() != cudaSuccess) return PSMMA_EDEVICE;
 
+  if (status_dev_out) {
+    if (cudaMemcpyAsync(status_dev_out, &b.prm->status, sizeof(unsigned), cudaMemcpyDeviceToDevice, stream) !=
+        cudaSuccess)
+      return PSMMA_EDEVICE;
+    return PSMMA_OK;
+  }
   unsigned st = 0;
-  if (cudaMemcpyAsync(&st, &prm->status, sizeof(st), cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
+  if (cudaMemcpyAsync(&st, &b.prm->status, sizeof(st), cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
       cudaStreamSynchronize(stream) != cudaSuccess)
     return PSMMA_EDEVICE;
   if (st & DEV_ERR_TIMEOUT) return PSMMA_ETIMEDOUT;

@@ -64,8 +64,8 @@ __device__ __forceinline__ bool status_aborted(const unsigned* status) {
 
 // Bounded wait for the phase with the given parity.  Returns false when the time limit
 // expires (recording DEV_ERR_TIMEOUT) or when this CTA or the launch has already aborted.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, unsigned* status,
-                                          volatile int* abort_flag) {
+__device__ __forceinline__ bool mbar_wait_for(uint64_t* bar, uint32_t parity, unsigned* status,
+                                              volatile int* abort_flag, unsigned long long limit_ns) {
   unsigned long long t0 = 0;
   for (uint32_t it = 0;; ++it) {
     if (mbar_try_wait(bar, parity)) return true;
@@ -77,13 +77,18 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, unsign
       unsigned long long now = globaltimer_ns();
       if (t0 == 0) {
         t0 = now;
-      } else if (now - t0 > WAIT_NS) {
+      } else if (now - t0 > limit_ns) {
         atomicOr(status, DEV_ERR_TIMEOUT);
         *abort_flag = 1;
         return false;
       }
     }
   }
+}
+
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, unsigned* status,
+                                          volatile int* abort_flag) {
+  return mbar_wait_for(bar, parity, status, abort_flag, WAIT_NS);
 }
 
 // Bounded wait that ignores the abort flags: used at exit to make sure this thread's own

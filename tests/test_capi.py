@@ -52,7 +52,9 @@ def test_options_are_validated(lib):
     o.precision = 7
     assert lib.psmma_cauchy(2, 2, 1.0, p, 2, p, 2, 0.0, p, 2, C.byref(o), None) == _lib.PSMMA_EUNSUPPORTED
     o.precision = _lib.PREC_SPLIT
+    o.n_moduli = 30
     assert lib.pzmdftl(2, 2, 1.0, p, 2, 0.0, p, 2, C.byref(o), None) == _lib.PSMMA_EUNSUPPORTED
+    o.n_moduli = 0
     o.precision = 0
     o.reserved[3] = 1
     assert lib.psmma_hankel(2, 2, 1.0, p, 2, p, 3, 0.0, p, 2, C.byref(o), None) == _lib.PSMMA_EUNSUPPORTED

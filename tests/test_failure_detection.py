@@ -1,0 +1,32 @@
+"""Failure detection without a GPU fault: a device-side wait that nothing releases must
+expire after its limit and come back as PSMMA_ETIMEDOUT, leaving the context usable."""
+import time
+
+import numpy as np
+import pytest
+
+from oracle import psmma_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def test_bounded_wait_expires_and_context_survives(lib, cuda):
+    import torch
+    from psmma_git_gb300 import _lib
+    import psmma_git_gb300 as P
+    t0 = time.perf_counter()
+    st = lib.psmma_selftest_wait_timeout(50_000_000)  # 50 ms
+    dt = time.perf_counter() - t0
+    assert st == _lib.PSMMA_ETIMEDOUT
+    assert 0.04 < dt < 5.0
+    # the context still works: a split multiply afterwards is correct
+    n = k = 128
+    A = O.cfg_matrix(n, k, seed=1)
+    gen = O.cfg_cauchy_generators(k, seed=2)
+    dA = torch.from_numpy(np.ascontiguousarray(A.T)).to(cuda).t()
+    dg = torch.from_numpy(np.ascontiguousarray(gen.T)).to(cuda).t()
+    dQ = P.fortran_empty(n, k, torch.float64, cuda)
+    P.psmma_cauchy(n, k, 1.0, dA, dg, 0.0, dQ, precision="split")
+    torch.cuda.synchronize()
+    got = dQ.t().contiguous().cpu().numpy().T
+    assert O.rel_fro(got, O.dense_product("cauchy", 1.0, A, gen, 0.0, None, k)) < 1e-12

@@ -176,3 +176,30 @@ def test_split_wide_exponent_range_rows(cuda):
     ref = O.dense_product("toeplitz", 1.0, A, gen, 0.0, None, k) * scale[:, None]
     for i in [0, 1, 100, 255]:
         assert np.linalg.norm(got[i] - ref[i]) / np.linalg.norm(ref[i]) < TOL
+
+
+def _split_dft(n, k, alpha, B, beta, C0, cuda, n_moduli=0, variant="pzmdftl"):
+    import psmma_git_gb300 as P
+    import torch
+    dB = _t(B.astype(np.complex128), cuda)
+    dC = _t(C0.astype(np.complex128), cuda)
+    getattr(P, variant)(n, k, alpha, dB, beta, dC, precision="split", n_moduli=n_moduli)
+    torch.cuda.synchronize()
+    return _np(dC)
+
+
+@pytest.mark.parametrize("n,k", [(1, 1), (3, 5), (96, 40), (250, 300), (1024, 512), (2048, 2048)])
+def test_split_dft_matches_fft(n, k, cuda):
+    B = O.cfg_matrix(n, k, seed=n + 3, complex_=True)
+    C0 = O.cfg_matrix(n, k, seed=k + 4, complex_=True)
+    got = _split_dft(n, k, 0.5, B, -2.0, C0, cuda)
+    ref = O.dft_product(0.5, B, -2.0, C0)
+    assert O.rel_fro(got, ref) < TOL
+
+
+def test_split_dft_ones_fixture(cuda):
+    z = np.load(GOLDEN / "dft_ones_kat.npz")
+    n = int(z["n"])
+    for variant in ["pzmdftl", "pzmdftl1"]:
+        got = _split_dft(n, n, 1.0, z["B"], 0.0, np.zeros((n, n), complex), cuda, variant=variant)
+        assert np.abs(got - z["X"]).max() < 1e-10
