@@ -350,6 +350,103 @@ def run_gpu(args, ws, rank, local):
     return 0
 
 
+def run_serving(args, ws, rank, local):
+    """Serving loop under a Poisson request stream (one line of JSON per sweep).  Requests:
+    kind uniform over cauchy/toeplitz/hankel/dft, n log-uniform in [512, 16384] (k = n),
+    operands uniform[-1,1] resident on the device (views into pre-generated pools), split
+    precision; the server admits by an HBM budget with at most --inflight requests."""
+    import math
+    import threading
+    import numpy as np
+    import torch
+    import psmma_git_gb300 as P
+    from psmma_git_gb300.server import Server
+    from oracle import psmma_oracle as O
+    if rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    nmax = args.serve_nmax
+    g = torch.Generator(device=dev)
+    g.manual_seed(11)
+    A = P.fortran_empty(nmax, nmax, torch.float64, dev)
+    A.copy_(torch.rand(nmax, nmax, generator=g, device=dev, dtype=torch.float64).mul_(2).sub_(1))
+    B = P.fortran_empty(nmax, nmax, torch.complex128, dev)
+    B.copy_(torch.complex(torch.rand(nmax, nmax, generator=g, device=dev, dtype=torch.float64) * 2 - 1,
+                          torch.rand(nmax, nmax, generator=g, device=dev, dtype=torch.float64) * 2 - 1))
+    gen_c = torch.from_numpy(np.ascontiguousarray(O.cfg_cauchy_generators(nmax, seed=0).T)).to(dev).t()
+    gvec = torch.rand(2 * nmax - 1, generator=g, device=dev, dtype=torch.float64).mul_(2).sub_(1)
+    nbuf = args.inflight * 3
+    # flat pools: viewed per request as a column-major n x n real or complex matrix
+    outs = [torch.empty(2 * nmax * nmax, dtype=torch.float64, device=dev) for _ in range(nbuf)]
+    kinds = ["cauchy", "toeplitz", "hankel", "dft"]
+    budget = args.serve_budget_gib << 30
+    results = []
+    for rate in args.rates:
+        rng = np.random.default_rng(int(rate * 1000) + 1)
+        n_req = max(8, int(rate * args.serve_seconds))
+        plan = []
+        t = 0.0
+        for i in range(n_req):
+            t += rng.exponential(1.0 / rate)
+            n = int(round(math.exp(rng.uniform(math.log(512), math.log(nmax)))))
+            plan.append((t, kinds[int(rng.integers(4))], n))
+        buf_ticket = [None] * nbuf
+        tickets, lat, flops, done = [], [], [], []
+        with Server(budget, max_inflight=args.inflight) as srv:
+            lock = threading.Lock()
+
+            def collect(tk, fl):
+                info = srv.wait(tk)
+                with lock:
+                    done.append((info, fl))
+
+            threads = []
+            t0 = time.perf_counter()
+            for i, (ta, kind, n) in enumerate(plan):
+                b = i % nbuf
+                if buf_ticket[b] is not None:
+                    buf_ticket[b].join()  # its previous request must be complete
+                while time.perf_counter() - t0 < ta:
+                    time.sleep(min(0.001, max(0.0, ta - (time.perf_counter() - t0))))
+                if kind == "dft":
+                    Q = torch.view_as_complex(outs[b][: 2 * n * n].view(n, n, 2)).t()
+                    tk = srv.submit("dft", n, n, 1.0, B[:n, :n], None, 0.0, Q, precision="split",
+                                    n_moduli=args.n_moduli, tag=i)
+                    fl = 8.0 * n ** 3
+                else:
+                    Q = outs[b][: n * n].view(n, n).t()
+                    gen = gen_c[:n] if kind == "cauchy" else gvec[: 2 * n - 1]
+                    tk = srv.submit(kind, n, n, 1.0, A[:n, :n], gen, 0.0, Q, precision="split",
+                                    n_moduli=args.n_moduli, tag=i)
+                    fl = 2.0 * n ** 3
+                th = threading.Thread(target=collect, args=(tk, fl))
+                th.start()
+                buf_ticket[b] = th
+                threads.append(th)
+            for th in threads:
+                th.join()
+            wall = max(i["end_s"] for i, _ in done) - min(i["submit_s"] for i, _ in done)
+        ok = all(i["status"] == 0 for i, _ in done)
+        lats = np.array([i["latency_s"] for i, _ in done]) * 1e3
+        tot_fl = sum(f for _, f in done)
+        results.append({"rate_req_s": rate, "requests": len(done), "all_ok": ok,
+                        "throughput_req_s": len(done) / wall, "throughput_tflops": tot_fl / wall / 1e12,
+                        "p50_ms": float(np.percentile(lats, 50)), "p99_ms": float(np.percentile(lats, 99)),
+                        "max_ms": float(lats.max()),
+                        "mean_gpu_ms": float(np.mean([i["gpu_ms"] for i, _ in done]))})
+        print(json.dumps({"serving_rate": results[-1]}), file=sys.stderr, flush=True)
+    line = {"metric": "serving: p50/p99 latency (ms) and effective TFLOP/s under a Poisson stream",
+            "unit": "ms", "n_gpus": 1, "data": "synthetic",
+            "config": {"workload": "kind uniform over cauchy/toeplitz/hankel/dft, n log-uniform in "
+                                   f"[512, {nmax}], split precision ({args.n_moduli} moduli), device-resident "
+                                   "operands", "hbm_budget_gib": args.serve_budget_gib,
+                       "max_inflight": args.inflight, "seconds_per_rate": args.serve_seconds},
+            "sweep": results}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 import ctypes  # noqa: E402
 
 C_float = ctypes.c_float
@@ -370,6 +467,12 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--serving", action="store_true", help="run the serving-loop sweep instead")
+    ap.add_argument("--rates", type=float, nargs="+", default=[5.0, 10.0, 20.0, 40.0])
+    ap.add_argument("--inflight", type=int, default=4)
+    ap.add_argument("--serve-seconds", type=float, default=6.0)
+    ap.add_argument("--serve-nmax", type=int, default=16384)
+    ap.add_argument("--serve-budget-gib", type=int, default=96)
     args = ap.parse_args()
     ws, rank, local = dist_init(args)
     if args.impl == "reference":
@@ -378,6 +481,8 @@ def main():
     if rank == 0:
         B.build()
     barrier(ws)
+    if args.serving:
+        return run_serving(args, ws, rank, local)
     return run_gpu(args, ws, rank, local)
 
 

@@ -170,6 +170,51 @@ void pzmdftl1_(const int* n, const int* k, const int* nb, const int* kb, const d
                double* rwork);
 int psmma_last_status(void);
 
+/* ---- serving loop (continuous batching) -------------------------------------------- */
+/* No counterpart in the reference, whose callers make one blocking call at a time.  A
+ * server admits queued requests in arrival order as soon as a stream slot is free and the
+ * request's workspace fits in the remaining part of an HBM budget allocated once at
+ * creation; admitted requests run concurrently on their own streams.  Operands stay on the
+ * device: A/B, generators and Q/C are device pointers owned by the caller, who must keep
+ * them alive (and not touch Q/C) until the request completes. */
+typedef struct psmma_request {
+  int kind;            /* PSMMA_KIND_CAUCHY / _TOEPLITZ / _HANKEL / _DFT                         */
+  int precision;       /* PSMMA_PREC_FP64 or PSMMA_PREC_SPLIT                                     */
+  int n_moduli;        /* split path: 0 = default                                                 */
+  int n, k;            /* sizes as in the matching entry point                                    */
+  double alpha, beta;
+  const void* A;       /* A (double) or, for the DFT, B (psmma_complex)                           */
+  int lda;
+  const double* gen;   /* generators (unused for the DFT)                                         */
+  int ldgen;
+  void* Q;             /* Q (double) or, for the DFT, C (psmma_complex)                           */
+  int ldq;
+  unsigned long long user_tag;
+} psmma_request;
+
+typedef struct psmma_completion {
+  unsigned long long ticket, user_tag;
+  int status;                    /* status of the request (0 = ok)                              */
+  double submit_s, start_s, end_s; /* host monotonic clock: submitted, admitted, completed      */
+  float gpu_ms;                  /* CUDA-event time of the request's work on its stream          */
+} psmma_completion;
+
+typedef struct psmma_server psmma_server;
+
+/* Creates a server on the current device with an HBM budget (bytes, allocated now) for
+ * request workspaces and at most max_inflight concurrent requests (1..64). */
+int psmma_server_create(size_t hbm_budget_bytes, int max_inflight, psmma_server** out);
+/* Queues a request (argument checks as the direct entry points; PSMMA_ENOMEM if its
+ * workspace exceeds the whole budget).  Returns at once with a ticket. */
+int psmma_server_submit(psmma_server* s, const psmma_request* r, unsigned long long* ticket);
+/* Waits up to timeout_s seconds for a ticket; fills *out and returns the request's status
+ * (PSMMA_ETIMEDOUT if the wait itself timed out; the ticket stays valid then). */
+int psmma_server_wait(psmma_server* s, unsigned long long ticket, double timeout_s, psmma_completion* out);
+/* Number of queued (not yet admitted) and in-flight requests. */
+int psmma_server_pending(psmma_server* s, int* queued, int* inflight);
+/* Completes in-flight requests, drops queued ones, frees the budget and the streams. */
+int psmma_server_destroy(psmma_server* s);
+
 /* ---- workspace and housekeeping ----------------------------------------------------- */
 
 /* Bytes of device workspace a call with these sizes and options needs (0 for the FP64

@@ -42,6 +42,22 @@ class PsmmaOpts(C.Structure):
     ]
 
 
+class PsmmaRequest(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int), ("precision", C.c_int), ("n_moduli", C.c_int), ("n", C.c_int), ("k", C.c_int),
+        ("alpha", C.c_double), ("beta", C.c_double),
+        ("A", C.c_void_p), ("lda", C.c_int), ("gen", C.c_void_p), ("ldgen", C.c_int),
+        ("Q", C.c_void_p), ("ldq", C.c_int), ("user_tag", C.c_ulonglong),
+    ]
+
+
+class PsmmaCompletion(C.Structure):
+    _fields_ = [
+        ("ticket", C.c_ulonglong), ("user_tag", C.c_ulonglong), ("status", C.c_int),
+        ("submit_s", C.c_double), ("start_s", C.c_double), ("end_s", C.c_double), ("gpu_ms", C.c_float),
+    ]
+
+
 _p = C.c_void_p
 _i = C.c_int
 _d = C.c_double
@@ -74,6 +90,11 @@ SIGNATURES = {
     "psmma_profile_read": (_i, [C.POINTER(C.c_float), C.POINTER(C.c_char_p), _i]),
     "psmma_version": (C.c_char_p, []),
     "psmma_selftest_wait_timeout": (_i, [C.c_ulonglong]),
+    "psmma_server_create": (_i, [C.c_size_t, _i, C.POINTER(C.c_void_p)]),
+    "psmma_server_submit": (_i, [_p, C.POINTER(PsmmaRequest), C.POINTER(C.c_ulonglong)]),
+    "psmma_server_wait": (_i, [_p, C.c_ulonglong, C.c_double, C.POINTER(PsmmaCompletion)]),
+    "psmma_server_pending": (_i, [_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "psmma_server_destroy": (_i, [_p]),
 }
 
 

@@ -19,7 +19,8 @@ CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libpsmma_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["psmma_capi.cu", "fp64_structured.cu", "split_crt.cu", "split_noalloc.cu", "selftest.cu"]
+SOURCES = ["psmma_capi.cu", "fp64_structured.cu", "split_crt.cu", "split_noalloc.cu", "selftest.cu",
+           "serving.cu"]
 HEADERS = ["psmma_internal.h", "tcgen05_util.cuh"]
 
 
