@@ -136,11 +136,8 @@ def barrier(ws):
 def max_over_ranks(x: float, ws: int, device=None) -> float:
     if ws == 1:
         return x
-    import torch
-    import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device=device)
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    return float(t.item())
+    from psmma_git_gb300.shard import max_over_ranks as _max
+    return _max(x)
 
 
 def cpu_inputs(n: int, seed_gen: int = 0, seed_a: int = 1):
