@@ -128,6 +128,55 @@ int psmma_cauchy_split_noalloc(int n, int k, double alpha, const double* A, int 
                                const double* gen, int ldgen, double beta, double* Q, int ldq,
                                int n_moduli, void* stream);
 
+/* ---- batched merge level with low-rank off-diagonal blocks ------------------------ */
+/* Replaces the low-rank branch of PSCAUCHY_COMPUTE (pscauchy_compute.f90:371-391) for a
+ * batch of independent Cauchy multiplies, the products of one level of a divide-and-conquer
+ * tree.  Each item is Q := alpha*A*H + beta*Q with H (n x n) the Cauchy-like matrix of the
+ * item's generators [D|F|U|V] (the psmma_cauchy layout, ldgen >= n).  H is split 2 x 2 at
+ * h = n/2; the diagonal blocks are multiplied as generated tiles, and each off-diagonal
+ * block H(R,C) is compressed to X*Y and multiplied as (A(:,R)*X)*Y:
+ *   PSMMA_COMPRESS_RRQR: the explicit tile is factorised by column-pivoted QR, rank = first
+ *     i with |R_ii| <= tol*|R_11| (Compress_RRQR, Auxil_2p5D.f90:1063-1189), X = Q(:,1:Rk),
+ *     Y = R(1:Rk,:)*P^T;
+ *   PSMMA_COMPRESS_RRLU: the structured rank-revealing LU in generator space (rrluCauchy and
+ *     compress_cauchy, Cauchylowrank.f90:7-134, 387-491), X = P^-1 [I; Z], Y = H(PL(1:Rk),:),
+ *     both Cauchy-like.
+ * A block compressed to full rank is multiplied as a generated tile (the reference reuses a
+ * stale buffer there, Cauchylowrank.f90:455-464).  The product phase runs as one CUDA graph.
+ * ranks_out (optional) receives 2 ranks per item with n >= 2, in item order: H(1:h, h+1:n)
+ * then H(h+1:n, 1:h).  stats (optional) reports the dense-equivalent flops sum(2 n^3), the
+ * flops actually executed, the compression flops and the largest rank.  Synchronises
+ * `stream` once after the compression (the ranks size the products). */
+#define PSMMA_COMPRESS_RRQR 0
+#define PSMMA_COMPRESS_RRLU 1
+
+typedef struct psmma_batch_item {
+  int n;
+  const double* A;    /* n x n, lda */
+  int lda;
+  const double* gen;  /* [D|F|U|V], ldgen >= n */
+  int ldgen;
+  double* Q;          /* n x n, ldq */
+  int ldq;
+} psmma_batch_item;
+
+typedef struct psmma_batch_stats {
+  double effective_flops;  /* sum of 2 n^3 */
+  double executed_flops;   /* tensor-core products actually run */
+  double compress_flops;   /* factorisations (QR: 4 m n r per block; RRLU: O(r (m + n))) */
+  int n_blocks;            /* off-diagonal blocks */
+  int max_rank;
+  int full_rank_blocks;    /* blocks multiplied as generated tiles */
+  int reserved;
+} psmma_batch_stats;
+
+int psmma_cauchy_batch_lowrank(int count, const psmma_batch_item* items, double alpha, double beta,
+                               int compressor, double tol, const psmma_opts* opts, int* ranks_out,
+                               psmma_batch_stats* stats, void* stream);
+/* Bytes of workspace psmma_cauchy_batch_lowrank needs for this batch (for opts->work). */
+size_t psmma_batch_workspace_size(int count, const psmma_batch_item* items, int compressor,
+                                  const psmma_opts* opts);
+
 /* ---- host-pointer entry points (copy in, compute, copy out, synchronise) ------------ */
 int psmma_cauchy_host(int n, int k, double alpha, const double* A, int lda,
                       const double* gen, int ldgen, double beta, double* Q, int ldq,

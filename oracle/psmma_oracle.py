@@ -668,3 +668,52 @@ def cfg_matrix(n: int, k: int, seed: int = 1, dist: str = "uniform", complex_: b
 def cfg_vector(m: int, seed: int = 2) -> np.ndarray:
     rng = np.random.Generator(np.random.PCG64(seed))
     return rng.uniform(-1.0, 1.0, m)
+
+
+# ---------------------------------------------------------------------------------------
+# Batched merge level with compressed off-diagonal blocks
+# ---------------------------------------------------------------------------------------
+def merge_level_product(A, gen, beta_Q, alpha: float, beta: float, compressor: str = "rrqr",
+                        tol: float = 1e-14):
+    """One problem of the batched merge level: Q = alpha*A*H + beta*Q with H the Cauchy-like
+    matrix of gen = [D|F|U|V], split 2 x 2 at h = n // 2.  The diagonal blocks are multiplied
+    as dense tiles (ConstCauchy + DGEMM, pscauchy_compute.f90:395-407); each off-diagonal
+    tile is compressed as the reference's low-rank branch does (pscauchy_compute.f90:371-391):
+    "rrqr" -> Compress_RRQR (X = Q_k, Y = R_k P^T), "rrlu" -> compress_cauchy('R') (X, Y from
+    rrluCauchy), then Q(:,C) += alpha * (A(:,R) X) Y.  A tile that does not compress is
+    multiplied as the dense tile (the mathematical A*H; the reference would reuse a stale
+    buffer there, Cauchylowrank.f90:455-464).  Returns (Q, [rank of H(R1,C2), rank of
+    H(R2,C1)]) -- ranks as the compressor reports them (min(M,N) or M when uncompressed)."""
+    A = np.asarray(A, dtype=np.float64)
+    gen = np.asarray(gen, dtype=np.float64)
+    n = A.shape[0]
+    Q = (beta * np.asarray(beta_Q, dtype=np.float64)) if beta != 0.0 else np.zeros((n, n))
+    if n == 0:
+        return Q, []
+    h = n // 2
+    H = cauchy_like(gen[:n, 0], gen[:n, 1], gen[:n, 2], gen[:n, 3])
+    Q[:, :h] += alpha * (A[:, :h] @ H[:h, :h])
+    Q[:, h:] += alpha * (A[:, h:] @ H[h:, h:])
+    ranks = []
+    if h == 0:
+        return Q, ranks
+    for (r0, r1, c0, c1) in [(0, h, h, n), (h, n, 0, h)]:
+        T = H[r0:r1, c0:c1]
+        M, N = T.shape
+        if compressor == "rrqr":
+            X, Y, rk = compress_rrqr(T, tol)
+        else:
+            X, Y, rk = compress_cauchy_rows(gen[r0:r1, 0].copy(), gen[c0:c1, 1].copy(), gen[r0:r1, 2].copy(),
+                                            gen[c0:c1, 3].copy(), tol, M, N)
+        ranks.append(rk)
+        if X is None or rk >= min(M, N):
+            Q[:, c0:c1] += alpha * (A[:, r0:r1] @ T)
+        elif rk > 0:
+            Q[:, c0:c1] += alpha * ((A[:, r0:r1] @ X) @ Y)
+    return Q, ranks
+
+
+def cfg_batch_sizes(count: int = 64, lo: int = 256, hi: int = 8192, seed: int = 7) -> list[int]:
+    """Seeded sizes of the batched merge level: n log-uniform in [lo, hi]."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    return [int(round(math.exp(x))) for x in rng.uniform(math.log(lo), math.log(hi), count)]

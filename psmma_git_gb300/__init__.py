@@ -9,6 +9,9 @@ Python mirror of the reference's public routines, calling the C ABI of
 * :func:`psmma_hankel`   -- PSMMA_HANKEL   (psmma_hankel.f90:2-3):   H(i,j) = G(i+j-1).
 * :func:`pzmdftl` / :func:`pzmdftl1` -- PZMDFTL / PZMDFTL1 (pzmdftL.f90:1-2):
   C := alpha*F*B + beta*C with F the N-by-N DFT matrix, w = exp(-2*pi*i/N).
+* :func:`cauchy_batch_lowrank` -- the low-rank branch of PSCAUCHY_COMPUTE
+  (pscauchy_compute.f90:371-391) for a batch of Cauchy multiplies: off-diagonal blocks
+  compressed by RRQR (Compress_RRQR) or the structured RRLU (compress_cauchy).
 
 Matrices are column-major.  Device operands are ``torch`` CUDA tensors with unit row
 stride (``t.stride(0) == 1``, leading dimension ``t.stride(1)``), as made by
@@ -22,13 +25,14 @@ import ctypes as C
 
 import numpy as np
 
-from ._lib import (KIND_CAUCHY, KIND_DFT, KIND_HANKEL, KIND_TOEPLITZ, PREC_FP64, PREC_SPLIT,
-                   PsmmaError, PsmmaOpts, load, status_string)
+from ._lib import (COMPRESS_RRLU, COMPRESS_RRQR, KIND_CAUCHY, KIND_DFT, KIND_HANKEL, KIND_TOEPLITZ,
+                   PREC_FP64, PREC_SPLIT, PsmmaBatchItem, PsmmaBatchStats, PsmmaError, PsmmaOpts, load,
+                   status_string)
 
 __all__ = [
     "psmma_cauchy", "psmma_toeplitz", "psmma_hankel", "pzmdftl", "pzmdftl1", "fortran_empty",
     "workspace_size", "PsmmaError", "PREC_FP64", "PREC_SPLIT", "load", "status_string",
-    "make_opts",
+    "make_opts", "cauchy_batch_lowrank", "batch_workspace_size",
 ]
 
 # The split path (exact modular slices on the BF16 tensor cores) is built into the library.
@@ -171,3 +175,51 @@ def pzmdftl1(n, k, alpha, B, beta, Cm, *, precision="fp64", n_moduli=0, stream=N
 def workspace_size(kind: int, n: int, k: int, precision="fp64", n_moduli: int = 0) -> int:
     opts = make_opts(precision, n_moduli)
     return int(load().psmma_workspace_size(kind, n, k, C.byref(opts)))
+
+
+_COMPRESS = {"rrqr": COMPRESS_RRQR, "rrlu": COMPRESS_RRLU, COMPRESS_RRQR: COMPRESS_RRQR,
+             COMPRESS_RRLU: COMPRESS_RRLU}
+
+
+def _batch_items(problems):
+    import torch
+    items = (PsmmaBatchItem * max(1, len(problems)))()
+    for i, (A, gen, Q) in enumerate(problems):
+        n = Q.shape[0]
+        pa, lda = _dev(A, "A", torch.float64)
+        pg, ldg = _dev(gen, "gen", torch.float64)
+        if gen.dim() == 1:
+            ldg = gen.numel() // 4
+        pq, ldq = _dev(Q, "Q", torch.float64)
+        items[i].n, items[i].A, items[i].lda = n, pa, max(lda, 1)
+        items[i].gen, items[i].ldgen = pg, ldg
+        items[i].Q, items[i].ldq = pq, max(ldq, 1)
+    return items
+
+
+def cauchy_batch_lowrank(problems, alpha, beta, *, compressor="rrqr", tol=1e-14, precision="fp64",
+                         n_moduli=0, stream=None, work=None):
+    """Q_i := alpha*A_i*H_i + beta*Q_i for problems = [(A_i, gen_i, Q_i), ...] (n_i x n_i CUDA
+    tensors, gen_i = [D|F|U|V]), H_i split 2 x 2 with its off-diagonal blocks compressed by
+    ``compressor`` ("rrqr" or "rrlu") at ``tol``.  Returns (ranks, stats): two ranks per
+    problem with n >= 2 (blocks H(1:h, h+1:n), H(h+1:n, 1:h)) and a dict of flop counts."""
+    lib = load()
+    items = _batch_items(problems)
+    opts = make_opts(precision, n_moduli, work)
+    nb = sum(2 for (_, _, Q) in problems if Q.shape[0] >= 2)
+    ranks = (C.c_int * max(1, nb))()
+    stats = PsmmaBatchStats()
+    st = lib.psmma_cauchy_batch_lowrank(len(problems), items, float(alpha), float(beta), _COMPRESS[compressor],
+                                        float(tol), C.byref(opts), ranks, C.byref(stats), _stream_ptr(stream))
+    if st != 0:
+        raise PsmmaError(st, "psmma_cauchy_batch_lowrank")
+    info = {"effective_flops": stats.effective_flops, "executed_flops": stats.executed_flops,
+            "compress_flops": stats.compress_flops, "n_blocks": stats.n_blocks, "max_rank": stats.max_rank,
+            "full_rank_blocks": stats.full_rank_blocks}
+    return list(ranks)[:nb], info
+
+
+def batch_workspace_size(problems, *, compressor="rrqr", precision="fp64", n_moduli=0) -> int:
+    opts = make_opts(precision, n_moduli)
+    items = _batch_items(problems)
+    return int(load().psmma_batch_workspace_size(len(problems), items, _COMPRESS[compressor], C.byref(opts)))

@@ -31,6 +31,9 @@ PREC_SPLIT = 1
 
 KIND_CAUCHY, KIND_TOEPLITZ, KIND_HANKEL, KIND_DFT = 0, 1, 2, 3
 
+COMPRESS_RRQR = 0
+COMPRESS_RRLU = 1
+
 
 class PsmmaOpts(C.Structure):
     _fields_ = [
@@ -55,6 +58,20 @@ class PsmmaCompletion(C.Structure):
     _fields_ = [
         ("ticket", C.c_ulonglong), ("user_tag", C.c_ulonglong), ("status", C.c_int),
         ("submit_s", C.c_double), ("start_s", C.c_double), ("end_s", C.c_double), ("gpu_ms", C.c_float),
+    ]
+
+
+class PsmmaBatchItem(C.Structure):
+    _fields_ = [
+        ("n", C.c_int), ("A", C.c_void_p), ("lda", C.c_int), ("gen", C.c_void_p), ("ldgen", C.c_int),
+        ("Q", C.c_void_p), ("ldq", C.c_int),
+    ]
+
+
+class PsmmaBatchStats(C.Structure):
+    _fields_ = [
+        ("effective_flops", C.c_double), ("executed_flops", C.c_double), ("compress_flops", C.c_double),
+        ("n_blocks", C.c_int), ("max_rank", C.c_int), ("full_rank_blocks", C.c_int), ("reserved", C.c_int),
     ]
 
 
@@ -95,6 +112,9 @@ SIGNATURES = {
     "psmma_server_wait": (_i, [_p, C.c_ulonglong, C.c_double, C.POINTER(PsmmaCompletion)]),
     "psmma_server_pending": (_i, [_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "psmma_server_destroy": (_i, [_p]),
+    "psmma_cauchy_batch_lowrank": (_i, [_i, C.POINTER(PsmmaBatchItem), _d, _d, _i, _d, _op, _ip,
+                                        C.POINTER(PsmmaBatchStats), _p]),
+    "psmma_batch_workspace_size": (C.c_size_t, [_i, C.POINTER(PsmmaBatchItem), _i, _op]),
 }
 
 

@@ -18,6 +18,8 @@
 //   w^t, t = 0..n-1, indexed by the exact integer (j*l) mod n.
 #include "psmma_internal.h"
 
+#include <vector>
+
 namespace psmma {
 
 // ------------------------------------------------------------------------------------
@@ -42,10 +44,7 @@ struct F64Args {
   double alpha, beta;
   const double* X; long ldx;  // streamed operand (A for real kinds, B' for DFT)
   double* C; long ldc;        // output (Q or C')
-  // generator data
-  const double* gen; long ldgen;   // Cauchy [D|F|U|V] columns / Toeplitz-Hankel vector
-  int korder;                      // order K of H (real kinds) or n (DFT)
-  const double2* wtab;             // DFT: w^t table, t = 0..n-1
+  GenSpec gs;                       // generators of the structured operand
 };
 
 __device__ __forceinline__ void cp_async8(void* smem, const void* gmem, bool pred) {
@@ -112,8 +111,20 @@ __device__ __forceinline__ void load_B_tile(double* Bs, const F64Args& p, int n0
   }
 }
 
+// B tile (dense H): Bs[kk][jj] = H[(k0+kk) + (n0+jj)*ldb], zero outside K x N.
+__device__ __forceinline__ void load_Hd_tile(double* Bs, const F64Args& p, int n0, int k0, int tid) {
+#pragma unroll
+  for (int e = tid; e < F64_BN * F64_BK; e += F64_THREADS) {
+    int kk = e % F64_BK, jj = e / F64_BK;
+    int gk = k0 + kk, gj = n0 + jj;
+    bool ok = gk < p.K && gj < p.N;
+    const double* src = ok ? p.gs.B + (long)gk + (long)gj * p.gs.ldb : p.gs.B;
+    cp_async8(&Bs[kk * F64_BPAD + jj], src, ok);
+  }
+}
+
 // ---- generated-operand builders -----------------------------------------------------------
-// H tile (real kinds): Bs[kk][jj] = H(k0+kk, n0+jj) (0-based), zero outside K x K.
+// H tile (real kinds): Bs[kk][jj] = H(k0+kk, n0+jj) (0-based), zero outside K x N.
 // Each thread owns one column jj and BK/2 consecutive rows.
 template <int KIND>
 __device__ __forceinline__ void gen_H_tile(double* Bs, const F64Args& p, int n0, int k0, int tid,
@@ -121,21 +132,20 @@ __device__ __forceinline__ void gen_H_tile(double* Bs, const F64Args& p, int n0,
   const int jj = tid % F64_BN;
   const int kh = tid / F64_BN;  // 0 or 1
   const int gj = n0 + jj;
-  const int K = p.korder;
 #pragma unroll
   for (int q = 0; q < F64_BK / 2; q++) {
     int kk = kh * (F64_BK / 2) + q;
     int gk = k0 + kk;
     double h = 0.0;
-    if (gk < K && gj < K) {
+    if (gk < p.K && gj < p.N) {
       if (KIND == KIND_CAUCHY) {
-        double d = __ldg(p.gen + gk);                 // D(i)
-        double u = __ldg(p.gen + 2 * p.ldgen + gk);   // U(i)
+        double d = __ldg(p.gs.Dr + gk);               // D(i)
+        double u = __ldg(p.gs.Ur + gk);               // U(i)
         h = (u * colV) / (d - colF);                  // U(i)*V(j) / (D(i)-F(j))
       } else if (KIND == KIND_TOEPLITZ) {
-        h = __ldg(p.gen + (K - 1) + gj - gk);         // G(K + j - i), 1-based
+        h = __ldg(p.gs.g + (p.gs.order - 1) + gj - gk);  // G(K + j - i), 1-based
       } else {
-        h = __ldg(p.gen + gk + gj);                   // G(i + j - 1), 1-based
+        h = __ldg(p.gs.g + gk + gj);                     // G(i + j - 1), 1-based
       }
     }
     Bs[kk * F64_BPAD + jj] = h;
@@ -149,7 +159,7 @@ __device__ __forceinline__ void gen_F_tile(double* As, const F64Args& p, int m0,
   const int ii = tid % F64_BM;
   const int kh = tid / F64_BM;  // 0 or 1
   const int gi = m0 + ii;
-  const long n = p.korder;
+  const long n = p.gs.n_dft;
   const int r = gi >> 1, a = gi & 1;
 #pragma unroll
   for (int q = 0; q < F64_BK / 4; q++) {
@@ -159,7 +169,7 @@ __device__ __forceinline__ void gen_F_tile(double* As, const F64Args& p, int m0,
     double v0 = 0.0, v1 = 0.0;
     if (gi < p.M && gk < p.K) {
       long t = ((long)r * (long)l) % n;
-      double2 w = __ldg(p.wtab + t);
+      double2 w = __ldg(p.gs.wtab + t);
       // row 2r  : [ Re, -Im ];  row 2r+1: [ Im, Re ]
       v0 = a ? w.y : w.x;
       v1 = a ? w.x : -w.y;
@@ -169,8 +179,9 @@ __device__ __forceinline__ void gen_F_tile(double* As, const F64Args& p, int m0,
   }
 }
 
+// One 128 x 128 output tile (bx, by) of the product described by p.
 template <int KIND>
-__global__ void __launch_bounds__(F64_THREADS, 1) k_struct_f64(F64Args p) {
+__device__ __forceinline__ void struct_f64_tile(const F64Args& p, int bx, int by) {
   extern __shared__ __align__(16) double smem[];
   double* As0 = smem;
   double* Bs0 = smem + F64_SMEM_A;
@@ -178,15 +189,15 @@ __global__ void __launch_bounds__(F64_THREADS, 1) k_struct_f64(F64Args p) {
   double* Bs1 = As1 + F64_SMEM_A;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int m0 = blockIdx.x * F64_BM, n0 = blockIdx.y * F64_BN;
+  const int m0 = bx * F64_BM, n0 = by * F64_BN;
   const int wm0 = (warp & 1) * F64_WM, wn0 = (warp >> 1) * F64_WN;
 
   double colF = 0.0, colV = 0.0;
   if (KIND == KIND_CAUCHY) {
     int gj = n0 + (tid % F64_BN);
-    if (gj < p.korder) {
-      colF = __ldg(p.gen + p.ldgen + gj);       // F(j)
-      colV = __ldg(p.gen + 3 * p.ldgen + gj);   // V(j)
+    if (gj < p.N) {
+      colF = __ldg(p.gs.Fc + gj);   // F(j)
+      colV = __ldg(p.gs.Vc + gj);   // V(j)
     }
   }
 
@@ -205,6 +216,10 @@ __global__ void __launch_bounds__(F64_THREADS, 1) k_struct_f64(F64Args p) {
       load_B_tile(Bs, p, n0, k0, tid);
       cp_async_commit();
       gen_F_tile(As, p, m0, k0, tid);
+    } else if (KIND == KIND_DENSE) {
+      load_A_tile(As, p, m0, k0, tid);
+      load_Hd_tile(Bs, p, n0, k0, tid);
+      cp_async_commit();
     } else {
       load_A_tile(As, p, m0, k0, tid);
       cp_async_commit();
@@ -243,6 +258,26 @@ __global__ void __launch_bounds__(F64_THREADS, 1) k_struct_f64(F64Args p) {
       }
 }
 
+template <int KIND>
+__global__ void __launch_bounds__(F64_THREADS, 1) k_struct_f64(F64Args p) {
+  struct_f64_tile<KIND>(p, blockIdx.x, blockIdx.y);
+}
+
+// Grouped: block b belongs to the product with the largest first block t0 <= b.
+template <int KIND>
+__global__ void __launch_bounds__(F64_THREADS, 1)
+    k_struct_f64_group(const F64Args* __restrict__ ps, const int* __restrict__ t0, int count) {
+  const int b = blockIdx.x;
+  int lo = 0, hi = count - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (t0[mid] <= b) lo = mid; else hi = mid - 1;
+  }
+  const F64Args& p = ps[lo];
+  const int local = b - t0[lo], gx = (p.M + F64_BM - 1) / F64_BM;
+  struct_f64_tile<KIND>(p, local % gx, local / gx);
+}
+
 // C := beta * C for an M x N column-major block (alpha == 0 path).
 __global__ void k_scale(double* C, long ldc, int M, int N, double beta) {
   long total = (long)M * N;
@@ -262,9 +297,9 @@ __global__ void k_dft_table(double2* w, int n) {
   }
 }
 
-int launch_struct_f64(int kind, int M, int N, int K, double alpha, const double* X, long ldx,
-                      const double* gen, long ldgen, int korder, const double2* wtab, double beta,
-                      double* C, long ldc, cudaStream_t stream) {
+int launch_struct_f64(int M, int N, int K, double alpha, const double* X, long ldx, const GenSpec& gs,
+                      double beta, double* C, long ldc, cudaStream_t stream) {
+  const int kind = gs.kind;
   if (M == 0 || N == 0) return PSMMA_OK;
   if (alpha == 0.0 || K == 0) {
     if (beta == 1.0) return PSMMA_OK;
@@ -275,7 +310,7 @@ int launch_struct_f64(int kind, int M, int N, int K, double alpha, const double*
   F64Args p;
   p.M = M; p.N = N; p.K = K; p.alpha = alpha; p.beta = beta;
   p.X = X; p.ldx = ldx; p.C = C; p.ldc = ldc;
-  p.gen = gen; p.ldgen = ldgen; p.korder = korder; p.wtab = wtab;
+  p.gs = gs;
   dim3 grid((M + F64_BM - 1) / F64_BM, (N + F64_BN - 1) / F64_BN);
   if (grid.y > 65535) return PSMMA_EUNSUPPORTED;
   prof_begin(stream);
@@ -296,6 +331,7 @@ int launch_struct_f64(int kind, int M, int N, int K, double alpha, const double*
     PSMMA_LAUNCH_F64(KIND_TOEPLITZ)
     PSMMA_LAUNCH_F64(KIND_HANKEL)
     PSMMA_LAUNCH_F64(KIND_DFT)
+    PSMMA_LAUNCH_F64(KIND_DENSE)
 #undef PSMMA_LAUNCH_F64
     default:
       return PSMMA_EUNSUPPORTED;
@@ -307,6 +343,62 @@ int launch_struct_f64(int kind, int M, int N, int K, double alpha, const double*
 int launch_dft_table(double2* w, int n, cudaStream_t stream) {
   int blocks = std::max(1, std::min((n + 255) / 256, 1024));
   k_dft_table<<<blocks, 256, 0, stream>>>(w, n);
+  return cudaGetLastError() == cudaSuccess ? PSMMA_OK : PSMMA_EDEVICE;
+}
+
+
+size_t f64_group_bytes(int count) {
+  if (count <= 0) return 0;
+  return ((sizeof(F64Args) * count + 255) & ~(size_t)255) + sizeof(int) * count + 512;
+}
+
+int f64_group_prepare(const F64Prob* P, int count, void* dev, cudaStream_t stream, F64Group* g) {
+  *g = F64Group();
+  if (count <= 0) return PSMMA_OK;
+  std::vector<F64Args> args(count);
+  std::vector<int> t0(count);
+  int blocks = 0;
+  for (int i = 0; i < count; ++i) {
+    const F64Prob& q = P[i];
+    if (q.M <= 0 || q.N <= 0 || q.K <= 0 || q.gs.kind != P[0].gs.kind) return PSMMA_EUNSUPPORTED;
+    if (q.gs.kind != KIND_CAUCHY && q.gs.kind != KIND_DENSE) return PSMMA_EUNSUPPORTED;
+    F64Args& a = args[i];
+    a.M = q.M; a.N = q.N; a.K = q.K; a.alpha = q.alpha; a.beta = q.beta;
+    a.X = q.X; a.ldx = q.ldx; a.C = q.C; a.ldc = q.ldc; a.gs = q.gs;
+    t0[i] = blocks;
+    const long nb = (long)((q.M + F64_BM - 1) / F64_BM) * ((q.N + F64_BN - 1) / F64_BN);
+    if (blocks + nb > 0x7fffffffL) return PSMMA_EUNSUPPORTED;
+    blocks += (int)nb;
+  }
+  uintptr_t base = ((uintptr_t)dev + 255) & ~(uintptr_t)255;
+  F64Args* d_args = (F64Args*)base;
+  int* d_t0 = (int*)(base + ((sizeof(F64Args) * count + 255) & ~(size_t)255));
+  if (cudaMemcpyAsync(d_args, args.data(), sizeof(F64Args) * count, cudaMemcpyHostToDevice, stream) != cudaSuccess ||
+      cudaMemcpyAsync(d_t0, t0.data(), sizeof(int) * count, cudaMemcpyHostToDevice, stream) != cudaSuccess)
+    return PSMMA_EDEVICE;
+  g->count = count;
+  g->kind = P[0].gs.kind;
+  g->blocks = blocks;
+  g->d_args = d_args;
+  g->d_t0 = d_t0;
+  return PSMMA_OK;
+}
+
+int f64_group_enqueue(const F64Group& g, cudaStream_t stream) {
+  if (g.count == 0) return PSMMA_OK;
+  const F64Args* a = (const F64Args*)g.d_args;
+  if (g.kind == KIND_CAUCHY) {
+    if (cudaFuncSetAttribute(k_struct_f64_group<KIND_CAUCHY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)F64_SMEM_BYTES) != cudaSuccess)
+      return PSMMA_EDEVICE;
+    k_struct_f64_group<KIND_CAUCHY><<<g.blocks, F64_THREADS, F64_SMEM_BYTES, stream>>>(a, g.d_t0, g.count);
+  } else {
+    if (cudaFuncSetAttribute(k_struct_f64_group<KIND_DENSE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)F64_SMEM_BYTES) != cudaSuccess)
+      return PSMMA_EDEVICE;
+    k_struct_f64_group<KIND_DENSE><<<g.blocks, F64_THREADS, F64_SMEM_BYTES, stream>>>(a, g.d_t0, g.count);
+  }
+  prof_mark(stream, g.kind == KIND_CAUCHY ? "f64_group_cauchy" : "f64_group_dense");
   return cudaGetLastError() == cudaSuccess ? PSMMA_OK : PSMMA_EDEVICE;
 }
 

@@ -1,0 +1,1180 @@
+// Low-rank path of the batched merge level: compression of the off-diagonal blocks of Cauchy
+// matrices and the products that use the factors.
+//
+// RRLU (rrluCauchy, Cauchylowrank.f90:7-134; pivoting helpers :137-296): structured
+// rank-revealing LU in generator space, one thread block per matrix block.  For a block
+// T(i,j) = A(i)V(j)/(D(i)-F(j)) (M x N) it gives
+//   T ~= X * Y,  X = P^-1 [I; Z'],  Z'(t,j) = U(Rk+t) W(j) / (LD(Rk+t) - LD(j)),
+//                Y(j,c) = LU(j) V(c) / (LD(j) - F(c)),  j <= Rk,
+// with LD, LU the pivoted row generators, U the Schur-complement row weights, W the
+// interpolation weights and PL the row permutation (compress_cauchy, :387-491).  Both
+// factors are Cauchy-like, so A*X*Y runs as two structured multiplies.
+//
+// RRQR (Compress_RRQR, Auxil_2p5D.f90:1063-1189, with MDGEQP3): the explicit tile is
+// factorised by Householder QR with column pivoting on the largest partial column norm,
+// truncated at the first |R_kk| <= tol |R_11|.  Left-looking form: with F = T^T V Tau
+// (T the pivoted tile, V the reflectors) the partially reduced tile is T - V F^T, so one
+// step reads the tile once (F(:,k) = tau_k (T^T v_k - F (V^T v_k))) and writes nothing
+// but O(M + N) numbers.  Each tile gets a group of co-resident CTAs (cooperative launch)
+// in proportion to its size; the groups synchronise with bounded barriers.
+#include "psmma_internal.h"
+#include "tcgen05_util.cuh"
+
+#include <cooperative_groups.h>
+
+#include <vector>
+
+namespace psmma {
+
+// ------------------------------------------------------------------------------------------
+// RRLU
+// ------------------------------------------------------------------------------------------
+struct RrluBlock {
+  int M, N;           // block size
+  const double *gD, *gU, *gF, *gV;  // generator slices: rows (D, U), columns (F, V)
+  double *D, *F;      // row / column poles (permuted in place)
+  double *A;          // row weights, permuted with D (becomes LU)
+  double *U, *V;      // Schur-complement weights (U becomes Z)
+  double* W;          // interpolation weights, min(M, N)
+  int *PL, *PU;       // 1-based permutations
+  int* rank;          // output Rk
+};
+
+constexpr int RRLU_THREADS = 512;
+
+// Block-wide argmax of |val| with the smallest index on ties (Fortran MAXLOC).
+struct ArgMax {
+  double v;
+  int i;
+};
+
+__device__ __forceinline__ ArgMax better(ArgMax a, ArgMax b) {
+  if (b.v > a.v || (b.v == a.v && b.i < a.i)) return b;
+  return a;
+}
+
+__device__ ArgMax block_argmax(ArgMax x, ArgMax* sm) {
+  for (int o = 16; o > 0; o >>= 1) {
+    ArgMax y;
+    y.v = __shfl_xor_sync(0xffffffffu, x.v, o);
+    y.i = __shfl_xor_sync(0xffffffffu, x.i, o);
+    x = better(x, y);
+  }
+  const int wid = threadIdx.x >> 5, ln = threadIdx.x & 31;
+  __syncthreads();
+  if (ln == 0) sm[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    x = (ln < (int)(blockDim.x >> 5)) ? sm[ln] : ArgMax{-1.0, 0x7fffffff};
+    for (int o = 16; o > 0; o >>= 1) {
+      ArgMax y;
+      y.v = __shfl_xor_sync(0xffffffffu, x.v, o);
+      y.i = __shfl_xor_sync(0xffffffffu, x.i, o);
+      x = better(x, y);
+    }
+    if (ln == 0) sm[32] = x;
+  }
+  __syncthreads();
+  ArgMax r = sm[32];
+  __syncthreads();
+  return r;
+}
+
+__device__ double block_sum(double x, double* sm) {
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+  const int wid = threadIdx.x >> 5, ln = threadIdx.x & 31;
+  __syncthreads();
+  if (ln == 0) sm[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    x = (ln < (int)(blockDim.x >> 5)) ? sm[ln] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if (ln == 0) sm[32] = x;
+  }
+  __syncthreads();
+  double r = sm[32];
+  __syncthreads();
+  return r;
+}
+
+// CauchyMax (Cauchylowrank.f90:166-188): max_i |u(i) / (D(i) - f)| over i in [0, len) and its
+// 1-based index.
+__device__ ArgMax cauchy_max(const double* D, double f, const double* u, int len, ArgMax* sm) {
+  ArgMax best{-1.0, 0x7fffffff};
+  for (int i = threadIdx.x; i < len; i += blockDim.x) {
+    const double v = fabs(u[i] / (D[i] - f));
+    best = better(best, ArgMax{v, i + 1});
+  }
+  return block_argmax(best, sm);
+}
+
+__device__ __forceinline__ void swapd(double* a, int i, int j) {
+  const double t = a[i];
+  a[i] = a[j];
+  a[j] = t;
+}
+__device__ __forceinline__ void swapi(int* a, int i, int j) {
+  const int t = a[i];
+  a[i] = a[j];
+  a[j] = t;
+}
+
+// CauchyPivtG (:191-243), 0-based k0 = k - 1.
+__device__ void pivt_g(RrluBlock& b, int k0, ArgMax* sm) {
+  const int M = b.M, N = b.N;
+  ArgMax L = cauchy_max(b.D + k0, b.F[k0], b.U + k0, M - k0, sm);
+  ArgMax R = cauchy_max(b.F + k0, b.D[k0], b.V + k0, N - k0, sm);
+  double junkL = L.v * fabs(b.V[k0]);
+  double junkU = R.v * fabs(b.U[k0]);
+  const double piv = fabs(b.U[k0] * b.V[k0] / (b.D[k0] - b.F[k0]));
+  if (junkL <= piv && junkU <= piv) return;
+  int flg = junkL > junkU ? 1 : 0;
+  int jjL = L.i, jjU = R.i;
+  for (int guard = 0; guard < 4 * (M + N); ++guard) {
+    if (flg == 1) {
+      const int jj = jjL;
+      if (threadIdx.x == 0) {
+        swapd(b.D, k0, jj + k0 - 1);
+        swapd(b.U, k0, jj + k0 - 1);
+        swapd(b.A, k0, jj + k0 - 1);
+        swapi(b.PL, k0, jj + k0 - 1);
+      }
+      __syncthreads();
+      R = cauchy_max(b.F + k0, b.D[k0], b.V + k0, N - k0, sm);
+      jjU = R.i;
+      if (jjU == 1) return;
+      flg = 0;
+    }
+    const int jj = jjU;
+    if (threadIdx.x == 0) {
+      swapd(b.F, k0, jj + k0 - 1);
+      swapd(b.V, k0, jj + k0 - 1);
+      swapi(b.PU, k0, jj + k0 - 1);
+    }
+    __syncthreads();
+    L = cauchy_max(b.D + k0, b.F[k0], b.U + k0, M - k0, sm);
+    jjL = L.i;
+    if (jjL == 1) return;
+    flg = 1;
+  }
+}
+
+// Candidate of a multi-column search: value, 1-based column, 1-based row of that column's max.
+struct Cand {
+  double v;
+  int j, i;
+};
+
+__device__ __forceinline__ Cand better_c(Cand a, Cand b) {
+  if (b.v > a.v || (b.v == a.v && b.j < a.j)) return b;  // earlier column wins ties
+  return a;
+}
+
+// max over columns j in [0, nc) of |Wt[j]| * max_i |u[i] / (D[i] - P[j])|, i in [0, len);
+// one warp per column, then one block reduction.  Ties: earlier column, earlier row
+// (the order of the reference's loops with strict '>' and MAXLOC).
+__device__ Cand multi_cauchy_max(const double* D, const double* u, int len, const double* P, const double* Wt,
+                                 int nc, Cand* smc) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  Cand wb{-1.0, 0x7fffffff, 0};
+  for (int j = warp; j < nc; j += nw) {
+    const double pj = P[j];
+    ArgMax a{-1.0, 0x7fffffff};
+    for (int i = lane; i < len; i += 32) a = better(a, ArgMax{fabs(u[i] / (D[i] - pj)), i + 1});
+    for (int o = 16; o > 0; o >>= 1) {
+      ArgMax y;
+      y.v = __shfl_xor_sync(0xffffffffu, a.v, o);
+      y.i = __shfl_xor_sync(0xffffffffu, a.i, o);
+      a = better(a, y);
+    }
+    wb = better_c(wb, Cand{a.v * fabs(Wt[j]), j + 1, a.i});
+  }
+  __syncthreads();
+  if (lane == 0) smc[warp] = wb;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    Cand r = smc[0];
+    for (int w = 1; w < nw; ++w) r = better_c(r, smc[w]);
+    smc[32] = r;
+  }
+  __syncthreads();
+  Cand r = smc[32];
+  __syncthreads();
+  return r;
+}
+
+// CauchyPivtG_CP (:246-296): complete pivoting on the k-th Schur complement.
+__device__ void pivt_g_cp(RrluBlock& b, int k0, Cand* smc) {
+  const int M = b.M, N = b.N;
+  const Cand c = multi_cauchy_max(b.D + k0, b.U + k0, M - k0, b.F + k0, b.V + k0, N - k0, smc);
+  const int ii = c.i, jj = c.j;
+  if (threadIdx.x == 0) {
+    swapd(b.D, k0, ii + k0 - 1);
+    swapd(b.U, k0, ii + k0 - 1);
+    swapd(b.A, k0, ii + k0 - 1);
+    swapi(b.PL, k0, ii + k0 - 1);
+    swapd(b.F, k0, jj + k0 - 1);
+    swapd(b.V, k0, jj + k0 - 1);
+    swapi(b.PU, k0, jj + k0 - 1);
+  }
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(RRLU_THREADS) k_rrlu_cauchy(const RrluBlock* blocks, double tol) {
+  __shared__ ArgMax sm[33];
+  __shared__ Cand smc[33];
+  RrluBlock b = blocks[blockIdx.x];
+  const int M = b.M, N = b.N, mn = min(M, N);
+  const double rho = 1.12;
+  const int prd = 10;
+  // D, A from the row generators, F, V from the column generators; U = A, PL = 1..M,
+  // PU = 1..N, W = 0 (rrluCauchy :64-71; compress_cauchy zeroes W)
+  for (int i = threadIdx.x; i < M; i += blockDim.x) {
+    b.D[i] = b.gD[i];
+    b.A[i] = b.gU[i];
+    b.U[i] = b.gU[i];
+    b.PL[i] = i + 1;
+  }
+  for (int j = threadIdx.x; j < N; j += blockDim.x) {
+    b.F[j] = b.gF[j];
+    b.V[j] = b.gV[j];
+    b.PU[j] = j + 1;
+  }
+  for (int j = threadIdx.x; j < mn; j += blockDim.x) b.W[j] = 0.0;
+  __syncthreads();
+  int Rk = mn;
+  double amax = 0.0;
+  for (int k = 1; k <= mn; ++k) {
+    const int k0 = k - 1;
+    pivt_g(b, k0, sm);
+    double ukk = b.U[k0] * b.V[k0] / (b.D[k0] - b.F[k0]);
+    amax = fmax(amax, fabs(ukk));
+    if (fabs(ukk) < tol * amax) {
+      pivt_g_cp(b, k0, smc);
+      ukk = b.U[k0] * b.V[k0] / (b.D[k0] - b.F[k0]);
+      amax = fmax(amax, fabs(ukk));
+      if (fabs(ukk) < tol * amax) {
+        Rk = k - 1;
+        break;
+      }
+    }
+    const double dk = b.D[k0], fk = b.F[k0];
+    for (int i = k + threadIdx.x; i < M; i += blockDim.x) b.U[i] = b.U[i] * (b.D[i] - dk) / (b.D[i] - fk);
+    for (int j = k + threadIdx.x; j < N; j += blockDim.x) b.V[j] = b.V[j] * (b.F[j] - fk) / (b.F[j] - dk);
+    for (int j = threadIdx.x; j < k - 1; j += blockDim.x) b.W[j] = b.W[j] * ((fk - b.D[j]) / (dk - b.D[j]));
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double wk = (dk - fk) / b.A[k0];
+      for (int j = 0; j < k - 1; ++j) wk = wk * (b.F[j] - dk) / (b.D[j] - dk);
+      b.W[k0] = wk;
+    }
+    __syncthreads();
+    // swap check every prd steps (searchMax2, :137-163, and the update of :103-129); each
+    // swap raises |det| of the leading block by more than rho, so the loop ends -- the guard
+    // only bounds it against rounding
+    int flgl = k % prd;
+    for (int guard = 0; flgl < 1 && guard < 4 * k + 64; ++guard) {
+      flgl = 1;
+      // max over j < k of |W(j)| * max_i |U(i)/(D(i)-D(j))|, i in [k, M)
+      const Cand best = multi_cauchy_max(b.D + k, b.U + k, M - k, b.D, b.W, k, smc);
+      if (M - k > 0 && best.v > rho) {
+        flgl = 0;
+        const int ii = best.j;        // 1-based position among the first k
+        const int jj = best.i + k;    // 1-based row beyond k
+        const int i0 = ii - 1, j0 = jj - 1;
+        const double dii = b.D[i0], djj = b.D[j0];
+        for (int j = k + threadIdx.x; j < N; j += blockDim.x) b.V[j] = b.V[j] * ((b.F[j] - dii) / (b.F[j] - djj));
+        for (int i = k + threadIdx.x; i < M; i += blockDim.x)
+          if (i != j0) b.U[i] = b.U[i] * ((b.D[i] - djj) / (b.D[i] - dii));
+        for (int j = threadIdx.x; j < k; j += blockDim.x)
+          if (j != i0) b.W[j] = b.W[j] * ((b.D[j] - dii) / (b.D[j] - djj));
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          double ujj = b.A[i0] * ((dii - djj) / (dii - b.F[i0]));
+          double wii = (djj - b.F[i0]) / b.A[j0];
+          for (int j = 0; j < k; ++j) {
+            if (j == i0) continue;
+            ujj = ujj * ((dii - b.D[j]) / (dii - b.F[j]));
+            wii = wii * ((b.F[j] - djj) / (b.D[j] - djj));
+          }
+          b.U[j0] = ujj;
+          b.W[i0] = wii;
+          swapi(b.PL, i0, j0);
+          swapd(b.D, i0, j0);
+          swapd(b.A, i0, j0);
+        }
+        __syncthreads();
+      }
+    }
+  }
+  if (threadIdx.x == 0) *b.rank = Rk;
+}
+
+// Columns of A(:, R) (n x M, lda) in RRLU pivot order for every compressed block:
+// T0(:, j) = A(:, PL(j)) for j < Rk, Ar(:, t) = A(:, PL(Rk + t)) for t < M - Rk (PL 1-based).
+// One block per column of the batch (columns numbered from c0 per block).
+struct GatherDesc {
+  const double* A;
+  long lda;
+  int n, M, Rk, c0;
+  const int* PL;
+  double *T0, *Ar;  // leading dimension n
+};
+
+__global__ void __launch_bounds__(256) k_gather_group(const GatherDesc* __restrict__ d, int count) {
+  const int gc = blockIdx.x;
+  int lo = 0, hi = count - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (d[mid].c0 <= gc) lo = mid; else hi = mid - 1;
+  }
+  const GatherDesc& e = d[lo];
+  const int c = gc - e.c0;
+  const double* src = e.A + (long)(e.PL[c] - 1) * e.lda;
+  double* dst = (c < e.Rk) ? e.T0 + (long)c * e.n : e.Ar + (long)(c - e.Rk) * e.n;
+  for (int i = threadIdx.x; i < e.n; i += blockDim.x) dst[i] = src[i];
+}
+
+// ------------------------------------------------------------------------------------------
+// RRQR
+// ------------------------------------------------------------------------------------------
+constexpr int QR_THREADS = 256;
+constexpr int QR_WARPS = QR_THREADS / 32;
+constexpr int QR_CAP = 256;  // largest rank a tile is factorised to; beyond it the tile is used as is
+
+struct QrTile {
+  int M, N, cap;                    // tile size; steps at most cap (<= min(M, N), <= QR_CAP)
+  const double *gD, *gU, *gF, *gV;  // generator slices
+  double* T;     // M x N (ld M), columns pivoted; Q(:, 0:r) on exit
+  double* V;     // M x cap (ld M): reflectors, V(k,k) = 1, rows < k unused
+  double* F;     // F[c*cap + j]; on exit Y = R(0:r,:) P^T (r x N, ld r)
+  double* R;     // R[c*cap + i], i <= c
+  double* tau;   // cap + 1 (tau[cap] = |R_11|)
+  double* s;     // cap: V(k:,0:k)^T v_k
+  double *vn1, *vn2;  // partial column norms
+  int* jpvt;     // original column of each pivoted column
+  int* rank;     // -1 running, -2 verifying; then r (< min(M,N)) or min(M,N) when not compressed
+  unsigned* bar; // group barrier counter
+  int cta0, ncta;
+  long col0;     // first column of this tile in the batch's column numbering
+};
+
+// Explicit tiles T(i,c) = U(i)V(c)/(D(i)-F(c)) (ConstCauchy, Auxil_2p5D.f90:138-144), their
+// column norms and the identity pivot; one block per column of the batch.
+__global__ void __launch_bounds__(QR_THREADS) k_qr_tiles(QrTile* tiles, int ntiles) {
+  __shared__ double sm[33];
+  const long gc = blockIdx.x;
+  int lo = 0, hi = ntiles - 1;
+  while (lo < hi) {  // last tile with col0 <= gc
+    const int mid = (lo + hi + 1) >> 1;
+    if (tiles[mid].col0 <= gc) lo = mid; else hi = mid - 1;
+  }
+  const QrTile& t = tiles[lo];
+  const int c = (int)(gc - t.col0);
+  if (c >= t.N) return;
+  const double f = t.gF[c], v = t.gV[c];
+  double ss = 0.0;
+  for (int i = threadIdx.x; i < t.M; i += blockDim.x) {
+    const double h = (t.gU[i] * v) / (t.gD[i] - f);
+    t.T[i + (long)c * t.M] = h;
+    ss = fma(h, h, ss);
+  }
+  ss = block_sum(ss, sm);
+  if (threadIdx.x == 0) {
+    const double nrm = sqrt(ss);
+    t.vn1[c] = nrm;
+    t.vn2[c] = nrm;
+    t.jpvt[c] = c;
+    if (c == 0) {
+      *t.rank = -1;
+      *t.bar = 0u;
+    }
+  }
+}
+
+// Barrier of the ncta CTAs of one tile (all co-resident: cooperative launch).  The counter
+// only grows; the e-th barrier waits for e * ncta arrivals.  Bounded: after WAIT_NS the
+// status word gets DEV_ERR_TIMEOUT and every waiter of the launch returns false.
+__device__ bool group_sync(unsigned* bar, unsigned target, unsigned* status) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(bar, 1u);
+    const unsigned long long t0 = globaltimer_ns();
+    int good = 1;
+    while (true) {
+      const unsigned v = *(volatile unsigned*)bar;
+      if (v >= target) break;
+      if (*(volatile unsigned*)status != 0u) { good = 0; break; }
+      if (globaltimer_ns() - t0 > WAIT_NS) {
+        atomicOr(status, DEV_ERR_TIMEOUT);
+        good = 0;
+        break;
+      }
+      __nanosleep(100);
+    }
+    __threadfence();
+    ok = good;
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+// Step k of the leader CTA: pivot, swap, the current column a = T(:,k) - V F(k,:)^T, its
+// Householder reflector (beta = -sign(alpha) ||a(k:)||, tau = (beta - alpha)/beta,
+// v = a(k+1:)/(alpha - beta)), the truncation test and s = V(k:,0:k)^T v.
+__device__ void qr_leader_step(const QrTile& t, int k, double tol, bool verified, ArgMax* am, double* red,
+                               double* fk) {
+  const int M = t.M, N = t.N, cap = t.cap;
+  ArgMax best{-1.0, 0x7fffffff};
+  for (int c = k + threadIdx.x; c < N; c += blockDim.x) best = better(best, ArgMax{__ldcg(t.vn1 + c), c});
+  best = block_argmax(best, am);
+  const int p = best.i;
+  if (p != k) {
+    for (int i = threadIdx.x; i < M; i += blockDim.x) {
+      double* a = t.T + i + (long)k * M;
+      double* b = t.T + i + (long)p * M;
+      const double x = __ldcg(a), y = __ldcg(b);
+      *a = y;
+      *b = x;
+    }
+    for (int j = threadIdx.x; j < k; j += blockDim.x) {
+      double x = __ldcg(t.F + (long)k * cap + j), y = __ldcg(t.F + (long)p * cap + j);
+      t.F[(long)k * cap + j] = y;
+      t.F[(long)p * cap + j] = x;
+      x = __ldcg(t.R + (long)k * cap + j);
+      y = __ldcg(t.R + (long)p * cap + j);
+      t.R[(long)k * cap + j] = y;
+      t.R[(long)p * cap + j] = x;
+    }
+    if (threadIdx.x == 0) {
+      double x = __ldcg(t.vn1 + k);
+      t.vn1[k] = __ldcg(t.vn1 + p);
+      t.vn1[p] = x;
+      x = __ldcg(t.vn2 + k);
+      t.vn2[k] = __ldcg(t.vn2 + p);
+      t.vn2[p] = x;
+      const int q = __ldcg(t.jpvt + k);
+      t.jpvt[k] = __ldcg(t.jpvt + p);
+      t.jpvt[p] = q;
+    }
+    __syncthreads();
+  }
+  for (int j = threadIdx.x; j < k; j += blockDim.x) fk[j] = __ldcg(t.F + (long)k * cap + j);
+  __syncthreads();
+  double* vk = t.V + (long)k * M;
+  double xsq = 0.0;
+  for (int i = k + threadIdx.x; i < M; i += blockDim.x) {
+    double a = __ldcg(t.T + i + (long)k * M);
+    for (int j = 0; j < k; ++j) a = fma(-__ldcg(t.V + i + (long)j * M), fk[j], a);
+    vk[i] = a;
+    if (i > k) xsq = fma(a, a, xsq);
+  }
+  xsq = block_sum(xsq, red);  // contains the barrier that publishes vk within the CTA
+  const double alpha = __ldcg(vk + k);
+  const double xnorm = sqrt(xsq);
+  double beta = alpha, tau = 0.0;
+  if (xnorm != 0.0) {
+    beta = -copysign(hypot(alpha, xnorm), alpha);
+    tau = (beta - alpha) / beta;
+    const double scal = 1.0 / (alpha - beta);
+    for (int i = k + 1 + threadIdx.x; i < M; i += blockDim.x) vk[i] = __ldcg(vk + i) * scal;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    vk[k] = 1.0;
+    t.R[(long)k * cap + k] = beta;
+    t.tau[k] = tau;
+    const double r11 = (k == 0) ? fabs(beta) : __ldcg(t.tau + cap);
+    if (k == 0) t.tau[cap] = r11;
+    // Compress_RRQR's scan (:1150-1156).  The pivot came from downdated norms, which drift
+    // at this level; the first time the test passes, the group recomputes every partial
+    // norm exactly (rank = -2) and the step is redone, so truncation means that no column
+    // of the reduced tile is larger than tol |R_11|.
+    if (fabs(beta) <= tol * r11) *t.rank = verified ? k : -2;
+  }
+  __syncthreads();
+  // s(j) = sum_{i >= k} V(i,j) v(i), j < k: one warp per j
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int j = warp; j < k; j += QR_WARPS) {
+    double a = 0.0;
+    for (int i = k + lane; i < M; i += 32) a = fma(__ldcg(t.V + i + (long)j * M), __ldcg(vk + i), a);
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    if (lane == 0) t.s[j] = a;
+  }
+}
+
+__global__ void __launch_bounds__(QR_THREADS) k_rrqr_grouped(QrTile* tiles, const int* __restrict__ cta_tile,
+                                                              double tol, unsigned* status) {
+  __shared__ ArgMax am[33];
+  __shared__ double red[33];
+  __shared__ double fk[QR_CAP + 1];
+  __shared__ double sv[QR_CAP + 1];
+  __shared__ double vrow[QR_CAP + 1];
+  __shared__ double fw[QR_WARPS][QR_CAP];
+  const int ti = cta_tile[blockIdx.x];
+  if (ti < 0) return;
+  const QrTile t = tiles[ti];
+  const int local = blockIdx.x - t.cta0;
+  const int M = t.M, N = t.N, cap = t.cap;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const double tol3z = 1.0536712127723509e-08;  // sqrt(2^-53), LAPACK dgeqp3's recompute threshold
+  unsigned epoch = 0;
+  bool truncated = false;
+  for (int k = 0; k < cap; ++k) {
+    if (local == 0) qr_leader_step(t, k, tol, false, am, red, fk);
+    if (!group_sync(t.bar, (++epoch) * t.ncta, status)) return;
+    int state = __ldcg(t.rank);
+    if (state == -2) {
+      // exact partial norms ||T(k:, c) - V(k:, 0:k) F(c, 0:k)^T||, c >= k, one warp per column
+      for (int c = k + local * QR_WARPS + warp; c < N; c += t.ncta * QR_WARPS) {
+        const double* tc = t.T + (long)c * M;
+        for (int j = lane; j < k; j += 32) fw[warp][j] = __ldcg(t.F + (long)c * cap + j);
+        __syncwarp();
+        double ss = 0.0;
+        for (int i = k + lane; i < M; i += 32) {
+          double a = __ldcg(tc + i);
+          for (int j = 0; j < k; ++j) a = fma(-__ldcg(t.V + i + (long)j * M), fw[warp][j], a);
+          ss = fma(a, a, ss);
+        }
+        for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
+        if (lane == 0) {
+          t.vn1[c] = sqrt(ss);
+          t.vn2[c] = sqrt(ss);
+        }
+        __syncwarp();
+      }
+      if (!group_sync(t.bar, (++epoch) * t.ncta, status)) return;
+      if (local == 0) {
+        if (threadIdx.x == 0) *t.rank = -1;
+        __syncthreads();
+        qr_leader_step(t, k, tol, true, am, red, fk);
+      }
+      if (!group_sync(t.bar, (++epoch) * t.ncta, status)) return;
+      state = __ldcg(t.rank);
+    }
+    if (state >= 0) {
+      truncated = true;
+      break;
+    }
+    // every other column c > k: F(c,k), R(k,c) and the norm downdate (dgeqp3/dlaqp2)
+    const double tk = __ldcg(t.tau + k);
+    for (int j = threadIdx.x; j < k; j += blockDim.x) sv[j] = __ldcg(t.s + j);
+    for (int j = threadIdx.x; j <= k; j += blockDim.x) vrow[j] = __ldcg(t.V + k + (long)j * M);
+    __syncthreads();
+    const double* vk = t.V + (long)k * M;
+    for (int c = k + 1 + local * QR_WARPS + warp; c < N; c += t.ncta * QR_WARPS) {
+      const double* tc = t.T + (long)c * M;
+      const double* fc = t.F + (long)c * cap;
+      double dot = 0.0;
+      for (int i = k + lane; i < M; i += 32) dot = fma(__ldcg(tc + i), __ldcg(vk + i), dot);
+      double fs = 0.0, rs = 0.0;
+      for (int j = lane; j < k; j += 32) {
+        const double fj = __ldcg(fc + j);
+        fs = fma(fj, sv[j], fs);
+        rs = fma(vrow[j], fj, rs);
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        dot += __shfl_xor_sync(0xffffffffu, dot, o);
+        fs += __shfl_xor_sync(0xffffffffu, fs, o);
+        rs += __shfl_xor_sync(0xffffffffu, rs, o);
+      }
+      const double f = tk * (dot - fs);
+      const double rkc = __ldcg(tc + k) - rs - f;  // V(k,k) = 1
+      const double v1 = __ldcg(t.vn1 + c), v2 = __ldcg(t.vn2 + c);
+      bool recompute = false;
+      double nv1 = v1;
+      if (v1 != 0.0) {
+        double temp = fabs(rkc) / v1;
+        temp = fmax(0.0, 1.0 - temp * temp);
+        const double q = v1 / v2;
+        const double temp2 = temp * q * q;
+        if (temp2 <= tol3z) recompute = true;
+        else nv1 = v1 * sqrt(temp);
+      }
+      if (recompute) {
+        // exact norm of the reduced column below row k: T(i,c) - sum_{j<=k} V(i,j) F(c,j)
+        double ss = 0.0;
+        for (int i = k + 1 + lane; i < M; i += 32) {
+          double a = __ldcg(tc + i) - __ldcg(vk + i) * f;
+          for (int j = 0; j < k; ++j) a = fma(-__ldcg(t.V + i + (long)j * M), __ldcg(fc + j), a);
+          ss = fma(a, a, ss);
+        }
+        for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
+        nv1 = sqrt(ss);
+      }
+      if (lane == 0) {
+        t.F[(long)c * cap + k] = f;
+        t.R[(long)c * cap + k] = rkc;
+        t.vn1[c] = nv1;
+        if (recompute) t.vn2[c] = nv1;
+      }
+    }
+    if (!group_sync(t.bar, (++epoch) * t.ncta, status)) return;
+  }
+  if (!truncated) {
+    // not truncated within cap steps: the tile is used as is
+    if (local == 0 && threadIdx.x == 0) *t.rank = min(M, N);
+    return;
+  }
+  const int r = __ldcg(t.rank);
+  if (r == 0) return;
+  // Q(:, j) = H_0 ... H_j e_j for j < r (warp per column, in place in T), and
+  // Y(i, jpvt(c)) = R(i, c) for c >= i (R P^T, DLAPMT) into F's storage
+  for (int j = local * QR_WARPS + warp; j < r; j += t.ncta * QR_WARPS) {
+    double* x = t.T + (long)j * M;
+    const double tj = __ldcg(t.tau + j);
+    const double* vj = t.V + (long)j * M;
+    for (int i = lane; i < M; i += 32) x[i] = (i < j) ? 0.0 : (i == j ? 1.0 - tj : -tj * __ldcg(vj + i));
+    __syncwarp();
+    for (int h = j - 1; h >= 0; --h) {
+      const double* vh = t.V + (long)h * M;
+      double d = 0.0;
+      for (int i = h + lane; i < M; i += 32) d = fma(__ldcg(vh + i), x[i], d);  // V(h,h) = 1
+      for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+      d *= __ldcg(t.tau + h);
+      __syncwarp();
+      for (int i = h + lane; i < M; i += 32) x[i] -= d * __ldcg(vh + i);
+      __syncwarp();
+    }
+  }
+  const long total = (long)r * N;
+  for (long e = (long)local * blockDim.x + threadIdx.x; e < total; e += (long)t.ncta * blockDim.x) {
+    const int c = (int)(e / r), i = (int)(e % r);
+    const double y = (c >= i) ? __ldcg(t.R + (long)c * cap + i) : 0.0;
+    t.F[(long)__ldcg(t.jpvt + c) * r + i] = y;
+  }
+}
+
+}  // namespace psmma
+
+// ------------------------------------------------------------------------------------------
+// Batched merge level: Q_i = alpha * A_i * H_i + beta * Q_i for a batch of Cauchy products,
+// the off-diagonal blocks of each H_i (2 x 2 split at n_i / 2) compressed.  After the
+// compression the products run in two grouped rounds (one launch per phase for all
+// products of a round), recorded in one CUDA graph:
+//   round 1: diagonal blocks (beta applied) and the first factor products,
+//   round 2: the second factor products and uncompressed off-diagonal blocks (beta = 1).
+// ------------------------------------------------------------------------------------------
+using namespace psmma;
+
+namespace {
+
+struct OffBlock {
+  int item, r0, M, c0, N;  // rows [r0, r0+M), columns [c0, c0+N) of H_item
+};
+
+// Bump allocation over one workspace; with base 0 it only measures.
+struct Bump {
+  uintptr_t base, off = 0;
+  explicit Bump(void* b) : base((uintptr_t)b) {}
+  template <class T>
+  T* take(size_t count, size_t align = 256) {
+    off = (off + align - 1) & ~(uintptr_t)(align - 1);
+    T* p = (T*)(base + off);
+    off += count * sizeof(T);
+    return p;
+  }
+};
+
+// Part A of the workspace: compression state, gather buffers, descriptors, status words.
+struct Plan {
+  std::vector<OffBlock> blocks;
+  std::vector<RrluBlock> lu;
+  std::vector<QrTile> qr;
+  RrluBlock* d_lu = nullptr;
+  QrTile* d_qr = nullptr;
+  int* d_ranks = nullptr;        // RRLU ranks
+  std::vector<double*> gather;   // per block: RRLU n x M, RRQR n x cap
+  GatherDesc* d_gather = nullptr;
+  unsigned* d_status = nullptr;  // [0..7] product rounds, [8] QR
+  int* d_map = nullptr;          // CTA -> tile of the grouped QR launch
+  long qr_cols = 0;
+  static constexpr int MAP_MAX = 8192;
+  static constexpr int N_STATUS = 16;
+};
+
+GenSpec cauchy_sub(const double* gen, long ldgen, int r0, int c0) {
+  GenSpec g;
+  g.kind = KIND_CAUCHY;
+  g.Dr = gen + r0;
+  g.Fc = gen + ldgen + c0;
+  g.Ur = gen + 2 * ldgen + r0;
+  g.Vc = gen + 3 * ldgen + c0;
+  return g;
+}
+
+void make_plan(Plan& P, Bump& bump, const psmma_batch_item* items, int count, int compressor) {
+  P.blocks.clear();
+  for (int i = 0; i < count; ++i) {
+    const int n = items[i].n, h = n / 2;
+    if (h == 0) continue;
+    P.blocks.push_back(OffBlock{i, 0, h, h, n - h});  // H(R1, C2)
+    P.blocks.push_back(OffBlock{i, h, n - h, 0, h});  // H(R2, C1)
+  }
+  const int nb = (int)P.blocks.size();
+  P.gather.assign(nb, nullptr);
+  if (compressor == PSMMA_COMPRESS_RRLU) {
+    P.lu.resize(nb);
+    for (int b = 0; b < nb; ++b) {
+      const OffBlock& ob = P.blocks[b];
+      const psmma_batch_item& it = items[ob.item];
+      RrluBlock& r = P.lu[b];
+      r.M = ob.M;
+      r.N = ob.N;
+      r.gD = it.gen + ob.r0;
+      r.gU = it.gen + 2 * (long)it.ldgen + ob.r0;
+      r.gF = it.gen + it.ldgen + ob.c0;
+      r.gV = it.gen + 3 * (long)it.ldgen + ob.c0;
+      r.D = bump.take<double>(ob.M);
+      r.A = bump.take<double>(ob.M);
+      r.U = bump.take<double>(ob.M);
+      r.F = bump.take<double>(ob.N);
+      r.V = bump.take<double>(ob.N);
+      r.W = bump.take<double>(std::min(ob.M, ob.N));
+      r.PL = bump.take<int>(ob.M);
+      r.PU = bump.take<int>(ob.N);
+      P.gather[b] = bump.take<double>((size_t)it.n * ob.M);
+    }
+    P.d_lu = bump.take<RrluBlock>(std::max(1, nb));
+    P.d_ranks = bump.take<int>(std::max(1, nb));
+    P.d_gather = bump.take<GatherDesc>(std::max(1, nb));
+    for (int b = 0; b < nb; ++b) P.lu[b].rank = P.d_ranks + b;
+  } else {
+    P.qr.resize(nb);
+    long col0 = 0;
+    for (int b = 0; b < nb; ++b) {
+      const OffBlock& ob = P.blocks[b];
+      const psmma_batch_item& it = items[ob.item];
+      QrTile& q = P.qr[b];
+      q.M = ob.M;
+      q.N = ob.N;
+      q.cap = std::min(std::min(ob.M, ob.N), QR_CAP);
+      q.gD = it.gen + ob.r0;
+      q.gU = it.gen + 2 * (long)it.ldgen + ob.r0;
+      q.gF = it.gen + it.ldgen + ob.c0;
+      q.gV = it.gen + 3 * (long)it.ldgen + ob.c0;
+      q.T = bump.take<double>((size_t)ob.M * ob.N);
+      q.V = bump.take<double>((size_t)ob.M * q.cap);
+      q.F = bump.take<double>((size_t)ob.N * q.cap);
+      q.R = bump.take<double>((size_t)ob.N * q.cap);
+      q.tau = bump.take<double>(q.cap + 1);
+      q.s = bump.take<double>(q.cap);
+      q.vn1 = bump.take<double>(ob.N);
+      q.vn2 = bump.take<double>(ob.N);
+      q.jpvt = bump.take<int>(ob.N);
+      q.rank = bump.take<int>(1);
+      q.bar = bump.take<unsigned>(1);
+      q.col0 = col0;
+      col0 += ob.N;
+      P.gather[b] = bump.take<double>((size_t)it.n * q.cap);
+    }
+    P.qr_cols = col0;
+    P.d_qr = bump.take<QrTile>(std::max(1, nb));
+    P.d_map = bump.take<int>(Plan::MAP_MAX);
+  }
+  P.d_status = bump.take<unsigned>(Plan::N_STATUS);
+}
+
+// Products of the two rounds for the given ranks (rank >= min(M, N): block not compressed).
+struct Rounds {
+  std::vector<SplitProblem> r1, r2;
+  double executed = 0.0;
+  int max_rank = 0, full_blocks = 0;
+};
+
+void build_rounds(const Plan& P, const psmma_batch_item* items, int count, int compressor, const int* ranks,
+                  double alpha, double beta, Rounds& R) {
+  for (int i = 0; i < count; ++i) {
+    const psmma_batch_item& it = items[i];
+    const int n = it.n, h = n / 2;
+    if (n == 0) continue;
+    // diagonal blocks: Q(:, C1) = alpha A(:, R1) H(R1, C1) + beta Q(:, C1), and for R2, C2
+    if (h > 0)
+      R.r1.push_back(SplitProblem{n, h, h, alpha, beta, it.A, it.lda, cauchy_sub(it.gen, it.ldgen, 0, 0), it.Q,
+                                  it.ldq});
+    R.r1.push_back(SplitProblem{n, n - h, n - h, alpha, beta, it.A + (long)h * it.lda, it.lda,
+                                cauchy_sub(it.gen, it.ldgen, h, h), it.Q + (long)h * it.ldq, it.ldq});
+    R.executed += 2.0 * n * ((double)h * h + (double)(n - h) * (n - h));
+  }
+  const int nb = (int)P.blocks.size();
+  for (int b = 0; b < nb; ++b) {
+    const OffBlock& ob = P.blocks[b];
+    const psmma_batch_item& it = items[ob.item];
+    const int n = it.n, mn = std::min(ob.M, ob.N), Rk = ranks[b];
+    const double* Ablk = it.A + (long)ob.r0 * it.lda;  // A(:, R)
+    double* Qblk = it.Q + (long)ob.c0 * it.ldq;        // Q(:, C)
+    if (Rk >= mn) {
+      // not compressed: the generated tile (the reference would reuse a stale buffer here)
+      ++R.full_blocks;
+      R.r2.push_back(SplitProblem{n, ob.N, ob.M, alpha, 1.0, Ablk, it.lda, cauchy_sub(it.gen, it.ldgen, ob.r0, ob.c0),
+                                  Qblk, it.ldq});
+      R.executed += 2.0 * n * (double)ob.M * ob.N;
+      continue;
+    }
+    R.max_rank = std::max(R.max_rank, Rk);
+    if (Rk == 0) continue;
+    double* T = P.gather[b];
+    if (compressor == PSMMA_COMPRESS_RRLU) {
+      const RrluBlock& r = P.lu[b];
+      // T0 += Ar * Z',  Z'(t, j) = U(Rk+t) W(j) / (LD(Rk+t) - LD(j))  (T0, Ar gathered)
+      GenSpec gz;
+      gz.kind = KIND_CAUCHY;
+      gz.Dr = r.D + Rk;
+      gz.Ur = r.U + Rk;
+      gz.Fc = r.D;
+      gz.Vc = r.W;
+      if (ob.M - Rk > 0)
+        R.r1.push_back(SplitProblem{n, Rk, ob.M - Rk, 1.0, 1.0, T + (size_t)n * Rk, n, gz, T, n});
+      // Q(:, C) += alpha * T0 * Y,  Y(j, c) = LU(j) V(c) / (LD(j) - F(c)) with the unpermuted F, V
+      GenSpec gy;
+      gy.kind = KIND_CAUCHY;
+      gy.Dr = r.D;
+      gy.Ur = r.A;
+      gy.Fc = r.gF;
+      gy.Vc = r.gV;
+      R.r2.push_back(SplitProblem{n, ob.N, Rk, alpha, 1.0, T, n, gy, Qblk, it.ldq});
+      R.executed += 2.0 * n * (double)(ob.M - Rk) * Rk + 2.0 * n * (double)Rk * ob.N;
+    } else {
+      const QrTile& q = P.qr[b];
+      // T = A(:, R) * Q(:, 1:Rk), then Q(:, C) += alpha * T * (R P^T)
+      GenSpec gq;
+      gq.kind = KIND_DENSE;
+      gq.B = q.T;
+      gq.ldb = ob.M;
+      R.r1.push_back(SplitProblem{n, Rk, ob.M, 1.0, 0.0, Ablk, it.lda, gq, T, n});
+      GenSpec gyy;
+      gyy.kind = KIND_DENSE;
+      gyy.B = q.F;
+      gyy.ldb = Rk;
+      R.r2.push_back(SplitProblem{n, ob.N, Rk, alpha, 1.0, T, n, gyy, Qblk, it.ldq});
+      R.executed += 2.0 * n * (double)ob.M * Rk + 2.0 * n * (double)Rk * ob.N;
+    }
+  }
+}
+
+// Workspace of the product rounds (part B).
+struct RoundGroups {
+  SplitGroup s1, s2;
+  F64Group f[4];  // round 1 Cauchy, round 1 dense, round 2 Cauchy, round 2 dense
+};
+
+std::vector<F64Prob> f64_of(const std::vector<SplitProblem>& v, int kind) {
+  std::vector<F64Prob> out;
+  for (const SplitProblem& q : v)
+    if (q.gs.kind == kind) out.push_back(F64Prob{q.M, q.N, q.K, q.alpha, q.beta, q.A, q.lda, q.gs, q.Q, q.ldq});
+  return out;
+}
+
+size_t rounds_bytes(const Rounds& R, int precision, int n_moduli) {
+  if (precision == PSMMA_PREC_SPLIT)
+    return split_group_bytes(R.r1.data(), (int)R.r1.size(), n_moduli) + 4096 +
+           split_group_bytes(R.r2.data(), (int)R.r2.size(), n_moduli) + 4096;
+  return f64_group_bytes((int)R.r1.size()) * 2 + f64_group_bytes((int)R.r2.size()) * 2 + 4096;
+}
+
+int prepare_rounds(const Rounds& R, int precision, int n_moduli, int narrow_max, int group_m, void* work,
+                   size_t lwork, cudaStream_t st, RoundGroups& G) {
+  Bump b(work);
+  if (precision == PSMMA_PREC_SPLIT) {
+    const size_t b1 = split_group_bytes(R.r1.data(), (int)R.r1.size(), n_moduli);
+    const size_t b2 = split_group_bytes(R.r2.data(), (int)R.r2.size(), n_moduli);
+    char* w1 = b.take<char>(b1, 4096);
+    char* w2 = b.take<char>(b2, 4096);
+    if (b.off > lwork) return PSMMA_EWORKSPACE;
+    int rc = split_group_prepare(R.r1.data(), (int)R.r1.size(), n_moduli, narrow_max, group_m, w1, b1, st, &G.s1);
+    if (!rc) rc = split_group_prepare(R.r2.data(), (int)R.r2.size(), n_moduli, narrow_max, group_m, w2, b2, st, &G.s2);
+    return rc;
+  }
+  const std::vector<SplitProblem>* rs[2] = {&R.r1, &R.r2};
+  for (int r = 0; r < 2; ++r)
+    for (int k = 0; k < 2; ++k) {
+      const std::vector<F64Prob> v = f64_of(*rs[r], k == 0 ? KIND_CAUCHY : KIND_DENSE);
+      char* w = b.take<char>(f64_group_bytes((int)v.size()), 256);
+      if (b.off > lwork) return PSMMA_EWORKSPACE;
+      const int rc = f64_group_prepare(v.data(), (int)v.size(), w, st, &G.f[2 * r + k]);
+      if (rc) return rc;
+    }
+  return PSMMA_OK;
+}
+
+int enqueue_rounds(const RoundGroups& G, int precision, unsigned* status, cudaStream_t st) {
+  int rc = PSMMA_OK;
+  if (precision == PSMMA_PREC_SPLIT) {
+    rc = split_group_enqueue(G.s1, st, status + 0);
+    if (!rc) rc = split_group_enqueue(G.s2, st, status + 1);
+    return rc;
+  }
+  for (int i = 0; i < 4 && !rc; ++i) rc = f64_group_enqueue(G.f[i], st);
+  return rc;
+}
+
+// Worst-case part B for a batch (every block at its largest rank and also uncompressed).
+size_t rounds_bound(const Plan& P, const psmma_batch_item* items, int count, int compressor, int precision,
+                    int n_moduli) {
+  const int nb = (int)P.blocks.size();
+  std::vector<int> rk(nb), full(nb);
+  for (int b = 0; b < nb; ++b) {
+    const int mn = std::min(P.blocks[b].M, P.blocks[b].N);
+    rk[b] = compressor == PSMMA_COMPRESS_RRLU ? std::max(0, mn - 1) : std::min(std::max(0, mn - 1), QR_CAP);
+    full[b] = mn;
+  }
+  Rounds a, f;
+  build_rounds(P, items, count, compressor, rk.data(), 1.0, 0.0, a);
+  build_rounds(P, items, count, compressor, full.data(), 1.0, 0.0, f);
+  return rounds_bytes(a, precision, n_moduli) + rounds_bytes(f, precision, n_moduli);
+}
+
+// Cooperative launch of the grouped QR over the tiles [t0, t1): every tile gets at least one
+// CTA and the rest in proportion to M * N.
+int launch_rrqr_wave(Plan& P, int t0, int t1, int grid, int* h_map, int* d_map, double tol, unsigned* status,
+                     cudaStream_t st) {
+  const int nt = t1 - t0;  // <= grid
+  double wsum = 0.0;
+  for (int b = t0; b < t1; ++b) wsum += (double)P.qr[b].M * P.qr[b].N;
+  int next = 0;
+  const int spare = grid - nt;
+  for (int b = t0; b < t1; ++b) {
+    QrTile& q = P.qr[b];
+    int extra = wsum > 0 ? (int)((double)spare * ((double)q.M * q.N) / wsum) : 0;
+    extra = std::min(extra, std::max(0, q.N / QR_WARPS - 1));  // at least a column per warp
+    q.cta0 = next;
+    q.ncta = 1 + extra;
+    for (int c = 0; c < q.ncta; ++c) h_map[next + c] = b;
+    next += q.ncta;
+  }
+  for (int c = next; c < grid; ++c) h_map[c] = -1;
+  if (cudaMemcpyAsync(P.d_qr + t0, P.qr.data() + t0, sizeof(QrTile) * (t1 - t0), cudaMemcpyHostToDevice, st) !=
+          cudaSuccess ||
+      cudaMemcpyAsync(d_map, h_map, sizeof(int) * grid, cudaMemcpyHostToDevice, st) != cudaSuccess)
+    return PSMMA_EDEVICE;
+  QrTile* tiles = P.d_qr;
+  const int* map = d_map;
+  void* args[] = {(void*)&tiles, (void*)&map, (void*)&tol, (void*)&status};
+  if (cudaLaunchCooperativeKernel((const void*)k_rrqr_grouped, dim3(next), dim3(QR_THREADS), args, 0, st) !=
+      cudaSuccess)
+    return PSMMA_EDEVICE;
+  // the host copies of the map and tiles are reused by the next wave: wait for this one
+  return cudaStreamSynchronize(st) == cudaSuccess ? PSMMA_OK : PSMMA_EDEVICE;
+}
+
+int check_batch(int count, const psmma_batch_item* items, int precision, int n_moduli, int compressor,
+                double tol) {
+  if (count < 0 || (count > 0 && !items)) return PSMMA_ENULL;
+  if (precision != PSMMA_PREC_FP64 && precision != PSMMA_PREC_SPLIT) return PSMMA_EUNSUPPORTED;
+  if (precision == PSMMA_PREC_SPLIT && n_moduli != 0 && (n_moduli < 8 || n_moduli > 16)) return PSMMA_EUNSUPPORTED;
+  if (compressor != PSMMA_COMPRESS_RRQR && compressor != PSMMA_COMPRESS_RRLU) return PSMMA_EUNSUPPORTED;
+  if (!(tol > 0.0) || !(tol < 1.0)) return PSMMA_EUNSUPPORTED;
+  for (int i = 0; i < count; ++i) {
+    const psmma_batch_item& it = items[i];
+    if (it.n < 0) return -2;
+    if (it.lda < std::max(1, it.n)) return -9;
+    if (it.ldq < std::max(1, it.n)) return -14;
+    if (it.n > 0 && (!it.A || !it.Q)) return PSMMA_ENULL;
+    if (it.n > 0 && (!it.gen || it.ldgen < it.n)) return PSMMA_EGEN;
+  }
+  return PSMMA_OK;
+}
+
+size_t part_a_bytes(Plan& P, const psmma_batch_item* items, int count, int compressor) {
+  Bump m(nullptr);
+  make_plan(P, m, items, count, compressor);
+  return m.off + 4096;
+}
+
+}  // namespace
+
+// Tuning knobs of the grouped split GEMM (set by the autotuner): output-tile width 64 for
+// products with N <= narrow_max, raster group of group_m row tiles.
+static int g_narrow_max = 64, g_group_m = 12;
+
+extern "C" size_t psmma_batch_workspace_size(int count, const psmma_batch_item* items, int compressor,
+                                             const psmma_opts* opts) {
+  const int precision = opts ? opts->precision : PSMMA_PREC_FP64;
+  const int n_moduli = opts ? opts->n_moduli : 0;
+  if (count <= 0 || !items || check_batch(count, items, precision, n_moduli, compressor, 0.5)) return 0;
+  Plan P;
+  const size_t a = part_a_bytes(P, items, count, compressor);
+  return a + rounds_bound(P, items, count, compressor, precision, n_moduli) + 4096;
+}
+
+extern "C" int psmma_cauchy_batch_lowrank(int count, const psmma_batch_item* items, double alpha, double beta,
+                                          int compressor, double tol, const psmma_opts* opts, int* ranks_out,
+                                          psmma_batch_stats* stats, void* stream) {
+  const int precision = opts ? opts->precision : PSMMA_PREC_FP64;
+  const int n_moduli = opts ? opts->n_moduli : 0;
+  int rc = check_batch(count, items, precision, n_moduli, compressor, tol);
+  if (rc) return rc;
+  if (stats) *stats = psmma_batch_stats{0.0, 0.0, 0.0, 0, 0, 0, 0};
+  if (count == 0) return PSMMA_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+
+  Plan P;
+  const size_t need_a = part_a_bytes(P, items, count, compressor);
+  char* work_a = nullptr;
+  char* work_b = nullptr;
+  size_t lwork_b = 0;
+  if (opts && opts->work) {
+    const size_t bound = need_a + rounds_bound(P, items, count, compressor, precision, n_moduli) + 4096;
+    if (opts->lwork < bound) return PSMMA_EWORKSPACE;
+    work_a = (char*)opts->work;
+    work_b = (char*)((((uintptr_t)work_a + need_a) + 4095) & ~(uintptr_t)4095);
+    lwork_b = (size_t)(work_a + opts->lwork - work_b);
+  } else {
+    work_a = (char*)pool_get(need_a, st, &rc, 0);
+    if (rc) return rc;
+  }
+  Bump bump((void*)(((uintptr_t)work_a + 255) & ~(uintptr_t)255));
+  make_plan(P, bump, items, count, compressor);
+  const int nb = (int)P.blocks.size();
+  if (cudaMemsetAsync(P.d_status, 0, sizeof(unsigned) * Plan::N_STATUS, st) != cudaSuccess) return PSMMA_EDEVICE;
+  unsigned* qr_status = P.d_status + 8;
+  prof_begin(st);
+
+  // ---- phase 1: compression of every off-diagonal block
+  std::vector<int> ranks(nb, 0);
+  double compress_flops = 0.0;
+  if (nb && compressor == PSMMA_COMPRESS_RRLU) {
+    if (cudaMemcpyAsync(P.d_lu, P.lu.data(), sizeof(RrluBlock) * nb, cudaMemcpyHostToDevice, st) != cudaSuccess)
+      return PSMMA_EDEVICE;
+    k_rrlu_cauchy<<<nb, RRLU_THREADS, 0, st>>>(P.d_lu, tol);
+    if (cudaGetLastError() != cudaSuccess) return PSMMA_EDEVICE;
+    if (cudaMemcpyAsync(ranks.data(), P.d_ranks, sizeof(int) * nb, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      return PSMMA_EDEVICE;
+    for (int b = 0; b < nb; ++b) compress_flops += 12.0 * (ranks[b] + 1) * (P.blocks[b].M + P.blocks[b].N);
+  } else if (nb) {
+    if (cudaMemcpyAsync(P.d_qr, P.qr.data(), sizeof(QrTile) * nb, cudaMemcpyHostToDevice, st) != cudaSuccess)
+      return PSMMA_EDEVICE;
+    if (P.qr_cols > 0x7fffffffL) return PSMMA_EUNSUPPORTED;
+    k_qr_tiles<<<(unsigned)P.qr_cols, QR_THREADS, 0, st>>>(P.d_qr, nb);
+    if (cudaGetLastError() != cudaSuccess) return PSMMA_EDEVICE;
+    int dev = 0, sms = 0, occ = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_rrqr_grouped, QR_THREADS, 0) != cudaSuccess || occ < 1)
+      return PSMMA_EDEVICE;
+    const int grid = std::min(sms * std::min(occ, 4), Plan::MAP_MAX);
+    std::vector<int> h_map(grid);
+    for (int t0 = 0; t0 < nb; t0 += grid) {
+      rc = launch_rrqr_wave(P, t0, std::min(nb, t0 + grid), grid, h_map.data(), P.d_map, tol, qr_status, st);
+      if (rc) return rc;
+    }
+    unsigned qs = 0;
+    if (cudaMemcpyAsync(&qs, qr_status, sizeof(unsigned), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+      return PSMMA_EDEVICE;
+    for (int b = 0; b < nb; ++b)
+      if (cudaMemcpyAsync(&ranks[b], P.qr[b].rank, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+        return PSMMA_EDEVICE;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return PSMMA_EDEVICE;
+    if (qs & DEV_ERR_TIMEOUT) return PSMMA_ETIMEDOUT;
+    for (int b = 0; b < nb; ++b) {
+      const double M = P.blocks[b].M, N = P.blocks[b].N, r = std::min(ranks[b], P.qr[b].cap);
+      compress_flops += 4.0 * M * N * (r + 1) + 4.0 * M * r * r;
+    }
+  }
+  if (ranks_out)
+    for (int b = 0; b < nb; ++b) ranks_out[b] = ranks[b];
+  prof_mark(st, compressor == PSMMA_COMPRESS_RRLU ? "compress_rrlu" : "compress_rrqr");
+
+  // ---- phase 2: the product rounds, one CUDA graph
+  Rounds R;
+  build_rounds(P, items, count, compressor, ranks.data(), alpha, beta, R);
+  const size_t need_b = rounds_bytes(R, precision, n_moduli);
+  if (!work_b) {
+    work_b = (char*)pool_get(need_b, st, &rc, 1);
+    if (rc) return rc;
+    lwork_b = need_b;
+  }
+  RoundGroups G;
+  rc = prepare_rounds(R, precision, n_moduli, g_narrow_max, g_group_m, work_b, lwork_b, st, G);
+  if (rc) return rc;
+  std::vector<GatherDesc> gd;
+  int gather_cols = 0;
+  if (compressor == PSMMA_COMPRESS_RRLU) {
+    for (int b = 0; b < nb; ++b) {
+      const OffBlock& ob = P.blocks[b];
+      const psmma_batch_item& it = items[ob.item];
+      if (ranks[b] <= 0 || ranks[b] >= std::min(ob.M, ob.N)) continue;
+      GatherDesc g;
+      g.A = it.A + (long)ob.r0 * it.lda;
+      g.lda = it.lda;
+      g.n = it.n;
+      g.M = ob.M;
+      g.Rk = ranks[b];
+      g.c0 = gather_cols;
+      g.PL = P.lu[b].PL;
+      g.T0 = P.gather[b];
+      g.Ar = P.gather[b] + (size_t)it.n * ranks[b];
+      gd.push_back(g);
+      gather_cols += ob.M;
+    }
+    if (!gd.empty() && cudaMemcpyAsync(P.d_gather, gd.data(), sizeof(GatherDesc) * gd.size(),
+                                       cudaMemcpyHostToDevice, st) != cudaSuccess)
+      return PSMMA_EDEVICE;
+  }
+  prof_mark(st, "prepare_rounds");
+  if (prof_enabled()) {
+    // traced run: the same launches directly on the stream, one event per phase
+    if (!gd.empty()) k_gather_group<<<gather_cols, 256, 0, st>>>(P.d_gather, (int)gd.size());
+    prof_mark(st, "gather");
+    rc = enqueue_rounds(G, precision, P.d_status, st);
+    unsigned sts[Plan::N_STATUS] = {0};
+    if (!rc && (cudaMemcpyAsync(sts, P.d_status, sizeof(sts), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+                cudaStreamSynchronize(st) != cudaSuccess))
+      rc = PSMMA_EDEVICE;
+    for (unsigned v : sts)
+      if (!rc && (v & DEV_ERR_TIMEOUT)) rc = PSMMA_ETIMEDOUT;
+    if (stats) {
+      double eff = 0.0;
+      for (int i = 0; i < count; ++i) eff += 2.0 * items[i].n * (double)items[i].n * items[i].n;
+      *stats = psmma_batch_stats{eff, R.executed, compress_flops, nb, R.max_rank, R.full_blocks, 0};
+    }
+    return rc;
+  }
+  cudaStream_t cap = nullptr;
+  if (cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking) != cudaSuccess) return PSMMA_EDEVICE;
+  cudaEvent_t ev = nullptr;
+  if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) {
+    cudaStreamDestroy(cap);
+    return PSMMA_EDEVICE;
+  }
+  cudaEventRecord(ev, st);
+  cudaStreamWaitEvent(cap, ev, 0);  // the graph follows the compression and the copies above
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  if (cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) != cudaSuccess) rc = PSMMA_EDEVICE;
+  if (!rc && !gd.empty()) {
+    k_gather_group<<<gather_cols, 256, 0, cap>>>(P.d_gather, (int)gd.size());
+    if (cudaGetLastError() != cudaSuccess) rc = PSMMA_EDEVICE;
+  }
+  if (!rc) rc = enqueue_rounds(G, precision, P.d_status, cap);
+  cudaError_t ce = cudaStreamEndCapture(cap, &graph);
+  if (!rc && ce != cudaSuccess) rc = PSMMA_EDEVICE;
+  if (!rc && cudaGraphInstantiate(&gexec, graph, 0) != cudaSuccess) rc = PSMMA_EDEVICE;
+  if (!rc && cudaGraphLaunch(gexec, cap) != cudaSuccess) rc = PSMMA_EDEVICE;
+  cudaEventRecord(ev, cap);
+  cudaStreamWaitEvent(st, ev, 0);  // later work on `stream` follows the graph
+  unsigned sts[Plan::N_STATUS] = {0};
+  if (!rc && (cudaMemcpyAsync(sts, P.d_status, sizeof(sts), cudaMemcpyDeviceToHost, cap) != cudaSuccess ||
+              cudaStreamSynchronize(cap) != cudaSuccess))
+    rc = PSMMA_EDEVICE;
+  if (gexec) cudaGraphExecDestroy(gexec);
+  if (graph) cudaGraphDestroy(graph);
+  cudaEventDestroy(ev);
+  cudaStreamDestroy(cap);
+  for (unsigned v : sts)
+    if (!rc && (v & DEV_ERR_TIMEOUT)) rc = PSMMA_ETIMEDOUT;
+  if (stats) {
+    double eff = 0.0;
+    for (int i = 0; i < count; ++i) eff += 2.0 * items[i].n * (double)items[i].n * items[i].n;
+    stats->effective_flops = eff;
+    stats->executed_flops = R.executed;
+    stats->compress_flops = compress_flops;
+    stats->n_blocks = nb;
+    stats->max_rank = R.max_rank;
+    stats->full_rank_blocks = R.full_blocks;
+  }
+  return rc;
+}

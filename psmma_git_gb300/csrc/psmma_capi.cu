@@ -4,6 +4,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <tuple>
 #include <mutex>
 #include <utility>
 
@@ -21,16 +22,16 @@ struct Pool {
   size_t bytes = 0;
 };
 std::mutex g_pool_mu;
-std::map<std::pair<int, cudaStream_t>, Pool> g_pools;
+std::map<std::tuple<int, cudaStream_t, int>, Pool> g_pools;
 }  // namespace
 
-void* pool_get(size_t bytes, cudaStream_t stream, int* status) {
+void* pool_get(size_t bytes, cudaStream_t stream, int* status, int slot) {
   *status = PSMMA_OK;
   if (bytes == 0) return nullptr;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) { *status = PSMMA_EDEVICE; return nullptr; }
   std::lock_guard<std::mutex> lk(g_pool_mu);
-  Pool& pl = g_pools[{dev, stream}];
+  Pool& pl = g_pools[std::make_tuple(dev, stream, slot)];
   if (pl.bytes >= bytes) return pl.ptr;
   if (pl.ptr) {
     if (cudaStreamSynchronize(stream) != cudaSuccess) { *status = PSMMA_EDEVICE; return nullptr; }
@@ -63,8 +64,14 @@ bool g_prof_created = false;
 
 bool prof_enabled() { return g_prof_on; }
 
+// Phases inside a stream capture are not traced (their events would belong to the graph).
+static bool capturing(cudaStream_t stream) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  return cudaStreamIsCapturing(stream, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone;
+}
+
 void prof_begin(cudaStream_t stream) {
-  if (!g_prof_on) return;
+  if (!g_prof_on || capturing(stream)) return;
   std::lock_guard<std::mutex> lk(g_prof_mu);
   if (!g_prof_created) {
     for (int i = 0; i <= PROF_MAX_PHASES; ++i) cudaEventCreate(&g_prof_ev[i]);
@@ -77,7 +84,7 @@ void prof_begin(cudaStream_t stream) {
 }
 
 void prof_mark(cudaStream_t stream, const char* name) {
-  if (!g_prof_on) return;
+  if (!g_prof_on || capturing(stream)) return;
   std::lock_guard<std::mutex> lk(g_prof_mu);
   if (g_prof_n > PROF_MAX_PHASES) return;
   cudaEventRecord(g_prof_ev[g_prof_n], stream);
@@ -150,7 +157,7 @@ int run_real(int kind, int n, int k, double alpha, const double* A, int lda, con
     return launch_split(kind, n, k, alpha, A, lda, gen, ldgen, beta, Q, ldq, o->n_moduli, work,
                         need, s);
   }
-  return launch_struct_f64(kind, n, k, k, alpha, A, lda, gen, ldgen, k, nullptr, beta, Q, ldq, s);
+  return launch_struct_f64(n, k, k, alpha, A, lda, reference_gens(kind, gen, ldgen, k), beta, Q, ldq, s);
 }
 
 int run_dft(int n, int k, double alpha, const psmma_complex* B, int ldb, double beta,
@@ -188,8 +195,11 @@ int run_dft(int n, int k, double alpha, const psmma_complex* B, int ldb, double 
     if (st) return st;
   }
   // Real view: C'(2n x k) = F'(2n x 2n) * B'(2n x k), ld doubled.
-  return launch_struct_f64(KIND_DFT, 2 * n, k, 2 * n, alpha, (const double*)B, 2L * ldb, nullptr,
-                           0, n, wtab, beta, (double*)C, 2L * ldc, s);
+  GenSpec gs;
+  gs.kind = KIND_DFT;
+  gs.n_dft = n;
+  gs.wtab = wtab;
+  return launch_struct_f64(2 * n, k, 2 * n, alpha, (const double*)B, 2L * ldb, gs, beta, (double*)C, 2L * ldc, s);
 }
 
 // ---- host-pointer wrappers -------------------------------------------------------------
@@ -383,8 +393,8 @@ void psmma_release_workspace(void) {
   {
     std::lock_guard<std::mutex> lk(g_pool_mu);
     for (auto it = g_pools.begin(); it != g_pools.end();) {
-      if (it->first.first == dev) {
-        cudaStreamSynchronize(it->first.second);
+      if (std::get<0>(it->first) == dev) {
+        cudaStreamSynchronize(std::get<1>(it->first));
         cudaFree(it->second.ptr);
         it = g_pools.erase(it);
       } else {

@@ -10,13 +10,46 @@
 
 namespace psmma {
 
-enum Kind { KIND_CAUCHY = 0, KIND_TOEPLITZ = 1, KIND_HANKEL = 2, KIND_DFT = 3 };
+enum Kind { KIND_CAUCHY = 0, KIND_TOEPLITZ = 1, KIND_HANKEL = 2, KIND_DFT = 3, KIND_DENSE = 4 };
+
+// Generators of the structured operand H (K x N) of one product.
+//   Cauchy    H(i,j) = Ur[i]*Vc[j] / (Dr[i] - Fc[j])   (row and column generators independent)
+//   Toeplitz  H(i,j) = g[(order-1) + j - i]           (sub-blocks: g offset by c0 - r0)
+//   Hankel    H(i,j) = g[i + j]                        (sub-blocks: g offset by r0 + c0)
+//   DFT       embedding of F = (w^(r c mod n_dft)), table wtab (t < n_dft)
+//   Dense     H(i,j) = B[i + j*ldb]                   (explicit factors of the low-rank path)
+struct GenSpec {
+  int kind = KIND_CAUCHY;
+  const double *Dr = nullptr, *Ur = nullptr, *Fc = nullptr, *Vc = nullptr;
+  const double* g = nullptr;
+  long order = 0;
+  const double2* wtab = nullptr;
+  int n_dft = 0;
+  const double* B = nullptr;
+  long ldb = 0;
+};
+
+// The generators of the reference's square H (k x k) from its storage conventions: Cauchy
+// [D|F|U|V] with leading dimension ldgen, Toeplitz/Hankel vector of 2k-1.
+inline GenSpec reference_gens(int kind, const double* gen, long ldgen, int k) {
+  GenSpec g;
+  g.kind = kind;
+  if (kind == KIND_CAUCHY) {
+    g.Dr = gen;
+    g.Fc = gen + ldgen;
+    g.Ur = gen + 2 * ldgen;
+    g.Vc = gen + 3 * ldgen;
+  } else {
+    g.g = gen;
+    g.order = k;
+  }
+  return g;
+}
 
 // FP64 plain path (fp64_structured.cu).  Real GEMM C(MxN) = alpha*X*G + beta*C where one
 // operand is streamed (X, column-major, ldx) and the other generated.
-int launch_struct_f64(int kind, int M, int N, int K, double alpha, const double* X, long ldx,
-                      const double* gen, long ldgen, int korder, const double2* wtab, double beta,
-                      double* C, long ldc, cudaStream_t stream);
+int launch_struct_f64(int M, int N, int K, double alpha, const double* X, long ldx, const GenSpec& gs,
+                      double beta, double* C, long ldc, cudaStream_t stream);
 int launch_dft_table(double2* w, int n, cudaStream_t stream);
 
 // Split path (split_crt.cu).
@@ -30,13 +63,69 @@ int launch_split(int kind, int n, int k, double alpha, const double* A, long lda
 int launch_split_any(int kind, int n, int k, double alpha, const double* A, long lda,
                      const double* gen, long ldgen, double beta, double* Q, long ldq, int n_moduli,
                      void* work, size_t lwork, cudaStream_t stream, unsigned* status_dev_out);
+// General real product on the split path: Q (M x N) = alpha * A (M x K) * H (K x N) + beta * Q
+// with H given by gs (Cauchy, Toeplitz or Hankel).
+size_t split_workspace_general(int M, int N, int K, int n_moduli);
+int launch_split_general(int M, int N, int K, double alpha, const double* A, long lda, const GenSpec& gs,
+                         double beta, double* Q, long ldq, int n_moduli, void* work, size_t lwork,
+                         cudaStream_t stream, unsigned* status_dev_out);
 
-// Library-owned device workspace (psmma_capi.cu): grow-only, one pool per (device, stream).
-void* pool_get(size_t bytes, cudaStream_t stream, int* status);
+// Grouped split path (split_crt.cu): independent real products of uneven sizes, each
+// Q = alpha * A * H + beta * Q (M, N, K >= 1; H from gs, not the DFT), run as one launch
+// per phase with one persistent modular GEMM per output-tile width (256, or 64 for products
+// with N <= narrow_max).  prepare lays out the workspace and copies the descriptors (not
+// capturable: it copies from host memory); enqueue only launches kernels.
+struct SplitProblem {
+  int M, N, K;
+  double alpha, beta;
+  const double* A;
+  long lda;
+  GenSpec gs;
+  double* Q;
+  long ldq;
+};
+struct SplitGroup {
+  int count = 0, nmod = 0, group_m = 12;
+  void* d_probs = nullptr;
+  void* d_gemm[2] = {nullptr, nullptr};
+  int n_gemm[2] = {0, 0}, tiles[2] = {0, 0};
+  int blocks_row = 0, blocks_h = 0, blocks_ra = 0, blocks_rh = 0, blocks_crt = 0;
+  void* small = nullptr;
+  size_t small_bytes = 0;
+  unsigned* status = nullptr;
+};
+size_t split_group_bytes(const SplitProblem* P, int count, int n_moduli);
+int split_group_prepare(const SplitProblem* P, int count, int n_moduli, int narrow_max, int group_m, void* work,
+                        size_t lwork, cudaStream_t stream, SplitGroup* g);
+int split_group_enqueue(const SplitGroup& g, cudaStream_t stream, unsigned* status_out);
+
+// Grouped FP64 path (fp64_structured.cu): products of one kind (Cauchy or dense H) in one
+// launch, blocks mapped to (product, tile).
+struct F64Prob {
+  int M, N, K;
+  double alpha, beta;
+  const double* X;
+  long ldx;
+  GenSpec gs;
+  double* C;
+  long ldc;
+};
+struct F64Group {
+  int count = 0, kind = 0, blocks = 0;
+  void* d_args = nullptr;
+  int* d_t0 = nullptr;
+};
+size_t f64_group_bytes(int count);
+int f64_group_prepare(const F64Prob* P, int count, void* dev, cudaStream_t stream, F64Group* g);
+int f64_group_enqueue(const F64Group& g, cudaStream_t stream);
+
+// Library-owned device workspace (psmma_capi.cu): grow-only, one pool per (device, stream,
+// slot); a call that needs two independent regions takes them from two slots.
+void* pool_get(size_t bytes, cudaStream_t stream, int* status, int slot = 0);
 
 // Per-phase tracing (psmma_capi.cu): when enabled, launchers record a CUDA event on the
 // launch stream after each phase; psmma_profile_read turns them into milliseconds.
-constexpr int PROF_MAX_PHASES = 16;
+constexpr int PROF_MAX_PHASES = 32;
 bool prof_enabled();
 void prof_begin(cudaStream_t stream);
 void prof_mark(cudaStream_t stream, const char* name);

@@ -162,11 +162,15 @@ int launch_job(psmma_server* s, Job& j) {
       int e = launch_dft_table((double2*)work, r.n, st);
       if (e) return e;
     }
-    return launch_struct_f64(KIND_DFT, 2 * r.n, r.k, 2 * r.n, r.alpha, (const double*)r.A, 2L * r.lda, nullptr, 0,
-                             r.n, (const double2*)work, r.beta, (double*)r.Q, 2L * r.ldq, st);
+    GenSpec gs;
+    gs.kind = KIND_DFT;
+    gs.n_dft = r.n;
+    gs.wtab = (const double2*)work;
+    return launch_struct_f64(2 * r.n, r.k, 2 * r.n, r.alpha, (const double*)r.A, 2L * r.lda, gs, r.beta,
+                             (double*)r.Q, 2L * r.ldq, st);
   }
-  return launch_struct_f64(r.kind, r.n, r.k, r.k, r.alpha, (const double*)r.A, r.lda, r.gen, r.ldgen, r.k, nullptr,
-                           r.beta, (double*)r.Q, r.ldq, st);
+  return launch_struct_f64(r.n, r.k, r.k, r.alpha, (const double*)r.A, r.lda,
+                           reference_gens(r.kind, r.gen, r.ldgen, r.k), r.beta, (double*)r.Q, r.ldq, st);
 }
 
 struct HostCbCtx {

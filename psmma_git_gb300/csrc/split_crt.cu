@@ -23,6 +23,7 @@
 #include <cmath>
 #include <cstring>
 #include <mutex>
+#include <vector>
 
 #include "psmma_internal.h"
 #include "tcgen05_util.cuh"
@@ -135,22 +136,23 @@ struct SplitLayout {
       total;
 };
 
-static SplitLayout split_layout(int n, int k, int nmod) {
+// M rows of A (and Q), K inner length, N columns of H (and Q).
+static SplitLayout split_layout(int M, int K, int N, int nmod) {
   SplitLayout L;
-  L.kp = (k + 63) / 64 * 64;
-  L.kr = (k + 255) / 256 * 256;
+  L.kp = (K + 63) / 64 * 64;
+  L.kr = (N + 255) / 256 * 256;
   size_t o = 0;
   L.off_params = o; o += al1k(sizeof(SplitDevParams));
-  L.off_amax = o;   o += al1k((size_t)n * 8);
-  L.off_hmax = o;   o += al1k((size_t)k * 8);
-  L.off_hsum = o;   o += al1k((size_t)k * 8);
-  L.off_asq = o;    o += al1k((size_t)n * 8);
-  L.off_hsq = o;    o += al1k((size_t)k * 8);
-  L.off_wtab = o;   o += al1k((size_t)(k / 2 + 1) * 16);
-  L.off_ht = o;     o += al1k((size_t)k * L.kp * 8);
-  L.off_ra = o;     o += al1k((size_t)nmod * n * L.kp * 2);
-  L.off_rh = o;     o += al1k((size_t)nmod * k * L.kp * 2);
-  L.off_r = o;      o += al1k((size_t)nmod * n * L.kr);
+  L.off_amax = o;   o += al1k((size_t)M * 8);
+  L.off_hmax = o;   o += al1k((size_t)N * 8);
+  L.off_hsum = o;   o += al1k((size_t)N * 8);
+  L.off_asq = o;    o += al1k((size_t)M * 8);
+  L.off_hsq = o;    o += al1k((size_t)N * 8);
+  L.off_wtab = o;   o += al1k((size_t)(K / 2 + 1) * 16);
+  L.off_ht = o;     o += al1k((size_t)N * L.kp * 8);
+  L.off_ra = o;     o += al1k((size_t)nmod * M * L.kp * 2);
+  L.off_rh = o;     o += al1k((size_t)nmod * N * L.kp * 2);
+  L.off_r = o;      o += al1k((size_t)nmod * M * L.kr);
   L.total = o;
   return L;
 }
@@ -160,8 +162,13 @@ static int resolve_nmod(int n_moduli) { return n_moduli == 0 ? SPL_DEFAULT_MODUL
 size_t split_workspace_bytes(int kind, int n, int k, int n_moduli) {
   if (n <= 0 || k <= 0) return 0;
   // DFT: the product runs as (B^T embedded, k x 2n) * (F embedded, 2n x 2n)
-  if (kind == KIND_DFT) return split_layout(k, 2 * n, resolve_nmod(n_moduli)).total;
-  return split_layout(n, k, resolve_nmod(n_moduli)).total;
+  if (kind == KIND_DFT) return split_layout(k, 2 * n, 2 * n, resolve_nmod(n_moduli)).total;
+  return split_layout(n, k, k, resolve_nmod(n_moduli)).total;
+}
+
+size_t split_workspace_general(int M, int N, int K, int n_moduli) {
+  if (M <= 0 || N <= 0 || K <= 0) return 0;
+  return split_layout(M, K, N, resolve_nmod(n_moduli)).total;
 }
 
 // ------------------------------------------------------------------------------------------
@@ -172,11 +179,12 @@ constexpr unsigned long long INF_BITS = 0x7FF0000000000000ull;
 
 // Row max of |A| as the bits of a non-negative double (NaN/Inf compare above all finite) and
 // row sums of squares (for the Cauchy-Schwarz bound of the integer product).
-__global__ void k_row_absmax(const double* __restrict__ A, long lda, int n, int k, int kchunk,
-                             unsigned long long* __restrict__ amax_bits, double* __restrict__ asq) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void row_absmax_blk(const double* __restrict__ A, long lda, int n, int k, int kchunk,
+                                               unsigned long long* __restrict__ amax_bits,
+                                               double* __restrict__ asq, int bx, int by) {
+  int i = bx * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  int k0 = blockIdx.y * kchunk, k1 = min(k, k0 + kchunk);
+  int k0 = by * kchunk, k1 = min(k, k0 + kchunk);
   unsigned long long mb = 0;
   double sq = 0.0;
   for (int kk = k0; kk < k1; ++kk) {
@@ -189,38 +197,44 @@ __global__ void k_row_absmax(const double* __restrict__ A, long lda, int n, int 
   if (sq != 0.0) atomicAdd(asq + i, sq);
 }
 
+__global__ void k_row_absmax(const double* __restrict__ A, long lda, int n, int k, int kchunk,
+                             unsigned long long* __restrict__ amax_bits, double* __restrict__ asq) {
+  row_absmax_blk(A, lda, n, k, kchunk, amax_bits, asq, blockIdx.x, blockIdx.y);
+}
+
 // H pass 1: Ht[j][kk] = H(kk, j) in FP64, column max |H| and column sum |H|, and the global
 // ratio rho = max_j sum/max over finite columns.  One block per column j.
 template <int KIND>
-__global__ void k_h_pass1(const double* __restrict__ gen, long ldgen, int k, int kp, double* __restrict__ Ht,
-                          unsigned long long* __restrict__ hmax_bits, double* __restrict__ hsum,
-                          double* __restrict__ hsq, SplitDevParams* prm) {
-  const int j = blockIdx.x;
+__device__ __forceinline__ void h_pass1_blk(const GenSpec& gs, int K, int kp, double* __restrict__ Ht,
+                                            unsigned long long* __restrict__ hmax_bits, double* __restrict__ hsum,
+                                            double* __restrict__ hsq, SplitDevParams* prm, int j) {
   double w = 0.0, v = 0.0;
   if (KIND == KIND_CAUCHY) {
-    w = __ldg(gen + ldgen + j);       // F(j)
-    v = __ldg(gen + 3 * ldgen + j);   // V(j)
+    w = __ldg(gs.Fc + j);   // F(j)
+    v = __ldg(gs.Vc + j);   // V(j)
   }
   unsigned long long mb = 0;
   double s = 0.0, s2 = 0.0;
   double* row = Ht + (long)j * kp;
   for (int kk = threadIdx.x; kk < kp; kk += blockDim.x) {
     double h = 0.0;
-    if (kk < k) {
+    if (kk < K) {
       if (KIND == KIND_CAUCHY) {
-        double d = __ldg(gen + kk), u = __ldg(gen + 2 * ldgen + kk);
+        double d = __ldg(gs.Dr + kk), u = __ldg(gs.Ur + kk);
         h = (u * v) / (d - w);        // U(i)*V(j) / (D(i)-F(j))
       } else if (KIND == KIND_TOEPLITZ) {
-        h = __ldg(gen + (k - 1) + j - kk);
+        h = __ldg(gs.g + (gs.order - 1) + j - kk);
       } else if (KIND == KIND_HANKEL) {
-        h = __ldg(gen + kk + j);
+        h = __ldg(gs.g + kk + j);
+      } else if (KIND == KIND_DENSE) {
+        h = __ldg(gs.B + kk + (long)j * gs.ldb);
       } else {
-        // DFT embedding F' = [[Re F, Im F], [-Im F, Re F]] of order k = 2n; gen is the table
+        // DFT embedding F' = [[Re F, Im F], [-Im F, Re F]] of order K = 2n; the table holds
         // w^t = (cos, -sin)(2 pi t / n), indexed by the exact (r c) mod n.
-        const int nn = k >> 1;
+        const int nn = gs.n_dft;
         const bool rb = kk >= nn, cb = j >= nn;
         const long rr = rb ? kk - nn : kk, cc2 = cb ? j - nn : j;
-        const double2 wv = __ldg((const double2*)gen + (rr * cc2) % nn);
+        const double2 wv = __ldg(gs.wtab + (rr * cc2) % nn);
         h = (rb == cb) ? wv.x : (rb ? -wv.y : wv.y);
       }
     }
@@ -264,6 +278,13 @@ __global__ void k_h_pass1(const double* __restrict__ gen, long ldgen, int k, int
   }
 }
 
+template <int KIND>
+__global__ void k_h_pass1(GenSpec gs, int K, int kp, double* __restrict__ Ht,
+                          unsigned long long* __restrict__ hmax_bits, double* __restrict__ hsum,
+                          double* __restrict__ hsq, SplitDevParams* prm) {
+  h_pass1_blk<KIND>(gs, K, kp, Ht, hmax_bits, hsum, hsq, prm, blockIdx.x);
+}
+
 // Bits PA (rows of A) and PH (columns of H).  The integer product must satisfy
 // |Z_ij| <= M/16 for the CRT, with M = prod m_l.  Two rigorous bounds of |Z_ij| =
 // |sum_k A'_ik H'_kj| for |A'| <= 2^PA, |H'| <= 2^PH (rounding adds at most 1/2 per entry):
@@ -273,11 +294,13 @@ __global__ void k_h_pass1(const double* __restrict__ gen, long ldgen, int k, int
 // The budget PA + PH comes from the smaller bound.  It is split to balance the two rounding
 // errors, ~2^-PA * c_A and ~2^-PH * c_H with c_A ~ rms_i(max|A_i:|)/rms(A),
 // c_H ~ rms_j(max|H_:j|)/rms(H) (same constant factor): PH - PA = round(log2(c_H/c_A)).
-__global__ void k_split_params(SplitDevParams* prm, double log2M, int n, int k,
-                               const unsigned long long* __restrict__ amax_bits, const double* __restrict__ asq,
-                               const unsigned long long* __restrict__ hmax_bits, const double* __restrict__ hsq) {
+__device__ __forceinline__ void split_params_blk(SplitDevParams* prm, double log2M, int n, int ncols, int k,
+                                                 const unsigned long long* __restrict__ amax_bits,
+                                                 const double* __restrict__ asq,
+                                                 const unsigned long long* __restrict__ hmax_bits,
+                                                 const double* __restrict__ hsq) {
   double ra = 0.0, amx2 = 0.0, afro = 0.0, rh = 0.0, hmx2 = 0.0, hfro = 0.0;
-  const double rk = sqrt((double)k);
+  const double rk = sqrt((double)k);  // k: inner length (rows of H, columns of A)
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     const unsigned long long b = amax_bits[i];
     if (b == 0 || b >= INF_BITS) continue;
@@ -286,7 +309,7 @@ __global__ void k_split_params(SplitDevParams* prm, double log2M, int n, int k,
     ra = fmax(ra, safe ? sqrt(q) / m : rk);
     if (safe) { amx2 += m * m; afro += q; }
   }
-  for (int j = threadIdx.x; j < k; j += blockDim.x) {
+  for (int j = threadIdx.x; j < ncols; j += blockDim.x) {
     const unsigned long long b = hmax_bits[j];
     if (b == 0 || b >= INF_BITS) continue;
     const double m = __longlong_as_double((long long)b), q = hsq[j];
@@ -331,6 +354,12 @@ __global__ void k_split_params(SplitDevParams* prm, double log2M, int n, int k,
     prm->PA = max(8, min(53, PA));
     prm->PH = max(8, min(53, PH));
   }
+}
+
+__global__ void k_split_params(SplitDevParams* prm, double log2M, int n, int ncols, int k,
+                               const unsigned long long* __restrict__ amax_bits, const double* __restrict__ asq,
+                               const unsigned long long* __restrict__ hmax_bits, const double* __restrict__ hsq) {
+  split_params_blk(prm, log2M, n, ncols, k, amax_bits, asq, hmax_bits, hsq);
 }
 
 // Exponent s such that |x * 2^s| < 2^P for all |x| <= amax (amax finite, > 0).
@@ -398,11 +427,12 @@ __device__ __forceinline__ void write_residue_pair(unsigned long long u0, bool n
 }
 
 // RA[l][i][kk] = residues of A' (bf16), rows i, K-major.  Block: 32 rows x 64 k.
-__global__ void k_residues_A(const double* __restrict__ A, long lda, int n, int k, int kp,
-                             const unsigned long long* __restrict__ amax_bits, const SplitDevParams* prm,
-                             CrtConsts cc, __nv_bfloat16* __restrict__ RA) {
+__device__ __forceinline__ void residues_A_blk(const double* __restrict__ A, long lda, int n, int k, int kp,
+                                               const unsigned long long* __restrict__ amax_bits,
+                                               const SplitDevParams* prm, const CrtConsts& cc,
+                                               __nv_bfloat16* __restrict__ RA, int bx, int by) {
   __shared__ double tile[64][33];
-  const int i0 = blockIdx.y * 32, k0 = blockIdx.x * 64;
+  const int i0 = by * 32, k0 = bx * 64;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 256 threads: 8 x 32
   for (int kk = ty; kk < 64; kk += 8) {
     int gi = i0 + tx, gk = k0 + kk;
@@ -426,12 +456,19 @@ __global__ void k_residues_A(const double* __restrict__ A, long lda, int n, int 
   }
 }
 
+__global__ void k_residues_A(const double* __restrict__ A, long lda, int n, int k, int kp,
+                             const unsigned long long* __restrict__ amax_bits, const SplitDevParams* prm,
+                             CrtConsts cc, __nv_bfloat16* __restrict__ RA) {
+  residues_A_blk(A, lda, n, k, kp, amax_bits, prm, cc, RA, blockIdx.x, blockIdx.y);
+}
+
 // RH[l][j][kk] = residues of H' (bf16) from Ht[j][kk]; one thread per 2 consecutive kk.
-__global__ void k_residues_H(const double* __restrict__ Ht, int k, int kp,
-                             const unsigned long long* __restrict__ hmax_bits, const SplitDevParams* prm,
-                             CrtConsts cc, __nv_bfloat16* __restrict__ RH) {
-  const int j = blockIdx.y;
-  const int kk = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+__device__ __forceinline__ void residues_H_blk(const double* __restrict__ Ht, int ncols, int kp,
+                                               const unsigned long long* __restrict__ hmax_bits,
+                                               const SplitDevParams* prm, const CrtConsts& cc,
+                                               __nv_bfloat16* __restrict__ RH, int bx, int by) {
+  const int j = by;
+  const int kk = 2 * (bx * blockDim.x + threadIdx.x);
   if (kk >= kp) return;
   const int P = prm->PH;
   unsigned long long hb = hmax_bits[j];
@@ -441,9 +478,15 @@ __global__ void k_residues_H(const double* __restrict__ Ht, int k, int kp,
   bool n0 = false, n1 = false;
   unsigned long long u0 = ok ? scaled_int(h.x, e, &n0) : 0ull;
   unsigned long long u1 = ok ? scaled_int(h.y, e, &n1) : 0ull;
-  const size_t plane = (size_t)k * kp;
+  const size_t plane = (size_t)ncols * kp;
   uint32_t* dst = (uint32_t*)(RH + (size_t)j * kp + kk);
   write_residue_pair(u0, n0, u1, n1, cc, dst, plane / 2);
+}
+
+__global__ void k_residues_H(const double* __restrict__ Ht, int ncols, int kp,
+                             const unsigned long long* __restrict__ hmax_bits, const SplitDevParams* prm,
+                             CrtConsts cc, __nv_bfloat16* __restrict__ RH) {
+  residues_H_blk(Ht, ncols, kp, hmax_bits, prm, cc, RH, blockIdx.x, blockIdx.y);
 }
 
 // DFT A side: row i of the embedded operand X' = [Re B^T | Im B^T] is column i of B, read
@@ -517,11 +560,9 @@ constexpr int G_CHUNK_KB = 8;  // 8 x 64 = 512 k per exact FP32 chunk: |sum| <= 
 constexpr int G_EPI_WARPS = 8;
 constexpr int G_THREADS = (G_EPI_WARPS + 2) * 32;
 constexpr uint32_t G_A_BYTES = G_BM * G_BK * 2;
-constexpr uint32_t G_B_BYTES = G_BN * G_BK * 2;
-constexpr size_t G_SMEM = 1024 + (size_t)G_STAGES * (G_A_BYTES + G_B_BYTES) + 256;
 
 struct GemmArgs {
-  int n, kr, nkb, tiles_m, tiles_n, group_m, nmod;
+  int n, kr, nkb, tiles_m, tiles_n, group_m, nmod;  // (a grouped launch uses group_m, nmod)
   int8_t* R;
   unsigned* status;
   int m[SPL_MAX_MODULI];
@@ -530,29 +571,102 @@ struct GemmArgs {
 
 // Tile t of the launch -> (modulus, row tile, column tile).  Moduli are outermost; inside a
 // modulus group_m row tiles sweep all column tiles together (L2 reuse of both operands).
-__device__ __forceinline__ void gemm_tile(const GemmArgs& g, int t, int& l, int& tm, int& tn) {
-  const int per_mod = g.tiles_m * g.tiles_n;
+__device__ __forceinline__ void raster_tile(int tiles_m, int tiles_n, int group_m, int t, int& l, int& tm, int& tn) {
+  const int per_mod = tiles_m * tiles_n;
   l = t / per_mod;
   const int b = t - l * per_mod;
-  const int per_group = g.group_m * g.tiles_n;
+  const int per_group = group_m * tiles_n;
   const int grp = b / per_group;
-  const int first_m = grp * g.group_m;
-  const int gm = min(g.group_m, g.tiles_m - first_m);
+  const int first_m = grp * group_m;
+  const int gm = min(group_m, tiles_m - first_m);
   const int rr = b - grp * per_group;
   tm = first_m + rr % gm;
   tn = rr / gm;
 }
 
+// One output tile of a launch: operands, destination and position.
+struct TileInfo {
+  const CUtensorMap* ta;
+  const CUtensorMap* tb;
+  int8_t* R;
+  int n, kr, nkb, l, tm, tn;
+};
+
+// Tile source of a single product (tensor maps in parameter space).
+struct OneGemm {
+  CUtensorMap ta, tb;
+  GemmArgs g;
+  static constexpr bool kGlobalMaps = false;
+  __device__ int total() const { return g.tiles_m * g.tiles_n * g.nmod; }
+  __device__ TileInfo tile(int t) const {
+    TileInfo ti;
+    raster_tile(g.tiles_m, g.tiles_n, g.group_m, t, ti.l, ti.tm, ti.tn);
+    ti.ta = &ta;
+    ti.tb = &tb;
+    ti.R = g.R;
+    ti.n = g.n;
+    ti.kr = g.kr;
+    ti.nkb = g.nkb;
+    return ti;
+  }
+};
+
+// One product of a grouped launch; tiles [t0, t0 + tiles_m * tiles_n * nmod).
+struct GemmDesc {
+  CUtensorMap ta, tb;
+  int8_t* R;
+  int n, kr, nkb, tiles_m, tiles_n, t0;
+};
+
+// Tile source of a grouped launch: the products' descriptors (and tensor maps) in global memory.
+struct GroupGemm {
+  GemmArgs g;  // nmod, group_m, status, moduli
+  const GemmDesc* d;
+  int count, total_tiles;
+  static constexpr bool kGlobalMaps = true;
+  __device__ int total() const { return total_tiles; }
+  __device__ TileInfo tile(int t) const {
+    int lo = 0, hi = count - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (d[mid].t0 <= t) lo = mid; else hi = mid - 1;
+    }
+    const GemmDesc& e = d[lo];
+    TileInfo ti;
+    raster_tile(e.tiles_m, e.tiles_n, g.group_m, t - e.t0, ti.l, ti.tm, ti.tn);
+    ti.ta = &e.ta;
+    ti.tb = &e.tb;
+    ti.R = e.R;
+    ti.n = e.n;
+    ti.kr = e.kr;
+    ti.nkb = e.nkb;
+    return ti;
+  }
+};
+
+template <int BN>
+struct GemmShape {
+  static constexpr uint32_t B_BYTES = BN * G_BK * 2;
+  static constexpr size_t SMEM = 1024 + (size_t)G_STAGES * (G_A_BYTES + B_BYTES) + 256;
+  static constexpr uint32_t TMEM_COLS = 2 * BN;  // two accumulators (a power of two >= 32)
+};
+
+__device__ __forceinline__ void tensormap_acquire(const CUtensorMap* m) {
+  asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;\n" ::"l"(m) : "memory");
+}
+
 // Persistent: one CTA per SM walks tiles t = blockIdx.x, blockIdx.x + gridDim.x, ...  The
-// stage ring and the two TMEM accumulators continue across tiles, so the loads and MMAs of
-// the next tile overlap the drain and residue store of the previous one.
-__global__ void __launch_bounds__(G_THREADS, 1)
-    k_crt_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, GemmArgs g) {
+// stage ring and the two TMEM accumulators continue across tiles (and, in a grouped launch,
+// across products), so the loads and MMAs of the next tile overlap the drain and residue
+// store of the previous one.  BN: output tile width (256, or 64 for narrow products).
+template <int BN, class TS>
+__global__ void __launch_bounds__(G_THREADS, 1) k_crt_gemm(const __grid_constant__ TS ts) {
+  using S = GemmShape<BN>;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint8_t* sA = base;
   uint8_t* sB = base + G_STAGES * G_A_BYTES;
-  uint64_t* bars = (uint64_t*)(sB + G_STAGES * G_B_BYTES);
+  uint64_t* bars = (uint64_t*)(sB + G_STAGES * S::B_BYTES);
   uint64_t* full = bars;
   uint64_t* empty = bars + G_STAGES;
   uint64_t* acc_full = bars + 2 * G_STAGES;
@@ -560,6 +674,7 @@ __global__ void __launch_bounds__(G_THREADS, 1)
   uint64_t* mma_done = acc_empty + 2;
   uint32_t* tmem_slot = (uint32_t*)(mma_done + 1);
   volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
+  const GemmArgs& g = ts.g;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
@@ -578,33 +693,38 @@ __global__ void __launch_bounds__(G_THREADS, 1)
     fence_barrier_init();
   }
   if (warp == 0) {
-    tmem_alloc(tmem_slot, 512);
+    tmem_alloc(tmem_slot, S::TMEM_COLS);
     tmem_relinquish();
   }
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem_base = *tmem_slot;
-  const int nkb = g.nkb;
-  const int cpt = (nkb + G_CHUNK_KB - 1) / G_CHUNK_KB;  // chunks per tile
-  const int total = *abort_flag ? 0 : g.tiles_m * g.tiles_n * g.nmod;
+  const int total = *abort_flag ? 0 : ts.total();
 
   if (warp == G_EPI_WARPS) {
     // ---------------- TMA producer ----------------
     if (lane == 0) {
-      prefetch_tmap(&tmA);
-      prefetch_tmap(&tmB);
       int it = 0, issued = 0;
       bool ok = true;
+      const CUtensorMap* last = nullptr;
       for (int t = blockIdx.x; t < total && ok; t += gridDim.x) {
-        int l, tm, tn;
-        gemm_tile(g, t, l, tm, tn);
-        for (int kb = 0; kb < nkb; ++kb, ++it) {
+        const TileInfo ti = ts.tile(t);
+        if (ti.ta != last) {
+          if (TS::kGlobalMaps) {
+            tensormap_acquire(ti.ta);
+            tensormap_acquire(ti.tb);
+          }
+          prefetch_tmap(ti.ta);
+          prefetch_tmap(ti.tb);
+          last = ti.ta;
+        }
+        for (int kb = 0; kb < ti.nkb; ++kb, ++it) {
           const int s = it % G_STAGES;
           if (!mbar_wait(&empty[s], ((it / G_STAGES) & 1) ^ 1, g.status, abort_flag)) { ok = false; break; }
-          mbar_arrive_expect_tx(&full[s], G_A_BYTES + G_B_BYTES);
-          tma_load_3d(sA + s * G_A_BYTES, &tmA, &full[s], kb * G_BK, tm * G_BM, l);
-          tma_load_3d(sB + s * G_B_BYTES, &tmB, &full[s], kb * G_BK, tn * G_BN, l);
+          mbar_arrive_expect_tx(&full[s], G_A_BYTES + S::B_BYTES);
+          tma_load_3d(sA + s * G_A_BYTES, ti.ta, &full[s], kb * G_BK, ti.tm * G_BM, ti.l);
+          tma_load_3d(sB + s * S::B_BYTES, ti.tb, &full[s], kb * G_BK, ti.tn * BN, ti.l);
           issued = it + 1;
         }
       }
@@ -616,23 +736,25 @@ __global__ void __launch_bounds__(G_THREADS, 1)
   } else if (warp == G_EPI_WARPS + 1) {
     // ---------------- MMA issuer ----------------
     if (lane == 0) {
-      const uint32_t idesc = idesc_bf16_f32(G_BM, G_BN);
+      const uint32_t idesc = idesc_bf16_f32(G_BM, BN);
       int it = 0, c = 0;
       bool ok = true;
       for (int t = blockIdx.x; t < total && ok; t += gridDim.x) {
+        const int nkb = ts.tile(t).nkb;
+        const int cpt = (nkb + G_CHUNK_KB - 1) / G_CHUNK_KB;  // chunks of this tile
         for (int cc = 0; cc < cpt && ok; ++cc, ++c) {
           const int buf = c & 1;
           const uint32_t use = (uint32_t)(c >> 1);
           if (!mbar_wait(&acc_empty[buf], (use & 1) ^ 1, g.status, abort_flag)) { ok = false; break; }
           tc_fence_after();
-          const uint32_t dt = tmem_base + (uint32_t)(buf * G_BN);
+          const uint32_t dt = tmem_base + (uint32_t)(buf * BN);
           const int kend = min(nkb, (cc + 1) * G_CHUNK_KB);
           uint32_t acc = 0;
           for (int kb = cc * G_CHUNK_KB; kb < kend; ++kb, ++it) {
             const int s = it % G_STAGES;
             if (!mbar_wait(&full[s], (it / G_STAGES) & 1, g.status, abort_flag)) { ok = false; break; }
             tc_fence_after();
-            const uint32_t a0 = smem_u32(sA + s * G_A_BYTES), b0 = smem_u32(sB + s * G_B_BYTES);
+            const uint32_t a0 = smem_u32(sA + s * G_A_BYTES), b0 = smem_u32(sB + s * S::B_BYTES);
 #pragma unroll
             for (int kk = 0; kk < G_BK / 16; ++kk) {
               tc_mma_bf16(dt, sdesc_sw128_kmajor(a0 + kk * 32), sdesc_sw128_kmajor(b0 + kk * 32), idesc, acc);
@@ -650,25 +772,26 @@ __global__ void __launch_bounds__(G_THREADS, 1)
     __syncwarp();
   } else {
     // ---------------- accumulator drain (epilogue) ----------------
+    constexpr int HALF = BN / 2;  // columns per epilogue warp
     const int q = warp & 3, h = warp >> 2;
     int c = 0;
     bool ok = true;
     for (int t = blockIdx.x; t < total && ok; t += gridDim.x) {
-      int l, tm, tn;
-      gemm_tile(g, t, l, tm, tn);
-      const float m = (float)g.m[l], inv_m = g.inv_m[l];
-      float res[128];
+      const TileInfo ti = ts.tile(t);
+      const int cpt = (ti.nkb + G_CHUNK_KB - 1) / G_CHUNK_KB;
+      const float m = (float)g.m[ti.l], inv_m = g.inv_m[ti.l];
+      float res[HALF];
 #pragma unroll
-      for (int e = 0; e < 128; ++e) res[e] = 0.0f;
+      for (int e = 0; e < HALF; ++e) res[e] = 0.0f;
       for (int cc = 0; cc < cpt; ++cc, ++c) {
         const int buf = c & 1;
         const uint32_t use = (uint32_t)(c >> 1);
         if (!mbar_wait(&acc_full[buf], use & 1, g.status, abort_flag)) { ok = false; break; }
         tc_fence_after();
 #pragma unroll
-        for (int cb = 0; cb < 4; ++cb) {
+        for (int cb = 0; cb < HALF / 32; ++cb) {
           uint32_t r[32];
-          tmem_ld32(tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * G_BN + h * 128 + cb * 32), r);
+          tmem_ld32(tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * BN + h * HALF + cb * 32), r);
           tmem_ld_wait();
 #pragma unroll
           for (int e = 0; e < 32; ++e) {
@@ -683,11 +806,11 @@ __global__ void __launch_bounds__(G_THREADS, 1)
         tc_fence_before();
         mbar_arrive(&acc_empty[buf]);
       }
-      const int i = tm * G_BM + q * 32 + lane;
-      if (ok && !*abort_flag && i < g.n) {
-        int8_t* dst = g.R + ((size_t)l * g.n + i) * g.kr + (size_t)tn * G_BN + h * 128;
+      const int i = ti.tm * G_BM + q * 32 + lane;
+      if (ok && !*abort_flag && i < ti.n) {
+        int8_t* dst = ti.R + ((size_t)ti.l * ti.n + i) * ti.kr + (size_t)ti.tn * BN + h * HALF;
 #pragma unroll
-        for (int v = 0; v < 8; ++v) {
+        for (int v = 0; v < HALF / 16; ++v) {
           uint32_t w[4];
 #pragma unroll
           for (int t4 = 0; t4 < 4; ++t4) {
@@ -705,7 +828,7 @@ __global__ void __launch_bounds__(G_THREADS, 1)
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
-  if (warp == 0) tmem_dealloc(tmem_base, 512);
+  if (warp == 0) tmem_dealloc(tmem_base, S::TMEM_COLS);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -762,14 +885,14 @@ constexpr int CRT_TI = 32, CRT_TJ = 128;
 // DFT_OUT: the product is [Re C^T | Im C^T] (rows = columns of C); element (i, j) goes to the
 // interleaved complex C at 2*(j mod nn) + (j >= nn) + i*ldq (ldq in doubles).
 template <bool DFT_OUT>
-__global__ void __launch_bounds__(256) k_crt_combine(const int8_t* __restrict__ R, int n, int k, int kr,
-                                                     CrtConsts cc, const unsigned long long* __restrict__ amax_bits,
-                                                     const unsigned long long* __restrict__ hmax_bits,
-                                                     const SplitDevParams* prm, double alpha, double beta,
-                                                     double* __restrict__ Q, long ldq) {
+__device__ __forceinline__ void crt_combine_blk(const int8_t* __restrict__ R, int n, int k, int kr,
+                                                const CrtConsts& cc, const unsigned long long* __restrict__ amax_bits,
+                                                const unsigned long long* __restrict__ hmax_bits,
+                                                const SplitDevParams* prm, double alpha, double beta,
+                                                double* __restrict__ Q, long ldq, int bx, int by) {
   __shared__ double tile[CRT_TJ][CRT_TI + 1];
   const int tx = threadIdx.x, ty = threadIdx.y;
-  const int i0 = blockIdx.y * CRT_TI, j0 = blockIdx.x * CRT_TJ;
+  const int i0 = by * CRT_TI, j0 = bx * CRT_TJ;
   const int PA = prm->PA, PH = prm->PH;
   const int jb = j0 + 4 * tx;
   unsigned long long hb[4];
@@ -873,6 +996,15 @@ __global__ void __launch_bounds__(256) k_crt_combine(const int8_t* __restrict__ 
   }
 }
 
+template <bool DFT_OUT>
+__global__ void __launch_bounds__(256) k_crt_combine(const int8_t* __restrict__ R, int n, int k, int kr,
+                                                     CrtConsts cc, const unsigned long long* __restrict__ amax_bits,
+                                                     const unsigned long long* __restrict__ hmax_bits,
+                                                     const SplitDevParams* prm, double alpha, double beta,
+                                                     double* __restrict__ Q, long ldq) {
+  crt_combine_blk<DFT_OUT>(R, n, k, kr, cc, amax_bits, hmax_bits, prm, alpha, beta, Q, ldq, blockIdx.x, blockIdx.y);
+}
+
 // ------------------------------------------------------------------------------------------
 // Host orchestration
 // ------------------------------------------------------------------------------------------
@@ -950,21 +1082,17 @@ int launch_split(int kind, int n, int k, double alpha, const double* A, long lda
                           nullptr);
 }
 
-// kind != DFT: Q (n x k) = alpha * A (n x k) * H (k x k) + beta * Q.
-// kind == DFT: C (n x k complex, ldq) = alpha * F (n x n) * B (n x k complex, lda) + beta * C,
-//   computed as [Re C^T | Im C^T] = [Re B^T | Im B^T] * [[Re F, Im F], [-Im F, Re F]].
-// With status_dev_out the call does not synchronise: the timeout flag is copied to that
-// device word at the end of the stream's work; otherwise it synchronises and returns it.
-int launch_split_any(int kind, int n, int k, double alpha, const double* A, long lda, const double* gen,
-                     long ldgen, double beta, double* Q, long ldq, int n_moduli, void* work, size_t lwork,
-                     cudaStream_t stream, unsigned* status_dev_out) {
-  const int nmod = resolve_nmod(n_moduli);
+// Core of the split path: Q (M x N) = alpha * A' (M x K) * H (K x N) + beta * Q where A' is
+// A (column-major, lda) or, for the DFT, the embedding [Re B^T | Im B^T] of B (complex, lda),
+// H is generated from gs, and the output is column-major Q (ldq) or, for the DFT, the
+// interleaved complex C (ldq).  With status_dev_out it does not synchronise.
+static int split_core(int M, int N, int K, double alpha, const double* A, long lda, const GenSpec& gs, double beta,
+                      double* Q, long ldq, int nmod, void* work, size_t lwork, cudaStream_t stream,
+                      unsigned* status_dev_out) {
+  const bool dft = gs.kind == KIND_DFT;
   if (nmod < 8 || nmod > SPL_MAX_MODULI) return PSMMA_EUNSUPPORTED;
-  const bool dft = kind == KIND_DFT;
-  const int M = dft ? k : n;      // rows of the product
-  const int K = dft ? 2 * n : k;  // order of the structured operand
-  if (K >= (1 << 24) || M >= (1 << 30)) return PSMMA_EUNSUPPORTED;
-  SplitLayout L = split_layout(M, K, nmod);
+  if (K >= (1 << 24) || M >= (1 << 30) || N >= (1 << 30)) return PSMMA_EUNSUPPORTED;
+  SplitLayout L = split_layout(M, K, N, nmod);
   if (lwork < L.total || !work) return PSMMA_EWORKSPACE;
   char* w = (char*)work;
   const SplitBuffers b = split_buffers(w, L);
@@ -979,63 +1107,68 @@ int launch_split_any(int kind, int n, int k, double alpha, const double* A, long
     dim3 g1((M + 127) / 128, (K + kchunk - 1) / kchunk);
     k_row_absmax<<<g1, 128, 0, stream>>>(A, lda, M, K, kchunk, b.amax, b.asq);
   } else {
-    k_row_absmax_dft<<<M, 256, 0, stream>>>(A, 2 * lda, n, b.amax, b.asq);
+    k_row_absmax_dft<<<M, 256, 0, stream>>>(A, 2 * lda, gs.n_dft, b.amax, b.asq);
   }
   prof_mark(stream, "row_scale");
   // ---- H side: generate, column maxima / sums / norms
-  switch (kind) {
-    case KIND_CAUCHY: k_h_pass1<KIND_CAUCHY><<<K, 256, 0, stream>>>(gen, ldgen, K, L.kp, b.Ht, b.hmax, b.hsum, b.hsq, b.prm); break;
-    case KIND_TOEPLITZ: k_h_pass1<KIND_TOEPLITZ><<<K, 256, 0, stream>>>(gen, ldgen, K, L.kp, b.Ht, b.hmax, b.hsum, b.hsq, b.prm); break;
-    case KIND_HANKEL: k_h_pass1<KIND_HANKEL><<<K, 256, 0, stream>>>(gen, ldgen, K, L.kp, b.Ht, b.hmax, b.hsum, b.hsq, b.prm); break;
+  switch (gs.kind) {
+    case KIND_CAUCHY: k_h_pass1<KIND_CAUCHY><<<N, 256, 0, stream>>>(gs, K, L.kp, b.Ht, b.hmax, b.hsum, b.hsq, b.prm); break;
+    case KIND_TOEPLITZ: k_h_pass1<KIND_TOEPLITZ><<<N, 256, 0, stream>>>(gs, K, L.kp, b.Ht, b.hmax, b.hsum, b.hsq, b.prm); break;
+    case KIND_HANKEL: k_h_pass1<KIND_HANKEL><<<N, 256, 0, stream>>>(gs, K, L.kp, b.Ht, b.hmax, b.hsum, b.hsq, b.prm); break;
+    case KIND_DENSE: k_h_pass1<KIND_DENSE><<<N, 256, 0, stream>>>(gs, K, L.kp, b.Ht, b.hmax, b.hsum, b.hsq, b.prm); break;
     case KIND_DFT: {
-      int st = launch_dft_table(b.wtab, n, stream);
+      int st = launch_dft_table(b.wtab, gs.n_dft, stream);
       if (st) return st;
-      k_h_pass1<KIND_DFT><<<K, 256, 0, stream>>>((const double*)b.wtab, 0, K, L.kp, b.Ht, b.hmax, b.hsum, b.hsq, b.prm);
+      GenSpec g2 = gs;
+      g2.wtab = b.wtab;
+      k_h_pass1<KIND_DFT><<<N, 256, 0, stream>>>(g2, K, L.kp, b.Ht, b.hmax, b.hsum, b.hsq, b.prm);
       break;
     }
     default: return PSMMA_EUNSUPPORTED;
   }
   prof_mark(stream, "h_generate");
-  k_split_params<<<1, 1024, 0, stream>>>(b.prm, cc.log2M, M, K, b.amax, b.asq, b.hmax, b.hsq);
+  k_split_params<<<1, 1024, 0, stream>>>(b.prm, cc.log2M, M, N, K, b.amax, b.asq, b.hmax, b.hsq);
   prof_mark(stream, "params");
   if (!dft)
     k_residues_A<<<dim3(L.kp / 64, (M + 31) / 32), 256, 0, stream>>>(A, lda, M, K, L.kp, b.amax, b.prm, cc, b.RA);
   else
-    k_residues_A_dft<<<dim3((L.kp / 2 + 127) / 128, M), 128, 0, stream>>>(A, 2 * lda, n, L.kp, b.amax, b.prm, cc,
-                                                                           b.RA, M);
+    k_residues_A_dft<<<dim3((L.kp / 2 + 127) / 128, M), 128, 0, stream>>>(A, 2 * lda, gs.n_dft, L.kp, b.amax,
+                                                                           b.prm, cc, b.RA, M);
   prof_mark(stream, "residues_A");
-  k_residues_H<<<dim3((L.kp / 2 + 127) / 128, K), 128, 0, stream>>>(b.Ht, K, L.kp, b.hmax, b.prm, cc, b.RH);
+  k_residues_H<<<dim3((L.kp / 2 + 127) / 128, N), 128, 0, stream>>>(b.Ht, N, L.kp, b.hmax, b.prm, cc, b.RH);
   prof_mark(stream, "residues_H");
 
-  CUtensorMap tmA, tmB;
-  if (!make_tmap(&tmA, b.RA, L.kp, M, nmod, G_BM) || !make_tmap(&tmB, b.RH, L.kp, K, nmod, G_BN))
+  OneGemm og;
+  memset(&og, 0, sizeof(og));
+  if (!make_tmap(&og.ta, b.RA, L.kp, M, nmod, G_BM) || !make_tmap(&og.tb, b.RH, L.kp, N, nmod, G_BN))
     return PSMMA_EDEVICE;
-  GemmArgs ga;
-  memset(&ga, 0, sizeof(ga));
+  GemmArgs& ga = og.g;
   ga.n = M;
   ga.kr = L.kr;
   ga.nkb = L.kp / G_BK;
   ga.tiles_m = (M + G_BM - 1) / G_BM;
-  ga.tiles_n = (K + G_BN - 1) / G_BN;
+  ga.tiles_n = (N + G_BN - 1) / G_BN;
   ga.group_m = 12;
   ga.R = b.R;
   ga.status = &b.prm->status;
   for (int l = 0; l < nmod; ++l) { ga.m[l] = cc.m[l]; ga.inv_m[l] = cc.inv_m[l]; }
-  if (cudaFuncSetAttribute(k_crt_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G_SMEM) != cudaSuccess)
+  using Shape = GemmShape<G_BN>;
+  if (cudaFuncSetAttribute(k_crt_gemm<G_BN, OneGemm>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)Shape::SMEM) != cudaSuccess)
     return PSMMA_EDEVICE;
   int dev = 0, sms = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
     return PSMMA_EDEVICE;
   ga.nmod = nmod;
   const int total_tiles = ga.tiles_m * ga.tiles_n * nmod;
-  k_crt_gemm<<<std::min(sms, total_tiles), G_THREADS, G_SMEM, stream>>>(tmA, tmB, ga);
+  k_crt_gemm<G_BN, OneGemm><<<std::min(sms, total_tiles), G_THREADS, Shape::SMEM, stream>>>(og);
   prof_mark(stream, "modular_gemm");
 
-  dim3 gc((K + CRT_TJ - 1) / CRT_TJ, (M + CRT_TI - 1) / CRT_TI);
+  dim3 gc((N + CRT_TJ - 1) / CRT_TJ, (M + CRT_TI - 1) / CRT_TI);
   if (!dft)
-    k_crt_combine<false><<<gc, dim3(32, 8), 0, stream>>>(b.R, M, K, L.kr, cc, b.amax, b.hmax, b.prm, alpha, beta, Q, ldq);
+    k_crt_combine<false><<<gc, dim3(32, 8), 0, stream>>>(b.R, M, N, L.kr, cc, b.amax, b.hmax, b.prm, alpha, beta, Q, ldq);
   else
-    k_crt_combine<true><<<gc, dim3(32, 8), 0, stream>>>(b.R, M, K, L.kr, cc, b.amax, b.hmax, b.prm, alpha, beta, Q,
+    k_crt_combine<true><<<gc, dim3(32, 8), 0, stream>>>(b.R, M, N, L.kr, cc, b.amax, b.hmax, b.prm, alpha, beta, Q,
                                                         2 * ldq);
   prof_mark(stream, "crt_combine");
   if (cudaGetLastError() != cudaSuccess) return PSMMA_EDEVICE;
@@ -1051,6 +1184,304 @@ int launch_split_any(int kind, int n, int k, double alpha, const double* A, long
       cudaStreamSynchronize(stream) != cudaSuccess)
     return PSMMA_EDEVICE;
   if (st & DEV_ERR_TIMEOUT) return PSMMA_ETIMEDOUT;
+  return PSMMA_OK;
+}
+
+// kind != DFT: Q (n x k) = alpha * A (n x k) * H (k x k) + beta * Q.
+// kind == DFT: C (n x k complex, ldq) = alpha * F (n x n) * B (n x k complex, lda) + beta * C,
+//   computed as [Re C^T | Im C^T] = [Re B^T | Im B^T] * [[Re F, Im F], [-Im F, Re F]].
+int launch_split_any(int kind, int n, int k, double alpha, const double* A, long lda, const double* gen,
+                     long ldgen, double beta, double* Q, long ldq, int n_moduli, void* work, size_t lwork,
+                     cudaStream_t stream, unsigned* status_dev_out) {
+  const int nmod = resolve_nmod(n_moduli);
+  if (kind == KIND_DFT) {
+    GenSpec gs;
+    gs.kind = KIND_DFT;
+    gs.n_dft = n;
+    return split_core(k, 2 * n, 2 * n, alpha, A, lda, gs, beta, Q, ldq, nmod, work, lwork, stream, status_dev_out);
+  }
+  const GenSpec gs = reference_gens(kind, gen, ldgen, k);
+  return split_core(n, k, k, alpha, A, lda, gs, beta, Q, ldq, nmod, work, lwork, stream, status_dev_out);
+}
+
+int launch_split_general(int M, int N, int K, double alpha, const double* A, long lda, const GenSpec& gs,
+                         double beta, double* Q, long ldq, int n_moduli, void* work, size_t lwork,
+                         cudaStream_t stream, unsigned* status_dev_out) {
+  if (gs.kind == KIND_DFT) return PSMMA_EUNSUPPORTED;
+  return split_core(M, N, K, alpha, A, lda, gs, beta, Q, ldq, resolve_nmod(n_moduli), work, lwork, stream,
+                    status_dev_out);
+}
+
+
+// ------------------------------------------------------------------------------------------
+// Grouped split path: many independent products (uneven sizes) in one launch per phase --
+// one persistent modular GEMM over the tiles of all products per tile width -- for the
+// batched merge level.  Device-side descriptors are copied once (prepare); the launches
+// (enqueue) are then plain kernel launches that a stream capture can record.
+// ------------------------------------------------------------------------------------------
+struct GProb {
+  int M, N, K, kp, kr, bn;
+  double alpha, beta;
+  const double* A;
+  long lda;
+  GenSpec gs;
+  double* Q;
+  long ldq;
+  SplitDevParams* prm;
+  unsigned long long *amax, *hmax;
+  double *hsum, *asq, *hsq, *Ht;
+  __nv_bfloat16 *RA, *RH;
+  int8_t* R;
+  int b_row, b_h, b_ra, b_rh, b_crt;  // first block of this product in each grouped launch
+};
+
+// Product owning block `blk` of grouped launch W (largest first-block <= blk).
+template <int W>
+__device__ __forceinline__ int gfind(const GProb* d, int count, int blk) {
+  int lo = 0, hi = count - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    const GProb& e = d[mid];
+    const int key = W == 0 ? e.b_row : W == 1 ? e.b_h : W == 2 ? e.b_ra : W == 3 ? e.b_rh : e.b_crt;
+    if (key <= blk) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+constexpr int G_ROW_KCHUNK = 1024;
+
+__global__ void __launch_bounds__(128) k_g_row_absmax(const GProb* d, int count) {
+  const GProb& e = d[gfind<0>(d, count, blockIdx.x)];
+  const int local = blockIdx.x - e.b_row, gx = (e.M + 127) / 128;
+  row_absmax_blk(e.A, e.lda, e.M, e.K, G_ROW_KCHUNK, e.amax, e.asq, local % gx, local / gx);
+}
+
+__global__ void __launch_bounds__(256) k_g_h_pass1(const GProb* d, int count) {
+  const GProb& e = d[gfind<1>(d, count, blockIdx.x)];
+  const int j = blockIdx.x - e.b_h;
+  switch (e.gs.kind) {
+    case KIND_CAUCHY: h_pass1_blk<KIND_CAUCHY>(e.gs, e.K, e.kp, e.Ht, e.hmax, e.hsum, e.hsq, e.prm, j); break;
+    case KIND_TOEPLITZ: h_pass1_blk<KIND_TOEPLITZ>(e.gs, e.K, e.kp, e.Ht, e.hmax, e.hsum, e.hsq, e.prm, j); break;
+    case KIND_HANKEL: h_pass1_blk<KIND_HANKEL>(e.gs, e.K, e.kp, e.Ht, e.hmax, e.hsum, e.hsq, e.prm, j); break;
+    default: h_pass1_blk<KIND_DENSE>(e.gs, e.K, e.kp, e.Ht, e.hmax, e.hsum, e.hsq, e.prm, j); break;
+  }
+}
+
+__global__ void __launch_bounds__(1024) k_g_split_params(const GProb* d, double log2M) {
+  const GProb& e = d[blockIdx.x];
+  split_params_blk(e.prm, log2M, e.M, e.N, e.K, e.amax, e.asq, e.hmax, e.hsq);
+}
+
+__global__ void __launch_bounds__(256) k_g_residues_A(const GProb* d, int count, CrtConsts cc) {
+  const GProb& e = d[gfind<2>(d, count, blockIdx.x)];
+  const int local = blockIdx.x - e.b_ra, gx = e.kp / 64;
+  residues_A_blk(e.A, e.lda, e.M, e.K, e.kp, e.amax, e.prm, cc, e.RA, local % gx, local / gx);
+}
+
+__global__ void __launch_bounds__(128) k_g_residues_H(const GProb* d, int count, CrtConsts cc) {
+  const GProb& e = d[gfind<3>(d, count, blockIdx.x)];
+  const int local = blockIdx.x - e.b_rh, gx = (e.kp / 2 + 127) / 128;
+  residues_H_blk(e.Ht, e.N, e.kp, e.hmax, e.prm, cc, e.RH, local % gx, local / gx);
+}
+
+__global__ void __launch_bounds__(256) k_g_crt_combine(const GProb* d, int count, CrtConsts cc) {
+  const GProb& e = d[gfind<4>(d, count, blockIdx.x)];
+  const int local = blockIdx.x - e.b_crt, gx = (e.N + CRT_TJ - 1) / CRT_TJ;
+  crt_combine_blk<false>(e.R, e.M, e.N, e.kr, cc, e.amax, e.hmax, e.prm, e.alpha, e.beta, e.Q, e.ldq, local % gx,
+                         local / gx);
+}
+
+namespace {
+
+// Bump allocation over a workspace (base 0: measure only).
+struct WsBump {
+  uintptr_t base, off = 0;
+  explicit WsBump(void* b) : base((uintptr_t)b) {}
+  template <class T>
+  T* take(size_t count, size_t align) {
+    off = (off + align - 1) & ~(uintptr_t)(align - 1);
+    T* p = (T*)(base + off);
+    off += count * sizeof(T);
+    return p;
+  }
+};
+
+// Lays out (and, with a real base, fills) the group's descriptors and buffers.
+int plan_group(const SplitProblem* P, int count, int nmod, int narrow_max, int group_m, WsBump& w,
+               std::vector<GProb>* probs, std::vector<GemmDesc>* gd, SplitGroup* g) {
+  GProb* d_probs = w.take<GProb>(count, 256);
+  GemmDesc* d_g0 = w.take<GemmDesc>(count, 128);
+  GemmDesc* d_g1 = w.take<GemmDesc>(count, 128);
+  // small region: status word, then per product params, maxima and sums (zeroed by one memset)
+  const uintptr_t small0 = (w.off + 1023) & ~(uintptr_t)1023;
+  unsigned* status = w.take<unsigned>(256, 1024);
+  std::vector<GProb> pr(count);
+  for (int i = 0; i < count; ++i) {
+    GProb& e = pr[i];
+    const SplitProblem& q = P[i];
+    e.M = q.M; e.N = q.N; e.K = q.K;
+    e.kp = (q.K + 63) / 64 * 64;
+    e.bn = (q.N <= narrow_max) ? 64 : 256;
+    e.kr = (q.N + e.bn - 1) / e.bn * e.bn;
+    e.alpha = q.alpha; e.beta = q.beta;
+    e.A = q.A; e.lda = q.lda; e.gs = q.gs; e.Q = q.Q; e.ldq = q.ldq;
+    e.prm = w.take<SplitDevParams>(1, 256);
+    e.amax = w.take<unsigned long long>(q.M, 256);
+    e.asq = w.take<double>(q.M, 256);
+    e.hmax = w.take<unsigned long long>(q.N, 256);
+    e.hsum = w.take<double>(q.N, 256);
+    e.hsq = w.take<double>(q.N, 256);
+  }
+  const uintptr_t small1 = (w.off + 1023) & ~(uintptr_t)1023;
+  int b_row = 0, b_h = 0, b_ra = 0, b_rh = 0, b_crt = 0;
+  for (int i = 0; i < count; ++i) {
+    GProb& e = pr[i];
+    e.Ht = w.take<double>((size_t)e.N * e.kp, 1024);
+    e.RA = w.take<__nv_bfloat16>((size_t)nmod * e.M * e.kp, 1024);
+    e.RH = w.take<__nv_bfloat16>((size_t)nmod * e.N * e.kp, 1024);
+    e.R = w.take<int8_t>((size_t)nmod * e.M * e.kr, 1024);
+    e.b_row = b_row; b_row += ((e.M + 127) / 128) * ((e.K + G_ROW_KCHUNK - 1) / G_ROW_KCHUNK);
+    e.b_h = b_h;     b_h += e.N;
+    e.b_ra = b_ra;   b_ra += (e.kp / 64) * ((e.M + 31) / 32);
+    e.b_rh = b_rh;   b_rh += ((e.kp / 2 + 127) / 128) * e.N;
+    e.b_crt = b_crt; b_crt += ((e.N + CRT_TJ - 1) / CRT_TJ) * ((e.M + CRT_TI - 1) / CRT_TI);
+  }
+  g->count = count;
+  g->nmod = nmod;
+  g->group_m = group_m;
+  g->d_probs = d_probs;
+  g->d_gemm[0] = d_g0;
+  g->d_gemm[1] = d_g1;
+  g->blocks_row = b_row; g->blocks_h = b_h; g->blocks_ra = b_ra; g->blocks_rh = b_rh; g->blocks_crt = b_crt;
+  g->small = (void*)(w.base + small0);  // small0, small1 are offsets from the base
+  g->small_bytes = small1 - small0;
+  g->status = status;
+  if (!probs) return PSMMA_OK;
+  // GEMM descriptors per tile width, larger products first (their tiles start the sweep)
+  std::vector<int> order(count);
+  for (int i = 0; i < count; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    return (double)pr[a].M * pr[a].N * pr[a].K > (double)pr[b].M * pr[b].N * pr[b].K;
+  });
+  gd[0].clear();
+  gd[1].clear();
+  int tiles[2] = {0, 0};
+  for (int i : order) {
+    const GProb& e = pr[i];
+    const int cls = e.bn == 64 ? 1 : 0;
+    GemmDesc x;
+    memset(&x, 0, sizeof(x));
+    if (!make_tmap(&x.ta, e.RA, e.kp, e.M, nmod, G_BM) || !make_tmap(&x.tb, e.RH, e.kp, e.N, nmod, e.bn))
+      return PSMMA_EDEVICE;
+    x.R = e.R;
+    x.n = e.M;
+    x.kr = e.kr;
+    x.nkb = e.kp / G_BK;
+    x.tiles_m = (e.M + G_BM - 1) / G_BM;
+    x.tiles_n = (e.N + e.bn - 1) / e.bn;
+    x.t0 = tiles[cls];
+    tiles[cls] += x.tiles_m * x.tiles_n * nmod;
+    gd[cls].push_back(x);
+  }
+  for (int c = 0; c < 2; ++c) {
+    g->n_gemm[c] = (int)gd[c].size();
+    g->tiles[c] = tiles[c];
+  }
+  *probs = pr;
+  return PSMMA_OK;
+}
+
+}  // namespace
+
+size_t split_group_bytes(const SplitProblem* P, int count, int n_moduli) {
+  if (count <= 0) return 0;
+  SplitGroup g;
+  WsBump w(nullptr);
+  plan_group(P, count, resolve_nmod(n_moduli), 64, 12, w, nullptr, nullptr, &g);
+  return w.off + 4096;
+}
+
+int split_group_prepare(const SplitProblem* P, int count, int n_moduli, int narrow_max, int group_m, void* work,
+                        size_t lwork, cudaStream_t stream, SplitGroup* g) {
+  const int nmod = resolve_nmod(n_moduli);
+  if (nmod < 8 || nmod > SPL_MAX_MODULI) return PSMMA_EUNSUPPORTED;
+  if (count <= 0) {
+    *g = SplitGroup();
+    return PSMMA_OK;
+  }
+  for (int i = 0; i < count; ++i) {
+    const SplitProblem& q = P[i];
+    if (q.M <= 0 || q.N <= 0 || q.K <= 0 || q.gs.kind == KIND_DFT) return PSMMA_EUNSUPPORTED;
+    if (q.K >= (1 << 24) || q.M >= (1 << 30) || q.N >= (1 << 30)) return PSMMA_EUNSUPPORTED;
+  }
+  if (!work || lwork < split_group_bytes(P, count, n_moduli)) return PSMMA_EWORKSPACE;
+  WsBump w((void*)(((uintptr_t)work + 255) & ~(uintptr_t)255));
+  std::vector<GProb> pr;
+  std::vector<GemmDesc> gd[2];
+  int st = plan_group(P, count, nmod, narrow_max, group_m, w, &pr, gd, g);
+  if (st) return st;
+  if (cudaMemcpyAsync(g->d_probs, pr.data(), sizeof(GProb) * count, cudaMemcpyHostToDevice, stream) != cudaSuccess)
+    return PSMMA_EDEVICE;
+  for (int c = 0; c < 2; ++c)
+    if (!gd[c].empty() && cudaMemcpyAsync(g->d_gemm[c], gd[c].data(), sizeof(GemmDesc) * gd[c].size(),
+                                          cudaMemcpyHostToDevice, stream) != cudaSuccess)
+      return PSMMA_EDEVICE;
+  return PSMMA_OK;
+}
+
+template <int BN>
+static int launch_group_gemm(const SplitGroup& g, int cls, const CrtConsts& cc, int sms, cudaStream_t stream) {
+  if (g.n_gemm[cls] == 0) return PSMMA_OK;
+  using Shape = GemmShape<BN>;
+  GroupGemm ts;
+  memset(&ts, 0, sizeof(ts));
+  ts.g.nmod = g.nmod;
+  ts.g.group_m = g.group_m;
+  ts.g.status = g.status;
+  for (int l = 0; l < g.nmod; ++l) {
+    ts.g.m[l] = cc.m[l];
+    ts.g.inv_m[l] = cc.inv_m[l];
+  }
+  ts.d = (const GemmDesc*)g.d_gemm[cls];
+  ts.count = g.n_gemm[cls];
+  ts.total_tiles = g.tiles[cls];
+  if (cudaFuncSetAttribute(k_crt_gemm<BN, GroupGemm>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)Shape::SMEM) != cudaSuccess)
+    return PSMMA_EDEVICE;
+  k_crt_gemm<BN, GroupGemm><<<std::min(sms, ts.total_tiles), G_THREADS, Shape::SMEM, stream>>>(ts);
+  return PSMMA_OK;
+}
+
+int split_group_enqueue(const SplitGroup& g, cudaStream_t stream, unsigned* status_out) {
+  if (g.count == 0) return PSMMA_OK;
+  const CrtConsts cc = get_consts(g.nmod);
+  const GProb* d = (const GProb*)g.d_probs;
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return PSMMA_EDEVICE;
+  if (cudaMemsetAsync(g.small, 0, g.small_bytes, stream) != cudaSuccess) return PSMMA_EDEVICE;
+  k_g_row_absmax<<<g.blocks_row, 128, 0, stream>>>(d, g.count);
+  prof_mark(stream, "g_row_scale");
+  k_g_h_pass1<<<g.blocks_h, 256, 0, stream>>>(d, g.count);
+  prof_mark(stream, "g_h_generate");
+  k_g_split_params<<<g.count, 1024, 0, stream>>>(d, cc.log2M);
+  prof_mark(stream, "g_params");
+  k_g_residues_A<<<g.blocks_ra, 256, 0, stream>>>(d, g.count, cc);
+  prof_mark(stream, "g_residues_A");
+  k_g_residues_H<<<g.blocks_rh, 128, 0, stream>>>(d, g.count, cc);
+  prof_mark(stream, "g_residues_H");
+  int st = launch_group_gemm<256>(g, 0, cc, sms, stream);
+  prof_mark(stream, "g_gemm_256");
+  if (!st) st = launch_group_gemm<64>(g, 1, cc, sms, stream);
+  prof_mark(stream, "g_gemm_64");
+  if (st) return st;
+  k_g_crt_combine<<<g.blocks_crt, dim3(32, 8), 0, stream>>>(d, g.count, cc);
+  prof_mark(stream, "g_crt_combine");
+  if (cudaGetLastError() != cudaSuccess) return PSMMA_EDEVICE;
+  if (status_out &&
+      cudaMemcpyAsync(status_out, g.status, sizeof(unsigned), cudaMemcpyDeviceToDevice, stream) != cudaSuccess)
+    return PSMMA_EDEVICE;
   return PSMMA_OK;
 }
 

@@ -1,0 +1,146 @@
+"""Batched merge level (psmma_cauchy_batch_lowrank): off-diagonal blocks compressed by RRQR
+(Compress_RRQR, Auxil_2p5D.f90:1063-1189) or the structured RRLU (compress_cauchy,
+Cauchylowrank.f90:387-491), products through the FP64 and split paths.  GPU results are
+compared with the oracle's restatement of the same merge level (ranks and result) and with
+the exact dense product."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from oracle import psmma_oracle as O
+from psmma_git_gb300 import _lib
+
+SIZES = [1, 2, 3, 37, 128, 300, 515, 1031]
+
+
+def _problems(sizes, seed=0):
+    out = []
+    for i, n in enumerate(sizes):
+        g = O.cfg_cauchy_generators(n, seed=seed + 10 * i)
+        A = O.cfg_matrix(n, n, seed=seed + 10 * i + 1)
+        Q0 = O.cfg_matrix(n, n, seed=seed + 10 * i + 2)
+        out.append((A, g, Q0))
+    return out
+
+
+def _to_dev(problems, ld_pad=0):
+    import torch
+    from psmma_git_gb300 import fortran_empty
+    dev = []
+    for A, g, Q0 in problems:
+        n = A.shape[0]
+        Ad = fortran_empty(n, n, ld=n + ld_pad)
+        Ad.copy_(torch.from_numpy(A))
+        gd = torch.from_numpy(np.asfortranarray(g)).cuda()
+        gd = gd.t().contiguous().t()  # column-major n x 4
+        Qd = fortran_empty(n, n, ld=n + ld_pad)
+        Qd.copy_(torch.from_numpy(Q0))
+        dev.append((Ad, gd, Qd))
+    return dev
+
+
+def test_batch_argument_checks(lib):
+    items = (_lib.PsmmaBatchItem * 1)()
+    buf = np.zeros(16)
+    p = buf.ctypes.data
+    items[0].n, items[0].A, items[0].lda, items[0].gen, items[0].ldgen = 4, p, 4, p, 4
+    items[0].Q, items[0].ldq = p, 4
+    f = lib.psmma_cauchy_batch_lowrank
+    assert f(0, items, 1.0, 0.0, 0, 1e-14, None, None, None, None) == 0          # empty batch
+    items[0].n = -1
+    assert f(1, items, 1.0, 0.0, 0, 1e-14, None, None, None, None) == -2
+    items[0].n, items[0].lda = 4, 3
+    assert f(1, items, 1.0, 0.0, 0, 1e-14, None, None, None, None) == -9
+    items[0].lda, items[0].ldq = 4, 3
+    assert f(1, items, 1.0, 0.0, 0, 1e-14, None, None, None, None) == -14
+    items[0].ldq, items[0].ldgen = 4, 3
+    assert f(1, items, 1.0, 0.0, 0, 1e-14, None, None, None, None) == _lib.PSMMA_EGEN
+    items[0].ldgen = 4
+    assert f(1, items, 1.0, 0.0, 7, 1e-14, None, None, None, None) == _lib.PSMMA_EUNSUPPORTED  # compressor
+    assert f(1, items, 1.0, 0.0, 0, 0.0, None, None, None, None) == _lib.PSMMA_EUNSUPPORTED    # tol
+
+
+def test_oracle_merge_level_matches_exact_product():
+    for comp in ["rrqr", "rrlu"]:
+        for (A, g, Q0) in _problems([2, 37, 300]):
+            n = A.shape[0]
+            Q, ranks = O.merge_level_product(A, g, Q0, 0.75, -0.5, comp, 1e-14)
+            ref = 0.75 * A @ O.dense_h("cauchy", g, n) - 0.5 * Q0
+            assert O.rel_fro(Q, ref) < 1e-14
+            assert len(ranks) == 2 and all(0 <= r <= n for r in ranks)
+
+
+def _run(problems, comp, precision, alpha, beta, ld_pad=0, n_moduli=0):
+    import torch
+    from psmma_git_gb300 import cauchy_batch_lowrank
+    dev = _to_dev(problems, ld_pad)
+    ranks, info = cauchy_batch_lowrank(dev, alpha, beta, compressor=comp, tol=1e-14, precision=precision,
+                                       n_moduli=n_moduli)
+    torch.cuda.synchronize()
+    return [Qd.cpu().numpy() for (_, _, Qd) in dev], ranks, info
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("comp", ["rrqr", "rrlu"])
+def test_batch_fp64_matches_oracle(comp):
+    problems = _problems(SIZES, seed=3)
+    alpha, beta = 0.75, -0.5
+    Qs, ranks, info = _run(problems, comp, "fp64", alpha, beta, ld_pad=3)
+    k = 0
+    for (A, g, Q0), Qg in zip(problems, Qs):
+        n = A.shape[0]
+        Qo, ro = O.merge_level_product(A, g, Q0, alpha, beta, comp, 1e-14)
+        exact = alpha * A @ O.dense_h("cauchy", g, n) + beta * Q0
+        rg = ranks[k:k + len(ro)]
+        k += len(ro)
+        for a, b in zip(rg, ro):  # QR pivots can differ at rounding-level near-ties
+            assert abs(a - b) <= 1, (n, rg, ro)
+        assert O.rel_fro(Qg, Qo) < 1e-13, n
+        assert O.rel_fro(Qg, exact) < 1e-13, n
+    assert k == len(ranks) == info["n_blocks"]
+    eff = sum(2.0 * n ** 3 for n in SIZES)
+    assert info["effective_flops"] == pytest.approx(eff)
+    assert 0 < info["executed_flops"] < eff
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("comp", ["rrqr", "rrlu"])
+def test_batch_split_matches_exact(comp):
+    problems = _problems([64, 300, 1031, 2048], seed=5)
+    Qs, ranks, info = _run(problems, comp, "split", 1.0, 0.0)
+    for (A, g, Q0), Qg in zip(problems, Qs):
+        n = A.shape[0]
+        exact = A @ O.dense_h("cauchy", g, n)
+        assert O.rel_fro(Qg, exact) < 1e-12, n
+
+
+@pytest.mark.gpu
+def test_batch_ranks_match_reference_scan_on_larger_blocks():
+    # off-diagonal blocks of 2048 x 2048: the RRQR rank is the first |R_kk| <= tol |R_11|
+    problems = _problems([4096], seed=11)
+    _, ranks, _ = _run(problems, "rrqr", "fp64", 1.0, 0.0)
+    A, g, _ = problems[0]
+    _, ro = O.merge_level_product(A, g, np.zeros((4096, 4096)), 1.0, 0.0, "rrqr", 1e-14)
+    assert all(abs(a - b) <= 1 for a, b in zip(ranks, ro)), (ranks, ro)
+
+
+@pytest.mark.gpu
+def test_batch_workspace_and_caller_buffer():
+    import torch
+    from psmma_git_gb300 import batch_workspace_size, cauchy_batch_lowrank
+    problems = _problems([300, 515], seed=9)
+    dev = _to_dev(problems)
+    need = batch_workspace_size(dev, compressor="rrqr")
+    assert need > 0
+    work = torch.empty(need, dtype=torch.uint8, device="cuda")
+    cauchy_batch_lowrank(dev, 1.0, 0.0, compressor="rrqr", work=work)
+    torch.cuda.synchronize()
+    for (A, g, _), (_, _, Qd) in zip(problems, dev):
+        exact = A @ O.dense_h("cauchy", g, A.shape[0])
+        assert O.rel_fro(Qd.cpu().numpy(), exact) < 1e-13
+    small = torch.empty(need // 2, dtype=torch.uint8, device="cuda")
+    from psmma_git_gb300 import PsmmaError
+    with pytest.raises(PsmmaError) as e:
+        cauchy_batch_lowrank(dev, 1.0, 0.0, compressor="rrqr", work=small)
+    assert e.value.status == _lib.PSMMA_EWORKSPACE
