@@ -444,6 +444,118 @@ def run_serving(args, ws, rank, local):
     return 0
 
 
+def run_merge_level(args, ws, rank, local):
+    """Batched divide-and-conquer merge level: 64 independent Cauchy multiplies Q_i = A_i H_i,
+    n_i log-uniform in [256, 8192] (seeded), generators as the n = 2048 workload (d sorted
+    uniform, w interlacing, u, v normal), A_i uniform[-1,1] resident in HBM.  The
+    off-diagonal blocks of each H_i are compressed at tol 1e-14 by RRQR (the reference's
+    Compress_RRQR) and by the structured RRLU; the products run as grouped launches in one
+    CUDA graph.  value = dense-equivalent sum(2 n^3) / time (effective), executed flops
+    reported beside it.  One JSON line."""
+    import numpy as np
+    import torch
+    import psmma_git_gb300 as P
+    from oracle import psmma_oracle as O
+    if rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    sizes = O.cfg_batch_sizes(args.batch_count, 256, 8192, seed=7)
+    g = torch.Generator(device=dev)
+    g.manual_seed(3)
+    probs = []
+    for i, n in enumerate(sizes):
+        gen = torch.from_numpy(np.ascontiguousarray(O.cfg_cauchy_generators(n, seed=100 + i).T)).to(dev).t()
+        A = P.fortran_empty(n, n, torch.float64, dev)
+        A.copy_(torch.rand(n, n, generator=g, device=dev, dtype=torch.float64).mul_(2).sub_(1))
+        Q = P.fortran_empty(n, n, torch.float64, dev)
+        Q.zero_()
+        probs.append((A, gen, Q))
+    torch.cuda.synchronize()
+    eff = sum(2.0 * n ** 3 for n in sizes)
+    # dense FP64 references of the smallest problems (accuracy check)
+    check = sorted(range(len(sizes)), key=lambda i: sizes[i])[: args.batch_check]
+    refs = {}
+    for i in check:
+        A, gen, _ = probs[i]
+        n = sizes[i]
+        R = P.fortran_empty(n, n, torch.float64, dev)
+        P.psmma_cauchy(n, n, 1.0, A, gen, 0.0, R)
+        refs[i] = R
+    torch.cuda.synchronize()
+    out = {}
+    precisions = ["split"] + (["fp64"] if args.merge_fp64 else [])
+    for comp in ["rrqr", "rrlu"]:
+        for prec in precisions:
+            kw = dict(compressor=comp, tol=1e-14, precision=prec, n_moduli=args.n_moduli)
+            for _ in range(args.warmup if prec == "split" else 1):
+                ranks, info = P.cauchy_batch_lowrank(probs, 1.0, 0.0, **kw)
+            torch.cuda.synchronize()
+            steps = args.steps if prec == "split" else 1
+            times = []
+            for _ in range(steps):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                torch.cuda.synchronize()
+                e0.record()
+                ranks, info = P.cauchy_batch_lowrank(probs, 1.0, 0.0, **kw)
+                e1.record()
+                torch.cuda.synchronize()
+                times.append(e0.elapsed_time(e1))
+            err = max(float(torch.linalg.norm(probs[i][2] - refs[i]) / torch.linalg.norm(refs[i])) for i in check)
+            # per-phase trace of one more call (eager launches, one event per phase)
+            lib = P.load()
+            lib.psmma_set_profiling(1)
+            P.cauchy_batch_lowrank(probs, 1.0, 0.0, **kw)
+            torch.cuda.synchronize()
+            ms = (C_float * 40)()
+            names = (C_charp * 40)()
+            m = lib.psmma_profile_read(ms, names, 40)
+            lib.psmma_set_profiling(0)
+            phases = [[names[j].decode(), round(ms[j], 3)] for j in range(max(0, m))]
+            t = statistics.median(times)
+            out[f"{comp}_{prec}"] = {
+                "ms_per_step": t, "steps": steps, "effective_tflops": eff / t / 1e9,
+                "executed_tflops": info["executed_flops"] / t / 1e9,
+                "executed_flops": info["executed_flops"], "compress_flops": info["compress_flops"],
+                "ranks": {"max": int(max(ranks)), "mean": float(np.mean(ranks)), "min": int(min(ranks))},
+                "full_rank_blocks": info["full_rank_blocks"], "rel_err_vs_dense_fp64": err,
+                "phases_ms": phases}
+            print(json.dumps({comp + "_" + prec: out[f"{comp}_{prec}"]}), file=sys.stderr, flush=True)
+    # CPU baseline: the oracle's restatement of the merge level (Compress_RRQR + DGEMMs) on the
+    # smallest problems until ~args.cpu_seconds of work
+    cpu = None
+    if not args.no_cpu:
+        order = sorted(range(len(sizes)), key=lambda i: sizes[i])
+        done_fl, t_cpu, used = 0.0, 0.0, []
+        for i in order:
+            n = sizes[i]
+            A = probs[i][0].cpu().numpy()
+            gen = probs[i][1].cpu().numpy()
+            t0 = time.perf_counter()
+            O.merge_level_product(A, gen, np.zeros((n, n)), 1.0, 0.0, "rrqr", 1e-14)
+            t_cpu += time.perf_counter() - t0
+            done_fl += 2.0 * n ** 3
+            used.append(n)
+            if t_cpu > args.cpu_seconds:
+                break
+        cpu = {"value": done_fl / t_cpu / 1e12, "unit": "TFLOP/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"{len(used)} smallest problems (n = {min(used)}..{max(used)}) of the batch, "
+                         "oracle merge level with RRQR, numpy/OpenBLAS threads = cores"}
+    head = out["rrqr_split"]
+    line = {"metric": "merge level: effective TFLOP/s, sum(2 n^3) / t, "
+                      f"{len(sizes)} Cauchy multiplies n log-uniform [256, 8192], off-diagonal blocks RRQR at 1e-14",
+            "value": head["effective_tflops"], "unit": "TFLOP/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64 (split: bf16 modular slices)",
+            "data": "synthetic",
+            "config": {"workload": "batched merge level", "count": len(sizes), "sum_n": sum(sizes),
+                       "n_max": max(sizes), "n_moduli": args.n_moduli, "tol": 1e-14,
+                       "l2": "inputs ~ 10 GB > L2, no flush needed"},
+            "compressors": out, "cpu_baseline": cpu}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 import ctypes  # noqa: E402
 
 C_float = ctypes.c_float
@@ -470,6 +582,11 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=6.0)
     ap.add_argument("--serve-nmax", type=int, default=16384)
     ap.add_argument("--serve-budget-gib", type=int, default=96)
+    ap.add_argument("--merge-level", action="store_true", help="run the batched merge level (64 problems)")
+    ap.add_argument("--batch-count", type=int, default=64)
+    ap.add_argument("--batch-check", type=int, default=8)
+    ap.add_argument("--merge-fp64", action="store_true", help="also time the FP64 path of the merge level")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
     args = ap.parse_args()
     ws, rank, local = dist_init(args)
     if args.impl == "reference":
@@ -480,6 +597,8 @@ def main():
     barrier(ws)
     if args.serving:
         return run_serving(args, ws, rank, local)
+    if args.merge_level:
+        return run_merge_level(args, ws, rank, local)
     return run_gpu(args, ws, rank, local)
 
 

@@ -38,6 +38,12 @@ struct RrluBlock {
   double* W;          // interpolation weights, min(M, N)
   int *PL, *PU;       // 1-based permutations
   int* rank;          // output Rk
+  // resumable state: the kernel stops at a step that needs a complete-pivot search, which a
+  // grid-wide kernel does for all such blocks at once (cp_i, cp_j), then resumes
+  int k_next;         // step to continue from (1-based)
+  int phase;          // 0 running, 1 waiting for the search at step k_next, 2 done
+  int cp_i, cp_j;     // search result: 1-based row / column offsets from k_next - 1
+  double amax;
 };
 
 constexpr int RRLU_THREADS = 512;
@@ -203,11 +209,8 @@ __device__ Cand multi_cauchy_max(const double* D, const double* u, int len, cons
   return r;
 }
 
-// CauchyPivtG_CP (:246-296): complete pivoting on the k-th Schur complement.
-__device__ void pivt_g_cp(RrluBlock& b, int k0, Cand* smc) {
-  const int M = b.M, N = b.N;
-  const Cand c = multi_cauchy_max(b.D + k0, b.U + k0, M - k0, b.F + k0, b.V + k0, N - k0, smc);
-  const int ii = c.i, jj = c.j;
+// Swaps of CauchyPivtG_CP (:246-296) for the search result (ii, jj) at step k0.
+__device__ void apply_cp(RrluBlock& b, int k0, int ii, int jj) {
   if (threadIdx.x == 0) {
     swapd(b.D, k0, ii + k0 - 1);
     swapd(b.U, k0, ii + k0 - 1);
@@ -220,42 +223,62 @@ __device__ void pivt_g_cp(RrluBlock& b, int k0, Cand* smc) {
   __syncthreads();
 }
 
-__global__ void __launch_bounds__(RRLU_THREADS) k_rrlu_cauchy(const RrluBlock* blocks, double tol) {
+// rrluCauchy (:7-134), one block per matrix block, resumable around the complete-pivot
+// search (CauchyPivtG_CP): a step whose pivot is below tol * amax saves its state, counts
+// itself in *pending and returns; the search runs grid-wide and the next launch resumes.
+__global__ void __launch_bounds__(RRLU_THREADS) k_rrlu_cauchy(RrluBlock* blocks, double tol, int* pending) {
   __shared__ ArgMax sm[33];
   __shared__ Cand smc[33];
-  RrluBlock b = blocks[blockIdx.x];
+  RrluBlock& gb = blocks[blockIdx.x];
+  RrluBlock b = gb;
+  if (b.phase == 2) return;
   const int M = b.M, N = b.N, mn = min(M, N);
   const double rho = 1.12;
   const int prd = 10;
-  // D, A from the row generators, F, V from the column generators; U = A, PL = 1..M,
-  // PU = 1..N, W = 0 (rrluCauchy :64-71; compress_cauchy zeroes W)
-  for (int i = threadIdx.x; i < M; i += blockDim.x) {
-    b.D[i] = b.gD[i];
-    b.A[i] = b.gU[i];
-    b.U[i] = b.gU[i];
-    b.PL[i] = i + 1;
+  bool resume_cp = b.phase == 1;
+  if (b.phase == 0 && b.k_next == 1) {
+    // D, A from the row generators, F, V from the column generators; U = A, PL = 1..M,
+    // PU = 1..N, W = 0 (rrluCauchy :64-71; compress_cauchy zeroes W)
+    for (int i = threadIdx.x; i < M; i += blockDim.x) {
+      b.D[i] = b.gD[i];
+      b.A[i] = b.gU[i];
+      b.U[i] = b.gU[i];
+      b.PL[i] = i + 1;
+    }
+    for (int j = threadIdx.x; j < N; j += blockDim.x) {
+      b.F[j] = b.gF[j];
+      b.V[j] = b.gV[j];
+      b.PU[j] = j + 1;
+    }
+    for (int j = threadIdx.x; j < mn; j += blockDim.x) b.W[j] = 0.0;
+    __syncthreads();
   }
-  for (int j = threadIdx.x; j < N; j += blockDim.x) {
-    b.F[j] = b.gF[j];
-    b.V[j] = b.gV[j];
-    b.PU[j] = j + 1;
-  }
-  for (int j = threadIdx.x; j < mn; j += blockDim.x) b.W[j] = 0.0;
-  __syncthreads();
   int Rk = mn;
-  double amax = 0.0;
-  for (int k = 1; k <= mn; ++k) {
+  double amax = b.amax;
+  for (int k = b.k_next; k <= mn; ++k) {
     const int k0 = k - 1;
-    pivt_g(b, k0, sm);
-    double ukk = b.U[k0] * b.V[k0] / (b.D[k0] - b.F[k0]);
-    amax = fmax(amax, fabs(ukk));
-    if (fabs(ukk) < tol * amax) {
-      pivt_g_cp(b, k0, smc);
+    double ukk;
+    if (resume_cp) {
+      resume_cp = false;
+      apply_cp(b, k0, b.cp_i, b.cp_j);
       ukk = b.U[k0] * b.V[k0] / (b.D[k0] - b.F[k0]);
       amax = fmax(amax, fabs(ukk));
       if (fabs(ukk) < tol * amax) {
         Rk = k - 1;
         break;
+      }
+    } else {
+      pivt_g(b, k0, sm);
+      ukk = b.U[k0] * b.V[k0] / (b.D[k0] - b.F[k0]);
+      amax = fmax(amax, fabs(ukk));
+      if (fabs(ukk) < tol * amax) {
+        if (threadIdx.x == 0) {
+          gb.phase = 1;
+          gb.k_next = k;
+          gb.amax = amax;
+          atomicAdd(pending, 1);
+        }
+        return;
       }
     }
     const double dk = b.D[k0], fk = b.F[k0];
@@ -307,7 +330,58 @@ __global__ void __launch_bounds__(RRLU_THREADS) k_rrlu_cauchy(const RrluBlock* b
       }
     }
   }
-  if (threadIdx.x == 0) *b.rank = Rk;
+  if (threadIdx.x == 0) {
+    *b.rank = Rk;
+    gb.phase = 2;
+  }
+}
+
+// Complete-pivot search (CauchyPivtG_CP's max over the Schur complement) for the blocks
+// waiting in the resumable RRLU: each CTA takes a chunk of columns of one block, one warp
+// per column, and leaves its best candidate in cand[blockIdx.x]; the maximum over the
+// chunks of a block (ties: earlier column, then earlier row) goes to cp_i, cp_j.
+struct CpChunk {
+  int blk, c0, c1;  // columns [c0, c1) (absolute) of block blk
+};
+
+__global__ void __launch_bounds__(RRLU_THREADS) k_cp_search(const RrluBlock* blocks, const CpChunk* chunks,
+                                                             Cand* cand) {
+  __shared__ Cand smc[33];
+  const CpChunk ch = chunks[blockIdx.x];
+  const RrluBlock& b = blocks[ch.blk];
+  const int k0 = b.k_next - 1;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  Cand wb{-1.0, 0x7fffffff, 0};
+  for (int j = ch.c0 + warp; j < ch.c1; j += nw) {
+    const double pj = b.F[j];
+    ArgMax a{-1.0, 0x7fffffff};
+    for (int i = k0 + lane; i < b.M; i += 32) a = better(a, ArgMax{fabs(b.U[i] / (b.D[i] - pj)), i - k0 + 1});
+    for (int o = 16; o > 0; o >>= 1) {
+      ArgMax y;
+      y.v = __shfl_xor_sync(0xffffffffu, a.v, o);
+      y.i = __shfl_xor_sync(0xffffffffu, a.i, o);
+      a = better(a, y);
+    }
+    wb = better_c(wb, Cand{a.v * fabs(b.V[j]), j - k0 + 1, a.i});
+  }
+  if (lane == 0) smc[warp] = wb;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    Cand r = smc[0];
+    for (int w = 1; w < nw; ++w) r = better_c(r, smc[w]);
+    cand[blockIdx.x] = r;
+  }
+}
+
+__global__ void k_cp_reduce(RrluBlock* blocks, const int* __restrict__ blk, const int* __restrict__ first,
+                            int count, int total, const Cand* __restrict__ cand) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  const int e = (t + 1 < count) ? first[t + 1] : total;
+  Cand r = cand[first[t]];
+  for (int c = first[t] + 1; c < e; ++c) r = better_c(r, cand[c]);
+  blocks[blk[t]].cp_i = r.i;
+  blocks[blk[t]].cp_j = r.j;
 }
 
 // Columns of A(:, R) (n x M, lda) in RRLU pivot order for every compressed block:
@@ -354,6 +428,7 @@ struct QrTile {
   double *vn1, *vn2;  // partial column norms
   int* jpvt;     // original column of each pivoted column
   int* rank;     // -1 running, -2 verifying; then r (< min(M,N)) or min(M,N) when not compressed
+  int* flag;     // k + 1 when step k flagged a partial norm for recomputation
   unsigned* bar; // group barrier counter
   int cta0, ncta;
   long col0;     // first column of this tile in the batch's column numbering
@@ -387,6 +462,7 @@ __global__ void __launch_bounds__(QR_THREADS) k_qr_tiles(QrTile* tiles, int ntil
     t.jpvt[c] = c;
     if (c == 0) {
       *t.rank = -1;
+      *t.flag = 0;
       *t.bar = 0u;
     }
   }
@@ -421,10 +497,26 @@ __device__ bool group_sync(unsigned* bar, unsigned target, unsigned* status) {
   return ok != 0;
 }
 
-// Step k of the leader CTA: pivot, swap, the current column a = T(:,k) - V F(k,:)^T, its
-// Householder reflector (beta = -sign(alpha) ||a(k:)||, tau = (beta - alpha)/beta,
-// v = a(k+1:)/(alpha - beta)), the truncation test and s = V(k:,0:k)^T v.
-__device__ void qr_leader_step(const QrTile& t, int k, double tol, bool verified, ArgMax* am, double* red,
+// Lane part of a warp dot product sum x[i] y[i], i = i0 (mod 32) in [i0, M): four independent
+// accumulators keep eight loads in flight.
+__device__ __forceinline__ double lane_dot(const double* x, const double* y, int i0, int M) {
+  double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+  int i = i0;
+  for (; i + 96 < M; i += 128) {
+    a0 = fma(__ldcg(x + i), __ldcg(y + i), a0);
+    a1 = fma(__ldcg(x + i + 32), __ldcg(y + i + 32), a1);
+    a2 = fma(__ldcg(x + i + 64), __ldcg(y + i + 64), a2);
+    a3 = fma(__ldcg(x + i + 96), __ldcg(y + i + 96), a3);
+  }
+  for (; i < M; i += 32) a0 = fma(__ldcg(x + i), __ldcg(y + i), a0);
+  return (a0 + a1) + (a2 + a3);
+}
+
+// Step k of the leader CTA: pivot, swap, the current column a = T(k:,k) - V F(k,:)^T over the
+// reflectors p0..k-1 of the current panel (earlier ones are applied to T), its Householder
+// reflector (beta = -sign(alpha) ||a||, tau = (beta - alpha)/beta, v = a(k+1:)/(alpha - beta)),
+// the truncation test and s = V(k:,p0:k)^T v.
+__device__ void qr_leader_step(const QrTile& t, int k, int p0, double tol, bool verified, ArgMax* am, double* red,
                                double* fk) {
   const int M = t.M, N = t.N, cap = t.cap;
   ArgMax best{-1.0, 0x7fffffff};
@@ -432,7 +524,7 @@ __device__ void qr_leader_step(const QrTile& t, int k, double tol, bool verified
   best = block_argmax(best, am);
   const int p = best.i;
   if (p != k) {
-    for (int i = threadIdx.x; i < M; i += blockDim.x) {
+    for (int i = k + threadIdx.x; i < M; i += blockDim.x) {
       double* a = t.T + i + (long)k * M;
       double* b = t.T + i + (long)p * M;
       const double x = __ldcg(a), y = __ldcg(b);
@@ -440,9 +532,13 @@ __device__ void qr_leader_step(const QrTile& t, int k, double tol, bool verified
       *b = x;
     }
     for (int j = threadIdx.x; j < k; j += blockDim.x) {
-      double x = __ldcg(t.F + (long)k * cap + j), y = __ldcg(t.F + (long)p * cap + j);
-      t.F[(long)k * cap + j] = y;
-      t.F[(long)p * cap + j] = x;
+      double x, y;
+      if (j >= p0) {
+        x = __ldcg(t.F + (long)k * cap + j);
+        y = __ldcg(t.F + (long)p * cap + j);
+        t.F[(long)k * cap + j] = y;
+        t.F[(long)p * cap + j] = x;
+      }
       x = __ldcg(t.R + (long)k * cap + j);
       y = __ldcg(t.R + (long)p * cap + j);
       t.R[(long)k * cap + j] = y;
@@ -461,13 +557,13 @@ __device__ void qr_leader_step(const QrTile& t, int k, double tol, bool verified
     }
     __syncthreads();
   }
-  for (int j = threadIdx.x; j < k; j += blockDim.x) fk[j] = __ldcg(t.F + (long)k * cap + j);
+  for (int j = p0 + threadIdx.x; j < k; j += blockDim.x) fk[j - p0] = __ldcg(t.F + (long)k * cap + j);
   __syncthreads();
   double* vk = t.V + (long)k * M;
   double xsq = 0.0;
   for (int i = k + threadIdx.x; i < M; i += blockDim.x) {
     double a = __ldcg(t.T + i + (long)k * M);
-    for (int j = 0; j < k; ++j) a = fma(-__ldcg(t.V + i + (long)j * M), fk[j], a);
+    for (int j = p0; j < k; ++j) a = fma(-__ldcg(t.V + i + (long)j * M), fk[j - p0], a);
     vk[i] = a;
     if (i > k) xsq = fma(a, a, xsq);
   }
@@ -495,85 +591,118 @@ __device__ void qr_leader_step(const QrTile& t, int k, double tol, bool verified
     if (fabs(beta) <= tol * r11) *t.rank = verified ? k : -2;
   }
   __syncthreads();
-  // s(j) = sum_{i >= k} V(i,j) v(i), j < k: one warp per j
+  // s(j) = sum_{i >= k} V(i,j) v(i), p0 <= j < k: one warp per j
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  for (int j = warp; j < k; j += QR_WARPS) {
-    double a = 0.0;
-    for (int i = k + lane; i < M; i += 32) a = fma(__ldcg(t.V + i + (long)j * M), __ldcg(vk + i), a);
+  for (int j = p0 + warp; j < k; j += QR_WARPS) {
+    double a = lane_dot(t.V + (long)j * M, vk, k + lane, M);
     for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
     if (lane == 0) t.s[j] = a;
   }
 }
 
-__global__ void __launch_bounds__(QR_THREADS) k_rrqr_grouped(QrTile* tiles, const int* __restrict__ cta_tile,
-                                                              double tol, unsigned* status) {
-  __shared__ ArgMax am[33];
-  __shared__ double red[33];
-  __shared__ double fk[QR_CAP + 1];
-  __shared__ double sv[QR_CAP + 1];
-  __shared__ double vrow[QR_CAP + 1];
-  __shared__ double fw[QR_WARPS][QR_CAP];
-  const int ti = cta_tile[blockIdx.x];
-  if (ti < 0) return;
-  const QrTile t = tiles[ti];
-  const int local = blockIdx.x - t.cta0;
+// Panel restart (the trailing update of DLAQPS): T(r0:, c) -= V(r0:, p0:k1) F(c, p0:k1)^T for
+// every column c >= c0, written back, and the exact partial norms ||T(r0:, c)||.  One warp
+// per column, the columns shared by the CTAs of the group.
+__device__ void qr_restart(const QrTile& t, int p0, int k1, int r0, int c0, int local, double (*fw)[QR_CAP]) {
+  const int M = t.M, N = t.N, cap = t.cap;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nj = k1 - p0;
+  for (int c = c0 + local * QR_WARPS + warp; c < N; c += t.ncta * QR_WARPS) {
+    double* tc = t.T + (long)c * M;
+    for (int j = lane; j < nj; j += 32) fw[warp][j] = __ldcg(t.F + (long)c * cap + p0 + j);
+    __syncwarp();
+    double ss = 0.0;
+    for (int i = r0 + lane; i < M; i += 128) {  // four rows per lane in flight
+      double a[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) a[u] = (i + 32 * u < M) ? __ldcg(tc + i + 32 * u) : 0.0;
+      for (int j = 0; j < nj; ++j) {
+        const double* vj = t.V + (long)(p0 + j) * M;
+        const double w = fw[warp][j];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          if (i + 32 * u < M) a[u] = fma(-__ldcg(vj + i + 32 * u), w, a[u]);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (i + 32 * u < M) {
+          if (nj > 0) tc[i + 32 * u] = a[u];
+          ss = fma(a[u], a[u], ss);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
+    if (lane == 0) {
+      t.vn1[c] = sqrt(ss);
+      t.vn2[c] = sqrt(ss);
+    }
+    __syncwarp();
+  }
+}
+
+struct QrSmem {
+  ArgMax am[33];
+  double red[33];
+  double fk[QR_CAP + 1];
+  double sv[QR_CAP + 1];
+  double vrow[QR_CAP + 1];
+  double fw[QR_WARPS][QR_CAP];
+};
+
+// The factorisation of one tile by CTA `local` of its group; false when a barrier gave up.
+__device__ bool qr_tile(const QrTile& t, int local, double tol, unsigned* status, QrSmem& sm) {
+  ArgMax* am = sm.am;
+  double* red = sm.red;
+  double* fk = sm.fk;
+  double* sv = sm.sv;
+  double* vrow = sm.vrow;
+  double(*fw)[QR_CAP] = sm.fw;
   const int M = t.M, N = t.N, cap = t.cap;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const double tol3z = 1.0536712127723509e-08;  // sqrt(2^-53), LAPACK dgeqp3's recompute threshold
   unsigned epoch = 0;
   bool truncated = false;
+  int p0 = 0;  // first reflector not yet applied to T (the current panel)
   for (int k = 0; k < cap; ++k) {
-    if (local == 0) qr_leader_step(t, k, tol, false, am, red, fk);
-    if (!group_sync(t.bar, (++epoch) * t.ncta, status)) return;
+    if (local == 0) qr_leader_step(t, k, p0, tol, false, am, red, fk);
+    if (!group_sync(t.bar, (++epoch) * t.ncta, status)) return false;
     int state = __ldcg(t.rank);
     if (state == -2) {
-      // exact partial norms ||T(k:, c) - V(k:, 0:k) F(c, 0:k)^T||, c >= k, one warp per column
-      for (int c = k + local * QR_WARPS + warp; c < N; c += t.ncta * QR_WARPS) {
-        const double* tc = t.T + (long)c * M;
-        for (int j = lane; j < k; j += 32) fw[warp][j] = __ldcg(t.F + (long)c * cap + j);
-        __syncwarp();
-        double ss = 0.0;
-        for (int i = k + lane; i < M; i += 32) {
-          double a = __ldcg(tc + i);
-          for (int j = 0; j < k; ++j) a = fma(-__ldcg(t.V + i + (long)j * M), fw[warp][j], a);
-          ss = fma(a, a, ss);
-        }
-        for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
-        if (lane == 0) {
-          t.vn1[c] = sqrt(ss);
-          t.vn2[c] = sqrt(ss);
-        }
-        __syncwarp();
-      }
-      if (!group_sync(t.bar, (++epoch) * t.ncta, status)) return;
+      // apply the panel to the trailing tile (rows and columns >= k), exact norms, redo step k
+      qr_restart(t, p0, k, k, k, local, fw);
+      p0 = k;
+      if (!group_sync(t.bar, (++epoch) * t.ncta, status)) return false;
       if (local == 0) {
         if (threadIdx.x == 0) *t.rank = -1;
         __syncthreads();
-        qr_leader_step(t, k, tol, true, am, red, fk);
+        qr_leader_step(t, k, p0, tol, true, am, red, fk);
       }
-      if (!group_sync(t.bar, (++epoch) * t.ncta, status)) return;
+      if (!group_sync(t.bar, (++epoch) * t.ncta, status)) return false;
       state = __ldcg(t.rank);
     }
     if (state >= 0) {
       truncated = true;
       break;
     }
-    // every other column c > k: F(c,k), R(k,c) and the norm downdate (dgeqp3/dlaqp2)
+    // every other column c > k: F(c,k), R(k,c) and the norm downdate (dgeqp3/dlaqps); a
+    // column whose norm needs recomputing flags a panel restart after this step (DLAQPS
+    // ends its panel there: the pending reflectors are applied to T, norms recomputed)
     const double tk = __ldcg(t.tau + k);
-    for (int j = threadIdx.x; j < k; j += blockDim.x) sv[j] = __ldcg(t.s + j);
-    for (int j = threadIdx.x; j <= k; j += blockDim.x) vrow[j] = __ldcg(t.V + k + (long)j * M);
+    for (int j = p0 + threadIdx.x; j < k; j += blockDim.x) {
+      sv[j - p0] = __ldcg(t.s + j);
+      vrow[j - p0] = __ldcg(t.V + k + (long)j * M);
+    }
     __syncthreads();
     const double* vk = t.V + (long)k * M;
+    bool flagged = false;
     for (int c = k + 1 + local * QR_WARPS + warp; c < N; c += t.ncta * QR_WARPS) {
       const double* tc = t.T + (long)c * M;
       const double* fc = t.F + (long)c * cap;
-      double dot = 0.0;
-      for (int i = k + lane; i < M; i += 32) dot = fma(__ldcg(tc + i), __ldcg(vk + i), dot);
+      double dot = lane_dot(tc, vk, k + lane, M);
       double fs = 0.0, rs = 0.0;
-      for (int j = lane; j < k; j += 32) {
+      for (int j = p0 + lane; j < k; j += 32) {
         const double fj = __ldcg(fc + j);
-        fs = fma(fj, sv[j], fs);
-        rs = fma(vrow[j], fj, rs);
+        fs = fma(fj, sv[j - p0], fs);
+        rs = fma(vrow[j - p0], fj, rs);
       }
       for (int o = 16; o > 0; o >>= 1) {
         dot += __shfl_xor_sync(0xffffffffu, dot, o);
@@ -583,8 +712,8 @@ __global__ void __launch_bounds__(QR_THREADS) k_rrqr_grouped(QrTile* tiles, cons
       const double f = tk * (dot - fs);
       const double rkc = __ldcg(tc + k) - rs - f;  // V(k,k) = 1
       const double v1 = __ldcg(t.vn1 + c), v2 = __ldcg(t.vn2 + c);
-      bool recompute = false;
       double nv1 = v1;
+      bool recompute = false;
       if (v1 != 0.0) {
         double temp = fabs(rkc) / v1;
         temp = fmax(0.0, 1.0 - temp * temp);
@@ -593,33 +722,29 @@ __global__ void __launch_bounds__(QR_THREADS) k_rrqr_grouped(QrTile* tiles, cons
         if (temp2 <= tol3z) recompute = true;
         else nv1 = v1 * sqrt(temp);
       }
-      if (recompute) {
-        // exact norm of the reduced column below row k: T(i,c) - sum_{j<=k} V(i,j) F(c,j)
-        double ss = 0.0;
-        for (int i = k + 1 + lane; i < M; i += 32) {
-          double a = __ldcg(tc + i) - __ldcg(vk + i) * f;
-          for (int j = 0; j < k; ++j) a = fma(-__ldcg(t.V + i + (long)j * M), __ldcg(fc + j), a);
-          ss = fma(a, a, ss);
-        }
-        for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
-        nv1 = sqrt(ss);
-      }
+      flagged |= recompute;
       if (lane == 0) {
         t.F[(long)c * cap + k] = f;
         t.R[(long)c * cap + k] = rkc;
         t.vn1[c] = nv1;
-        if (recompute) t.vn2[c] = nv1;
       }
     }
-    if (!group_sync(t.bar, (++epoch) * t.ncta, status)) return;
+    if (flagged && lane == 0) atomicMax(t.flag, k + 1);
+    if (!group_sync(t.bar, (++epoch) * t.ncta, status)) return false;
+    if (__ldcg(t.flag) == k + 1 && k + 1 < cap) {
+      // panel restart: apply reflectors p0..k to rows and columns > k, exact norms
+      qr_restart(t, p0, k + 1, k + 1, k + 1, local, fw);
+      p0 = k + 1;
+      if (!group_sync(t.bar, (++epoch) * t.ncta, status)) return false;
+    }
   }
   if (!truncated) {
     // not truncated within cap steps: the tile is used as is
     if (local == 0 && threadIdx.x == 0) *t.rank = min(M, N);
-    return;
+    return true;
   }
   const int r = __ldcg(t.rank);
-  if (r == 0) return;
+  if (r == 0) return true;
   // Q(:, j) = H_0 ... H_j e_j for j < r (warp per column, in place in T), and
   // Y(i, jpvt(c)) = R(i, c) for c >= i (R P^T, DLAPMT) into F's storage
   for (int j = local * QR_WARPS + warp; j < r; j += t.ncta * QR_WARPS) {
@@ -630,8 +755,7 @@ __global__ void __launch_bounds__(QR_THREADS) k_rrqr_grouped(QrTile* tiles, cons
     __syncwarp();
     for (int h = j - 1; h >= 0; --h) {
       const double* vh = t.V + (long)h * M;
-      double d = 0.0;
-      for (int i = h + lane; i < M; i += 32) d = fma(__ldcg(vh + i), x[i], d);  // V(h,h) = 1
+      double d = lane_dot(vh, x, h + lane, M);  // V(h,h) = 1
       for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
       d *= __ldcg(t.tau + h);
       __syncwarp();
@@ -644,6 +768,19 @@ __global__ void __launch_bounds__(QR_THREADS) k_rrqr_grouped(QrTile* tiles, cons
     const int c = (int)(e / r), i = (int)(e % r);
     const double y = (c >= i) ? __ldcg(t.R + (long)c * cap + i) : 0.0;
     t.F[(long)__ldcg(t.jpvt + c) * r + i] = y;
+  }
+  return true;
+}
+
+// Grouped column-pivoted QR: CTA b factorises the tiles list[start[b] .. start[b+1]) in turn
+// (a large tile has a group of CTAs, small tiles share one CTA).  Cooperative launch.
+__global__ void __launch_bounds__(QR_THREADS, 2) k_rrqr_grouped(QrTile* tiles, const int* __restrict__ start,
+                                                              const int* __restrict__ list, double tol,
+                                                              unsigned* status) {
+  __shared__ QrSmem sm;
+  for (int e = start[blockIdx.x]; e < start[blockIdx.x + 1]; ++e) {
+    const QrTile t = tiles[list[e]];
+    if (!qr_tile(t, blockIdx.x - t.cta0, tol, status, sm)) return;
   }
 }
 
@@ -686,10 +823,16 @@ struct Plan {
   RrluBlock* d_lu = nullptr;
   QrTile* d_qr = nullptr;
   int* d_ranks = nullptr;        // RRLU ranks
+  int* d_pending = nullptr;      // RRLU blocks waiting for a complete-pivot search
+  CpChunk* d_chunks = nullptr;   // column chunks of the search
+  Cand* d_cand = nullptr;
+  int *d_cpblk = nullptr, *d_cpfirst = nullptr;
+  int chunk_cap = 0;
+  static constexpr int CP_COLS = 64;
   std::vector<double*> gather;   // per block: RRLU n x M, RRQR n x cap
   GatherDesc* d_gather = nullptr;
   unsigned* d_status = nullptr;  // [0..7] product rounds, [8] QR
-  int* d_map = nullptr;          // CTA -> tile of the grouped QR launch
+  int* d_map = nullptr;          // CTA work lists of the grouped QR launch
   long qr_cols = 0;
   static constexpr int MAP_MAX = 8192;
   static constexpr int N_STATUS = 16;
@@ -735,10 +878,21 @@ void make_plan(Plan& P, Bump& bump, const psmma_batch_item* items, int count, in
       r.W = bump.take<double>(std::min(ob.M, ob.N));
       r.PL = bump.take<int>(ob.M);
       r.PU = bump.take<int>(ob.N);
+      r.k_next = 1;
+      r.phase = 0;
+      r.cp_i = r.cp_j = 0;
+      r.amax = 0.0;
       P.gather[b] = bump.take<double>((size_t)it.n * ob.M);
     }
     P.d_lu = bump.take<RrluBlock>(std::max(1, nb));
     P.d_ranks = bump.take<int>(std::max(1, nb));
+    P.chunk_cap = nb;
+    for (int b = 0; b < nb; ++b) P.chunk_cap += (P.blocks[b].N + Plan::CP_COLS - 1) / Plan::CP_COLS;
+    P.d_pending = bump.take<int>(1);
+    P.d_chunks = bump.take<CpChunk>(P.chunk_cap);
+    P.d_cand = bump.take<Cand>(P.chunk_cap);
+    P.d_cpblk = bump.take<int>(std::max(1, nb));
+    P.d_cpfirst = bump.take<int>(std::max(1, nb));
     P.d_gather = bump.take<GatherDesc>(std::max(1, nb));
     for (int b = 0; b < nb; ++b) P.lu[b].rank = P.d_ranks + b;
   } else {
@@ -765,6 +919,7 @@ void make_plan(Plan& P, Bump& bump, const psmma_batch_item* items, int count, in
       q.vn2 = bump.take<double>(ob.N);
       q.jpvt = bump.take<int>(ob.N);
       q.rank = bump.take<int>(1);
+      q.flag = bump.take<int>(1);
       q.bar = bump.take<unsigned>(1);
       q.col0 = col0;
       col0 += ob.N;
@@ -772,7 +927,7 @@ void make_plan(Plan& P, Bump& bump, const psmma_batch_item* items, int count, in
     }
     P.qr_cols = col0;
     P.d_qr = bump.take<QrTile>(std::max(1, nb));
-    P.d_map = bump.take<int>(Plan::MAP_MAX);
+    P.d_map = bump.take<int>(Plan::MAP_MAX + nb);
   }
   P.d_status = bump.take<unsigned>(Plan::N_STATUS);
 }
@@ -854,6 +1009,91 @@ void build_rounds(const Plan& P, const psmma_batch_item* items, int count, int c
   }
 }
 
+// Split path: round 1 holds only the first factor products; round 2 has one product per
+// output column block C, its diagonal block and the factor of the off-diagonal block (R_o, C)
+// concatenated along K, so each output is recombined (CRT) once:
+//   Q(:, C) = alpha * [A(:, R_d) | T] * [H(R_d, C); Y] + beta * Q(:, C),
+// with Y the rows of H(PL(1:Rk), C) (RRLU, Cauchy with the pivoted row generators) or
+// R P^T (RRQR, dense); an uncompressed block gives the whole column block A * H(:, C).
+void build_rounds_split(const Plan& P, const psmma_batch_item* items, int count, int compressor, const int* ranks,
+                        double alpha, double beta, Rounds& R) {
+  // the off-diagonal block whose columns are C1 (rows R2) and C2 (rows R1), per item
+  std::vector<int> blk_c1(count, -1), blk_c2(count, -1);
+  for (int b = 0; b < (int)P.blocks.size(); ++b) {
+    const OffBlock& ob = P.blocks[b];
+    (ob.c0 == 0 ? blk_c1 : blk_c2)[ob.item] = b;
+  }
+  for (int b = 0; b < (int)P.blocks.size(); ++b) {
+    const OffBlock& ob = P.blocks[b];
+    const psmma_batch_item& it = items[ob.item];
+    const int n = it.n, mn = std::min(ob.M, ob.N), Rk = ranks[b];
+    if (Rk >= mn) {
+      ++R.full_blocks;
+      continue;
+    }
+    R.max_rank = std::max(R.max_rank, Rk);
+    if (Rk == 0) continue;
+    double* T = P.gather[b];
+    if (compressor == PSMMA_COMPRESS_RRLU) {
+      const RrluBlock& r = P.lu[b];
+      GenSpec gz;  // Z'(t, j) = U(Rk+t) W(j) / (LD(Rk+t) - LD(j)): T0 += Ar * Z'
+      gz.kind = KIND_CAUCHY;
+      gz.Dr = r.D + Rk;
+      gz.Ur = r.U + Rk;
+      gz.Fc = r.D;
+      gz.Vc = r.W;
+      if (ob.M - Rk > 0) {
+        R.r1.push_back(SplitProblem{n, Rk, ob.M - Rk, 1.0, 1.0, T + (size_t)n * Rk, n, gz, T, n});
+        R.executed += 2.0 * n * (double)(ob.M - Rk) * Rk;
+      }
+    } else {
+      GenSpec gq;  // T = A(:, R) * Q(:, 1:Rk)
+      gq.kind = KIND_DENSE;
+      gq.B = P.qr[b].T;
+      gq.ldb = ob.M;
+      R.r1.push_back(SplitProblem{n, Rk, ob.M, 1.0, 0.0, it.A + (long)ob.r0 * it.lda, it.lda, gq, T, n});
+      R.executed += 2.0 * n * (double)ob.M * Rk;
+    }
+  }
+  for (int i = 0; i < count; ++i) {
+    const psmma_batch_item& it = items[i];
+    const int n = it.n, h = n / 2;
+    if (n == 0) continue;
+    for (int half = 0; half < 2; ++half) {
+      const int d0 = half == 0 ? 0 : h, dn = half == 0 ? h : n - h;  // R_d = C = [d0, d0 + dn)
+      if (dn == 0) continue;
+      double* Qc = it.Q + (long)d0 * it.ldq;
+      const int b = half == 0 ? blk_c1[i] : blk_c2[i];
+      const int Rk = b >= 0 ? ranks[b] : 0;
+      const int mn = b >= 0 ? std::min(P.blocks[b].M, P.blocks[b].N) : 0;
+      if (b >= 0 && Rk >= mn) {
+        // uncompressed: the whole column block A * H(:, C)
+        R.r2.push_back(SplitProblem{n, dn, n, alpha, beta, it.A, it.lda, cauchy_sub(it.gen, it.ldgen, 0, d0), Qc,
+                                    it.ldq});
+        R.executed += 2.0 * n * (double)n * dn;
+        continue;
+      }
+      SplitProblem q{n, dn, dn + Rk, alpha, beta, it.A + (long)d0 * it.lda, it.lda,
+                     cauchy_sub(it.gen, it.ldgen, d0, d0), Qc, it.ldq};
+      if (Rk > 0) {
+        q.A2 = P.gather[b];
+        q.lda2 = n;
+        q.ka = dn;
+        q.gs.k1 = dn;
+        if (compressor == PSMMA_COMPRESS_RRLU) {
+          q.gs.Dr2 = P.lu[b].D;  // LD(1:Rk)
+          q.gs.Ur2 = P.lu[b].A;  // LU(1:Rk)
+        } else {
+          q.gs.B = P.qr[b].F;  // R P^T (Rk x N, ld Rk)
+          q.gs.ldb = Rk;
+        }
+      }
+      R.r2.push_back(q);
+      R.executed += 2.0 * n * (double)dn * (dn + Rk);
+    }
+  }
+}
+
 // Workspace of the product rounds (part B).
 struct RoundGroups {
   SplitGroup s1, s2;
@@ -921,42 +1161,91 @@ size_t rounds_bound(const Plan& P, const psmma_batch_item* items, int count, int
     full[b] = mn;
   }
   Rounds a, f;
-  build_rounds(P, items, count, compressor, rk.data(), 1.0, 0.0, a);
-  build_rounds(P, items, count, compressor, full.data(), 1.0, 0.0, f);
+  auto build = precision == PSMMA_PREC_SPLIT ? build_rounds_split : build_rounds;
+  build(P, items, count, compressor, rk.data(), 1.0, 0.0, a);
+  build(P, items, count, compressor, full.data(), 1.0, 0.0, f);
   return rounds_bytes(a, precision, n_moduli) + rounds_bytes(f, precision, n_moduli);
 }
 
-// Cooperative launch of the grouped QR over the tiles [t0, t1): every tile gets at least one
-// CTA and the rest in proportion to M * N.
-int launch_rrqr_wave(Plan& P, int t0, int t1, int grid, int* h_map, int* d_map, double tol, unsigned* status,
-                     cudaStream_t st) {
-  const int nt = t1 - t0;  // <= grid
+// Work assignment of the grouped QR over `grid` co-resident CTAs: a tile of work w = M N gets
+// a group of round(w / W) CTAs (W = total / grid) when that is >= 2; the other tiles are
+// packed onto the remaining CTAs, largest first onto the least loaded (each alone on its CTA).
+int launch_rrqr(Plan& P, int grid, double tol, unsigned* status, cudaStream_t st) {
+  const int nb = (int)P.qr.size();
   double wsum = 0.0;
-  for (int b = t0; b < t1; ++b) wsum += (double)P.qr[b].M * P.qr[b].N;
-  int next = 0;
-  const int spare = grid - nt;
-  for (int b = t0; b < t1; ++b) {
-    QrTile& q = P.qr[b];
-    int extra = wsum > 0 ? (int)((double)spare * ((double)q.M * q.N) / wsum) : 0;
-    extra = std::min(extra, std::max(0, q.N / QR_WARPS - 1));  // at least a column per warp
-    q.cta0 = next;
-    q.ncta = 1 + extra;
-    for (int c = 0; c < q.ncta; ++c) h_map[next + c] = b;
-    next += q.ncta;
+  for (const QrTile& q : P.qr) wsum += (double)q.M * q.N;
+  const double W = wsum / grid;
+  std::vector<int> ncta(nb, 0);
+  int dedicated = 0;
+  for (int b = 0; b < nb; ++b) {
+    const QrTile& q = P.qr[b];
+    int c = (int)std::lround((double)q.M * q.N / W);
+    c = std::min(c, std::max(1, q.N / QR_WARPS));  // at least a column per warp
+    ncta[b] = c >= 2 ? c : 0;
+    dedicated += ncta[b];
   }
-  for (int c = next; c < grid; ++c) h_map[c] = -1;
-  if (cudaMemcpyAsync(P.d_qr + t0, P.qr.data() + t0, sizeof(QrTile) * (t1 - t0), cudaMemcpyHostToDevice, st) !=
-          cudaSuccess ||
-      cudaMemcpyAsync(d_map, h_map, sizeof(int) * grid, cudaMemcpyHostToDevice, st) != cudaSuccess)
+  int packable = 0;
+  for (int b = 0; b < nb; ++b) packable += ncta[b] == 0;
+  // leave at least one CTA per eight packed tiles (and one at all)
+  const int reserve = packable ? std::max(1, std::min(packable, grid / 8)) : 0;
+  while (dedicated > grid - reserve) {
+    int big = -1;
+    for (int b = 0; b < nb; ++b)
+      if (ncta[b] > 2 && (big < 0 || ncta[b] > ncta[big])) big = b;
+    if (big < 0) break;
+    --ncta[big];
+    --dedicated;
+  }
+  if (dedicated > grid - reserve) {  // too many groups: every tile alone
+    for (int b = 0; b < nb; ++b) ncta[b] = 0;
+    dedicated = 0;
+  }
+  std::vector<std::vector<int>> lists(grid);
+  int next = 0;
+  for (int b = 0; b < nb; ++b)
+    if (ncta[b] >= 2) {
+      P.qr[b].cta0 = next;
+      P.qr[b].ncta = ncta[b];
+      for (int c = 0; c < ncta[b]; ++c) lists[next + c].push_back(b);
+      next += ncta[b];
+    }
+  const int free0 = next, nfree = grid - next;
+  std::vector<int> small;
+  for (int b = 0; b < nb; ++b)
+    if (ncta[b] < 2) small.push_back(b);
+  std::sort(small.begin(), small.end(), [&](int a, int b) {
+    return (double)P.qr[a].M * P.qr[a].N > (double)P.qr[b].M * P.qr[b].N;
+  });
+  std::vector<double> load(std::max(1, nfree), 0.0);
+  for (int b : small) {
+    int c = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+    load[c] += (double)P.qr[b].M * P.qr[b].N;
+    P.qr[b].cta0 = free0 + c;
+    P.qr[b].ncta = 1;
+    lists[free0 + c].push_back(b);
+  }
+  std::vector<int> h_start(grid + 1, 0), h_list;
+  for (int c = 0; c < grid; ++c) {
+    h_start[c] = (int)h_list.size();
+    for (int b : lists[c]) h_list.push_back(b);
+  }
+  h_start[grid] = (int)h_list.size();
+  // a tile of a group appears once per CTA of the group: at most grid + nb entries
+  if (grid + 1 + (int)h_list.size() > Plan::MAP_MAX + nb) return PSMMA_EUNSUPPORTED;
+  int* d_start = P.d_map;
+  int* d_list = P.d_map + grid + 1;
+  if (cudaMemcpyAsync(P.d_qr, P.qr.data(), sizeof(QrTile) * nb, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      cudaMemcpyAsync(d_start, h_start.data(), sizeof(int) * (grid + 1), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      cudaMemcpyAsync(d_list, h_list.data(), sizeof(int) * h_list.size(), cudaMemcpyHostToDevice, st) != cudaSuccess)
     return PSMMA_EDEVICE;
   QrTile* tiles = P.d_qr;
-  const int* map = d_map;
-  void* args[] = {(void*)&tiles, (void*)&map, (void*)&tol, (void*)&status};
-  if (cudaLaunchCooperativeKernel((const void*)k_rrqr_grouped, dim3(next), dim3(QR_THREADS), args, 0, st) !=
+  const int* ps = d_start;
+  const int* pl = d_list;
+  void* args[] = {(void*)&tiles, (void*)&ps, (void*)&pl, (void*)&tol, (void*)&status};
+  if (cudaLaunchCooperativeKernel((const void*)k_rrqr_grouped, dim3(grid), dim3(QR_THREADS), args, 0, st) !=
       cudaSuccess)
     return PSMMA_EDEVICE;
-  // the host copies of the map and tiles are reused by the next wave: wait for this one
-  return cudaStreamSynchronize(st) == cudaSuccess ? PSMMA_OK : PSMMA_EDEVICE;
+  return PSMMA_OK;
 }
 
 int check_batch(int count, const psmma_batch_item* items, int precision, int n_moduli, int compressor,
@@ -1038,8 +1327,49 @@ extern "C" int psmma_cauchy_batch_lowrank(int count, const psmma_batch_item* ite
   if (nb && compressor == PSMMA_COMPRESS_RRLU) {
     if (cudaMemcpyAsync(P.d_lu, P.lu.data(), sizeof(RrluBlock) * nb, cudaMemcpyHostToDevice, st) != cudaSuccess)
       return PSMMA_EDEVICE;
-    k_rrlu_cauchy<<<nb, RRLU_THREADS, 0, st>>>(P.d_lu, tol);
+    if (cudaMemsetAsync(P.d_pending, 0, sizeof(int), st) != cudaSuccess) return PSMMA_EDEVICE;
+    k_rrlu_cauchy<<<nb, RRLU_THREADS, 0, st>>>(P.d_lu, tol, P.d_pending);
     if (cudaGetLastError() != cudaSuccess) return PSMMA_EDEVICE;
+    // every resume advances some block by at least one step, so the loop is bounded
+    int max_iter = 2;
+    for (const OffBlock& ob : P.blocks) max_iter = std::max(max_iter, std::min(ob.M, ob.N) + 2);
+    std::vector<RrluBlock> cur(nb);
+    std::vector<CpChunk> chunks;
+    std::vector<int> cpblk, cpfirst;
+    int iter = 0;
+    for (; iter < max_iter; ++iter) {
+      int pend = 0;
+      if (cudaMemcpyAsync(&pend, P.d_pending, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+          cudaMemcpyAsync(cur.data(), P.d_lu, sizeof(RrluBlock) * nb, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+          cudaStreamSynchronize(st) != cudaSuccess)
+        return PSMMA_EDEVICE;
+      if (pend == 0) break;
+      chunks.clear();
+      cpblk.clear();
+      cpfirst.clear();
+      for (int b = 0; b < nb; ++b) {
+        if (cur[b].phase != 1) continue;
+        cpblk.push_back(b);
+        cpfirst.push_back((int)chunks.size());
+        for (int c = cur[b].k_next - 1; c < cur[b].N; c += Plan::CP_COLS)
+          chunks.push_back(CpChunk{b, c, std::min(cur[b].N, c + Plan::CP_COLS)});
+      }
+      if (chunks.empty() || (int)chunks.size() > P.chunk_cap) return PSMMA_EDEVICE;
+      if (cudaMemcpyAsync(P.d_chunks, chunks.data(), sizeof(CpChunk) * chunks.size(), cudaMemcpyHostToDevice,
+                          st) != cudaSuccess ||
+          cudaMemcpyAsync(P.d_cpblk, cpblk.data(), sizeof(int) * cpblk.size(), cudaMemcpyHostToDevice, st) !=
+              cudaSuccess ||
+          cudaMemcpyAsync(P.d_cpfirst, cpfirst.data(), sizeof(int) * cpfirst.size(), cudaMemcpyHostToDevice, st) !=
+              cudaSuccess ||
+          cudaMemsetAsync(P.d_pending, 0, sizeof(int), st) != cudaSuccess)
+        return PSMMA_EDEVICE;
+      k_cp_search<<<(unsigned)chunks.size(), RRLU_THREADS, 0, st>>>(P.d_lu, P.d_chunks, P.d_cand);
+      k_cp_reduce<<<((int)cpblk.size() + 127) / 128, 128, 0, st>>>(P.d_lu, P.d_cpblk, P.d_cpfirst, (int)cpblk.size(),
+                                                                   (int)chunks.size(), P.d_cand);
+      k_rrlu_cauchy<<<nb, RRLU_THREADS, 0, st>>>(P.d_lu, tol, P.d_pending);
+      if (cudaGetLastError() != cudaSuccess) return PSMMA_EDEVICE;
+    }
+    if (iter == max_iter) return PSMMA_EDEVICE;
     if (cudaMemcpyAsync(ranks.data(), P.d_ranks, sizeof(int) * nb, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
         cudaStreamSynchronize(st) != cudaSuccess)
       return PSMMA_EDEVICE;
@@ -1055,12 +1385,9 @@ extern "C" int psmma_cauchy_batch_lowrank(int count, const psmma_batch_item* ite
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_rrqr_grouped, QR_THREADS, 0) != cudaSuccess || occ < 1)
       return PSMMA_EDEVICE;
-    const int grid = std::min(sms * std::min(occ, 4), Plan::MAP_MAX);
-    std::vector<int> h_map(grid);
-    for (int t0 = 0; t0 < nb; t0 += grid) {
-      rc = launch_rrqr_wave(P, t0, std::min(nb, t0 + grid), grid, h_map.data(), P.d_map, tol, qr_status, st);
-      if (rc) return rc;
-    }
+    const int grid = std::min(sms * std::min(occ, 4), Plan::MAP_MAX - 1);
+    rc = launch_rrqr(P, grid, tol, qr_status, st);
+    if (rc) return rc;
     unsigned qs = 0;
     if (cudaMemcpyAsync(&qs, qr_status, sizeof(unsigned), cudaMemcpyDeviceToHost, st) != cudaSuccess)
       return PSMMA_EDEVICE;
@@ -1080,7 +1407,8 @@ extern "C" int psmma_cauchy_batch_lowrank(int count, const psmma_batch_item* ite
 
   // ---- phase 2: the product rounds, one CUDA graph
   Rounds R;
-  build_rounds(P, items, count, compressor, ranks.data(), alpha, beta, R);
+  (precision == PSMMA_PREC_SPLIT ? build_rounds_split : build_rounds)(P, items, count, compressor, ranks.data(),
+                                                                      alpha, beta, R);
   const size_t need_b = rounds_bytes(R, precision, n_moduli);
   if (!work_b) {
     work_b = (char*)pool_get(need_b, st, &rc, 1);

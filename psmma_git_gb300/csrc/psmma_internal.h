@@ -18,6 +18,9 @@ enum Kind { KIND_CAUCHY = 0, KIND_TOEPLITZ = 1, KIND_HANKEL = 2, KIND_DFT = 3, K
 //   Hankel    H(i,j) = g[i + j]                        (sub-blocks: g offset by r0 + c0)
 //   DFT       embedding of F = (w^(r c mod n_dft)), table wtab (t < n_dft)
 //   Dense     H(i,j) = B[i + j*ldb]                   (explicit factors of the low-rank path)
+// Split path only: a Cauchy H with k1 > 0 has a tail of rows i >= k1, either dense
+// (B[(i-k1) + j*ldb]) or Cauchy with its own row generators (Dr2, Ur2 at i - k1) and the
+// same column generators.
 struct GenSpec {
   int kind = KIND_CAUCHY;
   const double *Dr = nullptr, *Ur = nullptr, *Fc = nullptr, *Vc = nullptr;
@@ -27,6 +30,8 @@ struct GenSpec {
   int n_dft = 0;
   const double* B = nullptr;
   long ldb = 0;
+  int k1 = 0;
+  const double *Dr2 = nullptr, *Ur2 = nullptr;
 };
 
 // The generators of the reference's square H (k x k) from its storage conventions: Cauchy
@@ -83,6 +88,9 @@ struct SplitProblem {
   GenSpec gs;
   double* Q;
   long ldq;
+  const double* A2 = nullptr;  // columns k >= ka of A come from A2 (ld lda2) at k - ka
+  long lda2 = 0;
+  int ka = 0;                  // 0: A alone
 };
 struct SplitGroup {
   int count = 0, nmod = 0, group_m = 12;

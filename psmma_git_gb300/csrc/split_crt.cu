@@ -179,7 +179,14 @@ constexpr unsigned long long INF_BITS = 0x7FF0000000000000ull;
 
 // Row max of |A| as the bits of a non-negative double (NaN/Inf compare above all finite) and
 // row sums of squares (for the Cauchy-Schwarz bound of the integer product).
-__device__ __forceinline__ void row_absmax_blk(const double* __restrict__ A, long lda, int n, int k, int kchunk,
+// Columns kk >= ka of A come from A2 (ld lda2) at kk - ka (ka = k: A alone).
+__device__ __forceinline__ const double* acol(const double* A, long lda, const double* A2, long lda2, int ka,
+                                              int kk) {
+  return kk < ka ? A + (long)kk * lda : A2 + (long)(kk - ka) * lda2;
+}
+
+__device__ __forceinline__ void row_absmax_blk(const double* __restrict__ A, long lda, const double* A2, long lda2,
+                                               int ka, int n, int k, int kchunk,
                                                unsigned long long* __restrict__ amax_bits,
                                                double* __restrict__ asq, int bx, int by) {
   int i = bx * blockDim.x + threadIdx.x;
@@ -188,7 +195,7 @@ __device__ __forceinline__ void row_absmax_blk(const double* __restrict__ A, lon
   unsigned long long mb = 0;
   double sq = 0.0;
   for (int kk = k0; kk < k1; ++kk) {
-    const double a = __ldg(A + i + (long)kk * lda);
+    const double a = __ldg(acol(A, lda, A2, lda2, ka, kk) + i);
     unsigned long long b = (unsigned long long)__double_as_longlong(a) & ABS_MASK;
     mb = b > mb ? b : mb;
     sq = fma(a, a, sq);
@@ -199,7 +206,7 @@ __device__ __forceinline__ void row_absmax_blk(const double* __restrict__ A, lon
 
 __global__ void k_row_absmax(const double* __restrict__ A, long lda, int n, int k, int kchunk,
                              unsigned long long* __restrict__ amax_bits, double* __restrict__ asq) {
-  row_absmax_blk(A, lda, n, k, kchunk, amax_bits, asq, blockIdx.x, blockIdx.y);
+  row_absmax_blk(A, lda, nullptr, 0, k, n, k, kchunk, amax_bits, asq, blockIdx.x, blockIdx.y);
 }
 
 // H pass 1: Ht[j][kk] = H(kk, j) in FP64, column max |H| and column sum |H|, and the global
@@ -220,8 +227,13 @@ __device__ __forceinline__ void h_pass1_blk(const GenSpec& gs, int K, int kp, do
     double h = 0.0;
     if (kk < K) {
       if (KIND == KIND_CAUCHY) {
-        double d = __ldg(gs.Dr + kk), u = __ldg(gs.Ur + kk);
-        h = (u * v) / (d - w);        // U(i)*V(j) / (D(i)-F(j))
+        if (gs.k1 > 0 && kk >= gs.k1) {
+          const int t = kk - gs.k1;  // tail rows: dense, or Cauchy with the second row generators
+          h = gs.B ? __ldg(gs.B + t + (long)j * gs.ldb) : (__ldg(gs.Ur2 + t) * v) / (__ldg(gs.Dr2 + t) - w);
+        } else {
+          double d = __ldg(gs.Dr + kk), u = __ldg(gs.Ur + kk);
+          h = (u * v) / (d - w);        // U(i)*V(j) / (D(i)-F(j))
+        }
       } else if (KIND == KIND_TOEPLITZ) {
         h = __ldg(gs.g + (gs.order - 1) + j - kk);
       } else if (KIND == KIND_HANKEL) {
@@ -427,7 +439,8 @@ __device__ __forceinline__ void write_residue_pair(unsigned long long u0, bool n
 }
 
 // RA[l][i][kk] = residues of A' (bf16), rows i, K-major.  Block: 32 rows x 64 k.
-__device__ __forceinline__ void residues_A_blk(const double* __restrict__ A, long lda, int n, int k, int kp,
+__device__ __forceinline__ void residues_A_blk(const double* __restrict__ A, long lda, const double* A2, long lda2,
+                                               int ka, int n, int k, int kp,
                                                const unsigned long long* __restrict__ amax_bits,
                                                const SplitDevParams* prm, const CrtConsts& cc,
                                                __nv_bfloat16* __restrict__ RA, int bx, int by) {
@@ -436,7 +449,7 @@ __device__ __forceinline__ void residues_A_blk(const double* __restrict__ A, lon
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 256 threads: 8 x 32
   for (int kk = ty; kk < 64; kk += 8) {
     int gi = i0 + tx, gk = k0 + kk;
-    tile[kk][tx] = (gi < n && gk < k) ? __ldg(A + gi + (long)gk * lda) : 0.0;
+    tile[kk][tx] = (gi < n && gk < k) ? __ldg(acol(A, lda, A2, lda2, ka, gk) + gi) : 0.0;
   }
   __syncthreads();
   const int P = prm->PA;
@@ -459,7 +472,7 @@ __device__ __forceinline__ void residues_A_blk(const double* __restrict__ A, lon
 __global__ void k_residues_A(const double* __restrict__ A, long lda, int n, int k, int kp,
                              const unsigned long long* __restrict__ amax_bits, const SplitDevParams* prm,
                              CrtConsts cc, __nv_bfloat16* __restrict__ RA) {
-  residues_A_blk(A, lda, n, k, kp, amax_bits, prm, cc, RA, blockIdx.x, blockIdx.y);
+  residues_A_blk(A, lda, nullptr, 0, k, n, k, kp, amax_bits, prm, cc, RA, blockIdx.x, blockIdx.y);
 }
 
 // RH[l][j][kk] = residues of H' (bf16) from Ht[j][kk]; one thread per 2 consecutive kk.
@@ -1224,6 +1237,9 @@ struct GProb {
   double alpha, beta;
   const double* A;
   long lda;
+  const double* A2;
+  long lda2;
+  int ka;
   GenSpec gs;
   double* Q;
   long ldq;
@@ -1253,7 +1269,7 @@ constexpr int G_ROW_KCHUNK = 1024;
 __global__ void __launch_bounds__(128) k_g_row_absmax(const GProb* d, int count) {
   const GProb& e = d[gfind<0>(d, count, blockIdx.x)];
   const int local = blockIdx.x - e.b_row, gx = (e.M + 127) / 128;
-  row_absmax_blk(e.A, e.lda, e.M, e.K, G_ROW_KCHUNK, e.amax, e.asq, local % gx, local / gx);
+  row_absmax_blk(e.A, e.lda, e.A2, e.lda2, e.ka, e.M, e.K, G_ROW_KCHUNK, e.amax, e.asq, local % gx, local / gx);
 }
 
 __global__ void __launch_bounds__(256) k_g_h_pass1(const GProb* d, int count) {
@@ -1275,7 +1291,7 @@ __global__ void __launch_bounds__(1024) k_g_split_params(const GProb* d, double 
 __global__ void __launch_bounds__(256) k_g_residues_A(const GProb* d, int count, CrtConsts cc) {
   const GProb& e = d[gfind<2>(d, count, blockIdx.x)];
   const int local = blockIdx.x - e.b_ra, gx = e.kp / 64;
-  residues_A_blk(e.A, e.lda, e.M, e.K, e.kp, e.amax, e.prm, cc, e.RA, local % gx, local / gx);
+  residues_A_blk(e.A, e.lda, e.A2, e.lda2, e.ka, e.M, e.K, e.kp, e.amax, e.prm, cc, e.RA, local % gx, local / gx);
 }
 
 __global__ void __launch_bounds__(128) k_g_residues_H(const GProb* d, int count, CrtConsts cc) {
@@ -1325,6 +1341,8 @@ int plan_group(const SplitProblem* P, int count, int nmod, int narrow_max, int g
     e.kr = (q.N + e.bn - 1) / e.bn * e.bn;
     e.alpha = q.alpha; e.beta = q.beta;
     e.A = q.A; e.lda = q.lda; e.gs = q.gs; e.Q = q.Q; e.ldq = q.ldq;
+    e.A2 = q.A2; e.lda2 = q.lda2;
+    e.ka = (q.ka > 0 && q.A2) ? q.ka : q.K;
     e.prm = w.take<SplitDevParams>(1, 256);
     e.amax = w.take<unsigned long long>(q.M, 256);
     e.asq = w.take<double>(q.M, 256);

@@ -144,3 +144,22 @@ def test_batch_workspace_and_caller_buffer():
     with pytest.raises(PsmmaError) as e:
         cauchy_batch_lowrank(dev, 1.0, 0.0, compressor="rrqr", work=small)
     assert e.value.status == _lib.PSMMA_EWORKSPACE
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("comp", ["rrqr", "rrlu"])
+@pytest.mark.parametrize("prec", ["fp64", "split"])
+def test_batch_uncompressed_blocks_use_the_generated_tile(comp, prec):
+    # tol so small that no block truncates: every off-diagonal block is multiplied as the
+    # generated tile (the reference would multiply a stale buffer there)
+    import torch
+    from psmma_git_gb300 import cauchy_batch_lowrank
+    problems = _problems([3, 37, 129], seed=21)
+    dev = _to_dev(problems)
+    ranks, info = cauchy_batch_lowrank(dev, 0.5, 2.0, compressor=comp, tol=1e-300, precision=prec)
+    torch.cuda.synchronize()
+    assert info["full_rank_blocks"] == len(ranks) == 6
+    tol = 1e-13 if prec == "fp64" else 1e-12
+    for (A, g, Q0), (_, _, Qd) in zip(problems, dev):
+        exact = 0.5 * A @ O.dense_h("cauchy", g, A.shape[0]) + 2.0 * Q0
+        assert O.rel_fro(Qd.cpu().numpy(), exact) < tol
