@@ -488,6 +488,9 @@ def run_merge_level(args, ws, rank, local):
     for comp in ["rrqr", "rrlu"]:
         for prec in precisions:
             kw = dict(compressor=comp, tol=1e-14, precision=prec, n_moduli=args.n_moduli)
+            tuned = None
+            if prec == "split" and not args.no_tune:
+                tuned = P.tune_batch(probs, 1.0, 0.0, **kw)  # untimed; later calls use its choice
             for _ in range(args.warmup if prec == "split" else 1):
                 ranks, info = P.cauchy_batch_lowrank(probs, 1.0, 0.0, **kw)
             torch.cuda.synchronize()
@@ -519,7 +522,7 @@ def run_merge_level(args, ws, rank, local):
                 "executed_flops": info["executed_flops"], "compress_flops": info["compress_flops"],
                 "ranks": {"max": int(max(ranks)), "mean": float(np.mean(ranks)), "min": int(min(ranks))},
                 "full_rank_blocks": info["full_rank_blocks"], "rel_err_vs_dense_fp64": err,
-                "phases_ms": phases}
+                "autotune": tuned, "phases_ms": phases}
             print(json.dumps({comp + "_" + prec: out[f"{comp}_{prec}"]}), file=sys.stderr, flush=True)
     # CPU baseline: the oracle's restatement of the merge level (Compress_RRQR + DGEMMs) on the
     # smallest problems until ~args.cpu_seconds of work
@@ -587,6 +590,7 @@ def main():
     ap.add_argument("--batch-check", type=int, default=8)
     ap.add_argument("--merge-fp64", action="store_true", help="also time the FP64 path of the merge level")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-tune", action="store_true", help="merge level: skip the grouped-GEMM autotuner")
     args = ap.parse_args()
     ws, rank, local = dist_init(args)
     if args.impl == "reference":

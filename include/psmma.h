@@ -173,6 +173,24 @@ typedef struct psmma_batch_stats {
 int psmma_cauchy_batch_lowrank(int count, const psmma_batch_item* items, double alpha, double beta,
                                int compressor, double tol, const psmma_opts* opts, int* ranks_out,
                                psmma_batch_stats* stats, void* stream);
+/* No counterpart in the reference.  Autotuner of the split path's grouped GEMM (output-tile
+ * widths 64/128/256 by product width, raster group): times psmma_cauchy_batch_lowrank on
+ * this batch for each candidate configuration and keeps the fastest for batches of the same
+ * signature (count, precision, moduli, compressor and the sizes in 1/8-octave bins); later
+ * calls with that signature use it.  With the environment variable PSMMA_TUNE_CACHE naming a
+ * file, results are appended there and read back by later processes.  Runs the batch about
+ * 40 times: the Q_i are overwritten (meaningless afterwards when beta != 0).  The FP64 path
+ * has one tile shape: returns at once. */
+typedef struct psmma_tune_result {
+  int narrow_max, mid_max, group_m;  /* chosen: width 64 for N <= narrow_max, 128 for N <= mid_max */
+  int candidates;                    /* configurations timed */
+  float ms_best, ms_default;          /* batch time of the chosen and of the default configuration */
+} psmma_tune_result;
+
+int psmma_tune_batch(int count, const psmma_batch_item* items, double alpha, double beta,
+                     int compressor, double tol, const psmma_opts* opts, psmma_tune_result* out,
+                     void* stream);
+
 /* Bytes of workspace psmma_cauchy_batch_lowrank needs for this batch (for opts->work). */
 size_t psmma_batch_workspace_size(int count, const psmma_batch_item* items, int compressor,
                                   const psmma_opts* opts);

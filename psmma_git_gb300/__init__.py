@@ -26,13 +26,13 @@ import ctypes as C
 import numpy as np
 
 from ._lib import (COMPRESS_RRLU, COMPRESS_RRQR, KIND_CAUCHY, KIND_DFT, KIND_HANKEL, KIND_TOEPLITZ,
-                   PREC_FP64, PREC_SPLIT, PsmmaBatchItem, PsmmaBatchStats, PsmmaError, PsmmaOpts, load,
-                   status_string)
+                   PREC_FP64, PREC_SPLIT, PsmmaBatchItem, PsmmaBatchStats, PsmmaError, PsmmaOpts,
+                   PsmmaTuneResult, load, status_string)
 
 __all__ = [
     "psmma_cauchy", "psmma_toeplitz", "psmma_hankel", "pzmdftl", "pzmdftl1", "fortran_empty",
     "workspace_size", "PsmmaError", "PREC_FP64", "PREC_SPLIT", "load", "status_string",
-    "make_opts", "cauchy_batch_lowrank", "batch_workspace_size",
+    "make_opts", "cauchy_batch_lowrank", "batch_workspace_size", "tune_batch",
 ]
 
 # The split path (exact modular slices on the BF16 tensor cores) is built into the library.
@@ -223,3 +223,19 @@ def batch_workspace_size(problems, *, compressor="rrqr", precision="fp64", n_mod
     opts = make_opts(precision, n_moduli)
     items = _batch_items(problems)
     return int(load().psmma_batch_workspace_size(len(problems), items, _COMPRESS[compressor], C.byref(opts)))
+
+
+def tune_batch(problems, alpha=1.0, beta=0.0, *, compressor="rrqr", tol=1e-14, precision="split", n_moduli=0,
+               stream=None) -> dict:
+    """Autotunes the grouped split GEMM on this batch (overwrites the Q_i) and returns the chosen
+    configuration; later cauchy_batch_lowrank calls on batches of the same signature use it."""
+    lib = load()
+    items = _batch_items(problems)
+    opts = make_opts(precision, n_moduli)
+    res = PsmmaTuneResult()
+    st = lib.psmma_tune_batch(len(problems), items, float(alpha), float(beta), _COMPRESS[compressor], float(tol),
+                              C.byref(opts), C.byref(res), _stream_ptr(stream))
+    if st != 0:
+        raise PsmmaError(st, "psmma_tune_batch")
+    return {"narrow_max": res.narrow_max, "mid_max": res.mid_max, "group_m": res.group_m,
+            "candidates": res.candidates, "ms_best": res.ms_best, "ms_default": res.ms_default}

@@ -75,6 +75,13 @@ class PsmmaBatchStats(C.Structure):
     ]
 
 
+class PsmmaTuneResult(C.Structure):
+    _fields_ = [
+        ("narrow_max", C.c_int), ("mid_max", C.c_int), ("group_m", C.c_int), ("candidates", C.c_int),
+        ("ms_best", C.c_float), ("ms_default", C.c_float),
+    ]
+
+
 _p = C.c_void_p
 _i = C.c_int
 _d = C.c_double
@@ -115,6 +122,7 @@ SIGNATURES = {
     "psmma_cauchy_batch_lowrank": (_i, [_i, C.POINTER(PsmmaBatchItem), _d, _d, _i, _d, _op, _ip,
                                         C.POINTER(PsmmaBatchStats), _p]),
     "psmma_batch_workspace_size": (C.c_size_t, [_i, C.POINTER(PsmmaBatchItem), _i, _op]),
+    "psmma_tune_batch": (_i, [_i, C.POINTER(PsmmaBatchItem), _d, _d, _i, _d, _op, C.POINTER(PsmmaTuneResult), _p]),
 }
 
 

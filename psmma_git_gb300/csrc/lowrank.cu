@@ -22,6 +22,11 @@
 
 #include <cooperative_groups.h>
 
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <map>
+#include <mutex>
 #include <vector>
 
 namespace psmma {
@@ -1114,7 +1119,7 @@ size_t rounds_bytes(const Rounds& R, int precision, int n_moduli) {
   return f64_group_bytes((int)R.r1.size()) * 2 + f64_group_bytes((int)R.r2.size()) * 2 + 4096;
 }
 
-int prepare_rounds(const Rounds& R, int precision, int n_moduli, int narrow_max, int group_m, void* work,
+int prepare_rounds(const Rounds& R, int precision, int n_moduli, const SplitTune& tune, void* work,
                    size_t lwork, cudaStream_t st, RoundGroups& G) {
   Bump b(work);
   if (precision == PSMMA_PREC_SPLIT) {
@@ -1123,8 +1128,8 @@ int prepare_rounds(const Rounds& R, int precision, int n_moduli, int narrow_max,
     char* w1 = b.take<char>(b1, 4096);
     char* w2 = b.take<char>(b2, 4096);
     if (b.off > lwork) return PSMMA_EWORKSPACE;
-    int rc = split_group_prepare(R.r1.data(), (int)R.r1.size(), n_moduli, narrow_max, group_m, w1, b1, st, &G.s1);
-    if (!rc) rc = split_group_prepare(R.r2.data(), (int)R.r2.size(), n_moduli, narrow_max, group_m, w2, b2, st, &G.s2);
+    int rc = split_group_prepare(R.r1.data(), (int)R.r1.size(), n_moduli, tune, w1, b1, st, &G.s1);
+    if (!rc) rc = split_group_prepare(R.r2.data(), (int)R.r2.size(), n_moduli, tune, w2, b2, st, &G.s2);
     return rc;
   }
   const std::vector<SplitProblem>* rs[2] = {&R.r1, &R.r2};
@@ -1274,9 +1279,75 @@ size_t part_a_bytes(Plan& P, const psmma_batch_item* items, int count, int compr
 
 }  // namespace
 
-// Tuning knobs of the grouped split GEMM (set by the autotuner): output-tile width 64 for
-// products with N <= narrow_max, raster group of group_m row tiles.
-static int g_narrow_max = 64, g_group_m = 12;
+// ------------------------------------------------------------------------------------------
+// Autotuner of the grouped split GEMM (tile widths, raster group): configurations are timed
+// on a whole batch and the best is kept per batch signature (and, with PSMMA_TUNE_CACHE set
+// to a file, across processes: one "signature narrow_max mid_max group_m" line each).
+// ------------------------------------------------------------------------------------------
+namespace {
+
+std::mutex g_tune_mu;
+std::map<unsigned long long, SplitTune> g_tune;
+bool g_tune_loaded = false;
+thread_local const SplitTune* t_force = nullptr;  // set while the tuner runs a candidate
+
+// FNV-1a of the batch shape: count, precision, moduli, compressor and the sizes binned at
+// 1/8 octave (batches of the same size distribution share a configuration).
+unsigned long long batch_signature(int count, const psmma_batch_item* items, int compressor, int precision,
+                                   int n_moduli) {
+  std::vector<int> bins;
+  for (int i = 0; i < count; ++i)
+    bins.push_back(items[i].n > 0 ? (int)std::lround(8.0 * std::log2((double)items[i].n)) : -1);
+  std::sort(bins.begin(), bins.end());
+  unsigned long long h = 1469598103934665603ull;
+  auto mix = [&](long long v) {
+    for (int b = 0; b < 8; ++b) {
+      h ^= (unsigned long long)((v >> (8 * b)) & 0xff);
+      h *= 1099511628211ull;
+    }
+  };
+  mix(count);
+  mix(precision);
+  mix(n_moduli);
+  mix(compressor);
+  for (int b : bins) mix(b);
+  return h;
+}
+
+void tune_load_locked() {
+  if (g_tune_loaded) return;
+  g_tune_loaded = true;
+  const char* path = std::getenv("PSMMA_TUNE_CACHE");
+  if (!path || !*path) return;
+  FILE* f = std::fopen(path, "r");
+  if (!f) return;
+  unsigned long long sig;
+  SplitTune t;
+  while (std::fscanf(f, "%llx %d %d %d", &sig, &t.narrow_max, &t.mid_max, &t.group_m) == 4) g_tune[sig] = t;
+  std::fclose(f);
+}
+
+SplitTune tune_for(unsigned long long sig) {
+  if (t_force) return *t_force;
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  tune_load_locked();
+  auto it = g_tune.find(sig);
+  return it == g_tune.end() ? SplitTune() : it->second;
+}
+
+void tune_store(unsigned long long sig, const SplitTune& t) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  tune_load_locked();
+  g_tune[sig] = t;
+  const char* path = std::getenv("PSMMA_TUNE_CACHE");
+  if (!path || !*path) return;
+  if (FILE* f = std::fopen(path, "a")) {
+    std::fprintf(f, "%llx %d %d %d\n", sig, t.narrow_max, t.mid_max, t.group_m);
+    std::fclose(f);
+  }
+}
+
+}  // namespace
 
 extern "C" size_t psmma_batch_workspace_size(int count, const psmma_batch_item* items, int compressor,
                                              const psmma_opts* opts) {
@@ -1416,7 +1487,8 @@ extern "C" int psmma_cauchy_batch_lowrank(int count, const psmma_batch_item* ite
     lwork_b = need_b;
   }
   RoundGroups G;
-  rc = prepare_rounds(R, precision, n_moduli, g_narrow_max, g_group_m, work_b, lwork_b, st, G);
+  const SplitTune tune = tune_for(batch_signature(count, items, compressor, precision, n_moduli));
+  rc = prepare_rounds(R, precision, n_moduli, tune, work_b, lwork_b, st, G);
   if (rc) return rc;
   std::vector<GatherDesc> gd;
   int gather_cols = 0;
@@ -1505,4 +1577,53 @@ extern "C" int psmma_cauchy_batch_lowrank(int count, const psmma_batch_item* ite
     stats->full_rank_blocks = R.full_blocks;
   }
   return rc;
+}
+
+extern "C" int psmma_tune_batch(int count, const psmma_batch_item* items, double alpha, double beta, int compressor,
+                                double tol, const psmma_opts* opts, psmma_tune_result* out, void* stream) {
+  const int precision = opts ? opts->precision : PSMMA_PREC_FP64;
+  const int n_moduli = opts ? opts->n_moduli : 0;
+  int rc = check_batch(count, items, precision, n_moduli, compressor, tol);
+  if (rc) return rc;
+  if (out) *out = psmma_tune_result{64, 128, 12, 0, 0.0f, 0.0f};
+  if (count == 0 || precision != PSMMA_PREC_SPLIT) return PSMMA_OK;  // FP64 path: one tile shape
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaEvent_t e0, e1;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return PSMMA_EDEVICE;
+  const SplitTune dflt;
+  const int widths[4][2] = {{0, 0}, {64, 0}, {64, 128}, {64, 256}};
+  const int groups[3] = {4, 8, 16};
+  std::vector<SplitTune> cands{dflt};
+  for (auto& w : widths)
+    for (int gm : groups) cands.push_back(SplitTune{w[0], w[1], gm});
+  float best = 0.0f, first = 0.0f;
+  SplitTune best_t = dflt;
+  for (size_t c = 0; c < cands.size() && !rc; ++c) {
+    t_force = &cands[c];
+    rc = psmma_cauchy_batch_lowrank(count, items, alpha, beta, compressor, tol, opts, nullptr, nullptr, stream);
+    float ms = 0.0f;
+    for (int rep = 0; rep < 2 && !rc; ++rep) {  // the faster of two timed runs (the first warmed up)
+      cudaEventRecord(e0, st);
+      rc = psmma_cauchy_batch_lowrank(count, items, alpha, beta, compressor, tol, opts, nullptr, nullptr, stream);
+      cudaEventRecord(e1, st);
+      float t = 0.0f;
+      if (!rc && (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&t, e0, e1) != cudaSuccess))
+        rc = PSMMA_EDEVICE;
+      ms = rep == 0 ? t : std::min(ms, t);
+    }
+    t_force = nullptr;
+    if (rc) break;
+    if (c == 0) first = ms;
+    if (c == 0 || ms < best) {
+      best = ms;
+      best_t = cands[c];
+    }
+  }
+  t_force = nullptr;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) return rc;
+  tune_store(batch_signature(count, items, compressor, precision, n_moduli), best_t);
+  if (out) *out = psmma_tune_result{best_t.narrow_max, best_t.mid_max, best_t.group_m, (int)cands.size(), best, first};
+  return PSMMA_OK;
 }

@@ -77,8 +77,7 @@ int launch_split_general(int M, int N, int K, double alpha, const double* A, lon
 
 // Grouped split path (split_crt.cu): independent real products of uneven sizes, each
 // Q = alpha * A * H + beta * Q (M, N, K >= 1; H from gs, not the DFT), run as one launch
-// per phase with one persistent modular GEMM per output-tile width (256, or 64 for products
-// with N <= narrow_max).  prepare lays out the workspace and copies the descriptors (not
+// per phase with one persistent modular GEMM per output-tile width (256, 128, 64).  prepare lays out the workspace and copies the descriptors (not
 // capturable: it copies from host memory); enqueue only launches kernels.
 struct SplitProblem {
   int M, N, K;
@@ -92,18 +91,23 @@ struct SplitProblem {
   long lda2 = 0;
   int ka = 0;                  // 0: A alone
 };
+// Tunables of the grouped GEMM: output-tile width 64 for products with N <= narrow_max, 128
+// for N <= mid_max, else 256; raster group of group_m row tiles.
+struct SplitTune {
+  int narrow_max = 64, mid_max = 128, group_m = 12;
+};
 struct SplitGroup {
   int count = 0, nmod = 0, group_m = 12;
   void* d_probs = nullptr;
-  void* d_gemm[2] = {nullptr, nullptr};
-  int n_gemm[2] = {0, 0}, tiles[2] = {0, 0};
+  void* d_gemm[3] = {nullptr, nullptr, nullptr};  // tile widths 256, 64, 128
+  int n_gemm[3] = {0, 0, 0}, tiles[3] = {0, 0, 0};
   int blocks_row = 0, blocks_h = 0, blocks_ra = 0, blocks_rh = 0, blocks_crt = 0;
   void* small = nullptr;
   size_t small_bytes = 0;
   unsigned* status = nullptr;
 };
 size_t split_group_bytes(const SplitProblem* P, int count, int n_moduli);
-int split_group_prepare(const SplitProblem* P, int count, int n_moduli, int narrow_max, int group_m, void* work,
+int split_group_prepare(const SplitProblem* P, int count, int n_moduli, const SplitTune& tune, void* work,
                         size_t lwork, cudaStream_t stream, SplitGroup* g);
 int split_group_enqueue(const SplitGroup& g, cudaStream_t stream, unsigned* status_out);
 

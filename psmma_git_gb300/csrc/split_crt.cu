@@ -1323,11 +1323,11 @@ struct WsBump {
 };
 
 // Lays out (and, with a real base, fills) the group's descriptors and buffers.
-int plan_group(const SplitProblem* P, int count, int nmod, int narrow_max, int group_m, WsBump& w,
+int plan_group(const SplitProblem* P, int count, int nmod, const SplitTune& tune, WsBump& w,
                std::vector<GProb>* probs, std::vector<GemmDesc>* gd, SplitGroup* g) {
   GProb* d_probs = w.take<GProb>(count, 256);
-  GemmDesc* d_g0 = w.take<GemmDesc>(count, 128);
-  GemmDesc* d_g1 = w.take<GemmDesc>(count, 128);
+  GemmDesc* d_gc[3];
+  for (int c = 0; c < 3; ++c) d_gc[c] = w.take<GemmDesc>(count, 128);
   // small region: status word, then per product params, maxima and sums (zeroed by one memset)
   const uintptr_t small0 = (w.off + 1023) & ~(uintptr_t)1023;
   unsigned* status = w.take<unsigned>(256, 1024);
@@ -1337,8 +1337,8 @@ int plan_group(const SplitProblem* P, int count, int nmod, int narrow_max, int g
     const SplitProblem& q = P[i];
     e.M = q.M; e.N = q.N; e.K = q.K;
     e.kp = (q.K + 63) / 64 * 64;
-    e.bn = (q.N <= narrow_max) ? 64 : 256;
-    e.kr = (q.N + e.bn - 1) / e.bn * e.bn;
+    e.bn = (q.N <= tune.narrow_max) ? 64 : (q.N <= tune.mid_max) ? 128 : 256;
+    e.kr = (q.N + 255) / 256 * 256;  // row stride of the residue products (any tile width)
     e.alpha = q.alpha; e.beta = q.beta;
     e.A = q.A; e.lda = q.lda; e.gs = q.gs; e.Q = q.Q; e.ldq = q.ldq;
     e.A2 = q.A2; e.lda2 = q.lda2;
@@ -1366,10 +1366,9 @@ int plan_group(const SplitProblem* P, int count, int nmod, int narrow_max, int g
   }
   g->count = count;
   g->nmod = nmod;
-  g->group_m = group_m;
+  g->group_m = tune.group_m;
   g->d_probs = d_probs;
-  g->d_gemm[0] = d_g0;
-  g->d_gemm[1] = d_g1;
+  for (int c = 0; c < 3; ++c) g->d_gemm[c] = d_gc[c];
   g->blocks_row = b_row; g->blocks_h = b_h; g->blocks_ra = b_ra; g->blocks_rh = b_rh; g->blocks_crt = b_crt;
   g->small = (void*)(w.base + small0);  // small0, small1 are offsets from the base
   g->small_bytes = small1 - small0;
@@ -1381,12 +1380,11 @@ int plan_group(const SplitProblem* P, int count, int nmod, int narrow_max, int g
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
     return (double)pr[a].M * pr[a].N * pr[a].K > (double)pr[b].M * pr[b].N * pr[b].K;
   });
-  gd[0].clear();
-  gd[1].clear();
-  int tiles[2] = {0, 0};
+  for (int c = 0; c < 3; ++c) gd[c].clear();
+  int tiles[3] = {0, 0, 0};
   for (int i : order) {
     const GProb& e = pr[i];
-    const int cls = e.bn == 64 ? 1 : 0;
+    const int cls = e.bn == 64 ? 1 : e.bn == 128 ? 2 : 0;
     GemmDesc x;
     memset(&x, 0, sizeof(x));
     if (!make_tmap(&x.ta, e.RA, e.kp, e.M, nmod, G_BM) || !make_tmap(&x.tb, e.RH, e.kp, e.N, nmod, e.bn))
@@ -1401,7 +1399,7 @@ int plan_group(const SplitProblem* P, int count, int nmod, int narrow_max, int g
     tiles[cls] += x.tiles_m * x.tiles_n * nmod;
     gd[cls].push_back(x);
   }
-  for (int c = 0; c < 2; ++c) {
+  for (int c = 0; c < 3; ++c) {
     g->n_gemm[c] = (int)gd[c].size();
     g->tiles[c] = tiles[c];
   }
@@ -1415,11 +1413,11 @@ size_t split_group_bytes(const SplitProblem* P, int count, int n_moduli) {
   if (count <= 0) return 0;
   SplitGroup g;
   WsBump w(nullptr);
-  plan_group(P, count, resolve_nmod(n_moduli), 64, 12, w, nullptr, nullptr, &g);
+  plan_group(P, count, resolve_nmod(n_moduli), SplitTune(), w, nullptr, nullptr, &g);
   return w.off + 4096;
 }
 
-int split_group_prepare(const SplitProblem* P, int count, int n_moduli, int narrow_max, int group_m, void* work,
+int split_group_prepare(const SplitProblem* P, int count, int n_moduli, const SplitTune& tune, void* work,
                         size_t lwork, cudaStream_t stream, SplitGroup* g) {
   const int nmod = resolve_nmod(n_moduli);
   if (nmod < 8 || nmod > SPL_MAX_MODULI) return PSMMA_EUNSUPPORTED;
@@ -1435,12 +1433,12 @@ int split_group_prepare(const SplitProblem* P, int count, int n_moduli, int narr
   if (!work || lwork < split_group_bytes(P, count, n_moduli)) return PSMMA_EWORKSPACE;
   WsBump w((void*)(((uintptr_t)work + 255) & ~(uintptr_t)255));
   std::vector<GProb> pr;
-  std::vector<GemmDesc> gd[2];
-  int st = plan_group(P, count, nmod, narrow_max, group_m, w, &pr, gd, g);
+  std::vector<GemmDesc> gd[3];
+  int st = plan_group(P, count, nmod, tune, w, &pr, gd, g);
   if (st) return st;
   if (cudaMemcpyAsync(g->d_probs, pr.data(), sizeof(GProb) * count, cudaMemcpyHostToDevice, stream) != cudaSuccess)
     return PSMMA_EDEVICE;
-  for (int c = 0; c < 2; ++c)
+  for (int c = 0; c < 3; ++c)
     if (!gd[c].empty() && cudaMemcpyAsync(g->d_gemm[c], gd[c].data(), sizeof(GemmDesc) * gd[c].size(),
                                           cudaMemcpyHostToDevice, stream) != cudaSuccess)
       return PSMMA_EDEVICE;
@@ -1491,6 +1489,8 @@ int split_group_enqueue(const SplitGroup& g, cudaStream_t stream, unsigned* stat
   prof_mark(stream, "g_residues_H");
   int st = launch_group_gemm<256>(g, 0, cc, sms, stream);
   prof_mark(stream, "g_gemm_256");
+  if (!st) st = launch_group_gemm<128>(g, 2, cc, sms, stream);
+  prof_mark(stream, "g_gemm_128");
   if (!st) st = launch_group_gemm<64>(g, 1, cc, sms, stream);
   prof_mark(stream, "g_gemm_64");
   if (st) return st;

@@ -163,3 +163,31 @@ def test_batch_uncompressed_blocks_use_the_generated_tile(comp, prec):
     for (A, g, Q0), (_, _, Qd) in zip(problems, dev):
         exact = 0.5 * A @ O.dense_h("cauchy", g, A.shape[0]) + 2.0 * Q0
         assert O.rel_fro(Qd.cpu().numpy(), exact) < tol
+
+
+def test_tuner_fp64_and_empty_batches_return_at_once(lib):
+    # no tunables on the FP64 path and nothing to do for an empty batch: no GPU work
+    items = (_lib.PsmmaBatchItem * 1)()
+    res = _lib.PsmmaTuneResult()
+    assert lib.psmma_tune_batch(0, items, 1.0, 0.0, 0, 1e-14, None, C.byref(res), None) == 0
+    o = _lib.PsmmaOpts()
+    o.precision = _lib.PREC_FP64
+    assert lib.psmma_tune_batch(0, items, 1.0, 0.0, 1, 1e-14, C.byref(o), C.byref(res), None) == 0
+    assert res.candidates == 0 and res.group_m > 0
+
+
+@pytest.mark.gpu
+def test_tuner_picks_a_configuration_and_results_stay_exact():
+    import torch
+    from psmma_git_gb300 import cauchy_batch_lowrank, tune_batch
+    problems = _problems([200, 700, 1500], seed=31)
+    dev = _to_dev(problems)
+    t = tune_batch(dev, compressor="rrlu", precision="split")
+    assert t["candidates"] >= 10 and t["ms_best"] > 0 and t["ms_best"] <= t["ms_default"] * 1.05
+    assert t["group_m"] in (4, 8, 12, 16)
+    dev = _to_dev(problems)
+    cauchy_batch_lowrank(dev, 1.0, 0.0, compressor="rrlu", precision="split")
+    torch.cuda.synchronize()
+    for (A, g, _), (_, _, Qd) in zip(problems, dev):
+        exact = A @ O.dense_h("cauchy", g, A.shape[0])
+        assert O.rel_fro(Qd.cpu().numpy(), exact) < 1e-12
