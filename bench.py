@@ -444,6 +444,91 @@ def run_serving(args, ws, rank, local):
     return 0
 
 
+def run_cfg1(args, ws, rank, local):
+    """Toeplitz, Hankel and DFT multiplies at n = k = 8192 (A uniform[-1,1], generator vector of
+    length 2n-1 uniform[-1,1]; DFT: complex B with both parts uniform[-1,1]) on the split path
+    (args.n_moduli) and the FP64 path.  Rates: 2n^3/t for Toeplitz/Hankel, 8n^3/t real flops
+    for the DFT (2n^3/t complex multiply-adds beside it).  Errors: split vs FP64 path on the
+    whole product, and both against the FFT-based oracle on a 256-row (DFT: 256-column)
+    sample.  One JSON line."""
+    import numpy as np
+    import torch
+    import psmma_git_gb300 as P
+    from oracle import psmma_oracle as O
+    if rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    n = k = args.cfg1_n
+    g = torch.Generator(device=dev)
+    g.manual_seed(5)
+    A = P.fortran_empty(n, k, torch.float64, dev)
+    A.copy_(torch.rand(k, n, generator=g, device=dev, dtype=torch.float64).mul_(2).sub_(1).t())
+    gv = torch.rand(2 * k - 1, generator=g, device=dev, dtype=torch.float64).mul_(2).sub_(1)
+    out = {}
+    for kind in ["toeplitz", "hankel", "dft"]:
+        if kind == "dft":
+            X = P.fortran_empty(n, k, torch.complex128, dev)
+            X.copy_(torch.complex(torch.rand(k, n, generator=g, device=dev, dtype=torch.float64) * 2 - 1,
+                                  torch.rand(k, n, generator=g, device=dev, dtype=torch.float64) * 2 - 1).t())
+            Y = P.fortran_empty(n, k, torch.complex128, dev)
+            Y64 = P.fortran_empty(n, k, torch.complex128, dev)
+            run = lambda prec, dst: P.pzmdftl(n, k, 1.0, X, 0.0, dst, precision=prec, n_moduli=args.n_moduli)
+            flops = 8.0 * n ** 3
+        else:
+            Y = P.fortran_empty(n, k, torch.float64, dev)
+            Y64 = P.fortran_empty(n, k, torch.float64, dev)
+            fn = P.psmma_toeplitz if kind == "toeplitz" else P.psmma_hankel
+            run = lambda prec, dst, fn=fn: fn(n, k, 1.0, A, gv, 0.0, dst, precision=prec, n_moduli=args.n_moduli)
+            flops = 2.0 * n ** 3
+        for _ in range(args.warmup):
+            run("split", Y)
+        torch.cuda.synchronize()
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+        e[0].record()
+        for i in range(args.steps):
+            run("split", Y)
+            e[i + 1].record()
+        torch.cuda.synchronize()
+        t = e[0].elapsed_time(e[args.steps]) / args.steps
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        run("fp64", Y64)
+        e1.record()
+        torch.cuda.synchronize()
+        t64 = e0.elapsed_time(e1)
+        rel = float(torch.linalg.norm(Y - Y64) / torch.linalg.norm(Y64))
+        if kind == "dft":
+            Xs = X[:, :256].cpu().numpy()
+            ref = O.dft_product(1.0, Xs, 0.0, None)
+            err_split = O.rel_fro(Y[:, :256].cpu().numpy(), ref)
+            err_64 = O.rel_fro(Y64[:, :256].cpu().numpy(), ref)
+        else:
+            As = np.ascontiguousarray(A[:256].cpu().numpy())
+            prod = O.toeplitz_product_fft if kind == "toeplitz" else O.hankel_product_fft
+            ref = prod(As, gv.cpu().numpy(), k)
+            err_split = O.rel_fro(Y[:256].cpu().numpy(), ref)
+            err_64 = O.rel_fro(Y64[:256].cpu().numpy(), ref)
+        out[kind] = {"split_ms": t, "split_tflops": flops / t / 1e9, "fp64_ms": t64,
+                     "fp64_tflops": flops / t64 / 1e9, "speedup": t64 / t,
+                     "rel_err_split_vs_fp64": rel, "rel_err_split_vs_fft_oracle_sample": err_split,
+                     "rel_err_fp64_vs_fft_oracle_sample": err_64}
+        if kind == "dft":
+            out[kind]["split_complex_mac_tflops"] = 2.0 * n ** 3 / t / 1e9
+        print(json.dumps({kind: out[kind]}), file=sys.stderr, flush=True)
+        del Y, Y64
+        torch.cuda.empty_cache()
+    line = {"metric": f"Toeplitz/Hankel/DFT A·C TFLOP/s n={n}, split vs FP64", "value": out["toeplitz"]["split_tflops"],
+            "unit": "TFLOP/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": out["toeplitz"]["split_ms"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64 (split: bf16 modular slices)", "data": "synthetic",
+            "config": {"workload": f"toeplitz/hankel/dft n=k={n}", "n_moduli": args.n_moduli,
+                       "l2": "inputs 0.5-1 GiB > L2, no flush"},
+            "kinds": out}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_merge_level(args, ws, rank, local):
     """Batched divide-and-conquer merge level: 64 independent Cauchy multiplies Q_i = A_i H_i,
     n_i log-uniform in [256, 8192] (seeded), generators as the n = 2048 workload (d sorted
@@ -586,6 +671,8 @@ def main():
     ap.add_argument("--serve-nmax", type=int, default=16384)
     ap.add_argument("--serve-budget-gib", type=int, default=96)
     ap.add_argument("--merge-level", action="store_true", help="run the batched merge level (64 problems)")
+    ap.add_argument("--cfg1", action="store_true", help="run the Toeplitz/Hankel/DFT multiplies at n = 8192")
+    ap.add_argument("--cfg1-n", type=int, default=8192)
     ap.add_argument("--batch-count", type=int, default=64)
     ap.add_argument("--batch-check", type=int, default=8)
     ap.add_argument("--merge-fp64", action="store_true", help="also time the FP64 path of the merge level")
@@ -603,6 +690,8 @@ def main():
         return run_serving(args, ws, rank, local)
     if args.merge_level:
         return run_merge_level(args, ws, rank, local)
+    if args.cfg1:
+        return run_cfg1(args, ws, rank, local)
     return run_gpu(args, ws, rank, local)
 
 
