@@ -306,6 +306,13 @@ int psmma_profile_read(float* ms, const char** names, int max_phases);
  * pipelined kernels use the same bounded waits with a 2 s limit. */
 int psmma_selftest_wait_timeout(unsigned long long limit_ns);
 
+/* No counterpart in the reference.  Self-check of the split path's fast FP64 division
+ * (Newton-Raphson refinement of the hardware reciprocal, used for the Cauchy entries
+ * U(i)V(j)/(D(i)-F(j))) against the IEEE division on `count` seeded operand pairs:
+ * returns the number of results that differ and the largest difference in ulp. */
+int psmma_selftest_division(long long count, unsigned long long seed, unsigned long long* mismatches,
+                            int* max_ulp);
+
 /* Text for a status code (static storage). */
 const char* psmma_status_string(int status);
 

@@ -114,6 +114,7 @@ SIGNATURES = {
     "psmma_profile_read": (_i, [C.POINTER(C.c_float), C.POINTER(C.c_char_p), _i]),
     "psmma_version": (C.c_char_p, []),
     "psmma_selftest_wait_timeout": (_i, [C.c_ulonglong]),
+    "psmma_selftest_division": (_i, [C.c_longlong, C.c_ulonglong, C.POINTER(C.c_ulonglong), C.POINTER(C.c_int)]),
     "psmma_server_create": (_i, [C.c_size_t, _i, C.POINTER(C.c_void_p)]),
     "psmma_server_submit": (_i, [_p, C.POINTER(PsmmaRequest), C.POINTER(C.c_ulonglong)]),
     "psmma_server_wait": (_i, [_p, C.c_ulonglong, C.c_double, C.POINTER(PsmmaCompletion)]),

@@ -40,3 +40,75 @@ extern "C" int psmma_selftest_wait_timeout(unsigned long long limit_ns) {
   if (st) return st;
   return (h & DEV_ERR_TIMEOUT) ? PSMMA_ETIMEDOUT : PSMMA_OK;
 }
+
+// ------------------------------------------------------------------------------------------
+// Self-check of div_nr (the split path's Cauchy entries) against the IEEE division on
+// count seeded pairs: Cauchy-like operands u*v / (d - w) with |d - w| log-uniform in
+// [1e-13, 1], plus arbitrary finite bit patterns (which exercise the fallback).
+// ------------------------------------------------------------------------------------------
+namespace psmma {
+
+__device__ __forceinline__ unsigned long long splitmix(unsigned long long& s) {
+  unsigned long long z = (s += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+__device__ __forceinline__ double unit(unsigned long long r) { return (double)(r >> 11) * 0x1.0p-53; }
+
+__global__ void k_selftest_div(long long count, unsigned long long seed, unsigned long long* mism, int* max_ulp) {
+  unsigned long long local = 0;
+  int worst = 0;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < count;
+       t += (long long)gridDim.x * blockDim.x) {
+    unsigned long long s = seed ^ (0xD1B54A32D192ED03ull * (unsigned long long)(t + 1));
+    double a, x;
+    if ((t & 7) != 7) {
+      const double u = 8.0 * unit(splitmix(s)) - 4.0, v = 8.0 * unit(splitmix(s)) - 4.0;
+      const double d = unit(splitmix(s));
+      const double gap = exp2(-43.2 * unit(splitmix(s)));  // 1e-13 .. 1
+      const double w = (splitmix(s) & 1) ? d - gap : d + gap;
+      a = u * v;
+      x = d - w;
+    } else {
+      unsigned long long ba = splitmix(s), bx = splitmix(s);
+      ba &= ~(0x7ffull << 52) | ((ba % 2046ull) << 52);  // finite exponents only
+      bx &= ~(0x7ffull << 52) | (((bx >> 3) % 2046ull + 1) << 52);
+      a = __longlong_as_double((long long)ba);
+      x = __longlong_as_double((long long)bx);
+    }
+    if (x == 0.0) continue;
+    const double q0 = a / x, q1 = div_nr(a, x);
+    if (__double_as_longlong(q0) != __double_as_longlong(q1)) {
+      ++local;
+      const long long d = __double_as_longlong(q0) - __double_as_longlong(q1);
+      const long long ad = d < 0 ? -d : d;
+      worst = max(worst, (int)min(ad, 1ll << 30));
+    }
+  }
+  if (local) atomicAdd(mism, local);
+  if (worst) atomicMax(max_ulp, worst);
+}
+
+}  // namespace psmma
+
+extern "C" int psmma_selftest_division(long long count, unsigned long long seed, unsigned long long* mismatches,
+                                       int* max_ulp) {
+  if (count <= 0 || !mismatches || !max_ulp) return PSMMA_EUNSUPPORTED;
+  unsigned long long* dm = nullptr;
+  if (cudaMalloc(&dm, 16) != cudaSuccess) return PSMMA_ENOMEM;
+  int st = PSMMA_OK;
+  if (cudaMemset(dm, 0, 16) != cudaSuccess) st = PSMMA_EDEVICE;
+  if (!st) {
+    k_selftest_div<<<1216, 256>>>(count, seed, dm, (int*)(dm + 1));
+    unsigned long long h[2] = {0, 0};
+    if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess ||
+        cudaMemcpy(h, dm, 16, cudaMemcpyDeviceToHost) != cudaSuccess)
+      st = PSMMA_EDEVICE;
+    *mismatches = h[0];
+    *max_ulp = (int)(unsigned)h[1];
+  }
+  cudaFree(dm);
+  return st;
+}

@@ -229,10 +229,10 @@ __device__ __forceinline__ void h_pass1_blk(const GenSpec& gs, int K, int kp, do
       if (KIND == KIND_CAUCHY) {
         if (gs.k1 > 0 && kk >= gs.k1) {
           const int t = kk - gs.k1;  // tail rows: dense, or Cauchy with the second row generators
-          h = gs.B ? __ldg(gs.B + t + (long)j * gs.ldb) : (__ldg(gs.Ur2 + t) * v) / (__ldg(gs.Dr2 + t) - w);
+          h = gs.B ? __ldg(gs.B + t + (long)j * gs.ldb) : div_nr(__ldg(gs.Ur2 + t) * v, __ldg(gs.Dr2 + t) - w);
         } else {
           double d = __ldg(gs.Dr + kk), u = __ldg(gs.Ur + kk);
-          h = (u * v) / (d - w);        // U(i)*V(j) / (D(i)-F(j))
+          h = div_nr(u * v, d - w);     // U(i)*V(j) / (D(i)-F(j))
         }
       } else if (KIND == KIND_TOEPLITZ) {
         h = __ldg(gs.g + (gs.order - 1) + j - kk);

@@ -30,3 +30,13 @@ def test_bounded_wait_expires_and_context_survives(lib, cuda):
     torch.cuda.synchronize()
     got = dQ.t().contiguous().cpu().numpy().T
     assert O.rel_fro(got, O.dense_product("cauchy", 1.0, A, gen, 0.0, None, k)) < 1e-12
+
+
+@pytest.mark.gpu
+def test_fast_division_matches_ieee_within_one_ulp(lib, cuda):
+    import ctypes as C
+    mism, ulp = C.c_ulonglong(0), C.c_int(0)
+    assert lib.psmma_selftest_division(1 << 26, 12345, C.byref(mism), C.byref(ulp)) == 0
+    # correctly rounded in all but rare ties; never more than one ulp away
+    assert ulp.value <= 1
+    assert mism.value < (1 << 26) // 10000
