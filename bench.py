@@ -445,7 +445,7 @@ def run_serving(args, ws, rank, local):
 
 
 def run_cfg1(args, ws, rank, local):
-    """Toeplitz, Hankel and DFT multiplies at n = k = 8192 (A uniform[-1,1], generator vector of
+    """Toeplitz, Hankel, DFT and accurate-denominator Cauchy (PSMMA_CAUCHYEIG) multiplies at n = k = 8192 (A uniform[-1,1], generator vector of
     length 2n-1 uniform[-1,1]; DFT: complex B with both parts uniform[-1,1]) on the split path
     (args.n_moduli) and the FP64 path.  Rates: 2n^3/t for Toeplitz/Hankel, 8n^3/t real flops
     for the DFT (2n^3/t complex multiply-adds beside it).  Errors: split vs FP64 path on the
@@ -466,8 +466,16 @@ def run_cfg1(args, ws, rank, local):
     A.copy_(torch.rand(k, n, generator=g, device=dev, dtype=torch.float64).mul_(2).sub_(1).t())
     gv = torch.rand(2 * k - 1, generator=g, device=dev, dtype=torch.float64).mul_(2).sub_(1)
     out = {}
-    for kind in ["toeplitz", "hankel", "dft"]:
-        if kind == "dft":
+    eig = O.eig_generators(k, seed=7, tiny=k // 100)  # F, U, V, DIFL, DIFR (1% of roots next to a pole)
+    eig_dev = [torch.from_numpy(np.ascontiguousarray(x)).to(dev) for x in eig]
+    for kind in ["toeplitz", "hankel", "dft", "cauchyeig"]:
+        if kind == "cauchyeig":
+            Y = P.fortran_empty(n, k, torch.float64, dev)
+            Y64 = P.fortran_empty(n, k, torch.float64, dev)
+            run = lambda prec, dst: P.psmma_cauchyeig(n, k, 1.0, A, *eig_dev, 0.0, dst, precision=prec,
+                                                      n_moduli=args.n_moduli)
+            flops = 2.0 * n ** 3
+        elif kind == "dft":
             X = P.fortran_empty(n, k, torch.complex128, dev)
             X.copy_(torch.complex(torch.rand(k, n, generator=g, device=dev, dtype=torch.float64) * 2 - 1,
                                   torch.rand(k, n, generator=g, device=dev, dtype=torch.float64) * 2 - 1).t())
@@ -498,7 +506,12 @@ def run_cfg1(args, ws, rank, local):
         torch.cuda.synchronize()
         t64 = e0.elapsed_time(e1)
         rel = float(torch.linalg.norm(Y - Y64) / torch.linalg.norm(Y64))
-        if kind == "dft":
+        if kind == "cauchyeig":
+            As = np.ascontiguousarray(A[:256].cpu().numpy())
+            ref = As @ O.cauchy_like_eig(*eig)
+            err_split = O.rel_fro(Y[:256].cpu().numpy(), ref)
+            err_64 = O.rel_fro(Y64[:256].cpu().numpy(), ref)
+        elif kind == "dft":
             Xs = X[:, :256].cpu().numpy()
             ref = O.dft_product(1.0, Xs, 0.0, None)
             err_split = O.rel_fro(Y[:, :256].cpu().numpy(), ref)
@@ -518,11 +531,12 @@ def run_cfg1(args, ws, rank, local):
         print(json.dumps({kind: out[kind]}), file=sys.stderr, flush=True)
         del Y, Y64
         torch.cuda.empty_cache()
-    line = {"metric": f"Toeplitz/Hankel/DFT A·C TFLOP/s n={n}, split vs FP64", "value": out["toeplitz"]["split_tflops"],
+    line = {"metric": f"Toeplitz/Hankel/DFT/CauchyEig A·C TFLOP/s n={n}, split vs FP64",
+            "value": out["toeplitz"]["split_tflops"],
             "unit": "TFLOP/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": out["toeplitz"]["split_ms"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64 (split: bf16 modular slices)", "data": "synthetic",
-            "config": {"workload": f"toeplitz/hankel/dft n=k={n}", "n_moduli": args.n_moduli,
+            "config": {"workload": f"toeplitz/hankel/dft/cauchyeig n=k={n}", "n_moduli": args.n_moduli,
                        "l2": "inputs 0.5-1 GiB > L2, no flush"},
             "kinds": out}
     print(json.dumps(line), flush=True)

@@ -80,6 +80,7 @@ typedef struct psmma_complex {
 #define PSMMA_KIND_TOEPLITZ 1
 #define PSMMA_KIND_HANKEL   2
 #define PSMMA_KIND_DFT      3
+#define PSMMA_KIND_CAUCHY_EIG 5
 
 /* ---- device-pointer entry points --------------------------------------------------- */
 
@@ -101,6 +102,22 @@ int psmma_toeplitz(int n, int k, double alpha, const double* A, int lda,
 int psmma_hankel(int n, int k, double alpha, const double* A, int lda,
                  const double* gen, int ldgen, double beta, double* Q, int ldq,
                  const psmma_opts* opts, void* stream);
+
+/* Replaces PSMMA_CAUCHYEIG(N,K,ID,ALPHA,A,IA,JA,DESCA,F,D,U,V,DIFL,DIFR,BETA,Q,IQ,JQ,DESCQ,
+ * WORK,REDIST) (psmma_cauchyeig.f90:2-3) and PSCAUCHYEIG_COMPUTE (pscauchyeig_compute.f90:2-3),
+ * the divide-and-conquer eigensolver's multiply: Q := alpha*A*H + beta*Q with
+ * H(i,j) = U(i)*V(j) / (F(i) - D(j)), F the old eigenvalues (sorted) and D(j) in
+ * (F(j), F(j+1)) the new ones, given by their distances DIFL(j) = D(j) - F(j) and
+ * DIFR(j) = D(j) - F(j+1).  The denominators are formed as (F(i) - F(j)) - DIFL(j) for i <= j
+ * and (F(i) - F(j+1)) - DIFR(j) for i > j (CauchylikeEig, CauchyHssEig.f90:1693-1774), so
+ * they keep full relative accuracy however close D(j) is to a pole.  F, U, V, DIFL, DIFR have
+ * k entries (DIFR(k) is not read); D is accepted for the reference's argument list and not
+ * read.  INFO numbers of PSCAUCHYEIG_COMPUTE (pscauchyeig_compute.f90:231-250): N -> -1,
+ * K -> -2, LDA -> -7, LDQ -> -17.  Both precisions. */
+int psmma_cauchyeig(int n, int k, double alpha, const double* A, int lda, const double* F,
+                    const double* D, const double* U, const double* V, const double* difl,
+                    const double* difr, double beta, double* Q, int ldq, const psmma_opts* opts,
+                    void* stream);
 
 /* Replaces PZMDFTL(N,K,NB,KB,ALPHA,B,LDB,BETA,C,LDC,IMROW,IMCOL,WORK,RWORK)
  * (pzmdftL.f90:1-2): C := alpha*F*B + beta*C with F the N-by-N DFT matrix on the left.
@@ -207,6 +224,9 @@ int psmma_hankel_host(int n, int k, double alpha, const double* A, int lda,
                       const psmma_opts* opts);
 int pzmdftl_host(int n, int k, double alpha, const psmma_complex* B, int ldb,
                  double beta, psmma_complex* C, int ldc, const psmma_opts* opts);
+int psmma_cauchyeig_host(int n, int k, double alpha, const double* A, int lda, const double* F,
+                         const double* D, const double* U, const double* V, const double* difl,
+                         const double* difr, double beta, double* Q, int ldq, const psmma_opts* opts);
 
 /* ---- Fortran-ABI entry points ------------------------------------------------------ */
 /* Same argument lists as the reference's Fortran subroutines, passed by reference with
@@ -235,6 +255,12 @@ void pzmdftl1_(const int* n, const int* k, const int* nb, const int* kb, const d
                const psmma_complex* B, const int* ldb, const double* beta, psmma_complex* C,
                const int* ldc, const int* imrow, const int* imcol, psmma_complex* work,
                double* rwork);
+void psmma_cauchyeig_(const int* n, const int* k, const int* id, const double* alpha,
+                      const double* A, const int* ia, const int* ja, const int* desca,
+                      const double* F, const double* D, const double* U, const double* V,
+                      const double* difl, const double* difr, const double* beta, double* Q,
+                      const int* iq, const int* jq, const int* descq, double* work,
+                      const int* redist);
 int psmma_last_status(void);
 
 /* ---- serving loop (continuous batching) -------------------------------------------- */

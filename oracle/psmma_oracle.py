@@ -717,3 +717,69 @@ def cfg_batch_sizes(count: int = 64, lo: int = 256, hi: int = 8192, seed: int = 
     """Seeded sizes of the batched merge level: n log-uniform in [lo, hi]."""
     rng = np.random.Generator(np.random.PCG64(seed))
     return [int(round(math.exp(x))) for x in rng.uniform(math.log(lo), math.log(hi), count)]
+
+
+# ---------------------------------------------------------------------------------------
+# Accurate-denominator Cauchy (PSMMA_CAUCHYEIG)
+# ---------------------------------------------------------------------------------------
+def cauchy_like_eig(F, U, V, DIFL, DIFR, rindex=None, cindex=None) -> np.ndarray:
+    """CauchylikeEig (CauchyHssEig.f90:1693-1774) as ConstCauchyEig calls it
+    (Auxil_2p5D.f90:532-637): T(i,j) = U(PL(i)) V(PU(j)) / den with, for PL(i) <= PU(j),
+    den = (F(PL(i)) - F(PU(j))) - DIFL(PU(j)), else (F(PL(i)) - F(PU(j)+1)) - DIFR(PU(j))
+    (1-based global indices PL = rindex, PU = cindex; default the whole k x k matrix)."""
+    F = np.asarray(F, dtype=np.float64)
+    k = len(U)
+    r = np.arange(1, k + 1) if rindex is None else np.asarray(rindex)
+    c = np.arange(1, k + 1) if cindex is None else np.asarray(cindex)
+    Fr = F[r - 1][:, None]
+    Fj = F[c - 1][None, :]
+    cj1 = np.minimum(c, len(F) - 1)          # F(PU(j)+1); not read when PU(j) = k
+    Fj1 = F[cj1][None, :]
+    upper = r[:, None] <= c[None, :]
+    dl = np.asarray(DIFL, dtype=np.float64)[c - 1][None, :]
+    dr = np.asarray(DIFR, dtype=np.float64)[np.minimum(c, len(DIFR)) - 1][None, :]
+    den = np.where(upper, (Fr - Fj) - dl, (Fr - Fj1) - dr)
+    return (np.asarray(U, dtype=np.float64)[r - 1][:, None] * np.asarray(V, dtype=np.float64)[c - 1][None, :]) / den
+
+
+def eig_generators(k: int, seed: int = 0, tiny: int = 0):
+    """Seeded generators of a secular-equation shaped Cauchy matrix: F sorted uniform(0,1) (old
+    eigenvalues), D(j) = F(j) + t_j (F(j+1) - F(j)) with t_j uniform(0.05, 0.95) (the last:
+    F(k) + t_k), except `tiny` roots placed 2^-70 relative above their pole (D(j) equal to F(j)
+    in FP64); DIFL(j) = D(j) - F(j) >= 0, DIFR(j) = D(j) - F(j+1) < 0 (exact from the gap
+    rounded once); U, V ~ N(0,1).  Returns F, U, V, DIFL, DIFR (length k each)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    F = np.sort(rng.uniform(0.0, 1.0, k))
+    gap = np.empty(k)
+    gap[:-1] = F[1:] - F[:-1]
+    gap[-1] = 1.0
+    t = rng.uniform(0.05, 0.95, k)
+    if tiny:
+        idx = rng.choice(np.arange(k - 1), size=min(tiny, k - 1), replace=False)
+        t[idx] = 2.0 ** -70
+    DIFL = t * gap
+    DIFR = DIFL - gap
+    DIFR[-1] = 0.0
+    return F, rng.standard_normal(k), rng.standard_normal(k), DIFL, DIFR
+
+
+def exact_cauchy_eig_product(A, F, U, V, DIFL, DIFR):
+    """A @ H in exact rational arithmetic on the FP64 inputs, H from cauchy_like_eig's rule
+    (small sizes only)."""
+    k = len(U)
+    Fq = [Fraction(float(x)) for x in F]
+    H = [[None] * k for _ in range(k)]
+    for i in range(k):
+        for j in range(k):
+            if i <= j:
+                den = (Fq[i] - Fq[j]) - Fraction(float(DIFL[j]))
+            else:
+                den = (Fq[i] - Fq[j + 1]) - Fraction(float(DIFR[j]))
+            H[i][j] = Fraction(float(U[i])) * Fraction(float(V[j])) / den
+    A = np.asarray(A)
+    out = np.empty((A.shape[0], k))
+    for r in range(A.shape[0]):
+        ar = [Fraction(float(x)) for x in A[r]]
+        for j in range(k):
+            out[r, j] = float(sum(ar[i] * H[i][j] for i in range(k)))
+    return out

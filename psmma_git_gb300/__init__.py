@@ -9,6 +9,8 @@ Python mirror of the reference's public routines, calling the C ABI of
 * :func:`psmma_hankel`   -- PSMMA_HANKEL   (psmma_hankel.f90:2-3):   H(i,j) = G(i+j-1).
 * :func:`pzmdftl` / :func:`pzmdftl1` -- PZMDFTL / PZMDFTL1 (pzmdftL.f90:1-2):
   C := alpha*F*B + beta*C with F the N-by-N DFT matrix, w = exp(-2*pi*i/N).
+* :func:`psmma_cauchyeig` -- PSMMA_CAUCHYEIG (psmma_cauchyeig.f90:2-3): the eigensolver's Cauchy
+  multiply with accurate denominators (F(i) - F(j)) - DIFL(j) / (F(i) - F(j+1)) - DIFR(j).
 * :func:`cauchy_batch_lowrank` -- the low-rank branch of PSCAUCHY_COMPUTE
   (pscauchy_compute.f90:371-391) for a batch of Cauchy multiplies: off-diagonal blocks
   compressed by RRQR (Compress_RRQR) or the structured RRLU (compress_cauchy).
@@ -32,7 +34,7 @@ from ._lib import (COMPRESS_RRLU, COMPRESS_RRQR, KIND_CAUCHY, KIND_DFT, KIND_HAN
 __all__ = [
     "psmma_cauchy", "psmma_toeplitz", "psmma_hankel", "pzmdftl", "pzmdftl1", "fortran_empty",
     "workspace_size", "PsmmaError", "PREC_FP64", "PREC_SPLIT", "load", "status_string",
-    "make_opts", "cauchy_batch_lowrank", "batch_workspace_size", "tune_batch",
+    "make_opts", "psmma_cauchyeig", "cauchy_batch_lowrank", "batch_workspace_size", "tune_batch",
 ]
 
 # The split path (exact modular slices on the BF16 tensor cores) is built into the library.
@@ -239,3 +241,29 @@ def tune_batch(problems, alpha=1.0, beta=0.0, *, compressor="rrqr", tol=1e-14, p
         raise PsmmaError(st, "psmma_tune_batch")
     return {"narrow_max": res.narrow_max, "mid_max": res.mid_max, "group_m": res.group_m,
             "candidates": res.candidates, "ms_best": res.ms_best, "ms_default": res.ms_default}
+
+
+def psmma_cauchyeig(n, k, alpha, A, F, U, V, difl, difr, beta, Q, *, D=None, precision="fp64", n_moduli=0,
+                    stream=None, work=None):
+    """Q := alpha*A*H + beta*Q, H(i,j) = U(i)V(j) / (F(i) - D(j)) with the denominators formed from
+    DIFL(j) = D(j) - F(j) and DIFR(j) = D(j) - F(j+1) (CauchylikeEig).  Vectors of length k."""
+    lib = load()
+    opts = make_opts(precision, n_moduli, work)
+    vecs = [F, D, U, V, difl, difr]
+    if _is_torch(Q):
+        import torch
+        pa, lda = _dev(A, "A", torch.float64) if A is not None else (0, max(1, n))
+        ptr = [C.c_void_p(x.data_ptr()) if x is not None else None for x in vecs]
+        pq, ldq = _dev(Q, "Q", torch.float64)
+        st = lib.psmma_cauchyeig(n, k, float(alpha), C.c_void_p(pa), lda, *ptr, float(beta), C.c_void_p(pq), ldq,
+                                 C.byref(opts), _stream_ptr(stream))
+    else:
+        pa, lda = _host(A, "A", np.float64) if A is not None else (0, max(1, n))
+        keep = [np.ascontiguousarray(x, dtype=np.float64) if x is not None else None for x in vecs]
+        ptr = [C.c_void_p(x.ctypes.data) if x is not None else None for x in keep]
+        pq, ldq = _host(Q, "Q", np.float64)
+        st = lib.psmma_cauchyeig_host(n, k, float(alpha), C.c_void_p(pa), lda, *ptr, float(beta), C.c_void_p(pq),
+                                      ldq, C.byref(opts))
+    if st != 0:
+        raise PsmmaError(st, "psmma_cauchyeig")
+    return Q

@@ -30,6 +30,7 @@ PREC_FP64 = 0
 PREC_SPLIT = 1
 
 KIND_CAUCHY, KIND_TOEPLITZ, KIND_HANKEL, KIND_DFT = 0, 1, 2, 3
+KIND_CAUCHY_EIG = 5
 
 COMPRESS_RRQR = 0
 COMPRESS_RRLU = 1
@@ -101,6 +102,10 @@ SIGNATURES = {
     "psmma_toeplitz_host": (_i, [_i, _i, _d, _p, _i, _p, _i, _d, _p, _i, _op]),
     "psmma_hankel_host": (_i, [_i, _i, _d, _p, _i, _p, _i, _d, _p, _i, _op]),
     "pzmdftl_host": (_i, [_i, _i, _d, _p, _i, _d, _p, _i, _op]),
+    "psmma_cauchyeig": (_i, [_i, _i, _d, _p, _i, _p, _p, _p, _p, _p, _p, _d, _p, _i, _op, _p]),
+    "psmma_cauchyeig_host": (_i, [_i, _i, _d, _p, _i, _p, _p, _p, _p, _p, _p, _d, _p, _i, _op]),
+    "psmma_cauchyeig_": (None, [_ip, _ip, _ip, _dp, _p, _ip, _ip, _ip, _p, _p, _p, _p, _p, _p, _dp, _p, _ip, _ip,
+                                _ip, _p, _ip]),
     "psmma_cauchy_": (None, [_ip, _ip, _dp, _p, _ip, _ip, _ip, _p, _ip, _dp, _p, _ip, _ip, _ip, _p, _ip]),
     "psmma_toeplitz_": (None, [_ip, _ip, _dp, _p, _ip, _ip, _ip, _p, _ip, _dp, _p, _ip, _ip, _ip, _p, _ip]),
     "psmma_hankel_": (None, [_ip, _ip, _dp, _p, _ip, _ip, _ip, _p, _ip, _dp, _p, _ip, _ip, _ip, _p, _ip]),

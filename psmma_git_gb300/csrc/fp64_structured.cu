@@ -126,9 +126,14 @@ __device__ __forceinline__ void load_Hd_tile(double* Bs, const F64Args& p, int n
 // ---- generated-operand builders -----------------------------------------------------------
 // H tile (real kinds): Bs[kk][jj] = H(k0+kk, n0+jj) (0-based), zero outside K x N.
 // Each thread owns one column jj and BK/2 consecutive rows.
+struct ColGen {
+  double F, V, F1, dl, dr;  // this thread's column generators
+};
+
 template <int KIND>
 __device__ __forceinline__ void gen_H_tile(double* Bs, const F64Args& p, int n0, int k0, int tid,
-                                           double colF, double colV) {
+                                           const ColGen& cg) {
+  const double colF = cg.F, colV = cg.V;
   const int jj = tid % F64_BN;
   const int kh = tid / F64_BN;  // 0 or 1
   const int gj = n0 + jj;
@@ -142,6 +147,9 @@ __device__ __forceinline__ void gen_H_tile(double* Bs, const F64Args& p, int n0,
         double d = __ldg(p.gs.Dr + gk);               // D(i)
         double u = __ldg(p.gs.Ur + gk);               // U(i)
         h = (u * colV) / (d - colF);                  // U(i)*V(j) / (D(i)-F(j))
+      } else if (KIND == KIND_CAUCHY_EIG) {
+        const double fi = __ldg(p.gs.Dr + gk), u = __ldg(p.gs.Ur + gk);
+        h = (u * colV) / eig_den(fi, colF, cg.F1, cg.dl, cg.dr, gk - gj <= p.gs.diag_off);
       } else if (KIND == KIND_TOEPLITZ) {
         h = __ldg(p.gs.g + (p.gs.order - 1) + gj - gk);  // G(K + j - i), 1-based
       } else {
@@ -192,12 +200,19 @@ __device__ __forceinline__ void struct_f64_tile(const F64Args& p, int bx, int by
   const int m0 = bx * F64_BM, n0 = by * F64_BN;
   const int wm0 = (warp & 1) * F64_WM, wn0 = (warp >> 1) * F64_WN;
 
-  double colF = 0.0, colV = 0.0;
-  if (KIND == KIND_CAUCHY) {
+  ColGen cg{0.0, 0.0, 0.0, 0.0, 0.0};
+  if (KIND == KIND_CAUCHY || KIND == KIND_CAUCHY_EIG) {
     int gj = n0 + (tid % F64_BN);
     if (gj < p.N) {
-      colF = __ldg(p.gs.Fc + gj);   // F(j)
-      colV = __ldg(p.gs.Vc + gj);   // V(j)
+      cg.F = __ldg(p.gs.Fc + gj);   // F(j)
+      cg.V = __ldg(p.gs.Vc + gj);   // V(j)
+      if (KIND == KIND_CAUCHY_EIG) {
+        cg.dl = __ldg(p.gs.dl + gj);  // DIFL(j)
+        if (gj < p.gs.fc1_len) {
+          cg.F1 = __ldg(p.gs.Fc1 + gj);  // F(j+1)
+          cg.dr = __ldg(p.gs.dr + gj);   // DIFR(j)
+        }
+      }
     }
   }
 
@@ -223,7 +238,7 @@ __device__ __forceinline__ void struct_f64_tile(const F64Args& p, int bx, int by
     } else {
       load_A_tile(As, p, m0, k0, tid);
       cp_async_commit();
-      gen_H_tile<KIND>(Bs, p, n0, k0, tid, colF, colV);
+      gen_H_tile<KIND>(Bs, p, n0, k0, tid, cg);
     }
   };
 
@@ -332,6 +347,7 @@ int launch_struct_f64(int M, int N, int K, double alpha, const double* X, long l
     PSMMA_LAUNCH_F64(KIND_HANKEL)
     PSMMA_LAUNCH_F64(KIND_DFT)
     PSMMA_LAUNCH_F64(KIND_DENSE)
+    PSMMA_LAUNCH_F64(KIND_CAUCHY_EIG)
 #undef PSMMA_LAUNCH_F64
     default:
       return PSMMA_EUNSUPPORTED;

@@ -275,6 +275,106 @@ int host_real(int kind, int n, int k, double alpha, const double* A, int lda, co
   return ok ? PSMMA_OK : PSMMA_EDEVICE;
 }
 
+// ---- accurate-denominator Cauchy (PSMMA_CAUCHYEIG) -----------------------------------------
+GenSpec eig_gens(const double* F, const double* U, const double* V, const double* difl, const double* difr, int k) {
+  GenSpec g;
+  g.kind = KIND_CAUCHY_EIG;
+  g.Dr = F;      // F(i), rows
+  g.Ur = U;
+  g.Fc = F;      // F(j), columns
+  g.Fc1 = F + 1; // F(j+1)
+  g.Vc = V;
+  g.dl = difl;
+  g.dr = difr;
+  g.fc1_len = k - 1;
+  g.diag_off = 0;
+  return g;
+}
+
+// Argument checks of PSCAUCHYEIG_COMPUTE (pscauchyeig_compute.f90:231-250: N -> 1, K -> 2,
+// LDA -> 7, LDC -> 17), with the leading dimensions checked against N as a 1x1 grid needs.
+int check_eig(int n, int k, double alpha, const double* A, int lda, const double* F, const double* U,
+              const double* V, const double* difl, const double* difr, double beta, const double* Q, int ldq) {
+  if (n < 0) return -1;
+  if (k < 0) return -2;
+  if (lda < std::max(1, n)) return -7;
+  if (ldq < std::max(1, n)) return -17;
+  if (n == 0 || k == 0 || (alpha == 0.0 && beta == 1.0)) return 1;  // quick return
+  if (!Q) return PSMMA_ENULL;
+  if (alpha != 0.0) {
+    if (!A) return PSMMA_ENULL;
+    if (!F || !U || !V || !difl || (k > 1 && !difr)) return PSMMA_EGEN;
+  }
+  return PSMMA_OK;
+}
+
+int run_eig(int n, int k, double alpha, const double* A, int lda, const double* F, const double* U,
+            const double* V, const double* difl, const double* difr, double beta, double* Q, int ldq,
+            const psmma_opts* opts, void* stream) {
+  const psmma_opts* o = opts ? opts : &kDefaultOpts;
+  int st = check_opts(o, KIND_CAUCHY);
+  if (st) return st;
+  st = check_eig(n, k, alpha, A, lda, F, U, V, difl, difr, beta, Q, ldq);
+  if (st == 1) return PSMMA_OK;
+  if (st) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  const GenSpec gs = eig_gens(F, U, V, difl, difr, k);
+  if (o->precision == PSMMA_PREC_SPLIT && alpha != 0.0) {
+    size_t need = split_workspace_general(n, k, k, o->n_moduli);
+    void* work = o->work;
+    if (work) {
+      if (o->lwork < need) return PSMMA_EWORKSPACE;
+    } else {
+      work = pool_get(need, s, &st);
+      if (st) return st;
+    }
+    unsigned* dstat = nullptr;
+    return launch_split_general(n, k, k, alpha, A, lda, gs, beta, Q, ldq, o->n_moduli, work, need, s, dstat);
+  }
+  return launch_struct_f64(n, k, k, alpha, A, lda, gs, beta, Q, ldq, s);
+}
+
+int host_eig(int n, int k, double alpha, const double* A, int lda, const double* F, const double* U,
+             const double* V, const double* difl, const double* difr, double beta, double* Q, int ldq,
+             const psmma_opts* opts) {
+  const psmma_opts* o = opts ? opts : &kDefaultOpts;
+  int st = check_opts(o, KIND_CAUCHY);
+  if (st) return st;
+  st = check_eig(n, k, alpha, A, lda, F, U, V, difl, difr, beta, Q, ldq);
+  if (st == 1) return PSMMA_OK;
+  if (st) return st;
+  std::lock_guard<std::mutex> lk(g_host_mu);
+  const size_t bA = align256((size_t)n * k * 8), bG = align256((size_t)5 * k * 8), bQ = align256((size_t)n * k * 8);
+  cudaStream_t s;
+  char* base = (char*)host_arena(bA + bG + bQ, &s, &st);
+  if (st) return st;
+  double* dA = (double*)base;
+  double* dG = (double*)(base + bA);  // F, U, V, DIFL, DIFR, k each
+  double* dQ = (double*)(base + bA + bG);
+  bool ok = true;
+  if (alpha != 0.0) {
+    ok &= cudaMemcpy2DAsync(dA, (size_t)n * 8, A, (size_t)lda * 8, (size_t)n * 8, k, cudaMemcpyHostToDevice, s) ==
+          cudaSuccess;
+    const double* src[5] = {F, U, V, difl, difr};
+    for (int t = 0; t < 5; ++t)
+      if (src[t]) ok &= cudaMemcpyAsync(dG + (size_t)t * k, src[t], (size_t)k * 8, cudaMemcpyHostToDevice, s) == cudaSuccess;
+  }
+  if (beta != 0.0)
+    ok &= cudaMemcpy2DAsync(dQ, (size_t)n * 8, Q, (size_t)ldq * 8, (size_t)n * 8, k, cudaMemcpyHostToDevice, s) ==
+          cudaSuccess;
+  if (!ok) return PSMMA_EDEVICE;
+  st = run_eig(n, k, alpha, dA, n, dG, dG + k, dG + 2 * (size_t)k, dG + 3 * (size_t)k, dG + 4 * (size_t)k, beta, dQ,
+               n, o, s);
+  if (st) {
+    cudaStreamSynchronize(s);
+    return st;
+  }
+  ok &= cudaMemcpy2DAsync(Q, (size_t)ldq * 8, dQ, (size_t)n * 8, (size_t)n * 8, k, cudaMemcpyDeviceToHost, s) ==
+        cudaSuccess;
+  ok &= cudaStreamSynchronize(s) == cudaSuccess;
+  return ok ? PSMMA_OK : PSMMA_EDEVICE;
+}
+
 int host_dft(int n, int k, double alpha, const psmma_complex* B, int ldb, double beta,
              psmma_complex* C, int ldc, const psmma_opts* opts) {
   const psmma_opts* o = opts ? opts : &kDefaultOpts;
@@ -366,6 +466,25 @@ void psmma_hankel_(const int* n, const int* k, const double* alpha, const double
                    double* Q, const int*, const int*, const int* descq, double*, const int*) {
   g_last_status = host_real(KIND_HANKEL, *n, *k, *alpha, A, desca[8], B, *ldb, *beta, Q, descq[8], nullptr);
 }
+int psmma_cauchyeig(int n, int k, double alpha, const double* A, int lda, const double* F, const double* D,
+                    const double* U, const double* V, const double* difl, const double* difr, double beta,
+                    double* Q, int ldq, const psmma_opts* opts, void* stream) {
+  (void)D;  // the updated eigenvalues enter through DIFL/DIFR (CauchylikeEig does not read D)
+  return run_eig(n, k, alpha, A, lda, F, U, V, difl, difr, beta, Q, ldq, opts, stream);
+}
+int psmma_cauchyeig_host(int n, int k, double alpha, const double* A, int lda, const double* F, const double* D,
+                         const double* U, const double* V, const double* difl, const double* difr, double beta,
+                         double* Q, int ldq, const psmma_opts* opts) {
+  (void)D;
+  return host_eig(n, k, alpha, A, lda, F, U, V, difl, difr, beta, Q, ldq, opts);
+}
+void psmma_cauchyeig_(const int* n, const int* k, const int*, const double* alpha, const double* A, const int*,
+                      const int*, const int* desca, const double* F, const double* D, const double* U,
+                      const double* V, const double* difl, const double* difr, const double* beta, double* Q,
+                      const int*, const int*, const int* descq, double*, const int*) {
+  (void)D;
+  g_last_status = host_eig(*n, *k, *alpha, A, desca[8], F, U, V, difl, difr, *beta, Q, descq[8], nullptr);
+}
 void pzmdftl_(const int* n, const int* k, const int*, const int*, const double* alpha,
               const psmma_complex* B, const int* ldb, const double* beta, psmma_complex* C,
               const int* ldc, const int*, const int*, psmma_complex*, double*) {
@@ -381,7 +500,9 @@ int psmma_last_status(void) { return g_last_status; }
 size_t psmma_workspace_size(int kind, int n, int k, const psmma_opts* opts) {
   const psmma_opts* o = opts ? opts : &kDefaultOpts;
   if (n <= 0 || k <= 0) return 0;
-  if (kind < KIND_CAUCHY || kind > KIND_DFT) return 0;
+  if (kind < KIND_CAUCHY || kind > KIND_CAUCHY_EIG || kind == KIND_DENSE) return 0;
+  if (kind == KIND_CAUCHY_EIG)
+    return o->precision == PSMMA_PREC_SPLIT ? split_workspace_general(n, k, k, o->n_moduli) : 0;
   if (o->precision == PSMMA_PREC_SPLIT) return split_workspace_bytes(kind, n, k, o->n_moduli);
   if (kind == KIND_DFT) return align256((size_t)n * sizeof(double2));
   return 0;

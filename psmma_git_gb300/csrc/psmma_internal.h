@@ -10,7 +10,7 @@
 
 namespace psmma {
 
-enum Kind { KIND_CAUCHY = 0, KIND_TOEPLITZ = 1, KIND_HANKEL = 2, KIND_DFT = 3, KIND_DENSE = 4 };
+enum Kind { KIND_CAUCHY = 0, KIND_TOEPLITZ = 1, KIND_HANKEL = 2, KIND_DFT = 3, KIND_DENSE = 4, KIND_CAUCHY_EIG = 5 };
 
 // Generators of the structured operand H (K x N) of one product.
 //   Cauchy    H(i,j) = Ur[i]*Vc[j] / (Dr[i] - Fc[j])   (row and column generators independent)
@@ -18,6 +18,10 @@ enum Kind { KIND_CAUCHY = 0, KIND_TOEPLITZ = 1, KIND_HANKEL = 2, KIND_DFT = 3, K
 //   Hankel    H(i,j) = g[i + j]                        (sub-blocks: g offset by r0 + c0)
 //   DFT       embedding of F = (w^(r c mod n_dft)), table wtab (t < n_dft)
 //   Dense     H(i,j) = B[i + j*ldb]                   (explicit factors of the low-rank path)
+//   CauchyEig H(i,j) = Ur[i]*Vc[j] / den(i,j), the accurate denominators of CauchylikeEig
+//             (CauchyHssEig.f90:1693-1774): with Dr = F(rows), Fc = F(cols), Fc1 = F(cols + 1),
+//             dl = DIFL(cols), dr = DIFR(cols) and global row <= global column (i - j <= diag_off):
+//             den = (Dr[i] - Fc[j]) - dl[j], else (Dr[i] - Fc1[j]) - dr[j]  (Fc1, dr: j < fc1_len)
 // Split path only: a Cauchy H with k1 > 0 has a tail of rows i >= k1, either dense
 // (B[(i-k1) + j*ldb]) or Cauchy with its own row generators (Dr2, Ur2 at i - k1) and the
 // same column generators.
@@ -32,7 +36,18 @@ struct GenSpec {
   long ldb = 0;
   int k1 = 0;
   const double *Dr2 = nullptr, *Ur2 = nullptr;
+  const double *Fc1 = nullptr, *dl = nullptr, *dr = nullptr;
+  int fc1_len = 0, diag_off = 0;
 };
+
+#ifdef __CUDACC__
+// The denominator F(i) - D(j) of CauchylikeEig with D(j) in (F(j), F(j+1)) given by its
+// distances DIFL(j) = D(j) - F(j) and DIFR(j) = D(j) - F(j+1): for i <= j it is
+// (F(i) - F(j)) - DIFL(j), else (F(i) - F(j+1)) - DIFR(j) (CauchyHssEig.f90:1759-1763).
+__device__ __forceinline__ double eig_den(double fi, double fj, double fj1, double dlj, double drj, bool upper) {
+  return upper ? (fi - fj) - dlj : (fi - fj1) - drj;
+}
+#endif
 
 // The generators of the reference's square H (k x k) from its storage conventions: Cauchy
 // [D|F|U|V] with leading dimension ldgen, Toeplitz/Hankel vector of 2k-1.

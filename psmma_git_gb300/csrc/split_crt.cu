@@ -215,10 +215,17 @@ template <int KIND>
 __device__ __forceinline__ void h_pass1_blk(const GenSpec& gs, int K, int kp, double* __restrict__ Ht,
                                             unsigned long long* __restrict__ hmax_bits, double* __restrict__ hsum,
                                             double* __restrict__ hsq, SplitDevParams* prm, int j) {
-  double w = 0.0, v = 0.0;
-  if (KIND == KIND_CAUCHY) {
+  double w = 0.0, v = 0.0, w1 = 0.0, dlj = 0.0, drj = 0.0;
+  if (KIND == KIND_CAUCHY || KIND == KIND_CAUCHY_EIG) {
     w = __ldg(gs.Fc + j);   // F(j)
     v = __ldg(gs.Vc + j);   // V(j)
+  }
+  if (KIND == KIND_CAUCHY_EIG) {
+    dlj = __ldg(gs.dl + j);  // DIFL(j)
+    if (j < gs.fc1_len) {
+      w1 = __ldg(gs.Fc1 + j);  // F(j+1)
+      drj = __ldg(gs.dr + j);  // DIFR(j)
+    }
   }
   unsigned long long mb = 0;
   double s = 0.0, s2 = 0.0;
@@ -234,6 +241,9 @@ __device__ __forceinline__ void h_pass1_blk(const GenSpec& gs, int K, int kp, do
           double d = __ldg(gs.Dr + kk), u = __ldg(gs.Ur + kk);
           h = div_nr(u * v, d - w);     // U(i)*V(j) / (D(i)-F(j))
         }
+      } else if (KIND == KIND_CAUCHY_EIG) {
+        const double fi = __ldg(gs.Dr + kk), u = __ldg(gs.Ur + kk);
+        h = div_nr(u * v, eig_den(fi, w, w1, dlj, drj, kk - j <= gs.diag_off));
       } else if (KIND == KIND_TOEPLITZ) {
         h = __ldg(gs.g + (gs.order - 1) + j - kk);
       } else if (KIND == KIND_HANKEL) {
@@ -1129,6 +1139,7 @@ static int split_core(int M, int N, int K, double alpha, const double* A, long l
     case KIND_TOEPLITZ: k_h_pass1<KIND_TOEPLITZ><<<N, 256, 0, stream>>>(gs, K, L.kp, b.Ht, b.hmax, b.hsum, b.hsq, b.prm); break;
     case KIND_HANKEL: k_h_pass1<KIND_HANKEL><<<N, 256, 0, stream>>>(gs, K, L.kp, b.Ht, b.hmax, b.hsum, b.hsq, b.prm); break;
     case KIND_DENSE: k_h_pass1<KIND_DENSE><<<N, 256, 0, stream>>>(gs, K, L.kp, b.Ht, b.hmax, b.hsum, b.hsq, b.prm); break;
+    case KIND_CAUCHY_EIG: k_h_pass1<KIND_CAUCHY_EIG><<<N, 256, 0, stream>>>(gs, K, L.kp, b.Ht, b.hmax, b.hsum, b.hsq, b.prm); break;
     case KIND_DFT: {
       int st = launch_dft_table(b.wtab, gs.n_dft, stream);
       if (st) return st;
@@ -1279,6 +1290,7 @@ __global__ void __launch_bounds__(256) k_g_h_pass1(const GProb* d, int count) {
     case KIND_CAUCHY: h_pass1_blk<KIND_CAUCHY>(e.gs, e.K, e.kp, e.Ht, e.hmax, e.hsum, e.hsq, e.prm, j); break;
     case KIND_TOEPLITZ: h_pass1_blk<KIND_TOEPLITZ>(e.gs, e.K, e.kp, e.Ht, e.hmax, e.hsum, e.hsq, e.prm, j); break;
     case KIND_HANKEL: h_pass1_blk<KIND_HANKEL>(e.gs, e.K, e.kp, e.Ht, e.hmax, e.hsum, e.hsq, e.prm, j); break;
+    case KIND_CAUCHY_EIG: h_pass1_blk<KIND_CAUCHY_EIG>(e.gs, e.K, e.kp, e.Ht, e.hmax, e.hsum, e.hsq, e.prm, j); break;
     default: h_pass1_blk<KIND_DENSE>(e.gs, e.K, e.kp, e.Ht, e.hmax, e.hsum, e.hsq, e.prm, j); break;
   }
 }
