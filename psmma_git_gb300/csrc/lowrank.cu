@@ -20,8 +20,6 @@
 #include "psmma_internal.h"
 #include "tcgen05_util.cuh"
 
-#include <cooperative_groups.h>
-
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
