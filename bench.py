@@ -584,45 +584,59 @@ def run_merge_level(args, ws, rank, local):
     torch.cuda.synchronize()
     out = {}
     precisions = ["split"] + (["fp64"] if args.merge_fp64 else [])
-    for comp in ["rrqr", "rrlu"]:
-        for prec in precisions:
-            kw = dict(compressor=comp, tol=1e-14, precision=prec, n_moduli=args.n_moduli)
-            tuned = None
-            if prec == "split" and not args.no_tune:
-                tuned = P.tune_batch(probs, 1.0, 0.0, **kw)  # untimed; later calls use its choice
-            for _ in range(args.warmup if prec == "split" else 1):
-                ranks, info = P.cauchy_batch_lowrank(probs, 1.0, 0.0, **kw)
+    # the eigensolver's matrices of the same sizes (psmma_cauchyeig generators, 1% of the roots
+    # next to their pole), compressed by RRQR: the natural caller of the merge level
+    eig_probs = []
+    for i, n in enumerate(sizes):
+        F, U, V, dl, dr = O.eig_generators(n, seed=200 + i, tiny=n // 100)
+        gen = torch.from_numpy(np.ascontiguousarray(np.stack([F, U, V, dl, dr]))).to(dev).t()
+        eig_probs.append((probs[i][0], gen, probs[i][2]))
+    runs = [(c, p, False) for c in ["rrqr", "rrlu"] for p in precisions] + [("rrqr", "split", True)]
+    for comp, prec, eig in runs:
+        batch = eig_probs if eig else probs
+        kw = dict(compressor=comp, tol=1e-14, precision=prec, n_moduli=args.n_moduli, eig=eig)
+        tuned = None
+        if prec == "split" and not args.no_tune and not eig:
+            tkw = {k: v for k, v in kw.items() if k != "eig"}
+            tuned = P.tune_batch(probs, 1.0, 0.0, **tkw)  # untimed; later calls use its choice
+        for _ in range(args.warmup if prec == "split" else 1):
+            ranks, info = P.cauchy_batch_lowrank(batch, 1.0, 0.0, **kw)
+        torch.cuda.synchronize()
+        steps = args.steps if prec == "split" else 1
+        times = []
+        for _ in range(steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             torch.cuda.synchronize()
-            steps = args.steps if prec == "split" else 1
-            times = []
-            for _ in range(steps):
-                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                torch.cuda.synchronize()
-                e0.record()
-                ranks, info = P.cauchy_batch_lowrank(probs, 1.0, 0.0, **kw)
-                e1.record()
-                torch.cuda.synchronize()
-                times.append(e0.elapsed_time(e1))
-            err = max(float(torch.linalg.norm(probs[i][2] - refs[i]) / torch.linalg.norm(refs[i])) for i in check)
-            # per-phase trace of one more call (eager launches, one event per phase)
-            lib = P.load()
-            lib.psmma_set_profiling(1)
-            P.cauchy_batch_lowrank(probs, 1.0, 0.0, **kw)
+            e0.record()
+            ranks, info = P.cauchy_batch_lowrank(batch, 1.0, 0.0, **kw)
+            e1.record()
             torch.cuda.synchronize()
-            ms = (C_float * 40)()
-            names = (C_charp * 40)()
-            m = lib.psmma_profile_read(ms, names, 40)
-            lib.psmma_set_profiling(0)
-            phases = [[names[j].decode(), round(ms[j], 3)] for j in range(max(0, m))]
-            t = statistics.median(times)
-            out[f"{comp}_{prec}"] = {
-                "ms_per_step": t, "steps": steps, "effective_tflops": eff / t / 1e9,
-                "executed_tflops": info["executed_flops"] / t / 1e9,
-                "executed_flops": info["executed_flops"], "compress_flops": info["compress_flops"],
-                "ranks": {"max": int(max(ranks)), "mean": float(np.mean(ranks)), "min": int(min(ranks))},
-                "full_rank_blocks": info["full_rank_blocks"], "rel_err_vs_dense_fp64": err,
-                "autotune": tuned, "phases_ms": phases}
-            print(json.dumps({comp + "_" + prec: out[f"{comp}_{prec}"]}), file=sys.stderr, flush=True)
+            times.append(e0.elapsed_time(e1))
+        if eig:
+            err = None  # checked against the dense product by the tests (no dense eig reference here)
+        else:
+            err = max(float(torch.linalg.norm(probs[i][2] - refs[i]) / torch.linalg.norm(refs[i]))
+                      for i in check)
+        # per-phase trace of one more call (eager launches, one event per phase)
+        lib = P.load()
+        lib.psmma_set_profiling(1)
+        P.cauchy_batch_lowrank(batch, 1.0, 0.0, **kw)
+        torch.cuda.synchronize()
+        ms = (C_float * 40)()
+        names = (C_charp * 40)()
+        m = lib.psmma_profile_read(ms, names, 40)
+        lib.psmma_set_profiling(0)
+        phases = [[names[j].decode(), round(ms[j], 3)] for j in range(max(0, m))]
+        t = statistics.median(times)
+        key = f"{comp}_{prec}" + ("_eig" if eig else "")
+        out[key] = {
+            "ms_per_step": t, "steps": steps, "effective_tflops": eff / t / 1e9,
+            "executed_tflops": info["executed_flops"] / t / 1e9,
+            "executed_flops": info["executed_flops"], "compress_flops": info["compress_flops"],
+            "ranks": {"max": int(max(ranks)), "mean": float(np.mean(ranks)), "min": int(min(ranks))},
+            "full_rank_blocks": info["full_rank_blocks"], "rel_err_vs_dense_fp64": err,
+            "autotune": tuned, "phases_ms": phases}
+        print(json.dumps({key: out[key]}), file=sys.stderr, flush=True)
     # CPU baseline: the oracle's restatement of the merge level (Compress_RRQR + DGEMMs) on the
     # smallest problems until ~args.cpu_seconds of work
     cpu = None

@@ -190,6 +190,18 @@ typedef struct psmma_batch_stats {
 int psmma_cauchy_batch_lowrank(int count, const psmma_batch_item* items, double alpha, double beta,
                                int compressor, double tol, const psmma_opts* opts, int* ranks_out,
                                psmma_batch_stats* stats, void* stream);
+/* The same merge level for the eigensolver's matrices (PSCAUCHYEIG_COMPUTE's low-rank
+ * branch, pscauchyeig_compute.f90:371-391 with ConstCauchyEiglowrank, Auxil_2p5D.f90:642-748):
+ * each item's gen is [F|U|V|DIFL|DIFR] (ldgen >= n, the arguments of psmma_cauchyeig) and H
+ * has the accurate denominators of CauchylikeEig.  Compressor: PSMMA_COMPRESS_RRQR on the
+ * explicit tiles (the reference's structured rrluCauchyEigrow is not built here:
+ * PSMMA_COMPRESS_RRLU returns PSMMA_EUNSUPPORTED). */
+int psmma_cauchyeig_batch_lowrank(int count, const psmma_batch_item* items, double alpha, double beta,
+                                  int compressor, double tol, const psmma_opts* opts, int* ranks_out,
+                                  psmma_batch_stats* stats, void* stream);
+size_t psmma_cauchyeig_batch_workspace_size(int count, const psmma_batch_item* items, int compressor,
+                                            const psmma_opts* opts);
+
 /* No counterpart in the reference.  Autotuner of the split path's grouped GEMM (output-tile
  * widths 64/128/256 by product width, raster group): times psmma_cauchy_batch_lowrank on
  * this batch for each candidate configuration and keeps the fastest for batches of the same

@@ -783,3 +783,32 @@ def exact_cauchy_eig_product(A, F, U, V, DIFL, DIFR):
         for j in range(k):
             out[r, j] = float(sum(ar[i] * H[i][j] for i in range(k)))
     return out
+
+
+def merge_level_eig_product(A, F, U, V, DIFL, DIFR, beta_Q, alpha: float, beta: float, tol: float = 1e-14):
+    """The merge level of merge_level_product for the eigensolver's matrix H =
+    cauchy_like_eig(F, U, V, DIFL, DIFR): diagonal blocks dense, off-diagonal tiles (built by
+    ConstCauchyEig's rule) compressed by Compress_RRQR, Q(:,C) += alpha (A(:,R) X) Y.  (The
+    reference compresses these tiles with the structured rrluCauchyEigrow,
+    CauchyHssEig.f90:7-212; RRQR is this build's compressor for them.)  Returns (Q, ranks)."""
+    A = np.asarray(A, dtype=np.float64)
+    n = A.shape[0]
+    Q = (beta * np.asarray(beta_Q, dtype=np.float64)) if beta != 0.0 else np.zeros((n, n))
+    if n == 0:
+        return Q, []
+    h = n // 2
+    H = cauchy_like_eig(F, U, V, DIFL, DIFR)
+    Q[:, :h] += alpha * (A[:, :h] @ H[:h, :h])
+    Q[:, h:] += alpha * (A[:, h:] @ H[h:, h:])
+    ranks = []
+    if h == 0:
+        return Q, ranks
+    for (r0, r1, c0, c1) in [(0, h, h, n), (h, n, 0, h)]:
+        T = H[r0:r1, c0:c1]
+        X, Y, rk = compress_rrqr(T, tol)
+        ranks.append(rk)
+        if X is None:
+            Q[:, c0:c1] += alpha * (A[:, r0:r1] @ T)
+        elif rk > 0:
+            Q[:, c0:c1] += alpha * ((A[:, r0:r1] @ X) @ Y)
+    return Q, ranks

@@ -191,7 +191,7 @@ def _batch_items(problems):
         pa, lda = _dev(A, "A", torch.float64)
         pg, ldg = _dev(gen, "gen", torch.float64)
         if gen.dim() == 1:
-            ldg = gen.numel() // 4
+            ldg = n
         pq, ldq = _dev(Q, "Q", torch.float64)
         items[i].n, items[i].A, items[i].lda = n, pa, max(lda, 1)
         items[i].gen, items[i].ldgen = pg, ldg
@@ -200,19 +200,22 @@ def _batch_items(problems):
 
 
 def cauchy_batch_lowrank(problems, alpha, beta, *, compressor="rrqr", tol=1e-14, precision="fp64",
-                         n_moduli=0, stream=None, work=None):
+                         n_moduli=0, stream=None, work=None, eig=False):
     """Q_i := alpha*A_i*H_i + beta*Q_i for problems = [(A_i, gen_i, Q_i), ...] (n_i x n_i CUDA
     tensors, gen_i = [D|F|U|V]), H_i split 2 x 2 with its off-diagonal blocks compressed by
-    ``compressor`` ("rrqr" or "rrlu") at ``tol``.  Returns (ranks, stats): two ranks per
-    problem with n >= 2 (blocks H(1:h, h+1:n), H(h+1:n, 1:h)) and a dict of flop counts."""
+    ``compressor`` ("rrqr" or "rrlu") at ``tol``.  With eig=True the H_i are the eigensolver's
+    matrices (psmma_cauchyeig) and gen_i = [F|U|V|DIFL|DIFR] (RRQR only).  Returns (ranks,
+    stats): two ranks per problem with n >= 2 (blocks H(1:h, h+1:n), H(h+1:n, 1:h)) and a dict
+    of flop counts."""
     lib = load()
     items = _batch_items(problems)
     opts = make_opts(precision, n_moduli, work)
     nb = sum(2 for (_, _, Q) in problems if Q.shape[0] >= 2)
     ranks = (C.c_int * max(1, nb))()
     stats = PsmmaBatchStats()
-    st = lib.psmma_cauchy_batch_lowrank(len(problems), items, float(alpha), float(beta), _COMPRESS[compressor],
-                                        float(tol), C.byref(opts), ranks, C.byref(stats), _stream_ptr(stream))
+    fn = lib.psmma_cauchyeig_batch_lowrank if eig else lib.psmma_cauchy_batch_lowrank
+    st = fn(len(problems), items, float(alpha), float(beta), _COMPRESS[compressor], float(tol), C.byref(opts), ranks,
+            C.byref(stats), _stream_ptr(stream))
     if st != 0:
         raise PsmmaError(st, "psmma_cauchy_batch_lowrank")
     info = {"effective_flops": stats.effective_flops, "executed_flops": stats.executed_flops,

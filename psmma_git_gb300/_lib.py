@@ -128,6 +128,9 @@ SIGNATURES = {
     "psmma_cauchy_batch_lowrank": (_i, [_i, C.POINTER(PsmmaBatchItem), _d, _d, _i, _d, _op, _ip,
                                         C.POINTER(PsmmaBatchStats), _p]),
     "psmma_batch_workspace_size": (C.c_size_t, [_i, C.POINTER(PsmmaBatchItem), _i, _op]),
+    "psmma_cauchyeig_batch_lowrank": (_i, [_i, C.POINTER(PsmmaBatchItem), _d, _d, _i, _d, _op, _ip,
+                                           C.POINTER(PsmmaBatchStats), _p]),
+    "psmma_cauchyeig_batch_workspace_size": (C.c_size_t, [_i, C.POINTER(PsmmaBatchItem), _i, _op]),
     "psmma_tune_batch": (_i, [_i, C.POINTER(PsmmaBatchItem), _d, _d, _i, _d, _op, C.POINTER(PsmmaTuneResult), _p]),
 }
 

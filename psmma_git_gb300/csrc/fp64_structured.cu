@@ -377,7 +377,9 @@ int f64_group_prepare(const F64Prob* P, int count, void* dev, cudaStream_t strea
   for (int i = 0; i < count; ++i) {
     const F64Prob& q = P[i];
     if (q.M <= 0 || q.N <= 0 || q.K <= 0 || q.gs.kind != P[0].gs.kind) return PSMMA_EUNSUPPORTED;
-    if (q.gs.kind != KIND_CAUCHY && q.gs.kind != KIND_DENSE) return PSMMA_EUNSUPPORTED;
+    if (q.gs.kind != KIND_CAUCHY && q.gs.kind != KIND_DENSE && q.gs.kind != KIND_CAUCHY_EIG)
+      return PSMMA_EUNSUPPORTED;
+    if (q.gs.k1 > 0) return PSMMA_EUNSUPPORTED;  // tail rows: split path only
     F64Args& a = args[i];
     a.M = q.M; a.N = q.N; a.K = q.K; a.alpha = q.alpha; a.beta = q.beta;
     a.X = q.X; a.ldx = q.ldx; a.C = q.C; a.ldc = q.ldc; a.gs = q.gs;
@@ -408,13 +410,19 @@ int f64_group_enqueue(const F64Group& g, cudaStream_t stream) {
                              (int)F64_SMEM_BYTES) != cudaSuccess)
       return PSMMA_EDEVICE;
     k_struct_f64_group<KIND_CAUCHY><<<g.blocks, F64_THREADS, F64_SMEM_BYTES, stream>>>(a, g.d_t0, g.count);
+  } else if (g.kind == KIND_CAUCHY_EIG) {
+    if (cudaFuncSetAttribute(k_struct_f64_group<KIND_CAUCHY_EIG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)F64_SMEM_BYTES) != cudaSuccess)
+      return PSMMA_EDEVICE;
+    k_struct_f64_group<KIND_CAUCHY_EIG><<<g.blocks, F64_THREADS, F64_SMEM_BYTES, stream>>>(a, g.d_t0, g.count);
   } else {
     if (cudaFuncSetAttribute(k_struct_f64_group<KIND_DENSE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)F64_SMEM_BYTES) != cudaSuccess)
       return PSMMA_EDEVICE;
     k_struct_f64_group<KIND_DENSE><<<g.blocks, F64_THREADS, F64_SMEM_BYTES, stream>>>(a, g.d_t0, g.count);
   }
-  prof_mark(stream, g.kind == KIND_CAUCHY ? "f64_group_cauchy" : "f64_group_dense");
+  prof_mark(stream, g.kind == KIND_CAUCHY ? "f64_group_cauchy"
+                    : g.kind == KIND_CAUCHY_EIG ? "f64_group_cauchyeig" : "f64_group_dense");
   return cudaGetLastError() == cudaSuccess ? PSMMA_OK : PSMMA_EDEVICE;
 }
 

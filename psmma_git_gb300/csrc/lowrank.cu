@@ -421,7 +421,7 @@ constexpr int QR_CAP = 256;  // largest rank a tile is factorised to; beyond it 
 
 struct QrTile {
   int M, N, cap;                    // tile size; steps at most cap (<= min(M, N), <= QR_CAP)
-  const double *gD, *gU, *gF, *gV;  // generator slices
+  GenSpec gs;                       // generators of the tile (Cauchy or accurate-denominator Cauchy)
   double* T;     // M x N (ld M), columns pivoted; Q(:, 0:r) on exit
   double* V;     // M x cap (ld M): reflectors, V(k,k) = 1, rows < k unused
   double* F;     // F[c*cap + j]; on exit Y = R(0:r,:) P^T (r x N, ld r)
@@ -437,7 +437,8 @@ struct QrTile {
   long col0;     // first column of this tile in the batch's column numbering
 };
 
-// Explicit tiles T(i,c) = U(i)V(c)/(D(i)-F(c)) (ConstCauchy, Auxil_2p5D.f90:138-144), their
+// Explicit tiles T(i,c) = U(i)V(c)/(D(i)-F(c)) (ConstCauchy, Auxil_2p5D.f90:138-144) or with
+// the accurate denominators of CauchylikeEig (ConstCauchyEig, Auxil_2p5D.f90:532-637), their
 // column norms and the identity pivot; one block per column of the batch.
 __global__ void __launch_bounds__(QR_THREADS) k_qr_tiles(QrTile* tiles, int ntiles) {
   __shared__ double sm[33];
@@ -450,10 +451,15 @@ __global__ void __launch_bounds__(QR_THREADS) k_qr_tiles(QrTile* tiles, int ntil
   const QrTile& t = tiles[lo];
   const int c = (int)(gc - t.col0);
   if (c >= t.N) return;
-  const double f = t.gF[c], v = t.gV[c];
+  const GenSpec& g = t.gs;
+  const bool eig = g.kind == KIND_CAUCHY_EIG;
+  const double f = g.Fc[c], v = g.Vc[c];
+  const double f1 = (eig && c < g.fc1_len) ? g.Fc1[c] : 0.0;
+  const double dl = eig ? g.dl[c] : 0.0, dr = (eig && c < g.fc1_len) ? g.dr[c] : 0.0;
   double ss = 0.0;
   for (int i = threadIdx.x; i < t.M; i += blockDim.x) {
-    const double h = (t.gU[i] * v) / (t.gD[i] - f);
+    const double h = eig ? (g.Ur[i] * v) / eig_den(g.Dr[i], f, f1, dl, dr, i - c <= g.diag_off)
+                         : (g.Ur[i] * v) / (g.Dr[i] - f);
     t.T[i + (long)c * t.M] = h;
     ss = fma(h, h, ss);
   }
@@ -841,9 +847,24 @@ struct Plan {
   static constexpr int N_STATUS = 16;
 };
 
-GenSpec cauchy_sub(const double* gen, long ldgen, int r0, int c0) {
+// Generators of the sub-block H(r0:, c0:) of an item's n x n matrix.  Cauchy: gen = [D|F|U|V]
+// (ldgen); accurate-denominator Cauchy: gen = [F|U|V|DIFL|DIFR].
+GenSpec sub_gens(int kind, const double* gen, long ldgen, int n, int r0, int c0) {
   GenSpec g;
-  g.kind = KIND_CAUCHY;
+  g.kind = kind;
+  if (kind == KIND_CAUCHY_EIG) {
+    const double *F = gen, *U = gen + ldgen, *V = gen + 2 * ldgen, *DL = gen + 3 * ldgen, *DR = gen + 4 * ldgen;
+    g.Dr = F + r0;
+    g.Ur = U + r0;
+    g.Fc = F + c0;
+    g.Fc1 = F + c0 + 1;
+    g.Vc = V + c0;
+    g.dl = DL + c0;
+    g.dr = DR + c0;
+    g.fc1_len = n - 1 - c0;
+    g.diag_off = c0 - r0;
+    return g;
+  }
   g.Dr = gen + r0;
   g.Fc = gen + ldgen + c0;
   g.Ur = gen + 2 * ldgen + r0;
@@ -851,7 +872,7 @@ GenSpec cauchy_sub(const double* gen, long ldgen, int r0, int c0) {
   return g;
 }
 
-void make_plan(Plan& P, Bump& bump, const psmma_batch_item* items, int count, int compressor) {
+void make_plan(Plan& P, Bump& bump, const psmma_batch_item* items, int count, int compressor, int kind) {
   P.blocks.clear();
   for (int i = 0; i < count; ++i) {
     const int n = items[i].n, h = n / 2;
@@ -908,10 +929,7 @@ void make_plan(Plan& P, Bump& bump, const psmma_batch_item* items, int count, in
       q.M = ob.M;
       q.N = ob.N;
       q.cap = std::min(std::min(ob.M, ob.N), QR_CAP);
-      q.gD = it.gen + ob.r0;
-      q.gU = it.gen + 2 * (long)it.ldgen + ob.r0;
-      q.gF = it.gen + it.ldgen + ob.c0;
-      q.gV = it.gen + 3 * (long)it.ldgen + ob.c0;
+      q.gs = sub_gens(kind, it.gen, it.ldgen, it.n, ob.r0, ob.c0);
       q.T = bump.take<double>((size_t)ob.M * ob.N);
       q.V = bump.take<double>((size_t)ob.M * q.cap);
       q.F = bump.take<double>((size_t)ob.N * q.cap);
@@ -942,18 +960,18 @@ struct Rounds {
   int max_rank = 0, full_blocks = 0;
 };
 
-void build_rounds(const Plan& P, const psmma_batch_item* items, int count, int compressor, const int* ranks,
-                  double alpha, double beta, Rounds& R) {
+void build_rounds(const Plan& P, const psmma_batch_item* items, int count, int compressor, int kind,
+                  const int* ranks, double alpha, double beta, Rounds& R) {
   for (int i = 0; i < count; ++i) {
     const psmma_batch_item& it = items[i];
     const int n = it.n, h = n / 2;
     if (n == 0) continue;
     // diagonal blocks: Q(:, C1) = alpha A(:, R1) H(R1, C1) + beta Q(:, C1), and for R2, C2
     if (h > 0)
-      R.r1.push_back(SplitProblem{n, h, h, alpha, beta, it.A, it.lda, cauchy_sub(it.gen, it.ldgen, 0, 0), it.Q,
+      R.r1.push_back(SplitProblem{n, h, h, alpha, beta, it.A, it.lda, sub_gens(kind, it.gen, it.ldgen, n, 0, 0), it.Q,
                                   it.ldq});
     R.r1.push_back(SplitProblem{n, n - h, n - h, alpha, beta, it.A + (long)h * it.lda, it.lda,
-                                cauchy_sub(it.gen, it.ldgen, h, h), it.Q + (long)h * it.ldq, it.ldq});
+                                sub_gens(kind, it.gen, it.ldgen, n, h, h), it.Q + (long)h * it.ldq, it.ldq});
     R.executed += 2.0 * n * ((double)h * h + (double)(n - h) * (n - h));
   }
   const int nb = (int)P.blocks.size();
@@ -966,7 +984,7 @@ void build_rounds(const Plan& P, const psmma_batch_item* items, int count, int c
     if (Rk >= mn) {
       // not compressed: the generated tile (the reference would reuse a stale buffer here)
       ++R.full_blocks;
-      R.r2.push_back(SplitProblem{n, ob.N, ob.M, alpha, 1.0, Ablk, it.lda, cauchy_sub(it.gen, it.ldgen, ob.r0, ob.c0),
+      R.r2.push_back(SplitProblem{n, ob.N, ob.M, alpha, 1.0, Ablk, it.lda, sub_gens(kind, it.gen, it.ldgen, n, ob.r0, ob.c0),
                                   Qblk, it.ldq});
       R.executed += 2.0 * n * (double)ob.M * ob.N;
       continue;
@@ -1018,8 +1036,8 @@ void build_rounds(const Plan& P, const psmma_batch_item* items, int count, int c
 //   Q(:, C) = alpha * [A(:, R_d) | T] * [H(R_d, C); Y] + beta * Q(:, C),
 // with Y the rows of H(PL(1:Rk), C) (RRLU, Cauchy with the pivoted row generators) or
 // R P^T (RRQR, dense); an uncompressed block gives the whole column block A * H(:, C).
-void build_rounds_split(const Plan& P, const psmma_batch_item* items, int count, int compressor, const int* ranks,
-                        double alpha, double beta, Rounds& R) {
+void build_rounds_split(const Plan& P, const psmma_batch_item* items, int count, int compressor, int kind,
+                        const int* ranks, double alpha, double beta, Rounds& R) {
   // the off-diagonal block whose columns are C1 (rows R2) and C2 (rows R1), per item
   std::vector<int> blk_c1(count, -1), blk_c2(count, -1);
   for (int b = 0; b < (int)P.blocks.size(); ++b) {
@@ -1071,13 +1089,13 @@ void build_rounds_split(const Plan& P, const psmma_batch_item* items, int count,
       const int mn = b >= 0 ? std::min(P.blocks[b].M, P.blocks[b].N) : 0;
       if (b >= 0 && Rk >= mn) {
         // uncompressed: the whole column block A * H(:, C)
-        R.r2.push_back(SplitProblem{n, dn, n, alpha, beta, it.A, it.lda, cauchy_sub(it.gen, it.ldgen, 0, d0), Qc,
+        R.r2.push_back(SplitProblem{n, dn, n, alpha, beta, it.A, it.lda, sub_gens(kind, it.gen, it.ldgen, n, 0, d0), Qc,
                                     it.ldq});
         R.executed += 2.0 * n * (double)n * dn;
         continue;
       }
       SplitProblem q{n, dn, dn + Rk, alpha, beta, it.A + (long)d0 * it.lda, it.lda,
-                     cauchy_sub(it.gen, it.ldgen, d0, d0), Qc, it.ldq};
+                     sub_gens(kind, it.gen, it.ldgen, n, d0, d0), Qc, it.ldq};
       if (Rk > 0) {
         q.A2 = P.gather[b];
         q.lda2 = n;
@@ -1100,8 +1118,10 @@ void build_rounds_split(const Plan& P, const psmma_batch_item* items, int count,
 // Workspace of the product rounds (part B).
 struct RoundGroups {
   SplitGroup s1, s2;
-  F64Group f[4];  // round 1 Cauchy, round 1 dense, round 2 Cauchy, round 2 dense
+  F64Group f[6];  // per round: Cauchy, accurate-denominator Cauchy, dense
 };
+
+constexpr int kF64Kinds[3] = {KIND_CAUCHY, KIND_CAUCHY_EIG, KIND_DENSE};
 
 std::vector<F64Prob> f64_of(const std::vector<SplitProblem>& v, int kind) {
   std::vector<F64Prob> out;
@@ -1114,7 +1134,7 @@ size_t rounds_bytes(const Rounds& R, int precision, int n_moduli) {
   if (precision == PSMMA_PREC_SPLIT)
     return split_group_bytes(R.r1.data(), (int)R.r1.size(), n_moduli) + 4096 +
            split_group_bytes(R.r2.data(), (int)R.r2.size(), n_moduli) + 4096;
-  return f64_group_bytes((int)R.r1.size()) * 2 + f64_group_bytes((int)R.r2.size()) * 2 + 4096;
+  return f64_group_bytes((int)R.r1.size()) * 3 + f64_group_bytes((int)R.r2.size()) * 3 + 4096;
 }
 
 int prepare_rounds(const Rounds& R, int precision, int n_moduli, const SplitTune& tune, void* work,
@@ -1132,11 +1152,11 @@ int prepare_rounds(const Rounds& R, int precision, int n_moduli, const SplitTune
   }
   const std::vector<SplitProblem>* rs[2] = {&R.r1, &R.r2};
   for (int r = 0; r < 2; ++r)
-    for (int k = 0; k < 2; ++k) {
-      const std::vector<F64Prob> v = f64_of(*rs[r], k == 0 ? KIND_CAUCHY : KIND_DENSE);
+    for (int k = 0; k < 3; ++k) {
+      const std::vector<F64Prob> v = f64_of(*rs[r], kF64Kinds[k]);
       char* w = b.take<char>(f64_group_bytes((int)v.size()), 256);
       if (b.off > lwork) return PSMMA_EWORKSPACE;
-      const int rc = f64_group_prepare(v.data(), (int)v.size(), w, st, &G.f[2 * r + k]);
+      const int rc = f64_group_prepare(v.data(), (int)v.size(), w, st, &G.f[3 * r + k]);
       if (rc) return rc;
     }
   return PSMMA_OK;
@@ -1149,13 +1169,13 @@ int enqueue_rounds(const RoundGroups& G, int precision, unsigned* status, cudaSt
     if (!rc) rc = split_group_enqueue(G.s2, st, status + 1);
     return rc;
   }
-  for (int i = 0; i < 4 && !rc; ++i) rc = f64_group_enqueue(G.f[i], st);
+  for (int i = 0; i < 6 && !rc; ++i) rc = f64_group_enqueue(G.f[i], st);
   return rc;
 }
 
 // Worst-case part B for a batch (every block at its largest rank and also uncompressed).
-size_t rounds_bound(const Plan& P, const psmma_batch_item* items, int count, int compressor, int precision,
-                    int n_moduli) {
+size_t rounds_bound(const Plan& P, const psmma_batch_item* items, int count, int compressor, int kind,
+                    int precision, int n_moduli) {
   const int nb = (int)P.blocks.size();
   std::vector<int> rk(nb), full(nb);
   for (int b = 0; b < nb; ++b) {
@@ -1165,8 +1185,8 @@ size_t rounds_bound(const Plan& P, const psmma_batch_item* items, int count, int
   }
   Rounds a, f;
   auto build = precision == PSMMA_PREC_SPLIT ? build_rounds_split : build_rounds;
-  build(P, items, count, compressor, rk.data(), 1.0, 0.0, a);
-  build(P, items, count, compressor, full.data(), 1.0, 0.0, f);
+  build(P, items, count, compressor, kind, rk.data(), 1.0, 0.0, a);
+  build(P, items, count, compressor, kind, full.data(), 1.0, 0.0, f);
   return rounds_bytes(a, precision, n_moduli) + rounds_bytes(f, precision, n_moduli);
 }
 
@@ -1269,9 +1289,9 @@ int check_batch(int count, const psmma_batch_item* items, int precision, int n_m
   return PSMMA_OK;
 }
 
-size_t part_a_bytes(Plan& P, const psmma_batch_item* items, int count, int compressor) {
+size_t part_a_bytes(Plan& P, const psmma_batch_item* items, int count, int compressor, int kind) {
   Bump m(nullptr);
-  make_plan(P, m, items, count, compressor);
+  make_plan(P, m, items, count, compressor, kind);
   return m.off + 4096;
 }
 
@@ -1347,34 +1367,46 @@ void tune_store(unsigned long long sig, const SplitTune& t) {
 
 }  // namespace
 
-extern "C" size_t psmma_batch_workspace_size(int count, const psmma_batch_item* items, int compressor,
-                                             const psmma_opts* opts) {
+static size_t batch_workspace(int kind, int count, const psmma_batch_item* items, int compressor,
+                              const psmma_opts* opts) {
   const int precision = opts ? opts->precision : PSMMA_PREC_FP64;
   const int n_moduli = opts ? opts->n_moduli : 0;
   if (count <= 0 || !items || check_batch(count, items, precision, n_moduli, compressor, 0.5)) return 0;
+  if (kind == KIND_CAUCHY_EIG && compressor != PSMMA_COMPRESS_RRQR) return 0;
   Plan P;
-  const size_t a = part_a_bytes(P, items, count, compressor);
-  return a + rounds_bound(P, items, count, compressor, precision, n_moduli) + 4096;
+  const size_t a = part_a_bytes(P, items, count, compressor, kind);
+  return a + rounds_bound(P, items, count, compressor, kind, precision, n_moduli) + 4096;
 }
 
-extern "C" int psmma_cauchy_batch_lowrank(int count, const psmma_batch_item* items, double alpha, double beta,
-                                          int compressor, double tol, const psmma_opts* opts, int* ranks_out,
-                                          psmma_batch_stats* stats, void* stream) {
+extern "C" size_t psmma_batch_workspace_size(int count, const psmma_batch_item* items, int compressor,
+                                             const psmma_opts* opts) {
+  return batch_workspace(KIND_CAUCHY, count, items, compressor, opts);
+}
+
+extern "C" size_t psmma_cauchyeig_batch_workspace_size(int count, const psmma_batch_item* items, int compressor,
+                                                       const psmma_opts* opts) {
+  return batch_workspace(KIND_CAUCHY_EIG, count, items, compressor, opts);
+}
+
+static int batch_run(int kind, int count, const psmma_batch_item* items, double alpha, double beta, int compressor,
+                     double tol, const psmma_opts* opts, int* ranks_out, psmma_batch_stats* stats, void* stream) {
   const int precision = opts ? opts->precision : PSMMA_PREC_FP64;
   const int n_moduli = opts ? opts->n_moduli : 0;
   int rc = check_batch(count, items, precision, n_moduli, compressor, tol);
   if (rc) return rc;
+  // the structured RRLU of accurate-denominator blocks (rrluCauchyEigrow) is not built
+  if (kind == KIND_CAUCHY_EIG && compressor != PSMMA_COMPRESS_RRQR) return PSMMA_EUNSUPPORTED;
   if (stats) *stats = psmma_batch_stats{0.0, 0.0, 0.0, 0, 0, 0, 0};
   if (count == 0) return PSMMA_OK;
   cudaStream_t st = (cudaStream_t)stream;
 
   Plan P;
-  const size_t need_a = part_a_bytes(P, items, count, compressor);
+  const size_t need_a = part_a_bytes(P, items, count, compressor, kind);
   char* work_a = nullptr;
   char* work_b = nullptr;
   size_t lwork_b = 0;
   if (opts && opts->work) {
-    const size_t bound = need_a + rounds_bound(P, items, count, compressor, precision, n_moduli) + 4096;
+    const size_t bound = need_a + rounds_bound(P, items, count, compressor, kind, precision, n_moduli) + 4096;
     if (opts->lwork < bound) return PSMMA_EWORKSPACE;
     work_a = (char*)opts->work;
     work_b = (char*)((((uintptr_t)work_a + need_a) + 4095) & ~(uintptr_t)4095);
@@ -1384,7 +1416,7 @@ extern "C" int psmma_cauchy_batch_lowrank(int count, const psmma_batch_item* ite
     if (rc) return rc;
   }
   Bump bump((void*)(((uintptr_t)work_a + 255) & ~(uintptr_t)255));
-  make_plan(P, bump, items, count, compressor);
+  make_plan(P, bump, items, count, compressor, kind);
   const int nb = (int)P.blocks.size();
   if (cudaMemsetAsync(P.d_status, 0, sizeof(unsigned) * Plan::N_STATUS, st) != cudaSuccess) return PSMMA_EDEVICE;
   unsigned* qr_status = P.d_status + 8;
@@ -1476,8 +1508,8 @@ extern "C" int psmma_cauchy_batch_lowrank(int count, const psmma_batch_item* ite
 
   // ---- phase 2: the product rounds, one CUDA graph
   Rounds R;
-  (precision == PSMMA_PREC_SPLIT ? build_rounds_split : build_rounds)(P, items, count, compressor, ranks.data(),
-                                                                      alpha, beta, R);
+  (precision == PSMMA_PREC_SPLIT ? build_rounds_split : build_rounds)(P, items, count, compressor, kind,
+                                                                      ranks.data(), alpha, beta, R);
   const size_t need_b = rounds_bytes(R, precision, n_moduli);
   if (!work_b) {
     work_b = (char*)pool_get(need_b, st, &rc, 1);
@@ -1485,7 +1517,7 @@ extern "C" int psmma_cauchy_batch_lowrank(int count, const psmma_batch_item* ite
     lwork_b = need_b;
   }
   RoundGroups G;
-  const SplitTune tune = tune_for(batch_signature(count, items, compressor, precision, n_moduli));
+  const SplitTune tune = tune_for(batch_signature(count, items, compressor + 4 * kind, precision, n_moduli));
   rc = prepare_rounds(R, precision, n_moduli, tune, work_b, lwork_b, st, G);
   if (rc) return rc;
   std::vector<GatherDesc> gd;
@@ -1577,6 +1609,18 @@ extern "C" int psmma_cauchy_batch_lowrank(int count, const psmma_batch_item* ite
   return rc;
 }
 
+extern "C" int psmma_cauchy_batch_lowrank(int count, const psmma_batch_item* items, double alpha, double beta,
+                                          int compressor, double tol, const psmma_opts* opts, int* ranks_out,
+                                          psmma_batch_stats* stats, void* stream) {
+  return batch_run(KIND_CAUCHY, count, items, alpha, beta, compressor, tol, opts, ranks_out, stats, stream);
+}
+
+extern "C" int psmma_cauchyeig_batch_lowrank(int count, const psmma_batch_item* items, double alpha, double beta,
+                                             int compressor, double tol, const psmma_opts* opts, int* ranks_out,
+                                             psmma_batch_stats* stats, void* stream) {
+  return batch_run(KIND_CAUCHY_EIG, count, items, alpha, beta, compressor, tol, opts, ranks_out, stats, stream);
+}
+
 extern "C" int psmma_tune_batch(int count, const psmma_batch_item* items, double alpha, double beta, int compressor,
                                 double tol, const psmma_opts* opts, psmma_tune_result* out, void* stream) {
   const int precision = opts ? opts->precision : PSMMA_PREC_FP64;
@@ -1598,11 +1642,11 @@ extern "C" int psmma_tune_batch(int count, const psmma_batch_item* items, double
   SplitTune best_t = dflt;
   for (size_t c = 0; c < cands.size() && !rc; ++c) {
     t_force = &cands[c];
-    rc = psmma_cauchy_batch_lowrank(count, items, alpha, beta, compressor, tol, opts, nullptr, nullptr, stream);
+    rc = batch_run(KIND_CAUCHY, count, items, alpha, beta, compressor, tol, opts, nullptr, nullptr, stream);
     float ms = 0.0f;
     for (int rep = 0; rep < 2 && !rc; ++rep) {  // the faster of two timed runs (the first warmed up)
       cudaEventRecord(e0, st);
-      rc = psmma_cauchy_batch_lowrank(count, items, alpha, beta, compressor, tol, opts, nullptr, nullptr, stream);
+      rc = batch_run(KIND_CAUCHY, count, items, alpha, beta, compressor, tol, opts, nullptr, nullptr, stream);
       cudaEventRecord(e1, st);
       float t = 0.0f;
       if (!rc && (cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&t, e0, e1) != cudaSuccess))

@@ -242,8 +242,12 @@ __device__ __forceinline__ void h_pass1_blk(const GenSpec& gs, int K, int kp, do
           h = div_nr(u * v, d - w);     // U(i)*V(j) / (D(i)-F(j))
         }
       } else if (KIND == KIND_CAUCHY_EIG) {
-        const double fi = __ldg(gs.Dr + kk), u = __ldg(gs.Ur + kk);
-        h = div_nr(u * v, eig_den(fi, w, w1, dlj, drj, kk - j <= gs.diag_off));
+        if (gs.k1 > 0 && kk >= gs.k1) {
+          h = __ldg(gs.B + (kk - gs.k1) + (long)j * gs.ldb);  // dense tail rows (merged products)
+        } else {
+          const double fi = __ldg(gs.Dr + kk), u = __ldg(gs.Ur + kk);
+          h = div_nr(u * v, eig_den(fi, w, w1, dlj, drj, kk - j <= gs.diag_off));
+        }
       } else if (KIND == KIND_TOEPLITZ) {
         h = __ldg(gs.g + (gs.order - 1) + j - kk);
       } else if (KIND == KIND_HANKEL) {

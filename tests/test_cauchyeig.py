@@ -110,3 +110,46 @@ def test_cauchyeig_host_and_fortran_abi():
                          C.c_void_p(Qf.ctypes.data), i(1), i(1), desc, None, i(0))
     assert lib.psmma_last_status() == 0
     assert O.rel_fro(Qf, ref) < 1e-13
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec,tol", [("fp64", 1e-13), ("split", 1e-12)])
+def test_cauchyeig_merge_level_rrqr(prec, tol):
+    import torch
+    import psmma_git_gb300 as P
+    sizes = [1, 2, 37, 300, 1031]
+    probs, dev = [], []
+    for i, n in enumerate(sizes):
+        F, U, V, dl, dr = O.eig_generators(n, seed=40 + i, tiny=n // 50)
+        A = O.cfg_matrix(n, n, seed=50 + i)
+        Q0 = O.cfg_matrix(n, n, seed=60 + i)
+        probs.append((A, (F, U, V, dl, dr), Q0))
+        dA = P.fortran_empty(n, n)
+        dA.copy_(torch.from_numpy(A))
+        g = torch.from_numpy(np.stack([F, U, V, dl, dr], axis=1)).cuda().t().contiguous().t()  # n x 5
+        dQ = P.fortran_empty(n, n)
+        dQ.copy_(torch.from_numpy(Q0))
+        dev.append((dA, g, dQ))
+    ranks, info = P.cauchy_batch_lowrank(dev, 0.5, -1.0, compressor="rrqr", tol=1e-14, precision=prec, eig=True)
+    torch.cuda.synchronize()
+    k = 0
+    for (A, gens, Q0), (_, _, dQ) in zip(probs, dev):
+        Qo, ro = O.merge_level_eig_product(A, *gens, Q0, 0.5, -1.0, 1e-14)
+        exact = 0.5 * A @ O.cauchy_like_eig(*gens) - Q0
+        got = dQ.cpu().numpy()
+        for a, b in zip(ranks[k:k + len(ro)], ro):
+            assert abs(a - b) <= 1
+        k += len(ro)
+        assert O.rel_fro(got, Qo) < tol
+        assert O.rel_fro(got, exact) < tol
+    assert info["n_blocks"] == k
+
+
+def test_cauchyeig_batch_rejects_rrlu(lib):
+    items = (_lib.PsmmaBatchItem * 1)()
+    buf = np.zeros(64)
+    p = buf.ctypes.data
+    items[0].n, items[0].A, items[0].lda, items[0].gen, items[0].ldgen = 4, p, 4, p, 4
+    items[0].Q, items[0].ldq = p, 4
+    assert lib.psmma_cauchyeig_batch_lowrank(1, items, 1.0, 0.0, _lib.COMPRESS_RRLU, 1e-14, None, None, None,
+                                             None) == _lib.PSMMA_EUNSUPPORTED
