@@ -591,7 +591,7 @@ def run_merge_level(args, ws, rank, local):
         F, U, V, dl, dr = O.eig_generators(n, seed=200 + i, tiny=n // 100)
         gen = torch.from_numpy(np.ascontiguousarray(np.stack([F, U, V, dl, dr]))).to(dev).t()
         eig_probs.append((probs[i][0], gen, probs[i][2]))
-    runs = [(c, p, False) for c in ["rrqr", "rrlu"] for p in precisions] + [("rrqr", "split", True)]
+    runs = [(c, p, False) for c in ["rrqr", "rrlu"] for p in precisions] + [(c, "split", True) for c in ["rrqr", "rrlu"]]
     for comp, prec, eig in runs:
         batch = eig_probs if eig else probs
         kw = dict(compressor=comp, tol=1e-14, precision=prec, n_moduli=args.n_moduli, eig=eig)

@@ -193,9 +193,10 @@ int psmma_cauchy_batch_lowrank(int count, const psmma_batch_item* items, double 
 /* The same merge level for the eigensolver's matrices (PSCAUCHYEIG_COMPUTE's low-rank
  * branch, pscauchyeig_compute.f90:371-391 with ConstCauchyEiglowrank, Auxil_2p5D.f90:642-748):
  * each item's gen is [F|U|V|DIFL|DIFR] (ldgen >= n, the arguments of psmma_cauchyeig) and H
- * has the accurate denominators of CauchylikeEig.  Compressor: PSMMA_COMPRESS_RRQR on the
- * explicit tiles (the reference's structured rrluCauchyEigrow is not built here:
- * PSMMA_COMPRESS_RRLU returns PSMMA_EUNSUPPORTED). */
+ * has the accurate denominators of CauchylikeEig.  Compressors: PSMMA_COMPRESS_RRLU is the
+ * reference's structured rrluCauchyEigrow with Compress_cauchyEig2's factors
+ * (CauchyHssEig.f90:7-212, 2640-2829: every F(i) - D(j) and D(j) - D(k) formed from DIFL/DIFR);
+ * PSMMA_COMPRESS_RRQR factorises the explicit tiles. */
 int psmma_cauchyeig_batch_lowrank(int count, const psmma_batch_item* items, double alpha, double beta,
                                   int compressor, double tol, const psmma_opts* opts, int* ranks_out,
                                   psmma_batch_stats* stats, void* stream);

@@ -785,12 +785,13 @@ def exact_cauchy_eig_product(A, F, U, V, DIFL, DIFR):
     return out
 
 
-def merge_level_eig_product(A, F, U, V, DIFL, DIFR, beta_Q, alpha: float, beta: float, tol: float = 1e-14):
+def merge_level_eig_product(A, F, U, V, DIFL, DIFR, beta_Q, alpha: float, beta: float, tol: float = 1e-14,
+                            compressor: str = "rrqr"):
     """The merge level of merge_level_product for the eigensolver's matrix H =
-    cauchy_like_eig(F, U, V, DIFL, DIFR): diagonal blocks dense, off-diagonal tiles (built by
-    ConstCauchyEig's rule) compressed by Compress_RRQR, Q(:,C) += alpha (A(:,R) X) Y.  (The
-    reference compresses these tiles with the structured rrluCauchyEigrow,
-    CauchyHssEig.f90:7-212; RRQR is this build's compressor for them.)  Returns (Q, ranks)."""
+    cauchy_like_eig(F, U, V, DIFL, DIFR): diagonal blocks dense, off-diagonal tiles
+    compressed by Compress_RRQR on the tile built by ConstCauchyEig's rule ("rrqr") or by the
+    structured Compress_cauchyEig2 (rrluCauchyEigrow, CauchyHssEig.f90:2640-2829; "rrlu",
+    the reference's own choice), then Q(:,C) += alpha (A(:,R) X) Y.  Returns (Q, ranks)."""
     A = np.asarray(A, dtype=np.float64)
     n = A.shape[0]
     Q = (beta * np.asarray(beta_Q, dtype=np.float64)) if beta != 0.0 else np.zeros((n, n))
@@ -805,10 +806,181 @@ def merge_level_eig_product(A, F, U, V, DIFL, DIFR, beta_Q, alpha: float, beta: 
         return Q, ranks
     for (r0, r1, c0, c1) in [(0, h, h, n), (h, n, 0, h)]:
         T = H[r0:r1, c0:c1]
-        X, Y, rk = compress_rrqr(T, tol)
+        if compressor == "rrqr":
+            X, Y, rk = compress_rrqr(T, tol)
+        else:
+            X, Y, rk = compress_cauchy_eig(F, U, V, DIFL, DIFR, np.arange(r0 + 1, r1 + 1),
+                                           np.arange(c0 + 1, c1 + 1), tol)
         ranks.append(rk)
         if X is None:
             Q[:, c0:c1] += alpha * (A[:, r0:r1] @ T)
         elif rk > 0:
             Q[:, c0:c1] += alpha * ((A[:, r0:r1] @ X) @ Y)
     return Q, ranks
+
+
+# ---------------------------------------------------------------------------------------
+# Structured RRLU of accurate-denominator Cauchy blocks (CauchyHssEig.f90)
+# ---------------------------------------------------------------------------------------
+def _fd(FF, DL, DR, pl, pu):
+    """computfd (CauchyHssEig.f90:519-568): F(pl) - D(pu) with 1-based global indices,
+    (FF(pl) - FF(pu)) - DIFL(pu) for pl <= pu, else (FF(pl) - FF(pu+1)) - DIFR(pu).  Arrays."""
+    pl = np.asarray(pl)
+    pu = np.asarray(pu)
+    pu1 = np.minimum(pu, len(FF) - 1)  # FF(pu+1), not used when pu = n
+    return np.where(pl <= pu, (FF[pl - 1] - FF[pu - 1]) - DL[pu - 1], (FF[pl - 1] - FF[pu1]) - DR[pu - 1])
+
+
+def _dd(FF, DL, DR, pj, pk):
+    """computdd (CauchyHssEig.f90:470-516): D(pj) - D(pk), 1-based global indices.  Arrays."""
+    pj = np.asarray(pj)
+    pk = np.asarray(pk)
+    a = np.minimum(pj, len(FF) - 1)
+    b = np.minimum(pk, len(FF) - 1)
+    return np.where(pj < pk, (FF[a] - FF[pk - 1]) + DR[pj - 1] - DL[pk - 1],
+                    (FF[pj - 1] - FF[b]) + DL[pj - 1] - DR[pk - 1])
+
+
+def _argmax1(v):
+    j = int(np.argmax(v))  # MAXLOC: the first maximum
+    return float(v[j]), j + 1
+
+
+def _pivt_eig(F, U, V, PL, PU, PQ, A, k, M, N, FF, DL, DR):
+    """CauchyPivtEig (CauchyHssEig.f90:571-717), with CauchyMaxEigmc / CauchyMaxEigm
+    (:1506-1589, :1418-1503).  The pivot magnitude uses FF(PL(k)) (the reference reads the
+    local row-pole array F at the global index PL(k), :676-678, which equals it only for an
+    unpermuted block starting at row 1)."""
+    k0 = k - 1
+    col = lambda: _argmax1(np.abs(U[k0:M] / _fd(FF, DL, DR, PL[k0:M], PU[k0])))
+    row = lambda: _argmax1(np.abs(V[k0:N] / _fd(FF, DL, DR, PL[k0], PU[k0:N])))
+    junkL, jjL = col()
+    junkU, jjU = row()
+    junkL *= abs(V[k0])
+    junkU *= abs(U[k0])
+    piv = abs(U[k0] * V[k0] / _fd(FF, DL, DR, PL[k0], PU[k0]))
+    if junkL <= piv and junkU <= piv:
+        return
+    flg = 1 if junkL > junkU else 0
+    while True:
+        if flg == 1:
+            a, b = k0, jjL + k0 - 1
+            for arr in (F, U, A, PL, PQ):
+                arr[a], arr[b] = arr[b], arr[a]
+            junkU, jjU = row()
+            if jjU == 1:
+                return
+            flg = 0
+        a, b = k0, jjU + k0 - 1
+        for arr in (V, PU):
+            arr[a], arr[b] = arr[b], arr[a]
+        junkL, jjL = col()
+        if jjL == 1:
+            return
+        flg = 1
+
+
+def _pivt_eig_cp(F, U, V, PL, PU, PQ, A, k, M, N, FF, DL, DR):
+    """CauchyPivtEig_CP (CauchyHssEig.f90:1004-1134): complete pivoting, strict '>' over
+    columns after the first, MAXLOC within a column."""
+    k0 = k - 1
+    best, ii, jj = -1.0, 1, 1
+    for j in range(1, N - k + 2):
+        junk, i1 = _argmax1(np.abs(U[k0:M] / _fd(FF, DL, DR, PL[k0:M], PU[k0 + j - 1])))
+        junk = abs(junk * V[k0 + j - 1])
+        if j == 1 or junk > best:
+            best, ii, jj = junk, i1, j
+    a, b = k0, ii + k0 - 1
+    for arr in (F, U, A, PL, PQ):
+        arr[a], arr[b] = arr[b], arr[a]
+    a, b = k0, jj + k0 - 1
+    for arr in (V, PU):
+        arr[a], arr[b] = arr[b], arr[a]
+
+
+def rrlu_cauchy_eig_row(F, A, V, PL, PU, tol, M, N, FF, DL, DR):
+    """rrluCauchyEigrow (CauchyHssEig.f90:7-212): the structured RRLU of a block of the
+    eigensolver's Cauchy matrix, rows with old eigenvalues F = FF(PL) and weights A, columns
+    PU (new eigenvalues, through DIFL/DIFR) with weights V.  rho = 1.2, swap check every 5
+    steps.  Returns (F, A, Z, V, W, PL, PU, PQ, Rk): permuted row poles and weights, the
+    Schur weights Z, interpolation weights W and the local row permutation PQ (1-based)."""
+    F = np.array(F, dtype=np.float64)
+    A = np.array(A, dtype=np.float64)
+    V = np.array(V, dtype=np.float64)
+    PL = np.array(PL)
+    PU = np.array(PU)
+    FF = np.asarray(FF, dtype=np.float64)
+    DL = np.asarray(DL, dtype=np.float64)
+    DR = np.asarray(DR, dtype=np.float64)
+    U = A.copy()
+    PQ = np.arange(1, M + 1)
+    mn = min(M, N)
+    W = np.zeros(mn)
+    Rk = mn
+    amax = 0.0
+    rho, prd = 1.2, 5
+    fd = lambda pl, pu: _fd(FF, DL, DR, pl, pu)
+    for k in range(1, mn + 1):
+        k0 = k - 1
+        _pivt_eig(F, U, V, PL, PU, PQ, A, k, M, N, FF, DL, DR)
+        ukk = U[k0] * V[k0] / fd(PL[k0], PU[k0])
+        amax = max(amax, abs(ukk))
+        if abs(ukk) < tol * amax:
+            _pivt_eig_cp(F, U, V, PL, PU, PQ, A, k, M, N, FF, DL, DR)
+            ukk = U[k0] * V[k0] / fd(PL[k0], PU[k0])
+            amax = max(amax, abs(ukk))
+            if abs(ukk) < tol * amax:
+                Rk = k - 1
+                break
+        U[k:M] = U[k:M] * ((F[k:M] - F[k0]) / fd(PL[k:M], PU[k0]))
+        V[k:N] = V[k:N] * (_dd(FF, DL, DR, PU[k:N], PU[k0]) / (-fd(PL[k0], PU[k:N])))
+        for j in range(k - 1):
+            W[j] = W[j] * ((-fd(PL[j], PU[k0])) / (F[k0] - F[j]))
+        W[k0] = fd(PL[k0], PU[k0]) / A[k0]
+        for j in range(k - 1):
+            W[k0] = W[k0] * ((-fd(PL[k0], PU[j])) / (F[j] - F[k0]))
+        flgl = k % prd
+        while flgl < 1:
+            flgl = 1
+            ii, jj, nmax = _search_max2(U[k:], W, F[k:], F, M - k, k)   # searchMax2Eig, :1137-1203
+            if nmax > rho:
+                flgl = 0
+                jj = jj + k
+                i0, j0 = ii - 1, jj - 1
+                V[k:N] = V[k:N] * ((-fd(PL[i0], PU[k:N])) / (-fd(PL[j0], PU[k:N])))
+                U[k:j0] = U[k:j0] * ((F[k:j0] - F[j0]) / (F[k:j0] - F[i0]))
+                U[jj:M] = U[jj:M] * ((F[jj:M] - F[j0]) / (F[jj:M] - F[i0]))
+                W[:i0] = W[:i0] * ((F[:i0] - F[i0]) / (F[:i0] - F[j0]))
+                W[ii:k] = W[ii:k] * ((F[ii:k] - F[i0]) / (F[ii:k] - F[j0]))
+                U[j0] = A[i0] * ((F[i0] - F[j0]) / fd(PL[i0], PU[i0]))
+                W[i0] = fd(PL[j0], PU[i0]) / A[j0]
+                for j in list(range(ii - 1)) + list(range(ii, k)):
+                    U[j0] = U[j0] * ((F[i0] - F[j]) / fd(PL[i0], PU[j]))
+                    W[i0] = W[i0] * ((-fd(PL[j0], PU[j])) / (F[j] - F[j0]))
+                for arr in (PL, PQ, F, A):
+                    arr[i0], arr[j0] = arr[j0], arr[i0]
+    return F, A, U, V, W, PL, PU, PQ, Rk
+
+
+def compress_cauchy_eig(FF, U, V, DL, DR, rows, cols, tol):
+    """Compress_cauchyEig2 (CauchyHssEig.f90:2640-2829) on the block rows x cols (1-based
+    global index arrays) of the eigensolver's matrix: rrluCauchyEigrow, then
+    X = P^-1 [I; Z'], Z'(t,j) = Z(Rk+t) W(j) / (F(Rk+t) - F(j)) (CauchylikeEigQ, :1882-1905)
+    and Y = CauchylikeEig rows PL(1:Rk) with the unpermuted columns.  Returns (X, Y, Rk);
+    (None, None, Rk) when Rk = min(M, N) (the tile is used as is)."""
+    FF = np.asarray(FF, dtype=np.float64)
+    rows = np.asarray(rows)
+    cols = np.asarray(cols)
+    M, N = len(rows), len(cols)
+    F0 = FF[rows - 1]
+    LF, LA, Z, _V, W, PL, _PU, PQ, Rk = rrlu_cauchy_eig_row(F0, np.asarray(U)[rows - 1], np.asarray(V)[cols - 1],
+                                                            rows.copy(), cols.copy(), tol, M, N, FF, DL, DR)
+    if Rk >= min(M, N):
+        return None, None, Rk
+    inv = np.empty(M, dtype=np.int64)
+    inv[PQ - 1] = np.arange(1, M + 1)
+    Q = cauchy_like2(LF[Rk:], LF, Z[Rk:], W, M, Rk)
+    X = Q[inv - 1, :]
+    den = _fd(FF, DL, DR, PL[:Rk, None], cols[None, :])
+    Y = (LA[:Rk, None] * np.asarray(V)[cols - 1][None, :]) / den
+    return X, Y, Rk

@@ -204,7 +204,7 @@ def cauchy_batch_lowrank(problems, alpha, beta, *, compressor="rrqr", tol=1e-14,
     """Q_i := alpha*A_i*H_i + beta*Q_i for problems = [(A_i, gen_i, Q_i), ...] (n_i x n_i CUDA
     tensors, gen_i = [D|F|U|V]), H_i split 2 x 2 with its off-diagonal blocks compressed by
     ``compressor`` ("rrqr" or "rrlu") at ``tol``.  With eig=True the H_i are the eigensolver's
-    matrices (psmma_cauchyeig) and gen_i = [F|U|V|DIFL|DIFR] (RRQR only).  Returns (ranks,
+    matrices (psmma_cauchyeig) and gen_i = [F|U|V|DIFL|DIFR].  Returns (ranks,
     stats): two ranks per problem with n >= 2 (blocks H(1:h, h+1:n), H(h+1:n, 1:h)) and a dict
     of flop counts."""
     lib = load()

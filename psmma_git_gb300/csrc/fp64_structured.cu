@@ -149,7 +149,8 @@ __device__ __forceinline__ void gen_H_tile(double* Bs, const F64Args& p, int n0,
         h = (u * colV) / (d - colF);                  // U(i)*V(j) / (D(i)-F(j))
       } else if (KIND == KIND_CAUCHY_EIG) {
         const double fi = __ldg(p.gs.Dr + gk), u = __ldg(p.gs.Ur + gk);
-        h = (u * colV) / eig_den(fi, colF, cg.F1, cg.dl, cg.dr, gk - gj <= p.gs.diag_off);
+        const bool upper = p.gs.rglob ? (__ldg(p.gs.rglob + gk) - 1 <= p.gs.cg0 + gj) : (gk - gj <= p.gs.diag_off);
+        h = (u * colV) / eig_den(fi, colF, cg.F1, cg.dl, cg.dr, upper);
       } else if (KIND == KIND_TOEPLITZ) {
         h = __ldg(p.gs.g + (p.gs.order - 1) + gj - gk);  // G(K + j - i), 1-based
       } else {

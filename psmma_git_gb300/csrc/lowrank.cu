@@ -376,7 +376,8 @@ __global__ void __launch_bounds__(RRLU_THREADS) k_cp_search(const RrluBlock* blo
   }
 }
 
-__global__ void k_cp_reduce(RrluBlock* blocks, const int* __restrict__ blk, const int* __restrict__ first,
+template <class Block>
+__global__ void k_cp_reduce(Block* blocks, const int* __restrict__ blk, const int* __restrict__ first,
                             int count, int total, const Cand* __restrict__ cand) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= count) return;
@@ -385,6 +386,237 @@ __global__ void k_cp_reduce(RrluBlock* blocks, const int* __restrict__ blk, cons
   for (int c = first[t] + 1; c < e; ++c) r = better_c(r, cand[c]);
   blocks[blk[t]].cp_i = r.i;
   blocks[blk[t]].cp_j = r.j;
+}
+
+
+// ------------------------------------------------------------------------------------------
+// RRLU of accurate-denominator blocks (rrluCauchyEigrow, CauchyHssEig.f90:7-212)
+// ------------------------------------------------------------------------------------------
+// Rows carry old eigenvalues F = FF(PL) and weights; columns the new eigenvalues D(PU), seen
+// only through DIFL/DIFR: every F(i) - D(j) and D(j) - D(k) is formed by computfd / computdd
+// (:470-568) from the global arrays with 1-based global indices PL, PU.
+struct RrluEigBlock {
+  int M, N;
+  const double *FF, *DL, *DR;  // global old eigenvalues and distances (n entries)
+  int nglob;
+  const double *gU, *gV;       // row weights U(r0 + i), column weights V(c0 + j)
+  int r0, c0;                  // global 0-based offsets of the block
+  double *F, *A, *U, *V, *W;   // row poles (permuted), row weights (becomes LU), Schur weights (Z),
+                               // column weights, interpolation weights (min(M, N))
+  int *PL, *PU, *PQ;           // global 1-based row / column indices (permuted), local row permutation
+  int* rank;
+  int k_next, phase, cp_i, cp_j;  // resumable state, as RrluBlock
+  double amax;
+};
+
+// computfd: F(pl) - D(pu) (CauchyHssEig.f90:519-568)
+__device__ __forceinline__ double eig_fd(const RrluEigBlock& b, int pl, int pu) {
+  return pl <= pu ? (b.FF[pl - 1] - b.FF[pu - 1]) - b.DL[pu - 1] : (b.FF[pl - 1] - b.FF[pu]) - b.DR[pu - 1];
+}
+// computdd: D(pj) - D(pk) (CauchyHssEig.f90:470-516), pj != pk
+__device__ __forceinline__ double eig_dd(const RrluEigBlock& b, int pj, int pk) {
+  return pj < pk ? (b.FF[pj] - b.FF[pk - 1]) + b.DR[pj - 1] - b.DL[pk - 1]
+                 : (b.FF[pj - 1] - b.FF[min(pk, b.nglob - 1)]) + b.DL[pj - 1] - b.DR[pk - 1];
+}
+
+// CauchyMaxEigmc (:1506-1589): max_i |U(i) / (F(PL(i)) - D(PU(k0)))|, i in [k0, M), 1-based offset
+__device__ ArgMax eig_col_max(const RrluEigBlock& b, int k0, ArgMax* sm) {
+  ArgMax best{-1.0, 0x7fffffff};
+  const int pu = b.PU[k0];
+  for (int i = k0 + threadIdx.x; i < b.M; i += blockDim.x)
+    best = better(best, ArgMax{fabs(b.U[i] / eig_fd(b, b.PL[i], pu)), i - k0 + 1});
+  return block_argmax(best, sm);
+}
+// CauchyMaxEigm (:1418-1503): max_j |V(j) / (F(PL(k0)) - D(PU(j)))|, j in [k0, N)
+__device__ ArgMax eig_row_max(const RrluEigBlock& b, int k0, ArgMax* sm) {
+  ArgMax best{-1.0, 0x7fffffff};
+  const int pl = b.PL[k0];
+  for (int j = k0 + threadIdx.x; j < b.N; j += blockDim.x)
+    best = better(best, ArgMax{fabs(b.V[j] / eig_fd(b, pl, b.PU[j])), j - k0 + 1});
+  return block_argmax(best, sm);
+}
+
+__device__ __forceinline__ void eig_swap_rows(RrluEigBlock& b, int a, int c) {
+  swapd(b.F, a, c);
+  swapd(b.U, a, c);
+  swapd(b.A, a, c);
+  swapi(b.PL, a, c);
+  swapi(b.PQ, a, c);
+}
+__device__ __forceinline__ void eig_swap_cols(RrluEigBlock& b, int a, int c) {
+  swapd(b.V, a, c);
+  swapi(b.PU, a, c);
+}
+
+// CauchyPivtEig (:571-717); the pivot magnitude is |U(k)V(k) / computfd(k, k)|.
+__device__ void pivt_eig(RrluEigBlock& b, int k0, ArgMax* sm) {
+  ArgMax L = eig_col_max(b, k0, sm);
+  ArgMax R = eig_row_max(b, k0, sm);
+  const double junkL = L.v * fabs(b.V[k0]);
+  const double junkU = R.v * fabs(b.U[k0]);
+  const double piv = fabs(b.U[k0] * b.V[k0] / eig_fd(b, b.PL[k0], b.PU[k0]));
+  if (junkL <= piv && junkU <= piv) return;
+  int flg = junkL > junkU ? 1 : 0;
+  int jjL = L.i, jjU = R.i;
+  for (int guard = 0; guard < 4 * (b.M + b.N); ++guard) {
+    if (flg == 1) {
+      if (threadIdx.x == 0) eig_swap_rows(b, k0, jjL + k0 - 1);
+      __syncthreads();
+      R = eig_row_max(b, k0, sm);
+      jjU = R.i;
+      if (jjU == 1) return;
+      flg = 0;
+    }
+    if (threadIdx.x == 0) eig_swap_cols(b, k0, jjU + k0 - 1);
+    __syncthreads();
+    L = eig_col_max(b, k0, sm);
+    jjL = L.i;
+    if (jjL == 1) return;
+    flg = 1;
+  }
+}
+
+__global__ void __launch_bounds__(RRLU_THREADS) k_rrlu_eig(RrluEigBlock* blocks, double tol, int* pending) {
+  __shared__ ArgMax sm[33];
+  __shared__ Cand smc[33];
+  RrluEigBlock& gb = blocks[blockIdx.x];
+  RrluEigBlock b = gb;
+  if (b.phase == 2) return;
+  const int M = b.M, N = b.N, mn = min(M, N);
+  const double rho = 1.2;  // rrluCauchyEigrow :49-50
+  const int prd = 5;
+  bool resume_cp = b.phase == 1;
+  if (b.phase == 0 && b.k_next == 1) {
+    for (int i = threadIdx.x; i < M; i += blockDim.x) {
+      b.F[i] = b.FF[b.r0 + i];
+      b.A[i] = b.gU[i];
+      b.U[i] = b.gU[i];
+      b.PL[i] = b.r0 + i + 1;
+      b.PQ[i] = i + 1;
+    }
+    for (int j = threadIdx.x; j < N; j += blockDim.x) {
+      b.V[j] = b.gV[j];
+      b.PU[j] = b.c0 + j + 1;
+    }
+    for (int j = threadIdx.x; j < mn; j += blockDim.x) b.W[j] = 0.0;
+    __syncthreads();
+  }
+  int Rk = mn;
+  double amax = b.amax;
+  for (int k = b.k_next; k <= mn; ++k) {
+    const int k0 = k - 1;
+    double ukk;
+    if (resume_cp) {
+      resume_cp = false;
+      if (threadIdx.x == 0) {  // CauchyPivtEig_CP's swaps (:1004-1134)
+        eig_swap_rows(b, k0, b.cp_i + k0 - 1);
+        eig_swap_cols(b, k0, b.cp_j + k0 - 1);
+      }
+      __syncthreads();
+      ukk = b.U[k0] * b.V[k0] / eig_fd(b, b.PL[k0], b.PU[k0]);
+      amax = fmax(amax, fabs(ukk));
+      if (fabs(ukk) < tol * amax) {
+        Rk = k - 1;
+        break;
+      }
+    } else {
+      pivt_eig(b, k0, sm);
+      ukk = b.U[k0] * b.V[k0] / eig_fd(b, b.PL[k0], b.PU[k0]);
+      amax = fmax(amax, fabs(ukk));
+      if (fabs(ukk) < tol * amax) {
+        if (threadIdx.x == 0) {
+          gb.phase = 1;
+          gb.k_next = k;
+          gb.amax = amax;
+          atomicAdd(pending, 1);
+        }
+        return;
+      }
+    }
+    const double fk = b.F[k0];
+    const int plk = b.PL[k0], puk = b.PU[k0];
+    for (int i = k + threadIdx.x; i < M; i += blockDim.x) b.U[i] = b.U[i] * ((b.F[i] - fk) / eig_fd(b, b.PL[i], puk));
+    for (int j = k + threadIdx.x; j < N; j += blockDim.x)
+      b.V[j] = b.V[j] * (eig_dd(b, b.PU[j], puk) / (-eig_fd(b, plk, b.PU[j])));
+    for (int j = threadIdx.x; j < k - 1; j += blockDim.x)
+      b.W[j] = b.W[j] * ((-eig_fd(b, b.PL[j], puk)) / (fk - b.F[j]));
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double wk = eig_fd(b, plk, puk) / b.A[k0];
+      for (int j = 0; j < k - 1; ++j) wk = wk * ((-eig_fd(b, plk, b.PU[j])) / (b.F[j] - fk));
+      b.W[k0] = wk;
+    }
+    __syncthreads();
+    // swap check every prd steps (searchMax2Eig, :1137-1203, and the update of :160-205)
+    int flgl = k % prd;
+    for (int guard = 0; flgl < 1 && guard < 4 * k + 64; ++guard) {
+      flgl = 1;
+      const Cand best = multi_cauchy_max(b.F + k, b.U + k, M - k, b.F, b.W, k, smc);
+      if (M - k > 0 && best.v > rho) {
+        flgl = 0;
+        const int i0 = best.j - 1, j0 = best.i + k - 1;
+        const double fii = b.F[i0], fjj = b.F[j0];
+        const int plii = b.PL[i0], pljj = b.PL[j0];
+        for (int j = k + threadIdx.x; j < N; j += blockDim.x)
+          b.V[j] = b.V[j] * ((-eig_fd(b, plii, b.PU[j])) / (-eig_fd(b, pljj, b.PU[j])));
+        for (int i = k + threadIdx.x; i < M; i += blockDim.x)
+          if (i != j0) b.U[i] = b.U[i] * ((b.F[i] - fjj) / (b.F[i] - fii));
+        for (int j = threadIdx.x; j < k; j += blockDim.x)
+          if (j != i0) b.W[j] = b.W[j] * ((b.F[j] - fii) / (b.F[j] - fjj));
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          double ujj = b.A[i0] * ((fii - fjj) / eig_fd(b, plii, b.PU[i0]));
+          double wii = eig_fd(b, pljj, b.PU[i0]) / b.A[j0];
+          for (int j = 0; j < k; ++j) {
+            if (j == i0) continue;
+            ujj = ujj * ((fii - b.F[j]) / eig_fd(b, plii, b.PU[j]));
+            wii = wii * ((-eig_fd(b, pljj, b.PU[j])) / (b.F[j] - fjj));
+          }
+          b.U[j0] = ujj;
+          b.W[i0] = wii;
+          swapi(b.PL, i0, j0);
+          swapi(b.PQ, i0, j0);
+          swapd(b.F, i0, j0);
+          swapd(b.A, i0, j0);
+        }
+        __syncthreads();
+      }
+    }
+  }
+  if (threadIdx.x == 0) {
+    *b.rank = Rk;
+    gb.phase = 2;
+  }
+}
+
+// Complete-pivot search for waiting eig blocks (CauchyPivtEig_CP's maximum), as k_cp_search.
+__global__ void __launch_bounds__(RRLU_THREADS) k_cp_search_eig(const RrluEigBlock* blocks, const CpChunk* chunks,
+                                                                 Cand* cand) {
+  __shared__ Cand smc[33];
+  const CpChunk ch = chunks[blockIdx.x];
+  const RrluEigBlock& b = blocks[ch.blk];
+  const int k0 = b.k_next - 1;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  Cand wb{-1.0, 0x7fffffff, 0};
+  for (int j = ch.c0 + warp; j < ch.c1; j += nw) {
+    const int pu = b.PU[j];
+    ArgMax a{-1.0, 0x7fffffff};
+    for (int i = k0 + lane; i < b.M; i += 32) a = better(a, ArgMax{fabs(b.U[i] / eig_fd(b, b.PL[i], pu)), i - k0 + 1});
+    for (int o = 16; o > 0; o >>= 1) {
+      ArgMax y;
+      y.v = __shfl_xor_sync(0xffffffffu, a.v, o);
+      y.i = __shfl_xor_sync(0xffffffffu, a.i, o);
+      a = better(a, y);
+    }
+    wb = better_c(wb, Cand{a.v * fabs(b.V[j]), j - k0 + 1, a.i});
+  }
+  if (lane == 0) smc[warp] = wb;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    Cand r = smc[0];
+    for (int w = 1; w < nw; ++w) r = better_c(r, smc[w]);
+    cand[blockIdx.x] = r;
+  }
 }
 
 // Columns of A(:, R) (n x M, lda) in RRLU pivot order for every compressed block:
@@ -828,8 +1060,10 @@ struct Bump {
 struct Plan {
   std::vector<OffBlock> blocks;
   std::vector<RrluBlock> lu;
+  std::vector<RrluEigBlock> lue;  // RRLU of accurate-denominator blocks
   std::vector<QrTile> qr;
   RrluBlock* d_lu = nullptr;
+  RrluEigBlock* d_lue = nullptr;
   QrTile* d_qr = nullptr;
   int* d_ranks = nullptr;        // RRLU ranks
   int* d_pending = nullptr;      // RRLU blocks waiting for a complete-pivot search
@@ -872,6 +1106,46 @@ GenSpec sub_gens(int kind, const double* gen, long ldgen, int n, int r0, int c0)
   return g;
 }
 
+// What the products need from the RRLU of block b: the poles and weights of
+// Z'(t, j) = Z(Rk+t) W(j) / (P(Rk+t) - P(j)) (plain Cauchy in the pivoted row poles), the
+// generators of Y = the rows PL(1:Rk) of the block with the unpermuted columns, and the
+// local row permutation for the gather.
+struct LuParts {
+  const double *pole, *z, *w;
+  GenSpec y;
+  const int* perm;
+};
+
+LuParts lu_parts(const Plan& P, int kind, int b, const psmma_batch_item* items) {
+  const OffBlock& ob = P.blocks[b];
+  const psmma_batch_item& it = items[ob.item];
+  LuParts lp;
+  if (kind == KIND_CAUCHY_EIG) {
+    const RrluEigBlock& r = P.lue[b];
+    lp.pole = r.F;
+    lp.z = r.U;
+    lp.w = r.W;
+    lp.y = sub_gens(kind, it.gen, it.ldgen, it.n, ob.r0, ob.c0);  // the columns C
+    lp.y.Dr = r.F;      // F(PL(i))
+    lp.y.Ur = r.A;      // LU
+    lp.y.rglob = r.PL;  // global rows, for the branch of the denominator
+    lp.y.cg0 = ob.c0;
+    lp.perm = r.PQ;
+  } else {
+    const RrluBlock& r = P.lu[b];
+    lp.pole = r.D;
+    lp.z = r.U;
+    lp.w = r.W;
+    lp.y.kind = KIND_CAUCHY;
+    lp.y.Dr = r.D;  // LD
+    lp.y.Ur = r.A;  // LU
+    lp.y.Fc = r.gF;
+    lp.y.Vc = r.gV;
+    lp.perm = r.PL;
+  }
+  return lp;
+}
+
 void make_plan(Plan& P, Bump& bump, const psmma_batch_item* items, int count, int compressor, int kind) {
   P.blocks.clear();
   for (int i = 0; i < count; ++i) {
@@ -882,7 +1156,48 @@ void make_plan(Plan& P, Bump& bump, const psmma_batch_item* items, int count, in
   }
   const int nb = (int)P.blocks.size();
   P.gather.assign(nb, nullptr);
-  if (compressor == PSMMA_COMPRESS_RRLU) {
+  if (compressor == PSMMA_COMPRESS_RRLU && kind == KIND_CAUCHY_EIG) {
+    P.lue.resize(nb);
+    for (int b = 0; b < nb; ++b) {
+      const OffBlock& ob = P.blocks[b];
+      const psmma_batch_item& it = items[ob.item];
+      RrluEigBlock& r = P.lue[b];
+      r.M = ob.M;
+      r.N = ob.N;
+      r.FF = it.gen;                       // [F|U|V|DIFL|DIFR]
+      r.DL = it.gen + 3 * (long)it.ldgen;
+      r.DR = it.gen + 4 * (long)it.ldgen;
+      r.nglob = it.n;
+      r.gU = it.gen + (long)it.ldgen + ob.r0;
+      r.gV = it.gen + 2 * (long)it.ldgen + ob.c0;
+      r.r0 = ob.r0;
+      r.c0 = ob.c0;
+      r.F = bump.take<double>(ob.M);
+      r.A = bump.take<double>(ob.M);
+      r.U = bump.take<double>(ob.M);
+      r.V = bump.take<double>(ob.N);
+      r.W = bump.take<double>(std::min(ob.M, ob.N));
+      r.PL = bump.take<int>(ob.M);
+      r.PU = bump.take<int>(ob.N);
+      r.PQ = bump.take<int>(ob.M);
+      r.k_next = 1;
+      r.phase = 0;
+      r.cp_i = r.cp_j = 0;
+      r.amax = 0.0;
+      P.gather[b] = bump.take<double>((size_t)it.n * ob.M);
+    }
+    P.d_lue = bump.take<RrluEigBlock>(std::max(1, nb));
+    P.d_ranks = bump.take<int>(std::max(1, nb));
+    P.chunk_cap = nb;
+    for (int b = 0; b < nb; ++b) P.chunk_cap += (P.blocks[b].N + Plan::CP_COLS - 1) / Plan::CP_COLS;
+    P.d_pending = bump.take<int>(1);
+    P.d_chunks = bump.take<CpChunk>(P.chunk_cap);
+    P.d_cand = bump.take<Cand>(P.chunk_cap);
+    P.d_cpblk = bump.take<int>(std::max(1, nb));
+    P.d_cpfirst = bump.take<int>(std::max(1, nb));
+    P.d_gather = bump.take<GatherDesc>(std::max(1, nb));
+    for (int b = 0; b < nb; ++b) P.lue[b].rank = P.d_ranks + b;
+  } else if (compressor == PSMMA_COMPRESS_RRLU) {
     P.lu.resize(nb);
     for (int b = 0; b < nb; ++b) {
       const OffBlock& ob = P.blocks[b];
@@ -993,24 +1308,18 @@ void build_rounds(const Plan& P, const psmma_batch_item* items, int count, int c
     if (Rk == 0) continue;
     double* T = P.gather[b];
     if (compressor == PSMMA_COMPRESS_RRLU) {
-      const RrluBlock& r = P.lu[b];
-      // T0 += Ar * Z',  Z'(t, j) = U(Rk+t) W(j) / (LD(Rk+t) - LD(j))  (T0, Ar gathered)
+      const LuParts lp = lu_parts(P, kind, b, items);
+      // T0 += Ar * Z',  Z'(t, j) = Z(Rk+t) W(j) / (P(Rk+t) - P(j))  (T0, Ar gathered)
       GenSpec gz;
       gz.kind = KIND_CAUCHY;
-      gz.Dr = r.D + Rk;
-      gz.Ur = r.U + Rk;
-      gz.Fc = r.D;
-      gz.Vc = r.W;
+      gz.Dr = lp.pole + Rk;
+      gz.Ur = lp.z + Rk;
+      gz.Fc = lp.pole;
+      gz.Vc = lp.w;
       if (ob.M - Rk > 0)
         R.r1.push_back(SplitProblem{n, Rk, ob.M - Rk, 1.0, 1.0, T + (size_t)n * Rk, n, gz, T, n});
-      // Q(:, C) += alpha * T0 * Y,  Y(j, c) = LU(j) V(c) / (LD(j) - F(c)) with the unpermuted F, V
-      GenSpec gy;
-      gy.kind = KIND_CAUCHY;
-      gy.Dr = r.D;
-      gy.Ur = r.A;
-      gy.Fc = r.gF;
-      gy.Vc = r.gV;
-      R.r2.push_back(SplitProblem{n, ob.N, Rk, alpha, 1.0, T, n, gy, Qblk, it.ldq});
+      // Q(:, C) += alpha * T0 * Y, Y = rows PL(1:Rk) of the block with the unpermuted columns
+      R.r2.push_back(SplitProblem{n, ob.N, Rk, alpha, 1.0, T, n, lp.y, Qblk, it.ldq});
       R.executed += 2.0 * n * (double)(ob.M - Rk) * Rk + 2.0 * n * (double)Rk * ob.N;
     } else {
       const QrTile& q = P.qr[b];
@@ -1056,13 +1365,13 @@ void build_rounds_split(const Plan& P, const psmma_batch_item* items, int count,
     if (Rk == 0) continue;
     double* T = P.gather[b];
     if (compressor == PSMMA_COMPRESS_RRLU) {
-      const RrluBlock& r = P.lu[b];
-      GenSpec gz;  // Z'(t, j) = U(Rk+t) W(j) / (LD(Rk+t) - LD(j)): T0 += Ar * Z'
+      const LuParts lp = lu_parts(P, kind, b, items);
+      GenSpec gz;  // Z'(t, j) = Z(Rk+t) W(j) / (P(Rk+t) - P(j)): T0 += Ar * Z'
       gz.kind = KIND_CAUCHY;
-      gz.Dr = r.D + Rk;
-      gz.Ur = r.U + Rk;
-      gz.Fc = r.D;
-      gz.Vc = r.W;
+      gz.Dr = lp.pole + Rk;
+      gz.Ur = lp.z + Rk;
+      gz.Fc = lp.pole;
+      gz.Vc = lp.w;
       if (ob.M - Rk > 0) {
         R.r1.push_back(SplitProblem{n, Rk, ob.M - Rk, 1.0, 1.0, T + (size_t)n * Rk, n, gz, T, n});
         R.executed += 2.0 * n * (double)(ob.M - Rk) * Rk;
@@ -1102,8 +1411,11 @@ void build_rounds_split(const Plan& P, const psmma_batch_item* items, int count,
         q.ka = dn;
         q.gs.k1 = dn;
         if (compressor == PSMMA_COMPRESS_RRLU) {
-          q.gs.Dr2 = P.lu[b].D;  // LD(1:Rk)
-          q.gs.Ur2 = P.lu[b].A;  // LU(1:Rk)
+          const LuParts lp = lu_parts(P, kind, b, items);
+          q.gs.Dr2 = lp.y.Dr;        // pivoted row poles (1:Rk)
+          q.gs.Ur2 = lp.y.Ur;        // LU(1:Rk)
+          q.gs.rglob2 = lp.y.rglob;  // CauchyEig: global rows of the tail
+          q.gs.cg0 = d0;
         } else {
           q.gs.B = P.qr[b].F;  // R P^T (Rk x N, ld Rk)
           q.gs.ldb = Rk;
@@ -1365,6 +1677,65 @@ void tune_store(unsigned long long sig, const SplitTune& t) {
   }
 }
 
+// The resumable RRLU of all blocks: launch, then while blocks wait for a complete-pivot
+// search run it grid-wide and resume them.  Every resume advances some block by a step, so
+// the loop is bounded by the largest min(M, N).
+template <class Block>
+int run_rrlu(Plan& P, std::vector<Block>& hb, Block* d_blocks, void (*krrlu)(Block*, double, int*),
+             void (*ksearch)(const Block*, const CpChunk*, Cand*), double tol, std::vector<int>& ranks,
+             cudaStream_t st) {
+  const int nb = (int)hb.size();
+  if (cudaMemcpyAsync(d_blocks, hb.data(), sizeof(Block) * nb, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+      cudaMemsetAsync(P.d_pending, 0, sizeof(int), st) != cudaSuccess)
+    return PSMMA_EDEVICE;
+  krrlu<<<nb, RRLU_THREADS, 0, st>>>(d_blocks, tol, P.d_pending);
+  if (cudaGetLastError() != cudaSuccess) return PSMMA_EDEVICE;
+  int max_iter = 2;
+  for (const OffBlock& ob : P.blocks) max_iter = std::max(max_iter, std::min(ob.M, ob.N) + 2);
+  std::vector<Block> cur(nb);
+  std::vector<CpChunk> chunks;
+  std::vector<int> cpblk, cpfirst;
+  int iter = 0;
+  for (; iter < max_iter; ++iter) {
+    int pend = 0;
+    if (cudaMemcpyAsync(&pend, P.d_pending, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaMemcpyAsync(cur.data(), d_blocks, sizeof(Block) * nb, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      return PSMMA_EDEVICE;
+    if (pend == 0) break;
+    chunks.clear();
+    cpblk.clear();
+    cpfirst.clear();
+    for (int b = 0; b < nb; ++b) {
+      if (cur[b].phase != 1) continue;
+      cpblk.push_back(b);
+      cpfirst.push_back((int)chunks.size());
+      for (int c = cur[b].k_next - 1; c < cur[b].N; c += Plan::CP_COLS)
+        chunks.push_back(CpChunk{b, c, std::min(cur[b].N, c + Plan::CP_COLS)});
+    }
+    if (chunks.empty() || (int)chunks.size() > P.chunk_cap) return PSMMA_EDEVICE;
+    if (cudaMemcpyAsync(P.d_chunks, chunks.data(), sizeof(CpChunk) * chunks.size(), cudaMemcpyHostToDevice, st) !=
+            cudaSuccess ||
+        cudaMemcpyAsync(P.d_cpblk, cpblk.data(), sizeof(int) * cpblk.size(), cudaMemcpyHostToDevice, st) !=
+            cudaSuccess ||
+        cudaMemcpyAsync(P.d_cpfirst, cpfirst.data(), sizeof(int) * cpfirst.size(), cudaMemcpyHostToDevice, st) !=
+            cudaSuccess ||
+        cudaMemsetAsync(P.d_pending, 0, sizeof(int), st) != cudaSuccess)
+      return PSMMA_EDEVICE;
+    ksearch<<<(unsigned)chunks.size(), RRLU_THREADS, 0, st>>>(d_blocks, P.d_chunks, P.d_cand);
+    k_cp_reduce<Block><<<((int)cpblk.size() + 127) / 128, 128, 0, st>>>(d_blocks, P.d_cpblk, P.d_cpfirst,
+                                                                        (int)cpblk.size(), (int)chunks.size(),
+                                                                        P.d_cand);
+    krrlu<<<nb, RRLU_THREADS, 0, st>>>(d_blocks, tol, P.d_pending);
+    if (cudaGetLastError() != cudaSuccess) return PSMMA_EDEVICE;
+  }
+  if (iter == max_iter) return PSMMA_EDEVICE;
+  if (cudaMemcpyAsync(ranks.data(), P.d_ranks, sizeof(int) * nb, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return PSMMA_EDEVICE;
+  return PSMMA_OK;
+}
+
 }  // namespace
 
 static size_t batch_workspace(int kind, int count, const psmma_batch_item* items, int compressor,
@@ -1372,7 +1743,6 @@ static size_t batch_workspace(int kind, int count, const psmma_batch_item* items
   const int precision = opts ? opts->precision : PSMMA_PREC_FP64;
   const int n_moduli = opts ? opts->n_moduli : 0;
   if (count <= 0 || !items || check_batch(count, items, precision, n_moduli, compressor, 0.5)) return 0;
-  if (kind == KIND_CAUCHY_EIG && compressor != PSMMA_COMPRESS_RRQR) return 0;
   Plan P;
   const size_t a = part_a_bytes(P, items, count, compressor, kind);
   return a + rounds_bound(P, items, count, compressor, kind, precision, n_moduli) + 4096;
@@ -1394,8 +1764,6 @@ static int batch_run(int kind, int count, const psmma_batch_item* items, double 
   const int n_moduli = opts ? opts->n_moduli : 0;
   int rc = check_batch(count, items, precision, n_moduli, compressor, tol);
   if (rc) return rc;
-  // the structured RRLU of accurate-denominator blocks (rrluCauchyEigrow) is not built
-  if (kind == KIND_CAUCHY_EIG && compressor != PSMMA_COMPRESS_RRQR) return PSMMA_EUNSUPPORTED;
   if (stats) *stats = psmma_batch_stats{0.0, 0.0, 0.0, 0, 0, 0, 0};
   if (count == 0) return PSMMA_OK;
   cudaStream_t st = (cudaStream_t)stream;
@@ -1426,54 +1794,9 @@ static int batch_run(int kind, int count, const psmma_batch_item* items, double 
   std::vector<int> ranks(nb, 0);
   double compress_flops = 0.0;
   if (nb && compressor == PSMMA_COMPRESS_RRLU) {
-    if (cudaMemcpyAsync(P.d_lu, P.lu.data(), sizeof(RrluBlock) * nb, cudaMemcpyHostToDevice, st) != cudaSuccess)
-      return PSMMA_EDEVICE;
-    if (cudaMemsetAsync(P.d_pending, 0, sizeof(int), st) != cudaSuccess) return PSMMA_EDEVICE;
-    k_rrlu_cauchy<<<nb, RRLU_THREADS, 0, st>>>(P.d_lu, tol, P.d_pending);
-    if (cudaGetLastError() != cudaSuccess) return PSMMA_EDEVICE;
-    // every resume advances some block by at least one step, so the loop is bounded
-    int max_iter = 2;
-    for (const OffBlock& ob : P.blocks) max_iter = std::max(max_iter, std::min(ob.M, ob.N) + 2);
-    std::vector<RrluBlock> cur(nb);
-    std::vector<CpChunk> chunks;
-    std::vector<int> cpblk, cpfirst;
-    int iter = 0;
-    for (; iter < max_iter; ++iter) {
-      int pend = 0;
-      if (cudaMemcpyAsync(&pend, P.d_pending, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-          cudaMemcpyAsync(cur.data(), P.d_lu, sizeof(RrluBlock) * nb, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-          cudaStreamSynchronize(st) != cudaSuccess)
-        return PSMMA_EDEVICE;
-      if (pend == 0) break;
-      chunks.clear();
-      cpblk.clear();
-      cpfirst.clear();
-      for (int b = 0; b < nb; ++b) {
-        if (cur[b].phase != 1) continue;
-        cpblk.push_back(b);
-        cpfirst.push_back((int)chunks.size());
-        for (int c = cur[b].k_next - 1; c < cur[b].N; c += Plan::CP_COLS)
-          chunks.push_back(CpChunk{b, c, std::min(cur[b].N, c + Plan::CP_COLS)});
-      }
-      if (chunks.empty() || (int)chunks.size() > P.chunk_cap) return PSMMA_EDEVICE;
-      if (cudaMemcpyAsync(P.d_chunks, chunks.data(), sizeof(CpChunk) * chunks.size(), cudaMemcpyHostToDevice,
-                          st) != cudaSuccess ||
-          cudaMemcpyAsync(P.d_cpblk, cpblk.data(), sizeof(int) * cpblk.size(), cudaMemcpyHostToDevice, st) !=
-              cudaSuccess ||
-          cudaMemcpyAsync(P.d_cpfirst, cpfirst.data(), sizeof(int) * cpfirst.size(), cudaMemcpyHostToDevice, st) !=
-              cudaSuccess ||
-          cudaMemsetAsync(P.d_pending, 0, sizeof(int), st) != cudaSuccess)
-        return PSMMA_EDEVICE;
-      k_cp_search<<<(unsigned)chunks.size(), RRLU_THREADS, 0, st>>>(P.d_lu, P.d_chunks, P.d_cand);
-      k_cp_reduce<<<((int)cpblk.size() + 127) / 128, 128, 0, st>>>(P.d_lu, P.d_cpblk, P.d_cpfirst, (int)cpblk.size(),
-                                                                   (int)chunks.size(), P.d_cand);
-      k_rrlu_cauchy<<<nb, RRLU_THREADS, 0, st>>>(P.d_lu, tol, P.d_pending);
-      if (cudaGetLastError() != cudaSuccess) return PSMMA_EDEVICE;
-    }
-    if (iter == max_iter) return PSMMA_EDEVICE;
-    if (cudaMemcpyAsync(ranks.data(), P.d_ranks, sizeof(int) * nb, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-        cudaStreamSynchronize(st) != cudaSuccess)
-      return PSMMA_EDEVICE;
+    rc = (kind == KIND_CAUCHY_EIG) ? run_rrlu(P, P.lue, P.d_lue, k_rrlu_eig, k_cp_search_eig, tol, ranks, st)
+                                   : run_rrlu(P, P.lu, P.d_lu, k_rrlu_cauchy, k_cp_search, tol, ranks, st);
+    if (rc) return rc;
     for (int b = 0; b < nb; ++b) compress_flops += 12.0 * (ranks[b] + 1) * (P.blocks[b].M + P.blocks[b].N);
   } else if (nb) {
     if (cudaMemcpyAsync(P.d_qr, P.qr.data(), sizeof(QrTile) * nb, cudaMemcpyHostToDevice, st) != cudaSuccess)
@@ -1534,7 +1857,7 @@ static int batch_run(int kind, int count, const psmma_batch_item* items, double 
       g.M = ob.M;
       g.Rk = ranks[b];
       g.c0 = gather_cols;
-      g.PL = P.lu[b].PL;
+      g.PL = lu_parts(P, kind, b, items).perm;
       g.T0 = P.gather[b];
       g.Ar = P.gather[b] + (size_t)it.n * ranks[b];
       gd.push_back(g);

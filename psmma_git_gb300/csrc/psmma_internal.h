@@ -38,6 +38,11 @@ struct GenSpec {
   const double *Dr2 = nullptr, *Ur2 = nullptr;
   const double *Fc1 = nullptr, *dl = nullptr, *dr = nullptr;
   int fc1_len = 0, diag_off = 0;
+  // CauchyEig rows in a permuted order (the RRLU's Y factor): rglob[i] is the 1-based global
+  // index of row i and cg0 the 0-based global index of column 0, so the branch is taken by
+  // rglob[i] - 1 <= cg0 + j; rglob2 likewise for Cauchy tail rows (Dr2, Ur2).
+  const int *rglob = nullptr, *rglob2 = nullptr;
+  int cg0 = 0;
 };
 
 #ifdef __CUDACC__

@@ -243,10 +243,15 @@ __device__ __forceinline__ void h_pass1_blk(const GenSpec& gs, int K, int kp, do
         }
       } else if (KIND == KIND_CAUCHY_EIG) {
         if (gs.k1 > 0 && kk >= gs.k1) {
-          h = __ldg(gs.B + (kk - gs.k1) + (long)j * gs.ldb);  // dense tail rows (merged products)
+          // tail rows of merged products: dense, or CauchyEig rows in permuted order
+          const int t = kk - gs.k1;
+          h = gs.B ? __ldg(gs.B + t + (long)j * gs.ldb)
+                   : div_nr(__ldg(gs.Ur2 + t) * v,
+                            eig_den(__ldg(gs.Dr2 + t), w, w1, dlj, drj, __ldg(gs.rglob2 + t) - 1 <= gs.cg0 + j));
         } else {
           const double fi = __ldg(gs.Dr + kk), u = __ldg(gs.Ur + kk);
-          h = div_nr(u * v, eig_den(fi, w, w1, dlj, drj, kk - j <= gs.diag_off));
+          const bool upper = gs.rglob ? (__ldg(gs.rglob + kk) - 1 <= gs.cg0 + j) : (kk - j <= gs.diag_off);
+          h = div_nr(u * v, eig_den(fi, w, w1, dlj, drj, upper));
         }
       } else if (KIND == KIND_TOEPLITZ) {
         h = __ldg(gs.g + (gs.order - 1) + j - kk);

@@ -112,9 +112,26 @@ def test_cauchyeig_host_and_fortran_abi():
     assert O.rel_fro(Qf, ref) < 1e-13
 
 
+def test_oracle_eig_rrlu_factorises_the_tile():
+    # rrluCauchyEigrow restated: X Y reproduces the off-diagonal tile at the truncation level and
+    # the rank matches the pivoted QR's
+    for n in [64, 300, 1031]:
+        F, U, V, dl, dr = O.eig_generators(n, seed=n, tiny=n // 100)
+        H = O.cauchy_like_eig(F, U, V, dl, dr)
+        h = n // 2
+        for (r0, r1, c0, c1) in [(0, h, h, n), (h, n, 0, h)]:
+            X, Y, rk = O.compress_cauchy_eig(F, U, V, dl, dr, np.arange(r0 + 1, r1 + 1),
+                                             np.arange(c0 + 1, c1 + 1), 1e-14)
+            T = H[r0:r1, c0:c1]
+            assert X is not None
+            assert np.linalg.norm(X @ Y - T) / np.linalg.norm(T) < 1e-13
+            assert abs(rk - O.compress_rrqr(T, 1e-14)[2]) <= 1
+
+
 @pytest.mark.gpu
+@pytest.mark.parametrize("comp", ["rrqr", "rrlu"])
 @pytest.mark.parametrize("prec,tol", [("fp64", 1e-13), ("split", 1e-12)])
-def test_cauchyeig_merge_level_rrqr(prec, tol):
+def test_cauchyeig_merge_level(prec, tol, comp):
     import torch
     import psmma_git_gb300 as P
     sizes = [1, 2, 37, 300, 1031]
@@ -130,11 +147,11 @@ def test_cauchyeig_merge_level_rrqr(prec, tol):
         dQ = P.fortran_empty(n, n)
         dQ.copy_(torch.from_numpy(Q0))
         dev.append((dA, g, dQ))
-    ranks, info = P.cauchy_batch_lowrank(dev, 0.5, -1.0, compressor="rrqr", tol=1e-14, precision=prec, eig=True)
+    ranks, info = P.cauchy_batch_lowrank(dev, 0.5, -1.0, compressor=comp, tol=1e-14, precision=prec, eig=True)
     torch.cuda.synchronize()
     k = 0
     for (A, gens, Q0), (_, _, dQ) in zip(probs, dev):
-        Qo, ro = O.merge_level_eig_product(A, *gens, Q0, 0.5, -1.0, 1e-14)
+        Qo, ro = O.merge_level_eig_product(A, *gens, Q0, 0.5, -1.0, 1e-14, comp)
         exact = 0.5 * A @ O.cauchy_like_eig(*gens) - Q0
         got = dQ.cpu().numpy()
         for a, b in zip(ranks[k:k + len(ro)], ro):
@@ -145,11 +162,13 @@ def test_cauchyeig_merge_level_rrqr(prec, tol):
     assert info["n_blocks"] == k
 
 
-def test_cauchyeig_batch_rejects_rrlu(lib):
+def test_cauchyeig_batch_argument_checks(lib):
     items = (_lib.PsmmaBatchItem * 1)()
     buf = np.zeros(64)
     p = buf.ctypes.data
-    items[0].n, items[0].A, items[0].lda, items[0].gen, items[0].ldgen = 4, p, 4, p, 4
+    items[0].n, items[0].A, items[0].lda, items[0].gen, items[0].ldgen = 4, p, 4, p, 3
     items[0].Q, items[0].ldq = p, 4
     assert lib.psmma_cauchyeig_batch_lowrank(1, items, 1.0, 0.0, _lib.COMPRESS_RRLU, 1e-14, None, None, None,
-                                             None) == _lib.PSMMA_EUNSUPPORTED
+                                             None) == _lib.PSMMA_EGEN
+    assert lib.psmma_cauchyeig_batch_lowrank(0, items, 1.0, 0.0, _lib.COMPRESS_RRLU, 1e-14, None, None, None,
+                                             None) == 0
