@@ -284,14 +284,14 @@ int psmma_last_status(void);
  * device: A/B, generators and Q/C are device pointers owned by the caller, who must keep
  * them alive (and not touch Q/C) until the request completes. */
 typedef struct psmma_request {
-  int kind;            /* PSMMA_KIND_CAUCHY / _TOEPLITZ / _HANKEL / _DFT                         */
+  int kind;            /* PSMMA_KIND_CAUCHY / _TOEPLITZ / _HANKEL / _DFT / _CAUCHY_EIG           */
   int precision;       /* PSMMA_PREC_FP64 or PSMMA_PREC_SPLIT                                     */
   int n_moduli;        /* split path: 0 = default                                                 */
   int n, k;            /* sizes as in the matching entry point                                    */
   double alpha, beta;
   const void* A;       /* A (double) or, for the DFT, B (psmma_complex)                           */
   int lda;
-  const double* gen;   /* generators (unused for the DFT)                                         */
+  const double* gen;   /* generators (unused for the DFT; CAUCHY_EIG: ldgen x 5 [F|U|V|DIFL|DIFR]) */
   int ldgen;
   void* Q;             /* Q (double) or, for the DFT, C (psmma_complex)                           */
   int ldq;

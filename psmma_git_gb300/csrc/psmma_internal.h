@@ -71,6 +71,23 @@ inline GenSpec reference_gens(int kind, const double* gen, long ldgen, int k) {
   return g;
 }
 
+// The generators of PSMMA_CAUCHYEIG's k x k matrix from a packed (ldgen x 5) array
+// [F|U|V|DIFL|DIFR] (the layout of the batch and serving calls).
+inline GenSpec eig_gens_packed(const double* gen, long ldgen, int k) {
+  GenSpec g;
+  g.kind = KIND_CAUCHY_EIG;
+  g.Dr = gen;
+  g.Fc = gen;
+  g.Fc1 = gen + 1;
+  g.Ur = gen + ldgen;
+  g.Vc = gen + 2 * ldgen;
+  g.dl = gen + 3 * ldgen;
+  g.dr = gen + 4 * ldgen;
+  g.fc1_len = k - 1;
+  g.diag_off = 0;
+  return g;
+}
+
 // FP64 plain path (fp64_structured.cu).  Real GEMM C(MxN) = alpha*X*G + beta*C where one
 // operand is streamed (X, column-major, ldx) and the other generated.
 int launch_struct_f64(int M, int N, int K, double alpha, const double* X, long ldx, const GenSpec& gs,

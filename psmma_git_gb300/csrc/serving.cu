@@ -121,6 +121,8 @@ size_t request_workspace(const psmma_request& r) {
   memset(&o, 0, sizeof(o));
   o.precision = r.precision;
   o.n_moduli = r.n_moduli;
+  if (r.kind == KIND_CAUCHY_EIG)
+    return r.precision == PSMMA_PREC_SPLIT ? split_workspace_general(r.n, r.k, r.k, r.n_moduli) : 0;
   if (r.precision == PSMMA_PREC_SPLIT) return split_workspace_bytes(r.kind, r.n, r.k, r.n_moduli);
   if (r.kind == KIND_DFT) return (size_t)r.n * sizeof(double2);
   return 0;
@@ -128,18 +130,18 @@ size_t request_workspace(const psmma_request& r) {
 
 // Validates a request (the same rules as the direct entry points).
 int check_request(const psmma_request& r) {
-  if (r.kind < KIND_CAUCHY || r.kind > KIND_DFT) return PSMMA_EUNSUPPORTED;
+  if ((r.kind < KIND_CAUCHY || r.kind > KIND_DFT) && r.kind != KIND_CAUCHY_EIG) return PSMMA_EUNSUPPORTED;
   if (r.precision != PSMMA_PREC_FP64 && r.precision != PSMMA_PREC_SPLIT) return PSMMA_EUNSUPPORTED;
   if (r.n_moduli != 0 && (r.n_moduli < 8 || r.n_moduli > 16)) return PSMMA_EUNSUPPORTED;
-  const bool dft = r.kind == KIND_DFT;
-  if (r.n < 0) return dft ? -1 : -2;
-  if (r.k < 0) return dft ? -2 : -3;
-  if (r.lda < std::max(1, r.n)) return dft ? -7 : -9;
-  if (r.ldq < std::max(1, r.n)) return dft ? -10 : -14;
+  const bool dft = r.kind == KIND_DFT, eig = r.kind == KIND_CAUCHY_EIG;  // INFO numbers of PZMDFTL,
+  if (r.n < 0) return dft || eig ? -1 : -2;                                   // PSCAUCHYEIG_COMPUTE
+  if (r.k < 0) return dft || eig ? -2 : -3;
+  if (r.lda < std::max(1, r.n)) return dft || eig ? -7 : -9;
+  if (r.ldq < std::max(1, r.n)) return dft ? -10 : eig ? -17 : -14;
   if (r.n > 0 && r.k > 0) {
     if (!r.Q || !r.A) return PSMMA_ENULL;
     if (!dft) {
-      long need = (r.kind == KIND_CAUCHY) ? (long)r.k : 2L * r.k - 1;
+      long need = (r.kind == KIND_CAUCHY || eig) ? (long)r.k : 2L * r.k - 1;
       if (!r.gen || r.ldgen < need) return PSMMA_EGEN;
     }
   }
@@ -154,6 +156,13 @@ int launch_job(psmma_server* s, Job& j) {
   unsigned* status = s->dev_status + j.slot;
   if (cudaMemsetAsync(status, 0, sizeof(unsigned), st) != cudaSuccess) return PSMMA_EDEVICE;
   if (r.n == 0 || r.k == 0) return PSMMA_OK;
+  if (r.kind == KIND_CAUCHY_EIG) {
+    const GenSpec gs = eig_gens_packed(r.gen, r.ldgen, r.k);
+    if (r.precision == PSMMA_PREC_SPLIT && r.alpha != 0.0)
+      return launch_split_general(r.n, r.k, r.k, r.alpha, (const double*)r.A, r.lda, gs, r.beta, (double*)r.Q,
+                                  r.ldq, r.n_moduli, work, j.work_bytes, st, status);
+    return launch_struct_f64(r.n, r.k, r.k, r.alpha, (const double*)r.A, r.lda, gs, r.beta, (double*)r.Q, r.ldq, st);
+  }
   if (r.precision == PSMMA_PREC_SPLIT && r.alpha != 0.0)
     return launch_split_any(r.kind, r.n, r.k, r.alpha, (const double*)r.A, r.lda, r.gen, r.ldgen, r.beta,
                             (double*)r.Q, r.ldq, r.n_moduli, work, j.work_bytes, st, status);

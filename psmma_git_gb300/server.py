@@ -5,16 +5,18 @@
         info = srv.wait(t)          # {'status', 'latency_s', 'queue_s', 'gpu_ms', ...}
 
 Operands are column-major CUDA tensors (see fortran_empty); they must stay alive and Q must
-not be touched until the request completes.  Kinds: cauchy, toeplitz, hankel, dft.
+not be touched until the request completes.  Kinds: cauchy, toeplitz, hankel, dft,
+cauchyeig (PSMMA_CAUCHYEIG's matrix; gen is n x 5 [F|U|V|DIFL|DIFR]).
 """
 from __future__ import annotations
 
 import ctypes as C
 
-from ._lib import (KIND_CAUCHY, KIND_DFT, KIND_HANKEL, KIND_TOEPLITZ, PREC_FP64, PREC_SPLIT, PsmmaCompletion,
-                   PsmmaError, PsmmaRequest, load)
+from ._lib import (KIND_CAUCHY, KIND_CAUCHY_EIG, KIND_DFT, KIND_HANKEL, KIND_TOEPLITZ, PREC_FP64, PREC_SPLIT,
+                   PsmmaCompletion, PsmmaError, PsmmaRequest, load)
 
-KINDS = {"cauchy": KIND_CAUCHY, "toeplitz": KIND_TOEPLITZ, "hankel": KIND_HANKEL, "dft": KIND_DFT}
+KINDS = {"cauchy": KIND_CAUCHY, "toeplitz": KIND_TOEPLITZ, "hankel": KIND_HANKEL, "dft": KIND_DFT,
+         "cauchyeig": KIND_CAUCHY_EIG}  # cauchyeig: gen is n x 5 [F|U|V|DIFL|DIFR]
 PRECS = {"fp64": PREC_FP64, "split": PREC_SPLIT}
 
 

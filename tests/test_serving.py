@@ -106,3 +106,22 @@ def test_server_results_match_oracle(cuda):
     gn = g.t().contiguous().cpu().numpy().T
     got = Q.t().contiguous().cpu().numpy().T
     assert O.rel_fro(got, O.dense_product("cauchy", 1.0, An, gn, 0.0, None, n)) < 1e-12
+
+
+def test_server_cauchyeig_requests_match_oracle(cuda):
+    import numpy as np
+    import torch
+    import psmma_git_gb300 as P
+    from psmma_git_gb300.server import Server
+    n = 257
+    F, U, V, dl, dr = O.eig_generators(n, seed=8, tiny=3)
+    gen = torch.from_numpy(np.ascontiguousarray(np.stack([F, U, V, dl, dr]))).cuda().t()  # n x 5
+    A = O.cfg_matrix(n, n, seed=9)
+    dA = P.fortran_empty(n, n)
+    dA.copy_(torch.from_numpy(A))
+    ref = A @ O.cauchy_like_eig(F, U, V, dl, dr)
+    with Server(1 << 30, max_inflight=2) as srv:
+        for prec, tol in [("fp64", 1e-13), ("split", 1e-12)]:
+            Q = P.fortran_empty(n, n)
+            assert srv.wait(srv.submit("cauchyeig", n, n, 1.0, dA, gen, 0.0, Q, precision=prec))["status"] == 0
+            assert O.rel_fro(Q.cpu().numpy(), ref) < tol, prec
