@@ -950,8 +950,14 @@ __device__ __forceinline__ void crt_combine_blk(const int8_t* __restrict__ R, in
         for (int t = 0; t < 4; ++t) acc[c][t] = 0;
       }
       const uint32_t* src = (const uint32_t*)(R + (size_t)i * kr + jb);
-      for (int l = 0; l < cc.nmod; ++l) {
-        const uint32_t w4 = __ldg(src + (size_t)l * plane_w);
+      // all residue words first (the loads are then in flight together), then the sums
+      uint32_t wl[SPL_MAX_MODULI];
+#pragma unroll
+      for (int l = 0; l < SPL_MAX_MODULI; ++l) wl[l] = (l < cc.nmod) ? __ldg(src + (size_t)l * plane_w) : 0u;
+#pragma unroll
+      for (int l = 0; l < SPL_MAX_MODULI; ++l) {
+        if (l >= cc.nmod) break;
+        const uint32_t w4 = wl[l];
         const int ff = cc.ffix[l];
         const unsigned c0 = cc.climb[l][0], c1 = cc.climb[l][1], c2 = cc.climb[l][2], c3 = cc.climb[l][3];
 #pragma unroll
@@ -1029,7 +1035,7 @@ __device__ __forceinline__ void crt_combine_blk(const int8_t* __restrict__ R, in
 }
 
 template <bool DFT_OUT>
-__global__ void __launch_bounds__(256) k_crt_combine(const int8_t* __restrict__ R, int n, int k, int kr,
+__global__ void __launch_bounds__(256, 3) k_crt_combine(const int8_t* __restrict__ R, int n, int k, int kr,
                                                      CrtConsts cc, const unsigned long long* __restrict__ amax_bits,
                                                      const unsigned long long* __restrict__ hmax_bits,
                                                      const SplitDevParams* prm, double alpha, double beta,
@@ -1321,7 +1327,7 @@ __global__ void __launch_bounds__(128) k_g_residues_H(const GProb* d, int count,
   residues_H_blk(e.Ht, e.N, e.kp, e.hmax, e.prm, cc, e.RH, local % gx, local / gx);
 }
 
-__global__ void __launch_bounds__(256) k_g_crt_combine(const GProb* d, int count, CrtConsts cc) {
+__global__ void __launch_bounds__(256, 3) k_g_crt_combine(const GProb* d, int count, CrtConsts cc) {
   const GProb& e = d[gfind<4>(d, count, blockIdx.x)];
   const int local = blockIdx.x - e.b_crt, gx = (e.N + CRT_TJ - 1) / CRT_TJ;
   crt_combine_blk<false>(e.R, e.M, e.N, e.kr, cc, e.amax, e.hmax, e.prm, e.alpha, e.beta, e.Q, e.ldq, local % gx,
