@@ -111,10 +111,11 @@ __device__ __forceinline__ bool mbar_wait_drain(uint64_t* bar, uint32_t parity, 
 
 // ---- division ------------------------------------------------------------------------------
 // a / x by Newton-Raphson refinement of the hardware reciprocal approximation and one
-// residual correction (Markstein's method, IBM J. Res. Dev. 34(1), 1990): y ~ 1/x to a few
-// ulp after two steps y <- y + y (1 - x y); then q = a y, q' = q + y (a - x q), which is the
-// correctly rounded quotient except in rare ties (at most 1 ulp off; checked against the
-// IEEE division by psmma_selftest_division).  Operands whose exponents are extreme
+// residual correction (Markstein's method, IBM J. Res. Dev. 34(1), 1990): one step
+// y <- y + y (1 - x y) squares the approximation's relative error; then q = a y and
+// q' = q + y (a - x q), whose error is about that squared error times |q| -- the correctly
+// rounded quotient except in rare ties (at most 1 ulp off; checked against the IEEE division
+// by psmma_selftest_division).  Operands whose exponents are extreme
 // (subnormal, huge, quotient near overflow or underflow, zero, Inf, NaN) take the IEEE
 // division.  Cheaper than the IEEE division on GB300, whose FP64 pipe is narrow.
 __device__ __forceinline__ double div_nr(double a, double x) {
@@ -122,9 +123,7 @@ __device__ __forceinline__ double div_nr(double a, double x) {
   if (ea < 64 || ea > 1983 || ex < 64 || ex > 1983 || ea - ex > 900 || ex - ea > 900) return a / x;
   double y;
   asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
-  double e = fma(-x, y, 1.0);
-  y = fma(y, e, y);
-  e = fma(-x, y, 1.0);
+  const double e = fma(-x, y, 1.0);
   y = fma(y, e, y);
   const double q = a * y;
   const double r = fma(-x, q, a);
