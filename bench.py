@@ -543,6 +543,96 @@ def run_cfg1(args, ws, rank, local):
     return 0
 
 
+def run_redist(args, ws, rank, local):
+    """The REDIST copy (PDGEMR2D) of an n x n matrix from the reference tests' layout (2 x 2
+    grid, 64 x 64 blocks, Test/psmma_testcauchy.f90:80) to row panels over the 4 ranks, with the
+    4 ranks' local arrays on one GPU: the pack kernel of every rank, then the unpack kernel of
+    every rank (the all-to-all between them is the caller's and is not timed here; its
+    receive buffers are assembled once before timing).  Algorithmic bytes: 16 per element
+    (8 read + 8 written) per kernel.  One JSON line."""
+    import torch
+    from psmma_git_gb300.redist import Grid, RedistPlan, descinit
+    if rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    n = args.redist_n
+    ga, gb = Grid(2, 2, "R"), Grid(4, 1, "R")
+    plans, A, sends, recvs, B = [], [], [], [], []
+    g = torch.Generator(device=dev)
+    g.manual_seed(3)
+    for r in range(4):
+        da = descinit(n, n, 64, 64, 0, 0, ga, r)
+        db = descinit(n, n, -(-n // 4), n, 0, 0, gb, r)
+        p = RedistPlan(n, n, da, ga, db, gb, r)
+        plans.append(p)
+        a = torch.empty((p.a_shape[1], da[8]), dtype=torch.float64, device=dev).t()
+        a.copy_(torch.rand(a.shape, generator=g, device=dev, dtype=torch.float64))
+        A.append(a)
+        sends.append(torch.empty(sum(p.send_counts), dtype=torch.float64, device=dev))
+        B.append(torch.empty((p.b_shape[1], db[8]), dtype=torch.float64, device=dev).t())
+    for r in range(4):
+        plans[r].pack(A[r], sends[r])
+    for r in range(4):  # the exchange, once: rank r's segments from every sender
+        parts = []
+        for s in range(4):
+            d = sum(plans[s].send_counts[:r])
+            parts.append(sends[s][d:d + plans[s].send_counts[r]])
+        recvs.append(torch.cat(parts))
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        for r in range(4):
+            plans[r].pack(A[r], sends[r], stream)
+        for r in range(4):
+            plans[r].unpack(recvs[r], B[r], stream)
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    t_pack = t_unpack = 0.0
+    for _ in range(args.steps):
+        ev[0].record(stream)
+        for r in range(4):
+            plans[r].pack(A[r], sends[r], stream)
+        ev[1].record(stream)
+        for r in range(4):
+            plans[r].unpack(recvs[r], B[r], stream)
+        ev[2].record(stream)
+        torch.cuda.synchronize()
+        t_pack += ev[0].elapsed_time(ev[1])
+        t_unpack += ev[1].elapsed_time(ev[2])
+    t_pack /= args.steps
+    t_unpack /= args.steps
+    # the round trip must reproduce A: gather the row panels back and compare with a
+    # direct construction of the 2x2 layout from the panels' global rows
+    rows = [torch.arange(n, device=dev)[torch.arange(n, device=dev) // (-(-n // 4)) == r] for r in range(4)]
+    Gm = torch.empty((n, n), dtype=torch.float64, device=dev)
+    for r in range(4):
+        Gm[rows[r]] = B[r]
+    bad = 0
+    for r in range(4):
+        pr, pc = ga.coords(r)
+        ri = torch.arange(n, device=dev)
+        rr = ri[(ri // 64) % 2 == pr]
+        cc = ri[(ri // 64) % 2 == pc]
+        bad += int((Gm[rr][:, cc] != A[r]).sum())
+    byts = 16.0 * n * n
+    pk = peaks()
+    gbs_pack, gbs_unpack = byts / t_pack / 1e6, byts / t_unpack / 1e6
+    line = {"metric": f"block-cyclic redistribution (PDGEMR2D pack + unpack) GB/s, n={n}, 2x2 nb=64 -> 4x1 panels",
+            "value": 2 * byts / (t_pack + t_unpack) / 1e6, "unit": "GB/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_pack + t_unpack, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"REDIST of an {n} x {n} FP64 matrix, 4 emulated ranks on one GPU",
+                       "l2": "2 GiB per pass > L2, no flush"},
+            "pack_ms": t_pack, "unpack_ms": t_unpack, "pack_gbs": gbs_pack, "unpack_gbs": gbs_unpack,
+            "mismatches": bad, "gpu_launches": 8 * args.steps,
+            "roofline": {"bound": "hbm", "achieved": 2 * byts / (t_pack + t_unpack) / 1e6, "peak": pk["hbm"],
+                         "unit": "GB/s", "frac": 2 * byts / (t_pack + t_unpack) / 1e6 / pk["hbm"],
+                         "traffic": None, "kernel": "k_pack / k_unpack", "peak_source": pk["source"]}}
+    print(json.dumps(line), flush=True)
+    return 0 if bad == 0 else 1
+
+
 def run_merge_level(args, ws, rank, local):
     """Batched divide-and-conquer merge level: 64 independent Cauchy multiplies Q_i = A_i H_i,
     n_i log-uniform in [256, 8192] (seeded), generators as the n = 2048 workload (d sorted
@@ -706,6 +796,8 @@ def main():
     ap.add_argument("--merge-fp64", action="store_true", help="also time the FP64 path of the merge level")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-tune", action="store_true", help="merge level: skip the grouped-GEMM autotuner")
+    ap.add_argument("--redist", action="store_true", help="time the block-cyclic redistribution kernels")
+    ap.add_argument("--redist-n", type=int, default=16384)
     args = ap.parse_args()
     ws, rank, local = dist_init(args)
     if args.impl == "reference":
@@ -720,6 +812,8 @@ def main():
         return run_merge_level(args, ws, rank, local)
     if args.cfg1:
         return run_cfg1(args, ws, rank, local)
+    if args.redist:
+        return run_redist(args, ws, rank, local)
     return run_gpu(args, ws, rank, local)
 
 

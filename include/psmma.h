@@ -225,6 +225,64 @@ int psmma_tune_batch(int count, const psmma_batch_item* items, double alpha, dou
 size_t psmma_batch_workspace_size(int count, const psmma_batch_item* items, int compressor,
                                   const psmma_opts* opts);
 
+/* ---- block-cyclic redistribution (REDIST / PDGEMR2D) -------------------------------- */
+
+/* With REDIST = .TRUE. the reference copies A from its block-cyclic layout to a blocked one
+ * and Q back with PDGEMR2D (psmma_cauchy.f90:113-162; the same in psmma_toeplitz.f90,
+ * psmma_hankel.f90, psmma_cauchyeig.f90).  Here that copy is: a plan (host, built once per
+ * pair of layouts), a pack kernel that gathers this rank's elements into one contiguous
+ * segment per destination rank, ONE all-to-all exchange run by the caller (MPI_Alltoallv,
+ * NCCL, torch.distributed all_to_all_single) with the plan's counts, and an unpack kernel
+ * that scatters the received segments into the destination's local array.
+ *
+ * A layout is a ScaLAPACK descriptor desc[9] = {DTYPE_=1, CTXT_ (unused), M_, N_, MB_, NB_,
+ * RSRC_, CSRC_, LLD_} on a process grid.  The sub-matrix A(ia:ia+m-1, ja:ja+n-1) (1-based)
+ * of layout a goes to B(ib:ib+m-1, jb:jb+n-1) of layout b; both grids span the same nprocs
+ * processes, `rank` is this process (its grid coordinates follow from the grid's order).
+ * Descriptor errors return -(100 * argument position + entry) as ScaLAPACK's CHK1MAT. */
+typedef struct psmma_grid {
+  int nprow, npcol;
+  int order;           /* 0: rank = prow * npcol + pcol (BLACS_GRIDINIT 'R'), 1: column-major ('C') */
+} psmma_grid;
+
+typedef struct psmma_redist_plan psmma_redist_plan;
+
+/* ScaLAPACK's NUMROC (0-based process numbers): the local count of an n-vector in blocks of
+ * nb on process iproc when block 0 is on isrcproc. */
+int psmma_numroc(int n, int nb, int iproc, int isrcproc, int nprocs);
+int psmma_redist_plan_create(int m, int n, const int* desca, int ia, int ja, psmma_grid ga,
+                             const int* descb, int ib, int jb, psmma_grid gb, int rank,
+                             psmma_redist_plan** out);
+/* Elements this rank sends to / receives from each rank (nprocs entries each, rank order);
+ * segments are packed in rank order, so the displacements are the prefix sums. */
+int psmma_redist_counts(const psmma_redist_plan* p, long long* send_counts, long long* recv_counts);
+/* This rank's local array shapes (rows x cols) in layout a and layout b. */
+int psmma_redist_local_shape(const psmma_redist_plan* p, int* a_rows, int* a_cols, int* b_rows,
+                             int* b_cols);
+/* The plan's index maps: which = 0/1 rows/cols of the a-local array (the b-grid process row /
+ * column that receives each local index, -1 outside the sub-matrix, and its place in that
+ * segment), 2/3 rows/cols of the b-local array (the a-grid sender).  Returns the entry count;
+ * part/pos may be NULL to query it. */
+int psmma_redist_maps(const psmma_redist_plan* p, int which, int* part, int* pos);
+/* Device pointers; elem_bytes 8 (double) or 16 (double complex).  The A-local array has
+ * leading dimension desca[8], the B-local array descb[8]; the buffers hold the sums of the
+ * send / receive counts.  The first call uploads the plan's maps to the current device. */
+int psmma_redist_pack(psmma_redist_plan* p, const void* A, void* sendbuf, int elem_bytes, void* stream);
+int psmma_redist_unpack(psmma_redist_plan* p, const void* recvbuf, void* B, int elem_bytes, void* stream);
+int psmma_redist_plan_destroy(psmma_redist_plan* p);
+
+/* 2.5D helpers (Auxil_2p5D.f90:315-419).  psmma_redist2p5_index is Redist2P5a: the 1-based
+ * indices 1..k ordered by process column, columns visited as I + J*(npcol/npzc) with I outer,
+ * J < npzc inner, each column's block-cyclic slice in order (npzc must divide npcol).
+ * psmma_redist2p5 is Redist2P5 on the device: TB(i,:) = B(pindex(i),:) for the ncb generator
+ * columns.  psmma_const_index1 is ConstIndex1: process column mycol's full block segments of a
+ * permuted list (cindex = pindex(mycol*nb + s*npcol*nb + 1 .. +nb)); it returns the count
+ * written and stops at n where the reference would read past it. */
+int psmma_redist2p5_index(int k, int nb, int npzc, int npcol, int* pindex);
+int psmma_redist2p5(int k, int nb, int npzc, int npcol, const double* B, int ldb, int ncb, double* TB,
+                    int ldtb, void* stream);
+int psmma_const_index1(int n, int nb, int mycol, int npcol, const int* pindex, int* cindex);
+
 /* ---- host-pointer entry points (copy in, compute, copy out, synchronise) ------------ */
 int psmma_cauchy_host(int n, int k, double alpha, const double* A, int lda,
                       const double* gen, int ldgen, double beta, double* Q, int ldq,

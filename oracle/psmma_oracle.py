@@ -21,8 +21,10 @@ The fixtures and answers are committed under tests/golden/ with the script that 
 
 Third-party arithmetic.  DGEMM/ZGEMM and the LAPACK routines (DGEQP3, DORGQR, ZGEQP3,
 ZUNMQR, ZGESVD) come from MKL or OpenBLAS in the reference builds (SLMakes/SLmake.inc*);
-here they are numpy/scipy (scipy-openblas).  ``NUMROC`` is ScaLAPACK's; it is restated
-from its documented definition.
+here they are numpy/scipy (scipy-openblas).  ``NUMROC``, ``INDXL2G`` and ``PDGEMR2D`` are
+ScaLAPACK's; they are restated from their documented definitions (PDGEMR2D as "assemble the
+global matrices, copy the sub-matrix, distribute again", sharing nothing with the library's
+per-peer plan).
 """
 from __future__ import annotations
 
@@ -81,6 +83,91 @@ def is_intersect(set_a: np.ndarray, set_b: np.ndarray) -> bool:
     two sets are DISJOINT (is_inters starts .TRUE. and is set .FALSE. on a common element);
     the caller stores the result in ``islowrank``."""
     return len(np.intersect1d(set_a, set_b)) == 0
+
+
+# ---------------------------------------------------------------------------------------
+# Block-cyclic layouts and their redistribution (PDGEMR2D, the 2.5D index helpers)
+# ---------------------------------------------------------------------------------------
+def indxl2g(l: int, nb: int, iproc: int, isrcproc: int, nprocs: int) -> int:
+    """ScaLAPACK INDXL2G (1-based local l -> 1-based global index), from its definition."""
+    return nprocs * nb * ((l - 1) // nb) + (l - 1) % nb + ((nprocs + iproc - isrcproc) % nprocs) * nb + 1
+
+
+def grid_coords(rank: int, nprow: int, npcol: int, order: str = "R") -> tuple[int, int]:
+    """BLACS grid coordinates of a rank ('R': row-major numbering, 'C': column-major)."""
+    if order.upper().startswith("R"):
+        return rank // npcol, rank % npcol
+    return rank % nprow, rank // nprow
+
+
+def bc_local(G: np.ndarray, desc, nprow: int, npcol: int, myrow: int, mycol: int) -> np.ndarray:
+    """Process (myrow, mycol)'s local array of the global matrix G in layout desc
+    (DTYPE, CTXT, M, N, MB, NB, RSRC, CSRC, LLD): the fill loop of the reference tests,
+    A(i,j) = G(indxl2g(i), indxl2g(j)) (Test/psmma_testcauchy.f90:93-101)."""
+    _, _, M, N, MB, NB, RS, CS, _ = desc
+    lr = numroc(M, MB, myrow, RS, nprow)
+    lc = numroc(N, NB, mycol, CS, npcol)
+    rows = [indxl2g(i, MB, myrow, RS, nprow) - 1 for i in range(1, lr + 1)]
+    cols = [indxl2g(j, NB, mycol, CS, npcol) - 1 for j in range(1, lc + 1)]
+    return np.asarray(G)[np.ix_(rows, cols)].copy()
+
+
+def bc_global(locals_: dict, desc, nprow: int, npcol: int, order: str = "R", fill=0.0) -> np.ndarray:
+    """Assembles the global M x N matrix from every rank's local array (dict rank -> array)."""
+    _, _, M, N, MB, NB, RS, CS, _ = desc
+    first = next(iter(locals_.values()))
+    G = np.full((M, N), fill, dtype=first.dtype)
+    for rank, L in locals_.items():
+        pr, pc = grid_coords(rank, nprow, npcol, order)
+        lr = numroc(M, MB, pr, RS, nprow)
+        lc = numroc(N, NB, pc, CS, npcol)
+        rows = [indxl2g(i, MB, pr, RS, nprow) - 1 for i in range(1, lr + 1)]
+        cols = [indxl2g(j, NB, pc, CS, npcol) - 1 for j in range(1, lc + 1)]
+        G[np.ix_(rows, cols)] = L[:lr, :lc]
+    return G
+
+
+def pdgemr2d(m: int, n: int, A_locals: dict, ia: int, ja: int, desca, grid_a, B_locals: dict, ib: int, jb: int,
+             descb, grid_b) -> dict:
+    """PDGEMR2D's result: B(ib:ib+m-1, jb:jb+n-1) := A(ia:ia+m-1, ja:ja+n-1), every other
+    element of B unchanged.  grid_* = (nprow, npcol, order).  Works on the assembled global
+    matrices, so it shares nothing with the library's per-peer plan."""
+    GA = bc_global(A_locals, desca, *grid_a)
+    GB = bc_global(B_locals, descb, *grid_b)
+    GB[ib - 1:ib - 1 + m, jb - 1:jb - 1 + n] = GA[ia - 1:ia - 1 + m, ja - 1:ja - 1 + n]
+    out = {}
+    for rank in B_locals:
+        pr, pc = grid_coords(rank, *grid_b)
+        out[rank] = bc_local(GB, descb, grid_b[0], grid_b[1], pr, pc)
+    return out
+
+
+def redist2p5a(k: int, nb: int, npzc: int, npcol: int) -> np.ndarray:
+    """Redist2P5a (Auxil_2p5D.f90:362-390): 1..k ordered by process column, the columns taken
+    as I + J*(npcol/npzc), I outer, J inner, each contributing its ConstIndex slice."""
+    if npcol % npzc:
+        raise ValueError("NPZC must divide NPCOL")
+    lnpcol = npcol // npzc
+    out = []
+    for i in range(lnpcol):
+        for j in range(npzc):
+            out.extend(const_index(k, nb, i + j * lnpcol, npcol).tolist())
+    return np.asarray(out, dtype=np.int64)
+
+
+def const_index1(n: int, nb: int, mycol: int, npcol: int, pindex) -> list:
+    """ConstIndex1 (Auxil_2p5D.f90:392-419): nfseg = ICEIL(n, nb) / npcol full segments of nb
+    entries of pindex starting at mycol*nb + 1, stride npcol*nb.  Entries past n (which the
+    reference would read out of bounds when the last block is partial) are returned as None."""
+    knb = -(-n // nb)
+    nfseg = knb // npcol
+    cstart = mycol * nb
+    out = []
+    for _ in range(nfseg):
+        for t in range(cstart, cstart + nb):
+            out.append(int(pindex[t]) if t < n else None)
+        cstart += npcol * nb
+    return out
 
 
 # ---------------------------------------------------------------------------------------

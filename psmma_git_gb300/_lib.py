@@ -46,6 +46,10 @@ class PsmmaOpts(C.Structure):
     ]
 
 
+class PsmmaGrid(C.Structure):
+    _fields_ = [("nprow", C.c_int), ("npcol", C.c_int), ("order", C.c_int)]
+
+
 class PsmmaRequest(C.Structure):
     _fields_ = [
         ("kind", C.c_int), ("precision", C.c_int), ("n_moduli", C.c_int), ("n", C.c_int), ("k", C.c_int),
@@ -132,6 +136,18 @@ SIGNATURES = {
                                            C.POINTER(PsmmaBatchStats), _p]),
     "psmma_cauchyeig_batch_workspace_size": (C.c_size_t, [_i, C.POINTER(PsmmaBatchItem), _i, _op]),
     "psmma_tune_batch": (_i, [_i, C.POINTER(PsmmaBatchItem), _d, _d, _i, _d, _op, C.POINTER(PsmmaTuneResult), _p]),
+    "psmma_numroc": (_i, [_i, _i, _i, _i, _i]),
+    "psmma_redist_plan_create": (_i, [_i, _i, _ip, _i, _i, PsmmaGrid, _ip, _i, _i, PsmmaGrid, _i,
+                                      C.POINTER(C.c_void_p)]),
+    "psmma_redist_counts": (_i, [_p, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
+    "psmma_redist_local_shape": (_i, [_p, _ip, _ip, _ip, _ip]),
+    "psmma_redist_maps": (_i, [_p, _i, _ip, _ip]),
+    "psmma_redist_pack": (_i, [_p, _p, _p, _i, _p]),
+    "psmma_redist_unpack": (_i, [_p, _p, _p, _i, _p]),
+    "psmma_redist_plan_destroy": (_i, [_p]),
+    "psmma_redist2p5_index": (_i, [_i, _i, _i, _i, _ip]),
+    "psmma_redist2p5": (_i, [_i, _i, _i, _i, _p, _i, _i, _p, _i, _p]),
+    "psmma_const_index1": (_i, [_i, _i, _i, _i, _ip, _ip]),
 }
 
 

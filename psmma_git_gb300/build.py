@@ -20,7 +20,7 @@ BUILD = PKG / "_build"
 LIB = PKG / "libpsmma_gb300.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["psmma_capi.cu", "fp64_structured.cu", "split_crt.cu", "split_noalloc.cu", "selftest.cu",
-           "serving.cu", "lowrank.cu"]
+           "serving.cu", "lowrank.cu", "redist.cu"]
 HEADERS = ["psmma_internal.h", "tcgen05_util.cuh"]
 
 
