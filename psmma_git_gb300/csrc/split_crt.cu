@@ -8,7 +8,7 @@
 //   2. For pairwise coprime moduli m_1..m_N <= 256 the residues A' mod m_l and H' mod m_l
 //      lie in [-128, 128] and are exact in BF16.
 //   3. One BF16 GEMM per modulus gives Z_l = A'H' mod m_l.  FP32 accumulation is exact
-//      because the tensor memory accumulator is drained every 512 k (|sum| <= 2^23) into a
+//      because the tensor memory accumulator is drained every 1024 k (|sum| <= 2^24) into a
 //      register-held residue.
 //   4. Z = A'H' is recovered exactly by CRT (128-bit integer arithmetic, |Z| < M/16 with
 //      M = prod m_l), scaled back by 2^-(s_i+f_j) and combined with alpha and beta in FP64.
@@ -588,7 +588,9 @@ __global__ void k_residues_A_dft(const double* __restrict__ Bre, long ldb2, int 
 // ------------------------------------------------------------------------------------------
 constexpr int G_BM = 128, G_BN = 256, G_BK = 64;
 constexpr int G_STAGES = 4;
-constexpr int G_CHUNK_KB = 8;  // 8 x 64 = 512 k per exact FP32 chunk: |sum| <= 512*128*128 = 2^23
+// 16 x 64 = 1024 k per FP32 chunk: residues |r| <= 128 (|r| <= 127 for the odd moduli), so every
+// partial sum is an integer with |sum| <= 1024 * 128 * 128 = 2^24, exact in FP32.
+constexpr int G_CHUNK_KB = 16;
 constexpr int G_EPI_WARPS = 8;
 constexpr int G_THREADS = (G_EPI_WARPS + 2) * 32;
 constexpr uint32_t G_A_BYTES = G_BM * G_BK * 2;
@@ -827,9 +829,11 @@ __global__ void __launch_bounds__(G_THREADS, 1) k_crt_gemm(const __grid_constant
           tmem_ld_wait();
 #pragma unroll
           for (int e = 0; e < 32; ++e) {
-            float v = __uint_as_float(r[e]) + res[cb * 32 + e];  // exact: |v| < 2^24
-            float qq = rintf(v * inv_m);
-            float x = fmaf(-qq, m, v);
+            // reduce the chunk's sum first (|v| <= 2^24: adding the carried residue could
+            // leave the exact range), then add the carried residue: |x| <= m/2 + 3 + 128
+            const float v = __uint_as_float(r[e]);
+            const float qq = rintf(v * inv_m);
+            float x = fmaf(-qq, m, v) + res[cb * 32 + e];
             x = (x > 127.0f) ? x - m : x;
             x = (x < -128.0f) ? x + m : x;
             res[cb * 32 + e] = x;
