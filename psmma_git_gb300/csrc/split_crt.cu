@@ -591,6 +591,8 @@ constexpr int G_STAGES = 4;
 // 16 x 64 = 1024 k per FP32 chunk: residues |r| <= 128 (|r| <= 127 for the odd moduli), so every
 // partial sum is an integer with |sum| <= 1024 * 128 * 128 = 2^24, exact in FP32.
 constexpr int G_CHUNK_KB = 16;
+// Chunk sums are added as int32 and reduced modulo m every 16 chunks: |sum| <= 2^28 + 128.
+constexpr int G_RED_CHUNKS = 16;
 constexpr int G_EPI_WARPS = 8;
 constexpr int G_THREADS = (G_EPI_WARPS + 2) * 32;
 constexpr uint32_t G_A_BYTES = G_BM * G_BK * 2;
@@ -677,6 +679,16 @@ struct GroupGemm {
     return ti;
   }
 };
+
+// s mod m in [-128, 127] for |s| <= 2^28 + 128 and m <= 256: the float quotient estimate is
+// within 0.3 of s / m, so q is off by at most one and one correction on each side suffices.
+__device__ __forceinline__ int mod_sym(int s, int m, float inv_m) {
+  const int q = __float2int_rn(__int2float_rn(s) * inv_m);
+  int x = s - q * m;
+  x = (x > 127) ? x - m : x;
+  x = (x < -128) ? x + m : x;
+  return x;
+}
 
 template <int BN>
 struct GemmShape {
@@ -813,10 +825,13 @@ __global__ void __launch_bounds__(G_THREADS, 1) k_crt_gemm(const __grid_constant
     for (int t = blockIdx.x; t < total && ok; t += gridDim.x) {
       const TileInfo ti = ts.tile(t);
       const int cpt = (ti.nkb + G_CHUNK_KB - 1) / G_CHUNK_KB;
-      const float m = (float)g.m[ti.l], inv_m = g.inv_m[ti.l];
-      float res[HALF];
+      const int mi = g.m[ti.l];
+      const float inv_m = g.inv_m[ti.l];
+      // int32 running sums of the chunks' exact FP32 sums (|chunk| <= 2^24), reduced to
+      // [-128, 127] every G_RED_CHUNKS chunks and at the end of the tile
+      int res[HALF];
 #pragma unroll
-      for (int e = 0; e < HALF; ++e) res[e] = 0.0f;
+      for (int e = 0; e < HALF; ++e) res[e] = 0;
       for (int cc = 0; cc < cpt; ++cc, ++c) {
         const int buf = c & 1;
         const uint32_t use = (uint32_t)(c >> 1);
@@ -828,19 +843,14 @@ __global__ void __launch_bounds__(G_THREADS, 1) k_crt_gemm(const __grid_constant
           tmem_ld32(tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * BN + h * HALF + cb * 32), r);
           tmem_ld_wait();
 #pragma unroll
-          for (int e = 0; e < 32; ++e) {
-            // reduce the chunk's sum first (|v| <= 2^24: adding the carried residue could
-            // leave the exact range), then add the carried residue: |x| <= m/2 + 3 + 128
-            const float v = __uint_as_float(r[e]);
-            const float qq = rintf(v * inv_m);
-            float x = fmaf(-qq, m, v) + res[cb * 32 + e];
-            x = (x > 127.0f) ? x - m : x;
-            x = (x < -128.0f) ? x + m : x;
-            res[cb * 32 + e] = x;
-          }
+          for (int e = 0; e < 32; ++e) res[cb * 32 + e] += __float2int_rn(__uint_as_float(r[e]));
         }
         tc_fence_before();
         mbar_arrive(&acc_empty[buf]);
+        if ((cc % G_RED_CHUNKS) == G_RED_CHUNKS - 1 || cc == cpt - 1) {
+#pragma unroll
+          for (int e = 0; e < HALF; ++e) res[e] = mod_sym(res[e], mi, inv_m);
+        }
       }
       const int i = ti.tm * G_BM + q * 32 + lane;
       if (ok && !*abort_flag && i < ti.n) {
@@ -850,10 +860,10 @@ __global__ void __launch_bounds__(G_THREADS, 1) k_crt_gemm(const __grid_constant
           uint32_t w[4];
 #pragma unroll
           for (int t4 = 0; t4 < 4; ++t4) {
-            uint32_t b0 = (uint32_t)(uint8_t)(int8_t)__float2int_rn(res[v * 16 + t4 * 4 + 0]);
-            uint32_t b1 = (uint32_t)(uint8_t)(int8_t)__float2int_rn(res[v * 16 + t4 * 4 + 1]);
-            uint32_t b2 = (uint32_t)(uint8_t)(int8_t)__float2int_rn(res[v * 16 + t4 * 4 + 2]);
-            uint32_t b3 = (uint32_t)(uint8_t)(int8_t)__float2int_rn(res[v * 16 + t4 * 4 + 3]);
+            uint32_t b0 = (uint32_t)(uint8_t)(int8_t)res[v * 16 + t4 * 4 + 0];
+            uint32_t b1 = (uint32_t)(uint8_t)(int8_t)res[v * 16 + t4 * 4 + 1];
+            uint32_t b2 = (uint32_t)(uint8_t)(int8_t)res[v * 16 + t4 * 4 + 2];
+            uint32_t b3 = (uint32_t)(uint8_t)(int8_t)res[v * 16 + t4 * 4 + 3];
             w[t4] = b0 | (b1 << 8) | (b2 << 16) | (b3 << 24);
           }
           *(uint4*)(dst + v * 16) = make_uint4(w[0], w[1], w[2], w[3]);
