@@ -176,6 +176,22 @@ size_t split_workspace_general(int M, int N, int K, int n_moduli) {
 // ------------------------------------------------------------------------------------------
 constexpr unsigned long long ABS_MASK = 0x7FFFFFFFFFFFFFFFull;
 constexpr unsigned long long INF_BITS = 0x7FF0000000000000ull;
+constexpr int NO_SCALE = -100000;
+
+// The bound sums (row sums of squares of A, column sums of |H| and of H^2) are accumulated in
+// FP32 on a per-thread power-of-two scale, because GB300 issues FP64 at about one operation
+// per SM per cycle.  abs_scaled_up gives |x| * 2^-e as a float that is never below the true
+// value (top 23 mantissa bits, rounded up; magnitudes under 2^-126 become 2^-126), from the
+// bits of x on the integer pipe, and sets *big when |x| * 2^-e >= 2^56 (then the caller sums
+// that thread's values in FP64 instead).  With round-up FP32 adds the sums stay upper bounds.
+__device__ __forceinline__ float abs_scaled_up(unsigned long long ab, int e, bool* big) {
+  const int fe = (int)(ab >> 52) - 1023 - e + 127;
+  *big |= fe >= 127 + 56;
+  const int fc = max(1, min(fe, 254));
+  unsigned fb = ((unsigned)fc << 23) | ((unsigned)(ab >> 29) & 0x7FFFFFu);
+  fb += (fe < 1 || (ab & 0x1FFFFFFFull) != 0ull) ? 1u : 0u;
+  return ab ? __uint_as_float(fb) : 0.0f;
+}
 
 // Row max of |A| as the bits of a non-negative double (NaN/Inf compare above all finite) and
 // row sums of squares (for the Cauchy-Schwarz bound of the integer product).
@@ -193,12 +209,47 @@ __device__ __forceinline__ void row_absmax_blk(const double* __restrict__ A, lon
   if (i >= n) return;
   int k0 = by * kchunk, k1 = min(k, k0 + kchunk);
   unsigned long long mb = 0;
-  double sq = 0.0;
-  for (int kk = k0; kk < k1; ++kk) {
-    const double a = __ldg(acol(A, lda, A2, lda2, ka, kk) + i);
-    unsigned long long b = (unsigned long long)__double_as_longlong(a) & ABS_MASK;
+  float sq32 = 0.0f;
+  int e = NO_SCALE;  // set by the first group with a nonzero entry
+  bool big = false;
+  int kk = k0;
+  // eight independent loads in flight per thread (a warp reads 32 consecutive rows)
+  for (; kk + 8 <= k1; kk += 8) {
+    unsigned long long b[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+      b[u] = (unsigned long long)__double_as_longlong(__ldg(acol(A, lda, A2, lda2, ka, kk + u) + i)) & ABS_MASK;
+    unsigned long long gm = 0;
+#pragma unroll
+    for (int u = 0; u < 8; ++u) gm = b[u] > gm ? b[u] : gm;
+    mb = gm > mb ? gm : mb;
+    if (e == NO_SCALE && gm) e = (int)(gm >> 52) - 1023;
+    if (e != NO_SCALE) {
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const float f = abs_scaled_up(b[u], e, &big);
+        sq32 = __fmaf_ru(f, f, sq32);
+      }
+    }
+  }
+  for (; kk < k1; ++kk) {
+    const unsigned long long b =
+        (unsigned long long)__double_as_longlong(__ldg(acol(A, lda, A2, lda2, ka, kk) + i)) & ABS_MASK;
     mb = b > mb ? b : mb;
-    sq = fma(a, a, sq);
+    if (e == NO_SCALE && b) e = (int)(b >> 52) - 1023;
+    if (e != NO_SCALE) {
+      const float f = abs_scaled_up(b, e, &big);
+      sq32 = __fmaf_ru(f, f, sq32);
+    }
+  }
+  double sq = 0.0;
+  if (big) {  // entries 2^56 times the thread's first ones (or Inf/NaN): FP64 sum
+    for (kk = k0; kk < k1; ++kk) {
+      const double a = __ldg(acol(A, lda, A2, lda2, ka, kk) + i);
+      sq = fma(a, a, sq);
+    }
+  } else if (e != NO_SCALE) {
+    sq = ldexp((double)sq32, 2 * e);
   }
   if (mb) atomicMax(amax_bits + i, mb);
   if (sq != 0.0) atomicAdd(asq + i, sq);
@@ -228,7 +279,9 @@ __device__ __forceinline__ void h_pass1_blk(const GenSpec& gs, int K, int kp, do
     }
   }
   unsigned long long mb = 0;
-  double s = 0.0, s2 = 0.0;
+  float s32 = 0.0f, s2_32 = 0.0f;
+  int e = NO_SCALE;  // set by the thread's first nonzero entry
+  bool big = false;
   double* row = Ht + (long)j * kp;
   for (int kk = threadIdx.x; kk < kp; kk += blockDim.x) {
     double h = 0.0;
@@ -272,8 +325,23 @@ __device__ __forceinline__ void h_pass1_blk(const GenSpec& gs, int K, int kp, do
     row[kk] = h;
     unsigned long long b = (unsigned long long)__double_as_longlong(h) & ABS_MASK;
     mb = b > mb ? b : mb;
-    s += fabs(h);
-    s2 = fma(h, h, s2);
+    if (e == NO_SCALE && b) e = (int)(b >> 52) - 1023;
+    if (e != NO_SCALE) {
+      const float f = abs_scaled_up(b, e, &big);
+      s32 = __fadd_ru(s32, f);
+      s2_32 = __fmaf_ru(f, f, s2_32);
+    }
+  }
+  double s = 0.0, s2 = 0.0;
+  if (big) {  // entries 2^56 times the thread's first one (or Inf/NaN): FP64 sums
+    for (int kk = threadIdx.x; kk < kp; kk += blockDim.x) {
+      const double h = row[kk];
+      s += fabs(h);
+      s2 = fma(h, h, s2);
+    }
+  } else if (e != NO_SCALE) {
+    s = ldexp((double)s32, e);
+    s2 = ldexp((double)s2_32, 2 * e);
   }
   __shared__ unsigned long long smax[32];
   __shared__ double ssum[32], ssq[32];
@@ -422,38 +490,38 @@ __device__ __forceinline__ unsigned long long scaled_int(double x, int e, bool* 
   return q;
 }
 
-// Symmetric residue (|r| <= m/2) of the integer x = x2*2^42 + x1*2^21 + x0 (x < 2^53, chunks
-// of 21 bits) modulo m, negated when neg.  t = x mod-equivalent < 2^30, reduced by Barrett
-// division with magic = floor(2^32/m) (quotient exact or one too small).
-__device__ __forceinline__ int sym_residue(unsigned x0, unsigned x1, unsigned x2, bool neg, unsigned m,
-                                           unsigned magic, unsigned c21, unsigned c42) {
-  const unsigned t = x2 * c42 + x1 * c21 + x0;
-  const unsigned q = __umulhi(t, magic);
-  int r = (int)(t - q * m);
-  r = (r >= (int)m) ? r - (int)m : r;
-  r = (r > (int)(m >> 1)) ? r - (int)m : r;
-  return neg ? -r : r;
-}
-
-// BF16 bits of an integer with |r| <= 2^8 (exact): float via the 1.5*2^23 magic number, then
-// the top half of its bits.
-__device__ __forceinline__ unsigned bf16_small(int r) {
-  return __float_as_uint(__int_as_float(0x4B400000 + r) - 12582912.0f) >> 16;
-}
-
 // Residues of two neighbouring integers for every modulus, packed as bf16x2 into planes.
+// For x = x2*2^42 + x1*2^21 + x0 (< 2^53) and modulus m with h = floor(m/2):
+// t = x2*(2^42 mod m) + x1*(2^21 mod m) + x0 + h < 2^30 is reduced by Barrett division
+// (magic = floor(2^32/m): the quotient is exact or one too small, so r = t - q*m < 2m and
+// one unsigned min corrects it); r - h is the symmetric residue of x in [-h, m-1-h].  Its
+// BF16 value, with the sign of x applied, is one FMA on the 1.5*2^23 magic number (exact
+// for integers of magnitude <= 2^8): fma(float(0x4B400000 - h + r), sign, -1.5*2^23*sign).
+// The modulus loop is unrolled over the maximum count, so the per-modulus constants are
+// kernel-parameter operands.
 __device__ __forceinline__ void write_residue_pair(unsigned long long u0, bool n0, unsigned long long u1, bool n1,
                                                    const CrtConsts& cc, uint32_t* dst, size_t plane_words) {
   const unsigned a0 = (unsigned)(u0 & 0x1FFFFFull), a1 = (unsigned)((u0 >> 21) & 0x1FFFFFull),
                  a2 = (unsigned)(u0 >> 42);
   const unsigned b0 = (unsigned)(u1 & 0x1FFFFFull), b1 = (unsigned)((u1 >> 21) & 0x1FFFFFull),
                  b2 = (unsigned)(u1 >> 42);
-#pragma unroll 4
-  for (int l = 0; l < cc.nmod; ++l) {
-    const unsigned m = (unsigned)cc.m[l], mg = cc.magic[l], c21 = (unsigned)cc.c21[l], c42 = (unsigned)cc.c42[l];
-    const int r0 = sym_residue(a0, a1, a2, n0, m, mg, c21, c42);
-    const int r1 = sym_residue(b0, b1, b2, n1, m, mg, c21, c42);
-    dst[l * plane_words] = bf16_small(r0) | (bf16_small(r1) << 16);
+  const float s0 = n0 ? -1.0f : 1.0f, s1 = n1 ? -1.0f : 1.0f;
+  const float o0 = -12582912.0f * s0, o1 = -12582912.0f * s1;
+#pragma unroll
+  for (int l = 0; l < SPL_MAX_MODULI; ++l) {
+    if (l < cc.nmod) {
+      const unsigned m = (unsigned)cc.m[l], mg = cc.magic[l], c21 = (unsigned)cc.c21[l],
+                     c42 = (unsigned)cc.c42[l], h = m >> 1;
+      const unsigned t0 = a2 * c42 + a1 * c21 + a0 + h;
+      const unsigned t1 = b2 * c42 + b1 * c21 + b0 + h;
+      unsigned r0 = t0 - __umulhi(t0, mg) * m;
+      unsigned r1 = t1 - __umulhi(t1, mg) * m;
+      r0 = min(r0, r0 - m);
+      r1 = min(r1, r1 - m);
+      const float f0 = fmaf(__uint_as_float(0x4B400000u - h + r0), s0, o0);
+      const float f1 = fmaf(__uint_as_float(0x4B400000u - h + r1), s1, o1);
+      dst[l * plane_words] = __byte_perm(__float_as_uint(f0), __float_as_uint(f1), 0x7632);
+    }
   }
 }
 
