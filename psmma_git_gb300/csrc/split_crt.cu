@@ -52,13 +52,22 @@ struct CrtConsts {
   int ffix[SPL_MAX_MODULI];            // round(2^19 * C_l / M): fixed-point quotient estimate
   unsigned long long biasl[4];         // sum_l 128 * climb[l][t], per limb, unreduced
   unsigned Mlimb[4];                   // M as four 32-bit limbs
+  // residue pass: exact Barrett division of t < 2^30 (q = umulhi(t, magic38) >> 6),
+  // h = floor(m/2) and the float bits 0x4B400000 - h of the symmetric shift
+  unsigned magic38[SPL_MAX_MODULI];    // ceil(2^38 / m)
+  unsigned half[SPL_MAX_MODULI];
+  unsigned hbase[SPL_MAX_MODULI];
 };
 
 // Device-side parameters of one call (in the workspace).
+constexpr int PARAMS_BLOCKS = 32;  // blocks of the single-product parameter pass
+
 struct SplitDevParams {
   unsigned status;
   int PA, PH;                   // bits of the integer-scaled A (per row) and H (per column)
   unsigned long long rho_bits;  // max_j sum_k |H_kj| / max_k |H_kj| (bits of a positive double)
+  unsigned done;                // parameter-pass blocks finished
+  double part[PARAMS_BLOCKS][6];  // their partial ratio maxima and sums, combined in block order
 };
 
 // ------------------------------------------------------------------------------------------
@@ -107,6 +116,12 @@ static CrtConsts make_consts(int nmod) {
   u128 bias = 0;
   for (int l = 0; l < nmod; l++) {
     c.magic[l] = (unsigned)((1ULL << 32) / (unsigned long long)kModuli[l]);
+    // ceil(2^38/m) * m - 2^38 < m <= 256, so t * magic38 / 2^38 < t/m + 2^-8 for t < 2^30:
+    // the floor is exact because frac(t/m) <= 1 - 1/m <= 1 - 2^-8 (equality only for m = 256,
+    // where the error term is 0)
+    c.magic38[l] = (unsigned)(((1ULL << 38) + kModuli[l] - 1) / (unsigned long long)kModuli[l]);
+    c.half[l] = (unsigned)(kModuli[l] >> 1);
+    c.hbase[l] = 0x4B400000u - c.half[l];
     u128 C = ((u128)c.C_hi[l] << 64) | c.C_lo[l];
     for (int t = 0; t < 4; t++) c.climb[l][t] = (unsigned)(C >> (32 * t));
     bias += (u128)128 * C;  // wraps modulo 2^128
@@ -393,14 +408,15 @@ __global__ void k_h_pass1(GenSpec gs, int K, int kp, double* __restrict__ Ht,
 // The budget PA + PH comes from the smaller bound.  It is split to balance the two rounding
 // errors, ~2^-PA * c_A and ~2^-PH * c_H with c_A ~ rms_i(max|A_i:|)/rms(A),
 // c_H ~ rms_j(max|H_:j|)/rms(H) (same constant factor): PH - PA = round(log2(c_H/c_A)).
-__device__ __forceinline__ void split_params_blk(SplitDevParams* prm, double log2M, int n, int ncols, int k,
-                                                 const unsigned long long* __restrict__ amax_bits,
-                                                 const double* __restrict__ asq,
-                                                 const unsigned long long* __restrict__ hmax_bits,
-                                                 const double* __restrict__ hsq) {
+// Partial maxima of the row / column ratios ||.||_2 / max|.| and sums of max^2 and ||.||_2^2
+// over rows [i0, i1) of A and columns [j0, j1) of H; the block's totals land in thread 0's v.
+__device__ __forceinline__ void params_partial(int i0, int i1, int j0, int j1, double rk,
+                                               const unsigned long long* __restrict__ amax_bits,
+                                               const double* __restrict__ asq,
+                                               const unsigned long long* __restrict__ hmax_bits,
+                                               const double* __restrict__ hsq, double v[6]) {
   double ra = 0.0, amx2 = 0.0, afro = 0.0, rh = 0.0, hmx2 = 0.0, hfro = 0.0;
-  const double rk = sqrt((double)k);  // k: inner length (rows of H, columns of A)
-  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+  for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
     const unsigned long long b = amax_bits[i];
     if (b == 0 || b >= INF_BITS) continue;
     const double m = __longlong_as_double((long long)b), q = asq[i];
@@ -408,7 +424,7 @@ __device__ __forceinline__ void split_params_blk(SplitDevParams* prm, double log
     ra = fmax(ra, safe ? sqrt(q) / m : rk);
     if (safe) { amx2 += m * m; afro += q; }
   }
-  for (int j = threadIdx.x; j < ncols; j += blockDim.x) {
+  for (int j = j0 + threadIdx.x; j < j1; j += blockDim.x) {
     const unsigned long long b = hmax_bits[j];
     if (b == 0 || b >= INF_BITS) continue;
     const double m = __longlong_as_double((long long)b), q = hsq[j];
@@ -416,7 +432,7 @@ __device__ __forceinline__ void split_params_blk(SplitDevParams* prm, double log
     rh = fmax(rh, safe ? sqrt(q) / m : rk);
     if (safe) { hmx2 += m * m; hfro += q; }
   }
-  double v[6] = {ra, amx2, afro, rh, hmx2, hfro};
+  v[0] = ra; v[1] = amx2; v[2] = afro; v[3] = rh; v[4] = hmx2; v[5] = hfro;
   // block reduction: max for ra/rh, sums otherwise
   for (int o = 16; o > 0; o >>= 1)
     for (int t = 0; t < 6; ++t) {
@@ -435,30 +451,68 @@ __device__ __forceinline__ void split_params_blk(SplitDevParams* prm, double log
       for (int w = 1; w < nw; ++w) acc = (t == 0 || t == 3) ? fmax(acc, sv[t][w]) : acc + sv[t][w];
       v[t] = acc;
     }
-    double rho = __longlong_as_double((long long)prm->rho_bits);
-    if (!(rho >= 1.0)) rho = rk * rk;
-    const double l1 = log2(rho * 1.01 + (double)k / 512.0);
-    const double cs = log2((v[0] * 1.01 + rk / 512.0) * (v[3] * 1.01 + rk / 512.0));
-    const double bound = fmin(l1, (v[0] > 0.0 && v[3] > 0.0) ? cs : l1);
-    int budget = (int)floor(log2M - 4.0 - bound);
-    int d = 0;
-    if (v[1] > 0.0 && v[2] > 0.0 && v[4] > 0.0 && v[5] > 0.0) {
-      const double cA = sqrt(v[1] / v[2]), cH = sqrt(v[4] / v[5]);
-      d = (int)lrint(log2(cH / cA));
-      d = max(-12, min(12, d));
-    }
-    int PA = (budget - d) >> 1, PH = budget - PA;
-    if (PH > 53) { PA += PH - 53; PH = 53; }
-    if (PA > 53) { PH += PA - 53; PA = 53; }
-    prm->PA = max(8, min(53, PA));
-    prm->PH = max(8, min(53, PH));
   }
 }
 
+// PA and PH from the totals (thread 0).
+__device__ __forceinline__ void params_finish(SplitDevParams* prm, double log2M, int k, const double v[6]) {
+  const double rk = sqrt((double)k);
+  double rho = __longlong_as_double((long long)prm->rho_bits);
+  if (!(rho >= 1.0)) rho = rk * rk;
+  const double l1 = log2(rho * 1.01 + (double)k / 512.0);
+  const double cs = log2((v[0] * 1.01 + rk / 512.0) * (v[3] * 1.01 + rk / 512.0));
+  const double bound = fmin(l1, (v[0] > 0.0 && v[3] > 0.0) ? cs : l1);
+  int budget = (int)floor(log2M - 4.0 - bound);
+  int d = 0;
+  if (v[1] > 0.0 && v[2] > 0.0 && v[4] > 0.0 && v[5] > 0.0) {
+    const double cA = sqrt(v[1] / v[2]), cH = sqrt(v[4] / v[5]);
+    d = (int)lrint(log2(cH / cA));
+    d = max(-12, min(12, d));
+  }
+  int PA = (budget - d) >> 1, PH = budget - PA;
+  if (PH > 53) { PA += PH - 53; PH = 53; }
+  if (PA > 53) { PH += PA - 53; PA = 53; }
+  prm->PA = max(8, min(53, PA));
+  prm->PH = max(8, min(53, PH));
+}
+
+// One block over all rows and columns (the grouped launches: one block per product).
+__device__ __forceinline__ void split_params_blk(SplitDevParams* prm, double log2M, int n, int ncols, int k,
+                                                 const unsigned long long* __restrict__ amax_bits,
+                                                 const double* __restrict__ asq,
+                                                 const unsigned long long* __restrict__ hmax_bits,
+                                                 const double* __restrict__ hsq) {
+  double v[6];
+  params_partial(0, n, 0, ncols, sqrt((double)k), amax_bits, asq, hmax_bits, hsq, v);
+  if (threadIdx.x == 0) params_finish(prm, log2M, k, v);
+}
+
+// PARAMS_BLOCKS blocks, each over a slice of the rows and columns (the square roots and
+// divisions are FP64); the last block to finish combines the partials in block order, so the
+// result does not depend on the finishing order.
 __global__ void k_split_params(SplitDevParams* prm, double log2M, int n, int ncols, int k,
                                const unsigned long long* __restrict__ amax_bits, const double* __restrict__ asq,
                                const unsigned long long* __restrict__ hmax_bits, const double* __restrict__ hsq) {
-  split_params_blk(prm, log2M, n, ncols, k, amax_bits, asq, hmax_bits, hsq);
+  const int G = gridDim.x, b = blockIdx.x;
+  const int i0 = (int)((long)n * b / G), i1 = (int)((long)n * (b + 1) / G);
+  const int j0 = (int)((long)ncols * b / G), j1 = (int)((long)ncols * (b + 1) / G);
+  double v[6];
+  params_partial(i0, i1, j0, j1, sqrt((double)k), amax_bits, asq, hmax_bits, hsq, v);
+  if (threadIdx.x == 0) {
+    for (int t = 0; t < 6; ++t) prm->part[b][t] = v[t];
+    __threadfence();
+    if (atomicAdd(&prm->done, 1u) == (unsigned)G - 1) {
+      __threadfence();
+      double tot[6];
+      for (int t = 0; t < 6; ++t) tot[t] = __ldcg(&prm->part[0][t]);
+      for (int q = 1; q < G; ++q)
+        for (int t = 0; t < 6; ++t) {
+          const double x = __ldcg(&prm->part[q][t]);
+          tot[t] = (t == 0 || t == 3) ? fmax(tot[t], x) : tot[t] + x;
+        }
+      params_finish(prm, log2M, k, tot);
+    }
+  }
 }
 
 // Exponent s such that |x * 2^s| < 2^P for all |x| <= amax (amax finite, > 0).
@@ -492,13 +546,12 @@ __device__ __forceinline__ unsigned long long scaled_int(double x, int e, bool* 
 
 // Residues of two neighbouring integers for every modulus, packed as bf16x2 into planes.
 // For x = x2*2^42 + x1*2^21 + x0 (< 2^53) and modulus m with h = floor(m/2):
-// t = x2*(2^42 mod m) + x1*(2^21 mod m) + x0 + h < 2^30 is reduced by Barrett division
-// (magic = floor(2^32/m): the quotient is exact or one too small, so r = t - q*m < 2m and
-// one unsigned min corrects it); r - h is the symmetric residue of x in [-h, m-1-h].  Its
-// BF16 value, with the sign of x applied, is one FMA on the 1.5*2^23 magic number (exact
-// for integers of magnitude <= 2^8): fma(float(0x4B400000 - h + r), sign, -1.5*2^23*sign).
-// The modulus loop is unrolled over the maximum count, so the per-modulus constants are
-// kernel-parameter operands.
+// t = x2*(2^42 mod m) + x1*(2^21 mod m) + x0 + h < 2^30, r = t mod m by exact Barrett
+// division (q = umulhi(t, ceil(2^38/m)) >> 6), and r - h is the symmetric residue of x in
+// [-h, m-1-h].  Its BF16 value, with the sign of x applied, is one FMA on the 1.5*2^23 magic
+// number (exact for integers of magnitude <= 2^8): fma(float(0x4B400000 - h + r), sign,
+// -1.5*2^23*sign).  The modulus loop is unrolled over the maximum count, so the per-modulus
+// constants are kernel-parameter operands.
 __device__ __forceinline__ void write_residue_pair(unsigned long long u0, bool n0, unsigned long long u1, bool n1,
                                                    const CrtConsts& cc, uint32_t* dst, size_t plane_words) {
   const unsigned a0 = (unsigned)(u0 & 0x1FFFFFull), a1 = (unsigned)((u0 >> 21) & 0x1FFFFFull),
@@ -510,17 +563,16 @@ __device__ __forceinline__ void write_residue_pair(unsigned long long u0, bool n
 #pragma unroll
   for (int l = 0; l < SPL_MAX_MODULI; ++l) {
     if (l < cc.nmod) {
-      const unsigned m = (unsigned)cc.m[l], mg = cc.magic[l], c21 = (unsigned)cc.c21[l],
-                     c42 = (unsigned)cc.c42[l], h = m >> 1;
+      const unsigned m = (unsigned)cc.m[l], mg = cc.magic38[l], c21 = (unsigned)cc.c21[l],
+                     c42 = (unsigned)cc.c42[l], h = cc.half[l], hb = cc.hbase[l];
       const unsigned t0 = a2 * c42 + a1 * c21 + a0 + h;
       const unsigned t1 = b2 * c42 + b1 * c21 + b0 + h;
-      unsigned r0 = t0 - __umulhi(t0, mg) * m;
-      unsigned r1 = t1 - __umulhi(t1, mg) * m;
-      r0 = min(r0, r0 - m);
-      r1 = min(r1, r1 - m);
-      const float f0 = fmaf(__uint_as_float(0x4B400000u - h + r0), s0, o0);
-      const float f1 = fmaf(__uint_as_float(0x4B400000u - h + r1), s1, o1);
-      dst[l * plane_words] = __byte_perm(__float_as_uint(f0), __float_as_uint(f1), 0x7632);
+      const unsigned r0 = t0 - (__umulhi(t0, mg) >> 6) * m;
+      const unsigned r1 = t1 - (__umulhi(t1, mg) >> 6) * m;
+      const float f0 = fmaf(__uint_as_float(hb + r0), s0, o0);
+      const float f1 = fmaf(__uint_as_float(hb + r1), s1, o1);
+      *dst = __byte_perm(__float_as_uint(f0), __float_as_uint(f1), 0x7632);
+      dst += plane_words;
     }
   }
 }
@@ -1248,7 +1300,7 @@ static int split_core(int M, int N, int K, double alpha, const double* A, long l
     default: return PSMMA_EUNSUPPORTED;
   }
   prof_mark(stream, "h_generate");
-  k_split_params<<<1, 1024, 0, stream>>>(b.prm, cc.log2M, M, N, K, b.amax, b.asq, b.hmax, b.hsq);
+  k_split_params<<<PARAMS_BLOCKS, 512, 0, stream>>>(b.prm, cc.log2M, M, N, K, b.amax, b.asq, b.hmax, b.hsq);
   prof_mark(stream, "params");
   if (!dft)
     k_residues_A<<<dim3(L.kp / 64, (M + 31) / 32), 256, 0, stream>>>(A, lda, M, K, L.kp, b.amax, b.prm, cc, b.RA);
