@@ -207,7 +207,11 @@ struct HostArena {
   void* ptr = nullptr;
   size_t bytes = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t copy = nullptr;  // host<->device copies of the overlapped split path
+  cudaEvent_t ev[12] = {};
+  bool have_ev = false;
 };
+constexpr int kHostEvents = 12;
 std::mutex g_host_mu;
 std::map<int, HostArena> g_host;
 
@@ -239,6 +243,32 @@ void* host_arena(size_t bytes, cudaStream_t* stream, int* status) {
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
+// The copy stream and events of the current device's arena (created on first use).
+int host_copy_stream(cudaStream_t* cs, cudaEvent_t** ev) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return PSMMA_EDEVICE;
+  HostArena& a = g_host[dev];
+  if (!a.copy && cudaStreamCreateWithFlags(&a.copy, cudaStreamNonBlocking) != cudaSuccess) return PSMMA_EDEVICE;
+  if (!a.have_ev) {
+    for (int i = 0; i < kHostEvents; ++i)
+      if (cudaEventCreateWithFlags(&a.ev[i], cudaEventDisableTiming) != cudaSuccess) return PSMMA_EDEVICE;
+    a.have_ev = true;
+  }
+  *cs = a.copy;
+  *ev = a.ev;
+  return PSMMA_OK;
+}
+
+// Split-path workspace for a host-pointer call: the caller's opts->work or the pool of s.
+void* host_split_work(size_t need, const psmma_opts* o, cudaStream_t s, int* st) {
+  *st = PSMMA_OK;
+  if (o->work) {
+    if (o->lwork < need) { *st = PSMMA_EWORKSPACE; return nullptr; }
+    return o->work;
+  }
+  return pool_get(need, s, st);
+}
+
 int host_real(int kind, int n, int k, double alpha, const double* A, int lda, const double* gen,
               int ldgen, double beta, double* Q, int ldq, const psmma_opts* opts) {
   const psmma_opts* o = opts ? opts : &kDefaultOpts;
@@ -257,12 +287,33 @@ int host_real(int kind, int n, int k, double alpha, const double* A, int lda, co
   double* dG = (double*)(base + bA);
   double* dQ = (double*)(base + bA + bG);
   bool ok = true;
+  const bool overlapped = o->precision == PSMMA_PREC_SPLIT && alpha != 0.0;
   if (alpha != 0.0) {
-    ok &= cudaMemcpy2DAsync(dA, (size_t)n * 8, A, (size_t)lda * 8, (size_t)n * 8, k, cudaMemcpyHostToDevice, s) == cudaSuccess;
+    if (!overlapped)
+      ok &= cudaMemcpy2DAsync(dA, (size_t)n * 8, A, (size_t)lda * 8, (size_t)n * 8, k, cudaMemcpyHostToDevice, s) ==
+            cudaSuccess;
     if (kind == KIND_CAUCHY)
       ok &= cudaMemcpy2DAsync(dG, (size_t)k * 8, gen, (size_t)ldgen * 8, (size_t)k * 8, 4, cudaMemcpyHostToDevice, s) == cudaSuccess;
     else
       ok &= cudaMemcpyAsync(dG, gen, (size_t)glen * 8, cudaMemcpyHostToDevice, s) == cudaSuccess;
+  }
+  if (o->precision == PSMMA_PREC_SPLIT && alpha != 0.0) {
+    // generators are up (A and Q travel inside the overlapped pipeline)
+    if (!ok) return PSMMA_EDEVICE;
+    cudaStream_t cs;
+    cudaEvent_t* ev;
+    st = host_copy_stream(&cs, &ev);
+    if (st) return st;
+    const size_t need = split_workspace_bytes(kind, n, k, o->n_moduli);
+    void* work = host_split_work(need, o, s, &st);
+    if (st) return st;
+    st = launch_split_host(kind, n, k, alpha, A, lda, dA, dG, (kind == KIND_CAUCHY) ? k : (int)glen, beta, Q, ldq,
+                           dQ, o->n_moduli, work, o->work ? o->lwork : need, s, cs, ev, kHostEvents);
+    if (st) {
+      cudaStreamSynchronize(s);
+      cudaStreamSynchronize(cs);
+    }
+    return st;
   }
   if (beta != 0.0)
     ok &= cudaMemcpy2DAsync(dQ, (size_t)n * 8, Q, (size_t)ldq * 8, (size_t)n * 8, k, cudaMemcpyHostToDevice, s) == cudaSuccess;
@@ -352,12 +403,32 @@ int host_eig(int n, int k, double alpha, const double* A, int lda, const double*
   double* dG = (double*)(base + bA);  // F, U, V, DIFL, DIFR, k each
   double* dQ = (double*)(base + bA + bG);
   bool ok = true;
+  const bool overlapped = o->precision == PSMMA_PREC_SPLIT && alpha != 0.0;
   if (alpha != 0.0) {
-    ok &= cudaMemcpy2DAsync(dA, (size_t)n * 8, A, (size_t)lda * 8, (size_t)n * 8, k, cudaMemcpyHostToDevice, s) ==
-          cudaSuccess;
+    if (!overlapped)
+      ok &= cudaMemcpy2DAsync(dA, (size_t)n * 8, A, (size_t)lda * 8, (size_t)n * 8, k, cudaMemcpyHostToDevice, s) ==
+            cudaSuccess;
     const double* src[5] = {F, U, V, difl, difr};
     for (int t = 0; t < 5; ++t)
       if (src[t]) ok &= cudaMemcpyAsync(dG + (size_t)t * k, src[t], (size_t)k * 8, cudaMemcpyHostToDevice, s) == cudaSuccess;
+  }
+  if (overlapped) {
+    if (!ok) return PSMMA_EDEVICE;
+    cudaStream_t cs;
+    cudaEvent_t* ev;
+    st = host_copy_stream(&cs, &ev);
+    if (st) return st;
+    const size_t need = split_workspace_general(n, k, k, o->n_moduli);
+    void* work = host_split_work(need, o, s, &st);
+    if (st) return st;
+    const GenSpec gs = eig_gens(dG, dG + k, dG + 2 * (size_t)k, dG + 3 * (size_t)k, dG + 4 * (size_t)k, k);
+    st = launch_split_host_general(n, k, k, alpha, A, lda, dA, gs, beta, Q, ldq, dQ, o->n_moduli, work,
+                                   o->work ? o->lwork : need, s, cs, ev, kHostEvents);
+    if (st) {
+      cudaStreamSynchronize(s);
+      cudaStreamSynchronize(cs);
+    }
+    return st;
   }
   if (beta != 0.0)
     ok &= cudaMemcpy2DAsync(dQ, (size_t)n * 8, Q, (size_t)ldq * 8, (size_t)n * 8, k, cudaMemcpyHostToDevice, s) ==

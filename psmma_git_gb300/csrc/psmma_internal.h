@@ -108,6 +108,16 @@ int launch_split_any(int kind, int n, int k, double alpha, const double* A, long
 // General real product on the split path: Q (M x N) = alpha * A (M x K) * H (K x N) + beta * Q
 // with H given by gs (Cauchy, Toeplitz or Hankel).
 size_t split_workspace_general(int M, int N, int K, int n_moduli);
+// Host-pointer split multiply with the host<->device copies overlapped (split_crt.cu): A
+// and Q on the host, dA / dQ device buffers (leading dimension M), the copies on stream cs,
+// nev >= 11 events.
+int launch_split_host(int kind, int n, int k, double alpha, const double* A_h, long lda_h, double* dA,
+                      const double* dgen, long ldgen, double beta, double* Q_h, long ldq_h, double* dQ,
+                      int n_moduli, void* work, size_t lwork, cudaStream_t s, cudaStream_t cs, cudaEvent_t* ev,
+                      int nev);
+int launch_split_host_general(int M, int N, int K, double alpha, const double* A_h, long lda_h, double* dA,
+                              const GenSpec& gs, double beta, double* Q_h, long ldq_h, double* dQ, int n_moduli,
+                              void* work, size_t lwork, cudaStream_t s, cudaStream_t cs, cudaEvent_t* ev, int nev);
 int launch_split_general(int M, int N, int K, double alpha, const double* A, long lda, const GenSpec& gs,
                          double beta, double* Q, long ldq, int n_moduli, void* work, size_t lwork,
                          cudaStream_t stream, unsigned* status_dev_out);

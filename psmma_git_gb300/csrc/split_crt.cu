@@ -719,6 +719,7 @@ constexpr uint32_t G_A_BYTES = G_BM * G_BK * 2;
 
 struct GemmArgs {
   int n, kr, nkb, tiles_m, tiles_n, group_m, nmod;  // (a grouped launch uses group_m, nmod)
+  int tm0;  // one product: first row tile of this launch (row panels)
   int8_t* R;
   unsigned* status;
   int m[SPL_MAX_MODULI];
@@ -757,6 +758,7 @@ struct OneGemm {
   __device__ TileInfo tile(int t) const {
     TileInfo ti;
     raster_tile(g.tiles_m, g.tiles_n, g.group_m, t, ti.l, ti.tm, ti.tn);
+    ti.tm += g.tm0;
     ti.ta = &ta;
     ti.tb = &tb;
     ti.R = g.R;
@@ -1173,8 +1175,9 @@ __global__ void __launch_bounds__(256, 3) k_crt_combine(const int8_t* __restrict
                                                      CrtConsts cc, const unsigned long long* __restrict__ amax_bits,
                                                      const unsigned long long* __restrict__ hmax_bits,
                                                      const SplitDevParams* prm, double alpha, double beta,
-                                                     double* __restrict__ Q, long ldq) {
-  crt_combine_blk<DFT_OUT>(R, n, k, kr, cc, amax_bits, hmax_bits, prm, alpha, beta, Q, ldq, blockIdx.x, blockIdx.y);
+                                                     double* __restrict__ Q, long ldq, int by0) {
+  crt_combine_blk<DFT_OUT>(R, n, k, kr, cc, amax_bits, hmax_bits, prm, alpha, beta, Q, ldq, blockIdx.x,
+                           by0 + blockIdx.y);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -1339,10 +1342,11 @@ static int split_core(int M, int N, int K, double alpha, const double* A, long l
 
   dim3 gc((N + CRT_TJ - 1) / CRT_TJ, (M + CRT_TI - 1) / CRT_TI);
   if (!dft)
-    k_crt_combine<false><<<gc, dim3(32, 8), 0, stream>>>(b.R, M, N, L.kr, cc, b.amax, b.hmax, b.prm, alpha, beta, Q, ldq);
+    k_crt_combine<false><<<gc, dim3(32, 8), 0, stream>>>(b.R, M, N, L.kr, cc, b.amax, b.hmax, b.prm, alpha, beta, Q, ldq,
+                                                         0);
   else
     k_crt_combine<true><<<gc, dim3(32, 8), 0, stream>>>(b.R, M, N, L.kr, cc, b.amax, b.hmax, b.prm, alpha, beta, Q,
-                                                        2 * ldq);
+                                                        2 * ldq, 0);
   prof_mark(stream, "crt_combine");
   if (cudaGetLastError() != cudaSuccess) return PSMMA_EDEVICE;
 
@@ -1358,6 +1362,133 @@ static int split_core(int M, int N, int K, double alpha, const double* A, long l
     return PSMMA_EDEVICE;
   if (st & DEV_ERR_TIMEOUT) return PSMMA_ETIMEDOUT;
   return PSMMA_OK;
+}
+
+// Host-pointer multiply with the copies overlapped (pinned host memory makes them
+// asynchronous).  A (host, column-major, lda_h) goes up in column chunks on the copy stream
+// `cs` while H is generated on `s`; each chunk's row maxima / norms start as soon as it has
+// landed.  After the parameter and residue passes the modular GEMM and the CRT run in row
+// panels of whole 128-row tiles, and each finished panel of Q goes back to the host on `cs`
+// while the next panel multiplies.  dA (M x K) and dQ (M x N) are device buffers with leading
+// dimension M; Q is read from the host first when beta != 0.  Synchronises both streams.
+static int split_core_host(int M, int N, int K, double alpha, const double* A_h, long lda_h, double* dA,
+                           const GenSpec& gs, double beta, double* Q_h, long ldq_h, double* dQ, int nmod, void* work,
+                           size_t lwork, cudaStream_t s, cudaStream_t cs, cudaEvent_t* ev, int nev) {
+  if (gs.kind == KIND_DFT) return PSMMA_EUNSUPPORTED;
+  if (nmod < 8 || nmod > SPL_MAX_MODULI) return PSMMA_EUNSUPPORTED;
+  if (K >= (1 << 24) || M >= (1 << 30) || N >= (1 << 30)) return PSMMA_EUNSUPPORTED;
+  constexpr int NCH = 4, NP = 4;
+  if (nev < NCH + NP + 3) return PSMMA_EUNSUPPORTED;
+  SplitLayout L = split_layout(M, K, N, nmod);
+  if (lwork < L.total || !work) return PSMMA_EWORKSPACE;
+  char* w = (char*)work;
+  const SplitBuffers b = split_buffers(w, L);
+  const CrtConsts cc = get_consts(nmod);
+  cudaEvent_t* ev_chunk = ev;            // NCH
+  cudaEvent_t* ev_panel = ev + NCH;      // NP
+  cudaEvent_t ev_start = ev[NCH + NP], ev_q = ev[NCH + NP + 1], ev_done = ev[NCH + NP + 2];
+  bool ok = true;
+  // the copy stream starts after everything already queued on s
+  ok &= cudaEventRecord(ev_start, s) == cudaSuccess;
+  ok &= cudaStreamWaitEvent(cs, ev_start, 0) == cudaSuccess;
+  ok &= cudaMemsetAsync(w, 0, L.off_wtab, s) == cudaSuccess;
+  // ---- H side (needs no A)
+  switch (gs.kind) {
+    case KIND_CAUCHY: k_h_pass1<KIND_CAUCHY><<<N, 256, 0, s>>>(gs, K, L.kp, b.Ht, b.hmax, b.hsum, b.hsq, b.prm); break;
+    case KIND_TOEPLITZ: k_h_pass1<KIND_TOEPLITZ><<<N, 256, 0, s>>>(gs, K, L.kp, b.Ht, b.hmax, b.hsum, b.hsq, b.prm); break;
+    case KIND_HANKEL: k_h_pass1<KIND_HANKEL><<<N, 256, 0, s>>>(gs, K, L.kp, b.Ht, b.hmax, b.hsum, b.hsq, b.prm); break;
+    case KIND_CAUCHY_EIG: k_h_pass1<KIND_CAUCHY_EIG><<<N, 256, 0, s>>>(gs, K, L.kp, b.Ht, b.hmax, b.hsum, b.hsq, b.prm); break;
+    default: return PSMMA_EUNSUPPORTED;
+  }
+  // ---- A in column chunks (multiples of the 1024-column row-norm chunk)
+  const int kchunk = 1024;
+  const int cols_per = std::max(kchunk, (K + NCH * kchunk - 1) / (NCH * kchunk) * kchunk);
+  for (int ch = 0; ch < NCH; ++ch) {
+    const int c0 = ch * cols_per, c1 = std::min(K, c0 + cols_per);
+    if (c0 >= c1) break;
+    ok &= cudaMemcpy2DAsync(dA + (size_t)c0 * M, (size_t)M * 8, A_h + (size_t)c0 * lda_h, (size_t)lda_h * 8,
+                            (size_t)M * 8, (size_t)(c1 - c0), cudaMemcpyHostToDevice, cs) == cudaSuccess;
+    ok &= cudaEventRecord(ev_chunk[ch], cs) == cudaSuccess;
+    ok &= cudaStreamWaitEvent(s, ev_chunk[ch], 0) == cudaSuccess;
+    dim3 g1((M + 127) / 128, (c1 - c0 + kchunk - 1) / kchunk);
+    k_row_absmax<<<g1, 128, 0, s>>>(dA + (size_t)c0 * M, M, M, c1 - c0, kchunk, b.amax, b.asq);
+  }
+  if (beta != 0.0) {
+    ok &= cudaMemcpy2DAsync(dQ, (size_t)M * 8, Q_h, (size_t)ldq_h * 8, (size_t)M * 8, (size_t)N,
+                            cudaMemcpyHostToDevice, cs) == cudaSuccess;
+    ok &= cudaEventRecord(ev_q, cs) == cudaSuccess;
+  }
+  if (!ok) return PSMMA_EDEVICE;
+  k_split_params<<<PARAMS_BLOCKS, 512, 0, s>>>(b.prm, cc.log2M, M, N, K, b.amax, b.asq, b.hmax, b.hsq);
+  k_residues_A<<<dim3(L.kp / 64, (M + 31) / 32), 256, 0, s>>>(dA, M, M, K, L.kp, b.amax, b.prm, cc, b.RA);
+  k_residues_H<<<dim3((L.kp / 2 + 127) / 128, N), 128, 0, s>>>(b.Ht, N, L.kp, b.hmax, b.prm, cc, b.RH);
+
+  OneGemm og;
+  memset(&og, 0, sizeof(og));
+  if (!make_tmap(&og.ta, b.RA, L.kp, M, nmod, G_BM) || !make_tmap(&og.tb, b.RH, L.kp, N, nmod, G_BN))
+    return PSMMA_EDEVICE;
+  GemmArgs& ga = og.g;
+  ga.n = M;
+  ga.kr = L.kr;
+  ga.nkb = L.kp / G_BK;
+  ga.tiles_n = (N + G_BN - 1) / G_BN;
+  ga.group_m = 12;
+  ga.R = b.R;
+  ga.status = &b.prm->status;
+  ga.nmod = nmod;
+  for (int l = 0; l < nmod; ++l) { ga.m[l] = cc.m[l]; ga.inv_m[l] = cc.inv_m[l]; }
+  using Shape = GemmShape<G_BN>;
+  if (cudaFuncSetAttribute(k_crt_gemm<G_BN, OneGemm>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)Shape::SMEM) != cudaSuccess)
+    return PSMMA_EDEVICE;
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return PSMMA_EDEVICE;
+  const int tiles_m = (M + G_BM - 1) / G_BM;
+  const int tiles_per = (tiles_m + NP - 1) / NP;
+  static_assert(G_BM % CRT_TI == 0, "row panels must cover whole CRT blocks");
+  if (beta != 0.0 && cudaStreamWaitEvent(s, ev_q, 0) != cudaSuccess) return PSMMA_EDEVICE;
+  for (int p = 0; p < NP; ++p) {
+    const int t0 = p * tiles_per, t1 = std::min(tiles_m, t0 + tiles_per);
+    if (t0 >= t1) break;
+    ga.tm0 = t0;
+    ga.tiles_m = t1 - t0;
+    const int total_tiles = ga.tiles_m * ga.tiles_n * nmod;
+    k_crt_gemm<G_BN, OneGemm><<<std::min(sms, total_tiles), G_THREADS, Shape::SMEM, s>>>(og);
+    const int r0 = t0 * G_BM, r1 = std::min(M, t1 * G_BM);
+    dim3 gc((N + CRT_TJ - 1) / CRT_TJ, (r1 - r0 + CRT_TI - 1) / CRT_TI);
+    k_crt_combine<false><<<gc, dim3(32, 8), 0, s>>>(b.R, M, N, L.kr, cc, b.amax, b.hmax, b.prm, alpha, beta, dQ, M,
+                                                     r0 / CRT_TI);
+    ok &= cudaEventRecord(ev_panel[p], s) == cudaSuccess;
+    ok &= cudaStreamWaitEvent(cs, ev_panel[p], 0) == cudaSuccess;
+    ok &= cudaMemcpy2DAsync(Q_h + r0, (size_t)ldq_h * 8, dQ + r0, (size_t)M * 8, (size_t)(r1 - r0) * 8, (size_t)N,
+                            cudaMemcpyDeviceToHost, cs) == cudaSuccess;
+  }
+  if (cudaGetLastError() != cudaSuccess) ok = false;
+  unsigned st = 0;
+  ok &= cudaMemcpyAsync(&st, &b.prm->status, sizeof(st), cudaMemcpyDeviceToHost, s) == cudaSuccess;
+  ok &= cudaEventRecord(ev_done, cs) == cudaSuccess;
+  ok &= cudaStreamSynchronize(s) == cudaSuccess;
+  ok &= cudaEventSynchronize(ev_done) == cudaSuccess;
+  if (!ok) return PSMMA_EDEVICE;
+  if (st & DEV_ERR_TIMEOUT) return PSMMA_ETIMEDOUT;
+  return PSMMA_OK;
+}
+
+int launch_split_host(int kind, int n, int k, double alpha, const double* A_h, long lda_h, double* dA,
+                      const double* dgen, long ldgen, double beta, double* Q_h, long ldq_h, double* dQ,
+                      int n_moduli, void* work, size_t lwork, cudaStream_t s, cudaStream_t cs, cudaEvent_t* ev,
+                      int nev) {
+  const GenSpec gs = reference_gens(kind, dgen, ldgen, k);
+  return split_core_host(n, k, k, alpha, A_h, lda_h, dA, gs, beta, Q_h, ldq_h, dQ, resolve_nmod(n_moduli), work,
+                         lwork, s, cs, ev, nev);
+}
+
+int launch_split_host_general(int M, int N, int K, double alpha, const double* A_h, long lda_h, double* dA,
+                              const GenSpec& gs, double beta, double* Q_h, long ldq_h, double* dQ, int n_moduli,
+                              void* work, size_t lwork, cudaStream_t s, cudaStream_t cs, cudaEvent_t* ev, int nev) {
+  return split_core_host(M, N, K, alpha, A_h, lda_h, dA, gs, beta, Q_h, ldq_h, dQ, resolve_nmod(n_moduli), work,
+                         lwork, s, cs, ev, nev);
 }
 
 // kind != DFT: Q (n x k) = alpha * A (n x k) * H (k x k) + beta * Q.

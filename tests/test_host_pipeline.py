@@ -1,0 +1,79 @@
+"""Host-pointer split multiply with the copies overlapped (psmma_*_host with precision split):
+A goes up in column chunks while H is generated, the GEMM and the CRT run in row panels and
+each panel of Q comes back while the next multiplies.  Results are compared with the device
+path and the exact product on ragged sizes (partial chunks and panels, one panel, padded
+leading dimensions, beta != 0), on pageable and pinned host memory."""
+import numpy as np
+import pytest
+
+from oracle import psmma_oracle as O
+
+
+def _gen(kind, k, seed):
+    return O.cfg_cauchy_generators(k, seed=seed) if kind == "cauchy" else O.cfg_vector(2 * k - 1, seed=seed)
+
+
+def _fortran_view(x, pad):
+    """x as a column-major view with leading dimension rows + pad."""
+    n, k = x.shape
+    base = np.zeros((n + pad, k), order="F")
+    base[:n] = x
+    return base[:n]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", ["cauchy", "toeplitz", "hankel"])
+@pytest.mark.parametrize("n,k,beta,pad", [(1000, 2500, 0.0, 0), (1000, 2500, -0.75, 5), (100, 700, 0.5, 0),
+                                          (513, 129, 0.0, 3)])
+def test_host_split_matches_device_and_exact(kind, n, k, beta, pad):
+    import torch
+    import psmma_git_gb300 as P
+    A = O.cfg_matrix(n, k, seed=1)
+    gen = np.asfortranarray(_gen(kind, k, 2))
+    Q0 = O.cfg_matrix(n, k, seed=3)
+    exact = O.dense_product(kind, 0.5, A, gen, beta, Q0, k)
+    Ah = _fortran_view(A, pad)
+    Qh = _fortran_view(Q0, pad)
+    getattr(P, "psmma_" + kind)(n, k, 0.5, Ah, gen, beta, Qh, precision="split")
+    assert O.rel_fro(Qh, exact) < 1e-12
+    # the device path on the same inputs
+    dev = torch.device("cuda")
+    col = lambda x: torch.from_numpy(np.ascontiguousarray(np.asarray(x).T)).to(dev).t()  # noqa: E731
+    dg = col(gen) if kind == "cauchy" else torch.from_numpy(gen).to(dev)
+    dQ = P.fortran_empty(n, k, torch.float64, dev)
+    dQ.copy_(torch.from_numpy(Q0))
+    getattr(P, "psmma_" + kind)(n, k, 0.5, col(A), dg, beta, dQ, precision="split")
+    torch.cuda.synchronize()
+    assert O.rel_fro(Qh, dQ.cpu().numpy()) < 1e-13
+
+
+@pytest.mark.gpu
+def test_host_split_pinned_memory_and_repeat():
+    import torch
+    import psmma_git_gb300 as P
+    n, k = 2048, 3000
+    A = O.cfg_matrix(n, k, seed=4)
+    gen = np.asfortranarray(O.cfg_cauchy_generators(k, seed=5))
+    exact = O.dense_product("cauchy", 1.0, A, gen, 0.0, None, k)
+    Ap = torch.empty((k, n), dtype=torch.float64, pin_memory=True)
+    Qp = torch.empty((k, n), dtype=torch.float64, pin_memory=True)
+    Ah = Ap.numpy().T
+    Qh = Qp.numpy().T
+    Ah[:] = A
+    for _ in range(3):  # the arena, streams and events are reused across calls
+        Qh[:] = np.nan
+        P.psmma_cauchy(n, k, 1.0, Ah, gen, 0.0, Qh, precision="split")
+        assert O.rel_fro(Qh, exact) < 1e-12
+
+
+@pytest.mark.gpu
+def test_host_split_cauchyeig():
+    import psmma_git_gb300 as P
+    k, n = 1500, 700
+    F, U, V, dl, dr = O.eig_generators(k, seed=6, tiny=3)
+    A = O.cfg_matrix(n, k, seed=7)
+    Q0 = O.cfg_matrix(n, k, seed=8)
+    ref = 2.0 * (A @ O.cauchy_like_eig(F, U, V, dl, dr)) + 0.25 * Q0
+    Qh = np.asfortranarray(Q0.copy())
+    P.psmma_cauchyeig(n, k, 2.0, A, F, U, V, dl, dr, 0.25, Qh, precision="split")
+    assert O.rel_fro(Qh, ref) < 1e-12
