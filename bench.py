@@ -543,6 +543,88 @@ def run_cfg1(args, ws, rank, local):
     return 0
 
 
+def run_cfg0(args, ws, rank, local):
+    """Cauchy multiply on the FP64 plain path at n = k = 2048 over seeds 0..4 (A ~ U[-1,1],
+    d = sort(U(0,1)), w_j ~ U(d_j, d_j+1), u, v ~ N(0,1)): median of args.steps timed calls per
+    seed (CUDA events, after args.warmup), error against the oracle's FP64 A@H, the split path
+    beside it, and the FP64 roofline against cuBLAS DGEMM measured in the same run.  CPU
+    baseline: the restatement of PSCAUCHY_COMPUTE on a 2 x 2 grid, block 64 (4 emulated ranks),
+    and a dense A@H, on all host cores.  One JSON line."""
+    import numpy as np
+    import torch
+    import psmma_git_gb300 as P
+    from oracle import psmma_oracle as O
+    if rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    n = 2048
+    flops = 2.0 * n ** 3
+    stream = torch.cuda.current_stream()
+    col = lambda x: torch.from_numpy(np.ascontiguousarray(np.asarray(x).T)).to(dev).t()  # noqa: E731
+    per_seed = []
+    for seed in range(5):
+        A = O.cfg_matrix(n, n, seed=seed)
+        gen = O.cfg_cauchy_generators(n, seed=seed)
+        dA, dg = col(A), col(gen)
+        out = {}
+        for prec in ["fp64", "split"]:
+            dQ = P.fortran_empty(n, n, torch.float64, dev)
+            for _ in range(args.warmup):
+                P.psmma_cauchy(n, n, 1.0, dA, dg, 0.0, dQ, precision=prec, n_moduli=args.n_moduli, stream=stream)
+            torch.cuda.synchronize()
+            ts = []
+            for _ in range(max(10, args.steps)):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                P.psmma_cauchy(n, n, 1.0, dA, dg, 0.0, dQ, precision=prec, n_moduli=args.n_moduli, stream=stream)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                ts.append(e0.elapsed_time(e1))
+            ref = O.dense_product("cauchy", 1.0, A, gen, 0.0, None, n)
+            out[prec] = {"ms": float(np.median(ts)), "tflops": flops / (np.median(ts) * 1e-3) / 1e12,
+                         "rel_err_vs_oracle": O.rel_fro(dQ.t().contiguous().cpu().numpy().T, ref)}
+        per_seed.append(out)
+    a = torch.randn(8192, 8192, device=dev, dtype=torch.float64)
+    torch.matmul(a, a)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    torch.matmul(a, a)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    dgemm = 2 * 8192 ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12
+    del a
+    # CPU baseline: the reference's ring on a 2 x 2 grid and a dense A@H (seed 0)
+    A = O.cfg_matrix(n, n, seed=0)
+    gen = O.cfg_cauchy_generators(n, seed=0)
+    t0 = time.perf_counter()
+    Qr = O.ps_compute("cauchy", n, n, 1.0, A, gen, 0.0, np.zeros((n, n)), nprow=2, npcol=2, nb=64)
+    t_ring = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    O.dense_product("cauchy", 1.0, A, gen, 0.0, None, n)
+    t_dense = time.perf_counter() - t0
+    fp64 = [s_["fp64"]["tflops"] for s_ in per_seed]
+    v = float(np.median(fp64))
+    line = {"metric": "Cauchy A·H TFLOP/s n=2048, FP64 plain path (cfg0)", "value": v, "unit": "TFLOP/s",
+            "n_gpus": 1, "steps": max(10, args.steps), "warmup": args.warmup,
+            "ms_per_step": float(np.median([s_["fp64"]["ms"] for s_ in per_seed])), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "psmma_cauchy FP64 n=k=2048, seeds 0..4 (median over seeds of the median "
+                                   "over steps)", "n": n, "l2": "inputs 32 MiB < L2: no flush (small case)"},
+            "seeds": per_seed,
+            "roofline": {"bound": "tensor", "achieved": v, "peak": dgemm, "unit": "TFLOP/s", "frac": v / dgemm,
+                         "traffic": None, "kernel": "k_struct_f64<KIND_CAUCHY>",
+                         "peak_source": "cuBLAS DGEMM 8192^3 measured in this run"},
+            "cpu_baseline": {"value": flops / t_ring / 1e12, "unit": "TFLOP/s", "cores": os.cpu_count(),
+                             "kind": "port", "sample": f"whole product, ring restatement 2x2 grid nb=64: "
+                                                       f"{t_ring:.2f} s; dense A@H: {t_dense:.2f} s"},
+            "ring_vs_dense_rel": O.rel_fro(Qr, O.dense_product("cauchy", 1.0, A, gen, 0.0, None, n)),
+            "gpu_launches": 2 * 5 * (max(10, args.steps) + args.warmup)}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_redist(args, ws, rank, local):
     """The REDIST copy (PDGEMR2D) of an n x n matrix from the reference tests' layout (2 x 2
     grid, 64 x 64 blocks, Test/psmma_testcauchy.f90:80) to row panels over the 4 ranks, with the
@@ -797,6 +879,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-tune", action="store_true", help="merge level: skip the grouped-GEMM autotuner")
     ap.add_argument("--redist", action="store_true", help="time the block-cyclic redistribution kernels")
+    ap.add_argument("--cfg0", action="store_true", help="run the FP64 Cauchy multiply at n = 2048 over 5 seeds")
     ap.add_argument("--redist-n", type=int, default=16384)
     args = ap.parse_args()
     ws, rank, local = dist_init(args)
@@ -814,6 +897,8 @@ def main():
         return run_cfg1(args, ws, rank, local)
     if args.redist:
         return run_redist(args, ws, rank, local)
+    if args.cfg0:
+        return run_cfg0(args, ws, rank, local)
     return run_gpu(args, ws, rank, local)
 
 

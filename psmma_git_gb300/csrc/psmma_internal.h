@@ -110,7 +110,7 @@ int launch_split_any(int kind, int n, int k, double alpha, const double* A, long
 size_t split_workspace_general(int M, int N, int K, int n_moduli);
 // Host-pointer split multiply with the host<->device copies overlapped (split_crt.cu): A
 // and Q on the host, dA / dQ device buffers (leading dimension M), the copies on stream cs,
-// nev >= 11 events.
+// nev >= 15 events.
 int launch_split_host(int kind, int n, int k, double alpha, const double* A_h, long lda_h, double* dA,
                       const double* dgen, long ldgen, double beta, double* Q_h, long ldq_h, double* dQ,
                       int n_moduli, void* work, size_t lwork, cudaStream_t s, cudaStream_t cs, cudaEvent_t* ev,

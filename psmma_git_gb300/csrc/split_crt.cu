@@ -1377,7 +1377,7 @@ static int split_core_host(int M, int N, int K, double alpha, const double* A_h,
   if (gs.kind == KIND_DFT) return PSMMA_EUNSUPPORTED;
   if (nmod < 8 || nmod > SPL_MAX_MODULI) return PSMMA_EUNSUPPORTED;
   if (K >= (1 << 24) || M >= (1 << 30) || N >= (1 << 30)) return PSMMA_EUNSUPPORTED;
-  constexpr int NCH = 4, NP = 4;
+  constexpr int NCH = 4, NP = 8;  // A column chunks, GEMM / CRT / download row panels
   if (nev < NCH + NP + 3) return PSMMA_EUNSUPPORTED;
   SplitLayout L = split_layout(M, K, N, nmod);
   if (lwork < L.total || !work) return PSMMA_EWORKSPACE;
