@@ -124,6 +124,8 @@ SIGNATURES = {
     "psmma_version": (C.c_char_p, []),
     "psmma_selftest_wait_timeout": (_i, [C.c_ulonglong]),
     "psmma_selftest_division": (_i, [C.c_longlong, C.c_ulonglong, C.POINTER(C.c_ulonglong), C.POINTER(C.c_int)]),
+    "psmma_selftest_division_split": (_i, [C.c_longlong, C.c_ulonglong, C.POINTER(C.c_ulonglong),
+                                           C.POINTER(C.c_int)]),
     "psmma_server_create": (_i, [C.c_size_t, _i, C.POINTER(C.c_void_p)]),
     "psmma_server_submit": (_i, [_p, C.POINTER(PsmmaRequest), C.POINTER(C.c_ulonglong)]),
     "psmma_server_wait": (_i, [_p, C.c_ulonglong, C.c_double, C.POINTER(PsmmaCompletion)]),

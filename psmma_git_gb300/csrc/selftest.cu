@@ -42,7 +42,8 @@ extern "C" int psmma_selftest_wait_timeout(unsigned long long limit_ns) {
 }
 
 // ------------------------------------------------------------------------------------------
-// Self-check of div_nr (the split path's Cauchy entries) against the IEEE division on
+// Self-check of div_nr (FP64-exact quotients) and div_split (the split path's Cauchy entries)
+// against the IEEE division on
 // count seeded pairs: Cauchy-like operands u*v / (d - w) with |d - w| log-uniform in
 // [1e-13, 1], plus arbitrary finite bit patterns (which exercise the fallback).
 // ------------------------------------------------------------------------------------------
@@ -57,6 +58,7 @@ __device__ __forceinline__ unsigned long long splitmix(unsigned long long& s) {
 
 __device__ __forceinline__ double unit(unsigned long long r) { return (double)(r >> 11) * 0x1.0p-53; }
 
+template <bool SPLIT>
 __global__ void k_selftest_div(long long count, unsigned long long seed, unsigned long long* mism, int* max_ulp) {
   unsigned long long local = 0;
   int worst = 0;
@@ -79,7 +81,7 @@ __global__ void k_selftest_div(long long count, unsigned long long seed, unsigne
       x = __longlong_as_double((long long)bx);
     }
     if (x == 0.0) continue;
-    const double q0 = a / x, q1 = div_nr(a, x);
+    const double q0 = a / x, q1 = SPLIT ? div_split(a, x) : div_nr(a, x);
     if (__double_as_longlong(q0) != __double_as_longlong(q1)) {
       ++local;
       const long long d = __double_as_longlong(q0) - __double_as_longlong(q1);
@@ -93,15 +95,18 @@ __global__ void k_selftest_div(long long count, unsigned long long seed, unsigne
 
 }  // namespace psmma
 
-extern "C" int psmma_selftest_division(long long count, unsigned long long seed, unsigned long long* mismatches,
-                                       int* max_ulp) {
+static int selftest_division(bool split, long long count, unsigned long long seed, unsigned long long* mismatches,
+                             int* max_ulp) {
   if (count <= 0 || !mismatches || !max_ulp) return PSMMA_EUNSUPPORTED;
   unsigned long long* dm = nullptr;
   if (cudaMalloc(&dm, 16) != cudaSuccess) return PSMMA_ENOMEM;
   int st = PSMMA_OK;
   if (cudaMemset(dm, 0, 16) != cudaSuccess) st = PSMMA_EDEVICE;
   if (!st) {
-    k_selftest_div<<<1216, 256>>>(count, seed, dm, (int*)(dm + 1));
+    if (split)
+      k_selftest_div<true><<<1216, 256>>>(count, seed, dm, (int*)(dm + 1));
+    else
+      k_selftest_div<false><<<1216, 256>>>(count, seed, dm, (int*)(dm + 1));
     unsigned long long h[2] = {0, 0};
     if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess ||
         cudaMemcpy(h, dm, 16, cudaMemcpyDeviceToHost) != cudaSuccess)
@@ -111,4 +116,14 @@ extern "C" int psmma_selftest_division(long long count, unsigned long long seed,
   }
   cudaFree(dm);
   return st;
+}
+
+extern "C" int psmma_selftest_division(long long count, unsigned long long seed, unsigned long long* mismatches,
+                                       int* max_ulp) {
+  return selftest_division(false, count, seed, mismatches, max_ulp);
+}
+
+extern "C" int psmma_selftest_division_split(long long count, unsigned long long seed,
+                                             unsigned long long* mismatches, int* max_ulp) {
+  return selftest_division(true, count, seed, mismatches, max_ulp);
 }

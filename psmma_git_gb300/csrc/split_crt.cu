@@ -304,22 +304,22 @@ __device__ __forceinline__ void h_pass1_blk(const GenSpec& gs, int K, int kp, do
       if (KIND == KIND_CAUCHY) {
         if (gs.k1 > 0 && kk >= gs.k1) {
           const int t = kk - gs.k1;  // tail rows: dense, or Cauchy with the second row generators
-          h = gs.B ? __ldg(gs.B + t + (long)j * gs.ldb) : div_nr(__ldg(gs.Ur2 + t) * v, __ldg(gs.Dr2 + t) - w);
+          h = gs.B ? __ldg(gs.B + t + (long)j * gs.ldb) : div_split(__ldg(gs.Ur2 + t) * v, __ldg(gs.Dr2 + t) - w);
         } else {
           double d = __ldg(gs.Dr + kk), u = __ldg(gs.Ur + kk);
-          h = div_nr(u * v, d - w);     // U(i)*V(j) / (D(i)-F(j))
+          h = div_split(u * v, d - w);     // U(i)*V(j) / (D(i)-F(j))
         }
       } else if (KIND == KIND_CAUCHY_EIG) {
         if (gs.k1 > 0 && kk >= gs.k1) {
           // tail rows of merged products: dense, or CauchyEig rows in permuted order
           const int t = kk - gs.k1;
           h = gs.B ? __ldg(gs.B + t + (long)j * gs.ldb)
-                   : div_nr(__ldg(gs.Ur2 + t) * v,
+                   : div_split(__ldg(gs.Ur2 + t) * v,
                             eig_den(__ldg(gs.Dr2 + t), w, w1, dlj, drj, __ldg(gs.rglob2 + t) - 1 <= gs.cg0 + j));
         } else {
           const double fi = __ldg(gs.Dr + kk), u = __ldg(gs.Ur + kk);
           const bool upper = gs.rglob ? (__ldg(gs.rglob + kk) - 1 <= gs.cg0 + j) : (kk - j <= gs.diag_off);
-          h = div_nr(u * v, eig_den(fi, w, w1, dlj, drj, upper));
+          h = div_split(u * v, eig_den(fi, w, w1, dlj, drj, upper));
         }
       } else if (KIND == KIND_TOEPLITZ) {
         h = __ldg(gs.g + (gs.order - 1) + j - kk);

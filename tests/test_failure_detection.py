@@ -40,3 +40,12 @@ def test_fast_division_matches_ieee_within_one_ulp(lib, cuda):
     # correctly rounded in all but rare ties; never more than one ulp away
     assert ulp.value <= 1
     assert mism.value < (1 << 26) // 10000
+
+
+@pytest.mark.gpu
+def test_split_path_division_error_bound(lib, cuda):
+    import ctypes as C
+    mism, ulp = C.c_ulonglong(0), C.c_int(0)
+    assert lib.psmma_selftest_division_split(1 << 26, 777, C.byref(mism), C.byref(ulp)) == 0
+    # FP32 reciprocal seed, one FP64 Newton step, no residual correction: within 2^-44 relative
+    assert ulp.value <= 256
