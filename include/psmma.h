@@ -381,8 +381,10 @@ int psmma_server_destroy(psmma_server* s);
 
 /* ---- workspace and housekeeping ----------------------------------------------------- */
 
-/* Bytes of device workspace a call with these sizes and options needs (0 for the FP64
- * path).  Pass a buffer at least this large in opts->work to avoid library allocation. */
+/* Bytes of device workspace a call with these sizes and options needs.  The FP64 path needs
+ * none, except for products with too few 128 x 128 output tiles to fill the SMs, which it
+ * splits along K into partial sums when workspace is available (0 otherwise).  Pass a buffer
+ * at least this large in opts->work to avoid library allocation. */
 size_t psmma_workspace_size(int kind, int n, int k, const psmma_opts* opts);
 
 /* Frees the library-owned workspace pools of the current device. */

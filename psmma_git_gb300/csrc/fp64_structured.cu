@@ -45,6 +45,11 @@ struct F64Args {
   const double* X; long ldx;  // streamed operand (A for real kinds, B' for DFT)
   double* C; long ldc;        // output (Q or C')
   GenSpec gs;                       // generators of the structured operand
+  // split K (single products that fill too few waves): block z of the launch covers
+  // k in [z*kc, (z+1)*kc) and writes alpha * its partial sum to W + z * ldw * N (ld ldw)
+  int kc = 0;
+  double* W = nullptr;
+  long ldw = 0;
 };
 
 __device__ __forceinline__ void cp_async8(void* smem, const void* gmem, bool pred) {
@@ -190,7 +195,7 @@ __device__ __forceinline__ void gen_F_tile(double* As, const F64Args& p, int m0,
 
 // One 128 x 128 output tile (bx, by) of the product described by p.
 template <int KIND>
-__device__ __forceinline__ void struct_f64_tile(const F64Args& p, int bx, int by) {
+__device__ __forceinline__ void struct_f64_tile(const F64Args& p, int bx, int by, int bz = 0) {
   extern __shared__ __align__(16) double smem[];
   double* As0 = smem;
   double* Bs0 = smem + F64_SMEM_A;
@@ -225,7 +230,9 @@ __device__ __forceinline__ void struct_f64_tile(const F64Args& p, int bx, int by
 #pragma unroll
       for (int r = 0; r < 4; r++) acc[i][j][r] = 0.0;
 
-  const int nk = (p.K + F64_BK - 1) / F64_BK;
+  // k-steps of this block (all of K, or split z's share of kc)
+  const int kt0 = p.W ? bz * (p.kc / F64_BK) : 0;
+  const int nk = p.W ? min((p.K + F64_BK - 1) / F64_BK, (bz + 1) * (p.kc / F64_BK)) : (p.K + F64_BK - 1) / F64_BK;
   auto stage = [&](int kt, double* As, double* Bs) {
     int k0 = kt * F64_BK;
     if (KIND == KIND_DFT) {
@@ -243,13 +250,16 @@ __device__ __forceinline__ void struct_f64_tile(const F64Args& p, int bx, int by
     }
   };
 
-  stage(0, As0, Bs0);
-  cp_async_wait_all();
-  __syncthreads();
-  for (int kt = 0; kt < nk; kt++) {
-    double* As = (kt & 1) ? As1 : As0;
-    double* Bs = (kt & 1) ? Bs1 : Bs0;
-    if (kt + 1 < nk) stage(kt + 1, (kt & 1) ? As0 : As1, (kt & 1) ? Bs0 : Bs1);
+  if (kt0 < nk) {
+    stage(kt0, As0, Bs0);
+    cp_async_wait_all();
+    __syncthreads();
+  }
+  for (int kt = kt0; kt < nk; kt++) {
+    const int ph = (kt - kt0) & 1;
+    double* As = ph ? As1 : As0;
+    double* Bs = ph ? Bs1 : Bs0;
+    if (kt + 1 < nk) stage(kt + 1, ph ? As0 : As1, ph ? Bs0 : Bs1);
     warp_mma_step(acc, As, Bs, wm0, wn0, lane);
     cp_async_wait_all();
     __syncthreads();
@@ -266,17 +276,35 @@ __device__ __forceinline__ void struct_f64_tile(const F64Args& p, int bx, int by
         int gi = m0 + wm0 + mt * 16 + g + 8 * (r >> 1);
         int gj = n0 + wn0 + nt * 8 + 2 * t + (r & 1);
         if (gi < p.M && gj < p.N) {
-          double* cp = p.C + (long)gi + (long)gj * p.ldc;
-          double v = p.alpha * acc[mt][nt][r];
-          if (p.beta != 0.0) v = fma(p.beta, *cp, v);
-          *cp = v;
+          if (p.W) {  // split K: this split's partial, combined by k_splitk_reduce
+            p.W[(long)bz * p.ldw * p.N + (long)gi + (long)gj * p.ldw] = p.alpha * acc[mt][nt][r];
+          } else {
+            double* cp = p.C + (long)gi + (long)gj * p.ldc;
+            double v = p.alpha * acc[mt][nt][r];
+            if (p.beta != 0.0) v = fma(p.beta, *cp, v);
+            *cp = v;
+          }
         }
       }
 }
 
 template <int KIND>
 __global__ void __launch_bounds__(F64_THREADS, 1) k_struct_f64(F64Args p) {
-  struct_f64_tile<KIND>(p, blockIdx.x, blockIdx.y);
+  struct_f64_tile<KIND>(p, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+// C := beta * C + sum_z W_z over the S split-K partials, in split order (deterministic).
+__global__ void k_splitk_reduce(double* __restrict__ C, long ldc, const double* __restrict__ W, long ldw, int M,
+                                int N, int S, double beta) {
+  const long total = (long)M * N;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total; e += (long)gridDim.x * blockDim.x) {
+    const long i = e % M, j = e / M;
+    double v = W[i + j * ldw];
+    for (int z = 1; z < S; ++z) v += W[(long)z * ldw * N + i + j * ldw];
+    double* cp = C + i + j * ldc;
+    if (beta != 0.0) v = fma(beta, *cp, v);
+    *cp = v;
+  }
 }
 
 // Grouped: block b belongs to the product with the largest first block t0 <= b.
@@ -313,8 +341,35 @@ __global__ void k_dft_table(double2* w, int n) {
   }
 }
 
+// Splits of K that fill the SMs in whole waves when the output has few tiles: the count S
+// (1..8, at least 256 k per split) maximising the useful fraction of the last wave, with a
+// small charge per extra split for the partial traffic.
+int f64_splitk_count(int M, int N, int K, int sms) {
+  const long tiles = (long)((M + F64_BM - 1) / F64_BM) * ((N + F64_BN - 1) / F64_BN);
+  if (tiles >= 4L * sms || K < 512) return 1;
+  int best = 1;
+  double best_v = -1.0;
+  for (int S = 1; S <= 8 && K / S >= 256; ++S) {
+    const long jobs = tiles * S;
+    const double eff = (double)jobs / (double)(((jobs + sms - 1) / sms) * sms);
+    const double v = eff - 0.01 * (S - 1);
+    if (v > best_v + 1e-9) { best_v = v; best = S; }
+  }
+  return best;
+}
+
+size_t f64_splitk_bytes(int M, int N, int K, int sms) {
+  const int S = f64_splitk_count(M, N, K, sms);
+  return S > 1 ? (size_t)S * (size_t)M * (size_t)N * sizeof(double) : 0;
+}
+
 int launch_struct_f64(int M, int N, int K, double alpha, const double* X, long ldx, const GenSpec& gs,
                       double beta, double* C, long ldc, cudaStream_t stream) {
+  return launch_struct_f64_ws(M, N, K, alpha, X, ldx, gs, beta, C, ldc, nullptr, 0, stream);
+}
+
+int launch_struct_f64_ws(int M, int N, int K, double alpha, const double* X, long ldx, const GenSpec& gs,
+                         double beta, double* C, long ldc, void* work, size_t lwork, cudaStream_t stream) {
   const int kind = gs.kind;
   if (M == 0 || N == 0) return PSMMA_OK;
   if (alpha == 0.0 || K == 0) {
@@ -329,6 +384,18 @@ int launch_struct_f64(int M, int N, int K, double alpha, const double* X, long l
   p.gs = gs;
   dim3 grid((M + F64_BM - 1) / F64_BM, (N + F64_BN - 1) / F64_BN);
   if (grid.y > 65535) return PSMMA_EUNSUPPORTED;
+  if (work) {
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      return PSMMA_EDEVICE;
+    const int S = f64_splitk_count(M, N, K, sms);
+    if (S > 1 && lwork >= f64_splitk_bytes(M, N, K, sms)) {
+      p.kc = ((K + S - 1) / S + F64_BK - 1) / F64_BK * F64_BK;
+      p.W = (double*)work;
+      p.ldw = M;
+      grid.z = (K + p.kc - 1) / p.kc;
+    }
+  }
   prof_begin(stream);
   switch (kind) {
 #define PSMMA_LAUNCH_F64(KD)                                                                  \
@@ -352,6 +419,11 @@ int launch_struct_f64(int M, int N, int K, double alpha, const double* X, long l
 #undef PSMMA_LAUNCH_F64
     default:
       return PSMMA_EUNSUPPORTED;
+  }
+  if (p.W) {
+    const long total = (long)M * N;
+    const int blocks = (int)std::min<long>((total + 255) / 256, 152L * 16);
+    k_splitk_reduce<<<blocks, 256, 0, stream>>>(C, ldc, p.W, p.ldw, M, N, (int)grid.z, beta);
   }
   prof_mark(stream, "struct_gemm_f64");
   return cudaGetLastError() == cudaSuccess ? PSMMA_OK : PSMMA_EDEVICE;

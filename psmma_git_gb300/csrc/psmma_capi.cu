@@ -136,6 +136,34 @@ int check_dft(int n, int k, double alpha, const void* B, int ldb, double beta, c
   return PSMMA_OK;
 }
 
+// SMs of the current device (0 on error).
+int device_sms() {
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return 0;
+  return sms;
+}
+
+// Split-K partials of the FP64 path for a product with too few output tiles to fill the SMs:
+// the caller's opts->work when it is large enough, else (no caller workspace) the stream's
+// pool, slot 2.  NULL (no split) when the product fills the SMs or the caller's buffer is short.
+void* f64_work(int M, int N, int K, const psmma_opts* o, cudaStream_t s, size_t* bytes, int* st) {
+  *st = PSMMA_OK;
+  *bytes = 0;
+  const int sms = device_sms();
+  const size_t need = sms ? f64_splitk_bytes(M, N, K, sms) : 0;
+  if (!need) return nullptr;
+  if (o->work) {
+    if (o->lwork < need) return nullptr;
+    *bytes = need;
+    return o->work;
+  }
+  void* w = pool_get(need, s, st, 2);
+  if (*st) return nullptr;
+  *bytes = need;
+  return w;
+}
+
 int run_real(int kind, int n, int k, double alpha, const double* A, int lda, const double* gen,
              int ldgen, double beta, double* Q, int ldq, const psmma_opts* opts, void* stream) {
   const psmma_opts* o = opts ? opts : &kDefaultOpts;
@@ -157,7 +185,10 @@ int run_real(int kind, int n, int k, double alpha, const double* A, int lda, con
     return launch_split(kind, n, k, alpha, A, lda, gen, ldgen, beta, Q, ldq, o->n_moduli, work,
                         need, s);
   }
-  return launch_struct_f64(n, k, k, alpha, A, lda, reference_gens(kind, gen, ldgen, k), beta, Q, ldq, s);
+  size_t wb = 0;
+  void* w = f64_work(n, k, k, o, s, &wb, &st);
+  if (st) return st;
+  return launch_struct_f64_ws(n, k, k, alpha, A, lda, reference_gens(kind, gen, ldgen, k), beta, Q, ldq, w, wb, s);
 }
 
 int run_dft(int n, int k, double alpha, const psmma_complex* B, int ldb, double beta,
@@ -382,7 +413,10 @@ int run_eig(int n, int k, double alpha, const double* A, int lda, const double* 
     unsigned* dstat = nullptr;
     return launch_split_general(n, k, k, alpha, A, lda, gs, beta, Q, ldq, o->n_moduli, work, need, s, dstat);
   }
-  return launch_struct_f64(n, k, k, alpha, A, lda, gs, beta, Q, ldq, s);
+  size_t wb = 0;
+  void* w = f64_work(n, k, k, o, s, &wb, &st);
+  if (st) return st;
+  return launch_struct_f64_ws(n, k, k, alpha, A, lda, gs, beta, Q, ldq, w, wb, s);
 }
 
 int host_eig(int n, int k, double alpha, const double* A, int lda, const double* F, const double* U,
@@ -573,10 +607,11 @@ size_t psmma_workspace_size(int kind, int n, int k, const psmma_opts* opts) {
   if (n <= 0 || k <= 0) return 0;
   if (kind < KIND_CAUCHY || kind > KIND_CAUCHY_EIG || kind == KIND_DENSE) return 0;
   if (kind == KIND_CAUCHY_EIG)
-    return o->precision == PSMMA_PREC_SPLIT ? split_workspace_general(n, k, k, o->n_moduli) : 0;
+    return o->precision == PSMMA_PREC_SPLIT ? split_workspace_general(n, k, k, o->n_moduli)
+                                            : f64_splitk_bytes(n, k, k, std::max(1, device_sms()));
   if (o->precision == PSMMA_PREC_SPLIT) return split_workspace_bytes(kind, n, k, o->n_moduli);
   if (kind == KIND_DFT) return align256((size_t)n * sizeof(double2));
-  return 0;
+  return f64_splitk_bytes(n, k, k, std::max(1, device_sms()));
 }
 
 void psmma_release_workspace(void) {

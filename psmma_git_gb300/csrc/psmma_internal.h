@@ -92,6 +92,11 @@ inline GenSpec eig_gens_packed(const double* gen, long ldgen, int k) {
 // operand is streamed (X, column-major, ldx) and the other generated.
 int launch_struct_f64(int M, int N, int K, double alpha, const double* X, long ldx, const GenSpec& gs,
                       double beta, double* C, long ldc, cudaStream_t stream);
+// The same with a workspace for split K (used when the output has too few tiles to fill the
+// SMs and lwork >= f64_splitk_bytes); work may be NULL.
+int launch_struct_f64_ws(int M, int N, int K, double alpha, const double* X, long ldx, const GenSpec& gs,
+                         double beta, double* C, long ldc, void* work, size_t lwork, cudaStream_t stream);
+size_t f64_splitk_bytes(int M, int N, int K, int sms);
 int launch_dft_table(double2* w, int n, cudaStream_t stream);
 
 // Split path (split_crt.cu).

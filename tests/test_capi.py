@@ -80,5 +80,8 @@ def test_status_strings(lib):
 
 def test_workspace_size_queries(lib):
     from psmma_git_gb300 import workspace_size
-    assert workspace_size(_lib.KIND_CAUCHY, 1024, 1024) == 0
+    # FP64 path: nothing once the output fills the SMs; small products may take split-K partials
+    assert workspace_size(_lib.KIND_CAUCHY, 16384, 16384) == 0
+    w = workspace_size(_lib.KIND_CAUCHY, 1024, 1024)
+    assert w == 0 or w % (1024 * 1024 * 8) == 0
     assert workspace_size(_lib.KIND_DFT, 1000, 10) >= 1000 * 16

@@ -174,3 +174,43 @@ def test_fortran_abi_matches(lib, cuda):
                   C.c_void_p(Cm.ctypes.data), i(64), i(0), i(0), None, None)
     assert lib.psmma_last_status() == 0
     assert O.rel_fro(Cm, O.dft_product(1.0, B, 0.0, None)) < TOL
+
+
+@pytest.mark.parametrize("kind", ["cauchy", "toeplitz", "hankel"])
+@pytest.mark.parametrize("n,k,beta", [(300, 1500, 0.0), (257, 2048, -0.5), (2048, 2048, 1.25)])
+def test_split_k_products_match_oracle(kind, n, k, beta, cuda):
+    # few output tiles and a long K: the FP64 path splits K into partial sums (pool workspace)
+    import torch
+    import psmma_git_gb300 as P
+    A = O.cfg_matrix(n, k, seed=21)
+    gen = _gen(kind, k)
+    Q0 = O.cfg_matrix(n, k, seed=22)
+    ref = O.dense_product(kind, 0.75, A, gen, beta, Q0, k)
+    dev = torch.device("cuda")
+    col = lambda x: torch.from_numpy(np.ascontiguousarray(np.asarray(x).T)).to(dev).t()  # noqa: E731
+    dg = col(gen) if kind == "cauchy" else torch.from_numpy(np.asarray(gen)).to(dev)
+    dQ = P.fortran_empty(n, k, torch.float64, dev, ld=n + 3)
+    dQ.copy_(torch.from_numpy(Q0))
+    getattr(P, "psmma_" + kind)(n, k, 0.75, col(A), dg, beta, dQ)
+    torch.cuda.synchronize()
+    assert O.rel_fro(dQ.cpu().numpy(), ref) < TOL
+
+
+def test_split_k_with_caller_workspace_and_short_buffer(cuda):
+    import torch
+    import psmma_git_gb300 as P
+    from psmma_git_gb300 import _lib
+    n, k = 200, 1800
+    A = O.cfg_matrix(n, k, seed=31)
+    gen = O.cfg_cauchy_generators(k, seed=32)
+    ref = O.dense_product("cauchy", 1.0, A, gen, 0.0, None, k)
+    dev = torch.device("cuda")
+    col = lambda x: torch.from_numpy(np.ascontiguousarray(np.asarray(x).T)).to(dev).t()  # noqa: E731
+    need = P.workspace_size(_lib.KIND_CAUCHY, n, k)
+    assert need > 0
+    for size in [need, need // 2]:  # the short buffer runs without split-K
+        work = torch.empty(size, dtype=torch.uint8, device=dev)
+        dQ = P.fortran_empty(n, k, torch.float64, dev)
+        P.psmma_cauchy(n, k, 1.0, col(A), col(gen), 0.0, dQ, work=work)
+        torch.cuda.synchronize()
+        assert O.rel_fro(dQ.cpu().numpy(), ref) < TOL
