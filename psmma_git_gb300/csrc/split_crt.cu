@@ -577,6 +577,41 @@ __device__ __forceinline__ void write_residue_pair(unsigned long long u0, bool n
   }
 }
 
+// The same for four neighbouring integers: one 8-byte store per plane.
+__device__ __forceinline__ void write_residue_quad(const unsigned long long (&u)[4], const bool (&ng)[4],
+                                                   const CrtConsts& cc, uint2* dst, size_t plane_u2) {
+  unsigned x0[4], x1[4], x2[4];
+  float sg[4], of[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    x0[q] = (unsigned)(u[q] & 0x1FFFFFull);
+    x1[q] = (unsigned)((u[q] >> 21) & 0x1FFFFFull);
+    x2[q] = (unsigned)(u[q] >> 42);
+    sg[q] = ng[q] ? -1.0f : 1.0f;
+    of[q] = -12582912.0f * sg[q];
+  }
+#pragma unroll
+  for (int l = 0; l < SPL_MAX_MODULI; ++l) {
+    if (l < cc.nmod) {
+      const unsigned m = (unsigned)cc.m[l], mg = cc.magic38[l], c21 = (unsigned)cc.c21[l],
+                     c42 = (unsigned)cc.c42[l], h = cc.half[l], hb = cc.hbase[l];
+      unsigned f[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const unsigned t = x2[q] * c42 + x1[q] * c21 + x0[q] + h;
+        const unsigned r = t - (__umulhi(t, mg) >> 6) * m;
+        f[q] = __float_as_uint(fmaf(__uint_as_float(hb + r), sg[q], of[q]));
+      }
+      *dst = make_uint2(__byte_perm(f[0], f[1], 0x7632), __byte_perm(f[2], f[3], 0x7632));
+      dst += plane_u2;
+    }
+  }
+}
+
+// residues_H: consecutive kk per thread, and the grid width of a column
+constexpr int RH_PER_THREAD = 4;
+__host__ __device__ __forceinline__ int rh_blocks_x(int kp) { return (kp / RH_PER_THREAD + 127) / 128; }
+
 // RA[l][i][kk] = residues of A' (bf16), rows i, K-major.  Block: 32 rows x 64 k.
 __device__ __forceinline__ void residues_A_blk(const double* __restrict__ A, long lda, const double* A2, long lda2,
                                                int ka, int n, int k, int kp,
@@ -593,18 +628,22 @@ __device__ __forceinline__ void residues_A_blk(const double* __restrict__ A, lon
   __syncthreads();
   const int P = prm->PA;
   const size_t plane = (size_t)n * kp;
-  for (int r = ty; r < 32; r += 8) {
+  const int tq = threadIdx.x & 15, tr = threadIdx.x >> 4;  // 16 quads of k x 16 rows
+  for (int r = tr; r < 32; r += 16) {
     int gi = i0 + r;
     if (gi >= n) continue;
     unsigned long long ab = amax_bits[gi];
     bool ok = ab > 0 && ab < INF_BITS;
     int e = ok ? scale_exp(ab, P) : 0;
-    int kk = 2 * tx;
-    bool n0 = false, n1 = false;
-    unsigned long long u0 = ok ? scaled_int(tile[kk][r], e, &n0) : 0ull;
-    unsigned long long u1 = ok ? scaled_int(tile[kk + 1][r], e, &n1) : 0ull;
-    uint32_t* dst = (uint32_t*)(RA + (size_t)gi * kp + k0 + kk);
-    write_residue_pair(u0, n0, u1, n1, cc, dst, plane / 2);
+    const int kk = 4 * tq;
+    unsigned long long u[4];
+    bool ng[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      ng[q] = false;
+      u[q] = ok ? scaled_int(tile[kk + q][r], e, &ng[q]) : 0ull;
+    }
+    write_residue_quad(u, ng, cc, (uint2*)(RA + (size_t)gi * kp + k0 + kk), plane / 4);
   }
 }
 
@@ -614,25 +653,30 @@ __global__ void k_residues_A(const double* __restrict__ A, long lda, int n, int 
   residues_A_blk(A, lda, nullptr, 0, k, n, k, kp, amax_bits, prm, cc, RA, blockIdx.x, blockIdx.y);
 }
 
-// RH[l][j][kk] = residues of H' (bf16) from Ht[j][kk]; one thread per 2 consecutive kk.
+// RH[l][j][kk] = residues of H' (bf16) from Ht[j][kk]; one thread per 4 consecutive kk.
 __device__ __forceinline__ void residues_H_blk(const double* __restrict__ Ht, int ncols, int kp,
                                                const unsigned long long* __restrict__ hmax_bits,
                                                const SplitDevParams* prm, const CrtConsts& cc,
                                                __nv_bfloat16* __restrict__ RH, int bx, int by) {
   const int j = by;
-  const int kk = 2 * (bx * blockDim.x + threadIdx.x);
-  if (kk >= kp) return;
+  const int kk = RH_PER_THREAD * (bx * blockDim.x + threadIdx.x);
+  if (kk >= kp) return;  // kp is a multiple of 64: a thread's four entries are all inside
   const int P = prm->PH;
   unsigned long long hb = hmax_bits[j];
   bool ok = hb > 0 && hb < INF_BITS;
   int e = ok ? scale_exp(hb, P) : 0;
-  double2 h = *(const double2*)(Ht + (size_t)j * kp + kk);
-  bool n0 = false, n1 = false;
-  unsigned long long u0 = ok ? scaled_int(h.x, e, &n0) : 0ull;
-  unsigned long long u1 = ok ? scaled_int(h.y, e, &n1) : 0ull;
+  const double2 h01 = *(const double2*)(Ht + (size_t)j * kp + kk);
+  const double2 h23 = *(const double2*)(Ht + (size_t)j * kp + kk + 2);
+  const double hv[4] = {h01.x, h01.y, h23.x, h23.y};
+  unsigned long long u[4];
+  bool ng[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    ng[q] = false;
+    u[q] = ok ? scaled_int(hv[q], e, &ng[q]) : 0ull;
+  }
   const size_t plane = (size_t)ncols * kp;
-  uint32_t* dst = (uint32_t*)(RH + (size_t)j * kp + kk);
-  write_residue_pair(u0, n0, u1, n1, cc, dst, plane / 2);
+  write_residue_quad(u, ng, cc, (uint2*)(RH + (size_t)j * kp + kk), plane / 4);
 }
 
 __global__ void k_residues_H(const double* __restrict__ Ht, int ncols, int kp,
@@ -1311,7 +1355,7 @@ static int split_core(int M, int N, int K, double alpha, const double* A, long l
     k_residues_A_dft<<<dim3((L.kp / 2 + 127) / 128, M), 128, 0, stream>>>(A, 2 * lda, gs.n_dft, L.kp, b.amax,
                                                                            b.prm, cc, b.RA, M);
   prof_mark(stream, "residues_A");
-  k_residues_H<<<dim3((L.kp / 2 + 127) / 128, N), 128, 0, stream>>>(b.Ht, N, L.kp, b.hmax, b.prm, cc, b.RH);
+  k_residues_H<<<dim3(rh_blocks_x(L.kp), N), 128, 0, stream>>>(b.Ht, N, L.kp, b.hmax, b.prm, cc, b.RH);
   prof_mark(stream, "residues_H");
 
   OneGemm og;
@@ -1421,7 +1465,7 @@ static int split_core_host(int M, int N, int K, double alpha, const double* A_h,
   if (!ok) return PSMMA_EDEVICE;
   k_split_params<<<PARAMS_BLOCKS, 512, 0, s>>>(b.prm, cc.log2M, M, N, K, b.amax, b.asq, b.hmax, b.hsq);
   k_residues_A<<<dim3(L.kp / 64, (M + 31) / 32), 256, 0, s>>>(dA, M, M, K, L.kp, b.amax, b.prm, cc, b.RA);
-  k_residues_H<<<dim3((L.kp / 2 + 127) / 128, N), 128, 0, s>>>(b.Ht, N, L.kp, b.hmax, b.prm, cc, b.RH);
+  k_residues_H<<<dim3(rh_blocks_x(L.kp), N), 128, 0, s>>>(b.Ht, N, L.kp, b.hmax, b.prm, cc, b.RH);
 
   OneGemm og;
   memset(&og, 0, sizeof(og));
@@ -1588,7 +1632,7 @@ __global__ void __launch_bounds__(256) k_g_residues_A(const GProb* d, int count,
 
 __global__ void __launch_bounds__(128) k_g_residues_H(const GProb* d, int count, CrtConsts cc) {
   const GProb& e = d[gfind<3>(d, count, blockIdx.x)];
-  const int local = blockIdx.x - e.b_rh, gx = (e.kp / 2 + 127) / 128;
+  const int local = blockIdx.x - e.b_rh, gx = rh_blocks_x(e.kp);
   residues_H_blk(e.Ht, e.N, e.kp, e.hmax, e.prm, cc, e.RH, local % gx, local / gx);
 }
 
@@ -1653,7 +1697,7 @@ int plan_group(const SplitProblem* P, int count, int nmod, const SplitTune& tune
     e.b_row = b_row; b_row += ((e.M + 127) / 128) * ((e.K + G_ROW_KCHUNK - 1) / G_ROW_KCHUNK);
     e.b_h = b_h;     b_h += e.N;
     e.b_ra = b_ra;   b_ra += (e.kp / 64) * ((e.M + 31) / 32);
-    e.b_rh = b_rh;   b_rh += ((e.kp / 2 + 127) / 128) * e.N;
+    e.b_rh = b_rh;   b_rh += rh_blocks_x(e.kp) * e.N;
     e.b_crt = b_crt; b_crt += ((e.N + CRT_TJ - 1) / CRT_TJ) * ((e.M + CRT_TI - 1) / CRT_TI);
   }
   g->count = count;
