@@ -203,3 +203,34 @@ def test_split_dft_ones_fixture(cuda):
     for variant in ["pzmdftl", "pzmdftl1"]:
         got = _split_dft(n, n, 1.0, z["B"], 0.0, np.zeros((n, n), complex), cuda, variant=variant)
         assert np.abs(got - z["X"]).max() < 1e-10
+
+
+def test_split_power_of_two_scaling_is_exact(cuda):
+    # scaling A by 2^300 and U by 2^-200 scales every step exactly (row / column exponents,
+    # the FP32 bound sums on their per-thread scales, the division, the CRT's exponent), so the
+    # result is the unscaled one times 2^100, bit for bit
+    n, k = 700, 900
+    A = O.cfg_matrix(n, k, seed=41, dist="normal")
+    gen = _gen("cauchy", k, seed=42, clustered=0.1)
+    base = _split("cauchy", n, k, 1.0, A, gen, 0.0, np.zeros((n, k)), cuda)
+    g2 = gen.copy()
+    g2[:, 2] *= 2.0 ** -200  # U
+    got = _split("cauchy", n, k, 1.0, A * 2.0 ** 300, g2, 0.0, np.zeros((n, k)), cuda)
+    np.testing.assert_array_equal(got, base * 2.0 ** 100)
+    assert O.rel_fro(base, O.dense_product("cauchy", 1.0, A, gen, 0.0, None, k)) < TOL
+
+
+def test_split_pole_gap_outside_the_fast_division_range(cuda):
+    # D(11) = 1e-32, F(11) = 2.5e-32: |D(11) - F(11)| < 2^-100 takes the full division, and the
+    # 1e32-sized entry is 2^100 times its column's others (the FP32 bound sums of that
+    # thread fall back to FP64)
+    n, k = 256, 512
+    A = O.cfg_matrix(n, k, seed=43)
+    gen = _gen("cauchy", k, seed=44)
+    gen[10, 0], gen[10, 1] = 1e-32, 2.5e-32
+    got = _split("cauchy", n, k, 1.0, A, gen, 0.0, np.zeros((n, k)), cuda)
+    ref = O.dense_product("cauchy", 1.0, A, gen, 0.0, None, k)
+    assert np.isfinite(got).all()
+    assert O.rel_fro(got, ref) < TOL
+    others = np.arange(k) != 10  # the other columns keep their own accuracy
+    assert O.rel_fro(got[:, others], ref[:, others]) < TOL
