@@ -21,8 +21,11 @@
 #include <cudaTypedefs.h>
 
 #include <cmath>
+#include <cstddef>
 #include <cstring>
+#include <map>
 #include <mutex>
+#include <tuple>
 #include <vector>
 
 #include "psmma_internal.h"
@@ -657,11 +660,11 @@ __global__ void k_residues_A(const double* __restrict__ A, long lda, int n, int 
 __device__ __forceinline__ void residues_H_blk(const double* __restrict__ Ht, int ncols, int kp,
                                                const unsigned long long* __restrict__ hmax_bits,
                                                const SplitDevParams* prm, const CrtConsts& cc,
-                                               __nv_bfloat16* __restrict__ RH, int bx, int by) {
+                                               __nv_bfloat16* __restrict__ RH, int bx, int by, int ph = -1) {
   const int j = by;
   const int kk = RH_PER_THREAD * (bx * blockDim.x + threadIdx.x);
   if (kk >= kp) return;  // kp is a multiple of 64: a thread's four entries are all inside
-  const int P = prm->PH;
+  const int P = ph >= 0 ? ph : prm->PH;
   unsigned long long hb = hmax_bits[j];
   bool ok = hb > 0 && hb < INF_BITS;
   int e = ok ? scale_exp(hb, P) : 0;
@@ -683,6 +686,16 @@ __global__ void k_residues_H(const double* __restrict__ Ht, int ncols, int kp,
                              const unsigned long long* __restrict__ hmax_bits, const SplitDevParams* prm,
                              CrtConsts cc, __nv_bfloat16* __restrict__ RH) {
   residues_H_blk(Ht, ncols, kp, hmax_bits, prm, cc, RH, blockIdx.x, blockIdx.y);
+}
+
+// Speculative H residues: with guess >= 0 and !redo, the planes for PH = guess (before the
+// parameter pass has run); with redo, nothing when the parameter pass chose PH == guess, else
+// the planes for the chosen PH.
+__global__ void k_residues_H_spec(const double* __restrict__ Ht, int ncols, int kp,
+                                  const unsigned long long* __restrict__ hmax_bits, const SplitDevParams* prm,
+                                  CrtConsts cc, __nv_bfloat16* __restrict__ RH, int guess, int redo) {
+  if (redo && prm->PH == guess) return;
+  residues_H_blk(Ht, ncols, kp, hmax_bits, prm, cc, RH, blockIdx.x, blockIdx.y, redo ? -1 : guess);
 }
 
 // DFT A side: row i of the embedded operand X' = [Re B^T | Im B^T] is column i of B, read
@@ -1415,9 +1428,14 @@ static int split_core(int M, int N, int K, double alpha, const double* A, long l
 // panels of whole 128-row tiles, and each finished panel of Q goes back to the host on `cs`
 // while the next panel multiplies.  dA (M x K) and dQ (M x N) are device buffers with leading
 // dimension M; Q is read from the host first when beta != 0.  Synchronises both streams.
+// The H residues need PH, which the parameter pass sets from A's statistics as well; with a
+// guess (the PH a previous call of the same shape chose) they are computed while A is still
+// being uploaded and recomputed after the parameter pass only if the guess was wrong.
+// *ph_out receives the PH this call used.
 static int split_core_host(int M, int N, int K, double alpha, const double* A_h, long lda_h, double* dA,
                            const GenSpec& gs, double beta, double* Q_h, long ldq_h, double* dQ, int nmod, void* work,
-                           size_t lwork, cudaStream_t s, cudaStream_t cs, cudaEvent_t* ev, int nev) {
+                           size_t lwork, cudaStream_t s, cudaStream_t cs, cudaEvent_t* ev, int nev, int ph_guess,
+                           int* ph_out) {
   if (gs.kind == KIND_DFT) return PSMMA_EUNSUPPORTED;
   if (nmod < 8 || nmod > SPL_MAX_MODULI) return PSMMA_EUNSUPPORTED;
   if (K >= (1 << 24) || M >= (1 << 30) || N >= (1 << 30)) return PSMMA_EUNSUPPORTED;
@@ -1444,6 +1462,9 @@ static int split_core_host(int M, int N, int K, double alpha, const double* A_h,
     case KIND_CAUCHY_EIG: k_h_pass1<KIND_CAUCHY_EIG><<<N, 256, 0, s>>>(gs, K, L.kp, b.Ht, b.hmax, b.hsum, b.hsq, b.prm); break;
     default: return PSMMA_EUNSUPPORTED;
   }
+  const dim3 grh(rh_blocks_x(L.kp), N);
+  if (ph_guess >= 8)
+    k_residues_H_spec<<<grh, 128, 0, s>>>(b.Ht, N, L.kp, b.hmax, b.prm, cc, b.RH, ph_guess, 0);
   // ---- A in column chunks (multiples of the 1024-column row-norm chunk)
   const int kchunk = 1024;
   const int cols_per = std::max(kchunk, (K + NCH * kchunk - 1) / (NCH * kchunk) * kchunk);
@@ -1465,7 +1486,10 @@ static int split_core_host(int M, int N, int K, double alpha, const double* A_h,
   if (!ok) return PSMMA_EDEVICE;
   k_split_params<<<PARAMS_BLOCKS, 512, 0, s>>>(b.prm, cc.log2M, M, N, K, b.amax, b.asq, b.hmax, b.hsq);
   k_residues_A<<<dim3(L.kp / 64, (M + 31) / 32), 256, 0, s>>>(dA, M, M, K, L.kp, b.amax, b.prm, cc, b.RA);
-  k_residues_H<<<dim3(rh_blocks_x(L.kp), N), 128, 0, s>>>(b.Ht, N, L.kp, b.hmax, b.prm, cc, b.RH);
+  if (ph_guess >= 8)
+    k_residues_H_spec<<<grh, 128, 0, s>>>(b.Ht, N, L.kp, b.hmax, b.prm, cc, b.RH, ph_guess, 1);
+  else
+    k_residues_H<<<grh, 128, 0, s>>>(b.Ht, N, L.kp, b.hmax, b.prm, cc, b.RH);
 
   OneGemm og;
   memset(&og, 0, sizeof(og));
@@ -1509,14 +1533,47 @@ static int split_core_host(int M, int N, int K, double alpha, const double* A_h,
                             cudaMemcpyDeviceToHost, cs) == cudaSuccess;
   }
   if (cudaGetLastError() != cudaSuccess) ok = false;
-  unsigned st = 0;
-  ok &= cudaMemcpyAsync(&st, &b.prm->status, sizeof(st), cudaMemcpyDeviceToHost, s) == cudaSuccess;
+  SplitDevParams head;  // status, PA, PH
+  ok &= cudaMemcpyAsync(&head, b.prm, offsetof(SplitDevParams, rho_bits), cudaMemcpyDeviceToHost, s) == cudaSuccess;
   ok &= cudaEventRecord(ev_done, cs) == cudaSuccess;
   ok &= cudaStreamSynchronize(s) == cudaSuccess;
   ok &= cudaEventSynchronize(ev_done) == cudaSuccess;
   if (!ok) return PSMMA_EDEVICE;
-  if (st & DEV_ERR_TIMEOUT) return PSMMA_ETIMEDOUT;
+  if (ph_out) *ph_out = head.PH;
+  if (head.status & DEV_ERR_TIMEOUT) return PSMMA_ETIMEDOUT;
   return PSMMA_OK;
+}
+
+// PH chosen by the last overlapped host call of each shape (the speculation's guess).
+struct PhKey {
+  int M, N, K, kind, nmod;
+  bool operator<(const PhKey& o) const {
+    return std::tie(M, N, K, kind, nmod) < std::tie(o.M, o.N, o.K, o.kind, o.nmod);
+  }
+};
+static std::mutex g_ph_mu;
+static std::map<PhKey, int> g_ph;
+
+static int split_core_host_cached(int M, int N, int K, double alpha, const double* A_h, long lda_h, double* dA,
+                                  const GenSpec& gs, double beta, double* Q_h, long ldq_h, double* dQ, int nmod,
+                                  void* work, size_t lwork, cudaStream_t s, cudaStream_t cs, cudaEvent_t* ev,
+                                  int nev) {
+  const PhKey key{M, N, K, gs.kind, nmod};
+  int guess = -1;
+  {
+    std::lock_guard<std::mutex> lk(g_ph_mu);
+    auto it = g_ph.find(key);
+    if (it != g_ph.end()) guess = it->second;
+  }
+  int ph = -1;
+  const int st = split_core_host(M, N, K, alpha, A_h, lda_h, dA, gs, beta, Q_h, ldq_h, dQ, nmod, work, lwork, s, cs,
+                                 ev, nev, guess, &ph);
+  if (!st && ph >= 8) {
+    std::lock_guard<std::mutex> lk(g_ph_mu);
+    if (g_ph.size() > 256) g_ph.clear();
+    g_ph[key] = ph;
+  }
+  return st;
 }
 
 int launch_split_host(int kind, int n, int k, double alpha, const double* A_h, long lda_h, double* dA,
@@ -1524,15 +1581,15 @@ int launch_split_host(int kind, int n, int k, double alpha, const double* A_h, l
                       int n_moduli, void* work, size_t lwork, cudaStream_t s, cudaStream_t cs, cudaEvent_t* ev,
                       int nev) {
   const GenSpec gs = reference_gens(kind, dgen, ldgen, k);
-  return split_core_host(n, k, k, alpha, A_h, lda_h, dA, gs, beta, Q_h, ldq_h, dQ, resolve_nmod(n_moduli), work,
-                         lwork, s, cs, ev, nev);
+  return split_core_host_cached(n, k, k, alpha, A_h, lda_h, dA, gs, beta, Q_h, ldq_h, dQ, resolve_nmod(n_moduli),
+                                work, lwork, s, cs, ev, nev);
 }
 
 int launch_split_host_general(int M, int N, int K, double alpha, const double* A_h, long lda_h, double* dA,
                               const GenSpec& gs, double beta, double* Q_h, long ldq_h, double* dQ, int n_moduli,
                               void* work, size_t lwork, cudaStream_t s, cudaStream_t cs, cudaEvent_t* ev, int nev) {
-  return split_core_host(M, N, K, alpha, A_h, lda_h, dA, gs, beta, Q_h, ldq_h, dQ, resolve_nmod(n_moduli), work,
-                         lwork, s, cs, ev, nev);
+  return split_core_host_cached(M, N, K, alpha, A_h, lda_h, dA, gs, beta, Q_h, ldq_h, dQ, resolve_nmod(n_moduli),
+                                work, lwork, s, cs, ev, nev);
 }
 
 // kind != DFT: Q (n x k) = alpha * A (n x k) * H (k x k) + beta * Q.

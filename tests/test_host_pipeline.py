@@ -77,3 +77,29 @@ def test_host_split_cauchyeig():
     Qh = np.asfortranarray(Q0.copy())
     P.psmma_cauchyeig(n, k, 2.0, A, F, U, V, dl, dr, 0.25, Qh, precision="split")
     assert O.rel_fro(Qh, ref) < 1e-12
+
+
+@pytest.mark.gpu
+def test_host_split_speculation_survives_changing_inputs():
+    # the H residues are computed for the PH of the previous call of the same shape while A is
+    # uploaded; inputs whose statistics move PH (flat rows, then one-hot rows, then flat rows
+    # again) must still give the exact product and the device path's result
+    import torch
+    import psmma_git_gb300 as P
+    n, k = 600, 700
+    gen = np.asfortranarray(O.cfg_cauchy_generators(k, seed=51))
+    rng = np.random.default_rng(52)
+    flat = O.cfg_matrix(n, k, seed=53)
+    spiky = 1e-3 * O.cfg_matrix(n, k, seed=54)
+    spiky[np.arange(n), rng.integers(0, k, n)] = 10.0
+    dev = torch.device("cuda")
+    col = lambda x: torch.from_numpy(np.ascontiguousarray(np.asarray(x).T)).to(dev).t()  # noqa: E731
+    for A in [flat, spiky, flat, spiky]:
+        Qh = np.zeros((n, k), order="F")
+        P.psmma_cauchy(n, k, 1.0, np.asfortranarray(A), gen, 0.0, Qh, precision="split")
+        exact = O.dense_product("cauchy", 1.0, A, gen, 0.0, None, k)
+        assert O.rel_fro(Qh, exact) < 1e-12
+        dQ = P.fortran_empty(n, k, torch.float64, dev)
+        P.psmma_cauchy(n, k, 1.0, col(A), col(gen), 0.0, dQ, precision="split")
+        torch.cuda.synchronize()
+        assert O.rel_fro(Qh, dQ.cpu().numpy()) < 1e-13
