@@ -29,6 +29,7 @@ import re
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 from pathlib import Path
 
@@ -72,7 +73,7 @@ class Clocks:
     def __init__(self, index: int):
         self.index = index
         self.proc = None
-        self.path = ROOT / "gpurun_out" / f"bench_clocks_{os.getpid()}.csv"
+        self.path = Path(tempfile.gettempdir()) / f"psmma_bench_clocks_{os.getpid()}_{index}.csv"
 
     def start(self):
         try:
