@@ -859,7 +859,7 @@ def main():
     ap.add_argument("--impl", default="psmma", choices=["psmma", "reference"])
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     # 13 moduli: the fewest that meet the metric's <= 1e-12 error on this workload (measured
-    # 6.6e-13; 14 give 4.1e-14 at 7% more time)
+    # 2.6e-13; 12 moduli lose 7.6 bits of budget)
     ap.add_argument("--n-moduli", type=int, default=13)
     ap.add_argument("--cpu-cols", type=int, default=CPU_COLS)
     ap.add_argument("--no-fp64", action="store_true")

@@ -10,7 +10,7 @@
 //   3. One BF16 GEMM per modulus gives Z_l = A'H' mod m_l.  FP32 accumulation is exact
 //      because the tensor memory accumulator is drained every 1024 k (|sum| <= 2^24) into a
 //      register-held residue.
-//   4. Z = A'H' is recovered exactly by CRT (128-bit integer arithmetic, |Z| < M/16 with
+//   4. Z = A'H' is recovered exactly by CRT (128-bit integer arithmetic, |Z| < 0.497 M with
 //      M = prod m_l), scaled back by 2^-(s_i+f_j) and combined with alpha and beta in FP64.
 // P is chosen on the device from the product bound |Z_ij| <= 2^(2P) * max_j(sum_k|H_kj| /
 // max_k|H_kj|), so no host synchronisation is needed between the passes.
@@ -403,7 +403,9 @@ __global__ void k_h_pass1(GenSpec gs, int K, int kp, double* __restrict__ Ht,
 }
 
 // Bits PA (rows of A) and PH (columns of H).  The integer product must satisfy
-// |Z_ij| <= M/16 for the CRT, with M = prod m_l.  Two rigorous bounds of |Z_ij| =
+// |Z_ij| < 0.497 M for the CRT, with M = prod m_l: the symmetric reconstruction needs |Z| < M/2
+// and the quotient estimate (ffix at 2^-19) errs by at most 16 * 128 * 0.5 * 2^-19 < 0.002 of M,
+// a margin of 1.01 bits.  Two rigorous bounds of |Z_ij| =
 // |sum_k A'_ik H'_kj| for |A'| <= 2^PA, |H'| <= 2^PH (rounding adds at most 1/2 per entry):
 //   L1: 2^(PA+PH) * (rho + k 2^-9),      rho = max_j sum_k|H_kj| / max_k|H_kj|
 //   CS: 2^(PA+PH) * (ra + sqrt(k)/512) * (rh + sqrt(k)/512),
@@ -465,7 +467,7 @@ __device__ __forceinline__ void params_finish(SplitDevParams* prm, double log2M,
   const double l1 = log2(rho * 1.01 + (double)k / 512.0);
   const double cs = log2((v[0] * 1.01 + rk / 512.0) * (v[3] * 1.01 + rk / 512.0));
   const double bound = fmin(l1, (v[0] > 0.0 && v[3] > 0.0) ? cs : l1);
-  int budget = (int)floor(log2M - 4.0 - bound);
+  int budget = (int)floor(log2M - 1.01 - bound);
   int d = 0;
   if (v[1] > 0.0 && v[2] > 0.0 && v[4] > 0.0 && v[5] > 0.0) {
     const double cA = sqrt(v[1] / v[2]), cH = sqrt(v[4] / v[5]);
