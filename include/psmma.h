@@ -203,6 +203,16 @@ int psmma_cauchyeig_batch_lowrank(int count, const psmma_batch_item* items, doub
 size_t psmma_cauchyeig_batch_workspace_size(int count, const psmma_batch_item* items, int compressor,
                                             const psmma_opts* opts);
 
+/* The merge level of Toeplitz multiplies (PSTOEPLITZ_COMPUTE's low-rank branch,
+ * pstoeplitz_compute.f90:262-294 with ConstToeplitzlowrank, Auxil_2p5D.f90:968-1060): each
+ * item's gen is the generator G of psmma_toeplitz (2n - 1 entries; ldgen holds its length), the
+ * off-diagonal blocks of H are explicit tiles compressed by the column-pivoted QR of
+ * Compress_RRQR (the reference has no structured RRLU for Toeplitz), and a block that does not
+ * compress is multiplied as the tile. */
+int psmma_toeplitz_batch_lowrank(int count, const psmma_batch_item* items, double alpha, double beta, double tol,
+                                 const psmma_opts* opts, int* ranks_out, psmma_batch_stats* stats, void* stream);
+size_t psmma_toeplitz_batch_workspace_size(int count, const psmma_batch_item* items, const psmma_opts* opts);
+
 /* No counterpart in the reference.  Autotuner of the split path's grouped GEMM (output-tile
  * widths 64/128/256 by product width, raster group): times psmma_cauchy_batch_lowrank on
  * this batch for each candidate configuration and keeps the fastest for batches of the same

@@ -761,7 +761,7 @@ def cfg_vector(m: int, seed: int = 2) -> np.ndarray:
 # Batched merge level with compressed off-diagonal blocks
 # ---------------------------------------------------------------------------------------
 def merge_level_product(A, gen, beta_Q, alpha: float, beta: float, compressor: str = "rrqr",
-                        tol: float = 1e-14):
+                        tol: float = 1e-14, kind: str = "cauchy"):
     """One problem of the batched merge level: Q = alpha*A*H + beta*Q with H the Cauchy-like
     matrix of gen = [D|F|U|V], split 2 x 2 at h = n // 2.  The diagonal blocks are multiplied
     as dense tiles (ConstCauchy + DGEMM, pscauchy_compute.f90:395-407); each off-diagonal
@@ -770,7 +770,10 @@ def merge_level_product(A, gen, beta_Q, alpha: float, beta: float, compressor: s
     rrluCauchy), then Q(:,C) += alpha * (A(:,R) X) Y.  A tile that does not compress is
     multiplied as the dense tile (the mathematical A*H; the reference would reuse a stale
     buffer there, Cauchylowrank.f90:455-464).  Returns (Q, [rank of H(R1,C2), rank of
-    H(R2,C1)]) -- ranks as the compressor reports them (min(M,N) or M when uncompressed)."""
+    H(R2,C1)]) -- ranks as the compressor reports them (min(M,N) or M when uncompressed).
+    kind="toeplitz": gen is G (2n - 1) and the tiles are ConstToeplitzlowrank's explicit tiles
+    compressed by Compress_RRQR (pstoeplitz_compute.f90:262-294, Auxil_2p5D.f90:968-1060); a
+    full-rank tile is multiplied dense, as the reference does there."""
     A = np.asarray(A, dtype=np.float64)
     gen = np.asarray(gen, dtype=np.float64)
     n = A.shape[0]
@@ -778,7 +781,9 @@ def merge_level_product(A, gen, beta_Q, alpha: float, beta: float, compressor: s
     if n == 0:
         return Q, []
     h = n // 2
-    H = cauchy_like(gen[:n, 0], gen[:n, 1], gen[:n, 2], gen[:n, 3])
+    H = cauchy_like(gen[:n, 0], gen[:n, 1], gen[:n, 2], gen[:n, 3]) if kind == "cauchy" else dense_h(kind, gen, n)
+    if kind != "cauchy" and compressor != "rrqr":
+        raise ValueError("only RRQR compresses Toeplitz / Hankel tiles")
     Q[:, :h] += alpha * (A[:, :h] @ H[:h, :h])
     Q[:, h:] += alpha * (A[:, h:] @ H[h:, h:])
     ranks = []

@@ -35,6 +35,7 @@ __all__ = [
     "psmma_cauchy", "psmma_toeplitz", "psmma_hankel", "pzmdftl", "pzmdftl1", "fortran_empty",
     "workspace_size", "PsmmaError", "PREC_FP64", "PREC_SPLIT", "load", "status_string",
     "make_opts", "psmma_cauchyeig", "cauchy_batch_lowrank", "batch_workspace_size", "tune_batch",
+    "toeplitz_batch_lowrank",
 ]
 
 # The split path (exact modular slices on the BF16 tensor cores) is built into the library.
@@ -191,7 +192,7 @@ def _batch_items(problems):
         pa, lda = _dev(A, "A", torch.float64)
         pg, ldg = _dev(gen, "gen", torch.float64)
         if gen.dim() == 1:
-            ldg = n
+            ldg = gen.numel()  # a generator vector (Toeplitz G): its length
         pq, ldq = _dev(Q, "Q", torch.float64)
         items[i].n, items[i].A, items[i].lda = n, pa, max(lda, 1)
         items[i].gen, items[i].ldgen = pg, ldg
@@ -218,6 +219,27 @@ def cauchy_batch_lowrank(problems, alpha, beta, *, compressor="rrqr", tol=1e-14,
             C.byref(stats), _stream_ptr(stream))
     if st != 0:
         raise PsmmaError(st, "psmma_cauchy_batch_lowrank")
+    info = {"effective_flops": stats.effective_flops, "executed_flops": stats.executed_flops,
+            "compress_flops": stats.compress_flops, "n_blocks": stats.n_blocks, "max_rank": stats.max_rank,
+            "full_rank_blocks": stats.full_rank_blocks}
+    return list(ranks)[:nb], info
+
+
+def toeplitz_batch_lowrank(problems, alpha, beta, *, tol=1e-14, precision="fp64", n_moduli=0, stream=None,
+                           work=None):
+    """The merge level of Toeplitz multiplies: problems = [(A_i, G_i, Q_i), ...] with G_i the
+    2n_i - 1 generator of psmma_toeplitz; off-diagonal blocks compressed by RRQR at ``tol``.
+    Returns (ranks, stats) as cauchy_batch_lowrank."""
+    lib = load()
+    items = _batch_items(problems)
+    opts = make_opts(precision, n_moduli, work)
+    nb = sum(2 for (_, _, Q) in problems if Q.shape[0] >= 2)
+    ranks = (C.c_int * max(1, nb))()
+    stats = PsmmaBatchStats()
+    st = lib.psmma_toeplitz_batch_lowrank(len(problems), items, float(alpha), float(beta), float(tol),
+                                          C.byref(opts), ranks, C.byref(stats), _stream_ptr(stream))
+    if st != 0:
+        raise PsmmaError(st, "psmma_toeplitz_batch_lowrank")
     info = {"effective_flops": stats.effective_flops, "executed_flops": stats.executed_flops,
             "compress_flops": stats.compress_flops, "n_blocks": stats.n_blocks, "max_rank": stats.max_rank,
             "full_rank_blocks": stats.full_rank_blocks}

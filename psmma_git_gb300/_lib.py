@@ -137,6 +137,9 @@ SIGNATURES = {
     "psmma_cauchyeig_batch_lowrank": (_i, [_i, C.POINTER(PsmmaBatchItem), _d, _d, _i, _d, _op, _ip,
                                            C.POINTER(PsmmaBatchStats), _p]),
     "psmma_cauchyeig_batch_workspace_size": (C.c_size_t, [_i, C.POINTER(PsmmaBatchItem), _i, _op]),
+    "psmma_toeplitz_batch_lowrank": (_i, [_i, C.POINTER(PsmmaBatchItem), _d, _d, _d, _op, _ip,
+                                          C.POINTER(PsmmaBatchStats), _p]),
+    "psmma_toeplitz_batch_workspace_size": (C.c_size_t, [_i, C.POINTER(PsmmaBatchItem), _op]),
     "psmma_tune_batch": (_i, [_i, C.POINTER(PsmmaBatchItem), _d, _d, _i, _d, _op, C.POINTER(PsmmaTuneResult), _p]),
     "psmma_numroc": (_i, [_i, _i, _i, _i, _i]),
     "psmma_redist_plan_create": (_i, [_i, _i, _ip, _i, _i, PsmmaGrid, _ip, _i, _i, PsmmaGrid, _i,

@@ -450,7 +450,8 @@ int f64_group_prepare(const F64Prob* P, int count, void* dev, cudaStream_t strea
   for (int i = 0; i < count; ++i) {
     const F64Prob& q = P[i];
     if (q.M <= 0 || q.N <= 0 || q.K <= 0 || q.gs.kind != P[0].gs.kind) return PSMMA_EUNSUPPORTED;
-    if (q.gs.kind != KIND_CAUCHY && q.gs.kind != KIND_DENSE && q.gs.kind != KIND_CAUCHY_EIG)
+    if (q.gs.kind != KIND_CAUCHY && q.gs.kind != KIND_DENSE && q.gs.kind != KIND_CAUCHY_EIG &&
+        q.gs.kind != KIND_TOEPLITZ && q.gs.kind != KIND_HANKEL)
       return PSMMA_EUNSUPPORTED;
     if (q.gs.k1 > 0) return PSMMA_EUNSUPPORTED;  // tail rows: split path only
     F64Args& a = args[i];
@@ -475,27 +476,29 @@ int f64_group_prepare(const F64Prob* P, int count, void* dev, cudaStream_t strea
   return PSMMA_OK;
 }
 
+template <int KIND>
+static int f64_group_launch(const F64Group& g, const F64Args* a, cudaStream_t stream) {
+  if (cudaFuncSetAttribute(k_struct_f64_group<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)F64_SMEM_BYTES) != cudaSuccess)
+    return PSMMA_EDEVICE;
+  k_struct_f64_group<KIND><<<g.blocks, F64_THREADS, F64_SMEM_BYTES, stream>>>(a, g.d_t0, g.count);
+  return PSMMA_OK;
+}
+
 int f64_group_enqueue(const F64Group& g, cudaStream_t stream) {
   if (g.count == 0) return PSMMA_OK;
   const F64Args* a = (const F64Args*)g.d_args;
-  if (g.kind == KIND_CAUCHY) {
-    if (cudaFuncSetAttribute(k_struct_f64_group<KIND_CAUCHY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)F64_SMEM_BYTES) != cudaSuccess)
-      return PSMMA_EDEVICE;
-    k_struct_f64_group<KIND_CAUCHY><<<g.blocks, F64_THREADS, F64_SMEM_BYTES, stream>>>(a, g.d_t0, g.count);
-  } else if (g.kind == KIND_CAUCHY_EIG) {
-    if (cudaFuncSetAttribute(k_struct_f64_group<KIND_CAUCHY_EIG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)F64_SMEM_BYTES) != cudaSuccess)
-      return PSMMA_EDEVICE;
-    k_struct_f64_group<KIND_CAUCHY_EIG><<<g.blocks, F64_THREADS, F64_SMEM_BYTES, stream>>>(a, g.d_t0, g.count);
-  } else {
-    if (cudaFuncSetAttribute(k_struct_f64_group<KIND_DENSE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)F64_SMEM_BYTES) != cudaSuccess)
-      return PSMMA_EDEVICE;
-    k_struct_f64_group<KIND_DENSE><<<g.blocks, F64_THREADS, F64_SMEM_BYTES, stream>>>(a, g.d_t0, g.count);
+  int st;
+  const char* name;
+  switch (g.kind) {
+    case KIND_CAUCHY: st = f64_group_launch<KIND_CAUCHY>(g, a, stream); name = "f64_group_cauchy"; break;
+    case KIND_CAUCHY_EIG: st = f64_group_launch<KIND_CAUCHY_EIG>(g, a, stream); name = "f64_group_cauchyeig"; break;
+    case KIND_TOEPLITZ: st = f64_group_launch<KIND_TOEPLITZ>(g, a, stream); name = "f64_group_toeplitz"; break;
+    case KIND_HANKEL: st = f64_group_launch<KIND_HANKEL>(g, a, stream); name = "f64_group_hankel"; break;
+    default: st = f64_group_launch<KIND_DENSE>(g, a, stream); name = "f64_group_dense"; break;
   }
-  prof_mark(stream, g.kind == KIND_CAUCHY ? "f64_group_cauchy"
-                    : g.kind == KIND_CAUCHY_EIG ? "f64_group_cauchyeig" : "f64_group_dense");
+  if (st) return st;
+  prof_mark(stream, name);
   return cudaGetLastError() == cudaSuccess ? PSMMA_OK : PSMMA_EDEVICE;
 }
 

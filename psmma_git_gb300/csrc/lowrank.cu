@@ -669,9 +669,10 @@ struct QrTile {
   long col0;     // first column of this tile in the batch's column numbering
 };
 
-// Explicit tiles T(i,c) = U(i)V(c)/(D(i)-F(c)) (ConstCauchy, Auxil_2p5D.f90:138-144) or with
-// the accurate denominators of CauchylikeEig (ConstCauchyEig, Auxil_2p5D.f90:532-637), their
-// column norms and the identity pivot; one block per column of the batch.
+// Explicit tiles T(i,c) = U(i)V(c)/(D(i)-F(c)) (ConstCauchy, Auxil_2p5D.f90:138-144), with the
+// accurate denominators of CauchylikeEig (ConstCauchyEig, Auxil_2p5D.f90:532-637), or Toeplitz /
+// Hankel entries (ConstToeplitzlowrank's tile, Auxil_2p5D.f90:968-1060), their column norms and
+// the identity pivot; one block per column of the batch.
 __global__ void __launch_bounds__(QR_THREADS) k_qr_tiles(QrTile* tiles, int ntiles) {
   __shared__ double sm[33];
   const long gc = blockIdx.x;
@@ -684,16 +685,26 @@ __global__ void __launch_bounds__(QR_THREADS) k_qr_tiles(QrTile* tiles, int ntil
   const int c = (int)(gc - t.col0);
   if (c >= t.N) return;
   const GenSpec& g = t.gs;
-  const bool eig = g.kind == KIND_CAUCHY_EIG;
-  const double f = g.Fc[c], v = g.Vc[c];
-  const double f1 = (eig && c < g.fc1_len) ? g.Fc1[c] : 0.0;
-  const double dl = eig ? g.dl[c] : 0.0, dr = (eig && c < g.fc1_len) ? g.dr[c] : 0.0;
   double ss = 0.0;
-  for (int i = threadIdx.x; i < t.M; i += blockDim.x) {
-    const double h = eig ? (g.Ur[i] * v) / eig_den(g.Dr[i], f, f1, dl, dr, i - c <= g.diag_off)
-                         : (g.Ur[i] * v) / (g.Dr[i] - f);
-    t.T[i + (long)c * t.M] = h;
-    ss = fma(h, h, ss);
+  if (g.kind == KIND_TOEPLITZ || g.kind == KIND_HANKEL) {
+    // ConstToeplitz / ConstHankel (Auxil_2p5D.f90:224-231, 309-316) on the shifted generator
+    const bool toep = g.kind == KIND_TOEPLITZ;
+    for (int i = threadIdx.x; i < t.M; i += blockDim.x) {
+      const double h = toep ? g.g[(g.order - 1) + c - i] : g.g[i + c];
+      t.T[i + (long)c * t.M] = h;
+      ss = fma(h, h, ss);
+    }
+  } else {
+    const bool eig = g.kind == KIND_CAUCHY_EIG;
+    const double f = g.Fc[c], v = g.Vc[c];
+    const double f1 = (eig && c < g.fc1_len) ? g.Fc1[c] : 0.0;
+    const double dl = eig ? g.dl[c] : 0.0, dr = (eig && c < g.fc1_len) ? g.dr[c] : 0.0;
+    for (int i = threadIdx.x; i < t.M; i += blockDim.x) {
+      const double h = eig ? (g.Ur[i] * v) / eig_den(g.Dr[i], f, f1, dl, dr, i - c <= g.diag_off)
+                           : (g.Ur[i] * v) / (g.Dr[i] - f);
+      t.T[i + (long)c * t.M] = h;
+      ss = fma(h, h, ss);
+    }
   }
   ss = block_sum(ss, sm);
   if (threadIdx.x == 0) {
@@ -1082,10 +1093,22 @@ struct Plan {
 };
 
 // Generators of the sub-block H(r0:, c0:) of an item's n x n matrix.  Cauchy: gen = [D|F|U|V]
-// (ldgen); accurate-denominator Cauchy: gen = [F|U|V|DIFL|DIFR].
+// (ldgen); accurate-denominator Cauchy: gen = [F|U|V|DIFL|DIFR]; Toeplitz / Hankel: gen = G
+// (2n - 1), H(i, j) = G(n + j - i) / G(i + j - 1) (1-based), so a sub-block is the same formula
+// on G shifted by c0 - r0 / r0 + c0.
 GenSpec sub_gens(int kind, const double* gen, long ldgen, int n, int r0, int c0) {
   GenSpec g;
   g.kind = kind;
+  if (kind == KIND_TOEPLITZ) {
+    g.g = gen + (c0 - r0);
+    g.order = n;
+    return g;
+  }
+  if (kind == KIND_HANKEL) {
+    g.g = gen + (r0 + c0);
+    g.order = n;
+    return g;
+  }
   if (kind == KIND_CAUCHY_EIG) {
     const double *F = gen, *U = gen + ldgen, *V = gen + 2 * ldgen, *DL = gen + 3 * ldgen, *DR = gen + 4 * ldgen;
     g.Dr = F + r0;
@@ -1430,10 +1453,12 @@ void build_rounds_split(const Plan& P, const psmma_batch_item* items, int count,
 // Workspace of the product rounds (part B).
 struct RoundGroups {
   SplitGroup s1, s2;
-  F64Group f[6];  // per round: Cauchy, accurate-denominator Cauchy, dense
+  F64Group f[2 * 5];  // per round: Cauchy, accurate-denominator Cauchy, Toeplitz, Hankel, dense
 };
 
-constexpr int kF64Kinds[3] = {KIND_CAUCHY, KIND_CAUCHY_EIG, KIND_DENSE};
+// dense last: within a round the beta-scaled product of an output block comes first
+constexpr int kNF64Kinds = 5;
+constexpr int kF64Kinds[kNF64Kinds] = {KIND_CAUCHY, KIND_CAUCHY_EIG, KIND_TOEPLITZ, KIND_HANKEL, KIND_DENSE};
 
 std::vector<F64Prob> f64_of(const std::vector<SplitProblem>& v, int kind) {
   std::vector<F64Prob> out;
@@ -1446,7 +1471,7 @@ size_t rounds_bytes(const Rounds& R, int precision, int n_moduli) {
   if (precision == PSMMA_PREC_SPLIT)
     return split_group_bytes(R.r1.data(), (int)R.r1.size(), n_moduli) + 4096 +
            split_group_bytes(R.r2.data(), (int)R.r2.size(), n_moduli) + 4096;
-  return f64_group_bytes((int)R.r1.size()) * 3 + f64_group_bytes((int)R.r2.size()) * 3 + 4096;
+  return f64_group_bytes((int)R.r1.size()) * kNF64Kinds + f64_group_bytes((int)R.r2.size()) * kNF64Kinds + 4096;
 }
 
 int prepare_rounds(const Rounds& R, int precision, int n_moduli, const SplitTune& tune, void* work,
@@ -1464,11 +1489,11 @@ int prepare_rounds(const Rounds& R, int precision, int n_moduli, const SplitTune
   }
   const std::vector<SplitProblem>* rs[2] = {&R.r1, &R.r2};
   for (int r = 0; r < 2; ++r)
-    for (int k = 0; k < 3; ++k) {
+    for (int k = 0; k < kNF64Kinds; ++k) {
       const std::vector<F64Prob> v = f64_of(*rs[r], kF64Kinds[k]);
       char* w = b.take<char>(f64_group_bytes((int)v.size()), 256);
       if (b.off > lwork) return PSMMA_EWORKSPACE;
-      const int rc = f64_group_prepare(v.data(), (int)v.size(), w, st, &G.f[3 * r + k]);
+      const int rc = f64_group_prepare(v.data(), (int)v.size(), w, st, &G.f[kNF64Kinds * r + k]);
       if (rc) return rc;
     }
   return PSMMA_OK;
@@ -1481,7 +1506,7 @@ int enqueue_rounds(const RoundGroups& G, int precision, unsigned* status, cudaSt
     if (!rc) rc = split_group_enqueue(G.s2, st, status + 1);
     return rc;
   }
-  for (int i = 0; i < 6 && !rc; ++i) rc = f64_group_enqueue(G.f[i], st);
+  for (int i = 0; i < 2 * kNF64Kinds && !rc; ++i) rc = f64_group_enqueue(G.f[i], st);
   return rc;
 }
 
@@ -1584,7 +1609,9 @@ int launch_rrqr(Plan& P, int grid, double tol, unsigned* status, cudaStream_t st
 }
 
 int check_batch(int count, const psmma_batch_item* items, int precision, int n_moduli, int compressor,
-                double tol) {
+                double tol, int kind = KIND_CAUCHY) {
+  const bool vec = kind == KIND_TOEPLITZ || kind == KIND_HANKEL;  // gen = G (2n - 1), ldgen = its length
+  if (vec && compressor != PSMMA_COMPRESS_RRQR) return PSMMA_EUNSUPPORTED;
   if (count < 0 || (count > 0 && !items)) return PSMMA_ENULL;
   if (precision != PSMMA_PREC_FP64 && precision != PSMMA_PREC_SPLIT) return PSMMA_EUNSUPPORTED;
   if (precision == PSMMA_PREC_SPLIT && n_moduli != 0 && (n_moduli < 8 || n_moduli > 16)) return PSMMA_EUNSUPPORTED;
@@ -1596,7 +1623,7 @@ int check_batch(int count, const psmma_batch_item* items, int precision, int n_m
     if (it.lda < std::max(1, it.n)) return -9;
     if (it.ldq < std::max(1, it.n)) return -14;
     if (it.n > 0 && (!it.A || !it.Q)) return PSMMA_ENULL;
-    if (it.n > 0 && (!it.gen || it.ldgen < it.n)) return PSMMA_EGEN;
+    if (it.n > 0 && (!it.gen || it.ldgen < (vec ? 2 * it.n - 1 : it.n))) return PSMMA_EGEN;
   }
   return PSMMA_OK;
 }
@@ -1742,7 +1769,7 @@ static size_t batch_workspace(int kind, int count, const psmma_batch_item* items
                               const psmma_opts* opts) {
   const int precision = opts ? opts->precision : PSMMA_PREC_FP64;
   const int n_moduli = opts ? opts->n_moduli : 0;
-  if (count <= 0 || !items || check_batch(count, items, precision, n_moduli, compressor, 0.5)) return 0;
+  if (count <= 0 || !items || check_batch(count, items, precision, n_moduli, compressor, 0.5, kind)) return 0;
   Plan P;
   const size_t a = part_a_bytes(P, items, count, compressor, kind);
   return a + rounds_bound(P, items, count, compressor, kind, precision, n_moduli) + 4096;
@@ -1758,11 +1785,16 @@ extern "C" size_t psmma_cauchyeig_batch_workspace_size(int count, const psmma_ba
   return batch_workspace(KIND_CAUCHY_EIG, count, items, compressor, opts);
 }
 
+extern "C" size_t psmma_toeplitz_batch_workspace_size(int count, const psmma_batch_item* items,
+                                                      const psmma_opts* opts) {
+  return batch_workspace(KIND_TOEPLITZ, count, items, PSMMA_COMPRESS_RRQR, opts);
+}
+
 static int batch_run(int kind, int count, const psmma_batch_item* items, double alpha, double beta, int compressor,
                      double tol, const psmma_opts* opts, int* ranks_out, psmma_batch_stats* stats, void* stream) {
   const int precision = opts ? opts->precision : PSMMA_PREC_FP64;
   const int n_moduli = opts ? opts->n_moduli : 0;
-  int rc = check_batch(count, items, precision, n_moduli, compressor, tol);
+  int rc = check_batch(count, items, precision, n_moduli, compressor, tol, kind);
   if (rc) return rc;
   if (stats) *stats = psmma_batch_stats{0.0, 0.0, 0.0, 0, 0, 0, 0};
   if (count == 0) return PSMMA_OK;
@@ -1942,6 +1974,12 @@ extern "C" int psmma_cauchyeig_batch_lowrank(int count, const psmma_batch_item* 
                                              int compressor, double tol, const psmma_opts* opts, int* ranks_out,
                                              psmma_batch_stats* stats, void* stream) {
   return batch_run(KIND_CAUCHY_EIG, count, items, alpha, beta, compressor, tol, opts, ranks_out, stats, stream);
+}
+
+extern "C" int psmma_toeplitz_batch_lowrank(int count, const psmma_batch_item* items, double alpha, double beta,
+                                            double tol, const psmma_opts* opts, int* ranks_out,
+                                            psmma_batch_stats* stats, void* stream) {
+  return batch_run(KIND_TOEPLITZ, count, items, alpha, beta, PSMMA_COMPRESS_RRQR, tol, opts, ranks_out, stats, stream);
 }
 
 extern "C" int psmma_tune_batch(int count, const psmma_batch_item* items, double alpha, double beta, int compressor,

@@ -22,9 +22,9 @@ enum Kind { KIND_CAUCHY = 0, KIND_TOEPLITZ = 1, KIND_HANKEL = 2, KIND_DFT = 3, K
 //             (CauchyHssEig.f90:1693-1774): with Dr = F(rows), Fc = F(cols), Fc1 = F(cols + 1),
 //             dl = DIFL(cols), dr = DIFR(cols) and global row <= global column (i - j <= diag_off):
 //             den = (Dr[i] - Fc[j]) - dl[j], else (Dr[i] - Fc1[j]) - dr[j]  (Fc1, dr: j < fc1_len)
-// Split path only: a Cauchy H with k1 > 0 has a tail of rows i >= k1, either dense
-// (B[(i-k1) + j*ldb]) or Cauchy with its own row generators (Dr2, Ur2 at i - k1) and the
-// same column generators.
+// Split path only: an H with k1 > 0 has a tail of rows i >= k1, either dense
+// (B[(i-k1) + j*ldb]; any kind) or, for Cauchy kinds, Cauchy with its own row generators
+// (Dr2, Ur2 at i - k1) and the same column generators.
 struct GenSpec {
   int kind = KIND_CAUCHY;
   const double *Dr = nullptr, *Ur = nullptr, *Fc = nullptr, *Vc = nullptr;

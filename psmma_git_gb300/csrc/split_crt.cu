@@ -324,10 +324,11 @@ __device__ __forceinline__ void h_pass1_blk(const GenSpec& gs, int K, int kp, do
           const bool upper = gs.rglob ? (__ldg(gs.rglob + kk) - 1 <= gs.cg0 + j) : (kk - j <= gs.diag_off);
           h = div_split(u * v, eig_den(fi, w, w1, dlj, drj, upper));
         }
-      } else if (KIND == KIND_TOEPLITZ) {
-        h = __ldg(gs.g + (gs.order - 1) + j - kk);
-      } else if (KIND == KIND_HANKEL) {
-        h = __ldg(gs.g + kk + j);
+      } else if (KIND == KIND_TOEPLITZ || KIND == KIND_HANKEL) {
+        if (gs.k1 > 0 && kk >= gs.k1)  // dense tail rows (the R P^T factor of a merged product)
+          h = __ldg(gs.B + (kk - gs.k1) + (long)j * gs.ldb);
+        else
+          h = KIND == KIND_TOEPLITZ ? __ldg(gs.g + (gs.order - 1) + j - kk) : __ldg(gs.g + kk + j);
       } else if (KIND == KIND_DENSE) {
         h = __ldg(gs.B + kk + (long)j * gs.ldb);
       } else {

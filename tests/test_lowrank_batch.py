@@ -191,3 +191,77 @@ def test_tuner_picks_a_configuration_and_results_stay_exact():
     for (A, g, _), (_, _, Qd) in zip(problems, dev):
         exact = A @ O.dense_h("cauchy", g, A.shape[0])
         assert O.rel_fro(Qd.cpu().numpy(), exact) < 1e-12
+
+
+# ---- Toeplitz merge level (PSTOEPLITZ_COMPUTE's low-rank branch, RRQR) ---------------------
+def _toeplitz_problems(sizes, seed=0, smooth=True):
+    out = []
+    for i, n in enumerate(sizes):
+        if smooth:  # H(i, j) = 1 / (j - i + 0.5 + s): Cauchy-like, numerically low-rank off the diagonal
+            s = 0.1 * ((seed + i) % 3)
+            g = 1.0 / (np.arange(2 * n - 1) - (n - 1) + 0.5 + s)
+        else:
+            g = O.cfg_vector(2 * n - 1, seed=seed + 10 * i)
+        A = O.cfg_matrix(n, n, seed=seed + 10 * i + 1)
+        Q0 = O.cfg_matrix(n, n, seed=seed + 10 * i + 2)
+        out.append((A, g, Q0))
+    return out
+
+
+def test_toeplitz_batch_argument_checks(lib):
+    items = (_lib.PsmmaBatchItem * 1)()
+    buf = np.zeros(16)
+    p = buf.ctypes.data
+    items[0].n, items[0].A, items[0].lda, items[0].gen, items[0].ldgen = 4, p, 4, p, 6  # G needs 2n - 1 = 7
+    items[0].Q, items[0].ldq = p, 4
+    f = lib.psmma_toeplitz_batch_lowrank
+    assert f(1, items, 1.0, 0.0, 1e-14, None, None, None, None) == _lib.PSMMA_EGEN
+    assert f(0, items, 1.0, 0.0, 1e-14, None, None, None, None) == 0
+
+
+def test_oracle_toeplitz_merge_level_matches_exact_product():
+    for smooth in [True, False]:
+        for (A, g, Q0) in _toeplitz_problems([2, 37, 300], seed=4, smooth=smooth):
+            n = A.shape[0]
+            Q, ranks = O.merge_level_product(A, g, Q0, 0.75, -0.5, "rrqr", 1e-14, kind="toeplitz")
+            ref = 0.75 * A @ O.dense_h("toeplitz", g, n) - 0.5 * Q0
+            assert O.rel_fro(Q, ref) < 1e-14
+
+
+def _run_toeplitz(problems, precision, alpha, beta, ld_pad=0):
+    import torch
+    from psmma_git_gb300 import fortran_empty, toeplitz_batch_lowrank
+    dev = []
+    for A, g, Q0 in problems:
+        n = A.shape[0]
+        Ad = fortran_empty(n, n, ld=n + ld_pad)
+        Ad.copy_(torch.from_numpy(A))
+        Qd = fortran_empty(n, n, ld=n + ld_pad)
+        Qd.copy_(torch.from_numpy(Q0))
+        dev.append((Ad, torch.from_numpy(np.ascontiguousarray(g)).cuda(), Qd))
+    ranks, info = toeplitz_batch_lowrank(dev, alpha, beta, tol=1e-14, precision=precision)
+    torch.cuda.synchronize()
+    return [Qd.cpu().numpy() for (_, _, Qd) in dev], ranks, info
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", ["fp64", "split"])
+def test_toeplitz_batch_matches_oracle_and_exact(prec):
+    problems = _toeplitz_problems([1, 2, 3, 37, 300, 515, 1031], seed=7) + _toeplitz_problems([200, 333], seed=9,
+                                                                                              smooth=False)
+    alpha, beta = 0.75, -0.5
+    Qs, ranks, info = _run_toeplitz(problems, prec, alpha, beta, ld_pad=2)
+    tol = 1e-13 if prec == "fp64" else 1e-12
+    k = 0
+    for (A, g, Q0), Qg in zip(problems, Qs):
+        n = A.shape[0]
+        Qo, ro = O.merge_level_product(A, g, Q0, alpha, beta, "rrqr", 1e-14, kind="toeplitz")
+        exact = alpha * A @ O.dense_h("toeplitz", g, n) + beta * Q0
+        rg = ranks[k:k + len(ro)]
+        k += len(ro)
+        for a, b in zip(rg, ro):
+            assert abs(a - b) <= 1 or min(a, b) >= 64, (n, rg, ro)  # full-rank tiles stop at the QR cap
+        assert O.rel_fro(Qg, exact) < tol, n
+        assert O.rel_fro(Qg, Qo) < tol, n
+    assert k == len(ranks) == info["n_blocks"]
+    assert info["full_rank_blocks"] >= 4  # the random generators do not compress
