@@ -764,16 +764,36 @@ def run_merge_level(args, ws, rank, local):
         F, U, V, dl, dr = O.eig_generators(n, seed=200 + i, tiny=n // 100)
         gen = torch.from_numpy(np.ascontiguousarray(np.stack([F, U, V, dl, dr]))).to(dev).t()
         eig_probs.append((probs[i][0], gen, probs[i][2]))
-    runs = [(c, p, False) for c in ["rrqr", "rrlu"] for p in precisions] + [(c, "split", True) for c in ["rrqr", "rrlu"]]
-    for comp, prec, eig in runs:
-        batch = eig_probs if eig else probs
+    # Toeplitz multiplies of the same sizes (PSTOEPLITZ_COMPUTE's low-rank branch, RRQR):
+    # H(i, j) = 1 / (j - i + 0.5), numerically low-rank off the diagonal blocks
+    toep_probs, toep_refs = [], {}
+    for i, n in enumerate(sizes):
+        g = torch.from_numpy(1.0 / (np.arange(2 * n - 1) - (n - 1) + 0.5)).to(dev)
+        toep_probs.append((probs[i][0], g, P.fortran_empty(n, n, torch.float64, dev)))
+    for i in check:
+        n = sizes[i]
+        R = P.fortran_empty(n, n, torch.float64, dev)
+        P.psmma_toeplitz(n, n, 1.0, toep_probs[i][0], toep_probs[i][1], 0.0, R)
+        toep_refs[i] = R
+    runs = ([(c, p, "cauchy") for c in ["rrqr", "rrlu"] for p in precisions] +
+            [(c, "split", "cauchyeig") for c in ["rrqr", "rrlu"]] + [("rrqr", "split", "toeplitz")])
+
+    def call(batch, kw, kind):
+        if kind == "toeplitz":
+            return P.toeplitz_batch_lowrank(batch, 1.0, 0.0, tol=kw["tol"], precision=kw["precision"],
+                                            n_moduli=kw["n_moduli"])
+        return P.cauchy_batch_lowrank(batch, 1.0, 0.0, **kw)
+
+    for comp, prec, kind in runs:
+        eig = kind == "cauchyeig"
+        batch = eig_probs if eig else toep_probs if kind == "toeplitz" else probs
         kw = dict(compressor=comp, tol=1e-14, precision=prec, n_moduli=args.n_moduli, eig=eig)
         tuned = None
-        if prec == "split" and not args.no_tune and not eig:
+        if prec == "split" and not args.no_tune and kind == "cauchy":
             tkw = {k: v for k, v in kw.items() if k != "eig"}
             tuned = P.tune_batch(probs, 1.0, 0.0, **tkw)  # untimed; later calls use its choice
         for _ in range(args.warmup if prec == "split" else 1):
-            ranks, info = P.cauchy_batch_lowrank(batch, 1.0, 0.0, **kw)
+            ranks, info = call(batch, kw, kind)
         torch.cuda.synchronize()
         steps = args.steps if prec == "split" else 1
         times = []
@@ -781,19 +801,22 @@ def run_merge_level(args, ws, rank, local):
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             torch.cuda.synchronize()
             e0.record()
-            ranks, info = P.cauchy_batch_lowrank(batch, 1.0, 0.0, **kw)
+            ranks, info = call(batch, kw, kind)
             e1.record()
             torch.cuda.synchronize()
             times.append(e0.elapsed_time(e1))
         if eig:
             err = None  # checked against the dense product by the tests (no dense eig reference here)
+        elif kind == "toeplitz":
+            err = max(float(torch.linalg.norm(toep_probs[i][2] - toep_refs[i]) / torch.linalg.norm(toep_refs[i]))
+                      for i in check)
         else:
             err = max(float(torch.linalg.norm(probs[i][2] - refs[i]) / torch.linalg.norm(refs[i]))
                       for i in check)
         # per-phase trace of one more call (eager launches, one event per phase)
         lib = P.load()
         lib.psmma_set_profiling(1)
-        P.cauchy_batch_lowrank(batch, 1.0, 0.0, **kw)
+        call(batch, kw, kind)
         torch.cuda.synchronize()
         ms = (C_float * 40)()
         names = (C_charp * 40)()
@@ -801,7 +824,7 @@ def run_merge_level(args, ws, rank, local):
         lib.psmma_set_profiling(0)
         phases = [[names[j].decode(), round(ms[j], 3)] for j in range(max(0, m))]
         t = statistics.median(times)
-        key = f"{comp}_{prec}" + ("_eig" if eig else "")
+        key = f"{comp}_{prec}" + ("_eig" if eig else "_toeplitz" if kind == "toeplitz" else "")
         out[key] = {
             "ms_per_step": t, "steps": steps, "effective_tflops": eff / t / 1e9,
             "executed_tflops": info["executed_flops"] / t / 1e9,
