@@ -17,6 +17,7 @@
 //   the 2x2 blocks [[Re F, -Im F], [Im F, Re F]].  F' tiles are generated from a table
 //   w^t, t = 0..n-1, indexed by the exact integer (j*l) mod n.
 #include "psmma_internal.h"
+#include "tcgen05_util.cuh"  // div_nr
 
 #include <vector>
 
@@ -151,11 +152,11 @@ __device__ __forceinline__ void gen_H_tile(double* Bs, const F64Args& p, int n0,
       if (KIND == KIND_CAUCHY) {
         double d = __ldg(p.gs.Dr + gk);               // D(i)
         double u = __ldg(p.gs.Ur + gk);               // U(i)
-        h = (u * colV) / (d - colF);                  // U(i)*V(j) / (D(i)-F(j))
+        h = div_nr(u * colV, d - colF);               // U(i)*V(j) / (D(i)-F(j))
       } else if (KIND == KIND_CAUCHY_EIG) {
         const double fi = __ldg(p.gs.Dr + gk), u = __ldg(p.gs.Ur + gk);
         const bool upper = p.gs.rglob ? (__ldg(p.gs.rglob + gk) - 1 <= p.gs.cg0 + gj) : (gk - gj <= p.gs.diag_off);
-        h = (u * colV) / eig_den(fi, colF, cg.F1, cg.dl, cg.dr, upper);
+        h = div_nr(u * colV, eig_den(fi, colF, cg.F1, cg.dl, cg.dr, upper));
       } else if (KIND == KIND_TOEPLITZ) {
         h = __ldg(p.gs.g + (p.gs.order - 1) + gj - gk);  // G(K + j - i), 1-based
       } else {
