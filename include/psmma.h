@@ -24,7 +24,9 @@
  *   DFT      the root of unity is implied by N, as in PZMDFTL (pzmdftL.f90:325-326).
  *
  * Entry points taking device pointers enqueue on `stream` (a cudaStream_t, NULL for the
- * legacy default stream) and return without synchronising.  The *_host entry points take
+ * legacy default stream) and return without synchronising.  Device-side failures of those
+ * calls (a bounded wait that gave up) are recorded per stream and returned by
+ * psmma_stream_status(stream).  The *_host entry points take
  * host pointers, copy to the device, run and copy back before returning; they are the
  * drop-in for the reference's host-array calls.
  *
@@ -399,6 +401,10 @@ size_t psmma_workspace_size(int kind, int n, int k, const psmma_opts* opts);
 
 /* Frees the library-owned workspace pools of the current device. */
 void psmma_release_workspace(void);
+
+/* Waits for `stream` and returns PSMMA_ETIMEDOUT if a split-path call enqueued on it since the
+ * last check recorded a device-side timeout (then clears the record), else PSMMA_OK. */
+int psmma_stream_status(void* stream);
 
 /* Per-phase tracing.  While enabled, each call records a CUDA event on its stream after
  * every phase (split path: row scales, H generation, parameters, A residues, H residues,

@@ -35,7 +35,7 @@ __all__ = [
     "psmma_cauchy", "psmma_toeplitz", "psmma_hankel", "pzmdftl", "pzmdftl1", "fortran_empty",
     "workspace_size", "PsmmaError", "PREC_FP64", "PREC_SPLIT", "load", "status_string",
     "make_opts", "psmma_cauchyeig", "cauchy_batch_lowrank", "batch_workspace_size", "tune_batch",
-    "toeplitz_batch_lowrank",
+    "toeplitz_batch_lowrank", "stream_status",
 ]
 
 # The split path (exact modular slices on the BF16 tensor cores) is built into the library.
@@ -173,6 +173,14 @@ def pzmdftl(n, k, alpha, B, beta, Cm, *, precision="fp64", n_moduli=0, stream=No
 def pzmdftl1(n, k, alpha, B, beta, Cm, *, precision="fp64", n_moduli=0, stream=None, work=None):
     """PZMDFTL1 (RRQR variant in the reference); the same exact product here."""
     return _dft("pzmdftl1", n, k, alpha, B, beta, Cm, stream, work, precision, n_moduli)
+
+
+def stream_status(stream=None) -> None:
+    """Waits for the stream and raises PsmmaError if a split-path call on it recorded a
+    device-side timeout since the last check (device-pointer calls return without waiting)."""
+    st = load().psmma_stream_status(_stream_ptr(stream))
+    if st != 0:
+        raise PsmmaError(st, "psmma_stream_status")
 
 
 def workspace_size(kind: int, n: int, k: int, precision="fp64", n_moduli: int = 0) -> int:

@@ -118,6 +118,7 @@ SIGNATURES = {
     "psmma_last_status": (_i, []),
     "psmma_workspace_size": (C.c_size_t, [_i, _i, _i, _op]),
     "psmma_release_workspace": (None, []),
+    "psmma_stream_status": (_i, [_p]),
     "psmma_status_string": (C.c_char_p, [_i]),
     "psmma_set_profiling": (None, [_i]),
     "psmma_profile_read": (_i, [C.POINTER(C.c_float), C.POINTER(C.c_char_p), _i]),

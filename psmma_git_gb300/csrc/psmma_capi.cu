@@ -9,6 +9,7 @@
 #include <utility>
 
 #include "psmma_internal.h"
+#include "tcgen05_util.cuh"  // DEV_ERR_TIMEOUT
 
 namespace psmma {
 
@@ -48,6 +49,33 @@ void* pool_get(size_t bytes, cudaStream_t stream, int* status, int slot) {
   }
   pl.bytes = want;
   return pl.ptr;
+}
+
+// ------------------------------------------------------------------------------------
+// Per-(device, stream) status words: the split path's asynchronous calls OR their device
+// status (DEV_ERR_TIMEOUT when a bounded wait gave up) into the word of their stream;
+// psmma_stream_status waits for the stream, reads and clears it.
+// ------------------------------------------------------------------------------------
+std::mutex g_stw_mu;
+std::map<std::pair<int, cudaStream_t>, unsigned*> g_stw;
+
+unsigned* stream_status_word(cudaStream_t stream) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+  std::lock_guard<std::mutex> lk(g_stw_mu);
+  auto it = g_stw.find({dev, stream});
+  if (it != g_stw.end()) return it->second;
+  unsigned* w = nullptr;
+  if (cudaMalloc(&w, 256) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (cudaMemsetAsync(w, 0, sizeof(unsigned), stream) != cudaSuccess) {
+    cudaFree(w);
+    return nullptr;
+  }
+  g_stw[{dev, stream}] = w;
+  return w;
 }
 
 // ------------------------------------------------------------------------------------
@@ -612,6 +640,27 @@ size_t psmma_workspace_size(int kind, int n, int k, const psmma_opts* opts) {
   if (o->precision == PSMMA_PREC_SPLIT) return split_workspace_bytes(kind, n, k, o->n_moduli);
   if (kind == KIND_DFT) return align256((size_t)n * sizeof(double2));
   return f64_splitk_bytes(n, k, k, std::max(1, device_sms()));
+}
+
+int psmma_stream_status(void* stream) {
+  cudaStream_t s = (cudaStream_t)stream;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return PSMMA_EDEVICE;
+  unsigned* w = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_stw_mu);
+    auto it = g_stw.find({dev, s});
+    if (it != g_stw.end()) w = it->second;
+  }
+  if (!w) return cudaStreamSynchronize(s) == cudaSuccess ? PSMMA_OK : PSMMA_EDEVICE;
+  unsigned h = 0;
+  if (cudaMemcpyAsync(&h, w, sizeof(h), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return PSMMA_EDEVICE;
+  if (h == 0) return PSMMA_OK;
+  if (cudaMemsetAsync(w, 0, sizeof(unsigned), s) != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess)
+    return PSMMA_EDEVICE;
+  return (h & DEV_ERR_TIMEOUT) ? PSMMA_ETIMEDOUT : PSMMA_EDEVICE;
 }
 
 void psmma_release_workspace(void) {

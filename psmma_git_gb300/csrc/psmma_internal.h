@@ -101,12 +101,20 @@ int launch_dft_table(double2* w, int n, cudaStream_t stream);
 
 // Split path (split_crt.cu).
 size_t split_workspace_bytes(int kind, int n, int k, int n_moduli);
+// wait_status: wait for the call and return its device status (for callers that must not
+// allocate); otherwise the status is ORed into the stream's status word (psmma_stream_status).
 int launch_split(int kind, int n, int k, double alpha, const double* A, long lda,
                  const double* gen, long ldgen, double beta, double* Q, long ldq, int n_moduli,
-                 void* work, size_t lwork, cudaStream_t stream);
+                 void* work, size_t lwork, cudaStream_t stream, bool wait_status = false);
+// The per-(device, stream) status word the asynchronous calls OR their device status into
+// (psmma_capi.cu; created on first use, NULL if that fails).
+unsigned* stream_status_word(cudaStream_t stream);
+// status_dev_out value asking the split path to wait for the call and return its status.
+static unsigned* const kStatusWait = reinterpret_cast<unsigned*>(1);
 // As launch_split, also for KIND_DFT (A = B and Q = C as interleaved complex, lda/ldq in
-// complex elements); with status_dev_out it does not synchronise (the device timeout flag
-// is copied there at the end of the stream's work).
+// complex elements).  status_dev_out: nullptr -> ORed into the stream's status word (no
+// synchronisation); kStatusWait -> wait and return it; any other pointer receives a copy of
+// the device timeout flag at the end of the stream's work (no synchronisation).
 int launch_split_any(int kind, int n, int k, double alpha, const double* A, long lda,
                      const double* gen, long ldgen, double beta, double* Q, long ldq, int n_moduli,
                      void* work, size_t lwork, cudaStream_t stream, unsigned* status_dev_out);

@@ -1312,15 +1312,24 @@ int launch_split_any(int kind, int n, int k, double alpha, const double* A, long
                      cudaStream_t stream, unsigned* status_dev_out);
 
 int launch_split(int kind, int n, int k, double alpha, const double* A, long lda, const double* gen, long ldgen,
-                 double beta, double* Q, long ldq, int n_moduli, void* work, size_t lwork, cudaStream_t stream) {
+                 double beta, double* Q, long ldq, int n_moduli, void* work, size_t lwork, cudaStream_t stream,
+                 bool wait_status) {
   return launch_split_any(kind, n, k, alpha, A, lda, gen, ldgen, beta, Q, ldq, n_moduli, work, lwork, stream,
-                          nullptr);
+                          wait_status ? kStatusWait : nullptr);
+}
+
+// The device status of a call ORed into the stream's status word.
+__global__ void k_status_or(unsigned* acc, const unsigned* st) {
+  const unsigned v = *st;
+  if (v) atomicOr(acc, v);
 }
 
 // Core of the split path: Q (M x N) = alpha * A' (M x K) * H (K x N) + beta * Q where A' is
 // A (column-major, lda) or, for the DFT, the embedding [Re B^T | Im B^T] of B (complex, lda),
 // H is generated from gs, and the output is column-major Q (ldq) or, for the DFT, the
-// interleaved complex C (ldq).  With status_dev_out it does not synchronise.
+// interleaved complex C (ldq).  Status: status_dev_out == nullptr ORs the call's device status
+// into the stream's status word (no synchronisation), kStatusWait waits and returns it, any other
+// pointer receives a copy of it (no synchronisation).
 static int split_core(int M, int N, int K, double alpha, const double* A, long lda, const GenSpec& gs, double beta,
                       double* Q, long ldq, int nmod, void* work, size_t lwork, cudaStream_t stream,
                       unsigned* status_dev_out) {
@@ -1410,13 +1419,21 @@ static int split_core(int M, int N, int K, double alpha, const double* A, long l
   prof_mark(stream, "crt_combine");
   if (cudaGetLastError() != cudaSuccess) return PSMMA_EDEVICE;
 
-  if (status_dev_out) {
+  if (status_dev_out && status_dev_out != kStatusWait) {
     if (cudaMemcpyAsync(status_dev_out, &b.prm->status, sizeof(unsigned), cudaMemcpyDeviceToDevice, stream) !=
         cudaSuccess)
       return PSMMA_EDEVICE;
     return PSMMA_OK;
   }
-  unsigned st = 0;
+  if (!status_dev_out) {
+    // asynchronous: the status joins the stream's word, reported by psmma_stream_status
+    unsigned* acc = stream_status_word(stream);
+    if (acc) {
+      k_status_or<<<1, 1, 0, stream>>>(acc, &b.prm->status);
+      return cudaGetLastError() == cudaSuccess ? PSMMA_OK : PSMMA_EDEVICE;
+    }
+  }
+  unsigned st = 0;  // kStatusWait (or no status word): wait for the call and read its status
   if (cudaMemcpyAsync(&st, &b.prm->status, sizeof(st), cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
       cudaStreamSynchronize(stream) != cudaSuccess)
     return PSMMA_EDEVICE;

@@ -77,5 +77,5 @@ extern "C" int psmma_cauchy_split_noalloc(int n, int k, double alpha, const doub
   void* work = noalloc_scratch(&st);
   if (st) return st;
   return launch_split(KIND_CAUCHY, n, k, alpha, A, lda, gen, ldgen, beta, Q, ldq, n_moduli, work,
-                      kNoAllocScratchBytes, (cudaStream_t)stream);
+                      kNoAllocScratchBytes, (cudaStream_t)stream, true);
 }

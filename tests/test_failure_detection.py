@@ -1,5 +1,6 @@
 """Failure detection without a GPU fault: a device-side wait that nothing releases must
 expire after its limit and come back as PSMMA_ETIMEDOUT, leaving the context usable."""
+import ctypes as C
 import time
 
 import numpy as np
@@ -49,3 +50,29 @@ def test_split_path_division_error_bound(lib, cuda):
     assert lib.psmma_selftest_division_split(1 << 26, 777, C.byref(mism), C.byref(ulp)) == 0
     # FP32 reciprocal seed, one FP64 Newton step, no residual correction: within 2^-44 relative
     assert ulp.value <= 256
+
+
+@pytest.mark.gpu
+def test_split_calls_report_device_status_per_stream(lib, cuda):
+    # device-pointer split calls enqueue and return; their device status joins the stream's word,
+    # which psmma_stream_status reads (clean after good calls) on that stream only
+    import torch
+    import psmma_git_gb300 as P
+    n = k = 512
+    A = O.cfg_matrix(n, k, seed=61)
+    gen = O.cfg_cauchy_generators(k, seed=62)
+    col = lambda x: torch.from_numpy(np.ascontiguousarray(np.asarray(x).T)).to(cuda).t()  # noqa: E731
+    s = torch.cuda.Stream()
+    dA, dg = col(A), col(gen)
+    torch.cuda.synchronize()
+    outs = []
+    with torch.cuda.stream(s):
+        for _ in range(3):
+            dQ = P.fortran_empty(n, k, torch.float64, cuda)
+            P.psmma_cauchy(n, k, 1.0, dA, dg, 0.0, dQ, precision="split", stream=s)
+            outs.append(dQ)
+    P.stream_status(s)  # waits; raises on a recorded timeout
+    assert lib.psmma_stream_status(C.c_void_p(s.cuda_stream)) == 0
+    ref = O.dense_product("cauchy", 1.0, A, gen, 0.0, None, k)
+    for dQ in outs:
+        assert O.rel_fro(dQ.cpu().numpy(), ref) < 1e-12
