@@ -1,5 +1,6 @@
 // Low-rank path of the batched merge level: compression of the off-diagonal blocks of Cauchy
-// matrices and the products that use the factors.
+// (and CAUCHYEIG) matrices by RRLU or RRQR, of Toeplitz matrices by RRQR, and the products
+// that use the factors.
 //
 // RRLU (rrluCauchy, Cauchylowrank.f90:7-134; pivoting helpers :137-296): structured
 // rank-revealing LU in generator space, one thread block per matrix block.  For a block

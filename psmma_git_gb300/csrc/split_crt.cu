@@ -8,8 +8,8 @@
 //   2. For pairwise coprime moduli m_1..m_N <= 256 the residues A' mod m_l and H' mod m_l
 //      lie in [-128, 128] and are exact in BF16.
 //   3. One BF16 GEMM per modulus gives Z_l = A'H' mod m_l.  FP32 accumulation is exact
-//      because the tensor memory accumulator is drained every 1024 k (|sum| <= 2^24) into a
-//      register-held residue.
+//      because the tensor memory accumulator is drained every 1024 k (|sum| <= 2^24) into
+//      register-held int32 sums, reduced modulo m_l every 16 chunks.
 //   4. Z = A'H' is recovered exactly by CRT (128-bit integer arithmetic, |Z| < 0.497 M with
 //      M = prod m_l), scaled back by 2^-(s_i+f_j) and combined with alpha and beta in FP64.
 // P is chosen on the device from the product bound |Z_ij| <= 2^(2P) * max_j(sum_k|H_kj| /
