@@ -60,6 +60,7 @@ struct CrtConsts {
   unsigned magic38[SPL_MAX_MODULI];    // ceil(2^38 / m)
   unsigned half[SPL_MAX_MODULI];
   unsigned hbase[SPL_MAX_MODULI];
+  int top32;                           // sum_l 255 * climb[l][3] < 2^32: top limb summed in 32 bits
 };
 
 // Device-side parameters of one call (in the workspace).
@@ -135,6 +136,7 @@ static CrtConsts make_consts(int nmod) {
     c.biasl[t] = 0;
     for (int l = 0; l < nmod; l++) c.biasl[t] += 128ull * c.climb[l][t];
   }
+  c.top32 = 2 * c.biasl[3] < (1ull << 32);  // 255 <= 2 * 128
   for (int l = 0; l < nmod; l++) {
     u128 C = ((u128)c.C_hi[l] << 64) | c.C_lo[l];
     long double cf = (long double)C / (long double)M;
@@ -1112,7 +1114,9 @@ constexpr int CRT_TI = 32, CRT_TJ = 128;
 
 // DFT_OUT: the product is [Re C^T | Im C^T] (rows = columns of C); element (i, j) goes to the
 // interleaved complex C at 2*(j mod nn) + (j >= nn) + i*ldq (ldq in doubles).
-template <bool DFT_OUT>
+// TOP32 (cc.top32): the sum over the moduli of (r_l + 128) times the top 32-bit limb of C_l
+// stays below 2^32 (true for M < 2^112: every top limb is below 2^16), so it is kept in 32 bits.
+template <bool DFT_OUT, bool TOP32 = false>
 __device__ __forceinline__ void crt_combine_blk(const int8_t* __restrict__ R, int n, int k, int kr,
                                                 const CrtConsts& cc, const unsigned long long* __restrict__ amax_bits,
                                                 const unsigned long long* __restrict__ hmax_bits,
@@ -1138,10 +1142,12 @@ __device__ __forceinline__ void crt_combine_blk(const int8_t* __restrict__ R, in
       const unsigned long long ab = amax_bits[i];
       const int sexp = (ab != 0 && ab < INF_BITS) ? scale_exp(ab, PA) : 0;
       unsigned long long acc[4][4];
+      unsigned acc3[4];
       int qi[4];
 #pragma unroll
       for (int c = 0; c < 4; ++c) {
         qi[c] = 0;
+        acc3[c] = 0;
 #pragma unroll
         for (int t = 0; t < 4; ++t) acc[c][t] = 0;
       }
@@ -1164,8 +1170,15 @@ __device__ __forceinline__ void crt_combine_blk(const int8_t* __restrict__ R, in
           acc[c][0] += (unsigned long long)ur * c0;
           acc[c][1] += (unsigned long long)ur * c1;
           acc[c][2] += (unsigned long long)ur * c2;
-          acc[c][3] += (unsigned long long)ur * c3;
+          if (TOP32)
+            acc3[c] += ur * c3;
+          else
+            acc[c][3] += (unsigned long long)ur * c3;
         }
+      }
+      if (TOP32) {
+#pragma unroll
+        for (int c = 0; c < 4; ++c) acc[c][3] = acc3[c];
       }
 #pragma unroll
       for (int c = 0; c < 4; ++c) {
@@ -1230,14 +1243,14 @@ __device__ __forceinline__ void crt_combine_blk(const int8_t* __restrict__ R, in
   }
 }
 
-template <bool DFT_OUT>
+template <bool DFT_OUT, bool TOP32>
 __global__ void __launch_bounds__(256, 3) k_crt_combine(const int8_t* __restrict__ R, int n, int k, int kr,
                                                      CrtConsts cc, const unsigned long long* __restrict__ amax_bits,
                                                      const unsigned long long* __restrict__ hmax_bits,
                                                      const SplitDevParams* prm, double alpha, double beta,
                                                      double* __restrict__ Q, long ldq, int by0) {
-  crt_combine_blk<DFT_OUT>(R, n, k, kr, cc, amax_bits, hmax_bits, prm, alpha, beta, Q, ldq, blockIdx.x,
-                           by0 + blockIdx.y);
+  crt_combine_blk<DFT_OUT, TOP32>(R, n, k, kr, cc, amax_bits, hmax_bits, prm, alpha, beta, Q, ldq, blockIdx.x,
+                                  by0 + blockIdx.y);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -1411,11 +1424,11 @@ static int split_core(int M, int N, int K, double alpha, const double* A, long l
 
   dim3 gc((N + CRT_TJ - 1) / CRT_TJ, (M + CRT_TI - 1) / CRT_TI);
   if (!dft)
-    k_crt_combine<false><<<gc, dim3(32, 8), 0, stream>>>(b.R, M, N, L.kr, cc, b.amax, b.hmax, b.prm, alpha, beta, Q, ldq,
-                                                         0);
+    (cc.top32 ? k_crt_combine<false, true> : k_crt_combine<false, false>)<<<gc, dim3(32, 8), 0, stream>>>(
+        b.R, M, N, L.kr, cc, b.amax, b.hmax, b.prm, alpha, beta, Q, ldq, 0);
   else
-    k_crt_combine<true><<<gc, dim3(32, 8), 0, stream>>>(b.R, M, N, L.kr, cc, b.amax, b.hmax, b.prm, alpha, beta, Q,
-                                                        2 * ldq, 0);
+    (cc.top32 ? k_crt_combine<true, true> : k_crt_combine<true, false>)<<<gc, dim3(32, 8), 0, stream>>>(
+        b.R, M, N, L.kr, cc, b.amax, b.hmax, b.prm, alpha, beta, Q, 2 * ldq, 0);
   prof_mark(stream, "crt_combine");
   if (cudaGetLastError() != cudaSuccess) return PSMMA_EDEVICE;
 
@@ -1545,8 +1558,8 @@ static int split_core_host(int M, int N, int K, double alpha, const double* A_h,
     k_crt_gemm<G_BN, OneGemm><<<std::min(sms, total_tiles), G_THREADS, Shape::SMEM, s>>>(og);
     const int r0 = t0 * G_BM, r1 = std::min(M, t1 * G_BM);
     dim3 gc((N + CRT_TJ - 1) / CRT_TJ, (r1 - r0 + CRT_TI - 1) / CRT_TI);
-    k_crt_combine<false><<<gc, dim3(32, 8), 0, s>>>(b.R, M, N, L.kr, cc, b.amax, b.hmax, b.prm, alpha, beta, dQ, M,
-                                                     r0 / CRT_TI);
+    (cc.top32 ? k_crt_combine<false, true> : k_crt_combine<false, false>)<<<gc, dim3(32, 8), 0, s>>>(
+        b.R, M, N, L.kr, cc, b.amax, b.hmax, b.prm, alpha, beta, dQ, M, r0 / CRT_TI);
     ok &= cudaEventRecord(ev_panel[p], s) == cudaSuccess;
     ok &= cudaStreamWaitEvent(cs, ev_panel[p], 0) == cudaSuccess;
     ok &= cudaMemcpy2DAsync(Q_h + r0, (size_t)ldq_h * 8, dQ + r0, (size_t)M * 8, (size_t)(r1 - r0) * 8, (size_t)N,
@@ -1713,10 +1726,11 @@ __global__ void __launch_bounds__(128) k_g_residues_H(const GProb* d, int count,
   residues_H_blk(e.Ht, e.N, e.kp, e.hmax, e.prm, cc, e.RH, local % gx, local / gx);
 }
 
+template <bool TOP32>
 __global__ void __launch_bounds__(256, 3) k_g_crt_combine(const GProb* d, int count, CrtConsts cc) {
   const GProb& e = d[gfind<4>(d, count, blockIdx.x)];
   const int local = blockIdx.x - e.b_crt, gx = (e.N + CRT_TJ - 1) / CRT_TJ;
-  crt_combine_blk<false>(e.R, e.M, e.N, e.kr, cc, e.amax, e.hmax, e.prm, e.alpha, e.beta, e.Q, e.ldq, local % gx,
+  crt_combine_blk<false, TOP32>(e.R, e.M, e.N, e.kr, cc, e.amax, e.hmax, e.prm, e.alpha, e.beta, e.Q, e.ldq, local % gx,
                          local / gx);
 }
 
@@ -1907,7 +1921,8 @@ int split_group_enqueue(const SplitGroup& g, cudaStream_t stream, unsigned* stat
   if (!st) st = launch_group_gemm<64>(g, 1, cc, sms, stream);
   prof_mark(stream, "g_gemm_64");
   if (st) return st;
-  k_g_crt_combine<<<g.blocks_crt, dim3(32, 8), 0, stream>>>(d, g.count, cc);
+  (cc.top32 ? k_g_crt_combine<true> : k_g_crt_combine<false>)<<<g.blocks_crt, dim3(32, 8), 0, stream>>>(d, g.count,
+                                                                                                      cc);
   prof_mark(stream, "g_crt_combine");
   if (cudaGetLastError() != cudaSuccess) return PSMMA_EDEVICE;
   if (status_out &&
