@@ -162,7 +162,7 @@ static SplitLayout split_layout(int M, int K, int N, int nmod) {
   L.kp = (K + 63) / 64 * 64;
   L.kr = (N + 255) / 256 * 256;
   size_t o = 0;
-  L.off_params = o; o += al1k(sizeof(SplitDevParams));
+  L.off_params = o; o += al1k(2 * sizeof(SplitDevParams));  // the call's parameters, then guessed PA/PH
   L.off_amax = o;   o += al1k((size_t)M * 8);
   L.off_hmax = o;   o += al1k((size_t)N * 8);
   L.off_hsum = o;   o += al1k((size_t)N * 8);
@@ -659,6 +659,19 @@ __global__ void k_residues_A(const double* __restrict__ A, long lda, int n, int 
                              const unsigned long long* __restrict__ amax_bits, const SplitDevParams* prm,
                              CrtConsts cc, __nv_bfloat16* __restrict__ RA) {
   residues_A_blk(A, lda, nullptr, 0, k, n, k, kp, amax_bits, prm, cc, RA, blockIdx.x, blockIdx.y);
+}
+
+// Rows [32 by0, 32 (by0 + gridDim.y)) of A only (a row panel of the host pipeline).
+__global__ void k_residues_A_rows(const double* __restrict__ A, long lda, int n, int k, int kp,
+                                  const unsigned long long* __restrict__ amax_bits, const SplitDevParams* prm,
+                                  CrtConsts cc, __nv_bfloat16* __restrict__ RA, int by0) {
+  residues_A_blk(A, lda, nullptr, 0, k, n, k, kp, amax_bits, prm, cc, RA, blockIdx.x, by0 + blockIdx.y);
+}
+
+// The guessed bit counts that a speculative host pipeline scales with.
+__global__ void k_guess_params(SplitDevParams* g, int PA, int PH) {
+  g->PA = PA;
+  g->PH = PH;
 }
 
 // RH[l][j][kk] = residues of H' (bf16) from Ht[j][kk]; one thread per 4 consecutive kk.
@@ -1297,6 +1310,7 @@ static CrtConsts get_consts(int nmod) {
 
 struct SplitBuffers {
   SplitDevParams* prm;
+  SplitDevParams* prm_guess;  // PA/PH of a speculative host pipeline (only those two fields are read)
   unsigned long long *amax, *hmax;
   double *hsum, *asq, *hsq, *Ht;
   double2* wtab;
@@ -1307,6 +1321,7 @@ struct SplitBuffers {
 static SplitBuffers split_buffers(char* w, const SplitLayout& L) {
   SplitBuffers b;
   b.prm = (SplitDevParams*)(w + L.off_params);
+  b.prm_guess = b.prm + 1;
   b.amax = (unsigned long long*)(w + L.off_amax);
   b.hmax = (unsigned long long*)(w + L.off_hmax);
   b.hsum = (double*)(w + L.off_hsum);
@@ -1406,7 +1421,7 @@ static int split_core(int M, int N, int K, double alpha, const double* A, long l
   ga.nkb = L.kp / G_BK;
   ga.tiles_m = (M + G_BM - 1) / G_BM;
   ga.tiles_n = (N + G_BN - 1) / G_BN;
-  ga.group_m = 12;
+  ga.group_m = 16;
   ga.R = b.R;
   ga.status = &b.prm->status;
   for (int l = 0; l < nmod; ++l) { ga.m[l] = cc.m[l]; ga.inv_m[l] = cc.inv_m[l]; }
@@ -1455,38 +1470,49 @@ static int split_core(int M, int N, int K, double alpha, const double* A, long l
 }
 
 // Host-pointer multiply with the copies overlapped (pinned host memory makes them
-// asynchronous).  A (host, column-major, lda_h) goes up in column chunks on the copy stream
-// `cs` while H is generated on `s`; each chunk's row maxima / norms start as soon as it has
-// landed.  After the parameter and residue passes the modular GEMM and the CRT run in row
-// panels of whole 128-row tiles, and each finished panel of Q goes back to the host on `cs`
-// while the next panel multiplies.  dA (M x K) and dQ (M x N) are device buffers with leading
-// dimension M; Q is read from the host first when beta != 0.  Synchronises both streams.
-// The H residues need PH, which the parameter pass sets from A's statistics as well; with a
-// guess (the PH a previous call of the same shape chose) they are computed while A is still
-// being uploaded and recomputed after the parameter pass only if the guess was wrong.
-// *ph_out receives the PH this call used.
+// asynchronous).  dA (M x K) and dQ (M x N) are device buffers with leading dimension M; Q is
+// read from the host first when beta != 0.  Synchronises both streams.  The modular GEMM and
+// the CRT run in row panels of whole 128-row tiles, and each finished panel of Q goes back to
+// the host on the copy stream `cs` while the next panel multiplies.  Two ways to get A up:
+//  - without guesses (or beta != 0): A goes up in column chunks while H is generated on `s`;
+//    each chunk's row maxima / norms start as soon as it has landed, and the residue passes
+//    wait for the parameter pass.  The H residues need PH, which the parameter pass sets from
+//    A's statistics as well; with ph_guess (the PH a previous call of the same shape chose)
+//    they are computed while A is still being uploaded and recomputed after the parameter
+//    pass only if the guess was wrong.
+//  - with pa_guess and ph_guess (beta == 0): A goes up in the GEMM's row panels of whole rows,
+//    and each panel's row maxima, residues (scaled with the guessed PA), GEMM and CRT start as
+//    soon as its rows have landed, so the upload hides behind the H passes and the products.
+//    The parameter pass runs last; if its PA or PH differs from the guesses, the residues,
+//    products and downloads are redone with the computed ones (A is resident by then), so
+//    the result is always the one the computed parameters give.
+// *pa_out / *ph_out receive the PA / PH of the call.
 static int split_core_host(int M, int N, int K, double alpha, const double* A_h, long lda_h, double* dA,
                            const GenSpec& gs, double beta, double* Q_h, long ldq_h, double* dQ, int nmod, void* work,
-                           size_t lwork, cudaStream_t s, cudaStream_t cs, cudaEvent_t* ev, int nev, int ph_guess,
-                           int* ph_out) {
+                           size_t lwork, cudaStream_t s, cudaStream_t cs, cudaEvent_t* ev, int nev, int pa_guess,
+                           int ph_guess, int* pa_out, int* ph_out) {
   if (gs.kind == KIND_DFT) return PSMMA_EUNSUPPORTED;
   if (nmod < 8 || nmod > SPL_MAX_MODULI) return PSMMA_EUNSUPPORTED;
   if (K >= (1 << 24) || M >= (1 << 30) || N >= (1 << 30)) return PSMMA_EUNSUPPORTED;
   constexpr int NCH = 4, NP = 8;  // A column chunks, GEMM / CRT / download row panels
-  if (nev < NCH + NP + 3) return PSMMA_EUNSUPPORTED;
+  if (nev < 2 * NP + 3) return PSMMA_EUNSUPPORTED;
+  static_assert(NCH <= NP, "column chunks and row panels share the upload events");
   SplitLayout L = split_layout(M, K, N, nmod);
   if (lwork < L.total || !work) return PSMMA_EWORKSPACE;
   char* w = (char*)work;
   const SplitBuffers b = split_buffers(w, L);
   const CrtConsts cc = get_consts(nmod);
-  cudaEvent_t* ev_chunk = ev;            // NCH
-  cudaEvent_t* ev_panel = ev + NCH;      // NP
-  cudaEvent_t ev_start = ev[NCH + NP], ev_q = ev[NCH + NP + 1], ev_done = ev[NCH + NP + 2];
+  const bool spec = pa_guess >= 8 && ph_guess >= 8 && beta == 0.0;
+  cudaEvent_t* ev_up = ev;               // NP: column chunks or row panels of A landed
+  cudaEvent_t* ev_panel = ev + NP;       // NP: panels of Q ready
+  cudaEvent_t ev_start = ev[2 * NP], ev_q = ev[2 * NP + 1], ev_done = ev[2 * NP + 2];
   bool ok = true;
   // the copy stream starts after everything already queued on s
   ok &= cudaEventRecord(ev_start, s) == cudaSuccess;
   ok &= cudaStreamWaitEvent(cs, ev_start, 0) == cudaSuccess;
+  prof_begin(s);
   ok &= cudaMemsetAsync(w, 0, L.off_wtab, s) == cudaSuccess;
+  if (spec) k_guess_params<<<1, 1, 0, s>>>(b.prm_guess, pa_guess, ph_guess);
   // ---- H side (needs no A)
   switch (gs.kind) {
     case KIND_CAUCHY: k_h_pass1<KIND_CAUCHY><<<N, 256, 0, s>>>(gs, K, L.kp, b.Ht, b.hmax, b.hsum, b.hsq, b.prm); break;
@@ -1498,31 +1524,7 @@ static int split_core_host(int M, int N, int K, double alpha, const double* A_h,
   const dim3 grh(rh_blocks_x(L.kp), N);
   if (ph_guess >= 8)
     k_residues_H_spec<<<grh, 128, 0, s>>>(b.Ht, N, L.kp, b.hmax, b.prm, cc, b.RH, ph_guess, 0);
-  // ---- A in column chunks (multiples of the 1024-column row-norm chunk)
-  const int kchunk = 1024;
-  const int cols_per = std::max(kchunk, (K + NCH * kchunk - 1) / (NCH * kchunk) * kchunk);
-  for (int ch = 0; ch < NCH; ++ch) {
-    const int c0 = ch * cols_per, c1 = std::min(K, c0 + cols_per);
-    if (c0 >= c1) break;
-    ok &= cudaMemcpy2DAsync(dA + (size_t)c0 * M, (size_t)M * 8, A_h + (size_t)c0 * lda_h, (size_t)lda_h * 8,
-                            (size_t)M * 8, (size_t)(c1 - c0), cudaMemcpyHostToDevice, cs) == cudaSuccess;
-    ok &= cudaEventRecord(ev_chunk[ch], cs) == cudaSuccess;
-    ok &= cudaStreamWaitEvent(s, ev_chunk[ch], 0) == cudaSuccess;
-    dim3 g1((M + 127) / 128, (c1 - c0 + kchunk - 1) / kchunk);
-    k_row_absmax<<<g1, 128, 0, s>>>(dA + (size_t)c0 * M, M, M, c1 - c0, kchunk, b.amax, b.asq);
-  }
-  if (beta != 0.0) {
-    ok &= cudaMemcpy2DAsync(dQ, (size_t)M * 8, Q_h, (size_t)ldq_h * 8, (size_t)M * 8, (size_t)N,
-                            cudaMemcpyHostToDevice, cs) == cudaSuccess;
-    ok &= cudaEventRecord(ev_q, cs) == cudaSuccess;
-  }
-  if (!ok) return PSMMA_EDEVICE;
-  k_split_params<<<PARAMS_BLOCKS, 512, 0, s>>>(b.prm, cc.log2M, M, N, K, b.amax, b.asq, b.hmax, b.hsq);
-  k_residues_A<<<dim3(L.kp / 64, (M + 31) / 32), 256, 0, s>>>(dA, M, M, K, L.kp, b.amax, b.prm, cc, b.RA);
-  if (ph_guess >= 8)
-    k_residues_H_spec<<<grh, 128, 0, s>>>(b.Ht, N, L.kp, b.hmax, b.prm, cc, b.RH, ph_guess, 1);
-  else
-    k_residues_H<<<grh, 128, 0, s>>>(b.Ht, N, L.kp, b.hmax, b.prm, cc, b.RH);
+  prof_mark(s, "h_side");
 
   OneGemm og;
   memset(&og, 0, sizeof(og));
@@ -1533,7 +1535,7 @@ static int split_core_host(int M, int N, int K, double alpha, const double* A_h,
   ga.kr = L.kr;
   ga.nkb = L.kp / G_BK;
   ga.tiles_n = (N + G_BN - 1) / G_BN;
-  ga.group_m = 12;
+  ga.group_m = 16;
   ga.R = b.R;
   ga.status = &b.prm->status;
   ga.nmod = nmod;
@@ -1547,11 +1549,11 @@ static int split_core_host(int M, int N, int K, double alpha, const double* A_h,
     return PSMMA_EDEVICE;
   const int tiles_m = (M + G_BM - 1) / G_BM;
   const int tiles_per = (tiles_m + NP - 1) / NP;
-  static_assert(G_BM % CRT_TI == 0, "row panels must cover whole CRT blocks");
-  if (beta != 0.0 && cudaStreamWaitEvent(s, ev_q, 0) != cudaSuccess) return PSMMA_EDEVICE;
-  for (int p = 0; p < NP; ++p) {
+  static_assert(G_BM % CRT_TI == 0 && G_BM % 32 == 0, "row panels must cover whole CRT and residue blocks");
+  const int kchunk = 1024;
+  // GEMM + CRT of panel p (rows [r0, r1)) with the bit counts in *pk, then its download
+  auto panel = [&](int p, const SplitDevParams* pk) {
     const int t0 = p * tiles_per, t1 = std::min(tiles_m, t0 + tiles_per);
-    if (t0 >= t1) break;
     ga.tm0 = t0;
     ga.tiles_m = t1 - t0;
     const int total_tiles = ga.tiles_m * ga.tiles_n * nmod;
@@ -1559,25 +1561,97 @@ static int split_core_host(int M, int N, int K, double alpha, const double* A_h,
     const int r0 = t0 * G_BM, r1 = std::min(M, t1 * G_BM);
     dim3 gc((N + CRT_TJ - 1) / CRT_TJ, (r1 - r0 + CRT_TI - 1) / CRT_TI);
     (cc.top32 ? k_crt_combine<false, true> : k_crt_combine<false, false>)<<<gc, dim3(32, 8), 0, s>>>(
-        b.R, M, N, L.kr, cc, b.amax, b.hmax, b.prm, alpha, beta, dQ, M, r0 / CRT_TI);
+        b.R, M, N, L.kr, cc, b.amax, b.hmax, pk, alpha, beta, dQ, M, r0 / CRT_TI);
+    prof_mark(s, "panel_gemm_crt");
     ok &= cudaEventRecord(ev_panel[p], s) == cudaSuccess;
     ok &= cudaStreamWaitEvent(cs, ev_panel[p], 0) == cudaSuccess;
     ok &= cudaMemcpy2DAsync(Q_h + r0, (size_t)ldq_h * 8, dQ + r0, (size_t)M * 8, (size_t)(r1 - r0) * 8, (size_t)N,
                             cudaMemcpyDeviceToHost, cs) == cudaSuccess;
-  }
-  if (cudaGetLastError() != cudaSuccess) ok = false;
+  };
+  const int npanels = (tiles_m + tiles_per - 1) / tiles_per;
+  // the parameters, then the caller's view of them once both streams are done
   SplitDevParams head;  // status, PA, PH
-  ok &= cudaMemcpyAsync(&head, b.prm, offsetof(SplitDevParams, rho_bits), cudaMemcpyDeviceToHost, s) == cudaSuccess;
-  ok &= cudaEventRecord(ev_done, cs) == cudaSuccess;
-  ok &= cudaStreamSynchronize(s) == cudaSuccess;
-  ok &= cudaEventSynchronize(ev_done) == cudaSuccess;
+  auto finish = [&]() {
+    if (cudaGetLastError() != cudaSuccess) ok = false;
+    ok &= cudaMemcpyAsync(&head, b.prm, offsetof(SplitDevParams, rho_bits), cudaMemcpyDeviceToHost, s) == cudaSuccess;
+    ok &= cudaEventRecord(ev_done, cs) == cudaSuccess;
+    ok &= cudaStreamSynchronize(s) == cudaSuccess;
+    ok &= cudaEventSynchronize(ev_done) == cudaSuccess;
+  };
+
+  if (spec) {
+    // ---- A in row panels: each panel is multiplied as soon as its rows have landed (all
+    // uploads are queued on the copy stream ahead of the downloads)
+    for (int p = 0; p < npanels; ++p) {
+      const int r0 = p * tiles_per * G_BM, r1 = std::min(M, (p + 1) * tiles_per * G_BM);
+      ok &= cudaMemcpy2DAsync(dA + r0, (size_t)M * 8, A_h + r0, (size_t)lda_h * 8, (size_t)(r1 - r0) * 8,
+                              (size_t)K, cudaMemcpyHostToDevice, cs) == cudaSuccess;
+      ok &= cudaEventRecord(ev_up[p], cs) == cudaSuccess;
+    }
+    for (int p = 0; p < npanels; ++p) {
+      const int r0 = p * tiles_per * G_BM, r1 = std::min(M, (p + 1) * tiles_per * G_BM);
+      ok &= cudaStreamWaitEvent(s, ev_up[p], 0) == cudaSuccess;
+      dim3 g1((r1 - r0 + 127) / 128, (K + kchunk - 1) / kchunk);
+      k_row_absmax<<<g1, 128, 0, s>>>(dA + r0, M, r1 - r0, K, kchunk, b.amax + r0, b.asq + r0);
+      k_residues_A_rows<<<dim3(L.kp / 64, (r1 - r0 + 31) / 32), 256, 0, s>>>(dA, M, M, K, L.kp, b.amax,
+                                                                             b.prm_guess, cc, b.RA, r0 / 32);
+      prof_mark(s, "panel_rows");
+      panel(p, b.prm_guess);
+    }
+    k_split_params<<<PARAMS_BLOCKS, 512, 0, s>>>(b.prm, cc.log2M, M, N, K, b.amax, b.asq, b.hmax, b.hsq);
+    finish();
+    if (!ok) return PSMMA_EDEVICE;
+    if (head.status & DEV_ERR_TIMEOUT) return PSMMA_ETIMEDOUT;
+    if (pa_out) *pa_out = head.PA;
+    if (ph_out) *ph_out = head.PH;
+    if (head.PA == pa_guess && head.PH == ph_guess) return PSMMA_OK;
+    // a wrong guess: everything after the parameter pass again, with the computed bit counts
+    k_residues_A<<<dim3(L.kp / 64, (M + 31) / 32), 256, 0, s>>>(dA, M, M, K, L.kp, b.amax, b.prm, cc, b.RA);
+    k_residues_H<<<grh, 128, 0, s>>>(b.Ht, N, L.kp, b.hmax, b.prm, cc, b.RH);
+    ok &= cudaEventRecord(ev_start, s) == cudaSuccess;
+    ok &= cudaStreamWaitEvent(cs, ev_start, 0) == cudaSuccess;
+    for (int p = 0; p < npanels; ++p) panel(p, b.prm);
+    finish();
+    if (!ok) return PSMMA_EDEVICE;
+    return (head.status & DEV_ERR_TIMEOUT) ? PSMMA_ETIMEDOUT : PSMMA_OK;
+  }
+
+  // ---- A in column chunks (multiples of the 1024-column row-norm chunk)
+  const int cols_per = std::max(kchunk, (K + NCH * kchunk - 1) / (NCH * kchunk) * kchunk);
+  for (int ch = 0; ch < NCH; ++ch) {
+    const int c0 = ch * cols_per, c1 = std::min(K, c0 + cols_per);
+    if (c0 >= c1) break;
+    ok &= cudaMemcpy2DAsync(dA + (size_t)c0 * M, (size_t)M * 8, A_h + (size_t)c0 * lda_h, (size_t)lda_h * 8,
+                            (size_t)M * 8, (size_t)(c1 - c0), cudaMemcpyHostToDevice, cs) == cudaSuccess;
+    ok &= cudaEventRecord(ev_up[ch], cs) == cudaSuccess;
+    ok &= cudaStreamWaitEvent(s, ev_up[ch], 0) == cudaSuccess;
+    dim3 g1((M + 127) / 128, (c1 - c0 + kchunk - 1) / kchunk);
+    k_row_absmax<<<g1, 128, 0, s>>>(dA + (size_t)c0 * M, M, M, c1 - c0, kchunk, b.amax, b.asq);
+  }
+  if (beta != 0.0) {
+    ok &= cudaMemcpy2DAsync(dQ, (size_t)M * 8, Q_h, (size_t)ldq_h * 8, (size_t)M * 8, (size_t)N,
+                            cudaMemcpyHostToDevice, cs) == cudaSuccess;
+    ok &= cudaEventRecord(ev_q, cs) == cudaSuccess;
+  }
   if (!ok) return PSMMA_EDEVICE;
+  prof_mark(s, "a_upload_rows");
+  k_split_params<<<PARAMS_BLOCKS, 512, 0, s>>>(b.prm, cc.log2M, M, N, K, b.amax, b.asq, b.hmax, b.hsq);
+  k_residues_A<<<dim3(L.kp / 64, (M + 31) / 32), 256, 0, s>>>(dA, M, M, K, L.kp, b.amax, b.prm, cc, b.RA);
+  if (ph_guess >= 8)
+    k_residues_H_spec<<<grh, 128, 0, s>>>(b.Ht, N, L.kp, b.hmax, b.prm, cc, b.RH, ph_guess, 1);
+  else
+    k_residues_H<<<grh, 128, 0, s>>>(b.Ht, N, L.kp, b.hmax, b.prm, cc, b.RH);
+  prof_mark(s, "params_residues");
+  if (beta != 0.0 && cudaStreamWaitEvent(s, ev_q, 0) != cudaSuccess) return PSMMA_EDEVICE;
+  for (int p = 0; p < npanels; ++p) panel(p, b.prm);
+  finish();
+  if (!ok) return PSMMA_EDEVICE;
+  if (pa_out) *pa_out = head.PA;
   if (ph_out) *ph_out = head.PH;
   if (head.status & DEV_ERR_TIMEOUT) return PSMMA_ETIMEDOUT;
   return PSMMA_OK;
 }
 
-// PH chosen by the last overlapped host call of each shape (the speculation's guess).
 struct PhKey {
   int M, N, K, kind, nmod;
   bool operator<(const PhKey& o) const {
@@ -1585,26 +1659,26 @@ struct PhKey {
   }
 };
 static std::mutex g_ph_mu;
-static std::map<PhKey, int> g_ph;
+static std::map<PhKey, std::pair<int, int>> g_ph;  // (PA, PH) of the last call of the shape
 
 static int split_core_host_cached(int M, int N, int K, double alpha, const double* A_h, long lda_h, double* dA,
                                   const GenSpec& gs, double beta, double* Q_h, long ldq_h, double* dQ, int nmod,
                                   void* work, size_t lwork, cudaStream_t s, cudaStream_t cs, cudaEvent_t* ev,
                                   int nev) {
   const PhKey key{M, N, K, gs.kind, nmod};
-  int guess = -1;
+  int pa_guess = -1, ph_guess = -1;
   {
     std::lock_guard<std::mutex> lk(g_ph_mu);
     auto it = g_ph.find(key);
-    if (it != g_ph.end()) guess = it->second;
+    if (it != g_ph.end()) std::tie(pa_guess, ph_guess) = it->second;
   }
-  int ph = -1;
+  int pa = -1, ph = -1;
   const int st = split_core_host(M, N, K, alpha, A_h, lda_h, dA, gs, beta, Q_h, ldq_h, dQ, nmod, work, lwork, s, cs,
-                                 ev, nev, guess, &ph);
-  if (!st && ph >= 8) {
+                                 ev, nev, pa_guess, ph_guess, &pa, &ph);
+  if (!st && pa >= 8 && ph >= 8) {
     std::lock_guard<std::mutex> lk(g_ph_mu);
     if (g_ph.size() > 256) g_ph.clear();
-    g_ph[key] = ph;
+    g_ph[key] = {pa, ph};
   }
   return st;
 }

@@ -103,3 +103,20 @@ def test_host_split_speculation_survives_changing_inputs():
         P.psmma_cauchy(n, k, 1.0, col(A), col(gen), 0.0, dQ, precision="split")
         torch.cuda.synchronize()
         assert O.rel_fro(Qh, dQ.cpu().numpy()) < 1e-13
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", ["cauchy", "toeplitz", "hankel"])
+def test_host_split_row_panels_repeat_ragged(kind):
+    # repeated calls of one shape upload A in row panels and scale with the previous call's
+    # PA / PH (ragged last panel: 1000 rows = 7 full 128-row tiles + 104 rows); fresh operands
+    # of the same statistics each call, plus one call with a different scale of A
+    import psmma_git_gb300 as P
+    n, k = 1000, 777
+    gen = np.asfortranarray(_gen(kind, k, 61))
+    for seed, scale in [(62, 1.0), (63, 1.0), (64, 1.0), (65, 2.0 ** 40), (66, 2.0 ** 40)]:
+        A = scale * O.cfg_matrix(n, k, seed=seed)
+        Qh = np.full((n, k), np.nan, order="F")
+        getattr(P, "psmma_" + kind)(n, k, 1.0, np.asfortranarray(A), gen, 0.0, Qh, precision="split")
+        exact = O.dense_product(kind, 1.0, A, gen, 0.0, None, k)
+        assert O.rel_fro(Qh, exact) < 1e-12
