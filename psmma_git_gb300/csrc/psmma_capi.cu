@@ -267,10 +267,10 @@ struct HostArena {
   size_t bytes = 0;
   cudaStream_t stream = nullptr;
   cudaStream_t copy = nullptr;  // host<->device copies of the overlapped split path
-  cudaEvent_t ev[24] = {};
+  cudaEvent_t ev[28] = {};
   bool have_ev = false;
 };
-constexpr int kHostEvents = 24;
+constexpr int kHostEvents = 28;
 std::mutex g_host_mu;
 std::map<int, HostArena> g_host;
 

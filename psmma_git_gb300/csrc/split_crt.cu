@@ -43,23 +43,18 @@ struct CrtConsts {
   int nmod;
   int m[SPL_MAX_MODULI];
   float inv_m[SPL_MAX_MODULI];
-  int c21[SPL_MAX_MODULI];  // 2^21 mod m
-  int c42[SPL_MAX_MODULI];  // 2^42 mod m
+  float mf[SPL_MAX_MODULI];   // m as a float
+  float g23[SPL_MAX_MODULI];  // 2^23 mod m, symmetric (|g| <= m/2)
+  float g38[SPL_MAX_MODULI];  // 2^38 mod m, symmetric
   unsigned long long C_lo[SPL_MAX_MODULI], C_hi[SPL_MAX_MODULI];  // CRT basis C_l < M
   float f[SPL_MAX_MODULI];                                        // C_l / M
   unsigned long long M_lo, M_hi;
   double log2M;
-  unsigned magic[SPL_MAX_MODULI];      // floor(2^32 / m): Barrett reduction of t < 2^30
   unsigned climb[SPL_MAX_MODULI][4];   // C_l as four 32-bit limbs
   unsigned bias[4];                    // 128 * sum_l C_l mod 2^128 (residues enter offset by 128)
   int ffix[SPL_MAX_MODULI];            // round(2^19 * C_l / M): fixed-point quotient estimate
   unsigned long long biasl[4];         // sum_l 128 * climb[l][t], per limb, unreduced
   unsigned Mlimb[4];                   // M as four 32-bit limbs
-  // residue pass: exact Barrett division of t < 2^30 (q = umulhi(t, magic38) >> 6),
-  // h = floor(m/2) and the float bits 0x4B400000 - h of the symmetric shift
-  unsigned magic38[SPL_MAX_MODULI];    // ceil(2^38 / m)
-  unsigned half[SPL_MAX_MODULI];
-  unsigned hbase[SPL_MAX_MODULI];
   int top32;                           // sum_l 255 * climb[l][3] < 2^32: top limb summed in 32 bits
 };
 
@@ -102,8 +97,10 @@ static CrtConsts make_consts(int nmod) {
     int m = kModuli[l];
     c.m[l] = m;
     c.inv_m[l] = 1.0f / (float)m;
-    c.c21[l] = (int)((1LL << 21) % m);
-    c.c42[l] = (int)(((1ULL << 42) % (unsigned long long)m));
+    c.mf[l] = (float)m;
+    const int g23 = (int)((1LL << 23) % m), g38 = (int)((1LL << 38) % m);
+    c.g23[l] = (float)(g23 > m / 2 ? g23 - m : g23);
+    c.g38[l] = (float)(g38 > m / 2 ? g38 - m : g38);
     u128 Ml = M / (u128)m;
     long long Ml_mod = (long long)(Ml % (u128)m);
     long long y = inv_mod(Ml_mod, m);
@@ -119,13 +116,6 @@ static CrtConsts make_consts(int nmod) {
   c.log2M = l2 - 1e-9;
   u128 bias = 0;
   for (int l = 0; l < nmod; l++) {
-    c.magic[l] = (unsigned)((1ULL << 32) / (unsigned long long)kModuli[l]);
-    // ceil(2^38/m) * m - 2^38 < m <= 256, so t * magic38 / 2^38 < t/m + 2^-8 for t < 2^30:
-    // the floor is exact because frac(t/m) <= 1 - 1/m <= 1 - 2^-8 (equality only for m = 256,
-    // where the error term is 0)
-    c.magic38[l] = (unsigned)(((1ULL << 38) + kModuli[l] - 1) / (unsigned long long)kModuli[l]);
-    c.half[l] = (unsigned)(kModuli[l] >> 1);
-    c.hbase[l] = 0x4B400000u - c.half[l];
     u128 C = ((u128)c.C_hi[l] << 64) | c.C_lo[l];
     for (int t = 0; t < 4; t++) c.climb[l][t] = (unsigned)(C >> (32 * t));
     bias += (u128)128 * C;  // wraps modulo 2^128
@@ -552,34 +542,47 @@ __device__ __forceinline__ unsigned long long scaled_int(double x, int e, bool* 
   return q;
 }
 
-// Residues of two neighbouring integers for every modulus, packed as bf16x2 into planes.
-// For x = x2*2^42 + x1*2^21 + x0 (< 2^53) and modulus m with h = floor(m/2):
-// t = x2*(2^42 mod m) + x1*(2^21 mod m) + x0 + h < 2^30, r = t mod m by exact Barrett
-// division (q = umulhi(t, ceil(2^38/m)) >> 6), and r - h is the symmetric residue of x in
-// [-h, m-1-h].  Its BF16 value, with the sign of x applied, is one FMA on the 1.5*2^23 magic
-// number (exact for integers of magnitude <= 2^8): fma(float(0x4B400000 - h + r), sign,
-// -1.5*2^23*sign).  The modulus loop is unrolled over the maximum count, so the per-modulus
+// Residues of neighbouring integers for every modulus, on the FP32 pipe.  A scaled integer
+// x < 2^53 with sign s is cut into x0 = x mod 2^23, x1 = (x >> 23) mod 2^15 and x2 = x >> 38
+// (< 2^15); the signed chunks s*x_i are exact floats.  With g1 = 2^23 mod m and g2 = 2^38 mod m
+// taken symmetric (|g| <= m/2 <= 128), t = s*x0 + g1*s*x1 + g2*s*x2 is congruent to s*x modulo
+// m and |t| < 2^23 + 2*128*2^15 = 2^24, so both FMAs are exact.  q = rint(t * fl(1/m)) comes from
+// one FMA on the magic number 1.5*2^23 (|t*fl(1/m) - t/m| <= |t|/m * 2^-24 < 1/m), and
+// r = t - q*m is one exact FMA with |r| < m/2 + 1, i.e. |r| <= 128 for every modulus <= 256
+// (1/m is exact for m = 256).  An integer of at most 8 significant bits is its own BF16: the
+// float's upper half.  The modulus loop is unrolled over the maximum count, so the per-modulus
 // constants are kernel-parameter operands.
+struct ResidueChunks {
+  float c0, c1, c2;
+};
+
+__device__ __forceinline__ ResidueChunks residue_chunks(unsigned long long u, bool neg) {
+  const float s = neg ? -1.0f : 1.0f, o = neg ? 8388608.0f : -8388608.0f;
+  const unsigned lo = (unsigned)u, hi = (unsigned)(u >> 32);
+  const unsigned x0 = lo & 0x7FFFFFu;
+  const unsigned x1 = __funnelshift_r(lo, hi, 23) & 0x7FFFu;
+  const unsigned x2 = hi >> 6;
+  ResidueChunks c;
+  c.c0 = fmaf(__uint_as_float(0x4B000000u | x0), s, o);  // s * (2^23 + x0) - s * 2^23
+  c.c1 = fmaf(__uint_as_float(0x4B000000u | x1), s, o);
+  c.c2 = fmaf(__uint_as_float(0x4B000000u | x2), s, o);
+  return c;
+}
+
+__device__ __forceinline__ unsigned residue_bits(const ResidueChunks& c, float g23, float g38, float inv, float mf) {
+  const float t = fmaf(c.c2, g38, fmaf(c.c1, g23, c.c0));
+  const float q = fmaf(t, inv, 12582912.0f) - 12582912.0f;
+  return __float_as_uint(fmaf(-q, mf, t));
+}
+
 __device__ __forceinline__ void write_residue_pair(unsigned long long u0, bool n0, unsigned long long u1, bool n1,
                                                    const CrtConsts& cc, uint32_t* dst, size_t plane_words) {
-  const unsigned a0 = (unsigned)(u0 & 0x1FFFFFull), a1 = (unsigned)((u0 >> 21) & 0x1FFFFFull),
-                 a2 = (unsigned)(u0 >> 42);
-  const unsigned b0 = (unsigned)(u1 & 0x1FFFFFull), b1 = (unsigned)((u1 >> 21) & 0x1FFFFFull),
-                 b2 = (unsigned)(u1 >> 42);
-  const float s0 = n0 ? -1.0f : 1.0f, s1 = n1 ? -1.0f : 1.0f;
-  const float o0 = -12582912.0f * s0, o1 = -12582912.0f * s1;
+  const ResidueChunks a = residue_chunks(u0, n0), b = residue_chunks(u1, n1);
 #pragma unroll
   for (int l = 0; l < SPL_MAX_MODULI; ++l) {
     if (l < cc.nmod) {
-      const unsigned m = (unsigned)cc.m[l], mg = cc.magic38[l], c21 = (unsigned)cc.c21[l],
-                     c42 = (unsigned)cc.c42[l], h = cc.half[l], hb = cc.hbase[l];
-      const unsigned t0 = a2 * c42 + a1 * c21 + a0 + h;
-      const unsigned t1 = b2 * c42 + b1 * c21 + b0 + h;
-      const unsigned r0 = t0 - (__umulhi(t0, mg) >> 6) * m;
-      const unsigned r1 = t1 - (__umulhi(t1, mg) >> 6) * m;
-      const float f0 = fmaf(__uint_as_float(hb + r0), s0, o0);
-      const float f1 = fmaf(__uint_as_float(hb + r1), s1, o1);
-      *dst = __byte_perm(__float_as_uint(f0), __float_as_uint(f1), 0x7632);
+      const float g23 = cc.g23[l], g38 = cc.g38[l], inv = cc.inv_m[l], mf = cc.mf[l];
+      *dst = __byte_perm(residue_bits(a, g23, g38, inv, mf), residue_bits(b, g23, g38, inv, mf), 0x7632);
       dst += plane_words;
     }
   }
@@ -588,28 +591,16 @@ __device__ __forceinline__ void write_residue_pair(unsigned long long u0, bool n
 // The same for four neighbouring integers: one 8-byte store per plane.
 __device__ __forceinline__ void write_residue_quad(const unsigned long long (&u)[4], const bool (&ng)[4],
                                                    const CrtConsts& cc, uint2* dst, size_t plane_u2) {
-  unsigned x0[4], x1[4], x2[4];
-  float sg[4], of[4];
+  ResidueChunks c[4];
 #pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    x0[q] = (unsigned)(u[q] & 0x1FFFFFull);
-    x1[q] = (unsigned)((u[q] >> 21) & 0x1FFFFFull);
-    x2[q] = (unsigned)(u[q] >> 42);
-    sg[q] = ng[q] ? -1.0f : 1.0f;
-    of[q] = -12582912.0f * sg[q];
-  }
+  for (int q = 0; q < 4; ++q) c[q] = residue_chunks(u[q], ng[q]);
 #pragma unroll
   for (int l = 0; l < SPL_MAX_MODULI; ++l) {
     if (l < cc.nmod) {
-      const unsigned m = (unsigned)cc.m[l], mg = cc.magic38[l], c21 = (unsigned)cc.c21[l],
-                     c42 = (unsigned)cc.c42[l], h = cc.half[l], hb = cc.hbase[l];
+      const float g23 = cc.g23[l], g38 = cc.g38[l], inv = cc.inv_m[l], mf = cc.mf[l];
       unsigned f[4];
 #pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const unsigned t = x2[q] * c42 + x1[q] * c21 + x0[q] + h;
-        const unsigned r = t - (__umulhi(t, mg) >> 6) * m;
-        f[q] = __float_as_uint(fmaf(__uint_as_float(hb + r), sg[q], of[q]));
-      }
+      for (int q = 0; q < 4; ++q) f[q] = residue_bits(c[q], g23, g38, inv, mf);
       *dst = make_uint2(__byte_perm(f[0], f[1], 0x7632), __byte_perm(f[2], f[3], 0x7632));
       dst += plane_u2;
     }
@@ -620,18 +611,21 @@ __device__ __forceinline__ void write_residue_quad(const unsigned long long (&u)
 constexpr int RH_PER_THREAD = 4;
 __host__ __device__ __forceinline__ int rh_blocks_x(int kp) { return (kp / RH_PER_THREAD + 127) / 128; }
 
-// RA[l][i][kk] = residues of A' (bf16), rows i, K-major.  Block: 32 rows x 64 k.
+// RA[l][i][kk] = residues of A' (bf16), rows i, K-major.  Block: 32 rows x 64 k, transposed
+// through shared memory with element (k, r) at column (r + k/4) mod 32 of row k, so that both
+// the column-wise writes (32 rows of one k) and the reads (16 threads, 4 consecutive k each, of
+// one row) touch 16 distinct 8-byte bank pairs per half-warp.
 __device__ __forceinline__ void residues_A_blk(const double* __restrict__ A, long lda, const double* A2, long lda2,
                                                int ka, int n, int k, int kp,
                                                const unsigned long long* __restrict__ amax_bits,
                                                const SplitDevParams* prm, const CrtConsts& cc,
                                                __nv_bfloat16* __restrict__ RA, int bx, int by) {
-  __shared__ double tile[64][33];
+  __shared__ double tile[64][32];
   const int i0 = by * 32, k0 = bx * 64;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 256 threads: 8 x 32
   for (int kk = ty; kk < 64; kk += 8) {
     int gi = i0 + tx, gk = k0 + kk;
-    tile[kk][tx] = (gi < n && gk < k) ? __ldg(acol(A, lda, A2, lda2, ka, gk) + gi) : 0.0;
+    tile[kk][(tx + (kk >> 2)) & 31] = (gi < n && gk < k) ? __ldg(acol(A, lda, A2, lda2, ka, gk) + gi) : 0.0;
   }
   __syncthreads();
   const int P = prm->PA;
@@ -649,7 +643,7 @@ __device__ __forceinline__ void residues_A_blk(const double* __restrict__ A, lon
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       ng[q] = false;
-      u[q] = ok ? scaled_int(tile[kk + q][r], e, &ng[q]) : 0ull;
+      u[q] = ok ? scaled_int(tile[kk + q][(r + tq) & 31], e, &ng[q]) : 0ull;
     }
     write_residue_quad(u, ng, cc, (uint2*)(RA + (size_t)gi * kp + k0 + kk), plane / 4);
   }
@@ -1135,7 +1129,9 @@ __device__ __forceinline__ void crt_combine_blk(const int8_t* __restrict__ R, in
                                                 const unsigned long long* __restrict__ hmax_bits,
                                                 const SplitDevParams* prm, double alpha, double beta,
                                                 double* __restrict__ Q, long ldq, int bx, int by) {
-  __shared__ double tile[CRT_TJ][CRT_TI + 1];
+  // element (jl, il) of the tile at column (il + jl/4) mod 32 of row jl: the row-wise writes
+  // (4 columns per thread) and the column-wise reads both hit distinct bank pairs
+  __shared__ double tile[CRT_TJ][CRT_TI];
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int i0 = by * CRT_TI, j0 = bx * CRT_TJ;
   const int PA = prm->PA, PH = prm->PH;
@@ -1221,7 +1217,7 @@ __device__ __forceinline__ void crt_combine_blk(const int8_t* __restrict__ R, in
       }
     }
 #pragma unroll
-    for (int c = 0; c < 4; ++c) tile[4 * tx + c][il] = val[c];
+    for (int c = 0; c < 4; ++c) tile[4 * tx + c][(il + tx) & 31] = val[c];
   }
   __syncthreads();
   const bool scale = alpha != 1.0, accumulate = beta != 0.0;  // uniform: decided once
@@ -1231,7 +1227,7 @@ __device__ __forceinline__ void crt_combine_blk(const int8_t* __restrict__ R, in
       const int jl = ty + 8 * b, jj = j0 + jl;
       if (i < n && jj < k) {
         double* qp = Q + i + (long)jj * ldq;
-        double v = tile[jl][tx];
+        double v = tile[jl][(tx + (jl >> 2)) & 31];
         if (scale) v *= alpha;
         if (accumulate) v = fma(beta, *qp, v);
         *qp = v;
@@ -1247,7 +1243,7 @@ __device__ __forceinline__ void crt_combine_blk(const int8_t* __restrict__ R, in
         const int jj = jb + c;
         if (jj >= k) continue;
         double* qp = Q + (long)i * ldq + 2 * (jj < nn ? jj : jj - nn) + (jj >= nn ? 1 : 0);
-        double v = tile[4 * tx + c][il];
+        double v = tile[4 * tx + c][(il + tx) & 31];
         if (scale) v *= alpha;
         if (accumulate) v = fma(beta, *qp, v);
         *qp = v;
@@ -1494,7 +1490,11 @@ static int split_core_host(int M, int N, int K, double alpha, const double* A_h,
   if (gs.kind == KIND_DFT) return PSMMA_EUNSUPPORTED;
   if (nmod < 8 || nmod > SPL_MAX_MODULI) return PSMMA_EUNSUPPORTED;
   if (K >= (1 << 24) || M >= (1 << 30) || N >= (1 << 30)) return PSMMA_EUNSUPPORTED;
-  constexpr int NCH = 4, NP = 8;  // A column chunks, GEMM / CRT / download row panels
+  // A column chunks; GEMM / CRT / download row panels: eighths of the row tiles, the first
+  // one cut to two row tiles (its pitched upload runs beside the H passes' HBM traffic and
+  // gates the first product) and the last one cut in three (the download left after the last
+  // product is short)
+  constexpr int NCH = 4, NP = 12;
   if (nev < 2 * NP + 3) return PSMMA_EUNSUPPORTED;
   static_assert(NCH <= NP, "column chunks and row panels share the upload events");
   SplitLayout L = split_layout(M, K, N, nmod);
@@ -1548,12 +1548,28 @@ static int split_core_host(int M, int N, int K, double alpha, const double* A_h,
   if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
     return PSMMA_EDEVICE;
   const int tiles_m = (M + G_BM - 1) / G_BM;
-  const int tiles_per = (tiles_m + NP - 1) / NP;
+  int pb[NP + 1], npanels = 0;  // panel p: row tiles [pb[p], pb[p + 1])
+  {
+    const int tp = (tiles_m + 7) / 8;
+    pb[0] = 0;
+    if (tp >= 4 && tiles_m > tp) {
+      pb[1] = 2;
+      pb[2] = tp;
+      npanels = 2;
+    }
+    while (tiles_m - pb[npanels] > tp) { pb[npanels + 1] = pb[npanels] + tp; ++npanels; }
+    for (int rest = tiles_m - pb[npanels], cut = 0; rest > 0; ++cut) {
+      const int t = cut < 2 ? (rest + 1) / 2 : rest;
+      pb[npanels + 1] = pb[npanels] + t;
+      ++npanels;
+      rest -= t;
+    }
+  }
   static_assert(G_BM % CRT_TI == 0 && G_BM % 32 == 0, "row panels must cover whole CRT and residue blocks");
   const int kchunk = 1024;
   // GEMM + CRT of panel p (rows [r0, r1)) with the bit counts in *pk, then its download
   auto panel = [&](int p, const SplitDevParams* pk) {
-    const int t0 = p * tiles_per, t1 = std::min(tiles_m, t0 + tiles_per);
+    const int t0 = pb[p], t1 = pb[p + 1];
     ga.tm0 = t0;
     ga.tiles_m = t1 - t0;
     const int total_tiles = ga.tiles_m * ga.tiles_n * nmod;
@@ -1568,12 +1584,13 @@ static int split_core_host(int M, int N, int K, double alpha, const double* A_h,
     ok &= cudaMemcpy2DAsync(Q_h + r0, (size_t)ldq_h * 8, dQ + r0, (size_t)M * 8, (size_t)(r1 - r0) * 8, (size_t)N,
                             cudaMemcpyDeviceToHost, cs) == cudaSuccess;
   };
-  const int npanels = (tiles_m + tiles_per - 1) / tiles_per;
   // the parameters, then the caller's view of them once both streams are done
   SplitDevParams head;  // status, PA, PH
   auto finish = [&]() {
     if (cudaGetLastError() != cudaSuccess) ok = false;
     ok &= cudaMemcpyAsync(&head, b.prm, offsetof(SplitDevParams, rho_bits), cudaMemcpyDeviceToHost, s) == cudaSuccess;
+    prof_mark(s, "params_head");
+    prof_mark(cs, "q_download_tail");  // on the copy stream: the end of the last download
     ok &= cudaEventRecord(ev_done, cs) == cudaSuccess;
     ok &= cudaStreamSynchronize(s) == cudaSuccess;
     ok &= cudaEventSynchronize(ev_done) == cudaSuccess;
@@ -1583,13 +1600,13 @@ static int split_core_host(int M, int N, int K, double alpha, const double* A_h,
     // ---- A in row panels: each panel is multiplied as soon as its rows have landed (all
     // uploads are queued on the copy stream ahead of the downloads)
     for (int p = 0; p < npanels; ++p) {
-      const int r0 = p * tiles_per * G_BM, r1 = std::min(M, (p + 1) * tiles_per * G_BM);
+      const int r0 = pb[p] * G_BM, r1 = std::min(M, pb[p + 1] * G_BM);
       ok &= cudaMemcpy2DAsync(dA + r0, (size_t)M * 8, A_h + r0, (size_t)lda_h * 8, (size_t)(r1 - r0) * 8,
                               (size_t)K, cudaMemcpyHostToDevice, cs) == cudaSuccess;
       ok &= cudaEventRecord(ev_up[p], cs) == cudaSuccess;
     }
     for (int p = 0; p < npanels; ++p) {
-      const int r0 = p * tiles_per * G_BM, r1 = std::min(M, (p + 1) * tiles_per * G_BM);
+      const int r0 = pb[p] * G_BM, r1 = std::min(M, pb[p + 1] * G_BM);
       ok &= cudaStreamWaitEvent(s, ev_up[p], 0) == cudaSuccess;
       dim3 g1((r1 - r0 + 127) / 128, (K + kchunk - 1) / kchunk);
       k_row_absmax<<<g1, 128, 0, s>>>(dA + r0, M, r1 - r0, K, kchunk, b.amax + r0, b.asq + r0);
