@@ -141,6 +141,28 @@ def max_over_ranks(x: float, ws: int, device=None) -> float:
     return _max(x)
 
 
+def link_rates(h_buf, dev, nbytes: int = 512 << 20) -> dict:
+    """Pinned host<->device copy rates (GB/s, best of 3) over the first nbytes of h_buf."""
+    import torch
+    h = h_buf.reshape(-1)[: nbytes // h_buf.element_size()]
+    d = torch.empty_like(h, device=dev)
+    out = {}
+    for name, fn in (("h2d", lambda: d.copy_(h, non_blocking=True)),
+                     ("d2h", lambda: h.copy_(d, non_blocking=True))):
+        best = float("inf")
+        for _ in range(3):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record()
+            fn()
+            e1.record()
+            torch.cuda.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        out[name] = round(h.numel() * h.element_size() / (best * 1e-3) / 1e9, 1)
+    del d
+    return out
+
+
 def cpu_inputs(n: int, seed_gen: int = 0, seed_a: int = 1):
     import numpy as np
     from oracle import psmma_oracle as O
@@ -327,15 +349,28 @@ def run_gpu(args, ws, rank, local):
             del A, Q
             torch.cuda.empty_cache()
             P.psmma_cauchy(n, k, 1.0, nA, nG, 0.0, nQ, precision="split", n_moduli=args.n_moduli)
-            e2e_steps = max(1, min(args.steps, 5))
+            e2e_steps = max(1, min(args.steps, 10))
+            call_ms = []
             t0 = time.perf_counter()
             for _ in range(e2e_steps):
+                t1 = time.perf_counter()
                 P.psmma_cauchy(n, k, 1.0, nA, nG, 0.0, nQ, precision="split", n_moduli=args.n_moduli)
+                call_ms.append(round((time.perf_counter() - t1) * 1e3, 2))
             te = (time.perf_counter() - t0) / e2e_steps
             result["e2e"] = {"value": flops_rank / te / 1e12, "unit": "TFLOP/s",
                              "h2d_bytes_per_step": n * k * 8 + 4 * k * 8, "d2h_bytes_per_step": n * k * 8,
-                             "ms_per_step": te * 1e3, "steps": e2e_steps,
+                             "ms_per_step": te * 1e3, "steps": e2e_steps, "call_ms": call_ms,
                              "api": "psmma_cauchy_host (pinned host buffers)"}
+            # after the timed calls: one traced call (library-stream phases) and the pinned
+            # copy rate of this host link, which bound the end-to-end time from below
+            lib.psmma_set_profiling(1)
+            P.psmma_cauchy(n, k, 1.0, nA, nG, 0.0, nQ, precision="split", n_moduli=args.n_moduli)
+            ms = (C_float * 40)()
+            names = (C_charp * 40)()
+            m = lib.psmma_profile_read(ms, names, 40)
+            lib.psmma_set_profiling(0)
+            result["e2e"]["phases_ms"] = [[names[j].decode(), round(ms[j], 3)] for j in range(max(0, m))]
+            result["e2e"]["link_gbs"] = link_rates(hA, dev)
             e2e_done = True
         # ---------------- CPU baseline + oracle panel ----------------
         if not args.no_cpu:

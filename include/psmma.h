@@ -427,9 +427,10 @@ int psmma_selftest_wait_timeout(unsigned long long limit_ns);
  * returns the number of results that differ and the largest difference in ulp. */
 int psmma_selftest_division(long long count, unsigned long long seed, unsigned long long* mismatches,
                             int* max_ulp);
-/* The same check for the split path's H generation (FP32 reciprocal seed, one FP64 Newton step,
- * no residual correction): max_ulp bounds its error (the split path is designed for about
- * 2^-45 relative; the test allows 2^-44, 256 ulp). */
+/* The same check for the split path's H entries u*v/(d-w) (double-float arithmetic on the FP32
+ * pipe, with an FP32-seeded FP64 Newton division for operands outside its range): max_ulp
+ * bounds the error against the IEEE quotient of the rounded product (the split path is
+ * designed for about 2^-45 relative; the test allows 2^-44, 256 ulp). */
 int psmma_selftest_division_split(long long count, unsigned long long seed, unsigned long long* mismatches,
                                   int* max_ulp);
 

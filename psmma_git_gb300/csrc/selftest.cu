@@ -42,8 +42,8 @@ extern "C" int psmma_selftest_wait_timeout(unsigned long long limit_ns) {
 }
 
 // ------------------------------------------------------------------------------------------
-// Self-check of div_nr (FP64-exact quotients) and div_split (the split path's Cauchy entries)
-// against the IEEE division on
+// Self-check of div_nr (FP64-exact quotients) and cauchy_entry (the split path's Cauchy entries
+// u*v/x, double-float with div_split for operands outside its range) against the IEEE division on
 // count seeded pairs: Cauchy-like operands u*v / (d - w) with |d - w| log-uniform in
 // [1e-13, 1], plus arbitrary finite bit patterns (which exercise the fallback).
 // ------------------------------------------------------------------------------------------
@@ -65,9 +65,10 @@ __global__ void k_selftest_div(long long count, unsigned long long seed, unsigne
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < count;
        t += (long long)gridDim.x * blockDim.x) {
     unsigned long long s = seed ^ (0xD1B54A32D192ED03ull * (unsigned long long)(t + 1));
-    double a, x;
+    double a, x, u = 1.0, v = 1.0;
     if ((t & 7) != 7) {
-      const double u = 8.0 * unit(splitmix(s)) - 4.0, v = 8.0 * unit(splitmix(s)) - 4.0;
+      u = 8.0 * unit(splitmix(s)) - 4.0;
+      v = 8.0 * unit(splitmix(s)) - 4.0;
       const double d = unit(splitmix(s));
       const double gap = exp2(-43.2 * unit(splitmix(s)));  // 1e-13 .. 1
       const double w = (splitmix(s) & 1) ? d - gap : d + gap;
@@ -79,9 +80,10 @@ __global__ void k_selftest_div(long long count, unsigned long long seed, unsigne
       bx &= ~(0x7ffull << 52) | (((bx >> 3) % 2046ull + 1) << 52);
       a = __longlong_as_double((long long)ba);
       x = __longlong_as_double((long long)bx);
+      u = a;
     }
     if (x == 0.0) continue;
-    const double q0 = a / x, q1 = SPLIT ? div_split(a, x) : div_nr(a, x);
+    const double q0 = a / x, q1 = SPLIT ? cauchy_entry(u, v, v_split(v), x) : div_nr(a, x);
     if (__double_as_longlong(q0) != __double_as_longlong(q1)) {
       ++local;
       const long long d = __double_as_longlong(q0) - __double_as_longlong(q1);

@@ -277,9 +277,12 @@ __device__ __forceinline__ void h_pass1_blk(const GenSpec& gs, int K, int kp, do
                                             unsigned long long* __restrict__ hmax_bits, double* __restrict__ hsum,
                                             double* __restrict__ hsq, SplitDevParams* prm, int j) {
   double w = 0.0, v = 0.0, w1 = 0.0, dlj = 0.0, drj = 0.0;
+  VSplit vs;
+  vs.ok = false;
   if (KIND == KIND_CAUCHY || KIND == KIND_CAUCHY_EIG) {
     w = __ldg(gs.Fc + j);   // F(j)
     v = __ldg(gs.Vc + j);   // V(j)
+    vs = v_split(v);
   }
   if (KIND == KIND_CAUCHY_EIG) {
     dlj = __ldg(gs.dl + j);  // DIFL(j)
@@ -299,22 +302,22 @@ __device__ __forceinline__ void h_pass1_blk(const GenSpec& gs, int K, int kp, do
       if (KIND == KIND_CAUCHY) {
         if (gs.k1 > 0 && kk >= gs.k1) {
           const int t = kk - gs.k1;  // tail rows: dense, or Cauchy with the second row generators
-          h = gs.B ? __ldg(gs.B + t + (long)j * gs.ldb) : div_split(__ldg(gs.Ur2 + t) * v, __ldg(gs.Dr2 + t) - w);
+          h = gs.B ? __ldg(gs.B + t + (long)j * gs.ldb) : cauchy_entry(__ldg(gs.Ur2 + t), v, vs, __ldg(gs.Dr2 + t) - w);
         } else {
           double d = __ldg(gs.Dr + kk), u = __ldg(gs.Ur + kk);
-          h = div_split(u * v, d - w);     // U(i)*V(j) / (D(i)-F(j))
+          h = cauchy_entry(u, v, vs, d - w);  // U(i)*V(j) / (D(i)-F(j))
         }
       } else if (KIND == KIND_CAUCHY_EIG) {
         if (gs.k1 > 0 && kk >= gs.k1) {
           // tail rows of merged products: dense, or CauchyEig rows in permuted order
           const int t = kk - gs.k1;
           h = gs.B ? __ldg(gs.B + t + (long)j * gs.ldb)
-                   : div_split(__ldg(gs.Ur2 + t) * v,
-                            eig_den(__ldg(gs.Dr2 + t), w, w1, dlj, drj, __ldg(gs.rglob2 + t) - 1 <= gs.cg0 + j));
+                   : cauchy_entry(__ldg(gs.Ur2 + t), v, vs,
+                                  eig_den(__ldg(gs.Dr2 + t), w, w1, dlj, drj, __ldg(gs.rglob2 + t) - 1 <= gs.cg0 + j));
         } else {
           const double fi = __ldg(gs.Dr + kk), u = __ldg(gs.Ur + kk);
           const bool upper = gs.rglob ? (__ldg(gs.rglob + kk) - 1 <= gs.cg0 + j) : (kk - j <= gs.diag_off);
-          h = div_split(u * v, eig_den(fi, w, w1, dlj, drj, upper));
+          h = cauchy_entry(u, v, vs, eig_den(fi, w, w1, dlj, drj, upper));
         }
       } else if (KIND == KIND_TOEPLITZ || KIND == KIND_HANKEL) {
         if (gs.k1 > 0 && kk >= gs.k1)  // dense tail rows (the R P^T factor of a merged product)
@@ -513,9 +516,16 @@ __global__ void k_split_params(SplitDevParams* prm, double log2M, int n, int nco
   }
 }
 
+// floor(log2 x) from the bits of a positive finite double, on the integer pipe (GB300's FP64
+// pipe is narrow, and the library ilogb goes through it).
+__device__ __forceinline__ int ilogb_bits(unsigned long long b) {
+  const int ex = (int)(b >> 52);
+  return ex ? ex - 1023 : 63 - __clzll((long long)b) - 1074;  // subnormal: b is the mantissa
+}
+
 // Exponent s such that |x * 2^s| < 2^P for all |x| <= amax (amax finite, > 0).
 __device__ __forceinline__ int scale_exp(unsigned long long amax_bits, int P) {
-  return P - 1 - ilogb(__longlong_as_double((long long)amax_bits));
+  return P - 1 - ilogb_bits(amax_bits);
 }
 
 // rint(x * 2^e) (round half to even) for finite x with |x * 2^e| < 2^53, computed from the
@@ -530,16 +540,12 @@ __device__ __forceinline__ unsigned long long scaled_int(double x, int e, bool* 
     m |= 1ull << 52;
     E = ex - 1075;
   }
-  if (m == 0) return 0;
   const int sh = E + e;
   if (sh >= 0) return m << sh;  // the caller's bound keeps the result below 2^53
   const int k = -sh;
   if (k > 63) return 0;  // below one half
-  unsigned long long q = m >> k;
-  const unsigned long long rem = m & ((1ull << k) - 1);
-  const unsigned long long half = 1ull << (k - 1);
-  if (rem > half || (rem == half && (q & 1))) ++q;
-  return q;
+  // round half to even: m / 2^k + 1/2 - 2^-k, plus 2^-k when the last kept bit is odd
+  return (m + ((1ull << (k - 1)) - 1) + ((m >> k) & 1)) >> k;
 }
 
 // Residues of neighbouring integers for every modulus, on the FP32 pipe.  A scaled integer

@@ -159,6 +159,85 @@ __device__ __forceinline__ double div_split(double a, double x) {
   return a * y;
 }
 
+// ---- double-float Cauchy entries -------------------------------------------------------------
+// The significand of a normal double x (x * 2^-E, in [1, 2) with x's sign) as hi + lo floats,
+// from its bits: hi = rounded to 24 significant bits (a rounding carry lands in the exponent
+// field, which is what an add of the bits gives), lo = the remainder, a signed multiple of 2^-52
+// of at most 2^28 units converted to a float: |lo| <= 2^-24 |hi|, |hi + lo - x 2^-E| <= 2^-49.
+__device__ __forceinline__ float2 df_split_unit(double x) {
+  const unsigned hx = (unsigned)__double2hiint(x), lx = (unsigned)__double2loint(x);
+  const unsigned sgn = hx & 0x80000000u, up = (lx >> 28) & 1u;
+  const float hi = __uint_as_float((sgn | (127u << 23) | ((hx & 0xFFFFFu) << 3) | (lx >> 29)) + up);
+  const int rem = (int)(lx & 0x1FFFFFFFu) - (int)(up << 29);
+  const float lo = __int2float_rn(rem) * 0x1.0p-52f;
+  return make_float2(hi, sgn ? -lo : lo);
+}
+
+// The double nearest hi + lo (|lo| < 2^-20 |hi|, both normal or lo zero): both widened exactly
+// from their bits, one FP64 add.
+__device__ __forceinline__ double df_to_double(float hi, float lo) {
+  const unsigned bh = __float_as_uint(hi), bl = __float_as_uint(lo);
+  const double dh = __hiloint2double((int)((bh & 0x80000000u) | ((((bh >> 23) & 0xFFu) + 896u) << 20) |
+                                           ((bh & 0x7FFFFFu) >> 3)),
+                                     (int)(bh << 29));
+  if ((bl & 0x7F800000u) == 0u) return dh;
+  const double dl = __hiloint2double((int)((bl & 0x80000000u) | ((((bl >> 23) & 0xFFu) + 896u) << 20) |
+                                           ((bl & 0x7FFFFFu) >> 3)),
+                                     (int)(bl << 29));
+  return dh + dl;
+}
+
+// A column generator v of the split path's Cauchy entries: its significand split once per
+// column and its exponent; ok for a normal v (else every entry of the column takes div_split).
+struct VSplit {
+  float2 s;
+  int e;
+  bool ok;
+};
+__device__ __forceinline__ VSplit v_split(double v) {
+  VSplit r;
+  const int f = (__double2hiint(v) >> 20) & 0x7FF;
+  r.ok = f >= 1 && f <= 2046;
+  r.e = f - 1023;
+  r.s = df_split_unit(v);
+  return r;
+}
+
+// u * v / x (x = D(i) - F(j), formed in FP64 by the caller) for the split path's H, in
+// double-float arithmetic on the FP32 pipe: GB300 issues FP64 at about two lanes per SM per
+// cycle, and this costs one FP64 add instead of div_split's product, two FMAs and product.
+// The significands are split (df_split_unit) and the exponents added back at the end, so the
+// result is exactly equivariant under power-of-two scalings of u, v and x.  With x = xh + xl:
+// y0 = the FP32 reciprocal of xh, one Newton step against the whole x gives y1 with
+// |1 - x y1| <~ 2^-24 (FP32 rounding of y1), e = 1 - x y1 from two FMAs (the first exact but
+// for a rounding at 2^-48, the second at 2^-48), and 1/x = y1 + y1 e to about 2^-48 (e^2 and
+// the rounding of y1 e); a = u v = ah + al by the usual FMA error terms, renormalised so that
+// |al| <= 2^-24 |ah|, and q = a (y1 + y1 e) = qh + ql.  The low parts reach a few 2^-24 of the
+// result, so their FP32 roundings set the relative error: about 2^-45.3 at most and 2^-49
+// typically (div_split: 2^-44 and 2^-45); checked by psmma_selftest_division_split.  Zero,
+// subnormal or non-finite operands, and quotients outside the normal range, take div_split.
+__device__ __forceinline__ double cauchy_entry(double u, double v, const VSplit& vs, double x) {
+  const int fu = (__double2hiint(u) >> 20) & 0x7FF, fx = (__double2hiint(x) >> 20) & 0x7FF;
+  if (!vs.ok || fu == 0 || fu == 0x7FF || fx == 0 || fx == 0x7FF) return div_split(u * v, x);
+  const float2 xs = df_split_unit(x), us = df_split_unit(u);
+  float y0;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y0) : "f"(xs.x));
+  const float y1 = fmaf(y0, fmaf(-xs.y, y0, fmaf(-xs.x, y0, 1.0f)), y0);
+  const float e = fmaf(-xs.y, y1, fmaf(-xs.x, y1, 1.0f));
+  const float p = us.x * vs.s.x;
+  const float pl = fmaf(us.y, vs.s.y, fmaf(us.x, vs.s.y, fmaf(us.y, vs.s.x, fmaf(us.x, vs.s.x, -p))));
+  const float ah = p + pl, al = pl - (ah - p);  // renormalised: |al| <= 2^-24 |ah|
+  // a (y1 + y1 e) - ah y1 = (ah y1 - qh) + y1 (al + ah e + al e)
+  const float qh = ah * y1;
+  const float ql = fmaf(y1, fmaf(al, e, fmaf(ah, e, al)), fmaf(ah, y1, -qh));
+  const double q = df_to_double(qh, ql);  // in (1/2, 4)
+  const int eq = fu + vs.e - fx;           // exponent of u v / x over that of the significands'
+  const int hq = __double2hiint(q);
+  const int fq = ((hq >> 20) & 0x7FF) + eq;
+  if (fq < 1 || fq > 2046) return div_split(u * v, x);
+  return __hiloint2double((int)((unsigned)hq + ((unsigned)eq << 20)), __double2loint(q));
+}
+
 // ---- TMA -------------------------------------------------------------------------------
 __device__ __forceinline__ void tma_load_3d(void* smem_dst, const CUtensorMap* map, uint64_t* bar, int c0,
                                             int c1, int c2) {

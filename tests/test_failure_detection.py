@@ -48,7 +48,8 @@ def test_split_path_division_error_bound(lib, cuda):
     import ctypes as C
     mism, ulp = C.c_ulonglong(0), C.c_int(0)
     assert lib.psmma_selftest_division_split(1 << 26, 777, C.byref(mism), C.byref(ulp)) == 0
-    # FP32 reciprocal seed, one FP64 Newton step, no residual correction: within 2^-44 relative
+    # double-float entries on the FP32 pipe (an FP32-seeded FP64 Newton division for operands
+    # outside their range): within 2^-44 relative
     assert ulp.value <= 256
 
 
