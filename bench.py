@@ -350,16 +350,26 @@ def run_gpu(args, ws, rank, local):
             torch.cuda.empty_cache()
             P.psmma_cauchy(n, k, 1.0, nA, nG, 0.0, nQ, precision="split", n_moduli=args.n_moduli)
             e2e_steps = max(1, min(args.steps, 10))
-            call_ms = []
+            call_ms, dev_ms, redo = [], [], 0
+            # each call is traced (one event per library phase, no synchronisation added): the
+            # device-side span of the call and whether its speculative bit counts were redone
+            lib.psmma_set_profiling(1)
             t0 = time.perf_counter()
             for _ in range(e2e_steps):
                 t1 = time.perf_counter()
                 P.psmma_cauchy(n, k, 1.0, nA, nG, 0.0, nQ, precision="split", n_moduli=args.n_moduli)
                 call_ms.append(round((time.perf_counter() - t1) * 1e3, 2))
+                ms = (C_float * 40)()
+                names = (C_charp * 40)()
+                m = lib.psmma_profile_read(ms, names, 40)
+                dev_ms.append(round(sum(ms[j] for j in range(max(0, m))), 2))
+                redo += any(names[j] == b"redo_wrong_guess" for j in range(max(0, m)))
             te = (time.perf_counter() - t0) / e2e_steps
+            lib.psmma_set_profiling(0)
             result["e2e"] = {"value": flops_rank / te / 1e12, "unit": "TFLOP/s",
                              "h2d_bytes_per_step": n * k * 8 + 4 * k * 8, "d2h_bytes_per_step": n * k * 8,
                              "ms_per_step": te * 1e3, "steps": e2e_steps, "call_ms": call_ms,
+                             "device_span_ms": dev_ms, "redone_calls": redo,
                              "api": "psmma_cauchy_host (pinned host buffers)"}
             # after the timed calls: one traced call (library-stream phases) and the pinned
             # copy rate of this host link, which bound the end-to-end time from below

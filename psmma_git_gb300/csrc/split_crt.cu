@@ -1629,6 +1629,7 @@ static int split_core_host(int M, int N, int K, double alpha, const double* A_h,
     if (ph_out) *ph_out = head.PH;
     if (head.PA == pa_guess && head.PH == ph_guess) return PSMMA_OK;
     // a wrong guess: everything after the parameter pass again, with the computed bit counts
+    prof_mark(s, "redo_wrong_guess");
     k_residues_A<<<dim3(L.kp / 64, (M + 31) / 32), 256, 0, s>>>(dA, M, M, K, L.kp, b.amax, b.prm, cc, b.RA);
     k_residues_H<<<grh, 128, 0, s>>>(b.Ht, N, L.kp, b.hmax, b.prm, cc, b.RH);
     ok &= cudaEventRecord(ev_start, s) == cudaSuccess;
