@@ -1081,6 +1081,13 @@ __global__ void __launch_bounds__(G_THREADS, 1) k_crt_gemm(const __grid_constant
 // ------------------------------------------------------------------------------------------
 typedef unsigned __int128 u128;
 
+// m * 2^x with the sign, for results outside the normal range; out of line, so that its FP64
+// instructions are not issued (predicated off) for every element.
+static __device__ __noinline__ double scaled_outside_normal(unsigned long long m, int x, bool neg) {
+  const double v = ldexp((double)m, x);
+  return neg ? -v : v;
+}
+
 // (hi:lo) * 2^-e as a double, (hi:lo) a non-negative 128-bit integer in two words, rounded
 // to nearest even from the bits; results outside the normal range go through ldexp.
 __device__ __forceinline__ double u128w_scaled(unsigned long long hi, unsigned long long lo, bool neg, int e) {
@@ -1115,8 +1122,7 @@ __device__ __forceinline__ double u128w_scaled(unsigned long long hi, unsigned l
     if (neg) bits |= 1ull << 63;
     return __longlong_as_double((long long)bits);
   }
-  const double v = ldexp((double)m, p - 52 - e);
-  return neg ? -v : v;
+  return scaled_outside_normal(m, p - 52 - e, neg);
 }
 
 // One block: 32 rows x 128 columns (32 x 8 threads); a thread recombines 4 neighbouring
@@ -1227,7 +1233,15 @@ __device__ __forceinline__ void crt_combine_blk(const int8_t* __restrict__ R, in
   }
   __syncthreads();
   const bool scale = alpha != 1.0, accumulate = beta != 0.0;  // uniform: decided once
-  if (!DFT_OUT) {
+  if (!DFT_OUT && !scale && !accumulate) {
+    // Q = Z 2^-(s+f): a loop of its own, without the FP64 epilogue (instructions predicated off
+    // would still be issued to GB300's narrow FP64 pipe)
+    const int i = i0 + tx;
+    for (int b = 0; b < CRT_TJ / 8; ++b) {
+      const int jl = ty + 8 * b, jj = j0 + jl;
+      if (i < n && jj < k) Q[i + (long)jj * ldq] = tile[jl][(tx + (jl >> 2)) & 31];
+    }
+  } else if (!DFT_OUT) {
     const int i = i0 + tx;
     for (int b = 0; b < CRT_TJ / 8; ++b) {
       const int jl = ty + 8 * b, jj = j0 + jl;

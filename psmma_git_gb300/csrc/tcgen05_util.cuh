@@ -216,9 +216,13 @@ __device__ __forceinline__ VSplit v_split(double v) {
 // result, so their FP32 roundings set the relative error: about 2^-45.3 at most and 2^-49
 // typically (div_split: 2^-44 and 2^-45); checked by psmma_selftest_division_split.  Zero,
 // subnormal or non-finite operands, and quotients outside the normal range, take div_split.
+// The operands cauchy_entry leaves to the FP64 division; out of line, so that the rare branch
+// stays a branch (its FP64 instructions are not issued, predicated off, for every entry).
+static __device__ __noinline__ double cauchy_entry_slow(double u, double v, double x) { return div_split(u * v, x); }
+
 __device__ __forceinline__ double cauchy_entry(double u, double v, const VSplit& vs, double x) {
   const int fu = (__double2hiint(u) >> 20) & 0x7FF, fx = (__double2hiint(x) >> 20) & 0x7FF;
-  if (!vs.ok || fu == 0 || fu == 0x7FF || fx == 0 || fx == 0x7FF) return div_split(u * v, x);
+  if (!vs.ok || fu == 0 || fu == 0x7FF || fx == 0 || fx == 0x7FF) return cauchy_entry_slow(u, v, x);
   const float2 xs = df_split_unit(x), us = df_split_unit(u);
   float y0;
   asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y0) : "f"(xs.x));
@@ -234,7 +238,7 @@ __device__ __forceinline__ double cauchy_entry(double u, double v, const VSplit&
   const int eq = fu + vs.e - fx;           // exponent of u v / x over that of the significands'
   const int hq = __double2hiint(q);
   const int fq = ((hq >> 20) & 0x7FF) + eq;
-  if (fq < 1 || fq > 2046) return div_split(u * v, x);
+  if (fq < 1 || fq > 2046) return cauchy_entry_slow(u, v, x);
   return __hiloint2double((int)((unsigned)hq + ((unsigned)eq << 20)), __double2loint(q));
 }
 
