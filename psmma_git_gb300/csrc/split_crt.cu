@@ -1512,8 +1512,8 @@ static int split_core_host(int M, int N, int K, double alpha, const double* A_h,
   if (K >= (1 << 24) || M >= (1 << 30) || N >= (1 << 30)) return PSMMA_EUNSUPPORTED;
   // A column chunks; GEMM / CRT / download row panels: eighths of the row tiles, the first
   // one cut to two row tiles (its pitched upload runs beside the H passes' HBM traffic and
-  // gates the first product) and the last one cut in three (the download left after the last
-  // product is short)
+  // gates the first product) and the last one halved three times (8 + 4 + 2 + 2 of 16 tiles:
+  // the download left after the last product is short)
   constexpr int NCH = 4, NP = 12;
   if (nev < 2 * NP + 3) return PSMMA_EUNSUPPORTED;
   static_assert(NCH <= NP, "column chunks and row panels share the upload events");
@@ -1579,7 +1579,7 @@ static int split_core_host(int M, int N, int K, double alpha, const double* A_h,
     }
     while (tiles_m - pb[npanels] > tp) { pb[npanels + 1] = pb[npanels] + tp; ++npanels; }
     for (int rest = tiles_m - pb[npanels], cut = 0; rest > 0; ++cut) {
-      const int t = cut < 2 ? (rest + 1) / 2 : rest;
+      const int t = cut < 3 ? (rest + 1) / 2 : rest;
       pb[npanels + 1] = pb[npanels] + t;
       ++npanels;
       rest -= t;
@@ -1628,8 +1628,10 @@ static int split_core_host(int M, int N, int K, double alpha, const double* A_h,
     for (int p = 0; p < npanels; ++p) {
       const int r0 = pb[p] * G_BM, r1 = std::min(M, pb[p + 1] * G_BM);
       ok &= cudaStreamWaitEvent(s, ev_up[p], 0) == cudaSuccess;
-      dim3 g1((r1 - r0 + 127) / 128, (K + kchunk - 1) / kchunk);
-      k_row_absmax<<<g1, 128, 0, s>>>(dA + r0, M, r1 - r0, K, kchunk, b.amax + r0, b.asq + r0);
+      // a panel has few rows: shorter K chunks keep enough blocks in flight
+      const int kc = 256;
+      dim3 g1((r1 - r0 + 127) / 128, (K + kc - 1) / kc);
+      k_row_absmax<<<g1, 128, 0, s>>>(dA + r0, M, r1 - r0, K, kc, b.amax + r0, b.asq + r0);
       k_residues_A_rows<<<dim3(L.kp / 64, (r1 - r0 + 31) / 32), 256, 0, s>>>(dA, M, M, K, L.kp, b.amax,
                                                                              b.prm_guess, cc, b.RA, r0 / 32);
       prof_mark(s, "panel_rows");
