@@ -169,10 +169,36 @@ static SplitLayout split_layout(int M, int K, int N, int nmod) {
 
 static int resolve_nmod(int n_moduli) { return n_moduli == 0 ? SPL_DEFAULT_MODULI : n_moduli; }
 
+// The DFT's split workspace: C^T = B^T F (k x n complex) as three real products of the 3M
+// form, T1 = Br^T Fr, T2 = Bi^T Fi, T3 = (Br + Bi)^T (Fr + Fi): row maxima and sums of B's
+// columns (M = k), column statistics of F (n), Ht = [Fr rows | Fi rows] (2n x kp doubles), three
+// sets of A and H residue planes (product p at p * nmod planes), and output planes with Re in
+// columns [0, n) and Im in [kr1, kr1 + n), kr1 = n rounded to 256 (the GEMMs' tile padding of
+// the Re half stays out of the Im half).
+static SplitLayout dft3_layout(int M, int n, int nmod) {
+  SplitLayout L;
+  L.kp = (n + 63) / 64 * 64;
+  const int kr1 = (n + 255) / 256 * 256;
+  L.kr = 2 * kr1;
+  size_t o = 0;
+  L.off_params = o; o += al1k(2 * sizeof(SplitDevParams));
+  L.off_amax = o;   o += al1k((size_t)M * 8);
+  L.off_hmax = o;   o += al1k((size_t)n * 8);
+  L.off_hsum = o;   o += al1k((size_t)n * 8);
+  L.off_asq = o;    o += al1k((size_t)M * 8);
+  L.off_hsq = o;    o += al1k((size_t)n * 8);
+  L.off_wtab = o;   o += al1k((size_t)(n + 1) * 16);
+  L.off_ht = o;     o += al1k((size_t)2 * n * L.kp * 8);
+  L.off_ra = o;     o += al1k((size_t)3 * nmod * M * L.kp * 2);
+  L.off_rh = o;     o += al1k((size_t)3 * nmod * n * L.kp * 2);
+  L.off_r = o;      o += al1k((size_t)nmod * M * L.kr);
+  L.total = o;
+  return L;
+}
+
 size_t split_workspace_bytes(int kind, int n, int k, int n_moduli) {
   if (n <= 0 || k <= 0) return 0;
-  // DFT: the product runs as (B^T embedded, k x 2n) * (F embedded, 2n x 2n)
-  if (kind == KIND_DFT) return split_layout(k, 2 * n, 2 * n, resolve_nmod(n_moduli)).total;
+  if (kind == KIND_DFT) return dft3_layout(k, n, resolve_nmod(n_moduli)).total;
   return split_layout(n, k, k, resolve_nmod(n_moduli)).total;
 }
 
@@ -324,16 +350,8 @@ __device__ __forceinline__ void h_pass1_blk(const GenSpec& gs, int K, int kp, do
           h = __ldg(gs.B + (kk - gs.k1) + (long)j * gs.ldb);
         else
           h = KIND == KIND_TOEPLITZ ? __ldg(gs.g + (gs.order - 1) + j - kk) : __ldg(gs.g + kk + j);
-      } else if (KIND == KIND_DENSE) {
+      } else {  // KIND_DENSE (the split DFT generates F in k_h_pass1_dft3)
         h = __ldg(gs.B + kk + (long)j * gs.ldb);
-      } else {
-        // DFT embedding F' = [[Re F, Im F], [-Im F, Re F]] of order K = 2n; the table holds
-        // w^t = (cos, -sin)(2 pi t / n), indexed by the exact (r c) mod n.
-        const int nn = gs.n_dft;
-        const bool rb = kk >= nn, cb = j >= nn;
-        const long rr = rb ? kk - nn : kk, cc2 = cb ? j - nn : j;
-        const double2 wv = __ldg(gs.wtab + (rr * cc2) % nn);
-        h = (rb == cb) ? wv.x : (rb ? -wv.y : wv.y);
       }
     }
     row[kk] = h;
@@ -575,23 +593,22 @@ __device__ __forceinline__ ResidueChunks residue_chunks(unsigned long long u, bo
   return c;
 }
 
-__device__ __forceinline__ unsigned residue_bits(const ResidueChunks& c, float g23, float g38, float inv, float mf) {
+__device__ __forceinline__ float residue_f(const ResidueChunks& c, float g23, float g38, float inv, float mf) {
   const float t = fmaf(c.c2, g38, fmaf(c.c1, g23, c.c0));
   const float q = fmaf(t, inv, 12582912.0f) - 12582912.0f;
-  return __float_as_uint(fmaf(-q, mf, t));
+  return fmaf(-q, mf, t);
 }
 
-__device__ __forceinline__ void write_residue_pair(unsigned long long u0, bool n0, unsigned long long u1, bool n1,
-                                                   const CrtConsts& cc, uint32_t* dst, size_t plane_words) {
-  const ResidueChunks a = residue_chunks(u0, n0), b = residue_chunks(u1, n1);
-#pragma unroll
-  for (int l = 0; l < SPL_MAX_MODULI; ++l) {
-    if (l < cc.nmod) {
-      const float g23 = cc.g23[l], g38 = cc.g38[l], inv = cc.inv_m[l], mf = cc.mf[l];
-      *dst = __byte_perm(residue_bits(a, g23, g38, inv, mf), residue_bits(b, g23, g38, inv, mf), 0x7632);
-      dst += plane_words;
-    }
-  }
+__device__ __forceinline__ unsigned residue_bits(const ResidueChunks& c, float g23, float g38, float inv, float mf) {
+  return __float_as_uint(residue_f(c, g23, g38, inv, mf));
+}
+
+// (a + b) mod m in [-128, 128] for residues |a|, |b| <= 128 (exact floats): the quotient
+// rint((a + b) / m) is in {-1, 0, 1} and its float estimate is off by at most 2^-23.
+__device__ __forceinline__ float residue_sum(float a, float b, float inv, float mf) {
+  const float t = a + b;
+  const float q = fmaf(t, inv, 12582912.0f) - 12582912.0f;
+  return fmaf(-q, mf, t);
 }
 
 // The same for four neighbouring integers: one 8-byte store per plane.
@@ -750,29 +767,170 @@ __global__ void k_row_absmax_dft(const double* __restrict__ Bre, long ldb2, int 
   }
 }
 
-// X'(i, e) = Re B(e, i) for e < n, Im B(e - n, i) for n <= e < 2n, 0 beyond.
-__device__ __forceinline__ double dft_x(const double* col, int nn, int e) {
-  if (e < nn) return __ldg(col + 2 * e);
-  if (e < 2 * nn) return __ldg(col + 2 * (e - nn) + 1);
-  return 0.0;
+// ---- the DFT as three real products (3M form) ----------------------------------------------
+// C^T = B^T F with F(j, l) = w^(j l), w = exp(-2 pi i / n), F symmetric: Re = T1 - T2 and
+// Im = T3 - T1 - T2 for T1 = Br^T Fr, T2 = Bi^T Fi, T3 = (Br + Bi)^T (Fr + Fi).  Rows of A (columns
+// of B) and columns of F are scaled as in the real embedding [Re B^T | Im B^T] x
+// [[Fr, Fi], [-Fi, Fr]] (one exponent per complex row / column), so the integer products, and
+// the result, are those of the embedding, with three BF16 GEMMs per modulus instead of four.
+
+// Ht = [Fr rows | Fi rows] (row j: column j of F = row j), the column maxima over |Fr| and |Fi|,
+// sum_l |Fr| + |Fi| and sum_l Fr^2 + Fi^2 (the statistics of the embedding's column j and
+// n + j).  One block per column.
+__global__ void __launch_bounds__(256) k_h_pass1_dft3(const double2* __restrict__ wtab, int nn, int kp,
+                                                      double* __restrict__ Ht, unsigned long long* __restrict__ hmax_bits,
+                                                      double* __restrict__ hsum, double* __restrict__ hsq,
+                                                      SplitDevParams* prm) {
+  const int j = blockIdx.x;
+  double* rr = Ht + (size_t)j * kp;
+  double* ri = Ht + ((size_t)nn + j) * kp;
+  unsigned long long mb = 0;
+  float s32 = 0.0f, s2_32 = 0.0f;
+  int e = NO_SCALE;
+  bool big = false;
+  for (int l = threadIdx.x; l < kp; l += blockDim.x) {
+    double2 wv = make_double2(0.0, 0.0);
+    if (l < nn) wv = __ldg(wtab + (int)(((long long)l * j) % nn));
+    rr[l] = wv.x;
+    ri[l] = wv.y;
+#pragma unroll
+    for (int part = 0; part < 2; ++part) {
+      const unsigned long long b = (unsigned long long)__double_as_longlong(part ? wv.y : wv.x) & ABS_MASK;
+      mb = b > mb ? b : mb;
+      if (e == NO_SCALE && b) e = (int)(b >> 52) - 1023;
+      if (e != NO_SCALE) {
+        const float f = abs_scaled_up(b, e, &big);
+        s32 = __fadd_ru(s32, f);
+        s2_32 = __fmaf_ru(f, f, s2_32);
+      }
+    }
+  }
+  double s = 0.0, s2 = 0.0;
+  if (big) {
+    for (int l = threadIdx.x; l < kp; l += blockDim.x) {
+      s += fabs(rr[l]) + fabs(ri[l]);
+      s2 = fma(rr[l], rr[l], fma(ri[l], ri[l], s2));
+    }
+  } else if (e != NO_SCALE) {
+    s = ldexp((double)s32, e);
+    s2 = ldexp((double)s2_32, 2 * e);
+  }
+  __shared__ unsigned long long smax[32];
+  __shared__ double ssum[32], ssq[32];
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long ob = __shfl_xor_sync(0xffffffffu, mb, o);
+    mb = ob > mb ? ob : mb;
+    s += __shfl_xor_sync(0xffffffffu, s, o);
+    s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+  }
+  const int wid = threadIdx.x >> 5, ln = threadIdx.x & 31;
+  if (ln == 0) { smax[wid] = mb; ssum[wid] = s; ssq[wid] = s2; }
+  __syncthreads();
+  if (wid == 0) {
+    const int nw = blockDim.x >> 5;
+    mb = ln < nw ? smax[ln] : 0ull;
+    s = ln < nw ? ssum[ln] : 0.0;
+    s2 = ln < nw ? ssq[ln] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long ob = __shfl_xor_sync(0xffffffffu, mb, o);
+      mb = ob > mb ? ob : mb;
+      s += __shfl_xor_sync(0xffffffffu, s, o);
+      s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+    }
+    if (ln == 0) {
+      hmax_bits[j] = mb;
+      hsum[j] = s;
+      hsq[j] = s2;
+      if (mb > 0 && mb < INF_BITS && isfinite(s)) {
+        const double rho = s / __longlong_as_double((long long)mb);
+        atomicMax(&prm->rho_bits, (unsigned long long)__double_as_longlong(rho));
+      }
+    }
+  }
 }
 
-__global__ void k_residues_A_dft(const double* __restrict__ Bre, long ldb2, int nn, int kp,
-                                 const unsigned long long* __restrict__ amax_bits, const SplitDevParams* prm,
-                                 CrtConsts cc, __nv_bfloat16* __restrict__ RA, int M) {
+// Residues of Ar = Re B^T, Ai = Im B^T and Ar + Ai (the last as the sum of the first two's
+// residues): row i is column i of B (interleaved complex, ldb2 doubles apart); a thread writes
+// two neighbouring k of all three planes of every modulus.  RA holds product p's planes at
+// p * nmod * M * kp.
+__global__ void k_residues_A_dft3(const double* __restrict__ Bre, long ldb2, int nn, int kp,
+                                  const unsigned long long* __restrict__ amax_bits, const SplitDevParams* prm,
+                                  CrtConsts cc, __nv_bfloat16* __restrict__ RA, int M) {
   const int i = blockIdx.y;
   const int kk = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
   if (kk >= kp) return;
-  const int P = prm->PA;
   const unsigned long long ab = amax_bits[i];
   const bool ok = ab > 0 && ab < INF_BITS;
-  const int e = ok ? scale_exp(ab, P) : 0;
+  const int e = ok ? scale_exp(ab, prm->PA) : 0;
   const double* col = Bre + (long)i * ldb2;
-  bool n0 = false, n1 = false;
-  const unsigned long long u0 = ok ? scaled_int(dft_x(col, nn, kk), e, &n0) : 0ull;
-  const unsigned long long u1 = ok ? scaled_int(dft_x(col, nn, kk + 1), e, &n1) : 0ull;
+  double2 z0 = make_double2(0.0, 0.0), z1 = make_double2(0.0, 0.0);
+  if (kk < nn) z0 = __ldg((const double2*)(col + 2 * kk));
+  if (kk + 1 < nn) z1 = __ldg((const double2*)(col + 2 * kk + 2));
+  bool n0 = false, n1 = false, n2 = false, n3 = false;
+  const ResidueChunks r0 = residue_chunks(ok ? scaled_int(z0.x, e, &n0) : 0ull, n0);
+  const ResidueChunks r1 = residue_chunks(ok ? scaled_int(z1.x, e, &n1) : 0ull, n1);
+  const ResidueChunks i0 = residue_chunks(ok ? scaled_int(z0.y, e, &n2) : 0ull, n2);
+  const ResidueChunks i1 = residue_chunks(ok ? scaled_int(z1.y, e, &n3) : 0ull, n3);
+  const size_t plane = (size_t)M * kp, prod = (size_t)cc.nmod * plane;
   uint32_t* dst = (uint32_t*)(RA + (size_t)i * kp + kk);
-  write_residue_pair(u0, n0, u1, n1, cc, dst, (size_t)M * kp / 2);
+#pragma unroll
+  for (int l = 0; l < SPL_MAX_MODULI; ++l) {
+    if (l < cc.nmod) {
+      const float g23 = cc.g23[l], g38 = cc.g38[l], inv = cc.inv_m[l], mf = cc.mf[l];
+      const float a0 = residue_f(r0, g23, g38, inv, mf), a1 = residue_f(r1, g23, g38, inv, mf);
+      const float b0 = residue_f(i0, g23, g38, inv, mf), b1 = residue_f(i1, g23, g38, inv, mf);
+      const float c0 = residue_sum(a0, b0, inv, mf), c1 = residue_sum(a1, b1, inv, mf);
+      uint32_t* d = dst + (size_t)l * plane / 2;
+      d[0] = __byte_perm(__float_as_uint(a0), __float_as_uint(a1), 0x7632);
+      d[prod / 2] = __byte_perm(__float_as_uint(b0), __float_as_uint(b1), 0x7632);
+      d[prod] = __byte_perm(__float_as_uint(c0), __float_as_uint(c1), 0x7632);
+    }
+  }
+}
+
+// Residues of Fr, Fi and Fr + Fi from Ht with column j's common exponent: four consecutive l
+// per thread; RH holds product p's planes at p * nmod * nn * kp.
+__global__ void k_residues_H_dft3(const double* __restrict__ Ht, int nn, int kp,
+                                  const unsigned long long* __restrict__ hmax_bits, const SplitDevParams* prm,
+                                  CrtConsts cc, __nv_bfloat16* __restrict__ RH) {
+  const int j = blockIdx.y;
+  const int kk = RH_PER_THREAD * (blockIdx.x * blockDim.x + threadIdx.x);
+  if (kk >= kp) return;  // kp is a multiple of 64
+  const unsigned long long hb = hmax_bits[j];
+  const bool ok = hb > 0 && hb < INF_BITS;
+  const int e = ok ? scale_exp(hb, prm->PH) : 0;
+  const double* pr = Ht + (size_t)j * kp + kk;
+  const double* pi = Ht + ((size_t)nn + j) * kp + kk;
+  const double2 r01 = *(const double2*)pr, r23 = *(const double2*)(pr + 2);
+  const double2 i01 = *(const double2*)pi, i23 = *(const double2*)(pi + 2);
+  const double vr[4] = {r01.x, r01.y, r23.x, r23.y}, vi[4] = {i01.x, i01.y, i23.x, i23.y};
+  ResidueChunks cr[4], ci[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    bool a = false, b = false;
+    cr[q] = residue_chunks(ok ? scaled_int(vr[q], e, &a) : 0ull, a);
+    ci[q] = residue_chunks(ok ? scaled_int(vi[q], e, &b) : 0ull, b);
+  }
+  const size_t plane = (size_t)nn * kp, prod = (size_t)cc.nmod * plane;
+  uint2* dst = (uint2*)(RH + (size_t)j * kp + kk);
+#pragma unroll
+  for (int l = 0; l < SPL_MAX_MODULI; ++l) {
+    if (l < cc.nmod) {
+      const float g23 = cc.g23[l], g38 = cc.g38[l], inv = cc.inv_m[l], mf = cc.mf[l];
+      unsigned fr[4], fi[4], fs[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const float a = residue_f(cr[q], g23, g38, inv, mf), b = residue_f(ci[q], g23, g38, inv, mf);
+        fr[q] = __float_as_uint(a);
+        fi[q] = __float_as_uint(b);
+        fs[q] = __float_as_uint(residue_sum(a, b, inv, mf));
+      }
+      uint2* d = dst + (size_t)l * plane / 4;
+      d[0] = make_uint2(__byte_perm(fr[0], fr[1], 0x7632), __byte_perm(fr[2], fr[3], 0x7632));
+      d[prod / 4] = make_uint2(__byte_perm(fi[0], fi[1], 0x7632), __byte_perm(fi[2], fi[3], 0x7632));
+      d[prod / 2] = make_uint2(__byte_perm(fs[0], fs[1], 0x7632), __byte_perm(fs[2], fs[3], 0x7632));
+    }
+  }
 }
 
 // ------------------------------------------------------------------------------------------
@@ -795,6 +953,10 @@ constexpr uint32_t G_A_BYTES = G_BM * G_BK * 2;
 struct GemmArgs {
   int n, kr, nkb, tiles_m, tiles_n, group_m, nmod;  // (a grouped launch uses group_m, nmod)
   int tm0;  // one product: first row tile of this launch (row panels)
+  // Epilogue of the 3M complex product (T1 = Ar Fr, T2 = Ai Fi, T3 = (Ar + Ai)(Fr + Fi)):
+  // 0 stores the residues; 1 reads T1 where it stores and writes T1 - x there and -T1 - x at
+  // +im_off bytes; 2 adds x to the residues already stored.
+  int mode, im_off;
   int8_t* R;
   unsigned* status;
   int m[SPL_MAX_MODULI];
@@ -885,6 +1047,36 @@ __device__ __forceinline__ int mod_sym(int s, int m, float inv_m) {
   x = (x > 127) ? x - m : x;
   x = (x < -128) ? x + m : x;
   return x;
+}
+
+// Epilogue of the 3M complex product's second and third GEMMs: combine this tile's residues x
+// (in [-128, 127]) with those already in the output plane, 16 bytes at a time.
+// mode 1: old = T1 -> store (T1 - x) mod m, and (-T1 - x) mod m at dst + im_off;
+// mode 2: old = -T1 - T2 -> store (old + x) mod m.
+template <int HALF>
+__device__ __forceinline__ void store_combined(int8_t* dst, const int (&res)[HALF], int mode, int im_off, int m,
+                                               float inv_m) {
+#pragma unroll
+  for (int v = 0; v < HALF / 16; ++v) {
+    const uint4 o = *(const uint4*)(dst + v * 16);
+    const uint32_t ow[4] = {o.x, o.y, o.z, o.w};
+    uint32_t w1[4], w2[4];
+#pragma unroll
+    for (int t4 = 0; t4 < 4; ++t4) {
+      w1[t4] = 0u;
+      w2[t4] = 0u;
+#pragma unroll
+      for (int bb = 0; bb < 4; ++bb) {
+        const int old = (int)(int8_t)(ow[t4] >> (8 * bb));
+        const int x = res[v * 16 + t4 * 4 + bb];
+        const int a = mod_sym(mode == 1 ? old - x : old + x, m, inv_m);
+        w1[t4] |= (uint32_t)(uint8_t)(int8_t)a << (8 * bb);
+        if (mode == 1) w2[t4] |= (uint32_t)(uint8_t)(int8_t)mod_sym(-old - x, m, inv_m) << (8 * bb);
+      }
+    }
+    *(uint4*)(dst + v * 16) = make_uint4(w1[0], w1[1], w1[2], w1[3]);
+    if (mode == 1) *(uint4*)(dst + im_off + v * 16) = make_uint4(w2[0], w2[1], w2[2], w2[3]);
+  }
 }
 
 template <int BN>
@@ -1050,7 +1242,10 @@ __global__ void __launch_bounds__(G_THREADS, 1) k_crt_gemm(const __grid_constant
         }
       }
       const int i = ti.tm * G_BM + q * 32 + lane;
-      if (ok && !*abort_flag && i < ti.n) {
+      if (ok && !*abort_flag && i < ti.n && g.mode != 0) {
+        int8_t* dst = ti.R + ((size_t)ti.l * ti.n + i) * ti.kr + (size_t)ti.tn * BN + h * HALF;
+        store_combined<HALF>(dst, res, g.mode, g.im_off, mi, inv_m);
+      } else if (ok && !*abort_flag && i < ti.n) {
         int8_t* dst = ti.R + ((size_t)ti.l * ti.n + i) * ti.kr + (size_t)ti.tn * BN + h * HALF;
 #pragma unroll
         for (int v = 0; v < HALF / 16; ++v) {
@@ -1131,8 +1326,18 @@ __device__ __forceinline__ double u128w_scaled(unsigned long long hi, unsigned l
 // the limbs of sum_l (r_l + 128) C_l and one for the fixed-point quotient estimate.
 constexpr int CRT_TI = 32, CRT_TJ = 128;
 
-// DFT_OUT: the product is [Re C^T | Im C^T] (rows = columns of C); element (i, j) goes to the
-// interleaved complex C at 2*(j mod nn) + (j >= nn) + i*ldq (ldq in doubles).
+// The column of C^T that residue column rc of the 3M DFT layout holds (Re: rc < nn, Im: from
+// kr/2), or -1 for the padding between and after.
+__device__ __forceinline__ int dft_col(int rc, int nn, int kr) {
+  if (rc < nn) return rc;
+  const int im = rc - (kr >> 1);
+  return (im >= 0 && im < nn) ? im : -1;
+}
+
+// DFT_OUT: the product is C^T (rows = columns of C, k = n its column count) with Re in R
+// columns [0, n) and Im in [kr/2, kr/2 + n) (the 3M layout); Re / Im of element (i, j) go to
+// the interleaved complex C at 2j / 2j + 1 + i*ldq (ldq in doubles); column j's exponent is
+// that of hmax_bits[j].
 // TOP32 (cc.top32): the sum over the moduli of (r_l + 128) times the top 32-bit limb of C_l
 // stays below 2^32 (true for M < 2^112: every top limb is below 2^16), so it is kept in 32 bits.
 template <bool DFT_OUT, bool TOP32 = false>
@@ -1148,18 +1353,20 @@ __device__ __forceinline__ void crt_combine_blk(const int8_t* __restrict__ R, in
   const int i0 = by * CRT_TI, j0 = bx * CRT_TJ;
   const int PA = prm->PA, PH = prm->PH;
   const int jb = j0 + 4 * tx;
+  const int kcols = DFT_OUT ? kr : k;  // residue columns covered
   unsigned long long hb[4];
   int fexp[4];
 #pragma unroll
   for (int c = 0; c < 4; ++c) {
-    hb[c] = (jb + c < k) ? hmax_bits[jb + c] : 0ull;
+    const int hc = DFT_OUT ? dft_col(jb + c, k, kr) : (jb + c < k ? jb + c : -1);
+    hb[c] = hc >= 0 ? hmax_bits[hc] : 0ull;
     fexp[c] = (hb[c] != 0 && hb[c] < INF_BITS) ? scale_exp(hb[c], PH) : 0;
   }
   const size_t plane_w = (size_t)n * kr / 4;
   for (int a = 0; a < CRT_TI / 8; ++a) {
     const int il = ty + 8 * a, i = i0 + il;
     double val[4] = {0.0, 0.0, 0.0, 0.0};
-    if (i < n && jb < k) {
+    if (i < n && jb < kcols) {
       const unsigned long long ab = amax_bits[i];
       const int sexp = (ab != 0 && ab < INF_BITS) ? scale_exp(ab, PA) : 0;
       unsigned long long acc[4][4];
@@ -1254,15 +1461,14 @@ __device__ __forceinline__ void crt_combine_blk(const int8_t* __restrict__ R, in
       }
     }
   } else {
-    const int nn = k >> 1;
     for (int a = 0; a < CRT_TI / 8; ++a) {
       const int il = ty + 8 * a, i = i0 + il;
       if (i >= n) continue;
 #pragma unroll
       for (int c = 0; c < 4; ++c) {
-        const int jj = jb + c;
-        if (jj >= k) continue;
-        double* qp = Q + (long)i * ldq + 2 * (jj < nn ? jj : jj - nn) + (jj >= nn ? 1 : 0);
+        const int jj = jb + c, hc = dft_col(jj, k, kr);
+        if (hc < 0) continue;
+        double* qp = Q + (long)i * ldq + 2 * hc + (jj >= (kr >> 1) ? 1 : 0);
         double v = tile[4 * tx + c][(il + tx) & 31];
         if (scale) v *= alpha;
         if (accumulate) v = fma(beta, *qp, v);
@@ -1374,10 +1580,35 @@ __global__ void k_status_or(unsigned* acc, const unsigned* st) {
 // interleaved complex C (ldq).  Status: status_dev_out == nullptr ORs the call's device status
 // into the stream's status word (no synchronisation), kStatusWait waits and returns it, any other
 // pointer receives a copy of it (no synchronisation).
+// The device status of a split call: copied to the caller's word, ORed into the stream's word
+// (asynchronous), or waited for and returned (kStatusWait, or no stream word).
+static int split_status(SplitDevParams* prm, cudaStream_t stream, unsigned* status_dev_out) {
+  if (status_dev_out && status_dev_out != kStatusWait) {
+    if (cudaMemcpyAsync(status_dev_out, &prm->status, sizeof(unsigned), cudaMemcpyDeviceToDevice, stream) !=
+        cudaSuccess)
+      return PSMMA_EDEVICE;
+    return PSMMA_OK;
+  }
+  if (!status_dev_out) {
+    // asynchronous: the status joins the stream's word, reported by psmma_stream_status
+    unsigned* acc = stream_status_word(stream);
+    if (acc) {
+      k_status_or<<<1, 1, 0, stream>>>(acc, &prm->status);
+      return cudaGetLastError() == cudaSuccess ? PSMMA_OK : PSMMA_EDEVICE;
+    }
+  }
+  unsigned st = 0;  // kStatusWait (or no status word): wait for the call and read its status
+  if (cudaMemcpyAsync(&st, &prm->status, sizeof(st), cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
+      cudaStreamSynchronize(stream) != cudaSuccess)
+    return PSMMA_EDEVICE;
+  if (st & DEV_ERR_TIMEOUT) return PSMMA_ETIMEDOUT;
+  return PSMMA_OK;
+}
+
 static int split_core(int M, int N, int K, double alpha, const double* A, long lda, const GenSpec& gs, double beta,
                       double* Q, long ldq, int nmod, void* work, size_t lwork, cudaStream_t stream,
                       unsigned* status_dev_out) {
-  const bool dft = gs.kind == KIND_DFT;
+  if (gs.kind == KIND_DFT) return PSMMA_EUNSUPPORTED;  // split_core_dft3
   if (nmod < 8 || nmod > SPL_MAX_MODULI) return PSMMA_EUNSUPPORTED;
   if (K >= (1 << 24) || M >= (1 << 30) || N >= (1 << 30)) return PSMMA_EUNSUPPORTED;
   SplitLayout L = split_layout(M, K, N, nmod);
@@ -1390,12 +1621,10 @@ static int split_core(int M, int N, int K, double alpha, const double* A, long l
   if (cudaMemsetAsync(w, 0, L.off_wtab, stream) != cudaSuccess) return PSMMA_EDEVICE;  // params, maxima, sums
 
   // ---- A side: row maxima and norms
-  if (!dft) {
+  {
     const int kchunk = 1024;
     dim3 g1((M + 127) / 128, (K + kchunk - 1) / kchunk);
     k_row_absmax<<<g1, 128, 0, stream>>>(A, lda, M, K, kchunk, b.amax, b.asq);
-  } else {
-    k_row_absmax_dft<<<M, 256, 0, stream>>>(A, 2 * lda, gs.n_dft, b.amax, b.asq);
   }
   prof_mark(stream, "row_scale");
   // ---- H side: generate, column maxima / sums / norms
@@ -1405,24 +1634,12 @@ static int split_core(int M, int N, int K, double alpha, const double* A, long l
     case KIND_HANKEL: k_h_pass1<KIND_HANKEL><<<N, 256, 0, stream>>>(gs, K, L.kp, b.Ht, b.hmax, b.hsum, b.hsq, b.prm); break;
     case KIND_DENSE: k_h_pass1<KIND_DENSE><<<N, 256, 0, stream>>>(gs, K, L.kp, b.Ht, b.hmax, b.hsum, b.hsq, b.prm); break;
     case KIND_CAUCHY_EIG: k_h_pass1<KIND_CAUCHY_EIG><<<N, 256, 0, stream>>>(gs, K, L.kp, b.Ht, b.hmax, b.hsum, b.hsq, b.prm); break;
-    case KIND_DFT: {
-      int st = launch_dft_table(b.wtab, gs.n_dft, stream);
-      if (st) return st;
-      GenSpec g2 = gs;
-      g2.wtab = b.wtab;
-      k_h_pass1<KIND_DFT><<<N, 256, 0, stream>>>(g2, K, L.kp, b.Ht, b.hmax, b.hsum, b.hsq, b.prm);
-      break;
-    }
     default: return PSMMA_EUNSUPPORTED;
   }
   prof_mark(stream, "h_generate");
   k_split_params<<<PARAMS_BLOCKS, 512, 0, stream>>>(b.prm, cc.log2M, M, N, K, b.amax, b.asq, b.hmax, b.hsq);
   prof_mark(stream, "params");
-  if (!dft)
-    k_residues_A<<<dim3(L.kp / 64, (M + 31) / 32), 256, 0, stream>>>(A, lda, M, K, L.kp, b.amax, b.prm, cc, b.RA);
-  else
-    k_residues_A_dft<<<dim3((L.kp / 2 + 127) / 128, M), 128, 0, stream>>>(A, 2 * lda, gs.n_dft, L.kp, b.amax,
-                                                                           b.prm, cc, b.RA, M);
+  k_residues_A<<<dim3(L.kp / 64, (M + 31) / 32), 256, 0, stream>>>(A, lda, M, K, L.kp, b.amax, b.prm, cc, b.RA);
   prof_mark(stream, "residues_A");
   k_residues_H<<<dim3(rh_blocks_x(L.kp), N), 128, 0, stream>>>(b.Ht, N, L.kp, b.hmax, b.prm, cc, b.RH);
   prof_mark(stream, "residues_H");
@@ -1454,35 +1671,12 @@ static int split_core(int M, int N, int K, double alpha, const double* A, long l
   prof_mark(stream, "modular_gemm");
 
   dim3 gc((N + CRT_TJ - 1) / CRT_TJ, (M + CRT_TI - 1) / CRT_TI);
-  if (!dft)
-    (cc.top32 ? k_crt_combine<false, true> : k_crt_combine<false, false>)<<<gc, dim3(32, 8), 0, stream>>>(
-        b.R, M, N, L.kr, cc, b.amax, b.hmax, b.prm, alpha, beta, Q, ldq, 0);
-  else
-    (cc.top32 ? k_crt_combine<true, true> : k_crt_combine<true, false>)<<<gc, dim3(32, 8), 0, stream>>>(
-        b.R, M, N, L.kr, cc, b.amax, b.hmax, b.prm, alpha, beta, Q, 2 * ldq, 0);
+  (cc.top32 ? k_crt_combine<false, true> : k_crt_combine<false, false>)<<<gc, dim3(32, 8), 0, stream>>>(
+      b.R, M, N, L.kr, cc, b.amax, b.hmax, b.prm, alpha, beta, Q, ldq, 0);
   prof_mark(stream, "crt_combine");
   if (cudaGetLastError() != cudaSuccess) return PSMMA_EDEVICE;
 
-  if (status_dev_out && status_dev_out != kStatusWait) {
-    if (cudaMemcpyAsync(status_dev_out, &b.prm->status, sizeof(unsigned), cudaMemcpyDeviceToDevice, stream) !=
-        cudaSuccess)
-      return PSMMA_EDEVICE;
-    return PSMMA_OK;
-  }
-  if (!status_dev_out) {
-    // asynchronous: the status joins the stream's word, reported by psmma_stream_status
-    unsigned* acc = stream_status_word(stream);
-    if (acc) {
-      k_status_or<<<1, 1, 0, stream>>>(acc, &b.prm->status);
-      return cudaGetLastError() == cudaSuccess ? PSMMA_OK : PSMMA_EDEVICE;
-    }
-  }
-  unsigned st = 0;  // kStatusWait (or no status word): wait for the call and read its status
-  if (cudaMemcpyAsync(&st, &b.prm->status, sizeof(st), cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
-      cudaStreamSynchronize(stream) != cudaSuccess)
-    return PSMMA_EDEVICE;
-  if (st & DEV_ERR_TIMEOUT) return PSMMA_ETIMEDOUT;
-  return PSMMA_OK;
+  return split_status(b.prm, stream, status_dev_out);
 }
 
 // Host-pointer multiply with the copies overlapped (pinned host memory makes them
@@ -1740,18 +1934,84 @@ int launch_split_host_general(int M, int N, int K, double alpha, const double* A
 }
 
 // kind != DFT: Q (n x k) = alpha * A (n x k) * H (k x k) + beta * Q.
+// C (n x k complex, ldc) = alpha * F * B + beta * C on the split path, F(j, l) = w^(j l): the
+// rows of the product are the k columns of B (M = k), three real products per modulus (3M).
+static int split_core_dft3(int M, int nn, double alpha, const double* B, long ldb, double beta, double* C,
+                           long ldc, int nmod, void* work, size_t lwork, cudaStream_t stream,
+                           unsigned* status_dev_out) {
+  if (nmod < 8 || nmod > SPL_MAX_MODULI) return PSMMA_EUNSUPPORTED;
+  if (2 * nn >= (1 << 24) || M >= (1 << 30)) return PSMMA_EUNSUPPORTED;
+  const SplitLayout L = dft3_layout(M, nn, nmod);
+  if (lwork < L.total || !work) return PSMMA_EWORKSPACE;
+  char* w = (char*)work;
+  const SplitBuffers b = split_buffers(w, L);
+  const CrtConsts cc = get_consts(nmod);
+
+  prof_begin(stream);
+  if (cudaMemsetAsync(w, 0, L.off_wtab, stream) != cudaSuccess) return PSMMA_EDEVICE;  // params, maxima, sums
+  k_row_absmax_dft<<<M, 256, 0, stream>>>(B, 2 * ldb, nn, b.amax, b.asq);
+  prof_mark(stream, "row_scale");
+  int st = launch_dft_table(b.wtab, nn, stream);
+  if (st) return st;
+  k_h_pass1_dft3<<<nn, 256, 0, stream>>>(b.wtab, nn, L.kp, b.Ht, b.hmax, b.hsum, b.hsq, b.prm);
+  prof_mark(stream, "h_generate");
+  // the bounds are those of the real embedding: n columns, inner dimension 2n
+  k_split_params<<<PARAMS_BLOCKS, 512, 0, stream>>>(b.prm, cc.log2M, M, nn, 2 * nn, b.amax, b.asq, b.hmax, b.hsq);
+  prof_mark(stream, "params");
+  k_residues_A_dft3<<<dim3((L.kp / 2 + 127) / 128, M), 128, 0, stream>>>(B, 2 * ldb, nn, L.kp, b.amax, b.prm, cc,
+                                                                         b.RA, M);
+  prof_mark(stream, "residues_A");
+  k_residues_H_dft3<<<dim3(rh_blocks_x(L.kp), nn), 128, 0, stream>>>(b.Ht, nn, L.kp, b.hmax, b.prm, cc, b.RH);
+  prof_mark(stream, "residues_H");
+
+  using Shape = GemmShape<G_BN>;
+  if (cudaFuncSetAttribute(k_crt_gemm<G_BN, OneGemm>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)Shape::SMEM) != cudaSuccess)
+    return PSMMA_EDEVICE;
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return PSMMA_EDEVICE;
+  // T1 into the Re half; T2: Re = T1 - T2, Im = -T1 - T2; T3: Im += T3
+  const int kr1 = L.kr / 2;
+  for (int p = 0; p < 3; ++p) {
+    OneGemm og;
+    memset(&og, 0, sizeof(og));
+    __nv_bfloat16* ra = b.RA + (size_t)p * nmod * M * L.kp;
+    __nv_bfloat16* rh = b.RH + (size_t)p * nmod * nn * L.kp;
+    if (!make_tmap(&og.ta, ra, L.kp, M, nmod, G_BM) || !make_tmap(&og.tb, rh, L.kp, nn, nmod, G_BN))
+      return PSMMA_EDEVICE;
+    GemmArgs& ga = og.g;
+    ga.n = M;
+    ga.kr = L.kr;
+    ga.nkb = L.kp / G_BK;
+    ga.tiles_m = (M + G_BM - 1) / G_BM;
+    ga.tiles_n = (nn + G_BN - 1) / G_BN;
+    ga.group_m = 16;
+    ga.R = b.R + (p == 2 ? kr1 : 0);
+    ga.status = &b.prm->status;
+    ga.nmod = nmod;
+    ga.mode = p;
+    ga.im_off = kr1;
+    for (int l = 0; l < nmod; ++l) { ga.m[l] = cc.m[l]; ga.inv_m[l] = cc.inv_m[l]; }
+    const int total_tiles = ga.tiles_m * ga.tiles_n * nmod;
+    k_crt_gemm<G_BN, OneGemm><<<std::min(sms, total_tiles), G_THREADS, Shape::SMEM, stream>>>(og);
+  }
+  prof_mark(stream, "modular_gemm");
+  dim3 gc(L.kr / CRT_TJ, (M + CRT_TI - 1) / CRT_TI);
+  (cc.top32 ? k_crt_combine<true, true> : k_crt_combine<true, false>)<<<gc, dim3(32, 8), 0, stream>>>(
+      b.R, M, nn, L.kr, cc, b.amax, b.hmax, b.prm, alpha, beta, C, 2 * ldc, 0);
+  prof_mark(stream, "crt_combine");
+  if (cudaGetLastError() != cudaSuccess) return PSMMA_EDEVICE;
+  return split_status(b.prm, stream, status_dev_out);
+}
+
 // kind == DFT: C (n x k complex, ldq) = alpha * F (n x n) * B (n x k complex, lda) + beta * C,
-//   computed as [Re C^T | Im C^T] = [Re B^T | Im B^T] * [[Re F, Im F], [-Im F, Re F]].
+//   computed as C^T = B^T F in the 3M form (split_core_dft3).
 int launch_split_any(int kind, int n, int k, double alpha, const double* A, long lda, const double* gen,
                      long ldgen, double beta, double* Q, long ldq, int n_moduli, void* work, size_t lwork,
                      cudaStream_t stream, unsigned* status_dev_out) {
   const int nmod = resolve_nmod(n_moduli);
-  if (kind == KIND_DFT) {
-    GenSpec gs;
-    gs.kind = KIND_DFT;
-    gs.n_dft = n;
-    return split_core(k, 2 * n, 2 * n, alpha, A, lda, gs, beta, Q, ldq, nmod, work, lwork, stream, status_dev_out);
-  }
+  if (kind == KIND_DFT) return split_core_dft3(k, n, alpha, A, lda, beta, Q, ldq, nmod, work, lwork, stream, status_dev_out);
   const GenSpec gs = reference_gens(kind, gen, ldgen, k);
   return split_core(n, k, k, alpha, A, lda, gs, beta, Q, ldq, nmod, work, lwork, stream, status_dev_out);
 }
