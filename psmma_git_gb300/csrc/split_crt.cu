@@ -634,27 +634,32 @@ __device__ __forceinline__ void write_residue_quad(const unsigned long long (&u)
 constexpr int RH_PER_THREAD = 4;
 __host__ __device__ __forceinline__ int rh_blocks_x(int kp) { return (kp / RH_PER_THREAD + 127) / 128; }
 
-// RA[l][i][kk] = residues of A' (bf16), rows i, K-major.  Block: 32 rows x 64 k, transposed
-// through shared memory with element (k, r) at column (r + k/4) mod 32 of row k, so that both
-// the column-wise writes (32 rows of one k) and the reads (16 threads, 4 consecutive k each, of
-// one row) touch 16 distinct 8-byte bank pairs per half-warp.
+// RA[l][i][kk] = residues of A' (bf16), rows i, K-major.  Block: TR (32 or 64) rows x 64 k,
+// transposed through shared memory with element (k, r) at column (r + k/4) mod TR of row k, so
+// that both the column-wise writes (the rows of one k) and the reads (16 threads, 4
+// consecutive k each, of one row) touch 16 distinct 8-byte bank pairs per half-warp.
+template <int TR = 32>
 __device__ __forceinline__ void residues_A_blk(const double* __restrict__ A, long lda, const double* A2, long lda2,
                                                int ka, int n, int k, int kp,
                                                const unsigned long long* __restrict__ amax_bits,
                                                const SplitDevParams* prm, const CrtConsts& cc,
                                                __nv_bfloat16* __restrict__ RA, int bx, int by) {
-  __shared__ double tile[64][32];
-  const int i0 = by * 32, k0 = bx * 64;
+  __shared__ double tile[64][TR];
+  const int i0 = by * TR, k0 = bx * 64;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 256 threads: 8 x 32
   for (int kk = ty; kk < 64; kk += 8) {
-    int gi = i0 + tx, gk = k0 + kk;
-    tile[kk][(tx + (kk >> 2)) & 31] = (gi < n && gk < k) ? __ldg(acol(A, lda, A2, lda2, ka, gk) + gi) : 0.0;
+    const int gk = k0 + kk;
+#pragma unroll
+    for (int rr = tx; rr < TR; rr += 32) {
+      const int gi = i0 + rr;
+      tile[kk][(rr + (kk >> 2)) & (TR - 1)] = (gi < n && gk < k) ? __ldg(acol(A, lda, A2, lda2, ka, gk) + gi) : 0.0;
+    }
   }
   __syncthreads();
   const int P = prm->PA;
   const size_t plane = (size_t)n * kp;
   const int tq = threadIdx.x & 15, tr = threadIdx.x >> 4;  // 16 quads of k x 16 rows
-  for (int r = tr; r < 32; r += 16) {
+  for (int r = tr; r < TR; r += 16) {
     int gi = i0 + r;
     if (gi >= n) continue;
     unsigned long long ab = amax_bits[gi];
@@ -666,7 +671,7 @@ __device__ __forceinline__ void residues_A_blk(const double* __restrict__ A, lon
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       ng[q] = false;
-      u[q] = ok ? scaled_int(tile[kk + q][(r + tq) & 31], e, &ng[q]) : 0ull;
+      u[q] = ok ? scaled_int(tile[kk + q][(r + tq) & (TR - 1)], e, &ng[q]) : 0ull;
     }
     write_residue_quad(u, ng, cc, (uint2*)(RA + (size_t)gi * kp + k0 + kk), plane / 4);
   }
@@ -675,14 +680,14 @@ __device__ __forceinline__ void residues_A_blk(const double* __restrict__ A, lon
 __global__ void k_residues_A(const double* __restrict__ A, long lda, int n, int k, int kp,
                              const unsigned long long* __restrict__ amax_bits, const SplitDevParams* prm,
                              CrtConsts cc, __nv_bfloat16* __restrict__ RA) {
-  residues_A_blk(A, lda, nullptr, 0, k, n, k, kp, amax_bits, prm, cc, RA, blockIdx.x, blockIdx.y);
+  residues_A_blk<64>(A, lda, nullptr, 0, k, n, k, kp, amax_bits, prm, cc, RA, blockIdx.x, blockIdx.y);
 }
 
-// Rows [32 by0, 32 (by0 + gridDim.y)) of A only (a row panel of the host pipeline).
+// Rows [64 by0, 64 (by0 + gridDim.y)) of A only (a row panel of the host pipeline).
 __global__ void k_residues_A_rows(const double* __restrict__ A, long lda, int n, int k, int kp,
                                   const unsigned long long* __restrict__ amax_bits, const SplitDevParams* prm,
                                   CrtConsts cc, __nv_bfloat16* __restrict__ RA, int by0) {
-  residues_A_blk(A, lda, nullptr, 0, k, n, k, kp, amax_bits, prm, cc, RA, blockIdx.x, by0 + blockIdx.y);
+  residues_A_blk<64>(A, lda, nullptr, 0, k, n, k, kp, amax_bits, prm, cc, RA, blockIdx.x, by0 + blockIdx.y);
 }
 
 // The guessed bit counts that a speculative host pipeline scales with.
@@ -1639,7 +1644,7 @@ static int split_core(int M, int N, int K, double alpha, const double* A, long l
   prof_mark(stream, "h_generate");
   k_split_params<<<PARAMS_BLOCKS, 512, 0, stream>>>(b.prm, cc.log2M, M, N, K, b.amax, b.asq, b.hmax, b.hsq);
   prof_mark(stream, "params");
-  k_residues_A<<<dim3(L.kp / 64, (M + 31) / 32), 256, 0, stream>>>(A, lda, M, K, L.kp, b.amax, b.prm, cc, b.RA);
+  k_residues_A<<<dim3(L.kp / 64, (M + 63) / 64), 256, 0, stream>>>(A, lda, M, K, L.kp, b.amax, b.prm, cc, b.RA);
   prof_mark(stream, "residues_A");
   k_residues_H<<<dim3(rh_blocks_x(L.kp), N), 128, 0, stream>>>(b.Ht, N, L.kp, b.hmax, b.prm, cc, b.RH);
   prof_mark(stream, "residues_H");
@@ -1779,7 +1784,7 @@ static int split_core_host(int M, int N, int K, double alpha, const double* A_h,
       rest -= t;
     }
   }
-  static_assert(G_BM % CRT_TI == 0 && G_BM % 32 == 0, "row panels must cover whole CRT and residue blocks");
+  static_assert(G_BM % CRT_TI == 0 && G_BM % 64 == 0, "row panels must cover whole CRT and residue blocks");
   const int kchunk = 1024;
   // GEMM + CRT of panel p (rows [r0, r1)) with the bit counts in *pk, then its download
   auto panel = [&](int p, const SplitDevParams* pk) {
@@ -1826,8 +1831,8 @@ static int split_core_host(int M, int N, int K, double alpha, const double* A_h,
       const int kc = 256;
       dim3 g1((r1 - r0 + 127) / 128, (K + kc - 1) / kc);
       k_row_absmax<<<g1, 128, 0, s>>>(dA + r0, M, r1 - r0, K, kc, b.amax + r0, b.asq + r0);
-      k_residues_A_rows<<<dim3(L.kp / 64, (r1 - r0 + 31) / 32), 256, 0, s>>>(dA, M, M, K, L.kp, b.amax,
-                                                                             b.prm_guess, cc, b.RA, r0 / 32);
+      k_residues_A_rows<<<dim3(L.kp / 64, (r1 - r0 + 63) / 64), 256, 0, s>>>(dA, M, M, K, L.kp, b.amax,
+                                                                             b.prm_guess, cc, b.RA, r0 / 64);
       prof_mark(s, "panel_rows");
       panel(p, b.prm_guess);
     }
@@ -1840,7 +1845,7 @@ static int split_core_host(int M, int N, int K, double alpha, const double* A_h,
     if (head.PA == pa_guess && head.PH == ph_guess) return PSMMA_OK;
     // a wrong guess: everything after the parameter pass again, with the computed bit counts
     prof_mark(s, "redo_wrong_guess");
-    k_residues_A<<<dim3(L.kp / 64, (M + 31) / 32), 256, 0, s>>>(dA, M, M, K, L.kp, b.amax, b.prm, cc, b.RA);
+    k_residues_A<<<dim3(L.kp / 64, (M + 63) / 64), 256, 0, s>>>(dA, M, M, K, L.kp, b.amax, b.prm, cc, b.RA);
     k_residues_H<<<grh, 128, 0, s>>>(b.Ht, N, L.kp, b.hmax, b.prm, cc, b.RH);
     ok &= cudaEventRecord(ev_start, s) == cudaSuccess;
     ok &= cudaStreamWaitEvent(cs, ev_start, 0) == cudaSuccess;
@@ -1870,7 +1875,7 @@ static int split_core_host(int M, int N, int K, double alpha, const double* A_h,
   if (!ok) return PSMMA_EDEVICE;
   prof_mark(s, "a_upload_rows");
   k_split_params<<<PARAMS_BLOCKS, 512, 0, s>>>(b.prm, cc.log2M, M, N, K, b.amax, b.asq, b.hmax, b.hsq);
-  k_residues_A<<<dim3(L.kp / 64, (M + 31) / 32), 256, 0, s>>>(dA, M, M, K, L.kp, b.amax, b.prm, cc, b.RA);
+  k_residues_A<<<dim3(L.kp / 64, (M + 63) / 64), 256, 0, s>>>(dA, M, M, K, L.kp, b.amax, b.prm, cc, b.RA);
   if (ph_guess >= 8)
     k_residues_H_spec<<<grh, 128, 0, s>>>(b.Ht, N, L.kp, b.hmax, b.prm, cc, b.RH, ph_guess, 1);
   else
@@ -2091,7 +2096,7 @@ __global__ void __launch_bounds__(1024) k_g_split_params(const GProb* d, double 
 __global__ void __launch_bounds__(256) k_g_residues_A(const GProb* d, int count, CrtConsts cc) {
   const GProb& e = d[gfind<2>(d, count, blockIdx.x)];
   const int local = blockIdx.x - e.b_ra, gx = e.kp / 64;
-  residues_A_blk(e.A, e.lda, e.A2, e.lda2, e.ka, e.M, e.K, e.kp, e.amax, e.prm, cc, e.RA, local % gx, local / gx);
+  residues_A_blk<64>(e.A, e.lda, e.A2, e.lda2, e.ka, e.M, e.K, e.kp, e.amax, e.prm, cc, e.RA, local % gx, local / gx);
 }
 
 __global__ void __launch_bounds__(128) k_g_residues_H(const GProb* d, int count, CrtConsts cc) {
@@ -2161,7 +2166,7 @@ int plan_group(const SplitProblem* P, int count, int nmod, const SplitTune& tune
     e.R = w.take<int8_t>((size_t)nmod * e.M * e.kr, 1024);
     e.b_row = b_row; b_row += ((e.M + 127) / 128) * ((e.K + G_ROW_KCHUNK - 1) / G_ROW_KCHUNK);
     e.b_h = b_h;     b_h += e.N;
-    e.b_ra = b_ra;   b_ra += (e.kp / 64) * ((e.M + 31) / 32);
+    e.b_ra = b_ra;   b_ra += (e.kp / 64) * ((e.M + 63) / 64);
     e.b_rh = b_rh;   b_rh += rh_blocks_x(e.kp) * e.N;
     e.b_crt = b_crt; b_crt += ((e.N + CRT_TJ - 1) / CRT_TJ) * ((e.M + CRT_TI - 1) / CRT_TI);
   }
