@@ -738,8 +738,9 @@ __global__ void k_residues_H_spec(const double* __restrict__ Ht, int ncols, int 
   residues_H_blk(Ht, ncols, kp, hmax_bits, prm, cc, RH, blockIdx.x, blockIdx.y, redo ? -1 : guess);
 }
 
-// DFT A side: row i of the embedded operand X' = [Re B^T | Im B^T] is column i of B, read
-// contiguously (Bre = B as interleaved doubles, ldb2 = 2*ldb).  One block per row.
+// DFT A side: row i of the product (B^T) is column i of B, read contiguously (Bre = B as
+// interleaved doubles, ldb2 = 2*ldb); its maximum and sum of squares run over both the real
+// and the imaginary parts.  One block per row.
 __global__ void k_row_absmax_dft(const double* __restrict__ Bre, long ldb2, int nn,
                                  unsigned long long* __restrict__ amax_bits, double* __restrict__ asq) {
   const int i = blockIdx.x;
@@ -1579,14 +1580,9 @@ __global__ void k_status_or(unsigned* acc, const unsigned* st) {
   if (v) atomicOr(acc, v);
 }
 
-// Core of the split path: Q (M x N) = alpha * A' (M x K) * H (K x N) + beta * Q where A' is
-// A (column-major, lda) or, for the DFT, the embedding [Re B^T | Im B^T] of B (complex, lda),
-// H is generated from gs, and the output is column-major Q (ldq) or, for the DFT, the
-// interleaved complex C (ldq).  Status: status_dev_out == nullptr ORs the call's device status
-// into the stream's status word (no synchronisation), kStatusWait waits and returns it, any other
-// pointer receives a copy of it (no synchronisation).
-// The device status of a split call: copied to the caller's word, ORed into the stream's word
-// (asynchronous), or waited for and returned (kStatusWait, or no stream word).
+// The device status of a split call: status_dev_out == nullptr ORs it into the stream's status
+// word (no synchronisation), kStatusWait waits and returns it, any other pointer receives a copy
+// of it (no synchronisation).
 static int split_status(SplitDevParams* prm, cudaStream_t stream, unsigned* status_dev_out) {
   if (status_dev_out && status_dev_out != kStatusWait) {
     if (cudaMemcpyAsync(status_dev_out, &prm->status, sizeof(unsigned), cudaMemcpyDeviceToDevice, stream) !=
@@ -1610,6 +1606,8 @@ static int split_status(SplitDevParams* prm, cudaStream_t stream, unsigned* stat
   return PSMMA_OK;
 }
 
+// Core of the split path: Q (M x N) = alpha * A (M x K, column-major, lda) * H (K x N) + beta * Q
+// (column-major, ldq), H generated from gs (any kind but the DFT: split_core_dft3).
 static int split_core(int M, int N, int K, double alpha, const double* A, long lda, const GenSpec& gs, double beta,
                       double* Q, long ldq, int nmod, void* work, size_t lwork, cudaStream_t stream,
                       unsigned* status_dev_out) {
