@@ -197,6 +197,27 @@ def test_split_dft_matches_fft(n, k, cuda):
     assert O.rel_fro(got, ref) < TOL
 
 
+@pytest.mark.parametrize("n,k,pad", [(300, 7, 5), (513, 130, 3)])
+def test_split_dft_padded_leading_dimensions(n, k, pad, cuda):
+    # B and C as column blocks of larger complex arrays (ldb = ldc = n + pad); n is not a
+    # multiple of 256, so the imaginary half of the residue planes starts after padding
+    import psmma_git_gb300 as P
+    import torch
+    B = O.cfg_matrix(n, k, seed=n + 11, complex_=True)
+    C0 = O.cfg_matrix(n, k, seed=k + 12, complex_=True)
+    Bbig = np.zeros((n + pad, k), np.complex128)
+    Bbig[:n] = B
+    Cbig = np.full((n + pad, k), 7.0 + 7.0j)
+    Cbig[:n] = C0
+    dB = _t(Bbig, cuda)[:n]
+    dC = _t(Cbig, cuda)
+    P.pzmdftl(n, k, 0.5, dB, -2.0, dC[:n], precision="split")
+    torch.cuda.synchronize()
+    got = _np(dC)
+    assert O.rel_fro(got[:n], O.dft_product(0.5, B, -2.0, C0)) < TOL
+    assert np.all(got[n:] == 7.0 + 7.0j)  # rows past n untouched
+
+
 def test_split_dft_ones_fixture(cuda):
     z = np.load(GOLDEN / "dft_ones_kat.npz")
     n = int(z["n"])
