@@ -794,9 +794,16 @@ __global__ void __launch_bounds__(256) k_h_pass1_dft3(const double2* __restrict_
   float s32 = 0.0f, s2_32 = 0.0f;
   int e = NO_SCALE;
   bool big = false;
+  // table index t = (l j) mod n, advanced by (blockDim j) mod n per step (no division per entry)
+  int t = (int)(((long long)threadIdx.x * j) % nn);
+  const int step = (int)(((long long)blockDim.x * j) % nn);
   for (int l = threadIdx.x; l < kp; l += blockDim.x) {
     double2 wv = make_double2(0.0, 0.0);
-    if (l < nn) wv = __ldg(wtab + (int)(((long long)l * j) % nn));
+    if (l < nn) {
+      wv = __ldg(wtab + t);
+      t += step;
+      t -= t >= nn ? nn : 0;
+    }
     rr[l] = wv.x;
     ri[l] = wv.y;
 #pragma unroll
