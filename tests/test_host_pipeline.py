@@ -120,3 +120,17 @@ def test_host_split_row_panels_repeat_ragged(kind):
         getattr(P, "psmma_" + kind)(n, k, 1.0, np.asfortranarray(A), gen, 0.0, Qh, precision="split")
         exact = O.dense_product(kind, 1.0, A, gen, 0.0, None, k)
         assert O.rel_fro(Qh, exact) < 1e-12
+
+
+@pytest.mark.gpu
+def test_host_split_panel_cuts():
+    # 4300 rows = 34 row tiles (the last one ragged): the speculative calls cut the first
+    # eighth to two tiles and halve the last one three times (panels 2, 3, 5 x 5, 2, 1, 1)
+    import psmma_git_gb300 as P
+    n, k = 4300, 300
+    gen = np.asfortranarray(O.cfg_cauchy_generators(k, seed=71, clustered=0.1))
+    for seed in (72, 73, 74):
+        A = O.cfg_matrix(n, k, seed=seed, dist="normal")
+        Qh = np.full((n, k), np.nan, order="F")
+        P.psmma_cauchy(n, k, 1.0, np.asfortranarray(A), gen, 0.0, Qh, precision="split")
+        assert O.rel_fro(Qh, O.dense_product("cauchy", 1.0, A, gen, 0.0, None, k)) < 1e-12
