@@ -746,12 +746,28 @@ __global__ void k_row_absmax_dft(const double* __restrict__ Bre, long ldb2, int 
   const int i = blockIdx.x;
   const double* col = Bre + (long)i * ldb2;
   unsigned long long mb = 0;
-  double sq = 0.0;
+  // sum of squares in round-up FP32 on the thread's power-of-two scale (an upper bound), FP64
+  // for a thread whose entries reach 2^56 times its first one
+  float sq32 = 0.0f;
+  int e = NO_SCALE;
+  bool big = false;
   for (int t = threadIdx.x; t < 2 * nn; t += blockDim.x) {
-    const double a = __ldg(col + t);
-    unsigned long long b = (unsigned long long)__double_as_longlong(a) & ABS_MASK;
+    const unsigned long long b = (unsigned long long)__double_as_longlong(__ldg(col + t)) & ABS_MASK;
     mb = b > mb ? b : mb;
-    sq = fma(a, a, sq);
+    if (e == NO_SCALE && b) e = (int)(b >> 52) - 1023;
+    if (e != NO_SCALE) {
+      const float f = abs_scaled_up(b, e, &big);
+      sq32 = __fmaf_ru(f, f, sq32);
+    }
+  }
+  double sq = 0.0;
+  if (big) {
+    for (int t = threadIdx.x; t < 2 * nn; t += blockDim.x) {
+      const double a = __ldg(col + t);
+      sq = fma(a, a, sq);
+    }
+  } else if (e != NO_SCALE) {
+    sq = ldexp((double)sq32, 2 * e);
   }
   __shared__ unsigned long long smax[32];
   __shared__ double ssq[32];
