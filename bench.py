@@ -561,6 +561,15 @@ def run_cfg1(args, ws, rank, local):
             e[i + 1].record()
         torch.cuda.synchronize()
         t = e[0].elapsed_time(e[args.steps]) / args.steps
+        # one traced call after the timed ones: the split path's phases
+        lib = P.load()
+        lib.psmma_set_profiling(1)
+        run("split", Y)
+        ms = (ctypes.c_float * 40)()
+        names = (ctypes.c_char_p * 40)()
+        m = lib.psmma_profile_read(ms, names, 40)
+        lib.psmma_set_profiling(0)
+        phases = [[names[j].decode(), round(ms[j], 3)] for j in range(max(0, m))]
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
         run("fp64", Y64)
@@ -587,7 +596,7 @@ def run_cfg1(args, ws, rank, local):
         out[kind] = {"split_ms": t, "split_tflops": flops / t / 1e9, "fp64_ms": t64,
                      "fp64_tflops": flops / t64 / 1e9, "speedup": t64 / t,
                      "rel_err_split_vs_fp64": rel, "rel_err_split_vs_fft_oracle_sample": err_split,
-                     "rel_err_fp64_vs_fft_oracle_sample": err_64}
+                     "rel_err_fp64_vs_fft_oracle_sample": err_64, "split_phases_ms": phases}
         if kind == "dft":
             out[kind]["split_complex_mac_tflops"] = 2.0 * n ** 3 / t / 1e9
         print(json.dumps({kind: out[kind]}), file=sys.stderr, flush=True)

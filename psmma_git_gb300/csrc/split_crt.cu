@@ -1078,13 +1078,20 @@ __device__ __forceinline__ int mod_sym(int s, int m, float inv_m) {
   return x;
 }
 
+// s mod m in [-128, 127] for |s| <= 256 and 191 <= m <= 256 (every modulus of the split path):
+// one conditional subtraction or addition of m (s - m >= -65 above 127, s + m <= 127 below -128).
+__device__ __forceinline__ int mod_sym_small(int s, int m) {
+  s -= s > 127 ? m : 0;
+  s += s < -128 ? m : 0;
+  return s;
+}
+
 // Epilogue of the 3M complex product's second and third GEMMs: combine this tile's residues x
 // (in [-128, 127]) with those already in the output plane, 16 bytes at a time.
 // mode 1: old = T1 -> store (T1 - x) mod m, and (-T1 - x) mod m at dst + im_off;
 // mode 2: old = -T1 - T2 -> store (old + x) mod m.
 template <int HALF>
-__device__ __forceinline__ void store_combined(int8_t* dst, const int (&res)[HALF], int mode, int im_off, int m,
-                                               float inv_m) {
+__device__ __forceinline__ void store_combined(int8_t* dst, const int (&res)[HALF], int mode, int im_off, int m) {
 #pragma unroll
   for (int v = 0; v < HALF / 16; ++v) {
     const uint4 o = *(const uint4*)(dst + v * 16);
@@ -1098,9 +1105,9 @@ __device__ __forceinline__ void store_combined(int8_t* dst, const int (&res)[HAL
       for (int bb = 0; bb < 4; ++bb) {
         const int old = (int)(int8_t)(ow[t4] >> (8 * bb));
         const int x = res[v * 16 + t4 * 4 + bb];
-        const int a = mod_sym(mode == 1 ? old - x : old + x, m, inv_m);
+        const int a = mod_sym_small(mode == 1 ? old - x : old + x, m);
         w1[t4] |= (uint32_t)(uint8_t)(int8_t)a << (8 * bb);
-        if (mode == 1) w2[t4] |= (uint32_t)(uint8_t)(int8_t)mod_sym(-old - x, m, inv_m) << (8 * bb);
+        if (mode == 1) w2[t4] |= (uint32_t)(uint8_t)(int8_t)mod_sym_small(-old - x, m) << (8 * bb);
       }
     }
     *(uint4*)(dst + v * 16) = make_uint4(w1[0], w1[1], w1[2], w1[3]);
@@ -1273,7 +1280,7 @@ __global__ void __launch_bounds__(G_THREADS, 1) k_crt_gemm(const __grid_constant
       const int i = ti.tm * G_BM + q * 32 + lane;
       if (ok && !*abort_flag && i < ti.n && g.mode != 0) {
         int8_t* dst = ti.R + ((size_t)ti.l * ti.n + i) * ti.kr + (size_t)ti.tn * BN + h * HALF;
-        store_combined<HALF>(dst, res, g.mode, g.im_off, mi, inv_m);
+        store_combined<HALF>(dst, res, g.mode, g.im_off, mi);
       } else if (ok && !*abort_flag && i < ti.n) {
         int8_t* dst = ti.R + ((size_t)ti.l * ti.n + i) * ti.kr + (size_t)ti.tn * BN + h * HALF;
 #pragma unroll
@@ -2021,8 +2028,8 @@ static int split_core_dft3(int M, int nn, double alpha, const double* B, long ld
     for (int l = 0; l < nmod; ++l) { ga.m[l] = cc.m[l]; ga.inv_m[l] = cc.inv_m[l]; }
     const int total_tiles = ga.tiles_m * ga.tiles_n * nmod;
     k_crt_gemm<G_BN, OneGemm><<<std::min(sms, total_tiles), G_THREADS, Shape::SMEM, stream>>>(og);
+    prof_mark(stream, p == 0 ? "gemm_T1" : p == 1 ? "gemm_T2_combine" : "gemm_T3_combine");
   }
-  prof_mark(stream, "modular_gemm");
   dim3 gc(L.kr / CRT_TJ, (M + CRT_TI - 1) / CRT_TI);
   (cc.top32 ? k_crt_combine<true, true> : k_crt_combine<true, false>)<<<gc, dim3(32, 8), 0, stream>>>(
       b.R, M, nn, L.kr, cc, b.amax, b.hmax, b.prm, alpha, beta, C, 2 * ldc, 0);
