@@ -38,9 +38,6 @@ __all__ = [
     "toeplitz_batch_lowrank", "stream_status",
 ]
 
-# The split path (exact modular slices on the BF16 tensor cores) is built into the library.
-SPLIT_AVAILABLE = True
-
 _PREC = {"fp64": PREC_FP64, "split": PREC_SPLIT, PREC_FP64: PREC_FP64, PREC_SPLIT: PREC_SPLIT}
 
 
