@@ -497,7 +497,8 @@ def run_serving(args, ws, rank, local):
                         "throughput_req_s": len(done) / wall, "throughput_tflops": tot_fl / wall / 1e12,
                         "p50_ms": float(np.percentile(lats, 50)), "p99_ms": float(np.percentile(lats, 99)),
                         "max_ms": float(lats.max()),
-                        "mean_gpu_ms": float(np.mean([i["gpu_ms"] for i, _ in done]))})
+                        "mean_gpu_ms": float(np.mean([i["gpu_ms"] for i, _ in done])),
+                        "p99_within_bound": bool(np.percentile(lats, 99) < args.p99_bound_ms)})
         print(json.dumps({"serving_rate": results[-1]}), file=sys.stderr, flush=True)
     line = {"metric": "serving: p50/p99 latency (ms) and effective TFLOP/s under a Poisson stream",
             "unit": "ms", "n_gpus": 1, "data": "synthetic",
@@ -505,7 +506,7 @@ def run_serving(args, ws, rank, local):
                                    f"[512, {nmax}], split precision ({args.n_moduli} moduli), device-resident "
                                    "operands", "hbm_budget_gib": args.serve_budget_gib,
                        "max_inflight": args.inflight, "seconds_per_rate": args.serve_seconds},
-            "sweep": results}
+            "p99_bound_ms": args.p99_bound_ms, "sweep": results}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -968,6 +969,8 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=6.0)
     ap.add_argument("--serve-nmax", type=int, default=16384)
     ap.add_argument("--serve-budget-gib", type=int, default=96)
+    ap.add_argument("--p99-bound-ms", type=float, default=250.0,
+                    help="serving: the stated p99 latency bound the sweep is checked against")
     ap.add_argument("--merge-level", action="store_true", help="run the batched merge level (64 problems)")
     ap.add_argument("--cfg1", action="store_true", help="run the Toeplitz/Hankel/DFT multiplies at n = 8192")
     ap.add_argument("--cfg1-n", type=int, default=8192)
