@@ -142,7 +142,11 @@ int pzmdftl1(int n, int k, double alpha, const psmma_complex* B, int ldb,
  * split workspace fits in it (n = k = 1024 with the default 14 moduli does) and returns
  * PSMMA_ESCRATCH otherwise.  All calls share that array: calls that overlap on the GPU
  * (other streams or threads) race and must be serialised by the caller.  The first call
- * on a device looks up the array's address; make it before any stream capture. */
+ * on a device looks up the array's address and keeps it until the process exits (a
+ * cudaDeviceReset afterwards is not supported); make that first call before any stream
+ * capture.  Unlike psmma_cauchy, the call blocks: it waits for its work on `stream` and
+ * returns the device status, so Q is written when it returns.  alpha = 0 only scales Q by
+ * beta (A and gen are not read), as in psmma_cauchy. */
 int psmma_cauchy_split_noalloc(int n, int k, double alpha, const double* A, int lda,
                                const double* gen, int ldgen, double beta, double* Q, int ldq,
                                int n_moduli, void* stream);
@@ -186,7 +190,8 @@ typedef struct psmma_batch_stats {
   int n_blocks;            /* off-diagonal blocks */
   int max_rank;
   int full_rank_blocks;    /* blocks multiplied as generated tiles */
-  int reserved;
+  int graph_reused;        /* 1: the product rounds relaunched the stream's cached CUDA graph,
+                              updated in place (cudaGraphExecUpdate); 0: it was instantiated */
 } psmma_batch_stats;
 
 int psmma_cauchy_batch_lowrank(int count, const psmma_batch_item* items, double alpha, double beta,
@@ -403,8 +408,17 @@ size_t psmma_workspace_size(int kind, int n, int k, const psmma_opts* opts);
 void psmma_release_workspace(void);
 
 /* Waits for `stream` and returns PSMMA_ETIMEDOUT if a split-path call enqueued on it since the
- * last check recorded a device-side timeout (then clears the record), else PSMMA_OK. */
+ * last check recorded a device-side timeout (then clears the record), else PSMMA_OK.  The
+ * record is kept per (device, stream handle) in a small device word created by the stream's
+ * first split-path call; a stream destroyed before its status was read leaves its record
+ * behind, and a new stream that gets the same handle value would inherit it: read the
+ * status, or call psmma_stream_release, before destroying a stream. */
 int psmma_stream_status(void* stream);
+
+/* Waits for `stream`, frees the status record of (current device, stream) and returns what
+ * psmma_stream_status would have returned.  Call it before cudaStreamDestroy on streams that
+ * ran split-path calls; a later call on the stream creates a fresh record. */
+int psmma_stream_release(void* stream);
 
 /* Per-phase tracing.  While enabled, each call records a CUDA event on its stream after
  * every phase (split path: row scales, H generation, parameters, A residues, H residues,

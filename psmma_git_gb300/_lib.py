@@ -76,7 +76,7 @@ class PsmmaBatchItem(C.Structure):
 class PsmmaBatchStats(C.Structure):
     _fields_ = [
         ("effective_flops", C.c_double), ("executed_flops", C.c_double), ("compress_flops", C.c_double),
-        ("n_blocks", C.c_int), ("max_rank", C.c_int), ("full_rank_blocks", C.c_int), ("reserved", C.c_int),
+        ("n_blocks", C.c_int), ("max_rank", C.c_int), ("full_rank_blocks", C.c_int), ("graph_reused", C.c_int),
     ]
 
 
@@ -119,6 +119,7 @@ SIGNATURES = {
     "psmma_workspace_size": (C.c_size_t, [_i, _i, _i, _op]),
     "psmma_release_workspace": (None, []),
     "psmma_stream_status": (_i, [_p]),
+    "psmma_stream_release": (_i, [_p]),
     "psmma_status_string": (C.c_char_p, [_i]),
     "psmma_set_profiling": (None, [_i]),
     "psmma_profile_read": (_i, [C.POINTER(C.c_float), C.POINTER(C.c_char_p), _i]),

@@ -539,6 +539,12 @@ int host_dft(int n, int k, double alpha, const psmma_complex* B, int ldb, double
 thread_local int g_last_status = PSMMA_OK;
 
 }  // namespace
+
+int check_real_args(int kind, int n, int k, double alpha, const double* A, int lda, const double* gen,
+                    int ldgen, double beta, const double* Q, int ldq) {
+  return check_real(kind, n, k, alpha, A, lda, gen, ldgen, beta, Q, ldq);
+}
+
 }  // namespace psmma
 
 using namespace psmma;
@@ -661,6 +667,23 @@ int psmma_stream_status(void* stream) {
   if (cudaMemsetAsync(w, 0, sizeof(unsigned), s) != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess)
     return PSMMA_EDEVICE;
   return (h & DEV_ERR_TIMEOUT) ? PSMMA_ETIMEDOUT : PSMMA_EDEVICE;
+}
+
+int psmma_stream_release(void* stream) {
+  const int st = psmma_stream_status(stream);
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return PSMMA_EDEVICE;
+  unsigned* w = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_stw_mu);
+    auto it = g_stw.find({dev, (cudaStream_t)stream});
+    if (it != g_stw.end()) {
+      w = it->second;
+      g_stw.erase(it);
+    }
+  }
+  if (w) cudaFree(w);  // the stream has drained (psmma_stream_status waited for it)
+  return st;
 }
 
 void psmma_release_workspace(void) {

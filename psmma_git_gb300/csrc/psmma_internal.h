@@ -99,6 +99,11 @@ int launch_struct_f64_ws(int M, int N, int K, double alpha, const double* X, lon
 size_t f64_splitk_bytes(int M, int N, int K, int sms);
 int launch_dft_table(double2* w, int n, cudaStream_t stream);
 
+// Argument checks of PSCAUCHY_COMPUTE / PSTOEPLITZ_COMPUTE / PSHANKEL_COMPUTE on a 1x1 grid
+// (psmma_capi.cu): 0 = run, 1 = quick return (nothing to do), else the status to return.
+int check_real_args(int kind, int n, int k, double alpha, const double* A, int lda, const double* gen,
+                    int ldgen, double beta, const double* Q, int ldq);
+
 // Split path (split_crt.cu).
 size_t split_workspace_bytes(int kind, int n, int k, int n_moduli);
 // wait_status: wait for the call and return its device status (for callers that must not

@@ -16,8 +16,14 @@
 //    other host threads) race on it and must be serialised by the caller; the buffers that
 //    must start at zero are cleared by every call, the rest are overwritten;
 //  * the first call on a device looks up the array's device address (cudaGetSymbolAddress,
-//    with that device current) and caches it; make that first call before any stream
-//    capture on that device.
+//    with that device current) and caches it until the process exits (a cudaDeviceReset,
+//    which reloads the module, is not supported afterwards); make that first call before
+//    any stream capture on that device;
+//  * the call blocks: it waits for its work on the stream to finish and reads the device
+//    status back (it may not allocate the per-stream status word of the asynchronous entry
+//    points), so it returns with Q written;
+//  * alpha = 0 scales Q by beta and reads neither A nor the generators, as psmma_cauchy and
+//    the reference's DGEMM do.
 #include <mutex>
 
 #include "psmma_internal.h"
@@ -62,20 +68,24 @@ using namespace psmma;
 extern "C" int psmma_cauchy_split_noalloc(int n, int k, double alpha, const double* A, int lda,
                                           const double* gen, int ldgen, double beta, double* Q, int ldq,
                                           int n_moduli, void* stream) {
-  // Argument checks with the numbering of PSCAUCHY_COMPUTE (pscauchy_compute.f90:234-255).
-  if (n < 0) return -2;
-  if (k < 0) return -3;
-  if (lda < (n > 1 ? n : 1)) return -9;
-  if (ldq < (n > 1 ? n : 1)) return -14;
+  // Argument checks and quick return of psmma_cauchy, with the numbering of PSCAUCHY_COMPUTE
+  // (pscauchy_compute.f90:234-255).
   if (n_moduli != 0 && (n_moduli < 8 || n_moduli > 16)) return PSMMA_EUNSUPPORTED;
-  if (n == 0 || k == 0 || ((alpha == 0.0) && beta == 1.0)) return PSMMA_OK;
-  if (!Q || !A) return PSMMA_ENULL;
-  if (!gen || ldgen < k) return PSMMA_EGEN;
+  int st = check_real_args(KIND_CAUCHY, n, k, alpha, A, lda, gen, ldgen, beta, Q, ldq);
+  if (st == 1) return PSMMA_OK;
+  if (st) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (alpha == 0.0) {
+    // Q := beta*Q: the DGEMM of pscauchy_compute.f90:406 with alpha = 0 reads neither operand.
+    GenSpec none;
+    st = launch_struct_f64_ws(n, k, k, 0.0, nullptr, lda, none, beta, Q, ldq, nullptr, 0, s);
+    if (st) return st;
+    return cudaStreamSynchronize(s) == cudaSuccess ? PSMMA_OK : PSMMA_EDEVICE;
+  }
   const size_t need = split_workspace_bytes(KIND_CAUCHY, n, k, n_moduli);
   if (need > kNoAllocScratchBytes) return PSMMA_ESCRATCH;
-  int st = PSMMA_OK;
   void* work = noalloc_scratch(&st);
   if (st) return st;
   return launch_split(KIND_CAUCHY, n, k, alpha, A, lda, gen, ldgen, beta, Q, ldq, n_moduli, work,
-                      kNoAllocScratchBytes, (cudaStream_t)stream, true);
+                      kNoAllocScratchBytes, s, true);
 }

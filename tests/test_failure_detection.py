@@ -77,3 +77,12 @@ def test_split_calls_report_device_status_per_stream(lib, cuda):
     ref = O.dense_product("cauchy", 1.0, A, gen, 0.0, None, k)
     for dQ in outs:
         assert O.rel_fro(dQ.cpu().numpy(), ref) < 1e-12
+    # releasing the stream's record before the stream goes away; a later call makes a new one
+    assert lib.psmma_stream_release(C.c_void_p(s.cuda_stream)) == 0
+    assert lib.psmma_stream_release(C.c_void_p(s.cuda_stream)) == 0  # nothing left: waits only
+    dQ = P.fortran_empty(n, k, torch.float64, cuda)
+    with torch.cuda.stream(s):
+        P.psmma_cauchy(n, k, 1.0, dA, dg, 0.0, dQ, precision="split", stream=s)
+    P.stream_status(s)
+    assert O.rel_fro(dQ.cpu().numpy(), ref) < 1e-12
+    assert lib.psmma_stream_release(C.c_void_p(s.cuda_stream)) == 0
