@@ -661,6 +661,43 @@ def exact_cauchy_product(A, gen, k: int):
     return out
 
 
+def decimal_cauchy_product(A_rows, gen, cols, k: int, digits: int = 40) -> np.ndarray:
+    """(A_rows @ H)[:, cols] with every operation in ``decimal`` arithmetic at ``digits``
+    significant digits on the exact values of the FP64 inputs (Decimal(float) is exact), for
+    samples of products too large for Fraction: relative error ~k * 10^-digits."""
+    import decimal
+    ctx = decimal.Context(prec=digits)
+    Dd = decimal.Decimal
+    gen = np.asarray(gen, dtype=np.float64)
+    D = [Dd(float(x)) for x in gen[:k, 0]]
+    U = [Dd(float(x)) for x in gen[:k, 2]]
+    cols = list(cols)
+    Hc = []
+    for j in cols:
+        fj, vj = Dd(float(gen[j, 1])), Dd(float(gen[j, 3]))
+        Hc.append([ctx.divide(ctx.multiply(U[i], vj), ctx.subtract(D[i], fj)) for i in range(k)])
+    A_rows = np.asarray(A_rows, dtype=np.float64)
+    out = np.empty((A_rows.shape[0], len(cols)))
+    for r in range(A_rows.shape[0]):
+        ar = [Dd(float(x)) for x in A_rows[r, :k]]
+        for c, h in enumerate(Hc):
+            s = Dd(0)
+            for i in range(k):
+                s = ctx.fma(ar[i], h[i], s)
+            out[r, c] = float(s)
+    return out
+
+
+def col_max_rel(x, ref) -> float:
+    """Largest per-column relative 2-norm error max_j ||x_j - ref_j|| / ||ref_j|| (columns
+    of zero norm count their absolute error)."""
+    x = np.asarray(x)
+    ref = np.asarray(ref)
+    num = np.linalg.norm(x - ref, axis=0)
+    den = np.linalg.norm(ref, axis=0)
+    return float(np.max(num / np.where(den > 0, den, 1.0)))
+
+
 def rel_fro(x, ref) -> float:
     """Relative Frobenius error ||x - ref||_F / ||ref||_F."""
     x = np.asarray(x)

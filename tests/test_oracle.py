@@ -60,6 +60,19 @@ def test_cauchy_golden_exact_rational():
             assert O.rel_fro(got, z["X"]) > 1e-6
 
 
+def test_decimal_cauchy_sample_matches_exact_rational():
+    # the 40-digit decimal product that checks the n = 768 reference recipe on the GPU agrees
+    # with the exact rational fixture (rounded once to FP64) at n = 24
+    z = np.load(GOLDEN / "cauchy_exact.npz")
+    n = int(z["n"])
+    got = O.decimal_cauchy_product(z["A"], z["gen"], range(n), n)
+    assert O.rel_fro(got, z["X"]) < 1e-16
+    assert O.col_max_rel(got, z["X"]) < 1e-16
+    # and a sample of its columns is the same sample of the whole
+    np.testing.assert_array_equal(O.decimal_cauchy_product(z["A"][3:9], z["gen"], [2, 7, 19], n),
+                                  got[3:9][:, [2, 7, 19]])
+
+
 def test_dft_ones_golden_and_restatement():
     z = np.load(GOLDEN / "dft_ones_kat.npz")
     n = int(z["n"])
