@@ -226,7 +226,7 @@ def cauchy_batch_lowrank(problems, alpha, beta, *, compressor="rrqr", tol=1e-14,
         raise PsmmaError(st, "psmma_cauchy_batch_lowrank")
     info = {"effective_flops": stats.effective_flops, "executed_flops": stats.executed_flops,
             "compress_flops": stats.compress_flops, "n_blocks": stats.n_blocks, "max_rank": stats.max_rank,
-            "full_rank_blocks": stats.full_rank_blocks}
+            "full_rank_blocks": stats.full_rank_blocks, "graph_reused": bool(stats.graph_reused)}
     return list(ranks)[:nb], info
 
 
@@ -247,7 +247,7 @@ def toeplitz_batch_lowrank(problems, alpha, beta, *, tol=1e-14, precision="fp64"
         raise PsmmaError(st, "psmma_toeplitz_batch_lowrank")
     info = {"effective_flops": stats.effective_flops, "executed_flops": stats.executed_flops,
             "compress_flops": stats.compress_flops, "n_blocks": stats.n_blocks, "max_rank": stats.max_rank,
-            "full_rank_blocks": stats.full_rank_blocks}
+            "full_rank_blocks": stats.full_rank_blocks, "graph_reused": bool(stats.graph_reused)}
     return list(ranks)[:nb], info
 
 

@@ -1764,6 +1764,65 @@ int run_rrlu(Plan& P, std::vector<Block>& hb, Block* d_blocks, void (*krrlu)(Blo
   return PSMMA_OK;
 }
 
+// ------------------------------------------------------------------------------------------
+// The product rounds' CUDA graph, kept per (device, stream): each call captures its launches
+// (cheap, host only) and, when an executable graph exists for the stream, updates it in place
+// with cudaGraphExecUpdate (new pointers, ranks, alpha/beta); only a change of topology (other
+// launch count or kernels) instantiates a new one.  The capture stream and its event persist
+// with the entry.
+// ------------------------------------------------------------------------------------------
+struct GraphSlot {
+  std::mutex mu;  // one call at a time uses a slot
+  cudaStream_t cap = nullptr;
+  cudaEvent_t ev = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+std::mutex g_graph_mu;
+std::map<std::pair<int, cudaStream_t>, GraphSlot*> g_graphs;
+
+GraphSlot* graph_slot(cudaStream_t stream) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+  std::lock_guard<std::mutex> lk(g_graph_mu);
+  GraphSlot*& g = g_graphs[{dev, stream}];
+  if (!g) {
+    GraphSlot* n = new GraphSlot;
+    if (cudaStreamCreateWithFlags(&n->cap, cudaStreamNonBlocking) != cudaSuccess) {
+      delete n;
+      return nullptr;
+    }
+    if (cudaEventCreateWithFlags(&n->ev, cudaEventDisableTiming) != cudaSuccess) {
+      cudaStreamDestroy(n->cap);
+      delete n;
+      return nullptr;
+    }
+    g = n;
+  }
+  return g;
+}
+
+// Updates the slot's executable graph to `graph`, or instantiates it when the slot has none or
+// the update is refused (topology changed).  *reused = 1 when the existing executable was kept.
+int graph_exec_for(GraphSlot* gs, cudaGraph_t graph, int* reused) {
+  *reused = 0;
+  if (gs->exec) {
+    cudaGraphExecUpdateResultInfo info;
+    if (cudaGraphExecUpdate(gs->exec, graph, &info) == cudaSuccess) {
+      *reused = 1;
+      return PSMMA_OK;
+    }
+    cudaGetLastError();
+    cudaGraphExecDestroy(gs->exec);
+    gs->exec = nullptr;
+  }
+  if (cudaGraphInstantiate(&gs->exec, graph, 0) != cudaSuccess) {
+    gs->exec = nullptr;
+    return PSMMA_EDEVICE;
+  }
+  return PSMMA_OK;
+}
+
 }  // namespace
 
 static size_t batch_workspace(int kind, int count, const psmma_batch_item* items, int compressor,
@@ -1919,17 +1978,15 @@ static int batch_run(int kind, int count, const psmma_batch_item* items, double 
     }
     return rc;
   }
-  cudaStream_t cap = nullptr;
-  if (cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking) != cudaSuccess) return PSMMA_EDEVICE;
-  cudaEvent_t ev = nullptr;
-  if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) {
-    cudaStreamDestroy(cap);
-    return PSMMA_EDEVICE;
-  }
+  GraphSlot* gsl = graph_slot(st);
+  if (!gsl) return PSMMA_EDEVICE;
+  std::lock_guard<std::mutex> glk(gsl->mu);
+  cudaStream_t cap = gsl->cap;
+  cudaEvent_t ev = gsl->ev;
   cudaEventRecord(ev, st);
   cudaStreamWaitEvent(cap, ev, 0);  // the graph follows the compression and the copies above
   cudaGraph_t graph = nullptr;
-  cudaGraphExec_t gexec = nullptr;
+  int reused = 0;
   if (cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) != cudaSuccess) rc = PSMMA_EDEVICE;
   if (!rc && !gd.empty()) {
     k_gather_group<<<gather_cols, 256, 0, cap>>>(P.d_gather, (int)gd.size());
@@ -1938,18 +1995,15 @@ static int batch_run(int kind, int count, const psmma_batch_item* items, double 
   if (!rc) rc = enqueue_rounds(G, precision, P.d_status, cap);
   cudaError_t ce = cudaStreamEndCapture(cap, &graph);
   if (!rc && ce != cudaSuccess) rc = PSMMA_EDEVICE;
-  if (!rc && cudaGraphInstantiate(&gexec, graph, 0) != cudaSuccess) rc = PSMMA_EDEVICE;
-  if (!rc && cudaGraphLaunch(gexec, cap) != cudaSuccess) rc = PSMMA_EDEVICE;
+  if (!rc) rc = graph_exec_for(gsl, graph, &reused);
+  if (!rc && cudaGraphLaunch(gsl->exec, cap) != cudaSuccess) rc = PSMMA_EDEVICE;
   cudaEventRecord(ev, cap);
   cudaStreamWaitEvent(st, ev, 0);  // later work on `stream` follows the graph
   unsigned sts[Plan::N_STATUS] = {0};
   if (!rc && (cudaMemcpyAsync(sts, P.d_status, sizeof(sts), cudaMemcpyDeviceToHost, cap) != cudaSuccess ||
               cudaStreamSynchronize(cap) != cudaSuccess))
     rc = PSMMA_EDEVICE;
-  if (gexec) cudaGraphExecDestroy(gexec);
   if (graph) cudaGraphDestroy(graph);
-  cudaEventDestroy(ev);
-  cudaStreamDestroy(cap);
   for (unsigned v : sts)
     if (!rc && (v & DEV_ERR_TIMEOUT)) rc = PSMMA_ETIMEDOUT;
   if (stats) {
@@ -1961,6 +2015,7 @@ static int batch_run(int kind, int count, const psmma_batch_item* items, double 
     stats->n_blocks = nb;
     stats->max_rank = R.max_rank;
     stats->full_rank_blocks = R.full_blocks;
+    stats->graph_reused = reused;
   }
   return rc;
 }

@@ -116,6 +116,33 @@ def test_batch_split_matches_exact(comp):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("prec", ["split", "fp64"])
+def test_repeated_batches_reuse_the_stream_graph(prec):
+    # the product rounds' CUDA graph of a stream is updated in place on later calls (new
+    # operands and buffers, alpha, beta; the same generators, hence the same ranks and
+    # topology), and the results stay those of a fresh call
+    import torch
+    from psmma_git_gb300 import cauchy_batch_lowrank
+    sizes = [64, 300, 515, 1031]
+    base = _problems(sizes, seed=21)
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        first = _to_dev(base)
+        _, info0 = cauchy_batch_lowrank(first, 1.0, 0.0, compressor="rrlu", tol=1e-14, precision=prec, stream=s)
+        for seed, (alpha, beta) in [(22, (0.5, 0.0)), (23, (-1.25, 0.75))]:
+            other = _problems(sizes, seed=seed)
+            problems = [(A, g, Q0) for (_, g, _), (A, _, Q0) in zip(base, other)]
+            dev = _to_dev(problems)
+            _, info = cauchy_batch_lowrank(dev, alpha, beta, compressor="rrlu", tol=1e-14, precision=prec, stream=s)
+            s.synchronize()
+            assert info["graph_reused"], "the second and later calls of the same shape update the graph"
+            for (A, g, Q0), (_, _, Qd) in zip(problems, dev):
+                exact = alpha * A @ O.dense_h("cauchy", g, A.shape[0]) + beta * Q0
+                assert O.rel_fro(Qd.cpu().numpy(), exact) < (1e-12 if prec == "split" else 1e-13)
+    assert info0["graph_reused"] in (True, False)
+
+
+@pytest.mark.gpu
 def test_batch_ranks_match_reference_scan_on_larger_blocks():
     # off-diagonal blocks of 2048 x 2048: the RRQR rank is the first |R_kk| <= tol |R_11|
     problems = _problems([4096], seed=11)
