@@ -85,3 +85,37 @@ def test_workspace_size_queries(lib):
     w = workspace_size(_lib.KIND_CAUCHY, 1024, 1024)
     assert w == 0 or w % (1024 * 1024 * 8) == 0
     assert workspace_size(_lib.KIND_DFT, 1000, 10) >= 1000 * 16
+
+
+def test_fortran_module_binds_declared_and_exported_symbols(lib):
+    # include/psmma_gb300.f90 (not compiled here: no Fortran compiler on either host) must name
+    # only functions that psmma.h declares and the library exports, keep free-form lines within
+    # 132 characters, close every interface body it opens, and give its bind(c) types the C
+    # structs' fields in the same order
+    import re
+    from pathlib import Path
+    root = Path(__file__).resolve().parents[1]
+    f90 = (root / "include" / "psmma_gb300.f90").read_text()
+    header = (root / "include" / "psmma.h").read_text()
+    code = "\n".join(line.split("!")[0] for line in f90.splitlines())
+    assert all(len(line) <= 132 for line in f90.splitlines())
+    names = re.findall(r'bind\(c,\s*name="([a-z0-9_]+)"\)', code)
+    assert len(names) >= 29 and len(set(names)) == len(names)
+    declared = set(_lib.header_symbols())
+    for name in names:
+        assert name in declared, f"{name} is not declared in psmma.h"
+        assert hasattr(lib, name), f"{name} is not exported"
+    opened = re.findall(r"^\s*(?:integer\(c_\w+\)\s+|type\(c_ptr\)\s+)?(function|subroutine)\s+(\w+)\s*\(", code,
+                        flags=re.M)
+    closed = re.findall(r"^\s*end\s+(function|subroutine)\s+(\w+)", code, flags=re.M)
+    assert sorted(opened) == sorted(closed) and len(opened) == len(names)
+    assert code.count("module psmma_gb300") == 2 and "end module psmma_gb300" in code
+    for ctype in ["psmma_opts", "psmma_batch_item", "psmma_batch_stats", "psmma_tune_result", "psmma_grid"]:
+        fbody = re.search(r"type, bind\(c\), public :: " + ctype + r"\n(.*?)end type " + ctype, code, flags=re.S)
+        cbody = re.search(r"typedef struct " + ctype + r" \{(.*?)\} " + ctype + ";",
+                          re.sub(r"/\*.*?\*/", "", header, flags=re.S), flags=re.S)
+        assert fbody and cbody, ctype
+        ffields = re.findall(r"([a-z_][a-z0-9_]*)(?:\(\d+\))?\s*(?:=\s*[^,\n]+)?(?=,|\n)",
+                             "".join(ln.split("::")[1] + "\n" for ln in fbody.group(1).splitlines() if "::" in ln))
+        cfields = re.findall(r"\b([a-z_][a-z0-9_]*)\s*(?:\[\d+\])?\s*[,;]", cbody.group(1))
+        assert ffields == cfields, (ctype, ffields, cfields)
