@@ -64,6 +64,21 @@ def ncu_traffic(n: int, nmod: int):
     return b0 * (nmod / m0) * (n / n0) ** 3
 
 
+def profile_traffic(tag: str):
+    """DRAM bytes per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum) recorded as
+    ``traffic_bytes_per_launch_<tag>: <bytes>`` in a committed profile summary under
+    profiles/, or None."""
+    d = ROOT / "profiles"
+    if not d.is_dir():
+        return None
+    pat = re.compile(r"traffic_bytes_per_launch_" + re.escape(tag) + r":\s*([0-9.eE+]+)")
+    for f in sorted(d.glob("*.md")):
+        m = pat.search(f.read_text())
+        if m:
+            return float(m.group(1))
+    return None
+
+
 class Clocks:
     """nvidia-smi clock/throttle sampling during the timed region."""
     Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
@@ -233,13 +248,29 @@ def run_gpu(args, ws, rank, local):
     gen = torch.from_numpy(np.ascontiguousarray(gen_np.T)).to(dev).t()
     g = torch.Generator(device=dev)
     g.manual_seed(1 + rank)
-    A = P.fortran_empty(n, k, torch.float64, dev)
-    A.copy_(torch.randn(k, n, generator=g, device=dev, dtype=torch.float64).t())
-    Q = P.fortran_empty(n, k, torch.float64, dev)
+    if args.strong:
+        # one n x k problem split in row panels over the ranks (shard.sharded_multiply): each
+        # rank holds and multiplies rows [lo, hi) only; the headline's side measurements
+        # (FP64 path, e2e, CPU baseline, other workloads) are skipped
+        from psmma_git_gb300.shard import local_panel, sharded_multiply
+        lo, hi = local_panel(n, rank, ws)
+        args.no_fp64 = args.no_e2e = args.no_cpu = args.no_extra = True
+        g.manual_seed(1)
+        A_full_rows = torch.randn(k, hi - lo, generator=g, device=dev, dtype=torch.float64)
+        n_rank = hi - lo
+    else:
+        n_rank = n
+    A = P.fortran_empty(n_rank, k, torch.float64, dev)
+    A.copy_(A_full_rows.t() if args.strong else torch.randn(k, n, generator=g, device=dev, dtype=torch.float64).t())
+    Q = P.fortran_empty(n_rank, k, torch.float64, dev)
     Q.zero_()
 
     def step():
-        P.psmma_cauchy(n, k, 1.0, A, gen, 0.0, Q, precision="split", n_moduli=args.n_moduli, stream=stream)
+        if args.strong:
+            sharded_multiply("cauchy", n, k, 1.0, A, gen, 0.0, Q, rank=rank, world=ws, precision="split",
+                             n_moduli=args.n_moduli, stream=stream)
+        else:
+            P.psmma_cauchy(n, k, 1.0, A, gen, 0.0, Q, precision="split", n_moduli=args.n_moduli, stream=stream)
 
     for _ in range(args.warmup):
         step()
@@ -273,18 +304,21 @@ def run_gpu(args, ws, rank, local):
     total_ms = ev[0].elapsed_time(ev[args.steps])
     total_ms = max_over_ranks(total_ms, ws, dev)
     flops_rank = 2.0 * n * k * k
-    value = flops_rank * ws * args.steps / (total_ms * 1e-3) / 1e12
+    flops_job = flops_rank if args.strong else flops_rank * ws  # strong: one problem over all ranks
+    value = flops_job * args.steps / (total_ms * 1e-3) / 1e12
     phases = {kname: v / args.steps for kname, v in phase_tot.items()}
     launches_per_step = len(phases) + 1  # one kernel per phase + the stream-status accumulation
 
     result = {"metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": ws, "steps": args.steps,
               "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
-              "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic"}
+              "scaling": "strong" if args.strong else "weak", "vs_baseline": None, "dtype": "bf16",
+              "data": "synthetic"}
     result["config"] = {
         "workload": f"psmma_cauchy split-precision n={n} (10% of poles within 1e-10 of a neighbour, A ~ N(0,1) FP64)",
         "n": n, "k": k, "kind": "cauchy", "precision": "split (CRT residues on BF16 tcgen05, FP64 recombination)",
         "n_moduli": args.n_moduli, "l2": "inputs larger than L2 (A = 2 GiB), no flush",
-        "parallelism": f"{ws} replica(s), row panels, no collective"}
+        "parallelism": (f"one problem in {ws} row panel(s) of {n_rank}+ rows, no collective" if args.strong
+                        else f"{ws} replica(s), row panels, no collective")}
     result["latency_ms"] = {"p50": statistics.median(step_ms),
                             "p99": float(np.percentile(np.asarray(step_ms), 99))}
     result["phases_ms"] = phases
@@ -303,7 +337,10 @@ def run_gpu(args, ws, rank, local):
                               "kernel": "k_crt_gemm", "flops_per_launch": flops_gemm,
                               "peak_note": f"{pk['source']} cuBLAS bf16 sustained (kernel timed inside a "
                                            f"multi-second loop); burst {pk['bf16']}",
-                              "frac_of_burst": achieved / pk["bf16"]}
+                              "frac_of_burst": achieved / pk["bf16"],
+                              "traffic_note": "DRAM bytes per launch from the one-pass ncu capture at n=16384, "
+                                              "13 moduli (profiles/crt_gemm_ncu.md), scaled by moduli and n^3; "
+                                              "not measured in this run"}
 
     if rank == 0:
         # ---------------- FP64 plain path on the same inputs ----------------
@@ -409,15 +446,115 @@ def run_gpu(args, ws, rank, local):
             result.setdefault("rel_err", {})["split_vs_cpu_oracle_panel"] = O.rel_fro(got, Qcpu)
         if cl is not None:
             result["clocks"] = cl
+        if not args.no_extra:
+            result["extra"] = run_extras(args, ws, rank, local)
         print(json.dumps(result), flush=True)
     return 0
 
 
-def run_serving(args, ws, rank, local):
+def run_case(args, ws, rank, local):
+    """One workload repeated, for profiling a kernel on a small case (``--case PREC:KIND``,
+    PREC fp64 or split, KIND cauchy / toeplitz / hankel / dft / cauchyeig, size --n): warm-up
+    calls, then --steps calls timed with CUDA events.  Inputs as the cfg0 / cfg1 workloads.
+    One JSON line with the mean time per call."""
+    import numpy as np
+    import torch
+    import psmma_git_gb300 as P
+    from oracle import psmma_oracle as O
+    if rank != 0:
+        return 0
+    prec, kind = args.case.split(":")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    n = k = args.n
+    g = torch.Generator(device=dev)
+    g.manual_seed(9)
+    col = lambda x: torch.from_numpy(np.ascontiguousarray(np.asarray(x).T)).to(dev).t()  # noqa: E731
+    if kind == "dft":
+        X = P.fortran_empty(n, k, torch.complex128, dev)
+        X.copy_(torch.complex(torch.rand(k, n, generator=g, device=dev, dtype=torch.float64) * 2 - 1,
+                              torch.rand(k, n, generator=g, device=dev, dtype=torch.float64) * 2 - 1).t())
+        Y = P.fortran_empty(n, k, torch.complex128, dev)
+        run = lambda: P.pzmdftl(n, k, 1.0, X, 0.0, Y, precision=prec, n_moduli=args.n_moduli)  # noqa: E731
+        flops = 8.0 * n ** 3
+    else:
+        A = P.fortran_empty(n, k, torch.float64, dev)
+        A.copy_(torch.rand(k, n, generator=g, device=dev, dtype=torch.float64).mul_(2).sub_(1).t())
+        Y = P.fortran_empty(n, k, torch.float64, dev)
+        flops = 2.0 * n ** 3
+        if kind == "cauchy":
+            gen = col(O.cfg_cauchy_generators(k, seed=0))
+            run = lambda: P.psmma_cauchy(n, k, 1.0, A, gen, 0.0, Y, precision=prec, n_moduli=args.n_moduli)  # noqa: E731
+        elif kind == "cauchyeig":
+            eig = [torch.from_numpy(np.ascontiguousarray(x)).to(dev) for x in O.eig_generators(k, seed=7, tiny=k // 100)]
+            run = lambda: P.psmma_cauchyeig(n, k, 1.0, A, *eig, 0.0, Y, precision=prec,  # noqa: E731
+                                            n_moduli=args.n_moduli)
+        else:
+            gv = torch.rand(2 * k - 1, generator=g, device=dev, dtype=torch.float64).mul_(2).sub_(1)
+            fn = P.psmma_toeplitz if kind == "toeplitz" else P.psmma_hankel
+            run = lambda: fn(n, k, 1.0, A, gv, 0.0, Y, precision=prec, n_moduli=args.n_moduli)  # noqa: E731
+    for _ in range(args.warmup):
+        run()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        run()
+    e1.record()
+    torch.cuda.synchronize()
+    t = e0.elapsed_time(e1) / args.steps
+    print(json.dumps({"case": args.case, "n": n, "ms_per_call": t, "tflops": flops / t / 1e9,
+                      "steps": args.steps, "warmup": args.warmup}), flush=True)
+    return 0
+
+
+def run_extras(args, ws, rank, local) -> dict:
+    """The other workloads of the benchmark, each in compact form, for the same JSON line (after
+    the headline's timed region, which they do not touch):
+      cfg0  FP64 Cauchy n = 2048, seeds 0..4 (roofline vs in-run DGEMM, e2e, CPU ring baseline);
+      cfg1  Toeplitz / Hankel / DFT / CAUCHYEIG n = 8192 on both paths (rooflines, CPU panels);
+      cfg3  the batched merge level, 64 problems (RRQR, RRLU, Toeplitz RRQR; GEMM and QR rooflines);
+      cfg4  a serving sweep (p50 / p99 per rate against the stated bound, saturation).
+    Each runs with its own fixed step counts (a few minutes in all); a failure is recorded in
+    its entry and does not stop the others."""
+    import copy
+    import torch
+    import psmma_git_gb300 as P
+    out = {}
+    plan = [
+        ("cfg0", run_cfg0, dict(steps=10, warmup=3)),
+        ("cfg1", run_cfg1, dict(steps=5, warmup=3)),
+        ("cfg3", run_merge_level, dict(steps=5, warmup=3, no_tune=False)),
+        ("cfg4", run_serving, dict(rates=[20.0, 40.0, 60.0], serve_seconds=4.0)),
+    ]
+    for name, fn, over in plan:
+        a = copy.copy(args)
+        for kk, vv in over.items():
+            setattr(a, kk, vv)
+        t0 = time.perf_counter()
+        try:
+            line = fn(a, ws, rank, local, compact=True)
+            if line is not None:
+                line = {kk: vv for kk, vv in line.items() if kk not in ("n_gpus", "data")}
+        except Exception as e:  # noqa: BLE001 - recorded in the line, the headline still prints
+            line = {"error": f"{type(e).__name__}: {e}"}
+        line["wall_s"] = round(time.perf_counter() - t0, 1)
+        out[name] = line
+        print(json.dumps({"extra_done": name, "wall_s": line["wall_s"]}), file=sys.stderr, flush=True)
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+        P.load().psmma_release_workspace()  # the library's per-stream pools of this workload
+    return out
+
+
+def run_serving(args, ws, rank, local, compact=False):
     """Serving loop under a Poisson request stream (one line of JSON per sweep).  Requests:
     kind uniform over cauchy/toeplitz/hankel/dft, n log-uniform in [512, 16384] (k = n),
     operands uniform[-1,1] resident on the device (views into pre-generated pools), split
-    precision; the server admits by an HBM budget with at most --inflight requests."""
+    precision; the server admits by an HBM budget with at most --inflight requests.  Reported
+    per rate: p50/p99 latency, throughput, whether p99 holds the stated bound; over the sweep:
+    the largest rate that holds it and the saturation throughput (the largest measured).
+    Returns the JSON object."""
     import math
     import threading
     import numpy as np
@@ -426,7 +563,7 @@ def run_serving(args, ws, rank, local):
     from psmma_git_gb300.server import Server
     from oracle import psmma_oracle as O
     if rank != 0:
-        return 0
+        return None
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     nmax = args.serve_nmax
@@ -500,33 +637,47 @@ def run_serving(args, ws, rank, local):
                         "mean_gpu_ms": float(np.mean([i["gpu_ms"] for i, _ in done])),
                         "p99_within_bound": bool(np.percentile(lats, 99) < args.p99_bound_ms)})
         print(json.dumps({"serving_rate": results[-1]}), file=sys.stderr, flush=True)
+    held = [r["rate_req_s"] for r in results if r["p99_within_bound"] and r["all_ok"]]
     line = {"metric": "serving: p50/p99 latency (ms) and effective TFLOP/s under a Poisson stream",
             "unit": "ms", "n_gpus": 1, "data": "synthetic",
             "config": {"workload": "kind uniform over cauchy/toeplitz/hankel/dft, n log-uniform in "
                                    f"[512, {nmax}], split precision ({args.n_moduli} moduli), device-resident "
                                    "operands", "hbm_budget_gib": args.serve_budget_gib,
                        "max_inflight": args.inflight, "seconds_per_rate": args.serve_seconds},
-            "p99_bound_ms": args.p99_bound_ms, "sweep": results}
-    print(json.dumps(line), flush=True)
-    return 0
+            "p99_bound_ms": args.p99_bound_ms, "sweep": results,
+            "largest_rate_within_bound_req_s": max(held) if held else None,
+            "saturation_tflops": max(r["throughput_tflops"] for r in results),
+            "all_ok": all(r["all_ok"] for r in results)}
+    return line
 
 
-def run_cfg1(args, ws, rank, local):
-    """Toeplitz, Hankel, DFT and accurate-denominator Cauchy (PSMMA_CAUCHYEIG) multiplies at n = k = 8192 (A uniform[-1,1], generator vector of
-    length 2n-1 uniform[-1,1]; DFT: complex B with both parts uniform[-1,1]) on the split path
-    (args.n_moduli) and the FP64 path.  Rates: 2n^3/t for Toeplitz/Hankel, 8n^3/t real flops
-    for the DFT (2n^3/t complex multiply-adds beside it).  Errors: split vs FP64 path on the
-    whole product, and both against the FFT-based oracle on a 256-row (DFT: 256-column)
-    sample.  One JSON line."""
+def run_cfg1(args, ws, rank, local, compact=False):
+    """Toeplitz, Hankel, DFT and accurate-denominator Cauchy (PSMMA_CAUCHYEIG) multiplies at
+    n = k = 8192 (A uniform[-1,1], generator vector of length 2n-1 uniform[-1,1]; DFT: complex
+    B with both parts uniform[-1,1]; CAUCHYEIG: eigensolver generators with 1% of the roots next
+    to their pole) on the split path (args.n_moduli) and the FP64 path.  Rates: 2n^3/t for
+    Toeplitz/Hankel/CAUCHYEIG, 8n^3/t real flops for the DFT (2n^3/t complex multiply-adds
+    beside it).  Errors: split vs FP64 path on the whole product, and both against the
+    oracle on a 256-row (DFT: 256-column) sample -- FFT correlation for Toeplitz/Hankel, FFT for
+    the DFT, the explicit CauchylikeEig matrix (FP64 BLAS) for CAUCHYEIG, whose per-column
+    maximum relative error is reported too (the eigensolver normalises columns).  Per kind a
+    roofline of the modular GEMMs (BF16, sustained peak) and of the FP64 path (in-run DGEMM),
+    and a CPU baseline: the oracle's restatement (ConstToeplitz / ConstHankel / CauchylikeEig
+    of an H column panel + DGEMM; the DFT: a row panel of F times B by ZGEMM) on all host
+    cores.  Returns the JSON object."""
     import numpy as np
     import torch
     import psmma_git_gb300 as P
     from oracle import psmma_oracle as O
     if rank != 0:
-        return 0
+        return None
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     n = k = args.cfg1_n
+    nmod = args.n_moduli
+    pk = peaks()
+    stream = torch.cuda.current_stream()
+    dgemm = fp64_dgemm_rate(dev, stream)
     g = torch.Generator(device=dev)
     g.manual_seed(5)
     A = P.fortran_empty(n, k, torch.float64, dev)
@@ -535,27 +686,33 @@ def run_cfg1(args, ws, rank, local):
     out = {}
     eig = O.eig_generators(k, seed=7, tiny=k // 100)  # F, U, V, DIFL, DIFR (1% of roots next to a pole)
     eig_dev = [torch.from_numpy(np.ascontiguousarray(x)).to(dev) for x in eig]
+    A_host = None
+    cpu_cols = 512 if not compact else 256
+    kp = (k + 63) // 64 * 64
     for kind in ["toeplitz", "hankel", "dft", "cauchyeig"]:
         if kind == "cauchyeig":
             Y = P.fortran_empty(n, k, torch.float64, dev)
             Y64 = P.fortran_empty(n, k, torch.float64, dev)
-            run = lambda prec, dst: P.psmma_cauchyeig(n, k, 1.0, A, *eig_dev, 0.0, dst, precision=prec,
-                                                      n_moduli=args.n_moduli)
+            run = lambda prec, dst: P.psmma_cauchyeig(n, k, 1.0, A, *eig_dev, 0.0, dst, precision=prec,  # noqa: E731
+                                                      n_moduli=nmod)
             flops = 2.0 * n ** 3
+            gemm_flops = 2.0 * nmod * n * k * kp
         elif kind == "dft":
             X = P.fortran_empty(n, k, torch.complex128, dev)
             X.copy_(torch.complex(torch.rand(k, n, generator=g, device=dev, dtype=torch.float64) * 2 - 1,
                                   torch.rand(k, n, generator=g, device=dev, dtype=torch.float64) * 2 - 1).t())
             Y = P.fortran_empty(n, k, torch.complex128, dev)
             Y64 = P.fortran_empty(n, k, torch.complex128, dev)
-            run = lambda prec, dst: P.pzmdftl(n, k, 1.0, X, 0.0, dst, precision=prec, n_moduli=args.n_moduli)
+            run = lambda prec, dst: P.pzmdftl(n, k, 1.0, X, 0.0, dst, precision=prec, n_moduli=nmod)  # noqa: E731
             flops = 8.0 * n ** 3
+            gemm_flops = 3 * 2.0 * nmod * k * n * kp  # 3M: three real products per modulus
         else:
             Y = P.fortran_empty(n, k, torch.float64, dev)
             Y64 = P.fortran_empty(n, k, torch.float64, dev)
             fn = P.psmma_toeplitz if kind == "toeplitz" else P.psmma_hankel
-            run = lambda prec, dst, fn=fn: fn(n, k, 1.0, A, gv, 0.0, dst, precision=prec, n_moduli=args.n_moduli)
+            run = lambda prec, dst, fn=fn: fn(n, k, 1.0, A, gv, 0.0, dst, precision=prec, n_moduli=nmod)  # noqa: E731
             flops = 2.0 * n ** 3
+            gemm_flops = 2.0 * nmod * n * k * kp
         for _ in range(args.warmup):
             run("split", Y)
         torch.cuda.synchronize()
@@ -575,6 +732,9 @@ def run_cfg1(args, ws, rank, local):
         m = lib.psmma_profile_read(ms, names, 40)
         lib.psmma_set_profiling(0)
         phases = [[names[j].decode(), round(ms[j], 3)] for j in range(max(0, m))]
+        gemm_ms = sum(v for nm, v in phases if "gemm" in nm)
+        run("fp64", Y64)  # warm-up (FP64 path: one call)
+        torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
         run("fp64", Y64)
@@ -582,29 +742,79 @@ def run_cfg1(args, ws, rank, local):
         torch.cuda.synchronize()
         t64 = e0.elapsed_time(e1)
         rel = float(torch.linalg.norm(Y - Y64) / torch.linalg.norm(Y64))
+        col_err = None
         if kind == "cauchyeig":
             As = np.ascontiguousarray(A[:256].cpu().numpy())
             ref = As @ O.cauchy_like_eig(*eig)
             err_split = O.rel_fro(Y[:256].cpu().numpy(), ref)
             err_64 = O.rel_fro(Y64[:256].cpu().numpy(), ref)
+            col_err = {"split": O.col_max_rel(Y[:256].cpu().numpy(), ref),
+                       "fp64": O.col_max_rel(Y64[:256].cpu().numpy(), ref)}
+            oracle = "A[0:256] @ CauchylikeEig matrix (FP64 BLAS)"
         elif kind == "dft":
             Xs = X[:, :256].cpu().numpy()
             ref = O.dft_product(1.0, Xs, 0.0, None)
             err_split = O.rel_fro(Y[:, :256].cpu().numpy(), ref)
             err_64 = O.rel_fro(Y64[:, :256].cpu().numpy(), ref)
+            oracle = "np.fft.fft of B[:, 0:256]"
         else:
             As = np.ascontiguousarray(A[:256].cpu().numpy())
             prod = O.toeplitz_product_fft if kind == "toeplitz" else O.hankel_product_fft
             ref = prod(As, gv.cpu().numpy(), k)
             err_split = O.rel_fro(Y[:256].cpu().numpy(), ref)
             err_64 = O.rel_fro(Y64[:256].cpu().numpy(), ref)
+            oracle = "FFT correlation of A[0:256] with G"
+        # CPU baseline: a bounded panel of the oracle's restatement on the host cores
+        if A_host is None and not args.no_cpu:
+            A_host = np.asfortranarray(A.cpu().numpy())
+        cpu = None
+        if not args.no_cpu:
+            if kind == "dft":
+                rows = 128 if compact else 256
+                Bh = np.asfortranarray(X.cpu().numpy())
+                t0 = time.perf_counter()
+                jj = np.arange(rows, dtype=np.int64)[:, None] * np.arange(n, dtype=np.int64)[None, :] % n
+                Fp = np.exp(-2j * np.pi * jj / n)
+                Cp = Fp @ Bh
+                tc = time.perf_counter() - t0
+                del Bh, Fp, Cp
+                cpu = {"value": 8.0 * rows * n * k / tc / 1e12, "unit": "TFLOP/s", "cores": os.cpu_count(),
+                       "kind": "port", "sample": f"C[0:{rows}, :] = F[0:{rows}, :] @ B (F row panel generated "
+                                                 f"+ ZGEMM), {tc:.2f} s"}
+            else:
+                cols = np.arange(1, cpu_cols + 1)
+                t0 = time.perf_counter()
+                if kind == "cauchyeig":
+                    Hp = O.cauchy_like_eig(*eig, cindex=cols)
+                else:
+                    const = O.const_toeplitz if kind == "toeplitz" else O.const_hankel
+                    Hp = const(gv.cpu().numpy(), k, np.arange(1, k + 1), cols)
+                Qp = A_host @ Hp
+                tc = time.perf_counter() - t0
+                del Hp, Qp
+                cpu = {"value": 2.0 * n * k * cpu_cols / tc / 1e12, "unit": "TFLOP/s", "cores": os.cpu_count(),
+                       "kind": "port", "sample": f"Q[:, 0:{cpu_cols}]: the H column panel by the oracle's "
+                                                 f"restatement + DGEMM, {tc:.2f} s"}
         out[kind] = {"split_ms": t, "split_tflops": flops / t / 1e9, "fp64_ms": t64,
                      "fp64_tflops": flops / t64 / 1e9, "speedup": t64 / t,
-                     "rel_err_split_vs_fp64": rel, "rel_err_split_vs_fft_oracle_sample": err_split,
-                     "rel_err_fp64_vs_fft_oracle_sample": err_64, "split_phases_ms": phases}
+                     "rel_err_split_vs_fp64": rel, "rel_err_split_vs_oracle_sample": err_split,
+                     "rel_err_fp64_vs_oracle_sample": err_64, "oracle": oracle,
+                     "roofline": {"bound": "tensor", "achieved": gemm_flops / (gemm_ms * 1e-3) / 1e12 if gemm_ms
+                                  else None, "peak": pk["bf16_sustained"], "unit": "TFLOP/s",
+                                  "frac": gemm_flops / (gemm_ms * 1e-3) / 1e12 / pk["bf16_sustained"]
+                                  if gemm_ms else None, "traffic": None, "kernel": "k_crt_gemm (modular BF16 GEMMs)",
+                                  "flops_per_call": gemm_flops,
+                                  "peak_note": f"{pk['source']} cuBLAS bf16 sustained"},
+                     "fp64_roofline": {"bound": "tensor", "achieved": flops / t64 / 1e9, "peak": dgemm,
+                                       "unit": "TFLOP/s", "frac": flops / t64 / 1e9 / dgemm,
+                                       "kernel": "k_struct_f64", "peak_source": "cuBLAS DGEMM in this run"},
+                     "cpu_baseline": cpu, "split_phases_ms": phases}
+        if col_err is not None:
+            out[kind]["col_max_rel_err_vs_oracle_sample"] = col_err
         if kind == "dft":
             out[kind]["split_complex_mac_tflops"] = 2.0 * n ** 3 / t / 1e9
-        print(json.dumps({kind: out[kind]}), file=sys.stderr, flush=True)
+        print(json.dumps({kind: {kk: vv for kk, vv in out[kind].items() if kk != "split_phases_ms"}}),
+              file=sys.stderr, flush=True)
         del Y, Y64
         torch.cuda.empty_cache()
     line = {"metric": f"Toeplitz/Hankel/DFT/CauchyEig A·C TFLOP/s n={n}, split vs FP64",
@@ -612,37 +822,58 @@ def run_cfg1(args, ws, rank, local):
             "unit": "TFLOP/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": out["toeplitz"]["split_ms"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64 (split: bf16 modular slices)", "data": "synthetic",
-            "config": {"workload": f"toeplitz/hankel/dft/cauchyeig n=k={n}", "n_moduli": args.n_moduli,
+            "config": {"workload": f"toeplitz/hankel/dft/cauchyeig n=k={n}", "n_moduli": nmod,
                        "l2": "inputs 0.5-1 GiB > L2, no flush"},
-            "kinds": out}
-    print(json.dumps(line), flush=True)
-    return 0
+            "cublas_dgemm_tflops": dgemm, "kinds": out}
+    return line
 
 
-def run_cfg0(args, ws, rank, local):
+def fp64_dgemm_rate(dev, stream):
+    """cuBLAS DGEMM 8192^3 TFLOP/s on this GPU (best of 3 after one warm-up): the FP64
+    tensor-core roofline denominator (MEASURED_PEAKS.json carries no FP64 figure)."""
+    import torch
+    a = torch.randn(8192, 8192, device=dev, dtype=torch.float64)
+    torch.matmul(a, a)
+    torch.cuda.synchronize()
+    best = float("inf")
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        torch.matmul(a, a)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    del a
+    return 2 * 8192 ** 3 / (best * 1e-3) / 1e12
+
+
+def run_cfg0(args, ws, rank, local, compact=False):
     """Cauchy multiply on the FP64 plain path at n = k = 2048 over seeds 0..4 (A ~ U[-1,1],
-    d = sort(U(0,1)), w_j ~ U(d_j, d_j+1), u, v ~ N(0,1)): median of args.steps timed calls per
-    seed (CUDA events, after args.warmup), error against the oracle's FP64 A@H, the split path
-    beside it, and the FP64 roofline against cuBLAS DGEMM measured in the same run.  CPU
-    baseline: the restatement of PSCAUCHY_COMPUTE on a 2 x 2 grid, block 64 (4 emulated ranks),
-    and a dense A@H, on all host cores.  One JSON line."""
+    d = sort(U(0,1)), w_j ~ U(d_j, d_j+1), u, v ~ N(0,1)): median of the timed calls per seed
+    (CUDA events, after args.warmup), error against the oracle's FP64 A@H, the split path
+    beside it, and the FP64 roofline against cuBLAS DGEMM measured in the same run.  e2e: the
+    same multiply through the host-pointer entry point (pinned host arrays, copies inside the
+    timed region).  CPU baseline: the restatement of PSCAUCHY_COMPUTE on a 2 x 2 grid, block 64
+    (4 emulated ranks), and a dense A@H, on all host cores.  Returns the JSON object."""
     import numpy as np
     import torch
     import psmma_git_gb300 as P
     from oracle import psmma_oracle as O
     if rank != 0:
-        return 0
+        return None
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     n = 2048
     flops = 2.0 * n ** 3
     stream = torch.cuda.current_stream()
+    steps = max(10, args.steps)
     col = lambda x: torch.from_numpy(np.ascontiguousarray(np.asarray(x).T)).to(dev).t()  # noqa: E731
     per_seed = []
     for seed in range(5):
         A = O.cfg_matrix(n, n, seed=seed)
         gen = O.cfg_cauchy_generators(n, seed=seed)
         dA, dg = col(A), col(gen)
+        ref = O.dense_product("cauchy", 1.0, A, gen, 0.0, None, n)
         out = {}
         for prec in ["fp64", "split"]:
             dQ = P.fortran_empty(n, n, torch.float64, dev)
@@ -650,55 +881,69 @@ def run_cfg0(args, ws, rank, local):
                 P.psmma_cauchy(n, n, 1.0, dA, dg, 0.0, dQ, precision=prec, n_moduli=args.n_moduli, stream=stream)
             torch.cuda.synchronize()
             ts = []
-            for _ in range(max(10, args.steps)):
+            for _ in range(steps):
                 e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
                 e0.record(stream)
                 P.psmma_cauchy(n, n, 1.0, dA, dg, 0.0, dQ, precision=prec, n_moduli=args.n_moduli, stream=stream)
                 e1.record(stream)
                 torch.cuda.synchronize()
                 ts.append(e0.elapsed_time(e1))
-            ref = O.dense_product("cauchy", 1.0, A, gen, 0.0, None, n)
             out[prec] = {"ms": float(np.median(ts)), "tflops": flops / (np.median(ts) * 1e-3) / 1e12,
                          "rel_err_vs_oracle": O.rel_fro(dQ.t().contiguous().cpu().numpy().T, ref)}
         per_seed.append(out)
-    a = torch.randn(8192, 8192, device=dev, dtype=torch.float64)
-    torch.matmul(a, a)
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    torch.matmul(a, a)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    dgemm = 2 * 8192 ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12
-    del a
-    # CPU baseline: the reference's ring on a 2 x 2 grid and a dense A@H (seed 0)
+    dgemm = fp64_dgemm_rate(dev, stream)
+    # e2e (seed 0): psmma_cauchy_host on pinned host arrays, FP64 path
     A = O.cfg_matrix(n, n, seed=0)
     gen = O.cfg_cauchy_generators(n, seed=0)
+    hA = torch.empty((n, n), dtype=torch.float64, pin_memory=True)
+    hA.numpy()[:] = A.T
+    hG = torch.empty((4, n), dtype=torch.float64, pin_memory=True)
+    hG.numpy()[:] = gen.T
+    hQ = torch.zeros((n, n), dtype=torch.float64, pin_memory=True)
+    nA, nG, nQ = hA.numpy().T, hG.numpy().T, hQ.numpy().T
+    for _ in range(args.warmup):
+        P.psmma_cauchy(n, n, 1.0, nA, nG, 0.0, nQ)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        P.psmma_cauchy(n, n, 1.0, nA, nG, 0.0, nQ)
+    te = (time.perf_counter() - t0) / steps
+    e2e_err = O.rel_fro(np.asarray(nQ), O.dense_product("cauchy", 1.0, A, gen, 0.0, None, n))
+    # CPU baseline: the reference's ring on a 2 x 2 grid and a dense A@H (seed 0)
     t0 = time.perf_counter()
     Qr = O.ps_compute("cauchy", n, n, 1.0, A, gen, 0.0, np.zeros((n, n)), nprow=2, npcol=2, nb=64)
     t_ring = time.perf_counter() - t0
     t0 = time.perf_counter()
-    O.dense_product("cauchy", 1.0, A, gen, 0.0, None, n)
+    dense = O.dense_product("cauchy", 1.0, A, gen, 0.0, None, n)
     t_dense = time.perf_counter() - t0
     fp64 = [s_["fp64"]["tflops"] for s_ in per_seed]
     v = float(np.median(fp64))
+    traffic = profile_traffic("fp64_cauchy_n2048")
     line = {"metric": "Cauchy A·H TFLOP/s n=2048, FP64 plain path (cfg0)", "value": v, "unit": "TFLOP/s",
-            "n_gpus": 1, "steps": max(10, args.steps), "warmup": args.warmup,
+            "n_gpus": 1, "steps": steps, "warmup": args.warmup,
             "ms_per_step": float(np.median([s_["fp64"]["ms"] for s_ in per_seed])), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": {"workload": "psmma_cauchy FP64 n=k=2048, seeds 0..4 (median over seeds of the median "
                                    "over steps)", "n": n, "l2": "inputs 32 MiB < L2: no flush (small case)"},
             "seeds": per_seed,
+            "split_tflops_median": float(np.median([s_["split"]["tflops"] for s_ in per_seed])),
+            "max_rel_err_vs_oracle": {p: max(s_[p]["rel_err_vs_oracle"] for s_ in per_seed)
+                                      for p in ("fp64", "split")},
             "roofline": {"bound": "tensor", "achieved": v, "peak": dgemm, "unit": "TFLOP/s", "frac": v / dgemm,
-                         "traffic": None, "kernel": "k_struct_f64<KIND_CAUCHY>",
-                         "peak_source": "cuBLAS DGEMM 8192^3 measured in this run"},
+                         "traffic": traffic, "kernel": "k_struct_f64<KIND_CAUCHY>",
+                         "algorithmic_bytes": 16.0 * n * n + 32.0 * n,
+                         "peak_source": "cuBLAS DGEMM 8192^3 measured in this run (FP64 tensor-core proxy; "
+                                        "MEASURED_PEAKS.json has no FP64 figure)",
+                         "traffic_source": "ncu dram__bytes_read+write of one launch (profiles/fp64_dmma_ncu.md)"
+                         if traffic else None},
+            "e2e": {"value": flops / te / 1e12, "unit": "TFLOP/s", "h2d_bytes_per_step": 8 * n * n + 32 * n,
+                    "d2h_bytes_per_step": 8 * n * n, "ms_per_step": te * 1e3, "steps": steps,
+                    "api": "psmma_cauchy_host (pinned host buffers), FP64 path", "rel_err_vs_oracle": e2e_err},
             "cpu_baseline": {"value": flops / t_ring / 1e12, "unit": "TFLOP/s", "cores": os.cpu_count(),
                              "kind": "port", "sample": f"whole product, ring restatement 2x2 grid nb=64: "
                                                        f"{t_ring:.2f} s; dense A@H: {t_dense:.2f} s"},
-            "ring_vs_dense_rel": O.rel_fro(Qr, O.dense_product("cauchy", 1.0, A, gen, 0.0, None, n)),
-            "gpu_launches": 2 * 5 * (max(10, args.steps) + args.warmup)}
-    print(json.dumps(line), flush=True)
-    return 0
+            "ring_vs_dense_rel": O.rel_fro(Qr, dense),
+            "gpu_launches": 2 * 5 * (steps + args.warmup)}
+    return line
 
 
 def run_redist(args, ws, rank, local):
@@ -791,22 +1036,28 @@ def run_redist(args, ws, rank, local):
     return 0 if bad == 0 else 1
 
 
-def run_merge_level(args, ws, rank, local):
+def run_merge_level(args, ws, rank, local, compact=False):
     """Batched divide-and-conquer merge level: 64 independent Cauchy multiplies Q_i = A_i H_i,
     n_i log-uniform in [256, 8192] (seeded), generators as the n = 2048 workload (d sorted
     uniform, w interlacing, u, v normal), A_i uniform[-1,1] resident in HBM.  The
     off-diagonal blocks of each H_i are compressed at tol 1e-14 by RRQR (the reference's
     Compress_RRQR) and by the structured RRLU; the products run as grouped launches in one
     CUDA graph.  value = dense-equivalent sum(2 n^3) / time (effective), executed flops
-    reported beside it.  One JSON line."""
+    reported beside it.  Rooflines: the grouped modular GEMMs (BF16 flops = executed product
+    flops x moduli, against the sustained BF16 peak) and the QR compression (its
+    factorisation flops against the in-run DGEMM rate, the FP64 tensor-core proxy; the QR runs
+    on the FP64 FMA pipe).  compact: the Cauchy RRQR / RRLU and Toeplitz RRQR runs only, a
+    shorter CPU sample.  Returns the JSON object."""
     import numpy as np
     import torch
     import psmma_git_gb300 as P
     from oracle import psmma_oracle as O
     if rank != 0:
-        return 0
+        return None
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
+    pk = peaks()
+    dgemm = fp64_dgemm_rate(dev, torch.cuda.current_stream())
     sizes = O.cfg_batch_sizes(args.batch_count, 256, 8192, seed=7)
     g = torch.Generator(device=dev)
     g.manual_seed(3)
@@ -851,7 +1102,8 @@ def run_merge_level(args, ws, rank, local):
         P.psmma_toeplitz(n, n, 1.0, toep_probs[i][0], toep_probs[i][1], 0.0, R)
         toep_refs[i] = R
     runs = ([(c, p, "cauchy") for c in ["rrqr", "rrlu"] for p in precisions] +
-            [(c, "split", "cauchyeig") for c in ["rrqr", "rrlu"]] + [("rrqr", "split", "toeplitz")])
+            ([] if compact else [(c, "split", "cauchyeig") for c in ["rrqr", "rrlu"]]) +
+            [("rrqr", "split", "toeplitz")])
 
     def call(batch, kw, kind):
         if kind == "toeplitz":
@@ -900,17 +1152,40 @@ def run_merge_level(args, ws, rank, local):
         phases = [[names[j].decode(), round(ms[j], 3)] for j in range(max(0, m))]
         t = statistics.median(times)
         key = f"{comp}_{prec}" + ("_eig" if eig else "_toeplitz" if kind == "toeplitz" else "")
+        gemm_ms = sum(v for nm, v in phases if nm.startswith("g_gemm"))
+        comp_ms = sum(v for nm, v in phases if nm.startswith("compress"))
+        roof = {}
+        if prec == "split" and gemm_ms > 0:
+            bf = info["executed_flops"] * args.n_moduli
+            roof["grouped_gemm"] = {"bound": "tensor", "achieved": bf / (gemm_ms * 1e-3) / 1e12,
+                                    "peak": pk["bf16_sustained"], "unit": "TFLOP/s",
+                                    "frac": bf / (gemm_ms * 1e-3) / 1e12 / pk["bf16_sustained"],
+                                    "traffic": None, "kernel": "k_crt_gemm<*, GroupGemm>",
+                                    "flops": bf, "ms": gemm_ms,
+                                    "note": "BF16 flops = executed product flops x moduli (K padding not "
+                                            f"counted); {pk['source']} cuBLAS bf16 sustained"}
+        if comp == "rrqr" and comp_ms > 0:
+            roof["qr_compression"] = {"bound": "tensor", "achieved": info["compress_flops"] / (comp_ms * 1e-3) / 1e12,
+                                      "peak": dgemm, "unit": "TFLOP/s",
+                                      "frac": info["compress_flops"] / (comp_ms * 1e-3) / 1e12 / dgemm,
+                                      "traffic": None, "kernel": "k_qr_tiles + k_rrqr_grouped",
+                                      "flops": info["compress_flops"], "ms": comp_ms,
+                                      "note": "factorisation flops (4 m n (r+1) + 4 m r^2 per block) against "
+                                              "the in-run cuBLAS DGEMM rate"}
         out[key] = {
             "ms_per_step": t, "steps": steps, "effective_tflops": eff / t / 1e9,
             "executed_tflops": info["executed_flops"] / t / 1e9,
             "executed_flops": info["executed_flops"], "compress_flops": info["compress_flops"],
             "ranks": {"max": int(max(ranks)), "mean": float(np.mean(ranks)), "min": int(min(ranks))},
             "full_rank_blocks": info["full_rank_blocks"], "rel_err_vs_dense_fp64": err,
-            "autotune": tuned, "phases_ms": phases}
-        print(json.dumps({key: out[key]}), file=sys.stderr, flush=True)
+            "graph_reused": info.get("graph_reused"),
+            "autotune": tuned, "roofline": roof or None, "phases_ms": phases}
+        print(json.dumps({key: {kk: vv for kk, vv in out[key].items() if kk != "phases_ms"}}), file=sys.stderr,
+              flush=True)
     # CPU baseline: the oracle's restatement of the merge level (Compress_RRQR + DGEMMs) on the
     # smallest problems until ~args.cpu_seconds of work
     cpu = None
+    cpu_seconds = min(args.cpu_seconds, 6.0) if compact else args.cpu_seconds
     if not args.no_cpu:
         order = sorted(range(len(sizes)), key=lambda i: sizes[i])
         done_fl, t_cpu, used = 0.0, 0.0, []
@@ -923,7 +1198,7 @@ def run_merge_level(args, ws, rank, local):
             t_cpu += time.perf_counter() - t0
             done_fl += 2.0 * n ** 3
             used.append(n)
-            if t_cpu > args.cpu_seconds:
+            if t_cpu > cpu_seconds:
                 break
         cpu = {"value": done_fl / t_cpu / 1e12, "unit": "TFLOP/s", "cores": os.cpu_count(), "kind": "port",
                "sample": f"{len(used)} smallest problems (n = {min(used)}..{max(used)}) of the batch, "
@@ -938,9 +1213,9 @@ def run_merge_level(args, ws, rank, local):
             "config": {"workload": "batched merge level", "count": len(sizes), "sum_n": sum(sizes),
                        "n_max": max(sizes), "n_moduli": args.n_moduli, "tol": 1e-14,
                        "l2": "inputs ~ 10 GB > L2, no flush needed"},
-            "compressors": out, "cpu_baseline": cpu}
-    print(json.dumps(line), flush=True)
-    return 0
+            "roofline": head["roofline"]["grouped_gemm"] if head.get("roofline") else None,
+            "cublas_dgemm_tflops": dgemm, "compressors": out, "cpu_baseline": cpu}
+    return line
 
 
 import ctypes  # noqa: E402
@@ -982,6 +1257,11 @@ def main():
     ap.add_argument("--redist", action="store_true", help="time the block-cyclic redistribution kernels")
     ap.add_argument("--cfg0", action="store_true", help="run the FP64 Cauchy multiply at n = 2048 over 5 seeds")
     ap.add_argument("--redist-n", type=int, default=16384)
+    ap.add_argument("--strong", action="store_true",
+                    help="with --gpus N: one n x n problem split in N row panels (strong scaling)")
+    ap.add_argument("--case", default="", help="profiling case PREC:KIND (e.g. fp64:cauchy) at size --n")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="default line: skip the compact cfg0 / cfg1 / merge-level / serving entries")
     args = ap.parse_args()
     ws, rank, local = dist_init(args)
     if args.impl == "reference":
@@ -990,16 +1270,17 @@ def main():
     if rank == 0:
         B.build()
     barrier(ws)
-    if args.serving:
-        return run_serving(args, ws, rank, local)
-    if args.merge_level:
-        return run_merge_level(args, ws, rank, local)
-    if args.cfg1:
-        return run_cfg1(args, ws, rank, local)
+    for flag, fn in (("serving", run_serving), ("merge_level", run_merge_level), ("cfg1", run_cfg1),
+                     ("cfg0", run_cfg0)):
+        if getattr(args, flag):
+            line = fn(args, ws, rank, local)
+            if line is not None:
+                print(json.dumps(line), flush=True)
+            return 0
     if args.redist:
         return run_redist(args, ws, rank, local)
-    if args.cfg0:
-        return run_cfg0(args, ws, rank, local)
+    if args.case:
+        return run_case(args, ws, rank, local)
     return run_gpu(args, ws, rank, local)
 
 

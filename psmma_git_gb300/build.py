@@ -45,18 +45,20 @@ def _newest_dep() -> float:
     return max(p.stat().st_mtime for p in deps)
 
 
-def _compile(src: str) -> Path:
+def _compile(src: str) -> tuple[Path, bool]:
+    """(object file, whether nvcc ran): an object newer than its source and the shared
+    headers is reused."""
     s = CSRC / src
     o = BUILD / (Path(src).stem + ".o")
     if o.exists() and o.stat().st_mtime >= max(s.stat().st_mtime, _newest_dep()):
-        return o
+        return o, False
     cmd = [nvcc(), "-c", str(s), "-o", str(o)] + _flags()
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")
     if r.stderr.strip() and os.environ.get("PSMMA_PTXAS_VERBOSE"):
         sys.stderr.write(r.stderr)
-    return o
+    return o, True
 
 
 def build(force: bool = False, verbose: bool = False) -> Path:
@@ -66,7 +68,10 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         for p in BUILD.glob("*.o"):
             p.unlink()
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
-        objs = list(ex.map(_compile, SOURCES))
+        res = list(ex.map(_compile, SOURCES))
+    objs = [o for o, _ in res]
+    compiled = [src for src, (_, ran) in zip(SOURCES, res) if ran]
+    linked = False
     if force or not LIB.exists() or LIB.stat().st_mtime < max(o.stat().st_mtime for o in objs):
         tmp = LIB.with_suffix(".so.tmp")
         cmd = [nvcc(), "-shared", "-o", str(tmp)] + [str(o) for o in objs] + ARCH + ["-lcuda"]
@@ -74,8 +79,11 @@ def build(force: bool = False, verbose: bool = False) -> Path:
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
         os.replace(tmp, LIB)
+        linked = True
     if verbose:
-        print(f"built {LIB}")
+        what = (f"compiled {len(compiled)} of {len(SOURCES)} sources ({', '.join(compiled)})" if compiled
+                else "all objects up to date")
+        print(f"{LIB}: {what}; {'linked' if linked else 'library up to date'}")
     return LIB
 
 
