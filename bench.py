@@ -391,7 +391,7 @@ def run_gpu(args, ws, rank, local):
             for _ in range(max(2, args.warmup)):
                 P.psmma_cauchy(n, k, 1.0, nA, nG, 0.0, nQ, precision="split", n_moduli=args.n_moduli)
             e2e_steps = max(1, min(args.steps, 10))
-            call_ms, dev_ms, redo, first_phases, slow = [], [], 0, None, (0.0, None)
+            call_ms, dev_ms, redo, first_phases, slow, timelines = [], [], 0, None, (0.0, None, None), []
             # each call is traced (one event per library phase, no synchronisation added): the
             # device-side span of the call and whether its speculative bit counts were redone
             lib.psmma_set_profiling(1)
@@ -400,15 +400,18 @@ def run_gpu(args, ws, rank, local):
                 t1 = time.perf_counter()
                 P.psmma_cauchy(n, k, 1.0, nA, nG, 0.0, nQ, precision="split", n_moduli=args.n_moduli)
                 call_ms.append(round((time.perf_counter() - t1) * 1e3, 2))
-                ms = (C_float * 40)()
-                names = (C_charp * 40)()
-                m = lib.psmma_profile_read(ms, names, 40)
+                ms = (C_float * 80)()
+                names = (C_charp * 80)()
+                m = lib.psmma_profile_read(ms, names, 80)
                 dev_ms.append(round(sum(ms[j] for j in range(max(0, m))), 2))
                 ph = [[names[j].decode(), round(ms[j], 3)] for j in range(max(0, m))]
+                mt = lib.psmma_profile_read_timeline(ms, names, 80)
+                tl = [[names[j].decode(), round(ms[j], 2)] for j in range(max(0, mt))]
                 if first_phases is None:
                     first_phases = ph
                 if dev_ms[-1] > slow[0]:
-                    slow = (dev_ms[-1], ph)
+                    slow = (dev_ms[-1], ph, tl)
+                timelines.append(tl)
                 redo += any(names[j] == b"redo_wrong_guess" for j in range(max(0, m)))
             te = (time.perf_counter() - t0) / e2e_steps
             lib.psmma_set_profiling(0)
@@ -417,6 +420,8 @@ def run_gpu(args, ws, rank, local):
                              "ms_per_step": te * 1e3, "steps": e2e_steps, "call_ms": call_ms,
                              "device_span_ms": dev_ms, "redone_calls": redo, "first_call_phases_ms": first_phases,
                              "slowest_call_phases_ms": slow[1],
+                             "slowest_call_timeline_ms": slow[2],
+                             "upload_done_ms": [[v for nm, v in tl if nm == "a_panel_up"] for tl in timelines],
                              "api": "psmma_cauchy_host (pinned host buffers)"}
             # after the timed calls: one traced call (library-stream phases) and the pinned
             # copy rate of this host link, which bound the end-to-end time from below

@@ -427,6 +427,11 @@ int psmma_stream_release(void* stream);
  * phase names (static strings); the return value is the number of phases. */
 void psmma_set_profiling(int on);
 int psmma_profile_read(float* ms, const char** names, int max_phases);
+/* The same marks as a timeline: each mark's time in milliseconds since the call began, in the
+ * order they were recorded, waiting for every one of them.  Host-pointer split calls also mark
+ * their copy stream (a_panel_up: a row panel of A has landed; q_panel_down: a panel of Q is
+ * back on the host), which psmma_profile_read's consecutive differences do not separate. */
+int psmma_profile_read_timeline(float* ms, const char** names, int max_phases);
 
 /* No counterpart in the reference.  Self-test of the failure detection: launches a kernel
  * that waits on a device barrier nothing ever releases, with a limit of limit_ns

@@ -123,6 +123,7 @@ SIGNATURES = {
     "psmma_status_string": (C.c_char_p, [_i]),
     "psmma_set_profiling": (None, [_i]),
     "psmma_profile_read": (_i, [C.POINTER(C.c_float), C.POINTER(C.c_char_p), _i]),
+    "psmma_profile_read_timeline": (_i, [C.POINTER(C.c_float), C.POINTER(C.c_char_p), _i]),
     "psmma_version": (C.c_char_p, []),
     "psmma_selftest_wait_timeout": (_i, [C.c_ulonglong]),
     "psmma_selftest_division": (_i, [C.c_longlong, C.c_ulonglong, C.POINTER(C.c_ulonglong), C.POINTER(C.c_int)]),

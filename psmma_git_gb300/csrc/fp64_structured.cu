@@ -134,6 +134,7 @@ __device__ __forceinline__ void load_Hd_tile(double* Bs, const F64Args& p, int n
 // Each thread owns one column jj and BK/2 consecutive rows.
 struct ColGen {
   double F, V, F1, dl, dr;  // this thread's column generators
+  VSplit vs;                // V(j) split for the double-float entries
 };
 
 template <int KIND>
@@ -152,11 +153,11 @@ __device__ __forceinline__ void gen_H_tile(double* Bs, const F64Args& p, int n0,
       if (KIND == KIND_CAUCHY) {
         double d = __ldg(p.gs.Dr + gk);               // D(i)
         double u = __ldg(p.gs.Ur + gk);               // U(i)
-        h = div_nr(u * colV, d - colF);               // U(i)*V(j) / (D(i)-F(j))
+        h = cauchy_entry(u, colV, cg.vs, d - colF);   // U(i)*V(j) / (D(i)-F(j))
       } else if (KIND == KIND_CAUCHY_EIG) {
         const double fi = __ldg(p.gs.Dr + gk), u = __ldg(p.gs.Ur + gk);
         const bool upper = p.gs.rglob ? (__ldg(p.gs.rglob + gk) - 1 <= p.gs.cg0 + gj) : (gk - gj <= p.gs.diag_off);
-        h = div_nr(u * colV, eig_den(fi, colF, cg.F1, cg.dl, cg.dr, upper));
+        h = cauchy_entry(u, colV, cg.vs, eig_den(fi, colF, cg.F1, cg.dl, cg.dr, upper));
       } else if (KIND == KIND_TOEPLITZ) {
         h = __ldg(p.gs.g + (p.gs.order - 1) + gj - gk);  // G(K + j - i), 1-based
       } else {
@@ -207,7 +208,7 @@ __device__ __forceinline__ void struct_f64_tile(const F64Args& p, int bx, int by
   const int m0 = bx * F64_BM, n0 = by * F64_BN;
   const int wm0 = (warp & 1) * F64_WM, wn0 = (warp >> 1) * F64_WN;
 
-  ColGen cg{0.0, 0.0, 0.0, 0.0, 0.0};
+  ColGen cg{0.0, 0.0, 0.0, 0.0, 0.0, VSplit{}};
   if (KIND == KIND_CAUCHY || KIND == KIND_CAUCHY_EIG) {
     int gj = n0 + (tid % F64_BN);
     if (gj < p.N) {
@@ -221,6 +222,7 @@ __device__ __forceinline__ void struct_f64_tile(const F64Args& p, int bx, int by
         }
       }
     }
+    cg.vs = v_split(cg.V);
   }
 
   double acc[F64_MT][F64_NT][4];

@@ -752,6 +752,22 @@ int psmma_profile_read(float* ms, const char** names, int max_phases) {
   return m;
 }
 
+int psmma_profile_read_timeline(float* ms, const char** names, int max_phases) {
+  std::lock_guard<std::mutex> lk(g_prof_mu);
+  int np = g_prof_n - 1;
+  if (np <= 0) return 0;
+  for (int i = 1; i < g_prof_n; ++i)  // marks may sit on several streams: wait for each
+    if (cudaEventSynchronize(g_prof_ev[i]) != cudaSuccess) return PSMMA_EDEVICE;
+  int m = std::min(np, max_phases);
+  for (int i = 0; i < m; ++i) {
+    float t = 0.0f;
+    cudaEventElapsedTime(&t, g_prof_ev[0], g_prof_ev[i + 1]);
+    if (ms) ms[i] = t;
+    if (names) names[i] = g_prof_name[i + 1];
+  }
+  return m;
+}
+
 const char* psmma_version(void) { return "psmma-gb300 0.1.0 (sm_103a)"; }
 
 }  // extern "C"

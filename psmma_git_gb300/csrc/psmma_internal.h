@@ -202,7 +202,7 @@ void* pool_get(size_t bytes, cudaStream_t stream, int* status, int slot = 0);
 
 // Per-phase tracing (psmma_capi.cu): when enabled, launchers record a CUDA event on the
 // launch stream after each phase; psmma_profile_read turns them into milliseconds.
-constexpr int PROF_MAX_PHASES = 32;
+constexpr int PROF_MAX_PHASES = 64;
 bool prof_enabled();
 void prof_begin(cudaStream_t stream);
 void prof_mark(cudaStream_t stream, const char* name);

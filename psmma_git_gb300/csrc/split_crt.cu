@@ -1830,12 +1830,21 @@ static int split_core_host(int M, int N, int K, double alpha, const double* A_h,
     ok &= cudaStreamWaitEvent(cs, ev_panel[p], 0) == cudaSuccess;
     ok &= cudaMemcpy2DAsync(Q_h + r0, (size_t)ldq_h * 8, dQ + r0, (size_t)M * 8, (size_t)(r1 - r0) * 8, (size_t)N,
                             cudaMemcpyDeviceToHost, cs) == cudaSuccess;
+    prof_mark(cs, "q_panel_down");
   };
   // the parameters, then the caller's view of them once both streams are done
-  SplitDevParams head;  // status, PA, PH
+  // status, PA, PH: read back into pinned memory (a pageable destination would take the
+  // driver's staged path behind the stream's other copies); host calls are serialised
+  static SplitDevParams* head_pinned = nullptr;
+  if (!head_pinned && cudaHostAlloc((void**)&head_pinned, sizeof(SplitDevParams), cudaHostAllocPortable) != cudaSuccess) {
+    head_pinned = nullptr;
+    return PSMMA_ENOMEM;
+  }
+  SplitDevParams& head = *head_pinned;
   auto finish = [&]() {
     if (cudaGetLastError() != cudaSuccess) ok = false;
-    ok &= cudaMemcpyAsync(&head, b.prm, offsetof(SplitDevParams, rho_bits), cudaMemcpyDeviceToHost, s) == cudaSuccess;
+    ok &= cudaMemcpyAsync(head_pinned, b.prm, offsetof(SplitDevParams, rho_bits), cudaMemcpyDeviceToHost, s) ==
+          cudaSuccess;
     prof_mark(s, "params_head");
     prof_mark(cs, "q_download_tail");  // on the copy stream: the end of the last download
     ok &= cudaEventRecord(ev_done, cs) == cudaSuccess;
@@ -1851,6 +1860,7 @@ static int split_core_host(int M, int N, int K, double alpha, const double* A_h,
       ok &= cudaMemcpy2DAsync(dA + r0, (size_t)M * 8, A_h + r0, (size_t)lda_h * 8, (size_t)(r1 - r0) * 8,
                               (size_t)K, cudaMemcpyHostToDevice, cs) == cudaSuccess;
       ok &= cudaEventRecord(ev_up[p], cs) == cudaSuccess;
+      prof_mark(cs, "a_panel_up");
     }
     for (int p = 0; p < npanels; ++p) {
       const int r0 = pb[p] * G_BM, r1 = std::min(M, pb[p + 1] * G_BM);
@@ -1891,6 +1901,7 @@ static int split_core_host(int M, int N, int K, double alpha, const double* A_h,
     ok &= cudaMemcpy2DAsync(dA + (size_t)c0 * M, (size_t)M * 8, A_h + (size_t)c0 * lda_h, (size_t)lda_h * 8,
                             (size_t)M * 8, (size_t)(c1 - c0), cudaMemcpyHostToDevice, cs) == cudaSuccess;
     ok &= cudaEventRecord(ev_up[ch], cs) == cudaSuccess;
+    prof_mark(cs, "a_chunk_up");
     ok &= cudaStreamWaitEvent(s, ev_up[ch], 0) == cudaSuccess;
     dim3 g1((M + 127) / 128, (c1 - c0 + kchunk - 1) / kchunk);
     k_row_absmax<<<g1, 128, 0, s>>>(dA + (size_t)c0 * M, M, M, c1 - c0, kchunk, b.amax, b.asq);
