@@ -120,6 +120,7 @@ SIGNATURES = {
     "psmma_release_workspace": (None, []),
     "psmma_stream_status": (_i, [_p]),
     "psmma_stream_release": (_i, [_p]),
+    "psmma_split_dft_radix": (_i, [_i]),
     "psmma_status_string": (C.c_char_p, [_i]),
     "psmma_set_profiling": (None, [_i]),
     "psmma_profile_read": (_i, [C.POINTER(C.c_float), C.POINTER(C.c_char_p), _i]),

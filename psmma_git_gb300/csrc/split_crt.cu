@@ -196,11 +196,41 @@ static SplitLayout dft3_layout(int M, int n, int nmod) {
   return L;
 }
 
+// Radix of the split DFT's first step (C = F_n B via F_(n/R) on R k columns): 4 when n is a
+// multiple of 4 and n / 4 >= 2048, 2 when n is even and n / 2 >= 2048, else 1 (the modular
+// GEMMs keep an inner length of at least 2048).
+static int dft_radix(int n) {
+  if (n % 4 == 0 && n / 4 >= 2048) return 4;
+  if (n % 2 == 0 && n / 2 >= 2048) return 2;
+  return 1;
+}
+
+// Radix-R workspace: the core's (M = R k, n / R) layout, then B' and P (n x k complex each) and
+// the n-entry table w_n^t.
+struct DftRadixLayout {
+  size_t core, off_bp, off_p, off_w, total;
+};
+static DftRadixLayout dft_radix_layout(int n, int k, int R, int nmod) {
+  DftRadixLayout D;
+  D.core = al1k(dft3_layout(R * k, n / R, nmod).total);
+  D.off_bp = D.core;
+  D.off_p = D.off_bp + al1k((size_t)n * k * 16);
+  D.off_w = D.off_p + al1k((size_t)n * k * 16);
+  D.total = D.off_w + al1k((size_t)n * 16);
+  return D;
+}
+
 size_t split_workspace_bytes(int kind, int n, int k, int n_moduli) {
   if (n <= 0 || k <= 0) return 0;
-  if (kind == KIND_DFT) return dft3_layout(k, n, resolve_nmod(n_moduli)).total;
+  if (kind == KIND_DFT) {
+    const int R = dft_radix(n);
+    return R == 1 ? dft3_layout(k, n, resolve_nmod(n_moduli)).total
+                  : dft_radix_layout(n, k, R, resolve_nmod(n_moduli)).total;
+  }
   return split_layout(n, k, k, resolve_nmod(n_moduli)).total;
 }
+
+extern "C" int psmma_split_dft_radix(int n) { return n > 0 ? dft_radix(n) : 0; }
 
 size_t split_workspace_general(int M, int N, int K, int n_moduli) {
   if (M <= 0 || N <= 0 || K <= 0) return 0;
@@ -1613,6 +1643,74 @@ __global__ void k_status_or(unsigned* acc, const unsigned* st) {
 // The device status of a split call: status_dev_out == nullptr ORs it into the stream's status
 // word (no synchronisation), kStatusWait waits and returns it, any other pointer receives a copy
 // of it (no synchronisation).
+// ---- the DFT with a radix-R first step -------------------------------------------------------
+// With l = R m + r and j = j' + (n/R) s (r, s < R; m, j' < n/R),
+//   C(j' + (n/R) s, c) = sum_r w_R^(s r) w_n^(j' r) P_r(j', c),   P_r = F_(n/R) B(r::R, :),
+// so the dense product becomes F_(n/R) times the R k columns B' = [B(0::R, :) | ... | B(R-1::R, :)]:
+// n^2 k / R complex multiply-adds instead of n^2 k.  The twiddles w_n^(j' r) come from the exact
+// table (j' r < n, no reduction), then R-point butterflies (w_2 = -1, w_4 = -i: additions only).
+
+// B' (n/R x R k complex, ld n/R): B'(m, r k + c) = B(R m + r, c).  One thread per element of B
+// (coalesced reads along a column; each warp writes R runs of 32 / R consecutive elements).
+__global__ void k_dft_deinterleave(const double2* __restrict__ B, long ldb, int n, int k, int R,
+                                   double2* __restrict__ Bp) {
+  const int nq = n / R;
+  for (int c = blockIdx.y; c < k; c += gridDim.y) {
+    const double2* col = B + (long)c * ldb;
+    for (int l = blockIdx.x * blockDim.x + threadIdx.x; l < n; l += gridDim.x * blockDim.x) {
+      const int r = l % R, m = l / R;
+      Bp[((size_t)r * k + c) * nq + m] = __ldg(col + l);
+    }
+  }
+}
+
+// C(j' + nq s, c) = sum_r w_R^(s r) X_r + beta C, X_r = w_n^(j' r) P(j', r k + c) (P already
+// carries alpha).  One thread per (j', c), j' fastest: coalesced reads of P and writes of C.
+template <int R>
+__global__ void k_dft_radix_combine(const double2* __restrict__ P, int nq, int k, const double2* __restrict__ wn,
+                                    double beta, double2* __restrict__ C, long ldc) {
+  for (int c = blockIdx.y; c < k; c += gridDim.y) {
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < nq; j += gridDim.x * blockDim.x) {
+      double2 X[R];
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        const double2 p = __ldg(P + ((size_t)r * k + c) * nq + j);
+        if (r == 0) {
+          X[r] = p;
+        } else {
+          const double2 w = __ldg(wn + j * r);
+          X[r] = make_double2(fma(p.x, w.x, -p.y * w.y), fma(p.x, w.y, p.y * w.x));
+        }
+      }
+      double2 Y[R];
+      if (R == 2) {
+        Y[0] = make_double2(X[0].x + X[1].x, X[0].y + X[1].y);
+        Y[1] = make_double2(X[0].x - X[1].x, X[0].y - X[1].y);
+      } else {
+        // w_4 = -i: Y0 = t0 + t2, Y2 = t0 - t2, Y1 = t1 - i t3, Y3 = t1 + i t3
+        const double2 t0 = make_double2(X[0].x + X[2 % R].x, X[0].y + X[2 % R].y);
+        const double2 t1 = make_double2(X[0].x - X[2 % R].x, X[0].y - X[2 % R].y);
+        const double2 t2 = make_double2(X[1].x + X[3 % R].x, X[1].y + X[3 % R].y);
+        const double2 t3 = make_double2(X[1].x - X[3 % R].x, X[1].y - X[3 % R].y);
+        Y[0] = make_double2(t0.x + t2.x, t0.y + t2.y);
+        Y[2 % R] = make_double2(t0.x - t2.x, t0.y - t2.y);
+        Y[1] = make_double2(t1.x + t3.y, t1.y - t3.x);
+        Y[3 % R] = make_double2(t1.x - t3.y, t1.y + t3.x);
+      }
+      double2* out = C + (long)c * ldc + j;
+#pragma unroll
+      for (int q = 0; q < R; ++q) {
+        double2 y = Y[q];
+        if (beta != 0.0) {
+          const double2 o = out[(size_t)q * nq];
+          y = make_double2(fma(beta, o.x, y.x), fma(beta, o.y, y.y));
+        }
+        out[(size_t)q * nq] = y;
+      }
+    }
+  }
+}
+
 static int split_status(SplitDevParams* prm, cudaStream_t stream, unsigned* status_dev_out) {
   if (status_dev_out && status_dev_out != kStatusWait) {
     if (cudaMemcpyAsync(status_dev_out, &prm->status, sizeof(unsigned), cudaMemcpyDeviceToDevice, stream) !=
@@ -1980,9 +2078,8 @@ int launch_split_host_general(int M, int N, int K, double alpha, const double* A
 // kind != DFT: Q (n x k) = alpha * A (n x k) * H (k x k) + beta * Q.
 // C (n x k complex, ldc) = alpha * F * B + beta * C on the split path, F(j, l) = w^(j l): the
 // rows of the product are the k columns of B (M = k), three real products per modulus (3M).
-static int split_core_dft3(int M, int nn, double alpha, const double* B, long ldb, double beta, double* C,
-                           long ldc, int nmod, void* work, size_t lwork, cudaStream_t stream,
-                           unsigned* status_dev_out) {
+static int dft3_enqueue(int M, int nn, double alpha, const double* B, long ldb, double beta, double* C, long ldc,
+                        int nmod, void* work, size_t lwork, cudaStream_t stream, SplitDevParams** prm_out) {
   if (nmod < 8 || nmod > SPL_MAX_MODULI) return PSMMA_EUNSUPPORTED;
   if (2 * nn >= (1 << 24) || M >= (1 << 30)) return PSMMA_EUNSUPPORTED;
   const SplitLayout L = dft3_layout(M, nn, nmod);
@@ -2046,7 +2143,48 @@ static int split_core_dft3(int M, int nn, double alpha, const double* B, long ld
       b.R, M, nn, L.kr, cc, b.amax, b.hmax, b.prm, alpha, beta, C, 2 * ldc, 0);
   prof_mark(stream, "crt_combine");
   if (cudaGetLastError() != cudaSuccess) return PSMMA_EDEVICE;
-  return split_status(b.prm, stream, status_dev_out);
+  *prm_out = b.prm;
+  return PSMMA_OK;
+}
+
+// C (n x k complex, ldc) = alpha * F_n * B + beta * C: with R = dft_radix(n) > 1 the modular
+// products run on F_(n/R) and the R k columns of B' (k_dft_deinterleave), their result P =
+// alpha F_(n/R) B' goes to the workspace, and k_dft_radix_combine applies the twiddles, the
+// R-point butterflies and beta; R = 1 is the plain 3M product.
+static int split_core_dft3(int k, int n, double alpha, const double* B, long ldb, double beta, double* C,
+                           long ldc, int nmod, void* work, size_t lwork, cudaStream_t stream,
+                           unsigned* status_dev_out) {
+  const int R = dft_radix(n);
+  SplitDevParams* prm = nullptr;
+  int st;
+  if (R == 1) {
+    st = dft3_enqueue(k, n, alpha, B, ldb, beta, C, ldc, nmod, work, lwork, stream, &prm);
+  } else {
+    if ((size_t)k * R >= (1u << 30)) return PSMMA_EUNSUPPORTED;
+    const DftRadixLayout D = dft_radix_layout(n, k, R, nmod);
+    if (!work || lwork < D.total) return PSMMA_EWORKSPACE;
+    char* w = (char*)work;
+    double2* Bp = (double2*)(w + D.off_bp);
+    double2* P = (double2*)(w + D.off_p);
+    double2* wn = (double2*)(w + D.off_w);
+    const int nq = n / R;
+    const dim3 gd((n + 255) / 256 < 64 ? (n + 255) / 256 : 64, k < 65535 ? k : 65535);
+    k_dft_deinterleave<<<gd, 256, 0, stream>>>((const double2*)B, ldb, n, k, R, Bp);
+    st = launch_dft_table(wn, n, stream);
+    if (st) return st;
+    st = dft3_enqueue(R * k, nq, alpha, (const double*)Bp, nq, 0.0, (double*)P, nq, nmod, work, D.core, stream,
+                      &prm);
+    if (st) return st;
+    const dim3 gc((nq + 255) / 256 < 64 ? (nq + 255) / 256 : 64, k < 65535 ? k : 65535);
+    if (R == 4)
+      k_dft_radix_combine<4><<<gc, 256, 0, stream>>>(P, nq, k, wn, beta, (double2*)C, ldc);
+    else
+      k_dft_radix_combine<2><<<gc, 256, 0, stream>>>(P, nq, k, wn, beta, (double2*)C, ldc);
+    prof_mark(stream, "radix_combine");
+    if (cudaGetLastError() != cudaSuccess) return PSMMA_EDEVICE;
+  }
+  if (st) return st;
+  return split_status(prm, stream, status_dev_out);
 }
 
 // kind == DFT: C (n x k complex, ldq) = alpha * F (n x n) * B (n x k complex, lda) + beta * C,

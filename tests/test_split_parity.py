@@ -218,6 +218,33 @@ def test_split_dft_padded_leading_dimensions(n, k, pad, cuda):
     assert np.all(got[n:] == 7.0 + 7.0j)  # rows past n untouched
 
 
+@pytest.mark.parametrize("n,k,pad,beta", [(4100, 77, 3, -0.5), (8192, 300, 5, 0.0), (8192, 129, 0, 1.5),
+                                         (12288, 64, 1, 0.25)])
+def test_split_dft_radix_steps_match_fft(n, k, pad, beta, cuda):
+    # n / 2 >= 2048 (radix 2: n = 4100) and n / 4 >= 2048 (radix 4): the modular products run on
+    # F_(n/R) and R k columns, the twiddles and butterflies afterwards; padded leading
+    # dimensions, beta on and off, rows past n untouched
+    import psmma_git_gb300 as P
+    import torch
+    assert [P.load().psmma_split_dft_radix(m) for m in (n, 4094, 4096, 8190, 0)] == \
+        [2 if n == 4100 else 4, 1, 2, 2, 0]
+    B = O.cfg_matrix(n, k, seed=n + 21, complex_=True)
+    C0 = O.cfg_matrix(n, k, seed=k + 22, complex_=True)
+    Bbig = np.zeros((n + pad, k), np.complex128)
+    Bbig[:n] = B
+    Cbig = np.full((n + pad, k), 7.0 + 7.0j)
+    Cbig[:n] = C0
+    dB = _t(Bbig, cuda)[:n]
+    dC = _t(Cbig, cuda)
+    P.pzmdftl(n, k, 0.75, dB, beta, dC[:n], precision="split")
+    torch.cuda.synchronize()
+    got = _np(dC)
+    ref = O.dft_product(0.75, B, beta, C0)
+    assert O.rel_fro(got[:n], ref) < TOL
+    assert O.col_max_rel(got[:n], ref) < TOL
+    assert np.all(got[n:] == 7.0 + 7.0j)
+
+
 def test_split_dft_ones_fixture(cuda):
     z = np.load(GOLDEN / "dft_ones_kat.npz")
     n = int(z["n"])
