@@ -362,7 +362,8 @@ int psmma_last_status(void);
 /* No counterpart in the reference, whose callers make one blocking call at a time.  A
  * server admits queued requests in arrival order as soon as a stream slot is free and the
  * request's workspace fits in the remaining part of an HBM budget allocated once at
- * creation; admitted requests run concurrently on their own streams.  Operands stay on the
+ * creation; admitted requests run concurrently on their own streams, whose priorities follow
+ * admission order (the oldest request in flight has the highest).  Operands stay on the
  * device: A/B, generators and Q/C are device pointers owned by the caller, who must keep
  * them alive (and not touch Q/C) until the request completes. */
 typedef struct psmma_request {

@@ -5,7 +5,11 @@
 // stream slots is free and (b) the request's workspace fits in the remaining part of an
 // HBM budget that was allocated once at creation (first-fit arena, no allocation per
 // request).  Each admitted request runs on its own stream, so requests that arrive while
-// others are on the GPU overlap with them.  A host function enqueued after the request's
+// others are on the GPU overlap with them.  The stream's priority follows admission order: a
+// request admitted while c others are in flight runs at the c-th highest priority (clamped
+// to the device's range), so when SMs free up the GPU prefers the oldest request's kernels.
+// Without it the requests share the SMs evenly and a large request is slowed by every request
+// admitted after it, which sets the latency tail.  A host function enqueued after the request's
 // kernels hands it to a completion thread, which frees its arena slice and slot, reads its
 // CUDA-event GPU time and status, and wakes the waiters and the dispatcher.
 #include <atomic>
@@ -95,7 +99,9 @@ struct psmma_server {
   void* arena_base = nullptr;
   psmma::Arena arena;
   int max_inflight = 1;
-  std::vector<cudaStream_t> streams;
+  std::vector<std::vector<cudaStream_t>> streams;  // [slot][priority level], level 0 highest
+  std::vector<cudaStream_t> slot_stream;           // the stream of the slot's current request
+  int levels = 1;
   std::vector<cudaEvent_t> ev_start, ev_end;
   std::vector<bool> slot_busy;
   unsigned* dev_status = nullptr;   // one word per slot
@@ -151,7 +157,7 @@ int check_request(const psmma_request& r) {
 // Enqueues the request's kernels on the slot's stream (no synchronisation).
 int launch_job(psmma_server* s, Job& j) {
   const psmma_request& r = j.req;
-  cudaStream_t st = s->streams[j.slot];
+  cudaStream_t st = s->slot_stream[j.slot];
   void* work = j.work_bytes ? (char*)s->arena_base + j.work_off : nullptr;
   unsigned* status = s->dev_status + j.slot;
   if (cudaMemsetAsync(status, 0, sizeof(unsigned), st) != cudaSuccess) return PSMMA_EDEVICE;
@@ -216,6 +222,9 @@ void dispatcher_main(psmma_server* s) {
       return head.work_bytes == 0 || s->arena.alloc(head.work_bytes, &off);
     });
     if (s->stop) return;
+    int busy = 0;
+    for (int i = 0; i < s->max_inflight; ++i) busy += s->slot_busy[i] ? 1 : 0;
+    s->slot_stream[slot] = s->streams[slot][std::min(busy, s->levels - 1)];
     const unsigned long long t = s->pending.front();
     s->pending.pop_front();
     Job& j = s->jobs[t];
@@ -227,7 +236,7 @@ void dispatcher_main(psmma_server* s) {
     Job copy = j;
     lk.unlock();
     // enqueue outside the lock; only this thread launches work
-    cudaStream_t st = s->streams[slot];
+    cudaStream_t st = s->slot_stream[slot];
     int e = (cudaEventRecord(s->ev_start[slot], st) == cudaSuccess) ? PSMMA_OK : PSMMA_EDEVICE;
     if (!e) e = launch_job(s, copy);
     if (cudaEventRecord(s->ev_end[slot], st) != cudaSuccess && !e) e = PSMMA_EDEVICE;
@@ -298,13 +307,19 @@ int psmma_server_create(size_t hbm_budget_bytes, int max_inflight, psmma_server*
     delete s;
     return PSMMA_ENOMEM;
   }
-  s->streams.resize(max_inflight);
+  int least = 0, greatest = 0;
+  if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) least = greatest = 0;
+  s->levels = std::max(1, std::min(least - greatest + 1, max_inflight));
+  s->streams.assign(max_inflight, std::vector<cudaStream_t>(s->levels, nullptr));
+  s->slot_stream.assign(max_inflight, nullptr);
   s->ev_start.resize(max_inflight);
   s->ev_end.resize(max_inflight);
   s->slot_busy.assign(max_inflight, false);
   s->slot_ticket.assign(max_inflight, 0);
   for (int i = 0; i < max_inflight; ++i) {
-    cudaStreamCreateWithFlags(&s->streams[i], cudaStreamNonBlocking);
+    for (int l = 0; l < s->levels; ++l)
+      cudaStreamCreateWithPriority(&s->streams[i][l], cudaStreamNonBlocking, greatest + l);
+    s->slot_stream[i] = s->streams[i][0];
     cudaEventCreate(&s->ev_start[i]);
     cudaEventCreate(&s->ev_end[i]);
   }
@@ -385,8 +400,10 @@ int psmma_server_destroy(psmma_server* s) {
   s->dispatcher.join();
   s->completer.join();
   for (int i = 0; i < s->max_inflight; ++i) {
-    cudaStreamSynchronize(s->streams[i]);
-    cudaStreamDestroy(s->streams[i]);
+    for (int l = 0; l < s->levels; ++l) {
+      cudaStreamSynchronize(s->streams[i][l]);
+      cudaStreamDestroy(s->streams[i][l]);
+    }
     cudaEventDestroy(s->ev_start[i]);
     cudaEventDestroy(s->ev_end[i]);
   }
