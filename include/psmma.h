@@ -230,7 +230,8 @@ size_t psmma_toeplitz_batch_workspace_size(int count, const psmma_batch_item* it
 /* No counterpart in the reference.  Autotuner of the split path's grouped GEMM (output-tile
  * widths 64/128/256 by product width, raster group): times psmma_cauchy_batch_lowrank on
  * this batch for each candidate configuration and keeps the fastest for batches of the same
- * signature (count, precision, moduli, compressor and the sizes in 1/8-octave bins); later
+ * signature (count, precision, moduli, compressor and the sizes in 1/8-octave bins), if it
+ * beats the default configuration by more than 2 % (else the default is kept); later
  * calls with that signature use it.  With the environment variable PSMMA_TUNE_CACHE naming a
  * file, results are appended there and read back by later processes.  Runs the batch about
  * 40 times: the Q_i are overwritten (meaningless afterwards when beta != 0).  The FP64 path

@@ -73,3 +73,51 @@ def test_row_panels_assemble_the_full_product_gloo():
     ref = O.dense_product("cauchy", 1.0, O.cfg_matrix(n, k, seed=3), O.cfg_cauchy_generators(k, seed=4), 0.0,
                           None, k)
     assert O.rel_fro(Q, ref) < 1e-14
+
+
+def _strong_worker(rank, world, port, n, k, out_q):
+    # the bench's --strong mode on CPU: one n x k problem, rank r holds rows local_panel(n, r, world)
+    # of A only, multiplies them, and the slowest rank's time is the job's
+    import torch.distributed as dist
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        from oracle import psmma_oracle as O
+        from psmma_git_gb300.shard import max_over_ranks, sharded_multiply
+        lo, hi = local_panel(n, rank, world)
+        A_rows = O.cfg_matrix(n, k, seed=5)[lo:hi]
+        gen = O.cfg_vector(2 * k - 1, seed=6)
+
+        def oracle_compute(rows, kk, alpha, Ap, g, beta, Qp):
+            assert rows == Ap.shape[0] == hi - lo
+            return O.dense_product("toeplitz", alpha, Ap, g, beta, Qp, kk)
+
+        Qp = sharded_multiply("toeplitz", n, k, 0.5, A_rows, gen, 0.0, np.zeros((hi - lo, k)), rank=rank,
+                              world=world, compute=oracle_compute)
+        out_q.put((rank, lo, hi, Qp, max_over_ranks(float(hi - lo))))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_strong_scaling_row_panels_gloo():
+    # world size 3 on n = 40 rows: uneven panels (14, 13, 13) that assemble the whole product
+    import multiprocessing as mp
+    from oracle import psmma_oracle as O
+    n, k, world = 40, 23, 3
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_strong_worker, args=(r, world, port, n, k, q)) for r in range(world)]
+    for p in procs:
+        p.start()
+    got = [q.get(timeout=120) for _ in range(world)]
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    Q = np.full((n, k), np.nan)
+    for rank, lo, hi, Qp, slowest in got:
+        Q[lo:hi] = Qp
+        assert slowest == 14.0
+    ref = O.dense_product("toeplitz", 0.5, O.cfg_matrix(n, k, seed=5), O.cfg_vector(2 * k - 1, seed=6), 0.0, None, k)
+    assert O.rel_fro(Q, ref) < 1e-14
