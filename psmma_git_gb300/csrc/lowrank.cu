@@ -696,13 +696,17 @@ __global__ void __launch_bounds__(QR_THREADS) k_qr_tiles(QrTile* tiles, int ntil
       ss = fma(h, h, ss);
     }
   } else {
+    // the entries in the double-float form of the split path's H (cauchy_entry: the FP64 pole
+    // difference, then u v / x on the FP32 pipe, about 2^-49 relative): the IEEE division
+    // would be a dozen instructions on GB300's narrow FP64 pipe, which the QR itself needs
     const bool eig = g.kind == KIND_CAUCHY_EIG;
     const double f = g.Fc[c], v = g.Vc[c];
+    const VSplit vs = v_split(v);
     const double f1 = (eig && c < g.fc1_len) ? g.Fc1[c] : 0.0;
     const double dl = eig ? g.dl[c] : 0.0, dr = (eig && c < g.fc1_len) ? g.dr[c] : 0.0;
     for (int i = threadIdx.x; i < t.M; i += blockDim.x) {
-      const double h = eig ? (g.Ur[i] * v) / eig_den(g.Dr[i], f, f1, dl, dr, i - c <= g.diag_off)
-                           : (g.Ur[i] * v) / (g.Dr[i] - f);
+      const double h = eig ? cauchy_entry(g.Ur[i], v, vs, eig_den(g.Dr[i], f, f1, dl, dr, i - c <= g.diag_off))
+                           : cauchy_entry(g.Ur[i], v, vs, g.Dr[i] - f);
       t.T[i + (long)c * t.M] = h;
       ss = fma(h, h, ss);
     }

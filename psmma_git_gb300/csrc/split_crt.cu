@@ -2247,21 +2247,51 @@ __device__ __forceinline__ int gfind(const GProb* d, int count, int blk) {
 
 constexpr int G_ROW_KCHUNK = 1024;
 
-__global__ void __launch_bounds__(128) k_g_row_absmax(const GProb* d, int count) {
-  const GProb& e = d[gfind<0>(d, count, blockIdx.x)];
-  const int local = blockIdx.x - e.b_row, gx = (e.M + 127) / 128;
-  row_absmax_blk(e.A, e.lda, e.A2, e.lda2, e.ka, e.M, e.K, G_ROW_KCHUNK, e.amax, e.asq, local % gx, local / gx);
+// Each CTA of a grouped pass kernel walks a run of consecutive logical blocks (one binary
+// search per CTA, then a linear advance across product boundaries): a lookup per logical block
+// (seven dependent loads of the descriptor table before any data moves) had made the small
+// blocks of these passes latency-bound.  Runs per kernel: rows 2, H columns 2, residue and CRT
+// tiles 8, H residue strips 16.
+template <int W>
+__device__ __forceinline__ int gkey(const GProb& e) {
+  return W == 0 ? e.b_row : W == 1 ? e.b_h : W == 2 ? e.b_ra : W == 3 ? e.b_rh : e.b_crt;
+}
+template <int W>
+struct GRun {
+  int b, end, p;
+  __device__ GRun(const GProb* d, int count, int total, int chunk) {
+    b = blockIdx.x * chunk;
+    end = min(b + chunk, total);
+    p = b < end ? gfind<W>(d, count, b) : 0;
+  }
+  // the product owning logical block b (the last one whose first block is <= b)
+  __device__ __forceinline__ const GProb& owner(const GProb* d, int count) {
+    while (p + 1 < count && gkey<W>(d[p + 1]) <= b) ++p;
+    return d[p];
+  }
+};
+constexpr int G_RUN_ROW = 2, G_RUN_H = 2, G_RUN_RA = 8, G_RUN_RH = 16, G_RUN_CRT = 8;
+
+__global__ void __launch_bounds__(128) k_g_row_absmax(const GProb* d, int count, int total) {
+  for (GRun<0> r(d, count, total, G_RUN_ROW); r.b < r.end; ++r.b) {
+    const GProb& e = r.owner(d, count);
+    const int local = r.b - e.b_row, gx = (e.M + 127) / 128;
+    row_absmax_blk(e.A, e.lda, e.A2, e.lda2, e.ka, e.M, e.K, G_ROW_KCHUNK, e.amax, e.asq, local % gx, local / gx);
+  }
 }
 
-__global__ void __launch_bounds__(256) k_g_h_pass1(const GProb* d, int count) {
-  const GProb& e = d[gfind<1>(d, count, blockIdx.x)];
-  const int j = blockIdx.x - e.b_h;
-  switch (e.gs.kind) {
-    case KIND_CAUCHY: h_pass1_blk<KIND_CAUCHY>(e.gs, e.K, e.kp, e.Ht, e.hmax, e.hsum, e.hsq, e.prm, j); break;
-    case KIND_TOEPLITZ: h_pass1_blk<KIND_TOEPLITZ>(e.gs, e.K, e.kp, e.Ht, e.hmax, e.hsum, e.hsq, e.prm, j); break;
-    case KIND_HANKEL: h_pass1_blk<KIND_HANKEL>(e.gs, e.K, e.kp, e.Ht, e.hmax, e.hsum, e.hsq, e.prm, j); break;
-    case KIND_CAUCHY_EIG: h_pass1_blk<KIND_CAUCHY_EIG>(e.gs, e.K, e.kp, e.Ht, e.hmax, e.hsum, e.hsq, e.prm, j); break;
-    default: h_pass1_blk<KIND_DENSE>(e.gs, e.K, e.kp, e.Ht, e.hmax, e.hsum, e.hsq, e.prm, j); break;
+__global__ void __launch_bounds__(256) k_g_h_pass1(const GProb* d, int count, int total) {
+  for (GRun<1> r(d, count, total, G_RUN_H); r.b < r.end; ++r.b) {
+    const GProb& e = r.owner(d, count);
+    const int j = r.b - e.b_h;
+    switch (e.gs.kind) {
+      case KIND_CAUCHY: h_pass1_blk<KIND_CAUCHY>(e.gs, e.K, e.kp, e.Ht, e.hmax, e.hsum, e.hsq, e.prm, j); break;
+      case KIND_TOEPLITZ: h_pass1_blk<KIND_TOEPLITZ>(e.gs, e.K, e.kp, e.Ht, e.hmax, e.hsum, e.hsq, e.prm, j); break;
+      case KIND_HANKEL: h_pass1_blk<KIND_HANKEL>(e.gs, e.K, e.kp, e.Ht, e.hmax, e.hsum, e.hsq, e.prm, j); break;
+      case KIND_CAUCHY_EIG: h_pass1_blk<KIND_CAUCHY_EIG>(e.gs, e.K, e.kp, e.Ht, e.hmax, e.hsum, e.hsq, e.prm, j); break;
+      default: h_pass1_blk<KIND_DENSE>(e.gs, e.K, e.kp, e.Ht, e.hmax, e.hsum, e.hsq, e.prm, j); break;
+    }
+    __syncthreads();  // the block's shared reduction buffers are reused by the next column
   }
 }
 
@@ -2270,24 +2300,33 @@ __global__ void __launch_bounds__(1024) k_g_split_params(const GProb* d, double 
   split_params_blk(e.prm, log2M, e.M, e.N, e.K, e.amax, e.asq, e.hmax, e.hsq);
 }
 
-__global__ void __launch_bounds__(256) k_g_residues_A(const GProb* d, int count, CrtConsts cc) {
-  const GProb& e = d[gfind<2>(d, count, blockIdx.x)];
-  const int local = blockIdx.x - e.b_ra, gx = e.kp / 64;
-  residues_A_blk<64>(e.A, e.lda, e.A2, e.lda2, e.ka, e.M, e.K, e.kp, e.amax, e.prm, cc, e.RA, local % gx, local / gx);
+__global__ void __launch_bounds__(256) k_g_residues_A(const GProb* d, int count, int total, CrtConsts cc) {
+  for (GRun<2> r(d, count, total, G_RUN_RA); r.b < r.end; ++r.b) {
+    const GProb& e = r.owner(d, count);
+    const int local = r.b - e.b_ra, gx = e.kp / 64;
+    residues_A_blk<64>(e.A, e.lda, e.A2, e.lda2, e.ka, e.M, e.K, e.kp, e.amax, e.prm, cc, e.RA, local % gx,
+                       local / gx);
+    __syncthreads();  // the shared tile is refilled for the next block
+  }
 }
 
-__global__ void __launch_bounds__(128) k_g_residues_H(const GProb* d, int count, CrtConsts cc) {
-  const GProb& e = d[gfind<3>(d, count, blockIdx.x)];
-  const int local = blockIdx.x - e.b_rh, gx = rh_blocks_x(e.kp);
-  residues_H_blk(e.Ht, e.N, e.kp, e.hmax, e.prm, cc, e.RH, local % gx, local / gx);
+__global__ void __launch_bounds__(128) k_g_residues_H(const GProb* d, int count, int total, CrtConsts cc) {
+  for (GRun<3> r(d, count, total, G_RUN_RH); r.b < r.end; ++r.b) {
+    const GProb& e = r.owner(d, count);
+    const int local = r.b - e.b_rh, gx = rh_blocks_x(e.kp);
+    residues_H_blk(e.Ht, e.N, e.kp, e.hmax, e.prm, cc, e.RH, local % gx, local / gx);
+  }
 }
 
 template <bool TOP32>
-__global__ void __launch_bounds__(256, 3) k_g_crt_combine(const GProb* d, int count, CrtConsts cc) {
-  const GProb& e = d[gfind<4>(d, count, blockIdx.x)];
-  const int local = blockIdx.x - e.b_crt, gx = (e.N + CRT_TJ - 1) / CRT_TJ;
-  crt_combine_blk<false, TOP32>(e.R, e.M, e.N, e.kr, cc, e.amax, e.hmax, e.prm, e.alpha, e.beta, e.Q, e.ldq, local % gx,
-                         local / gx);
+__global__ void __launch_bounds__(256, 3) k_g_crt_combine(const GProb* d, int count, int total, CrtConsts cc) {
+  for (GRun<4> r(d, count, total, G_RUN_CRT); r.b < r.end; ++r.b) {
+    const GProb& e = r.owner(d, count);
+    const int local = r.b - e.b_crt, gx = (e.N + CRT_TJ - 1) / CRT_TJ;
+    crt_combine_blk<false, TOP32>(e.R, e.M, e.N, e.kr, cc, e.amax, e.hmax, e.prm, e.alpha, e.beta, e.Q, e.ldq,
+                                  local % gx, local / gx);
+    __syncthreads();  // the shared transpose tile is reused by the next block
+  }
 }
 
 namespace {
@@ -2460,15 +2499,16 @@ int split_group_enqueue(const SplitGroup& g, cudaStream_t stream, unsigned* stat
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
     return PSMMA_EDEVICE;
   if (cudaMemsetAsync(g.small, 0, g.small_bytes, stream) != cudaSuccess) return PSMMA_EDEVICE;
-  k_g_row_absmax<<<g.blocks_row, 128, 0, stream>>>(d, g.count);
+  auto runs = [](int total, int chunk) { return (unsigned)((total + chunk - 1) / chunk); };
+  if (g.blocks_row > 0) k_g_row_absmax<<<runs(g.blocks_row, G_RUN_ROW), 128, 0, stream>>>(d, g.count, g.blocks_row);
   prof_mark(stream, "g_row_scale");
-  k_g_h_pass1<<<g.blocks_h, 256, 0, stream>>>(d, g.count);
+  if (g.blocks_h > 0) k_g_h_pass1<<<runs(g.blocks_h, G_RUN_H), 256, 0, stream>>>(d, g.count, g.blocks_h);
   prof_mark(stream, "g_h_generate");
   k_g_split_params<<<g.count, 1024, 0, stream>>>(d, cc.log2M);
   prof_mark(stream, "g_params");
-  k_g_residues_A<<<g.blocks_ra, 256, 0, stream>>>(d, g.count, cc);
+  if (g.blocks_ra > 0) k_g_residues_A<<<runs(g.blocks_ra, G_RUN_RA), 256, 0, stream>>>(d, g.count, g.blocks_ra, cc);
   prof_mark(stream, "g_residues_A");
-  k_g_residues_H<<<g.blocks_rh, 128, 0, stream>>>(d, g.count, cc);
+  if (g.blocks_rh > 0) k_g_residues_H<<<runs(g.blocks_rh, G_RUN_RH), 128, 0, stream>>>(d, g.count, g.blocks_rh, cc);
   prof_mark(stream, "g_residues_H");
   int st = launch_group_gemm<256>(g, 0, cc, sms, stream);
   prof_mark(stream, "g_gemm_256");
@@ -2477,8 +2517,9 @@ int split_group_enqueue(const SplitGroup& g, cudaStream_t stream, unsigned* stat
   if (!st) st = launch_group_gemm<64>(g, 1, cc, sms, stream);
   prof_mark(stream, "g_gemm_64");
   if (st) return st;
-  (cc.top32 ? k_g_crt_combine<true> : k_g_crt_combine<false>)<<<g.blocks_crt, dim3(32, 8), 0, stream>>>(d, g.count,
-                                                                                                      cc);
+  if (g.blocks_crt > 0)
+    (cc.top32 ? k_g_crt_combine<true> : k_g_crt_combine<false>)<<<runs(g.blocks_crt, G_RUN_CRT), dim3(32, 8), 0,
+                                                                   stream>>>(d, g.count, g.blocks_crt, cc);
   prof_mark(stream, "g_crt_combine");
   if (cudaGetLastError() != cudaSuccess) return PSMMA_EDEVICE;
   if (status_out &&
