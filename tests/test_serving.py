@@ -125,3 +125,26 @@ def test_server_cauchyeig_requests_match_oracle(cuda):
             Q = P.fortran_empty(n, n)
             assert srv.wait(srv.submit("cauchyeig", n, n, 1.0, dA, gen, 0.0, Q, precision=prec))["status"] == 0
             assert O.rel_fro(Q.cpu().numpy(), ref) < tol, prec
+
+
+def test_large_request_between_small_ones(cuda):
+    # small requests, two large ones (n = 8192, split DFT with its radix step, and a split
+    # Cauchy multiply of n = 6144) in the middle, small ones after: every result is its multiply
+    # alone within the split path's bound, all statuses are ok, and the small request admitted
+    # first (highest-priority stream) is done before the large ones
+    import torch
+    from psmma_git_gb300.server import Server
+    plan = [("hankel", 512), ("toeplitz", 700), ("dft", 8192), ("cauchy", 600), ("cauchy", 6144),
+            ("hankel", 256), ("dft", 384), ("toeplitz", 1000)]
+    reqs = [(k, n) + _make(k, n, 300 + i, cuda) for i, (k, n) in enumerate(plan)]
+    torch.cuda.synchronize()
+    with Server(64 << 30, max_inflight=4) as srv:
+        tickets = [srv.submit(k, n, n, 1.0, A, g, 0.0, Q, precision="split", tag=i)
+                   for i, (k, n, A, g, Q) in enumerate(reqs)]
+        infos = [srv.wait(t) for t in tickets]
+    assert all(i["status"] == 0 for i in infos)
+    for (k, n, A, g, Q), info in zip(reqs, infos):
+        ref = _alone(k, n, A, g, "split", cuda)
+        assert (torch.linalg.norm(Q - ref) / torch.linalg.norm(ref)).item() < 1e-12, (k, n)
+    large_end = max(infos[2]["end_s"], infos[4]["end_s"])
+    assert infos[0]["end_s"] <= large_end
