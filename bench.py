@@ -508,9 +508,24 @@ def run_case(args, ws, rank, local):
     e1.record()
     torch.cuda.synchronize()
     t = e0.elapsed_time(e1) / args.steps
+    # the timed result checked on a sample: 4 columns against the FFT (DFT), or 64 rows against
+    # the FP64 path (the other kinds)
+    if kind == "dft":
+        ref = np.fft.fft(X[:, :4].cpu().numpy(), axis=0)
+        err = O.rel_fro(Y[:, :4].cpu().numpy(), ref)
+    else:
+        R64 = P.fortran_empty(64, k, torch.float64, dev)
+        if kind == "cauchy":
+            P.psmma_cauchy(64, k, 1.0, A[:64], gen, 0.0, R64)
+        elif kind == "cauchyeig":
+            P.psmma_cauchyeig(64, k, 1.0, A[:64], *eig, 0.0, R64)
+        else:
+            fn(64, k, 1.0, A[:64], gv, 0.0, R64)
+        torch.cuda.synchronize()
+        err = float(torch.linalg.norm(Y[:64] - R64) / torch.linalg.norm(R64))
     print(json.dumps({"case": args.case, "n": n, "ms_per_call": t, "tflops": flops / t / 1e9,
-                      "steps": args.steps, "warmup": args.warmup}), flush=True)
-    return 0
+                      "steps": args.steps, "warmup": args.warmup, "rel_err_sample": err}), flush=True)
+    return 0 if err < (1e-12 if prec == "split" else 1e-13) else 1
 
 
 def run_extras(args, ws, rank, local) -> dict:

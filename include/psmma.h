@@ -133,11 +133,11 @@ int pzmdftl(int n, int k, double alpha, const psmma_complex* B, int ldb,
 int pzmdftl1(int n, int k, double alpha, const psmma_complex* B, int ldb,
              double beta, psmma_complex* C, int ldc, const psmma_opts* opts, void* stream);
 
-/* No counterpart in the reference.  The radix R (1, 2 or 4) of the split path's first DFT step
- * for size n: with R > 1, pzmdftl / pzmdftl1 on the split path multiply F_(n/R) by the R k
+/* No counterpart in the reference.  The radix R (1, 2, 4 or 8) of the split path's first DFT
+ * step for size n: with R > 1, pzmdftl / pzmdftl1 on the split path multiply F_(n/R) by the R k
  * columns B(r::R, :) (n^2 k / R complex multiply-adds on the tensor cores) and combine the R
- * partial transforms with the twiddles w^(j r) and R-point butterflies in FP64; R = 4 when
- * n / 4 >= 2048, R = 2 when n / 2 >= 2048 (n divisible by R), else 1.  0 for n <= 0. */
+ * partial transforms with the twiddles w^(j r) and R-point butterflies in FP64; R is the
+ * largest of 8, 4, 2 that divides n with n / R >= 1024, else 1.  0 for n <= 0. */
 int psmma_split_dft_radix(int n);
 
 /* No counterpart in the reference.  The split-path Cauchy multiply (same arguments and

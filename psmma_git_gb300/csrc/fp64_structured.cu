@@ -405,8 +405,7 @@ int launch_struct_f64_ws(int M, int N, int K, double alpha, const double* X, lon
   case KD: {                                                                                  \
     static bool attr_set = false;                                                             \
     if (!attr_set) {                                                                          \
-      if (cudaFuncSetAttribute(k_struct_f64<KD>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                               (int)F64_SMEM_BYTES) != cudaSuccess)                           \
+      if (set_smem_attr(k_struct_f64<KD>, (int)F64_SMEM_BYTES) != cudaSuccess)                           \
         return PSMMA_EDEVICE;                                                                 \
       attr_set = true;                                                                        \
     }                                                                                         \
@@ -481,8 +480,7 @@ int f64_group_prepare(const F64Prob* P, int count, void* dev, cudaStream_t strea
 
 template <int KIND>
 static int f64_group_launch(const F64Group& g, const F64Args* a, cudaStream_t stream) {
-  if (cudaFuncSetAttribute(k_struct_f64_group<KIND>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)F64_SMEM_BYTES) != cudaSuccess)
+  if (set_smem_attr(k_struct_f64_group<KIND>, (int)F64_SMEM_BYTES) != cudaSuccess)
     return PSMMA_EDEVICE;
   k_struct_f64_group<KIND><<<g.blocks, F64_THREADS, F64_SMEM_BYTES, stream>>>(a, g.d_t0, g.count);
   return PSMMA_OK;

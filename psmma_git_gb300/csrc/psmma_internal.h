@@ -88,6 +88,16 @@ inline GenSpec eig_gens_packed(const double* gen, long ldgen, int k) {
   return g;
 }
 
+// cudaFuncSetAttribute(fn, MaxDynamicSharedMemorySize, bytes), after reading any launch error
+// still pending from an earlier <<<>>> launch on this thread: the attribute call succeeds and
+// clears that error, so without the read a launch the device refused would go unreported.
+template <class F>
+inline cudaError_t set_smem_attr(F* fn, int bytes) {
+  const cudaError_t pending = cudaGetLastError();
+  if (pending != cudaSuccess) return pending;
+  return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
 // FP64 plain path (fp64_structured.cu).  Real GEMM C(MxN) = alpha*X*G + beta*C where one
 // operand is streamed (X, column-major, ldx) and the other generated.
 int launch_struct_f64(int M, int N, int K, double alpha, const double* X, long ldx, const GenSpec& gs,

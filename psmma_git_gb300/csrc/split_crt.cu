@@ -167,6 +167,11 @@ static SplitLayout split_layout(int M, int K, int N, int nmod) {
   return L;
 }
 
+// Rows of one split product: the residue and CRT passes tile rows in blocks of 64 and 32
+// along the grid's y dimension (at most 65535 blocks), so M <= 32 * 65535; larger products
+// are refused with PSMMA_EUNSUPPORTED rather than launched with a grid the device rejects.
+constexpr int kSplitMaxRows = 32 * 65535;
+
 static int resolve_nmod(int n_moduli) { return n_moduli == 0 ? SPL_DEFAULT_MODULI : n_moduli; }
 
 // The DFT's split workspace: C^T = B^T F (k x n complex) as three real products of the 3M
@@ -196,12 +201,13 @@ static SplitLayout dft3_layout(int M, int n, int nmod) {
   return L;
 }
 
-// Radix of the split DFT's first step (C = F_n B via F_(n/R) on R k columns): 4 when n is a
-// multiple of 4 and n / 4 >= 2048, 2 when n is even and n / 2 >= 2048, else 1 (the modular
-// GEMMs keep an inner length of at least 2048).
+// Radix of the split DFT's first step (C = F_n B via F_(n/R) on R k columns): the largest R in
+// {8, 4, 2} dividing n with n / R >= kDftMinInner (the modular GEMMs keep that inner length),
+// else 1.
+constexpr int kDftMinInner = 1024;
 static int dft_radix(int n) {
-  if (n % 4 == 0 && n / 4 >= 2048) return 4;
-  if (n % 2 == 0 && n / 2 >= 2048) return 2;
+  for (int R = 8; R >= 2; R >>= 1)
+    if (n % R == 0 && n / R >= kDftMinInner) return R;
   return 1;
 }
 
@@ -755,7 +761,7 @@ __device__ __forceinline__ void residues_H_blk(const double* __restrict__ Ht, in
 __global__ void k_residues_H(const double* __restrict__ Ht, int ncols, int kp,
                              const unsigned long long* __restrict__ hmax_bits, const SplitDevParams* prm,
                              CrtConsts cc, __nv_bfloat16* __restrict__ RH) {
-  residues_H_blk(Ht, ncols, kp, hmax_bits, prm, cc, RH, blockIdx.x, blockIdx.y);
+  residues_H_blk(Ht, ncols, kp, hmax_bits, prm, cc, RH, blockIdx.y, blockIdx.x);  // x: column (any count)
 }
 
 // Speculative H residues: with guess >= 0 and !redo, the planes for PH = guess (before the
@@ -765,7 +771,7 @@ __global__ void k_residues_H_spec(const double* __restrict__ Ht, int ncols, int 
                                   const unsigned long long* __restrict__ hmax_bits, const SplitDevParams* prm,
                                   CrtConsts cc, __nv_bfloat16* __restrict__ RH, int guess, int redo) {
   if (redo && prm->PH == guess) return;
-  residues_H_blk(Ht, ncols, kp, hmax_bits, prm, cc, RH, blockIdx.x, blockIdx.y, redo ? -1 : guess);
+  residues_H_blk(Ht, ncols, kp, hmax_bits, prm, cc, RH, blockIdx.y, blockIdx.x, redo ? -1 : guess);
 }
 
 // DFT A side: row i of the product (B^T) is column i of B, read contiguously (Bre = B as
@@ -915,8 +921,8 @@ __global__ void __launch_bounds__(256) k_h_pass1_dft3(const double2* __restrict_
 __global__ void k_residues_A_dft3(const double* __restrict__ Bre, long ldb2, int nn, int kp,
                                   const unsigned long long* __restrict__ amax_bits, const SplitDevParams* prm,
                                   CrtConsts cc, __nv_bfloat16* __restrict__ RA, int M) {
-  const int i = blockIdx.y;
-  const int kk = 2 * (blockIdx.x * blockDim.x + threadIdx.x);
+  const int i = blockIdx.x;  // rows in x: M = R k can pass the 65535 limit of y
+  const int kk = 2 * (blockIdx.y * blockDim.x + threadIdx.x);
   if (kk >= kp) return;
   const unsigned long long ab = amax_bits[i];
   const bool ok = ab > 0 && ab < INF_BITS;
@@ -952,8 +958,8 @@ __global__ void k_residues_A_dft3(const double* __restrict__ Bre, long ldb2, int
 __global__ void k_residues_H_dft3(const double* __restrict__ Ht, int nn, int kp,
                                   const unsigned long long* __restrict__ hmax_bits, const SplitDevParams* prm,
                                   CrtConsts cc, __nv_bfloat16* __restrict__ RH) {
-  const int j = blockIdx.y;
-  const int kk = RH_PER_THREAD * (blockIdx.x * blockDim.x + threadIdx.x);
+  const int j = blockIdx.x;  // columns in x (any count)
+  const int kk = RH_PER_THREAD * (blockIdx.y * blockDim.x + threadIdx.x);
   if (kk >= kp) return;  // kp is a multiple of 64
   const unsigned long long hb = hmax_bits[j];
   const bool ok = hb > 0 && hb < INF_BITS;
@@ -1664,6 +1670,19 @@ __global__ void k_dft_deinterleave(const double2* __restrict__ B, long ldb, int 
   }
 }
 
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+// The 4-point DFT with w_4 = -i: y0 = t0 + t2, y2 = t0 - t2, y1 = t1 - i t3, y3 = t1 + i t3 for
+// t0 = x0 + x2, t1 = x0 - x2, t2 = x1 + x3, t3 = x1 - x3.
+__device__ __forceinline__ void dft4(double2 x0, double2 x1, double2 x2, double2 x3, double2& y0, double2& y1,
+                                     double2& y2, double2& y3) {
+  const double2 t0 = cadd(x0, x2), t1 = csub(x0, x2), t2 = cadd(x1, x3), t3 = csub(x1, x3);
+  y0 = cadd(t0, t2);
+  y2 = csub(t0, t2);
+  y1 = make_double2(t1.x + t3.y, t1.y - t3.x);
+  y3 = make_double2(t1.x - t3.y, t1.y + t3.x);
+}
+
 // C(j' + nq s, c) = sum_r w_R^(s r) X_r + beta C, X_r = w_n^(j' r) P(j', r k + c) (P already
 // carries alpha).  One thread per (j', c), j' fastest: coalesced reads of P and writes of C.
 template <int R>
@@ -1684,18 +1703,25 @@ __global__ void k_dft_radix_combine(const double2* __restrict__ P, int nq, int k
       }
       double2 Y[R];
       if (R == 2) {
-        Y[0] = make_double2(X[0].x + X[1].x, X[0].y + X[1].y);
-        Y[1] = make_double2(X[0].x - X[1].x, X[0].y - X[1].y);
+        Y[0] = cadd(X[0], X[1]);
+        Y[1] = csub(X[0], X[1]);
+      } else if (R == 4) {
+        dft4(X[0], X[1 % R], X[2 % R], X[3 % R], Y[0], Y[1 % R], Y[2 % R], Y[3 % R]);
       } else {
-        // w_4 = -i: Y0 = t0 + t2, Y2 = t0 - t2, Y1 = t1 - i t3, Y3 = t1 + i t3
-        const double2 t0 = make_double2(X[0].x + X[2 % R].x, X[0].y + X[2 % R].y);
-        const double2 t1 = make_double2(X[0].x - X[2 % R].x, X[0].y - X[2 % R].y);
-        const double2 t2 = make_double2(X[1].x + X[3 % R].x, X[1].y + X[3 % R].y);
-        const double2 t3 = make_double2(X[1].x - X[3 % R].x, X[1].y - X[3 % R].y);
-        Y[0] = make_double2(t0.x + t2.x, t0.y + t2.y);
-        Y[2 % R] = make_double2(t0.x - t2.x, t0.y - t2.y);
-        Y[1] = make_double2(t1.x + t3.y, t1.y - t3.x);
-        Y[3 % R] = make_double2(t1.x - t3.y, t1.y + t3.x);
+        // w_8 = (1 - i)/sqrt(2): a_r = X_r + X_(r+4) and b_r = w_8^r (X_r - X_(r+4)) give the
+        // even outputs Y_2t = DFT4(a)_t and the odd ones Y_(2t+1) = DFT4(b)_t
+        double2 a[4], b[4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          a[r] = cadd(X[r % R], X[(r + 4) % R]);
+          b[r] = csub(X[r % R], X[(r + 4) % R]);
+        }
+        const double h = 0.70710678118654752440;  // 1/sqrt(2)
+        b[1] = make_double2(h * (b[1].x + b[1].y), h * (b[1].y - b[1].x));   // * (1 - i)/sqrt(2)
+        b[2] = make_double2(b[2].y, -b[2].x);                                // * -i
+        b[3] = make_double2(h * (b[3].y - b[3].x), -h * (b[3].x + b[3].y));  // * (-1 - i)/sqrt(2)
+        dft4(a[0], a[1], a[2], a[3], Y[0], Y[2 % R], Y[4 % R], Y[6 % R]);
+        dft4(b[0], b[1], b[2], b[3], Y[1 % R], Y[3 % R], Y[5 % R], Y[7 % R]);
       }
       double2* out = C + (long)c * ldc + j;
 #pragma unroll
@@ -1741,7 +1767,7 @@ static int split_core(int M, int N, int K, double alpha, const double* A, long l
                       unsigned* status_dev_out) {
   if (gs.kind == KIND_DFT) return PSMMA_EUNSUPPORTED;  // split_core_dft3
   if (nmod < 8 || nmod > SPL_MAX_MODULI) return PSMMA_EUNSUPPORTED;
-  if (K >= (1 << 24) || M >= (1 << 30) || N >= (1 << 30)) return PSMMA_EUNSUPPORTED;
+  if (K >= (1 << 24) || M > kSplitMaxRows || N >= (1 << 30)) return PSMMA_EUNSUPPORTED;
   SplitLayout L = split_layout(M, K, N, nmod);
   if (lwork < L.total || !work) return PSMMA_EWORKSPACE;
   char* w = (char*)work;
@@ -1772,7 +1798,7 @@ static int split_core(int M, int N, int K, double alpha, const double* A, long l
   prof_mark(stream, "params");
   k_residues_A<<<dim3(L.kp / 64, (M + 63) / 64), 256, 0, stream>>>(A, lda, M, K, L.kp, b.amax, b.prm, cc, b.RA);
   prof_mark(stream, "residues_A");
-  k_residues_H<<<dim3(rh_blocks_x(L.kp), N), 128, 0, stream>>>(b.Ht, N, L.kp, b.hmax, b.prm, cc, b.RH);
+  k_residues_H<<<dim3(N, rh_blocks_x(L.kp)), 128, 0, stream>>>(b.Ht, N, L.kp, b.hmax, b.prm, cc, b.RH);
   prof_mark(stream, "residues_H");
 
   OneGemm og;
@@ -1790,8 +1816,7 @@ static int split_core(int M, int N, int K, double alpha, const double* A, long l
   ga.status = &b.prm->status;
   for (int l = 0; l < nmod; ++l) { ga.m[l] = cc.m[l]; ga.inv_m[l] = cc.inv_m[l]; }
   using Shape = GemmShape<G_BN>;
-  if (cudaFuncSetAttribute(k_crt_gemm<G_BN, OneGemm>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)Shape::SMEM) != cudaSuccess)
+  if (set_smem_attr(k_crt_gemm<G_BN, OneGemm>, (int)Shape::SMEM) != cudaSuccess)
     return PSMMA_EDEVICE;
   int dev = 0, sms = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
@@ -1834,7 +1859,7 @@ static int split_core_host(int M, int N, int K, double alpha, const double* A_h,
                            int ph_guess, int* pa_out, int* ph_out) {
   if (gs.kind == KIND_DFT) return PSMMA_EUNSUPPORTED;
   if (nmod < 8 || nmod > SPL_MAX_MODULI) return PSMMA_EUNSUPPORTED;
-  if (K >= (1 << 24) || M >= (1 << 30) || N >= (1 << 30)) return PSMMA_EUNSUPPORTED;
+  if (K >= (1 << 24) || M > kSplitMaxRows || N >= (1 << 30)) return PSMMA_EUNSUPPORTED;
   // A column chunks; GEMM / CRT / download row panels: eighths of the row tiles, the first
   // one cut to two row tiles (its pitched upload runs beside the H passes' HBM traffic and
   // gates the first product) and the last one halved three times (8 + 4 + 2 + 2 of 16 tiles:
@@ -1866,7 +1891,7 @@ static int split_core_host(int M, int N, int K, double alpha, const double* A_h,
     case KIND_CAUCHY_EIG: k_h_pass1<KIND_CAUCHY_EIG><<<N, 256, 0, s>>>(gs, K, L.kp, b.Ht, b.hmax, b.hsum, b.hsq, b.prm); break;
     default: return PSMMA_EUNSUPPORTED;
   }
-  const dim3 grh(rh_blocks_x(L.kp), N);
+  const dim3 grh(N, rh_blocks_x(L.kp));
   if (ph_guess >= 8)
     k_residues_H_spec<<<grh, 128, 0, s>>>(b.Ht, N, L.kp, b.hmax, b.prm, cc, b.RH, ph_guess, 0);
   prof_mark(s, "h_side");
@@ -1886,8 +1911,7 @@ static int split_core_host(int M, int N, int K, double alpha, const double* A_h,
   ga.nmod = nmod;
   for (int l = 0; l < nmod; ++l) { ga.m[l] = cc.m[l]; ga.inv_m[l] = cc.inv_m[l]; }
   using Shape = GemmShape<G_BN>;
-  if (cudaFuncSetAttribute(k_crt_gemm<G_BN, OneGemm>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)Shape::SMEM) != cudaSuccess)
+  if (set_smem_attr(k_crt_gemm<G_BN, OneGemm>, (int)Shape::SMEM) != cudaSuccess)
     return PSMMA_EDEVICE;
   int dev = 0, sms = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
@@ -2081,7 +2105,7 @@ int launch_split_host_general(int M, int N, int K, double alpha, const double* A
 static int dft3_enqueue(int M, int nn, double alpha, const double* B, long ldb, double beta, double* C, long ldc,
                         int nmod, void* work, size_t lwork, cudaStream_t stream, SplitDevParams** prm_out) {
   if (nmod < 8 || nmod > SPL_MAX_MODULI) return PSMMA_EUNSUPPORTED;
-  if (2 * nn >= (1 << 24) || M >= (1 << 30)) return PSMMA_EUNSUPPORTED;
+  if (2 * nn >= (1 << 24) || M > kSplitMaxRows) return PSMMA_EUNSUPPORTED;
   const SplitLayout L = dft3_layout(M, nn, nmod);
   if (lwork < L.total || !work) return PSMMA_EWORKSPACE;
   char* w = (char*)work;
@@ -2099,15 +2123,14 @@ static int dft3_enqueue(int M, int nn, double alpha, const double* B, long ldb, 
   // the bounds are those of the real embedding: n columns, inner dimension 2n
   k_split_params<<<PARAMS_BLOCKS, 512, 0, stream>>>(b.prm, cc.log2M, M, nn, 2 * nn, b.amax, b.asq, b.hmax, b.hsq);
   prof_mark(stream, "params");
-  k_residues_A_dft3<<<dim3((L.kp / 2 + 127) / 128, M), 128, 0, stream>>>(B, 2 * ldb, nn, L.kp, b.amax, b.prm, cc,
+  k_residues_A_dft3<<<dim3(M, (L.kp / 2 + 127) / 128), 128, 0, stream>>>(B, 2 * ldb, nn, L.kp, b.amax, b.prm, cc,
                                                                          b.RA, M);
   prof_mark(stream, "residues_A");
-  k_residues_H_dft3<<<dim3(rh_blocks_x(L.kp), nn), 128, 0, stream>>>(b.Ht, nn, L.kp, b.hmax, b.prm, cc, b.RH);
+  k_residues_H_dft3<<<dim3(nn, rh_blocks_x(L.kp)), 128, 0, stream>>>(b.Ht, nn, L.kp, b.hmax, b.prm, cc, b.RH);
   prof_mark(stream, "residues_H");
 
   using Shape = GemmShape<G_BN>;
-  if (cudaFuncSetAttribute(k_crt_gemm<G_BN, OneGemm>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)Shape::SMEM) != cudaSuccess)
+  if (set_smem_attr(k_crt_gemm<G_BN, OneGemm>, (int)Shape::SMEM) != cudaSuccess)
     return PSMMA_EDEVICE;
   int dev = 0, sms = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
@@ -2160,7 +2183,7 @@ static int split_core_dft3(int k, int n, double alpha, const double* B, long ldb
   if (R == 1) {
     st = dft3_enqueue(k, n, alpha, B, ldb, beta, C, ldc, nmod, work, lwork, stream, &prm);
   } else {
-    if ((size_t)k * R >= (1u << 30)) return PSMMA_EUNSUPPORTED;
+    if ((long)k * R > kSplitMaxRows) return PSMMA_EUNSUPPORTED;
     const DftRadixLayout D = dft_radix_layout(n, k, R, nmod);
     if (!work || lwork < D.total) return PSMMA_EWORKSPACE;
     char* w = (char*)work;
@@ -2176,7 +2199,9 @@ static int split_core_dft3(int k, int n, double alpha, const double* B, long ldb
                       &prm);
     if (st) return st;
     const dim3 gc((nq + 255) / 256 < 64 ? (nq + 255) / 256 : 64, k < 65535 ? k : 65535);
-    if (R == 4)
+    if (R == 8)
+      k_dft_radix_combine<8><<<gc, 256, 0, stream>>>(P, nq, k, wn, beta, (double2*)C, ldc);
+    else if (R == 4)
       k_dft_radix_combine<4><<<gc, 256, 0, stream>>>(P, nq, k, wn, beta, (double2*)C, ldc);
     else
       k_dft_radix_combine<2><<<gc, 256, 0, stream>>>(P, nq, k, wn, beta, (double2*)C, ldc);
@@ -2483,8 +2508,7 @@ static int launch_group_gemm(const SplitGroup& g, int cls, const CrtConsts& cc, 
   ts.d = (const GemmDesc*)g.d_gemm[cls];
   ts.count = g.n_gemm[cls];
   ts.total_tiles = g.tiles[cls];
-  if (cudaFuncSetAttribute(k_crt_gemm<BN, GroupGemm>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)Shape::SMEM) != cudaSuccess)
+  if (set_smem_attr(k_crt_gemm<BN, GroupGemm>, (int)Shape::SMEM) != cudaSuccess)
     return PSMMA_EDEVICE;
   k_crt_gemm<BN, GroupGemm><<<std::min(sms, ts.total_tiles), G_THREADS, Shape::SMEM, stream>>>(ts);
   return PSMMA_OK;

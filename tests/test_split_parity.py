@@ -218,16 +218,16 @@ def test_split_dft_padded_leading_dimensions(n, k, pad, cuda):
     assert np.all(got[n:] == 7.0 + 7.0j)  # rows past n untouched
 
 
-@pytest.mark.parametrize("n,k,pad,beta", [(4100, 77, 3, -0.5), (8192, 300, 5, 0.0), (8192, 129, 0, 1.5),
-                                         (12288, 64, 1, 0.25)])
+@pytest.mark.parametrize("n,k,pad,beta", [(2050, 33, 2, 1.0), (4100, 77, 3, -0.5), (8192, 300, 5, 0.0),
+                                         (8192, 129, 0, 1.5), (12288, 64, 1, 0.25)])
 def test_split_dft_radix_steps_match_fft(n, k, pad, beta, cuda):
-    # n / 2 >= 2048 (radix 2: n = 4100) and n / 4 >= 2048 (radix 4): the modular products run on
-    # F_(n/R) and R k columns, the twiddles and butterflies afterwards; padded leading
-    # dimensions, beta on and off, rows past n untouched
+    # radix 2 (n = 2050: n / 2 = 1025), 4 (n = 4100: n / 4 = 1025, odd) and 8 (n = 8192, 12288):
+    # the modular products run on F_(n/R) and R k columns, the twiddles and butterflies
+    # afterwards; padded leading dimensions, beta on and off, rows past n untouched
     import psmma_git_gb300 as P
     import torch
-    assert [P.load().psmma_split_dft_radix(m) for m in (n, 4094, 4096, 8190, 0)] == \
-        [2 if n == 4100 else 4, 1, 2, 2, 0]
+    radix = {2050: 2, 4100: 4, 8192: 8, 12288: 8}[n]
+    assert [P.load().psmma_split_dft_radix(m) for m in (n, 2046, 4094, 4096, 8190, 0)] == [radix, 1, 2, 4, 2, 0]
     B = O.cfg_matrix(n, k, seed=n + 21, complex_=True)
     C0 = O.cfg_matrix(n, k, seed=k + 22, complex_=True)
     Bbig = np.zeros((n + pad, k), np.complex128)
@@ -243,6 +243,27 @@ def test_split_dft_radix_steps_match_fft(n, k, pad, beta, cuda):
     assert O.rel_fro(got[:n], ref) < TOL
     assert O.col_max_rel(got[:n], ref) < TOL
     assert np.all(got[n:] == 7.0 + 7.0j)
+
+
+def test_split_dft_radix_rows_past_the_grid_y_limit(cuda):
+    # n = k = 8192 at radix 8: the modular products have R k = 65536 rows, one more than a grid's
+    # y dimension holds, so the row-indexed passes must index rows along x
+    import psmma_git_gb300 as P
+    import torch
+    n = k = 8192
+    g = torch.Generator(device=cuda)
+    g.manual_seed(8192)
+    X = P.fortran_empty(n, k, torch.complex128, cuda)
+    X.copy_(torch.complex(torch.rand(k, n, generator=g, device=cuda, dtype=torch.float64) * 2 - 1,
+                          torch.rand(k, n, generator=g, device=cuda, dtype=torch.float64) * 2 - 1).t())
+    Y = P.fortran_empty(n, k, torch.complex128, cuda)
+    P.pzmdftl(n, k, 1.0, X, 0.0, Y, precision="split")
+    torch.cuda.synchronize()
+    cols = torch.tensor([0, 1, 4095, 8191], device=cuda)
+    ref = np.fft.fft(X[:, cols].cpu().numpy(), axis=0)
+    assert O.rel_fro(Y[:, cols].cpu().numpy(), ref) < TOL
+    del X, Y
+    torch.cuda.empty_cache()
 
 
 def test_split_dft_ones_fixture(cuda):
