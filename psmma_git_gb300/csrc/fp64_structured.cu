@@ -438,6 +438,58 @@ int launch_dft_table(double2* w, int n, cudaStream_t stream) {
 }
 
 
+// ---- the DFT on the FP64 path ---------------------------------------------------------------
+// C (n x k complex) = alpha F_n B + beta C as the real GEMM C' = F' B' of the embedding, F'
+// generated tile by tile from the table w^t.  With R = dft_radix_for(n) > 1 (the split path's
+// rule) the embedding is F_(n/R)'s, applied to the R k columns B(r::R, :), and the twiddles and
+// R-point butterflies follow in one pass: n^2 k / R complex multiply-adds instead of n^2 k.
+// Workspace: the n-entry table (plain); B' and P (n x k complex each) and the tables of n and
+// n / R entries (radix).
+size_t dft_f64_workspace(int n, int k) {
+  if (n <= 0 || k <= 0) return 0;
+  const size_t a = 256;
+  auto al = [&](size_t x) { return (x + a - 1) / a * a; };
+  const int R = dft_radix_for(n);
+  if (R == 1) return al((size_t)n * 16);
+  return 2 * al((size_t)n * k * 16) + al((size_t)n * 16) + al((size_t)(n / R) * 16);
+}
+
+int launch_dft_f64(int n, int k, double alpha, const double* B, long ldb, double beta, double* C, long ldc,
+                   void* work, size_t lwork, cudaStream_t stream) {
+  if (n <= 0 || k <= 0) return PSMMA_OK;
+  if (lwork < dft_f64_workspace(n, k) || !work) return PSMMA_EWORKSPACE;
+  const int R = dft_radix_for(n);
+  auto al = [](size_t x) { return (x + 255) / 256 * 256; };
+  char* w = (char*)work;
+  GenSpec gs;
+  gs.kind = KIND_DFT;
+  if (R == 1) {
+    double2* wtab = (double2*)w;
+    int st = launch_dft_table(wtab, n, stream);
+    if (st) return st;
+    gs.n_dft = n;
+    gs.wtab = wtab;
+    // real view: C'(2n x k) = F'(2n x 2n) * B'(2n x k), leading dimensions doubled
+    return launch_struct_f64(2 * n, k, 2 * n, alpha, B, 2 * ldb, gs, beta, C, 2 * ldc, stream);
+  }
+  const int nq = n / R;
+  if ((long)R * k > 65535L * F64_BN) return PSMMA_EUNSUPPORTED;  // the kernel's grid y covers R k columns
+  double2* Bp = (double2*)w;
+  double2* P = (double2*)(w + al((size_t)n * k * 16));
+  double2* wn = (double2*)(w + 2 * al((size_t)n * k * 16));
+  double2* wq = (double2*)((char*)wn + al((size_t)n * 16));
+  int st = launch_dft_deinterleave((const double2*)B, ldb, n, k, R, Bp, stream);
+  if (!st) st = launch_dft_table(wq, nq, stream);
+  if (!st) st = launch_dft_table(wn, n, stream);
+  if (st) return st;
+  gs.n_dft = nq;
+  gs.wtab = wq;
+  st = launch_struct_f64(2 * nq, R * k, 2 * nq, alpha, (const double*)Bp, 2L * nq, gs, 0.0, (double*)P, 2L * nq,
+                         stream);
+  if (st) return st;
+  return launch_dft_radix_combine(P, nq, k, wn, beta, (double2*)C, ldc, R, stream);
+}
+
 size_t f64_group_bytes(int count) {
   if (count <= 0) return 0;
   return ((sizeof(F64Args) * count + 255) & ~(size_t)255) + sizeof(int) * count + 512;

@@ -240,25 +240,20 @@ int run_dft(int n, int k, double alpha, const psmma_complex* B, int ldb, double 
     return launch_split_any(KIND_DFT, n, k, alpha, (const double*)B, ldb, nullptr, 0, beta, (double*)C, ldc,
                             o->n_moduli, work, need, s, nullptr);
   }
-  double2* wtab = nullptr;
-  if (alpha != 0.0) {
-    size_t need = (size_t)n * sizeof(double2);
-    if (o->work) {
-      if (o->lwork < need) return PSMMA_EWORKSPACE;
-      wtab = (double2*)o->work;
-    } else {
-      wtab = (double2*)pool_get(need, s, &st);
-      if (st) return st;
-    }
-    st = launch_dft_table(wtab, n, s);
+  if (alpha == 0.0) {  // C := beta C (B not read)
+    GenSpec gs;
+    gs.kind = KIND_DFT;
+    return launch_struct_f64(2 * n, k, 2 * n, 0.0, nullptr, 2L * ldb, gs, beta, (double*)C, 2L * ldc, s);
+  }
+  const size_t need = dft_f64_workspace(n, k);
+  void* work = o->work;
+  if (work) {
+    if (o->lwork < need) return PSMMA_EWORKSPACE;
+  } else {
+    work = pool_get(need, s, &st);
     if (st) return st;
   }
-  // Real view: C'(2n x k) = F'(2n x 2n) * B'(2n x k), ld doubled.
-  GenSpec gs;
-  gs.kind = KIND_DFT;
-  gs.n_dft = n;
-  gs.wtab = wtab;
-  return launch_struct_f64(2 * n, k, 2 * n, alpha, (const double*)B, 2L * ldb, gs, beta, (double*)C, 2L * ldc, s);
+  return launch_dft_f64(n, k, alpha, (const double*)B, ldb, beta, (double*)C, ldc, work, need, s);
 }
 
 // ---- host-pointer wrappers -------------------------------------------------------------
@@ -644,7 +639,7 @@ size_t psmma_workspace_size(int kind, int n, int k, const psmma_opts* opts) {
     return o->precision == PSMMA_PREC_SPLIT ? split_workspace_general(n, k, k, o->n_moduli)
                                             : f64_splitk_bytes(n, k, k, std::max(1, device_sms()));
   if (o->precision == PSMMA_PREC_SPLIT) return split_workspace_bytes(kind, n, k, o->n_moduli);
-  if (kind == KIND_DFT) return align256((size_t)n * sizeof(double2));
+  if (kind == KIND_DFT) return dft_f64_workspace(n, k);
   return f64_splitk_bytes(n, k, k, std::max(1, device_sms()));
 }
 

@@ -108,6 +108,18 @@ int launch_struct_f64_ws(int M, int N, int K, double alpha, const double* X, lon
                          double beta, double* C, long ldc, void* work, size_t lwork, cudaStream_t stream);
 size_t f64_splitk_bytes(int M, int N, int K, int sms);
 int launch_dft_table(double2* w, int n, cudaStream_t stream);
+// C (n x k complex, ldc) = alpha F_n B + beta C on the FP64 path (plain embedding, or the
+// radix-R first step of dft_radix_for(n)); workspace dft_f64_workspace(n, k) bytes.
+size_t dft_f64_workspace(int n, int k);
+int launch_dft_f64(int n, int k, double alpha, const double* B, long ldb, double beta, double* C, long ldc,
+                   void* work, size_t lwork, cudaStream_t stream);
+// The DFT's radix step (split_crt.cu): the radix for size n (1, 2, 4 or 8); B' (n/R x R k
+// complex) = [B(0::R,:) | ... | B(R-1::R,:)]; C(j + (n/R) s, c) = sum_r w_R^(s r) w_n^(j r)
+// P(j, r k + c) + beta C.
+int dft_radix_for(int n);
+int launch_dft_deinterleave(const double2* B, long ldb, int n, int k, int R, double2* Bp, cudaStream_t stream);
+int launch_dft_radix_combine(const double2* P, int nq, int k, const double2* wn, double beta, double2* C, long ldc,
+                             int R, cudaStream_t stream);
 
 // Argument checks of PSCAUCHY_COMPUTE / PSTOEPLITZ_COMPUTE / PSHANKEL_COMPUTE on a 1x1 grid
 // (psmma_capi.cu): 0 = run, 1 = quick return (nothing to do), else the status to return.

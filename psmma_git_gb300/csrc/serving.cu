@@ -130,7 +130,7 @@ size_t request_workspace(const psmma_request& r) {
   if (r.kind == KIND_CAUCHY_EIG)
     return r.precision == PSMMA_PREC_SPLIT ? split_workspace_general(r.n, r.k, r.k, r.n_moduli) : 0;
   if (r.precision == PSMMA_PREC_SPLIT) return split_workspace_bytes(r.kind, r.n, r.k, r.n_moduli);
-  if (r.kind == KIND_DFT) return (size_t)r.n * sizeof(double2);
+  if (r.kind == KIND_DFT) return dft_f64_workspace(r.n, r.k);
   return 0;
 }
 
@@ -173,16 +173,14 @@ int launch_job(psmma_server* s, Job& j) {
     return launch_split_any(r.kind, r.n, r.k, r.alpha, (const double*)r.A, r.lda, r.gen, r.ldgen, r.beta,
                             (double*)r.Q, r.ldq, r.n_moduli, work, j.work_bytes, st, status);
   if (r.kind == KIND_DFT) {
-    if (r.alpha != 0.0) {
-      int e = launch_dft_table((double2*)work, r.n, st);
-      if (e) return e;
+    if (r.alpha == 0.0) {
+      GenSpec gs;
+      gs.kind = KIND_DFT;
+      return launch_struct_f64(2 * r.n, r.k, 2 * r.n, 0.0, nullptr, 2L * r.lda, gs, r.beta, (double*)r.Q, 2L * r.ldq,
+                               st);
     }
-    GenSpec gs;
-    gs.kind = KIND_DFT;
-    gs.n_dft = r.n;
-    gs.wtab = (const double2*)work;
-    return launch_struct_f64(2 * r.n, r.k, 2 * r.n, r.alpha, (const double*)r.A, 2L * r.lda, gs, r.beta,
-                             (double*)r.Q, 2L * r.ldq, st);
+    return launch_dft_f64(r.n, r.k, r.alpha, (const double*)r.A, r.lda, r.beta, (double*)r.Q, r.ldq, work,
+                          j.work_bytes, st);
   }
   return launch_struct_f64(r.n, r.k, r.k, r.alpha, (const double*)r.A, r.lda,
                            reference_gens(r.kind, r.gen, r.ldgen, r.k), r.beta, (double*)r.Q, r.ldq, st);

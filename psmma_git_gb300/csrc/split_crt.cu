@@ -238,6 +238,8 @@ size_t split_workspace_bytes(int kind, int n, int k, int n_moduli) {
 
 extern "C" int psmma_split_dft_radix(int n) { return n > 0 ? dft_radix(n) : 0; }
 
+int dft_radix_for(int n) { return n > 0 ? dft_radix(n) : 1; }
+
 size_t split_workspace_general(int M, int N, int K, int n_moduli) {
   if (M <= 0 || N <= 0 || K <= 0) return 0;
   return split_layout(M, K, N, resolve_nmod(n_moduli)).total;
@@ -1737,6 +1739,26 @@ __global__ void k_dft_radix_combine(const double2* __restrict__ P, int nq, int k
   }
 }
 
+int launch_dft_deinterleave(const double2* B, long ldb, int n, int k, int R, double2* Bp, cudaStream_t stream) {
+  const dim3 gd((n + 255) / 256 < 64 ? (n + 255) / 256 : 64, k < 65535 ? k : 65535);
+  k_dft_deinterleave<<<gd, 256, 0, stream>>>(B, ldb, n, k, R, Bp);
+  return cudaGetLastError() == cudaSuccess ? PSMMA_OK : PSMMA_EDEVICE;
+}
+
+int launch_dft_radix_combine(const double2* P, int nq, int k, const double2* wn, double beta, double2* C, long ldc,
+                             int R, cudaStream_t stream) {
+  const dim3 gc((nq + 255) / 256 < 64 ? (nq + 255) / 256 : 64, k < 65535 ? k : 65535);
+  if (R == 8)
+    k_dft_radix_combine<8><<<gc, 256, 0, stream>>>(P, nq, k, wn, beta, C, ldc);
+  else if (R == 4)
+    k_dft_radix_combine<4><<<gc, 256, 0, stream>>>(P, nq, k, wn, beta, C, ldc);
+  else if (R == 2)
+    k_dft_radix_combine<2><<<gc, 256, 0, stream>>>(P, nq, k, wn, beta, C, ldc);
+  else
+    return PSMMA_EUNSUPPORTED;
+  return cudaGetLastError() == cudaSuccess ? PSMMA_OK : PSMMA_EDEVICE;
+}
+
 static int split_status(SplitDevParams* prm, cudaStream_t stream, unsigned* status_dev_out) {
   if (status_dev_out && status_dev_out != kStatusWait) {
     if (cudaMemcpyAsync(status_dev_out, &prm->status, sizeof(unsigned), cudaMemcpyDeviceToDevice, stream) !=
@@ -2191,22 +2213,16 @@ static int split_core_dft3(int k, int n, double alpha, const double* B, long ldb
     double2* P = (double2*)(w + D.off_p);
     double2* wn = (double2*)(w + D.off_w);
     const int nq = n / R;
-    const dim3 gd((n + 255) / 256 < 64 ? (n + 255) / 256 : 64, k < 65535 ? k : 65535);
-    k_dft_deinterleave<<<gd, 256, 0, stream>>>((const double2*)B, ldb, n, k, R, Bp);
+    st = launch_dft_deinterleave((const double2*)B, ldb, n, k, R, Bp, stream);
+    if (st) return st;
     st = launch_dft_table(wn, n, stream);
     if (st) return st;
     st = dft3_enqueue(R * k, nq, alpha, (const double*)Bp, nq, 0.0, (double*)P, nq, nmod, work, D.core, stream,
                       &prm);
     if (st) return st;
-    const dim3 gc((nq + 255) / 256 < 64 ? (nq + 255) / 256 : 64, k < 65535 ? k : 65535);
-    if (R == 8)
-      k_dft_radix_combine<8><<<gc, 256, 0, stream>>>(P, nq, k, wn, beta, (double2*)C, ldc);
-    else if (R == 4)
-      k_dft_radix_combine<4><<<gc, 256, 0, stream>>>(P, nq, k, wn, beta, (double2*)C, ldc);
-    else
-      k_dft_radix_combine<2><<<gc, 256, 0, stream>>>(P, nq, k, wn, beta, (double2*)C, ldc);
+    st = launch_dft_radix_combine(P, nq, k, wn, beta, (double2*)C, ldc, R, stream);
+    if (st) return st;
     prof_mark(stream, "radix_combine");
-    if (cudaGetLastError() != cudaSuccess) return PSMMA_EDEVICE;
   }
   if (st) return st;
   return split_status(prm, stream, status_dev_out);

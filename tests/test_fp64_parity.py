@@ -124,6 +124,27 @@ def test_dft_matches_fft(n, k, cuda):
     assert O.rel_fro(got, ref) < TOL
 
 
+@pytest.mark.parametrize("n,k,pad,beta", [(2050, 33, 2, -2.0), (4100, 17, 0, 0.0), (8192, 40, 3, 0.5)])
+def test_dft_radix_steps_match_fft(n, k, pad, beta, cuda):
+    # the FP64 path takes the split path's radix step (2, 4, 8 at these n): F_(n/R) on R k
+    # columns, then the twiddles and butterflies; padded leading dimensions, rows past n untouched
+    import psmma_git_gb300 as P
+    import torch
+    B = O.cfg_matrix(n, k, seed=n + 5, complex_=True)
+    C0 = O.cfg_matrix(n, k, seed=k + 6, complex_=True)
+    Bbig = np.zeros((n + pad, k), np.complex128)
+    Bbig[:n] = B
+    Cbig = np.full((n + pad, k), 3.0 - 1.0j)
+    Cbig[:n] = C0
+    dB = _t(Bbig, cuda)[:n]
+    dC = _t(Cbig, cuda)
+    P.pzmdftl(n, k, 0.5, dB, beta, dC[:n])
+    torch.cuda.synchronize()
+    got = _np(dC)
+    assert O.rel_fro(got[:n], O.dft_product(0.5, B, beta, C0)) < TOL
+    assert np.all(got[n:] == 3.0 - 1.0j)
+
+
 def test_dft_ones_fixture_and_variant(cuda):
     z = np.load(GOLDEN / "dft_ones_kat.npz")
     n = int(z["n"])
