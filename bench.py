@@ -741,7 +741,10 @@ def run_cfg1(args, ws, rank, local, compact=False):
             fn = P.psmma_toeplitz if kind == "toeplitz" else P.psmma_hankel
             run = lambda prec, dst, fn=fn: fn(n, k, 1.0, A, gv, 0.0, dst, precision=prec, n_moduli=nmod)  # noqa: E731
             flops = 2.0 * n ** 3
-            gemm_flops = 2.0 * nmod * n * k * kp
+            # the block step (automatic levels L): 3^L modular products of width w = k / 2^L
+            levels = P.load().psmma_split_block_levels(1 if kind == "toeplitz" else 2, n, k)
+            w = k >> levels
+            gemm_flops = 2.0 * nmod * n * w * ((w + 63) // 64 * 64) * 3 ** levels
         for _ in range(args.warmup):
             run("split", Y)
         torch.cuda.synchronize()
@@ -843,6 +846,9 @@ def run_cfg1(args, ws, rank, local, compact=False):
                      "cpu_baseline": cpu, "split_phases_ms": phases}
         if col_err is not None:
             out[kind]["col_max_rel_err_vs_oracle_sample"] = col_err
+        if kind in ("toeplitz", "hankel"):
+            out[kind]["block_levels"] = levels
+            out[kind]["executed_tflops"] = flops * 0.75 ** levels / t / 1e9
         if kind == "dft":
             out[kind]["split_complex_mac_tflops"] = 2.0 * n ** 3 / t / 1e9
             out[kind]["radix"] = R

@@ -69,7 +69,10 @@ typedef struct psmma_opts {
   int    n_moduli;    /* split path: number of moduli, 0 = default (14); 8..16                 */
   void*  work;        /* optional caller-owned device workspace (NULL: library-owned pool)      */
   size_t lwork;       /* size of `work` in bytes                                               */
-  int    reserved[8]; /* must be zero                                                          */
+  int    block_levels; /* split path, Toeplitz / Hankel: levels of the block step (see
+                          psmma_split_block_levels): 0 = automatic, -1 = none (one product),
+                          1..3 = that many (fewer where k is not divisible by 64 * 2^L)       */
+  int    reserved[7]; /* must be zero                                                          */
 } psmma_opts;
 
 /* Interleaved complex double, layout-compatible with cuDoubleComplex and COMPLEX*16. */
@@ -139,6 +142,22 @@ int pzmdftl1(int n, int k, double alpha, const psmma_complex* B, int ldb,
  * partial transforms with the twiddles w^(j r) and R-point butterflies in FP64; R is the
  * largest of 8, 4, 2 that divides n with n / R >= 1024, else 1.  0 for n <= 0. */
 int psmma_split_dft_radix(int n);
+
+/* No counterpart in the reference.  The levels L (0 to 3) of the block step that
+ * psmma_toeplitz / psmma_hankel take on the split path (kind PSMMA_KIND_TOEPLITZ or
+ * PSMMA_KIND_HANKEL; 0 for the other kinds): H (k x k) is cut into 2 x 2 blocks, and the
+ * structure (Toeplitz: Y11 = Y00; Hankel: Y10 = Y01) turns the four block products into three,
+ * (X1 + X2) Y00, X2 (Y10 - Y00) and X1 (Y01 - Y00) for Toeplitz; L levels give 3^L products of
+ * width w = k / 2^L, (3/4)^L of the modular GEMM work, in exact modular arithmetic.  Columns j
+ * and j + c w share one scaling exponent.  This returns the automatic choice
+ * (opts->block_levels = 0): the largest L up to 2 with k divisible by 64 * 2^L and w >= 4096
+ * (smaller leaves make the modular GEMMs' per-tile epilogue outweigh their MMAs).  The
+ * device-pointer calls and the server take the step; the host-pointer calls keep the single
+ * product.  On the device, without a synchronisation, the call takes the single product
+ * instead when an entry of H is not finite (NaN then appears in exactly the columns it does
+ * there) or when a nonzero column's maximum is more than 2^4 below the largest of its group
+ * j + c w (the shared exponent would cost that column's entries more than 4 bits). */
+int psmma_split_block_levels(int kind, int n, int k);
 
 /* No counterpart in the reference.  The split-path Cauchy multiply (same arguments and
  * result as psmma_cauchy with opts->precision = PSMMA_PREC_SPLIT) for callers that cannot

@@ -32,13 +32,15 @@ module psmma_gb300
   integer(c_int), parameter, public :: PSMMA_COMPRESS_RRQR = 0, PSMMA_COMPRESS_RRLU = 1
 
   ! psmma_opts: precision, moduli count of the split path (0 = default), optional caller
-  ! workspace (device address and bytes), reserved words that must stay zero
+  ! workspace (device address and bytes), Toeplitz / Hankel block levels of the split path
+  ! (0 = automatic, -1 = none), reserved words that must stay zero
   type, bind(c), public :: psmma_opts
      integer(c_int)    :: precision = PSMMA_PREC_FP64
      integer(c_int)    :: n_moduli = 0
      type(c_ptr)       :: work = c_null_ptr
      integer(c_size_t) :: lwork = 0
-     integer(c_int)    :: reserved(8) = 0
+     integer(c_int)    :: block_levels = 0
+     integer(c_int)    :: reserved(7) = 0
   end type psmma_opts
 
   ! one multiply of a merge level: A (n x n, lda), generators gen (ldgen), Q (ldq), device

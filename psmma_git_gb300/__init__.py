@@ -41,10 +41,11 @@ __all__ = [
 _PREC = {"fp64": PREC_FP64, "split": PREC_SPLIT, PREC_FP64: PREC_FP64, PREC_SPLIT: PREC_SPLIT}
 
 
-def make_opts(precision="fp64", n_moduli: int = 0, work=None, lwork: int = 0) -> PsmmaOpts:
+def make_opts(precision="fp64", n_moduli: int = 0, work=None, lwork: int = 0, block_levels: int = 0) -> PsmmaOpts:
     o = PsmmaOpts()
     o.precision = _PREC[precision]
     o.n_moduli = n_moduli
+    o.block_levels = block_levels
     if work is not None:
         o.work = C.c_void_p(work.data_ptr())
         o.lwork = lwork or work.numel() * work.element_size()
@@ -101,9 +102,9 @@ def _stream_ptr(stream):
     return C.c_void_p(stream.cuda_stream)
 
 
-def _real(kind: int, name: str, n, k, alpha, A, gen, beta, Q, precision, n_moduli, stream, work):
+def _real(kind: int, name: str, n, k, alpha, A, gen, beta, Q, precision, n_moduli, stream, work, block_levels=0):
     lib = load()
-    opts = make_opts(precision, n_moduli, work)
+    opts = make_opts(precision, n_moduli, work, block_levels=block_levels)
     if _is_torch(Q):
         import torch
         pa, lda = _dev(A, "A", torch.float64) if A is not None else (0, max(1, n))
@@ -133,14 +134,20 @@ def psmma_cauchy(n, k, alpha, A, gen, beta, Q, *, precision="fp64", n_moduli=0, 
     return _real(KIND_CAUCHY, "psmma_cauchy", n, k, alpha, A, gen, beta, Q, precision, n_moduli, stream, work)
 
 
-def psmma_toeplitz(n, k, alpha, A, gen, beta, Q, *, precision="fp64", n_moduli=0, stream=None, work=None):
-    """Q := alpha*A*H + beta*Q with H(i,j) = G(K+j-i) (1-based), len(G) = 2K-1."""
-    return _real(KIND_TOEPLITZ, "psmma_toeplitz", n, k, alpha, A, gen, beta, Q, precision, n_moduli, stream, work)
+def psmma_toeplitz(n, k, alpha, A, gen, beta, Q, *, precision="fp64", n_moduli=0, stream=None, work=None,
+                   block_levels=0):
+    """Q := alpha*A*H + beta*Q with H(i,j) = G(K+j-i) (1-based), len(G) = 2K-1.  block_levels:
+    the split path's block step (0 = automatic, -1 = none, 1..3 = that many levels)."""
+    return _real(KIND_TOEPLITZ, "psmma_toeplitz", n, k, alpha, A, gen, beta, Q, precision, n_moduli, stream, work,
+                 block_levels)
 
 
-def psmma_hankel(n, k, alpha, A, gen, beta, Q, *, precision="fp64", n_moduli=0, stream=None, work=None):
-    """Q := alpha*A*H + beta*Q with H(i,j) = G(i+j-1) (1-based), len(G) = 2K-1."""
-    return _real(KIND_HANKEL, "psmma_hankel", n, k, alpha, A, gen, beta, Q, precision, n_moduli, stream, work)
+def psmma_hankel(n, k, alpha, A, gen, beta, Q, *, precision="fp64", n_moduli=0, stream=None, work=None,
+                 block_levels=0):
+    """Q := alpha*A*H + beta*Q with H(i,j) = G(i+j-1) (1-based), len(G) = 2K-1.  block_levels as
+    for psmma_toeplitz."""
+    return _real(KIND_HANKEL, "psmma_hankel", n, k, alpha, A, gen, beta, Q, precision, n_moduli, stream, work,
+                 block_levels)
 
 
 def _dft(name: str, n, k, alpha, B, beta, Cm, stream, work, precision="fp64", n_moduli=0):
@@ -180,8 +187,8 @@ def stream_status(stream=None) -> None:
         raise PsmmaError(st, "psmma_stream_status")
 
 
-def workspace_size(kind: int, n: int, k: int, precision="fp64", n_moduli: int = 0) -> int:
-    opts = make_opts(precision, n_moduli)
+def workspace_size(kind: int, n: int, k: int, precision="fp64", n_moduli: int = 0, block_levels: int = 0) -> int:
+    opts = make_opts(precision, n_moduli, block_levels=block_levels)
     return int(load().psmma_workspace_size(kind, n, k, C.byref(opts)))
 
 

@@ -42,7 +42,8 @@ class PsmmaOpts(C.Structure):
         ("n_moduli", C.c_int),
         ("work", C.c_void_p),
         ("lwork", C.c_size_t),
-        ("reserved", C.c_int * 8),
+        ("block_levels", C.c_int),
+        ("reserved", C.c_int * 7),
     ]
 
 
@@ -121,6 +122,7 @@ SIGNATURES = {
     "psmma_stream_status": (_i, [_p]),
     "psmma_stream_release": (_i, [_p]),
     "psmma_split_dft_radix": (_i, [_i]),
+    "psmma_split_block_levels": (_i, [_i, _i, _i]),
     "psmma_status_string": (C.c_char_p, [_i]),
     "psmma_set_profiling": (None, [_i]),
     "psmma_profile_read": (_i, [C.POINTER(C.c_float), C.POINTER(C.c_char_p), _i]),

@@ -122,12 +122,13 @@ void prof_mark(cudaStream_t stream, const char* name) {
 
 namespace {
 
-const psmma_opts kDefaultOpts = {PSMMA_PREC_FP64, 0, nullptr, 0, {0, 0, 0, 0, 0, 0, 0, 0}};
+const psmma_opts kDefaultOpts = {PSMMA_PREC_FP64, 0, nullptr, 0, 0, {0, 0, 0, 0, 0, 0, 0}};
 
 int check_opts(const psmma_opts* o, int kind) {
   if (o->precision != PSMMA_PREC_FP64 && o->precision != PSMMA_PREC_SPLIT) return PSMMA_EUNSUPPORTED;
   if (o->n_moduli != 0 && (o->n_moduli < 8 || o->n_moduli > 16)) return PSMMA_EUNSUPPORTED;
-  for (int i = 0; i < 8; i++)
+  if (o->block_levels < -1 || o->block_levels > 3) return PSMMA_EUNSUPPORTED;
+  for (int i = 0; i < 7; i++)
     if (o->reserved[i] != 0) return PSMMA_EUNSUPPORTED;
   return PSMMA_OK;
 }
@@ -202,7 +203,7 @@ int run_real(int kind, int n, int k, double alpha, const double* A, int lda, con
   if (st) return st;
   cudaStream_t s = (cudaStream_t)stream;
   if (o->precision == PSMMA_PREC_SPLIT && alpha != 0.0) {
-    size_t need = split_workspace_bytes(kind, n, k, o->n_moduli);
+    size_t need = split_workspace_bytes(kind, n, k, o->n_moduli, o->block_levels);
     void* work = o->work;
     if (work) {
       if (o->lwork < need) return PSMMA_EWORKSPACE;
@@ -211,7 +212,7 @@ int run_real(int kind, int n, int k, double alpha, const double* A, int lda, con
       if (st) return st;
     }
     return launch_split(kind, n, k, alpha, A, lda, gen, ldgen, beta, Q, ldq, o->n_moduli, work,
-                        need, s);
+                        need, s, false, o->block_levels);
   }
   size_t wb = 0;
   void* w = f64_work(n, k, k, o, s, &wb, &st);
@@ -638,7 +639,7 @@ size_t psmma_workspace_size(int kind, int n, int k, const psmma_opts* opts) {
   if (kind == KIND_CAUCHY_EIG)
     return o->precision == PSMMA_PREC_SPLIT ? split_workspace_general(n, k, k, o->n_moduli)
                                             : f64_splitk_bytes(n, k, k, std::max(1, device_sms()));
-  if (o->precision == PSMMA_PREC_SPLIT) return split_workspace_bytes(kind, n, k, o->n_moduli);
+  if (o->precision == PSMMA_PREC_SPLIT) return split_workspace_bytes(kind, n, k, o->n_moduli, o->block_levels);
   if (kind == KIND_DFT) return dft_f64_workspace(n, k);
   return f64_splitk_bytes(n, k, k, std::max(1, device_sms()));
 }

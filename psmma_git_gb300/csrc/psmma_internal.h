@@ -127,12 +127,14 @@ int check_real_args(int kind, int n, int k, double alpha, const double* A, int l
                     int ldgen, double beta, const double* Q, int ldq);
 
 // Split path (split_crt.cu).
-size_t split_workspace_bytes(int kind, int n, int k, int n_moduli);
+// block_levels: psmma_opts::block_levels (Toeplitz / Hankel block step; 0 = automatic).
+size_t split_workspace_bytes(int kind, int n, int k, int n_moduli, int block_levels = 0);
 // wait_status: wait for the call and return its device status (for callers that must not
 // allocate); otherwise the status is ORed into the stream's status word (psmma_stream_status).
 int launch_split(int kind, int n, int k, double alpha, const double* A, long lda,
                  const double* gen, long ldgen, double beta, double* Q, long ldq, int n_moduli,
-                 void* work, size_t lwork, cudaStream_t stream, bool wait_status = false);
+                 void* work, size_t lwork, cudaStream_t stream, bool wait_status = false,
+                 int block_levels = 0);
 // The per-(device, stream) status word the asynchronous calls OR their device status into
 // (psmma_capi.cu; created on first use, NULL if that fails).
 unsigned* stream_status_word(cudaStream_t stream);
@@ -144,7 +146,8 @@ static unsigned* const kStatusWait = reinterpret_cast<unsigned*>(1);
 // the device timeout flag at the end of the stream's work (no synchronisation).
 int launch_split_any(int kind, int n, int k, double alpha, const double* A, long lda,
                      const double* gen, long ldgen, double beta, double* Q, long ldq, int n_moduli,
-                     void* work, size_t lwork, cudaStream_t stream, unsigned* status_dev_out);
+                     void* work, size_t lwork, cudaStream_t stream, unsigned* status_dev_out,
+                     int block_levels = 0);
 // General real product on the split path: Q (M x N) = alpha * A (M x K) * H (K x N) + beta * Q
 // with H given by gs (Cauchy, Toeplitz or Hankel).
 size_t split_workspace_general(int M, int N, int K, int n_moduli);

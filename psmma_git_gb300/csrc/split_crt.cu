@@ -46,6 +46,7 @@ struct CrtConsts {
   float mf[SPL_MAX_MODULI];   // m as a float
   float g23[SPL_MAX_MODULI];  // 2^23 mod m, symmetric (|g| <= m/2)
   float g38[SPL_MAX_MODULI];  // 2^38 mod m, symmetric
+  float g14[SPL_MAX_MODULI], g28[SPL_MAX_MODULI], g42[SPL_MAX_MODULI];  // 2^14, 2^28, 2^42 mod m, symmetric
   unsigned long long C_lo[SPL_MAX_MODULI], C_hi[SPL_MAX_MODULI];  // CRT basis C_l < M
   float f[SPL_MAX_MODULI];                                        // C_l / M
   unsigned long long M_lo, M_hi;
@@ -66,6 +67,7 @@ struct SplitDevParams {
   int PA, PH;                   // bits of the integer-scaled A (per row) and H (per column)
   unsigned long long rho_bits;  // max_j sum_k |H_kj| / max_k |H_kj| (bits of a positive double)
   unsigned done;                // parameter-pass blocks finished
+  unsigned hbad;                // block-recursive products: some column of H is not finite
   double part[PARAMS_BLOCKS][6];  // their partial ratio maxima and sums, combined in block order
 };
 
@@ -101,6 +103,10 @@ static CrtConsts make_consts(int nmod) {
     const int g23 = (int)((1LL << 23) % m), g38 = (int)((1LL << 38) % m);
     c.g23[l] = (float)(g23 > m / 2 ? g23 - m : g23);
     c.g38[l] = (float)(g38 > m / 2 ? g38 - m : g38);
+    const int g14 = (int)((1LL << 14) % m), g28 = (int)((1LL << 28) % m), g42 = (int)((1LL << 42) % m);
+    c.g14[l] = (float)(g14 > m / 2 ? g14 - m : g14);
+    c.g28[l] = (float)(g28 > m / 2 ? g28 - m : g28);
+    c.g42[l] = (float)(g42 > m / 2 ? g42 - m : g42);
     u128 Ml = M / (u128)m;
     long long Ml_mod = (long long)(Ml % (u128)m);
     long long y = inv_mod(Ml_mod, m);
@@ -144,6 +150,7 @@ struct SplitLayout {
   int kp, kr;
   size_t off_params, off_amax, off_hmax, off_hsum, off_asq, off_hsq, off_wtab, off_ht, off_ra, off_rh, off_r,
       total;
+  size_t off_rs = 0, off_gmax = 0;  // block-recursive products: A block sums, group column maxima
 };
 
 // M rows of A (and Q), K inner length, N columns of H (and Q).
@@ -226,8 +233,16 @@ static DftRadixLayout dft_radix_layout(int n, int k, int R, int nmod) {
   return D;
 }
 
-size_t split_workspace_bytes(int kind, int n, int k, int n_moduli) {
+static int block_levels(int kind, int N, int K, int req);
+static SplitLayout block_layout(int M, int N, int L, int nmod);
+
+size_t split_workspace_bytes(int kind, int n, int k, int n_moduli, int block_req) {
   if (n <= 0 || k <= 0) return 0;
+  if (kind == KIND_TOEPLITZ || kind == KIND_HANKEL) {
+    const int L = block_levels(kind, k, k, block_req);
+    const size_t plain = split_layout(n, k, k, resolve_nmod(n_moduli)).total;
+    return L > 0 ? std::max(plain, block_layout(n, k, L, resolve_nmod(n_moduli)).total) : plain;
+  }
   if (kind == KIND_DFT) {
     const int R = dft_radix(n);
     return R == 1 ? dft3_layout(k, n, resolve_nmod(n_moduli)).total
@@ -641,6 +656,33 @@ __device__ __forceinline__ unsigned residue_bits(const ResidueChunks& c, float g
   return __float_as_uint(residue_f(c, g23, g38, inv, mf));
 }
 
+// Residues of a signed integer V with |V| < 2^56 (a signed sum of up to eight scaled integers
+// below 2^53): its magnitude cut into four 14-bit chunks c_i (exact floats by the same
+// 2^23-offset trick, signed), t = c0 + g14 c1 + g28 c2 + g42 c3 with g = 2^(14 i) mod m taken
+// symmetric is congruent to V and |t| < 2^14 * (1 + 3 * 128) < 2^23, so the FMAs are exact;
+// quotient and remainder as in residue_f.
+struct ResidueChunks4 {
+  float c[4];
+};
+
+__device__ __forceinline__ ResidueChunks4 residue_chunks4(long long V) {
+  const bool neg = V < 0;
+  const unsigned long long u = neg ? (unsigned long long)(-V) : (unsigned long long)V;
+  const float s = neg ? -1.0f : 1.0f, o = neg ? 8388608.0f : -8388608.0f;
+  ResidueChunks4 r;
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+    r.c[i] = fmaf(__uint_as_float(0x4B000000u | (unsigned)((u >> (14 * i)) & 0x3FFFull)), s, o);
+  return r;
+}
+
+__device__ __forceinline__ float residue4_f(const ResidueChunks4& c, float g14, float g28, float g42, float inv,
+                                            float mf) {
+  const float t = fmaf(c.c[3], g42, fmaf(c.c[2], g28, fmaf(c.c[1], g14, c.c[0])));
+  const float q = fmaf(t, inv, 12582912.0f) - 12582912.0f;
+  return fmaf(-q, mf, t);
+}
+
 // (a + b) mod m in [-128, 128] for residues |a|, |b| <= 128 (exact floats): the quotient
 // rint((a + b) / m) is in {-1, 0, 1} and its float estimate is off by at most 2^-23.
 __device__ __forceinline__ float residue_sum(float a, float b, float inv, float mf) {
@@ -774,6 +816,197 @@ __global__ void k_residues_H_spec(const double* __restrict__ Ht, int ncols, int 
                                   CrtConsts cc, __nv_bfloat16* __restrict__ RH, int guess, int redo) {
   if (redo && prm->PH == guess) return;
   residues_H_blk(Ht, ncols, kp, hmax_bits, prm, cc, RH, blockIdx.y, blockIdx.x, redo ? -1 : guess);
+}
+
+// ---- Block-recursive Toeplitz / Hankel products (split_core_block) --------------------------
+// H (N x N) is cut into 2^L x 2^L blocks of width w = N / 2^L.  Columns j, j + w, ..., j + (2^L - 1) w
+// form a group that shares one scaling exponent, from the group maximum gmax[j] of the column
+// maxima, so that the integer-scaled H' keeps the block identities of the structure (Toeplitz:
+// block (r, c) depends on c - r only; Hankel: on r + c) exactly.  The per-column maxima stay
+// in hmax (the parameter pass's bounds hold for either exponent, which is never larger).
+// prm->hbad turns the block step off for the call -- the gated kernels then take the single
+// product with per-column exponents (k_residues_H_gated, the plain GEMM) -- when a column is
+// not finite (zeroing it would break the identities; the single product returns NaN in exactly
+// the non-finite columns) or when a nonzero column's maximum is more than 2^kBlockMaxSpread
+// below its group's (its entries would lose that many bits to the shared exponent).
+constexpr int kBlockMaxSpread = 4;
+__global__ void k_group_colmax(const unsigned long long* __restrict__ hmax_bits,
+                               unsigned long long* __restrict__ gmax_bits, int w, int nq, SplitDevParams* prm) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= w) return;
+  unsigned long long m = 0, mn = ~0ull;
+  bool bad = false;
+  for (int c = 0; c < nq; ++c) {
+    const unsigned long long b = hmax_bits[g + (size_t)c * w];
+    bad |= b >= INF_BITS;
+    if (b < INF_BITS && b > m) m = b;
+    if (b > 0 && b < mn) mn = b;
+  }
+  if (!bad && m > 0 && ilogb_bits(m) - ilogb_bits(mn) > kBlockMaxSpread) bad = true;
+  if (bad) prm->hbad = 1u;
+  gmax_bits[g] = m;
+}
+
+// Sums of A's column blocks that the leaf products take as their A operand: bit q of mask[p]
+// selects block q (columns [q w, (q + 1) w)).
+constexpr int BLK_MAX_LEVELS = 3;
+constexpr int BLK_MAX_LEAVES = 27;  // 3^BLK_MAX_LEVELS
+struct BlockSums {
+  int nsum;
+  int mask[BLK_MAX_LEAVES];
+};
+
+// A residues of the block-recursive product: RA[l][i][kk] (every column, as k_residues_A) and
+// RS[p][l][i][kk'] = sum over the blocks q of mask[p] of RA[l][i][q w + kk'] mod m_l, kk' < w.
+// One block: 32 rows x 64 columns of each of the NQ column blocks, transposed through shared
+// memory (NQ tiles of 64 x 32 doubles, the swizzle of residues_A_blk); each thread keeps the
+// residue chunks of its 4 columns of every block, so the sums need no second pass over A.
+template <int NQ>
+__global__ void __launch_bounds__(256) k_residues_A_blocks(const double* __restrict__ A, long lda, int M, int w,
+                                                           int kp, const unsigned long long* __restrict__ amax_bits,
+                                                           const SplitDevParams* prm, CrtConsts cc,
+                                                           __nv_bfloat16* __restrict__ RA,
+                                                           __nv_bfloat16* __restrict__ RS,
+                                                           const __grid_constant__ BlockSums bs) {
+  constexpr int TR = 32;
+  extern __shared__ double blk_tiles[];  // [NQ][64][TR]
+  const int i0 = blockIdx.y * TR, k0 = blockIdx.x * 64;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < NQ; ++q)
+    for (int kk = ty; kk < 64; kk += 8) {
+      const int gi = i0 + tx;
+      const long gk = (long)q * w + k0 + kk;
+      blk_tiles[(q * 64 + kk) * TR + ((tx + (kk >> 2)) & (TR - 1))] = gi < M ? __ldg(A + gk * lda + gi) : 0.0;
+    }
+  __syncthreads();
+  const int P = prm->PA;
+  const int nsum = prm->hbad ? 0 : bs.nsum;  // the single product needs no block sums
+  const size_t plane = (size_t)M * kp, splane = (size_t)M * w;
+  const int tq = threadIdx.x & 15, tr = threadIdx.x >> 4;
+  for (int r = tr; r < TR; r += 16) {
+    const int gi = i0 + r;
+    if (gi >= M) continue;
+    const unsigned long long ab = amax_bits[gi];
+    const bool ok = ab > 0 && ab < INF_BITS;
+    const int e = ok ? scale_exp(ab, P) : 0;
+    const int kk = 4 * tq;
+    long long sv[NQ][4];  // the signed scaled integers of the thread's 4 columns of every block
+#pragma unroll
+    for (int q = 0; q < NQ; ++q)
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        bool ng = false;
+        const unsigned long long u =
+            ok ? scaled_int(blk_tiles[(q * 64 + kk + v) * TR + ((r + tq) & (TR - 1))], e, &ng) : 0ull;
+        sv[q][v] = ng ? -(long long)u : (long long)u;
+      }
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) {
+      unsigned long long u[4];
+      bool ng[4];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        ng[v] = sv[q][v] < 0;
+        u[v] = ng[v] ? (unsigned long long)(-sv[q][v]) : (unsigned long long)sv[q][v];
+      }
+      write_residue_quad(u, ng, cc, (uint2*)(RA + (size_t)gi * kp + (size_t)q * w + k0 + kk), plane / 4);
+    }
+    for (int p = 0; p < nsum; ++p) {
+      const int mk = bs.mask[p];
+      ResidueChunks4 c4[4];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        long long V = 0;
+#pragma unroll
+        for (int q = 0; q < NQ; ++q) V += ((mk >> q) & 1) ? sv[q][v] : 0ll;
+        c4[v] = residue_chunks4(V);
+      }
+      uint2* dst = (uint2*)(RS + (size_t)p * cc.nmod * splane + (size_t)gi * w + k0 + kk);
+#pragma unroll
+      for (int l = 0; l < SPL_MAX_MODULI; ++l) {
+        if (l < cc.nmod) {
+          const float g14 = cc.g14[l], g28 = cc.g28[l], g42 = cc.g42[l], inv = cc.inv_m[l], mf = cc.mf[l];
+          unsigned f[4];
+#pragma unroll
+          for (int v = 0; v < 4; ++v) f[v] = __float_as_uint(residue4_f(c4[v], g14, g28, g42, inv, mf));
+          *dst = make_uint2(__byte_perm(f[0], f[1], 0x7632), __byte_perm(f[2], f[3], 0x7632));
+          dst += splane / 4;
+        }
+      }
+    }
+  }
+}
+
+// H operands of the leaf products: leaf y is sum_t sign[y][t] * H'(kk' + koff[y][t], j' + joff[y][t])
+// for kk', j' < w, a signed sum of up to 2^L blocks of the integer-scaled H (scaled with the
+// group exponent of column j').  Entries of a non-finite column count as zero (the
+// recombination returns NaN there).
+struct LeafTerms {
+  int nterm[BLK_MAX_LEAVES];
+  signed char sign[BLK_MAX_LEAVES][1 << BLK_MAX_LEVELS];
+  int koff[BLK_MAX_LEAVES][1 << BLK_MAX_LEVELS], joff[BLK_MAX_LEAVES][1 << BLK_MAX_LEVELS];
+};
+
+// RHL[y][l][j'][kk'] from Ht: grid (w columns j', kk' blocks of 512, leaves y); one thread per
+// 4 consecutive kk'.
+template <int NT>
+__global__ void __launch_bounds__(128) k_residues_H_leaf(const double* __restrict__ Ht, int kp, int w,
+                                                         const unsigned long long* __restrict__ hmax_bits,
+                                                         const unsigned long long* __restrict__ gmax_bits,
+                                                         const SplitDevParams* prm, CrtConsts cc,
+                                                         const __grid_constant__ LeafTerms lt,
+                                                         __nv_bfloat16* __restrict__ RHL) {
+  const int j = blockIdx.x, y = blockIdx.z;
+  const int kk = RH_PER_THREAD * (blockIdx.y * blockDim.x + threadIdx.x);
+  if (kk >= w || prm->hbad) return;  // w is a multiple of 64: a thread's four entries are all inside
+  const unsigned long long gb = gmax_bits[j];
+  const bool gok = gb > 0 && gb < INF_BITS;
+  const int e = gok ? scale_exp(gb, prm->PH) : 0;
+  const int nt = lt.nterm[y];
+  long long V[4] = {0, 0, 0, 0};  // exact: up to 8 terms below 2^53
+#pragma unroll
+  for (int t = 0; t < NT; ++t) {
+    if (t >= nt) break;
+    const int col = j + lt.joff[y][t];
+    if (!gok || hmax_bits[col] >= INF_BITS) continue;
+    const double* src = Ht + (size_t)col * kp + lt.koff[y][t] + kk;
+    const double2 h01 = *(const double2*)src, h23 = *(const double2*)(src + 2);
+    const double hv[4] = {h01.x, h01.y, h23.x, h23.y};
+    const int sg = lt.sign[y][t];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      bool ng = false;
+      const long long u = (long long)scaled_int(hv[v], e, &ng);
+      V[v] += (ng != (sg < 0)) ? -u : u;
+    }
+  }
+  ResidueChunks4 c4[4];
+#pragma unroll
+  for (int v = 0; v < 4; ++v) c4[v] = residue_chunks4(V[v]);
+  const size_t plane = (size_t)w * w;
+  uint2* dst = (uint2*)(RHL + (size_t)y * cc.nmod * plane + (size_t)j * w + kk);
+#pragma unroll
+  for (int l = 0; l < SPL_MAX_MODULI; ++l) {
+    if (l < cc.nmod) {
+      const float g14 = cc.g14[l], g28 = cc.g28[l], g42 = cc.g42[l], inv = cc.inv_m[l], mf = cc.mf[l];
+      unsigned f[4];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) f[v] = __float_as_uint(residue4_f(c4[v], g14, g28, g42, inv, mf));
+      *dst = make_uint2(__byte_perm(f[0], f[1], 0x7632), __byte_perm(f[2], f[3], 0x7632));
+      dst += plane / 4;
+    }
+  }
+}
+
+// The residues of the whole H (as k_residues_H) when prm->hbad is set; columns j = blockIdx.x +
+// gridDim.x t.
+__global__ void k_residues_H_gated(const double* __restrict__ Ht, int ncols, int kp,
+                                   const unsigned long long* __restrict__ hmax_bits, const SplitDevParams* prm,
+                                   CrtConsts cc, __nv_bfloat16* __restrict__ RH) {
+  if (!prm->hbad) return;
+  for (int j = blockIdx.x; j < ncols; j += gridDim.x)
+    residues_H_blk(Ht, ncols, kp, hmax_bits, prm, cc, RH, blockIdx.y, j);
 }
 
 // DFT A side: row i of the product (B^T) is column i of B, read contiguously (Bre = B as
@@ -1024,6 +1257,15 @@ struct GemmArgs {
   // 0 stores the residues; 1 reads T1 where it stores and writes T1 - x there and -T1 - x at
   // +im_off bytes; 2 adds x to the residues already stored.
   int mode, im_off;
+  // Block-recursive products: modes 0 and 2 write each residue to ndst places, column offsets
+  // dst_col[d] (ndst = 0: one place, offset 0), and only the product's first ncols columns
+  // (ncols = 0: every column of the tile).
+  int ndst, ncols;
+  int dst_col[8];
+  // gate != nullptr: the launch runs only when (*gate != 0) == gate_set (the block-recursive
+  // products and their single-product fallback, chosen on the device)
+  const unsigned* gate;
+  int gate_set;
   int8_t* R;
   unsigned* status;
   int m[SPL_MAX_MODULI];
@@ -1128,10 +1370,13 @@ __device__ __forceinline__ int mod_sym_small(int s, int m) {
 // (in [-128, 127]) with those already in the output plane, 16 bytes at a time.
 // mode 1: old = T1 -> store (T1 - x) mod m, and (-T1 - x) mod m at dst + im_off;
 // mode 2: old = -T1 - T2 -> store (old + x) mod m.
+// Only the first `valid` columns (a multiple of 16) are touched.
 template <int HALF>
-__device__ __forceinline__ void store_combined(int8_t* dst, const int (&res)[HALF], int mode, int im_off, int m) {
+__device__ __forceinline__ void store_combined(int8_t* dst, const int (&res)[HALF], int mode, int im_off, int m,
+                                               int valid = HALF) {
 #pragma unroll
   for (int v = 0; v < HALF / 16; ++v) {
+    if (v * 16 >= valid) break;
     const uint4 o = *(const uint4*)(dst + v * 16);
     const uint32_t ow[4] = {o.x, o.y, o.z, o.w};
     uint32_t w1[4], w2[4];
@@ -1168,7 +1413,9 @@ __device__ __forceinline__ void tensormap_acquire(const CUtensorMap* m) {
 // stage ring and the two TMEM accumulators continue across tiles (and, in a grouped launch,
 // across products), so the loads and MMAs of the next tile overlap the drain and residue
 // store of the previous one.  BN: output tile width (256, or 64 for narrow products).
-template <int BN, class TS>
+// MULTI: the block-recursive products' epilogue (GemmArgs::ndst, dst_col, ncols); without it
+// every residue goes to one place and the epilogue keeps fewer registers live.
+template <int BN, class TS, bool MULTI = false>
 __global__ void __launch_bounds__(G_THREADS, 1) k_crt_gemm(const __grid_constant__ TS ts) {
   using S = GemmShape<BN>;
   extern __shared__ uint8_t smem_raw[];
@@ -1197,8 +1444,9 @@ __global__ void __launch_bounds__(G_THREADS, 1) k_crt_gemm(const __grid_constant
       mbar_init(&acc_empty[b], G_EPI_WARPS * 32);
     }
     mbar_init(mma_done, 1);
-    // a launch whose pipeline already timed out does no further work
-    *abort_flag = status_aborted(g.status) ? 1 : 0;
+    // a launch whose pipeline already timed out does no further work, nor one gated off
+    const bool gated_off = g.gate != nullptr && ((*(const volatile unsigned*)g.gate != 0u) != (g.gate_set != 0));
+    *abort_flag = (status_aborted(g.status) || gated_off) ? 1 : 0;
     fence_barrier_init();
   }
   if (warp == 0) {
@@ -1316,13 +1564,70 @@ __global__ void __launch_bounds__(G_THREADS, 1) k_crt_gemm(const __grid_constant
         }
       }
       const int i = ti.tm * G_BM + q * 32 + lane;
-      if (ok && !*abort_flag && i < ti.n && g.mode != 0) {
-        int8_t* dst = ti.R + ((size_t)ti.l * ti.n + i) * ti.kr + (size_t)ti.tn * BN + h * HALF;
-        store_combined<HALF>(dst, res, g.mode, g.im_off, mi);
-      } else if (ok && !*abort_flag && i < ti.n) {
-        int8_t* dst = ti.R + ((size_t)ti.l * ti.n + i) * ti.kr + (size_t)ti.tn * BN + h * HALF;
+      if (MULTI) {
+        // per place every 16-byte load issued before the first add: one round trip per place
+        const int col0 = ti.tn * BN + h * HALF;
+        const int valid = g.ncols > 0 ? g.ncols - col0 : HALF;  // columns of this half in the product
+        if (ok && !*abort_flag && i < ti.n && valid > 0) {
+          // the residues packed to bytes (32 registers instead of 128); the volatile move keeps
+          // the compiler from re-deriving them from the int32 sums inside the place loop,
+          // which would keep all 128 sums live there and spill
+          uint32_t pk[HALF / 4];
+#pragma unroll
+          for (int e4 = 0; e4 < HALF / 4; ++e4) {
+            const uint32_t pv = (uint32_t)(uint8_t)(int8_t)res[4 * e4] |
+                                ((uint32_t)(uint8_t)(int8_t)res[4 * e4 + 1] << 8) |
+                                ((uint32_t)(uint8_t)(int8_t)res[4 * e4 + 2] << 16) |
+                                ((uint32_t)(uint8_t)(int8_t)res[4 * e4 + 3] << 24);
+            asm volatile("mov.b32 %0, %1;" : "=r"(pk[e4]) : "r"(pv));
+          }
+          int8_t* row = ti.R + ((size_t)ti.l * ti.n + i) * ti.kr + (size_t)col0;
+          const int nd = g.ndst > 0 ? g.ndst : 1;
+          for (int d = 0; d < nd; ++d) {
+            int8_t* dst = row + (g.ndst > 0 ? g.dst_col[d] : 0);
+            if (g.mode == 2) {
+              uint4 o[HALF / 16];
+#pragma unroll
+              for (int v = 0; v < HALF / 16; ++v)
+                o[v] = v * 16 < valid ? *(const uint4*)(dst + v * 16) : make_uint4(0u, 0u, 0u, 0u);
+#pragma unroll
+              for (int v = 0; v < HALF / 16; ++v) {
+                if (v * 16 >= valid) break;
+                const uint32_t ow[4] = {o[v].x, o[v].y, o[v].z, o[v].w};
+                uint32_t nw[4];
+#pragma unroll
+                for (int t4 = 0; t4 < 4; ++t4) {
+                  nw[t4] = 0u;
+#pragma unroll
+                  for (int bb = 0; bb < 4; ++bb) {
+                    const int a = (int)(int8_t)(ow[t4] >> (8 * bb)) + (int)(int8_t)(pk[4 * v + t4] >> (8 * bb));
+                    nw[t4] |= (uint32_t)(uint8_t)(int8_t)mod_sym_small(a, mi) << (8 * bb);
+                  }
+                }
+                *(uint4*)(dst + v * 16) = make_uint4(nw[0], nw[1], nw[2], nw[3]);
+              }
+            } else {
+#pragma unroll
+              for (int v = 0; v < HALF / 16; ++v)
+                if (v * 16 < valid)
+                  *(uint4*)(dst + v * 16) = make_uint4(pk[4 * v], pk[4 * v + 1], pk[4 * v + 2], pk[4 * v + 3]);
+            }
+          }
+        }
+        continue;
+      }
+      const int col0 = ti.tn * BN + h * HALF;
+      const int valid = HALF;
+      const int nd = 1;
+      for (int d = 0; d < nd && ok && !*abort_flag && i < ti.n && valid > 0; ++d) {
+        int8_t* dst = ti.R + ((size_t)ti.l * ti.n + i) * ti.kr + (size_t)col0;
+        if (g.mode != 0) {
+          store_combined<HALF>(dst, res, g.mode, g.im_off, mi, valid);
+          continue;
+        }
 #pragma unroll
         for (int v = 0; v < HALF / 16; ++v) {
+          if (v * 16 >= valid) break;
           uint32_t w[4];
 #pragma unroll
           for (int t4 = 0; t4 < 4; ++t4) {
@@ -1419,7 +1724,9 @@ __device__ __forceinline__ void crt_combine_blk(const int8_t* __restrict__ R, in
                                                 const CrtConsts& cc, const unsigned long long* __restrict__ amax_bits,
                                                 const unsigned long long* __restrict__ hmax_bits,
                                                 const SplitDevParams* prm, double alpha, double beta,
-                                                double* __restrict__ Q, long ldq, int bx, int by) {
+                                                double* __restrict__ Q, long ldq, int bx, int by,
+                                                const unsigned long long* __restrict__ gmax_bits = nullptr,
+                                                int gw = 1) {
   // element (jl, il) of the tile at column (il + jl/4) mod 32 of row jl: the row-wise writes
   // (4 columns per thread) and the column-wise reads both hit distinct bank pairs
   __shared__ double tile[CRT_TJ][CRT_TI];
@@ -1434,6 +1741,8 @@ __device__ __forceinline__ void crt_combine_blk(const int8_t* __restrict__ R, in
   for (int c = 0; c < 4; ++c) {
     const int hc = DFT_OUT ? dft_col(jb + c, k, kr) : (jb + c < k ? jb + c : -1);
     hb[c] = hc >= 0 ? hmax_bits[hc] : 0ull;
+    // block-recursive products: finite columns scaled with their group's exponent
+    if (gmax_bits != nullptr && hc >= 0 && hb[c] < INF_BITS && !prm->hbad) hb[c] = gmax_bits[hc % gw];
     fexp[c] = (hb[c] != 0 && hb[c] < INF_BITS) ? scale_exp(hb[c], PH) : 0;
   }
   const size_t plane_w = (size_t)n * kr / 4;
@@ -1562,6 +1871,19 @@ __global__ void __launch_bounds__(256, 3) k_crt_combine(const int8_t* __restrict
                                   by0 + blockIdx.y);
 }
 
+// The recombination of the block-recursive products (group exponents unless prm->hbad).
+template <bool TOP32>
+__global__ void __launch_bounds__(256, 3) k_crt_combine_blocks(const int8_t* __restrict__ R, int n, int k, int kr,
+                                                            CrtConsts cc,
+                                                            const unsigned long long* __restrict__ amax_bits,
+                                                            const unsigned long long* __restrict__ hmax_bits,
+                                                            const unsigned long long* __restrict__ gmax_bits, int gw,
+                                                            const SplitDevParams* prm, double alpha, double beta,
+                                                            double* __restrict__ Q, long ldq) {
+  crt_combine_blk<false, TOP32>(R, n, k, kr, cc, amax_bits, hmax_bits, prm, alpha, beta, Q, ldq, blockIdx.x,
+                                blockIdx.y, gmax_bits, gw);
+}
+
 // ------------------------------------------------------------------------------------------
 // Host orchestration
 // ------------------------------------------------------------------------------------------
@@ -1633,13 +1955,13 @@ static SplitBuffers split_buffers(char* w, const SplitLayout& L) {
 
 int launch_split_any(int kind, int n, int k, double alpha, const double* A, long lda, const double* gen,
                      long ldgen, double beta, double* Q, long ldq, int n_moduli, void* work, size_t lwork,
-                     cudaStream_t stream, unsigned* status_dev_out);
+                     cudaStream_t stream, unsigned* status_dev_out, int block_levels);
 
 int launch_split(int kind, int n, int k, double alpha, const double* A, long lda, const double* gen, long ldgen,
                  double beta, double* Q, long ldq, int n_moduli, void* work, size_t lwork, cudaStream_t stream,
-                 bool wait_status) {
+                 bool wait_status, int block_levels) {
   return launch_split_any(kind, n, k, alpha, A, lda, gen, ldgen, beta, Q, ldq, n_moduli, work, lwork, stream,
-                          wait_status ? kStatusWait : nullptr);
+                          wait_status ? kStatusWait : nullptr, block_levels);
 }
 
 // The device status of a call ORed into the stream's status word.
@@ -1854,6 +2176,309 @@ static int split_core(int M, int N, int K, double alpha, const double* A, long l
   prof_mark(stream, "crt_combine");
   if (cudaGetLastError() != cudaSuccess) return PSMMA_EDEVICE;
 
+  return split_status(b.prm, stream, status_dev_out);
+}
+
+// ---- Block-recursive Toeplitz / Hankel products --------------------------------------------
+// With A = [X1 X2] (column halves) and H = [Y00 Y01; Y10 Y11] (Y_rc: rows block r, columns block
+// c), Q = [Q1 Q2] takes three half-size products instead of four:
+//   Toeplitz (Y11 = Y00):  P = (X1 + X2) Y00,  Q1 = P + X2 (Y10 - Y00),  Q2 = P + X1 (Y01 - Y00);
+//   Hankel   (Y10 = Y01):  P = (X1 + X2) Y01,  Q1 = P + X1 (Y00 - Y01),  Q2 = P + X2 (Y11 - Y01).
+// Sums and differences of Toeplitz (Hankel) blocks are Toeplitz (Hankel) again, so the step
+// repeats on each of the three products: L levels give 3^L leaf products of width w = N / 2^L,
+// (3/4)^L of the modular GEMM work.  All of it is exact integer arithmetic modulo m_l on the
+// residues of the scaled A' and H' (the shared group exponents keep H' structured), so the
+// recombined Z = A'H' is the same integer matrix the single product gives.  Each leaf's A
+// operand is a sum of A's column blocks, its H operand a signed sum of up to 2^L blocks of H',
+// and its result goes to (is added to) 1 to 2^L column blocks of the output residues; the
+// first leaf (the sums at every level) covers every block and stores, the others add.
+struct BlkNode {
+  int amask;  // column blocks of A (at the node's level) summed into its A operand
+  int nterm;
+  int sign[1 << BLK_MAX_LEVELS], r[1 << BLK_MAX_LEVELS], c[1 << BLK_MAX_LEVELS];  // H blocks (r, c)
+  int ndst;
+  int dst[1 << BLK_MAX_LEVELS];  // output column blocks
+};
+
+static void block_expand(int kind, int level, int L, const BlkNode& nd, std::vector<BlkNode>& leaves) {
+  if (level == L) {
+    leaves.push_back(nd);
+    return;
+  }
+  // per choice: A halves (0 both, 1 first, 2 second), H terms (sign, row block, column block of
+  // the node's 2 x 2 split), output halves (0 both, 1 first, 2 second)
+  struct Choice {
+    int ahalf, nt, s[2], a[2], b[2], dsel;
+  };
+  static const Choice kToeplitz[3] = {{0, 1, {1, 0}, {0, 0}, {0, 0}, 0},
+                                      {2, 2, {1, -1}, {1, 0}, {0, 0}, 1},
+                                      {1, 2, {1, -1}, {0, 0}, {1, 0}, 2}};
+  static const Choice kHankel[3] = {{0, 1, {1, 0}, {0, 0}, {1, 0}, 0},
+                                    {1, 2, {1, -1}, {0, 0}, {0, 1}, 1},
+                                    {2, 2, {1, -1}, {1, 0}, {1, 1}, 2}};
+  const Choice* ch = kind == KIND_TOEPLITZ ? kToeplitz : kHankel;
+  for (int x = 0; x < 3; ++x) {
+    const Choice& cb = ch[x];
+    BlkNode c;
+    memset(&c, 0, sizeof(c));
+    for (int p = 0; p < 32; ++p)
+      if ((nd.amask >> p) & 1) {
+        if (cb.ahalf != 2) c.amask |= 1 << (2 * p);
+        if (cb.ahalf != 1) c.amask |= 1 << (2 * p + 1);
+      }
+    for (int t = 0; t < nd.nterm; ++t)
+      for (int u = 0; u < cb.nt; ++u) {
+        c.sign[c.nterm] = nd.sign[t] * cb.s[u];
+        c.r[c.nterm] = 2 * nd.r[t] + cb.a[u];
+        c.c[c.nterm] = 2 * nd.c[t] + cb.b[u];
+        ++c.nterm;
+      }
+    for (int d = 0; d < nd.ndst; ++d) {
+      if (cb.dsel != 2) c.dst[c.ndst++] = 2 * nd.dst[d];
+      if (cb.dsel != 1) c.dst[c.ndst++] = 2 * nd.dst[d] + 1;
+    }
+    block_expand(kind, level + 1, L, c, leaves);
+  }
+}
+
+static std::vector<BlkNode> block_leaves(int kind, int L) {
+  BlkNode root;
+  memset(&root, 0, sizeof(root));
+  root.amask = 1;
+  root.nterm = 1;
+  root.sign[0] = 1;
+  root.ndst = 1;
+  std::vector<BlkNode> leaves;
+  block_expand(kind, 0, L, root, leaves);
+  return leaves;
+}
+
+// Leaves need w = N / 2^L to be a multiple of 64 (whole k blocks and 128-byte operand offsets).
+// req (psmma_opts::block_levels): 0 = automatic -- the largest L <= kBlockAutoLevels with
+// w >= kBlockMinLeaf: below that the modular GEMMs' per-tile epilogue (2 drains at k = 2048)
+// weighs about as much as their MMAs and the step stops paying; -1 = none; 1..3 = that many
+// levels, fewer where N is not divisible.
+constexpr int kBlockMinLeaf = 4096;
+constexpr int kBlockAutoLevels = 2;
+static int block_levels(int kind, int N, int K, int req) {
+  if ((kind != KIND_TOEPLITZ && kind != KIND_HANKEL) || N != K || req < 0) return 0;
+  int L = 0;
+  if (req == 0) {
+    while (L < kBlockAutoLevels && N % (64 << (L + 1)) == 0 && (N >> (L + 1)) >= kBlockMinLeaf) ++L;
+  } else {
+    while (L < std::min(req, BLK_MAX_LEVELS) && N % (64 << (L + 1)) == 0) ++L;
+  }
+  return L;
+}
+
+extern "C" int psmma_split_block_levels(int kind, int n, int k) {
+  return (n > 0 && k > 0) ? block_levels(kind, k, k, 0) : 0;
+}
+
+static int ipow3(int L) { return L == 0 ? 1 : 3 * ipow3(L - 1); }
+
+// The split layout with the H residues replaced by the 3^L leaf operands (w x w each) followed
+// by the A block sums (3^L - 2^L planes of M x w); the region also holds the whole H's residues
+// of the single-product fallback.  The group maxima come last.
+static SplitLayout block_layout(int M, int N, int L, int nmod) {
+  const int w = N >> L, nleaf = ipow3(L), nsum = nleaf - (1 << L);
+  SplitLayout B;
+  B.kp = (N + 63) / 64 * 64;
+  B.kr = (N + 255) / 256 * 256;
+  size_t o = 0;
+  B.off_params = o; o += al1k(2 * sizeof(SplitDevParams));
+  B.off_amax = o;   o += al1k((size_t)M * 8);
+  B.off_hmax = o;   o += al1k((size_t)N * 8);
+  B.off_hsum = o;   o += al1k((size_t)N * 8);
+  B.off_asq = o;    o += al1k((size_t)M * 8);
+  B.off_hsq = o;    o += al1k((size_t)N * 8);
+  B.off_wtab = o;   o += al1k(16);
+  B.off_ht = o;     o += al1k((size_t)N * B.kp * 8);
+  B.off_ra = o;     o += al1k((size_t)nmod * M * B.kp * 2);
+  B.off_rh = o;
+  B.off_rs = o + al1k((size_t)nleaf * nmod * w * w * 2);
+  o += std::max(al1k((size_t)nleaf * nmod * w * w * 2) + al1k((size_t)nsum * nmod * M * w * 2),
+                al1k((size_t)nmod * N * B.kp * 2));
+  B.off_r = o;      o += al1k((size_t)nmod * M * B.kr);
+  B.off_gmax = o;   o += al1k((size_t)w * 8);
+  B.total = o;
+  return B;
+}
+
+// Tensor map of residue planes [nmod][rows][pitch] (bf16), the first `inner` entries of each row.
+static bool make_tmap_view(CUtensorMap* map, void* ptr, int inner, long pitch, int rows, int nmod, long plane,
+                           int box_rows) {
+  auto enc = get_encode();
+  if (!enc) return false;
+  cuuint64_t dims[3] = {(cuuint64_t)inner, (cuuint64_t)rows, (cuuint64_t)nmod};
+  cuuint64_t strides[2] = {(cuuint64_t)pitch * 2, (cuuint64_t)plane * 2};
+  cuuint32_t box[3] = {(cuuint32_t)G_BK, (cuuint32_t)box_rows, 1};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, ptr, dims, strides, box, estr,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+// Q (M x N) = alpha * A (M x N) * H + beta * Q for Toeplitz / Hankel H (N x N) with L >= 1 levels
+// of the block step (block_levels).
+static int split_core_block(int M, int N, int L, double alpha, const double* A, long lda, const GenSpec& gs,
+                            double beta, double* Q, long ldq, int nmod, void* work, size_t lwork,
+                            cudaStream_t stream, unsigned* status_dev_out) {
+  if (nmod < 8 || nmod > SPL_MAX_MODULI) return PSMMA_EUNSUPPORTED;
+  if (N >= (1 << 24) || M > kSplitMaxRows || L < 1 || L > BLK_MAX_LEVELS) return PSMMA_EUNSUPPORTED;
+  const int w = N >> L, NQ = 1 << L;
+  const SplitLayout Lo = block_layout(M, N, L, nmod);
+  if (lwork < Lo.total || !work) return PSMMA_EWORKSPACE;
+  char* wk = (char*)work;
+  const SplitBuffers b = split_buffers(wk, Lo);
+  __nv_bfloat16* RS = (__nv_bfloat16*)(wk + Lo.off_rs);
+  unsigned long long* gmax = (unsigned long long*)(wk + Lo.off_gmax);
+  const CrtConsts cc = get_consts(nmod);
+  const std::vector<BlkNode> leaves = block_leaves(gs.kind, L);
+  const int nleaf = (int)leaves.size();
+
+  // A operands: one block (a view of RA) or a sum plane (RS), numbered in leaf order
+  BlockSums bs;
+  memset(&bs, 0, sizeof(bs));
+  std::vector<int> a_sum(nleaf, -1);
+  for (int y = 0; y < nleaf; ++y) {
+    const int mk = leaves[y].amask;
+    if ((mk & (mk - 1)) == 0) continue;
+    int p = 0;
+    while (p < bs.nsum && bs.mask[p] != mk) ++p;
+    if (p == bs.nsum) bs.mask[bs.nsum++] = mk;
+    a_sum[y] = p;
+  }
+  LeafTerms lt;
+  memset(&lt, 0, sizeof(lt));
+  for (int y = 0; y < nleaf; ++y) {
+    lt.nterm[y] = leaves[y].nterm;
+    for (int t = 0; t < leaves[y].nterm; ++t) {
+      lt.sign[y][t] = (signed char)leaves[y].sign[t];
+      lt.koff[y][t] = leaves[y].r[t] * w;
+      lt.joff[y][t] = leaves[y].c[t] * w;
+    }
+  }
+
+  prof_begin(stream);
+  if (cudaMemsetAsync(wk, 0, Lo.off_wtab, stream) != cudaSuccess) return PSMMA_EDEVICE;
+  {
+    const int kchunk = 1024;
+    dim3 g1((M + 127) / 128, (N + kchunk - 1) / kchunk);
+    k_row_absmax<<<g1, 128, 0, stream>>>(A, lda, M, N, kchunk, b.amax, b.asq);
+  }
+  prof_mark(stream, "row_scale");
+  if (gs.kind == KIND_TOEPLITZ)
+    k_h_pass1<KIND_TOEPLITZ><<<N, 256, 0, stream>>>(gs, N, Lo.kp, b.Ht, b.hmax, b.hsum, b.hsq, b.prm);
+  else
+    k_h_pass1<KIND_HANKEL><<<N, 256, 0, stream>>>(gs, N, Lo.kp, b.Ht, b.hmax, b.hsum, b.hsq, b.prm);
+  k_group_colmax<<<(w + 255) / 256, 256, 0, stream>>>(b.hmax, gmax, w, NQ, b.prm);
+  prof_mark(stream, "h_generate");
+  k_split_params<<<PARAMS_BLOCKS, 512, 0, stream>>>(b.prm, cc.log2M, M, N, N, b.amax, b.asq, b.hmax, b.hsq);
+  prof_mark(stream, "params");
+  {
+    const dim3 ga(w / 64, (M + 31) / 32);
+    const int smem = NQ * 64 * 32 * 8;
+    cudaError_t e = cudaSuccess;
+    if (NQ == 2) {
+      e = set_smem_attr(k_residues_A_blocks<2>, smem);
+      if (e == cudaSuccess)
+        k_residues_A_blocks<2><<<ga, 256, smem, stream>>>(A, lda, M, w, Lo.kp, b.amax, b.prm, cc, b.RA, RS, bs);
+    } else if (NQ == 4) {
+      e = set_smem_attr(k_residues_A_blocks<4>, smem);
+      if (e == cudaSuccess)
+        k_residues_A_blocks<4><<<ga, 256, smem, stream>>>(A, lda, M, w, Lo.kp, b.amax, b.prm, cc, b.RA, RS, bs);
+    } else {
+      e = set_smem_attr(k_residues_A_blocks<8>, smem);
+      if (e == cudaSuccess)
+        k_residues_A_blocks<8><<<ga, 256, smem, stream>>>(A, lda, M, w, Lo.kp, b.amax, b.prm, cc, b.RA, RS, bs);
+    }
+    if (e != cudaSuccess) return PSMMA_EDEVICE;
+  }
+  prof_mark(stream, "residues_A");
+  {
+    const dim3 gh(w, rh_blocks_x(w), nleaf);
+    if (NQ == 2)
+      k_residues_H_leaf<2><<<gh, 128, 0, stream>>>(b.Ht, Lo.kp, w, b.hmax, gmax, b.prm, cc, lt, b.RH);
+    else if (NQ == 4)
+      k_residues_H_leaf<4><<<gh, 128, 0, stream>>>(b.Ht, Lo.kp, w, b.hmax, gmax, b.prm, cc, lt, b.RH);
+    else
+      k_residues_H_leaf<8><<<gh, 128, 0, stream>>>(b.Ht, Lo.kp, w, b.hmax, gmax, b.prm, cc, lt, b.RH);
+    k_residues_H_gated<<<dim3(std::min(N, 608), rh_blocks_x(Lo.kp)), 128, 0, stream>>>(b.Ht, N, Lo.kp, b.hmax,
+                                                                                        b.prm, cc, b.RH);
+  }
+  prof_mark(stream, "residues_H");
+
+  constexpr int LBN = G_BN;
+  using Shape = GemmShape<G_BN>;
+  using LShape = GemmShape<LBN>;
+  if (set_smem_attr(k_crt_gemm<LBN, OneGemm, true>, (int)LShape::SMEM) != cudaSuccess) return PSMMA_EDEVICE;
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return PSMMA_EDEVICE;
+  for (int y = 0; y < nleaf; ++y) {
+    const BlkNode& lf = leaves[y];
+    OneGemm og;
+    memset(&og, 0, sizeof(og));
+    bool ok;
+    if (a_sum[y] < 0) {
+      int q = 0;
+      while (!((lf.amask >> q) & 1)) ++q;
+      ok = make_tmap_view(&og.ta, b.RA + (size_t)q * w, w, Lo.kp, M, nmod, (long)M * Lo.kp, G_BM);
+    } else {
+      ok = make_tmap_view(&og.ta, RS + (size_t)a_sum[y] * nmod * M * w, w, w, M, nmod, (long)M * w, G_BM);
+    }
+    ok = ok && make_tmap_view(&og.tb, b.RH + (size_t)y * nmod * w * w, w, w, w, nmod, (long)w * w, LBN);
+    if (!ok) return PSMMA_EDEVICE;
+    GemmArgs& ga = og.g;
+    ga.n = M;
+    ga.kr = Lo.kr;
+    ga.nkb = w / G_BK;
+    ga.tiles_m = (M + G_BM - 1) / G_BM;
+    ga.tiles_n = (w + LBN - 1) / LBN;
+    ga.group_m = 16;
+    ga.nmod = nmod;
+    ga.R = b.R;
+    ga.status = &b.prm->status;
+    for (int l = 0; l < nmod; ++l) { ga.m[l] = cc.m[l]; ga.inv_m[l] = cc.inv_m[l]; }
+    ga.mode = y == 0 ? 0 : 2;  // the first leaf covers every block (block_expand takes the sums first)
+    ga.ndst = lf.ndst;
+    for (int d = 0; d < lf.ndst; ++d) ga.dst_col[d] = lf.dst[d] * w;
+    ga.ncols = w;
+    ga.gate = &b.prm->hbad;
+    ga.gate_set = 0;
+    const int total_tiles = ga.tiles_m * ga.tiles_n * nmod;
+    k_crt_gemm<LBN, OneGemm, true><<<std::min(sms, total_tiles), G_THREADS, LShape::SMEM, stream>>>(og);
+    prof_mark(stream, "modular_gemm");
+  }
+  {  // the single product, when some column of H is not finite
+    OneGemm og;
+    memset(&og, 0, sizeof(og));
+    if (!make_tmap(&og.ta, b.RA, Lo.kp, M, nmod, G_BM) || !make_tmap(&og.tb, b.RH, Lo.kp, N, nmod, G_BN))
+      return PSMMA_EDEVICE;
+    GemmArgs& ga = og.g;
+    ga.n = M;
+    ga.kr = Lo.kr;
+    ga.nkb = Lo.kp / G_BK;
+    ga.tiles_m = (M + G_BM - 1) / G_BM;
+    ga.tiles_n = (N + G_BN - 1) / G_BN;
+    ga.group_m = 16;
+    ga.nmod = nmod;
+    ga.R = b.R;
+    ga.status = &b.prm->status;
+    for (int l = 0; l < nmod; ++l) { ga.m[l] = cc.m[l]; ga.inv_m[l] = cc.inv_m[l]; }
+    ga.gate = &b.prm->hbad;
+    ga.gate_set = 1;
+    if (set_smem_attr(k_crt_gemm<G_BN, OneGemm>, (int)Shape::SMEM) != cudaSuccess) return PSMMA_EDEVICE;
+    k_crt_gemm<G_BN, OneGemm><<<std::min(sms, ga.tiles_m * ga.tiles_n * nmod), G_THREADS, Shape::SMEM, stream>>>(og);
+  }
+
+  dim3 gc((N + CRT_TJ - 1) / CRT_TJ, (M + CRT_TI - 1) / CRT_TI);
+  (cc.top32 ? k_crt_combine_blocks<true> : k_crt_combine_blocks<false>)<<<gc, dim3(32, 8), 0, stream>>>(
+      b.R, M, N, Lo.kr, cc, b.amax, b.hmax, gmax, w, b.prm, alpha, beta, Q, ldq);
+  prof_mark(stream, "crt_combine");
+  if (cudaGetLastError() != cudaSuccess) return PSMMA_EDEVICE;
   return split_status(b.prm, stream, status_dev_out);
 }
 
@@ -2232,10 +2857,13 @@ static int split_core_dft3(int k, int n, double alpha, const double* B, long ldb
 //   computed as C^T = B^T F in the 3M form (split_core_dft3).
 int launch_split_any(int kind, int n, int k, double alpha, const double* A, long lda, const double* gen,
                      long ldgen, double beta, double* Q, long ldq, int n_moduli, void* work, size_t lwork,
-                     cudaStream_t stream, unsigned* status_dev_out) {
+                     cudaStream_t stream, unsigned* status_dev_out, int block_req) {
   const int nmod = resolve_nmod(n_moduli);
   if (kind == KIND_DFT) return split_core_dft3(k, n, alpha, A, lda, beta, Q, ldq, nmod, work, lwork, stream, status_dev_out);
   const GenSpec gs = reference_gens(kind, gen, ldgen, k);
+  const int L = block_levels(kind, k, k, block_req);
+  if (L > 0 && gs.k1 == 0)
+    return split_core_block(n, k, L, alpha, A, lda, gs, beta, Q, ldq, nmod, work, lwork, stream, status_dev_out);
   return split_core(n, k, k, alpha, A, lda, gs, beta, Q, ldq, nmod, work, lwork, stream, status_dev_out);
 }
 

@@ -58,6 +58,10 @@ def test_options_are_validated(lib):
     o.precision = 0
     o.reserved[3] = 1
     assert lib.psmma_hankel(2, 2, 1.0, p, 2, p, 3, 0.0, p, 2, C.byref(o), None) == _lib.PSMMA_EUNSUPPORTED
+    o.reserved[3] = 0
+    for bad in (-2, 4):
+        o.block_levels = bad
+        assert lib.psmma_toeplitz(2, 2, 1.0, p, 2, p, 3, 0.0, p, 2, C.byref(o), None) == _lib.PSMMA_EUNSUPPORTED
 
 
 def test_fortran_abi_argument_check(lib):
@@ -85,6 +89,24 @@ def test_workspace_size_queries(lib):
     w = workspace_size(_lib.KIND_CAUCHY, 1024, 1024)
     assert w == 0 or w % (1024 * 1024 * 8) == 0
     assert workspace_size(_lib.KIND_DFT, 1000, 10) >= 1000 * 16
+
+
+def test_split_block_levels_rule(lib):
+    # the Toeplitz / Hankel block step chosen automatically: the largest L <= 2 with k divisible
+    # by 64 * 2^L and k / 2^L >= 4096; other kinds never take it (host logic only, no GPU work)
+    ks = [1024, 2048, 4096, 6144, 8192, 8256, 12288, 16384, 24576, 32768, 0]
+    for kind in (_lib.KIND_TOEPLITZ, _lib.KIND_HANKEL):
+        assert [lib.psmma_split_block_levels(kind, 100, k) for k in ks] == [0, 0, 0, 0, 1, 0, 1, 2, 2, 2, 0]
+    for kind in (_lib.KIND_CAUCHY, _lib.KIND_DFT):
+        assert [lib.psmma_split_block_levels(kind, 100, k) for k in ks] == [0] * len(ks)
+    # the workspace covers the block step's operands and the single product's, for the
+    # automatic choice and for levels asked for by opts->block_levels
+    from psmma_git_gb300 import workspace_size
+    for k, lv in ((8192, 0), (16384, 0), (2048, 2), (1536, 3), (4096, -1)):
+        plain = workspace_size(_lib.KIND_CAUCHY, 4096, k, precision="split")
+        assert workspace_size(_lib.KIND_TOEPLITZ, 4096, k, precision="split", block_levels=lv) >= plain
+    assert workspace_size(_lib.KIND_HANKEL, 4096, 2048, precision="split", block_levels=2) > \
+        workspace_size(_lib.KIND_HANKEL, 4096, 2048, precision="split", block_levels=-1)
 
 
 def test_fortran_module_binds_declared_and_exported_symbols(lib):

@@ -22,7 +22,7 @@ def _np(t):
     return t.t().contiguous().cpu().numpy().T
 
 
-def _split(kind, n, k, alpha, A, gen, beta, Q0, cuda, n_moduli=0, ld_pad=0):
+def _split(kind, n, k, alpha, A, gen, beta, Q0, cuda, n_moduli=0, ld_pad=0, **kw):
     import psmma_git_gb300 as P
     import torch
     dA = P.fortran_empty(n, k, torch.float64, cuda, ld=n + ld_pad)
@@ -30,7 +30,7 @@ def _split(kind, n, k, alpha, A, gen, beta, Q0, cuda, n_moduli=0, ld_pad=0):
     dQ = P.fortran_empty(n, k, torch.float64, cuda, ld=n + ld_pad)
     dQ.copy_(_t(Q0, cuda))
     dg = _t(gen, cuda) if kind == "cauchy" else torch.from_numpy(np.asarray(gen)).to(cuda)
-    getattr(P, "psmma_" + kind)(n, k, alpha, dA, dg, beta, dQ, precision="split", n_moduli=n_moduli)
+    getattr(P, "psmma_" + kind)(n, k, alpha, dA, dg, beta, dQ, precision="split", n_moduli=n_moduli, **kw)
     torch.cuda.synchronize()
     return _np(dQ)
 
@@ -176,6 +176,96 @@ def test_split_wide_exponent_range_rows(cuda):
     ref = O.dense_product("toeplitz", 1.0, A, gen, 0.0, None, k) * scale[:, None]
     for i in [0, 1, 100, 255]:
         assert np.linalg.norm(got[i] - ref[i]) / np.linalg.norm(ref[i]) < TOL
+
+
+@pytest.mark.parametrize("kind", ["toeplitz", "hankel"])
+@pytest.mark.parametrize("n,k,levels,pad", [(1000, 2048, 1, 3), (2048, 4096, 2, 0), (333, 6144, 2, 5),
+                                            (70, 3072, 1, 1), (130, 1536, 3, 2), (257, 8192, 0, 4)])
+def test_split_block_step_matches_dense_oracle(kind, n, k, levels, pad, cuda):
+    # the block step (3^L products of width k / 2^L on sums and differences of blocks), asked
+    # for by opts->block_levels (0: the automatic choice, one level at k = 8192): ragged row
+    # counts, padded leading dimensions, alpha and beta, leaves narrower than a GEMM tile
+    # (k = 1536 at L = 3: 192 columns), against the dense oracle on the whole product and
+    # column by column
+    import psmma_git_gb300 as P
+    if levels == 0:
+        assert P.load().psmma_split_block_levels({"toeplitz": 1, "hankel": 2}[kind], n, k) == 1
+    A = O.cfg_matrix(n, k, seed=n + k)
+    gen = _gen(kind, k, seed=k + 1)
+    Q0 = O.cfg_matrix(n, k, seed=n + 2)
+    got = _split(kind, n, k, 0.75, A, gen, -1.5, Q0, cuda, ld_pad=pad, block_levels=levels)
+    ref = O.dense_product(kind, 0.75, A, gen, -1.5, Q0, k)
+    assert O.rel_fro(got, ref) < TOL
+    assert O.col_max_rel(got, ref) < 10 * TOL
+
+
+@pytest.mark.parametrize("n,levels", [(2048, 2), (4096, 3), (8192, 0)])
+def test_split_block_step_toeplitz_known_answer_bit_exact(n, levels, cuda):
+    # the reference test's generator (G(i) = N - i, G(N) = N^2) with integer A: the block
+    # step's sums and differences are exact, so the closed form comes back bit for bit
+    g = O.reference_toeplitz_generator(n)
+    rng = np.random.Generator(np.random.PCG64(n))
+    A = rng.integers(-4, 5, size=(300, n)).astype(np.float64)
+    got = _split("toeplitz", 300, n, 1.0, A, g, 0.0, np.zeros((300, n)), cuda, block_levels=levels)
+    np.testing.assert_array_equal(got, O.toeplitz_reference_known_answer(A))
+
+
+@pytest.mark.parametrize("k,levels", [(2048, 1), (4096, 2), (4096, 3)])
+def test_split_block_step_range_bound_exact(k, levels, cuda):
+    # all-positive operands at the moduli's range bound, through the block step
+    n = 130
+    A = np.ones((n, k))
+    g = np.ones(2 * k - 1)
+    for kind in ["toeplitz", "hankel"]:
+        got = _split(kind, n, k, 1.0, A, g, 0.0, np.zeros((n, k)), cuda, block_levels=levels)
+        np.testing.assert_array_equal(got, np.full((n, k), float(k)))
+
+
+@pytest.mark.parametrize("kind", ["toeplitz", "hankel"])
+def test_split_block_step_same_result_as_single_product(kind, cuda):
+    # generators whose column groups share their exponent: the block step computes the same
+    # integer product as the single one, so the results are identical bit for bit
+    n, k = 300, 4096
+    A = O.cfg_matrix(n, k, seed=41)
+    gen = _gen(kind, k, seed=42)
+    one = _split(kind, n, k, 1.0, A, gen, 0.0, np.zeros((n, k)), cuda, block_levels=-1)
+    for levels in (1, 2, 3):
+        got = _split(kind, n, k, 1.0, A, gen, 0.0, np.zeros((n, k)), cuda, block_levels=levels)
+        np.testing.assert_array_equal(got, one)
+
+
+@pytest.mark.parametrize("kind", ["toeplitz", "hankel"])
+def test_split_block_step_nonfinite_generator_takes_single_product(kind, cuda):
+    # a NaN and an Inf in the generator: the call falls back (on the device) to the single
+    # product, which returns NaN in exactly the columns that hold them and the oracle's
+    # values elsewhere
+    n, k = 200, 4096
+    A = O.cfg_matrix(n, k, seed=31)
+    gen = _gen(kind, k, seed=32)
+    gen[k // 3] = np.nan
+    gen[2 * k - 900] = np.inf
+    got = _split(kind, n, k, 1.0, A, gen, 0.0, np.zeros((n, k)), cuda, block_levels=2)
+    H = O.const_toeplitz(gen, k, np.arange(1, k + 1), np.arange(1, k + 1)) if kind == "toeplitz" else \
+        O.const_hankel(gen, k, np.arange(1, k + 1), np.arange(1, k + 1))
+    bad = ~np.isfinite(H).all(axis=0)
+    assert bad.any() and not bad.all()
+    assert np.isnan(got[:, bad]).all()
+    gen_f = np.where(np.isfinite(gen), gen, 0.0)
+    ref = O.dense_product(kind, 1.0, A, gen_f, 0.0, None, k)
+    assert O.rel_fro(got[:, ~bad], ref[:, ~bad]) < TOL
+
+
+@pytest.mark.parametrize("kind", ["toeplitz", "hankel"])
+def test_split_block_step_graded_generator_keeps_column_accuracy(kind, cuda):
+    # g(x) = 2^(-x/64): columns j and j + w differ by w/64 binades, more than the block step
+    # lets a group share; the call takes the single product and every column keeps its own
+    # relative accuracy
+    n, k = 128, 4096
+    A = O.cfg_matrix(n, k, seed=33)
+    gen = 2.0 ** (-np.arange(2 * k - 1) / 64.0)
+    got = _split(kind, n, k, 1.0, A, gen, 0.0, np.zeros((n, k)), cuda, block_levels=2)
+    ref = O.dense_product(kind, 1.0, A, gen, 0.0, None, k)
+    assert O.col_max_rel(got, ref) < TOL
 
 
 def _split_dft(n, k, alpha, B, beta, C0, cuda, n_moduli=0, variant="pzmdftl"):
