@@ -69,9 +69,12 @@ typedef struct psmma_opts {
   int    n_moduli;    /* split path: number of moduli, 0 = default (14); 8..16                 */
   void*  work;        /* optional caller-owned device workspace (NULL: library-owned pool)      */
   size_t lwork;       /* size of `work` in bytes                                               */
-  int    block_levels; /* split path, Toeplitz / Hankel: levels of the block step (see
+  int    block_levels; /* split path: Toeplitz / Hankel: levels of the block step (see
                           psmma_split_block_levels): 0 = automatic, -1 = none (one product),
-                          1..3 = that many (fewer where k is not divisible by 64 * 2^L)       */
+                          1..3 = that many (fewer where k is not divisible by 64 * 2^L);
+                          Cauchy / CAUCHYEIG: 1 = Strassen's step on the residue planes
+                          (n even, k divisible by 128; the same result bit for bit, seven
+                          half-size modular products instead of eight), else none        */
   int    reserved[7]; /* must be zero                                                          */
 } psmma_opts;
 
@@ -156,7 +159,9 @@ int psmma_split_dft_radix(int n);
  * product.  On the device, without a synchronisation, the call takes the single product
  * instead when an entry of H is not finite (NaN then appears in exactly the columns it does
  * there) or when a nonzero column's maximum is more than 2^4 below the largest of its group
- * j + c w (the shared exponent would cost that column's entries more than 4 bits). */
+ * j + c w (the shared exponent would cost that column's entries more than 4 bits).  Cauchy and
+ * CAUCHYEIG: 0 (Strassen's step runs only when opts->block_levels asks for it: its operands
+ * take 7/4 of the residue planes' HBM traffic, which costs about what it saves). */
 int psmma_split_block_levels(int kind, int n, int k);
 
 /* No counterpart in the reference.  The split-path Cauchy multiply (same arguments and

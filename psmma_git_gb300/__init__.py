@@ -129,9 +129,12 @@ def _real(kind: int, name: str, n, k, alpha, A, gen, beta, Q, precision, n_modul
     return Q
 
 
-def psmma_cauchy(n, k, alpha, A, gen, beta, Q, *, precision="fp64", n_moduli=0, stream=None, work=None):
-    """Q := alpha*A*H + beta*Q with H(i,j) = U(i)*V(j)/(D(i)-F(j)), gen = [D|F|U|V]."""
-    return _real(KIND_CAUCHY, "psmma_cauchy", n, k, alpha, A, gen, beta, Q, precision, n_moduli, stream, work)
+def psmma_cauchy(n, k, alpha, A, gen, beta, Q, *, precision="fp64", n_moduli=0, stream=None, work=None,
+                 block_levels=0):
+    """Q := alpha*A*H + beta*Q with H(i,j) = U(i)*V(j)/(D(i)-F(j)), gen = [D|F|U|V].  block_levels:
+    the split path's Strassen step on the residue planes (0 = automatic, -1 = none, 1 = one)."""
+    return _real(KIND_CAUCHY, "psmma_cauchy", n, k, alpha, A, gen, beta, Q, precision, n_moduli, stream, work,
+                 block_levels)
 
 
 def psmma_toeplitz(n, k, alpha, A, gen, beta, Q, *, precision="fp64", n_moduli=0, stream=None, work=None,
@@ -281,11 +284,11 @@ def tune_batch(problems, alpha=1.0, beta=0.0, *, compressor="rrqr", tol=1e-14, p
 
 
 def psmma_cauchyeig(n, k, alpha, A, F, U, V, difl, difr, beta, Q, *, D=None, precision="fp64", n_moduli=0,
-                    stream=None, work=None):
+                    stream=None, work=None, block_levels=0):
     """Q := alpha*A*H + beta*Q, H(i,j) = U(i)V(j) / (F(i) - D(j)) with the denominators formed from
     DIFL(j) = D(j) - F(j) and DIFR(j) = D(j) - F(j+1) (CauchylikeEig).  Vectors of length k."""
     lib = load()
-    opts = make_opts(precision, n_moduli, work)
+    opts = make_opts(precision, n_moduli, work, block_levels=block_levels)
     vecs = [F, D, U, V, difl, difr]
     if _is_torch(Q):
         import torch

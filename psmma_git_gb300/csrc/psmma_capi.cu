@@ -426,7 +426,7 @@ int run_eig(int n, int k, double alpha, const double* A, int lda, const double* 
   cudaStream_t s = (cudaStream_t)stream;
   const GenSpec gs = eig_gens(F, U, V, difl, difr, k);
   if (o->precision == PSMMA_PREC_SPLIT && alpha != 0.0) {
-    size_t need = split_workspace_general(n, k, k, o->n_moduli);
+    size_t need = split_workspace_general(n, k, k, o->n_moduli, o->block_levels);
     void* work = o->work;
     if (work) {
       if (o->lwork < need) return PSMMA_EWORKSPACE;
@@ -435,7 +435,8 @@ int run_eig(int n, int k, double alpha, const double* A, int lda, const double* 
       if (st) return st;
     }
     unsigned* dstat = nullptr;
-    return launch_split_general(n, k, k, alpha, A, lda, gs, beta, Q, ldq, o->n_moduli, work, need, s, dstat);
+    return launch_split_general(n, k, k, alpha, A, lda, gs, beta, Q, ldq, o->n_moduli, work, need, s, dstat,
+                                o->block_levels);
   }
   size_t wb = 0;
   void* w = f64_work(n, k, k, o, s, &wb, &st);
@@ -637,7 +638,7 @@ size_t psmma_workspace_size(int kind, int n, int k, const psmma_opts* opts) {
   if (n <= 0 || k <= 0) return 0;
   if (kind < KIND_CAUCHY || kind > KIND_CAUCHY_EIG || kind == KIND_DENSE) return 0;
   if (kind == KIND_CAUCHY_EIG)
-    return o->precision == PSMMA_PREC_SPLIT ? split_workspace_general(n, k, k, o->n_moduli)
+    return o->precision == PSMMA_PREC_SPLIT ? split_workspace_general(n, k, k, o->n_moduli, o->block_levels)
                                             : f64_splitk_bytes(n, k, k, std::max(1, device_sms()));
   if (o->precision == PSMMA_PREC_SPLIT) return split_workspace_bytes(kind, n, k, o->n_moduli, o->block_levels);
   if (kind == KIND_DFT) return dft_f64_workspace(n, k);

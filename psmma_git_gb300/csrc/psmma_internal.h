@@ -150,7 +150,7 @@ int launch_split_any(int kind, int n, int k, double alpha, const double* A, long
                      int block_levels = 0);
 // General real product on the split path: Q (M x N) = alpha * A (M x K) * H (K x N) + beta * Q
 // with H given by gs (Cauchy, Toeplitz or Hankel).
-size_t split_workspace_general(int M, int N, int K, int n_moduli);
+size_t split_workspace_general(int M, int N, int K, int n_moduli, int block_levels = 0);
 // Host-pointer split multiply with the host<->device copies overlapped (split_crt.cu): A
 // and Q on the host, dA / dQ device buffers (leading dimension M), the copies on stream cs,
 // nev >= 15 events.
@@ -163,7 +163,7 @@ int launch_split_host_general(int M, int N, int K, double alpha, const double* A
                               void* work, size_t lwork, cudaStream_t s, cudaStream_t cs, cudaEvent_t* ev, int nev);
 int launch_split_general(int M, int N, int K, double alpha, const double* A, long lda, const GenSpec& gs,
                          double beta, double* Q, long ldq, int n_moduli, void* work, size_t lwork,
-                         cudaStream_t stream, unsigned* status_dev_out);
+                         cudaStream_t stream, unsigned* status_dev_out, int block_levels = 0);
 
 // Grouped split path (split_crt.cu): independent real products of uneven sizes, each
 // Q = alpha * A * H + beta * Q (M, N, K >= 1; H from gs, not the DFT), run as one launch

@@ -235,6 +235,8 @@ static DftRadixLayout dft_radix_layout(int n, int k, int R, int nmod) {
 
 static int block_levels(int kind, int N, int K, int req);
 static SplitLayout block_layout(int M, int N, int L, int nmod);
+static bool s2_use(int kind, int M, int K, int N, int req);
+static SplitLayout s2_layout(int M, int K, int N, int rows, int nmod);
 
 size_t split_workspace_bytes(int kind, int n, int k, int n_moduli, int block_req) {
   if (n <= 0 || k <= 0) return 0;
@@ -243,6 +245,8 @@ size_t split_workspace_bytes(int kind, int n, int k, int n_moduli, int block_req
     const size_t plain = split_layout(n, k, k, resolve_nmod(n_moduli)).total;
     return L > 0 ? std::max(plain, block_layout(n, k, L, resolve_nmod(n_moduli)).total) : plain;
   }
+  if (s2_use(kind, n, k, k, block_req))
+    return std::max(split_layout(n, k, k, resolve_nmod(n_moduli)).total, s2_layout(n, k, k, n, resolve_nmod(n_moduli)).total);
   if (kind == KIND_DFT) {
     const int R = dft_radix(n);
     return R == 1 ? dft3_layout(k, n, resolve_nmod(n_moduli)).total
@@ -255,9 +259,12 @@ extern "C" int psmma_split_dft_radix(int n) { return n > 0 ? dft_radix(n) : 0; }
 
 int dft_radix_for(int n) { return n > 0 ? dft_radix(n) : 1; }
 
-size_t split_workspace_general(int M, int N, int K, int n_moduli) {
+size_t split_workspace_general(int M, int N, int K, int n_moduli, int block_req) {
   if (M <= 0 || N <= 0 || K <= 0) return 0;
-  return split_layout(M, K, N, resolve_nmod(n_moduli)).total;
+  const size_t plain = split_layout(M, K, N, resolve_nmod(n_moduli)).total;
+  return s2_use(KIND_CAUCHY_EIG, M, K, N, block_req)
+             ? std::max(plain, s2_layout(M, K, N, M, resolve_nmod(n_moduli)).total)
+             : plain;
 }
 
 // ------------------------------------------------------------------------------------------
@@ -847,23 +854,28 @@ __global__ void k_group_colmax(const unsigned long long* __restrict__ hmax_bits,
   gmax_bits[g] = m;
 }
 
-// Sums of A's column blocks that the leaf products take as their A operand: bit q of mask[p]
-// selects block q (columns [q w, (q + 1) w)).
+// Signed sums of A's blocks that the leaf products take as their A operand.  Block q starts at
+// row qrow[q] (relative to the pass's first row) and column qcol[q]; operand p adds the blocks
+// of mask[p] and subtracts those of neg[p] (a subset of mask[p]).
 constexpr int BLK_MAX_LEVELS = 3;
 constexpr int BLK_MAX_LEAVES = 27;  // 3^BLK_MAX_LEVELS
 struct BlockSums {
   int nsum;
-  int mask[BLK_MAX_LEAVES];
+  int wmask;  // blocks whose own residues are written to RA (the others are only summed)
+  int mask[BLK_MAX_LEAVES], neg[BLK_MAX_LEAVES];
+  int qrow[1 << BLK_MAX_LEVELS], qcol[1 << BLK_MAX_LEVELS];
 };
 
-// A residues of the block-recursive product: RA[l][i][kk] (every column, as k_residues_A) and
-// RS[p][l][i][kk'] = sum over the blocks q of mask[p] of RA[l][i][q w + kk'] mod m_l, kk' < w.
-// One block: 32 rows x 64 columns of each of the NQ column blocks, transposed through shared
-// memory (NQ tiles of 64 x 32 doubles, the swizzle of residues_A_blk); each thread keeps the
-// residue chunks of its 4 columns of every block, so the sums need no second pass over A.
+// A residues of a block product: RA[l][r0 + qrow[q] + i][qcol[q] + kk] for every block q (as
+// k_residues_A writes them) and RS[p][l][i][kk] = the signed block sum p mod m_l, for i < rows,
+// kk < w.  Each block row keeps its own exponent (rows of different blocks are different rows of
+// A).  One CTA: 32 rows x 64 columns of each of the NQ blocks, transposed through shared memory
+// (NQ tiles of 64 x 32 doubles, the swizzle of residues_A_blk); each thread keeps the signed
+// scaled integers of its 4 columns of every block, so the sums need no second pass over A.
 template <int NQ>
-__global__ void __launch_bounds__(256) k_residues_A_blocks(const double* __restrict__ A, long lda, int M, int w,
-                                                           int kp, const unsigned long long* __restrict__ amax_bits,
+__global__ void __launch_bounds__(256) k_residues_A_blocks(const double* __restrict__ A, long lda, int M, int r0,
+                                                           int rows, int w, int kp,
+                                                           const unsigned long long* __restrict__ amax_bits,
                                                            const SplitDevParams* prm, CrtConsts cc,
                                                            __nv_bfloat16* __restrict__ RA,
                                                            __nv_bfloat16* __restrict__ RS,
@@ -875,54 +887,48 @@ __global__ void __launch_bounds__(256) k_residues_A_blocks(const double* __restr
 #pragma unroll
   for (int q = 0; q < NQ; ++q)
     for (int kk = ty; kk < 64; kk += 8) {
-      const int gi = i0 + tx;
-      const long gk = (long)q * w + k0 + kk;
-      blk_tiles[(q * 64 + kk) * TR + ((tx + (kk >> 2)) & (TR - 1))] = gi < M ? __ldg(A + gk * lda + gi) : 0.0;
+      const long gi = (long)r0 + bs.qrow[q] + i0 + tx;
+      const long gk = (long)bs.qcol[q] + k0 + kk;
+      blk_tiles[(q * 64 + kk) * TR + ((tx + (kk >> 2)) & (TR - 1))] =
+          i0 + tx < rows ? __ldg(A + gk * lda + gi) : 0.0;
     }
   __syncthreads();
   const int P = prm->PA;
   const int nsum = prm->hbad ? 0 : bs.nsum;  // the single product needs no block sums
-  const size_t plane = (size_t)M * kp, splane = (size_t)M * w;
+  const size_t plane = (size_t)M * kp, splane = (size_t)rows * w;
   const int tq = threadIdx.x & 15, tr = threadIdx.x >> 4;
   for (int r = tr; r < TR; r += 16) {
-    const int gi = i0 + r;
-    if (gi >= M) continue;
-    const unsigned long long ab = amax_bits[gi];
-    const bool ok = ab > 0 && ab < INF_BITS;
-    const int e = ok ? scale_exp(ab, P) : 0;
+    if (i0 + r >= rows) continue;
     const int kk = 4 * tq;
     long long sv[NQ][4];  // the signed scaled integers of the thread's 4 columns of every block
 #pragma unroll
-    for (int q = 0; q < NQ; ++q)
-#pragma unroll
-      for (int v = 0; v < 4; ++v) {
-        bool ng = false;
-        const unsigned long long u =
-            ok ? scaled_int(blk_tiles[(q * 64 + kk + v) * TR + ((r + tq) & (TR - 1))], e, &ng) : 0ull;
-        sv[q][v] = ng ? -(long long)u : (long long)u;
-      }
-#pragma unroll
     for (int q = 0; q < NQ; ++q) {
+      const long gi = (long)r0 + bs.qrow[q] + i0 + r;
+      const unsigned long long ab = amax_bits[gi];
+      const bool ok = ab > 0 && ab < INF_BITS;
+      const int e = ok ? scale_exp(ab, P) : 0;
       unsigned long long u[4];
       bool ng[4];
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
-        ng[v] = sv[q][v] < 0;
-        u[v] = ng[v] ? (unsigned long long)(-sv[q][v]) : (unsigned long long)sv[q][v];
+        ng[v] = false;
+        u[v] = ok ? scaled_int(blk_tiles[(q * 64 + kk + v) * TR + ((r + tq) & (TR - 1))], e, &ng[v]) : 0ull;
+        sv[q][v] = ng[v] ? -(long long)u[v] : (long long)u[v];
       }
-      write_residue_quad(u, ng, cc, (uint2*)(RA + (size_t)gi * kp + (size_t)q * w + k0 + kk), plane / 4);
+      if ((bs.wmask >> q) & 1)
+        write_residue_quad(u, ng, cc, (uint2*)(RA + (size_t)gi * kp + bs.qcol[q] + k0 + kk), plane / 4);
     }
     for (int p = 0; p < nsum; ++p) {
-      const int mk = bs.mask[p];
+      const int mk = bs.mask[p], ngm = bs.neg[p];
       ResidueChunks4 c4[4];
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
         long long V = 0;
 #pragma unroll
-        for (int q = 0; q < NQ; ++q) V += ((mk >> q) & 1) ? sv[q][v] : 0ll;
+        for (int q = 0; q < NQ; ++q) V += ((mk >> q) & 1) ? (((ngm >> q) & 1) ? -sv[q][v] : sv[q][v]) : 0ll;
         c4[v] = residue_chunks4(V);
       }
-      uint2* dst = (uint2*)(RS + (size_t)p * cc.nmod * splane + (size_t)gi * w + k0 + kk);
+      uint2* dst = (uint2*)(RS + (size_t)p * cc.nmod * splane + (size_t)(i0 + r) * w + k0 + kk);
 #pragma unroll
       for (int l = 0; l < SPL_MAX_MODULI; ++l) {
         if (l < cc.nmod) {
@@ -939,37 +945,40 @@ __global__ void __launch_bounds__(256) k_residues_A_blocks(const double* __restr
 }
 
 // H operands of the leaf products: leaf y is sum_t sign[y][t] * H'(kk' + koff[y][t], j' + joff[y][t])
-// for kk', j' < w, a signed sum of up to 2^L blocks of the integer-scaled H (scaled with the
-// group exponent of column j').  Entries of a non-finite column count as zero (the
-// recombination returns NaN there).
+// for kk' < wk, j' < wn, a signed sum of up to 2^L blocks of the integer-scaled H, each entry
+// scaled with the group exponent of column j' (group != 0: the structured block step) or with
+// its own column's (Strassen's step, which needs no structure).  Entries of a non-finite column
+// count as zero (the recombination returns NaN there).
 struct LeafTerms {
   int nterm[BLK_MAX_LEAVES];
   signed char sign[BLK_MAX_LEAVES][1 << BLK_MAX_LEVELS];
   int koff[BLK_MAX_LEAVES][1 << BLK_MAX_LEVELS], joff[BLK_MAX_LEAVES][1 << BLK_MAX_LEVELS];
 };
 
-// RHL[y][l][j'][kk'] from Ht: grid (w columns j', kk' blocks of 512, leaves y); one thread per
-// 4 consecutive kk'.
+// RHL[y][l][j'][kk'] (pitch wk) from Ht: grid (wn columns j', kk' blocks of 512, leaves y); one
+// thread per 4 consecutive kk'.
 template <int NT>
-__global__ void __launch_bounds__(128) k_residues_H_leaf(const double* __restrict__ Ht, int kp, int w,
+__global__ void __launch_bounds__(128) k_residues_H_leaf(const double* __restrict__ Ht, int kp, int wk, int wn,
                                                          const unsigned long long* __restrict__ hmax_bits,
                                                          const unsigned long long* __restrict__ gmax_bits,
-                                                         const SplitDevParams* prm, CrtConsts cc,
+                                                         int group, const SplitDevParams* prm, CrtConsts cc,
                                                          const __grid_constant__ LeafTerms lt,
                                                          __nv_bfloat16* __restrict__ RHL) {
   const int j = blockIdx.x, y = blockIdx.z;
   const int kk = RH_PER_THREAD * (blockIdx.y * blockDim.x + threadIdx.x);
-  if (kk >= w || prm->hbad) return;  // w is a multiple of 64: a thread's four entries are all inside
-  const unsigned long long gb = gmax_bits[j];
-  const bool gok = gb > 0 && gb < INF_BITS;
-  const int e = gok ? scale_exp(gb, prm->PH) : 0;
+  if (kk >= wk || prm->hbad) return;  // wk is a multiple of 64: a thread's four entries are all inside
+  const int PH = prm->PH;
+  const unsigned long long gb = group ? gmax_bits[j] : 0ull;
+  const bool gok = !group || (gb > 0 && gb < INF_BITS);
   const int nt = lt.nterm[y];
   long long V[4] = {0, 0, 0, 0};  // exact: up to 8 terms below 2^53
 #pragma unroll
   for (int t = 0; t < NT; ++t) {
     if (t >= nt) break;
     const int col = j + lt.joff[y][t];
-    if (!gok || hmax_bits[col] >= INF_BITS) continue;
+    const unsigned long long hb = hmax_bits[col];
+    if (!gok || hb == 0 || hb >= INF_BITS) continue;
+    const int e = scale_exp(group ? gb : hb, PH);
     const double* src = Ht + (size_t)col * kp + lt.koff[y][t] + kk;
     const double2 h01 = *(const double2*)src, h23 = *(const double2*)(src + 2);
     const double hv[4] = {h01.x, h01.y, h23.x, h23.y};
@@ -984,8 +993,8 @@ __global__ void __launch_bounds__(128) k_residues_H_leaf(const double* __restric
   ResidueChunks4 c4[4];
 #pragma unroll
   for (int v = 0; v < 4; ++v) c4[v] = residue_chunks4(V[v]);
-  const size_t plane = (size_t)w * w;
-  uint2* dst = (uint2*)(RHL + (size_t)y * cc.nmod * plane + (size_t)j * w + kk);
+  const size_t plane = (size_t)wn * wk;
+  uint2* dst = (uint2*)(RHL + (size_t)y * cc.nmod * plane + (size_t)j * wk + kk);
 #pragma unroll
   for (int l = 0; l < SPL_MAX_MODULI; ++l) {
     if (l < cc.nmod) {
@@ -995,6 +1004,67 @@ __global__ void __launch_bounds__(128) k_residues_H_leaf(const double* __restric
       for (int v = 0; v < 4; ++v) f[v] = __float_as_uint(residue4_f(c4[v], g14, g28, g42, inv, mf));
       *dst = make_uint2(__byte_perm(f[0], f[1], 0x7632), __byte_perm(f[2], f[3], 0x7632));
       dst += plane / 4;
+    }
+  }
+}
+
+// The seven H operands of Strassen's step (B00 + B11, B00, B01 - B11, B10 - B00, B11, B00 + B01,
+// B10 + B11 in the order of the products) from the four blocks of Ht read once: RHS[y][l][j'][kk']
+// (pitch wk) for j' < wn, kk' < wk; every entry scaled with its own column's exponent.  Grid (wn
+// columns, kk' blocks of 512); one thread per 4 consecutive kk'.
+__global__ void __launch_bounds__(128) k_residues_H_s2(const double* __restrict__ Ht, int kp, int wk, int wn,
+                                                       const unsigned long long* __restrict__ hmax_bits,
+                                                       const SplitDevParams* prm, CrtConsts cc,
+                                                       __nv_bfloat16* __restrict__ RHS) {
+  const int j = blockIdx.x;
+  const int kk = RH_PER_THREAD * (blockIdx.y * blockDim.x + threadIdx.x);
+  if (kk >= wk) return;
+  const int PH = prm->PH;
+  long long b[2][2][4];  // b[r][c][v]: block (r, c), the thread's 4 entries
+#pragma unroll
+  for (int c = 0; c < 2; ++c) {
+    const int col = j + c * wn;
+    const unsigned long long hb = hmax_bits[col];
+    const bool ok = hb > 0 && hb < INF_BITS;
+    const int e = ok ? scale_exp(hb, PH) : 0;
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+      double hv[4] = {0.0, 0.0, 0.0, 0.0};
+      if (ok) {
+        const double* src = Ht + (size_t)col * kp + r * wk + kk;
+        const double2 h01 = *(const double2*)src, h23 = *(const double2*)(src + 2);
+        hv[0] = h01.x; hv[1] = h01.y; hv[2] = h23.x; hv[3] = h23.y;
+      }
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        bool ng = false;
+        const long long u = ok ? (long long)scaled_int(hv[v], e, &ng) : 0ll;
+        b[r][c][v] = ng ? -u : u;
+      }
+    }
+  }
+  const size_t plane = (size_t)wn * wk;
+#pragma unroll
+  for (int y = 0; y < 7; ++y) {
+    ResidueChunks4 c4[4];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const long long V = y == 0 ? b[0][0][v] + b[1][1][v] : y == 1 ? b[0][0][v] : y == 2 ? b[0][1][v] - b[1][1][v]
+                        : y == 3 ? b[1][0][v] - b[0][0][v] : y == 4 ? b[1][1][v] : y == 5 ? b[0][0][v] + b[0][1][v]
+                                                                                        : b[1][0][v] + b[1][1][v];
+      c4[v] = residue_chunks4(V);
+    }
+    uint2* dst = (uint2*)(RHS + (size_t)y * cc.nmod * plane + (size_t)j * wk + kk);
+#pragma unroll
+    for (int l = 0; l < SPL_MAX_MODULI; ++l) {
+      if (l < cc.nmod) {
+        const float g14 = cc.g14[l], g28 = cc.g28[l], g42 = cc.g42[l], inv = cc.inv_m[l], mf = cc.mf[l];
+        unsigned f[4];
+#pragma unroll
+        for (int v = 0; v < 4; ++v) f[v] = __float_as_uint(residue4_f(c4[v], g14, g28, g42, inv, mf));
+        *dst = make_uint2(__byte_perm(f[0], f[1], 0x7632), __byte_perm(f[2], f[3], 0x7632));
+        dst += plane / 4;
+      }
     }
   }
 }
@@ -1257,11 +1327,11 @@ struct GemmArgs {
   // 0 stores the residues; 1 reads T1 where it stores and writes T1 - x there and -T1 - x at
   // +im_off bytes; 2 adds x to the residues already stored.
   int mode, im_off;
-  // Block-recursive products: modes 0 and 2 write each residue to ndst places, column offsets
-  // dst_col[d] (ndst = 0: one place, offset 0), and only the product's first ncols columns
-  // (ncols = 0: every column of the tile).
-  int ndst, ncols;
-  int dst_col[8];
+  // Block products (MULTI): each residue goes to ndst places, place d at row dst_row[d] and
+  // column dst_col[d] of planes of r_rows rows, stored (dst_op 0), added (2) or subtracted (3);
+  // only the product's first ncols columns are written (ncols = 0: every column of the tile).
+  int ndst, ncols, r_rows;
+  int dst_col[8], dst_row[8], dst_op[8];
   // gate != nullptr: the launch runs only when (*gate != 0) == gate_set (the block-recursive
   // products and their single-product fallback, chosen on the device)
   const unsigned* gate;
@@ -1581,11 +1651,13 @@ __global__ void __launch_bounds__(G_THREADS, 1) k_crt_gemm(const __grid_constant
                                 ((uint32_t)(uint8_t)(int8_t)res[4 * e4 + 3] << 24);
             asm volatile("mov.b32 %0, %1;" : "=r"(pk[e4]) : "r"(pv));
           }
-          int8_t* row = ti.R + ((size_t)ti.l * ti.n + i) * ti.kr + (size_t)col0;
           const int nd = g.ndst > 0 ? g.ndst : 1;
+          const size_t plane_rows = g.r_rows > 0 ? (size_t)g.r_rows : (size_t)ti.n;
           for (int d = 0; d < nd; ++d) {
-            int8_t* dst = row + (g.ndst > 0 ? g.dst_col[d] : 0);
-            if (g.mode == 2) {
+            int8_t* dst = ti.R + ((size_t)ti.l * plane_rows + i + (g.ndst > 0 ? g.dst_row[d] : 0)) * ti.kr +
+                          (size_t)col0 + (g.ndst > 0 ? g.dst_col[d] : 0);
+            const int op = g.ndst > 0 ? g.dst_op[d] : g.mode;
+            if (op >= 2) {
               uint4 o[HALF / 16];
 #pragma unroll
               for (int v = 0; v < HALF / 16; ++v)
@@ -1600,7 +1672,8 @@ __global__ void __launch_bounds__(G_THREADS, 1) k_crt_gemm(const __grid_constant
                   nw[t4] = 0u;
 #pragma unroll
                   for (int bb = 0; bb < 4; ++bb) {
-                    const int a = (int)(int8_t)(ow[t4] >> (8 * bb)) + (int)(int8_t)(pk[4 * v + t4] >> (8 * bb));
+                    const int x = (int)(int8_t)(pk[4 * v + t4] >> (8 * bb));
+                    const int a = (int)(int8_t)(ow[t4] >> (8 * bb)) + (op == 3 ? -x : x);
                     nw[t4] |= (uint32_t)(uint8_t)(int8_t)mod_sym_small(a, mi) << (8 * bb);
                   }
                 }
@@ -2271,8 +2344,11 @@ static int block_levels(int kind, int N, int K, int req) {
   return L;
 }
 
+static bool s2_use(int kind, int M, int K, int N, int req);
+
 extern "C" int psmma_split_block_levels(int kind, int n, int k) {
-  return (n > 0 && k > 0) ? block_levels(kind, k, k, 0) : 0;
+  if (n <= 0 || k <= 0) return 0;
+  return (kind == KIND_TOEPLITZ || kind == KIND_HANKEL) ? block_levels(kind, k, k, 0) : (s2_use(kind, n, k, k, 0) ? 1 : 0);
 }
 
 static int ipow3(int L) { return L == 0 ? 1 : 3 * ipow3(L - 1); }
@@ -2341,6 +2417,8 @@ static int split_core_block(int M, int N, int L, double alpha, const double* A, 
   // A operands: one block (a view of RA) or a sum plane (RS), numbered in leaf order
   BlockSums bs;
   memset(&bs, 0, sizeof(bs));
+  for (int q = 0; q < NQ; ++q) bs.qcol[q] = q * w;  // column blocks of every row
+  bs.wmask = (1 << NQ) - 1;
   std::vector<int> a_sum(nleaf, -1);
   for (int y = 0; y < nleaf; ++y) {
     const int mk = leaves[y].amask;
@@ -2384,15 +2462,18 @@ static int split_core_block(int M, int N, int L, double alpha, const double* A, 
     if (NQ == 2) {
       e = set_smem_attr(k_residues_A_blocks<2>, smem);
       if (e == cudaSuccess)
-        k_residues_A_blocks<2><<<ga, 256, smem, stream>>>(A, lda, M, w, Lo.kp, b.amax, b.prm, cc, b.RA, RS, bs);
+        k_residues_A_blocks<2><<<ga, 256, smem, stream>>>(A, lda, M, 0, M, w, Lo.kp, b.amax, b.prm, cc, b.RA, RS,
+                                                           bs);
     } else if (NQ == 4) {
       e = set_smem_attr(k_residues_A_blocks<4>, smem);
       if (e == cudaSuccess)
-        k_residues_A_blocks<4><<<ga, 256, smem, stream>>>(A, lda, M, w, Lo.kp, b.amax, b.prm, cc, b.RA, RS, bs);
+        k_residues_A_blocks<4><<<ga, 256, smem, stream>>>(A, lda, M, 0, M, w, Lo.kp, b.amax, b.prm, cc, b.RA, RS,
+                                                           bs);
     } else {
       e = set_smem_attr(k_residues_A_blocks<8>, smem);
       if (e == cudaSuccess)
-        k_residues_A_blocks<8><<<ga, 256, smem, stream>>>(A, lda, M, w, Lo.kp, b.amax, b.prm, cc, b.RA, RS, bs);
+        k_residues_A_blocks<8><<<ga, 256, smem, stream>>>(A, lda, M, 0, M, w, Lo.kp, b.amax, b.prm, cc, b.RA, RS,
+                                                           bs);
     }
     if (e != cudaSuccess) return PSMMA_EDEVICE;
   }
@@ -2400,11 +2481,11 @@ static int split_core_block(int M, int N, int L, double alpha, const double* A, 
   {
     const dim3 gh(w, rh_blocks_x(w), nleaf);
     if (NQ == 2)
-      k_residues_H_leaf<2><<<gh, 128, 0, stream>>>(b.Ht, Lo.kp, w, b.hmax, gmax, b.prm, cc, lt, b.RH);
+      k_residues_H_leaf<2><<<gh, 128, 0, stream>>>(b.Ht, Lo.kp, w, w, b.hmax, gmax, 1, b.prm, cc, lt, b.RH);
     else if (NQ == 4)
-      k_residues_H_leaf<4><<<gh, 128, 0, stream>>>(b.Ht, Lo.kp, w, b.hmax, gmax, b.prm, cc, lt, b.RH);
+      k_residues_H_leaf<4><<<gh, 128, 0, stream>>>(b.Ht, Lo.kp, w, w, b.hmax, gmax, 1, b.prm, cc, lt, b.RH);
     else
-      k_residues_H_leaf<8><<<gh, 128, 0, stream>>>(b.Ht, Lo.kp, w, b.hmax, gmax, b.prm, cc, lt, b.RH);
+      k_residues_H_leaf<8><<<gh, 128, 0, stream>>>(b.Ht, Lo.kp, w, w, b.hmax, gmax, 1, b.prm, cc, lt, b.RH);
     k_residues_H_gated<<<dim3(std::min(N, 608), rh_blocks_x(Lo.kp)), 128, 0, stream>>>(b.Ht, N, Lo.kp, b.hmax,
                                                                                         b.prm, cc, b.RH);
   }
@@ -2442,9 +2523,11 @@ static int split_core_block(int M, int N, int L, double alpha, const double* A, 
     ga.R = b.R;
     ga.status = &b.prm->status;
     for (int l = 0; l < nmod; ++l) { ga.m[l] = cc.m[l]; ga.inv_m[l] = cc.inv_m[l]; }
-    ga.mode = y == 0 ? 0 : 2;  // the first leaf covers every block (block_expand takes the sums first)
     ga.ndst = lf.ndst;
-    for (int d = 0; d < lf.ndst; ++d) ga.dst_col[d] = lf.dst[d] * w;
+    for (int d = 0; d < lf.ndst; ++d) {
+      ga.dst_col[d] = lf.dst[d] * w;
+      ga.dst_op[d] = y == 0 ? 0 : 2;  // the first leaf covers every block (block_expand takes the sums first)
+    }
     ga.ncols = w;
     ga.gate = &b.prm->hbad;
     ga.gate_set = 0;
@@ -2477,6 +2560,199 @@ static int split_core_block(int M, int N, int L, double alpha, const double* A, 
   dim3 gc((N + CRT_TJ - 1) / CRT_TJ, (M + CRT_TI - 1) / CRT_TI);
   (cc.top32 ? k_crt_combine_blocks<true> : k_crt_combine_blocks<false>)<<<gc, dim3(32, 8), 0, stream>>>(
       b.R, M, N, Lo.kr, cc, b.amax, b.hmax, gmax, w, b.prm, alpha, beta, Q, ldq);
+  prof_mark(stream, "crt_combine");
+  if (cudaGetLastError() != cudaSuccess) return PSMMA_EDEVICE;
+  return split_status(b.prm, stream, status_dev_out);
+}
+
+// ---- Strassen's step on the residue planes -----------------------------------------------
+// Over any ring, the 2 x 2 block product C = A B takes seven block products instead of eight:
+//   M1 = (A00 + A11)(B00 + B11)   M2 = (A10 + A11) B00   M3 = A00 (B01 - B11)   M4 = A11 (B10 - B00)
+//   M5 = (A00 + A01) B11          M6 = (A10 - A00)(B00 + B01)                   M7 = (A01 - A11)(B10 + B11)
+//   C00 = M1 + M4 - M5 + M7   C01 = M3 + M5   C10 = M2 + M4   C11 = M1 - M2 + M3 + M6.
+// Applied to the residue planes of the integer-scaled A' (rows of a panel, columns K) and H'
+// modulo each m_l, it is exact and needs no structure: the recombined Z = A'H' is the same
+// integer matrix, so the result is the single product's bit for bit, with 7/8 of its modular
+// GEMM work.  A blocks are numbered q = 2 row-block + column-block; H blocks (r, c) are the row
+// (k) and column blocks.  Products run in this order; each output block's first contribution
+// stores and has a positive sign, the later ones add or subtract.
+struct S2Prod {
+  int amask, aneg;           // A blocks summed / subtracted
+  int nh, hs[2], hr[2], hc[2];  // H terms
+  int nd, drb[2], dcb[2], dop[2];  // output blocks (row block, column block), operation
+};
+static const S2Prod kStrassen[7] = {
+    {0x9, 0x0, 2, {1, 1}, {0, 1}, {0, 1}, 2, {0, 1}, {0, 1}, {0, 0}},   // M1 -> C00, C11 (stores)
+    {0xC, 0x0, 1, {1, 0}, {0, 0}, {0, 0}, 2, {1, 1}, {0, 1}, {0, 3}},   // M2 -> C10 (store), C11 -
+    {0x1, 0x0, 2, {1, -1}, {0, 1}, {1, 1}, 2, {0, 1}, {1, 1}, {0, 2}},  // M3 -> C01 (store), C11 +
+    {0x8, 0x0, 2, {1, -1}, {1, 0}, {0, 0}, 2, {0, 1}, {0, 0}, {2, 2}},  // M4 -> C00 +, C10 +
+    {0x3, 0x0, 1, {1, 0}, {1, 0}, {1, 0}, 2, {0, 0}, {0, 1}, {3, 2}},   // M5 -> C00 -, C01 +
+    {0x5, 0x1, 2, {1, 1}, {0, 0}, {0, 1}, 1, {1, 0}, {1, 0}, {2, 0}},   // M6 -> C11 +
+    {0xA, 0x8, 2, {1, 1}, {1, 1}, {0, 1}, 1, {0, 0}, {0, 0}, {2, 0}},   // M7 -> C00 +
+};
+
+// Strassen's step for a product of M rows, K inner, N columns: M even, K and N multiples of
+// 128 (block widths of whole 64-column k blocks, 16-byte output offsets).  Only on request
+// (psmma_opts::block_levels = 1): its operands take 7/4 of the residue planes' HBM traffic, and
+// at n = 16384 those passes cost about what the eighth of the modular GEMM work saves.
+static bool s2_fits(int M, int K, int N) { return M % 2 == 0 && K % 128 == 0 && N % 128 == 0 && M >= 2; }
+// Strassen's step is for the unstructured kinds (Toeplitz and Hankel take their own block step).
+static bool s2_use(int kind, int M, int K, int N, int req) {
+  if (kind != KIND_CAUCHY && kind != KIND_CAUCHY_EIG && kind != KIND_DENSE) return false;
+  return req > 0 && s2_fits(M, K, N);
+}
+
+// Workspace: the split layout with the H residues replaced by the seven H operands (N/2 x K/2
+// each) and the five A block sums (rows / 2 x K/2 each) of a pass over `rows` rows.
+static SplitLayout s2_layout(int M, int K, int N, int rows, int nmod) {
+  SplitLayout B = split_layout(M, K, N, nmod);
+  const size_t rh = al1k((size_t)7 * nmod * (N / 2) * (K / 2) * 2);
+  const size_t rs = al1k((size_t)5 * nmod * (rows / 2) * (K / 2) * 2);
+  // split_layout's H residue region [off_rh, off_r) becomes the H operands, then the sums
+  const size_t tail = B.total - B.off_r;
+  B.off_rs = B.off_rh + rh;
+  const size_t off_r = B.off_rs + rs;
+  B.total = off_r + tail;
+  B.off_r = off_r;
+  return B;
+}
+
+// Prepared state of Strassen's step for one call: operand numbering and the constant parts of
+// the seven GEMM launches.
+struct S2State {
+  int M, K, N, nmod, kp, kr, sms;
+  __nv_bfloat16 *RA, *RS, *RHL;
+  int8_t* R;
+  unsigned* status;
+  int a_sum[7];  // A operand: sum plane index, or -1 for a block of RA
+  BlockSums bs;  // qrow filled per pass
+  CrtConsts cc;
+};
+
+static void s2_prepare(S2State& st) {
+  memset(&st.bs, 0, sizeof(st.bs));
+  for (int y = 0; y < 7; ++y) {
+    const int mk = kStrassen[y].amask;
+    st.a_sum[y] = -1;
+    if ((mk & (mk - 1)) == 0 && kStrassen[y].aneg == 0) continue;
+    st.a_sum[y] = st.bs.nsum;
+    st.bs.mask[st.bs.nsum] = mk;
+    st.bs.neg[st.bs.nsum] = kStrassen[y].aneg;
+    ++st.bs.nsum;
+  }
+  for (int q = 0; q < 4; ++q) st.bs.qcol[q] = (q & 1) * (st.K / 2);
+  for (int y = 0; y < 7; ++y)
+    if (st.a_sum[y] < 0) st.bs.wmask |= kStrassen[y].amask;  // A00 and A11: read in place
+}
+
+// The seven H operands from Ht, in the order of kStrassen (k_residues_H_s2 writes that order).
+static void s2_h_operands(const S2State& st, const double* Ht, const unsigned long long* hmax, const SplitDevParams* prm,
+                          cudaStream_t stream) {
+  const dim3 gh(st.N / 2, rh_blocks_x(st.K / 2));
+  k_residues_H_s2<<<gh, 128, 0, stream>>>(Ht, st.kp, st.K / 2, st.N / 2, hmax, prm, st.cc, st.RHL);
+}
+
+// Rows [r0, r0 + P) (P even) of A: block residues and sums, then the seven products into the
+// residue planes of R.  pk: the bit counts to scale A with.
+static int s2_pass(S2State& st, const double* A, long lda, const unsigned long long* amax, const SplitDevParams* pk,
+                   int r0, int P, cudaStream_t stream) {
+  const int h = P / 2, wk = st.K / 2, wn = st.N / 2;
+  BlockSums bs = st.bs;
+  for (int q = 0; q < 4; ++q) bs.qrow[q] = (q >> 1) * h;
+  const int smem = 4 * 64 * 32 * 8;
+  if (set_smem_attr(k_residues_A_blocks<4>, smem) != cudaSuccess) return PSMMA_EDEVICE;
+  k_residues_A_blocks<4><<<dim3(wk / 64, (h + 31) / 32), 256, smem, stream>>>(A, lda, st.M, r0, h, wk, st.kp, amax, pk,
+                                                                               st.cc, st.RA, st.RS, bs);
+  prof_mark(stream, "residues_A");
+  using Shape = GemmShape<G_BN>;
+  if (set_smem_attr(k_crt_gemm<G_BN, OneGemm, true>, (int)Shape::SMEM) != cudaSuccess) return PSMMA_EDEVICE;
+  for (int y = 0; y < 7; ++y) {
+    const S2Prod& pr = kStrassen[y];
+    OneGemm og;
+    memset(&og, 0, sizeof(og));
+    bool ok;
+    if (st.a_sum[y] < 0) {
+      const int q = __builtin_ctz(pr.amask);
+      ok = make_tmap_view(&og.ta, st.RA + (size_t)(r0 + (q >> 1) * h) * st.kp + (q & 1) * wk, wk, st.kp, h, st.nmod,
+                          (long)st.M * st.kp, G_BM);
+    } else {
+      ok = make_tmap_view(&og.ta, st.RS + (size_t)st.a_sum[y] * st.nmod * h * wk, wk, wk, h, st.nmod, (long)h * wk,
+                          G_BM);
+    }
+    ok = ok && make_tmap_view(&og.tb, st.RHL + (size_t)y * st.nmod * wn * wk, wk, wk, wn, st.nmod, (long)wn * wk, G_BN);
+    if (!ok) return PSMMA_EDEVICE;
+    GemmArgs& ga = og.g;
+    ga.n = h;
+    ga.kr = st.kr;
+    ga.nkb = wk / G_BK;
+    ga.tiles_m = (h + G_BM - 1) / G_BM;
+    ga.tiles_n = (wn + G_BN - 1) / G_BN;
+    ga.group_m = 16;
+    ga.nmod = st.nmod;
+    ga.R = st.R;
+    ga.status = st.status;
+    for (int l = 0; l < st.nmod; ++l) { ga.m[l] = st.cc.m[l]; ga.inv_m[l] = st.cc.inv_m[l]; }
+    ga.ncols = wn;
+    ga.r_rows = st.M;
+    ga.ndst = pr.nd;
+    for (int d = 0; d < pr.nd; ++d) {
+      ga.dst_row[d] = r0 + pr.drb[d] * h;
+      ga.dst_col[d] = pr.dcb[d] * wn;
+      ga.dst_op[d] = pr.dop[d];
+    }
+    const int total_tiles = ga.tiles_m * ga.tiles_n * st.nmod;
+    k_crt_gemm<G_BN, OneGemm, true><<<std::min(st.sms, total_tiles), G_THREADS, Shape::SMEM, stream>>>(og);
+    prof_mark(stream, "modular_gemm");
+  }
+  return cudaGetLastError() == cudaSuccess ? PSMMA_OK : PSMMA_EDEVICE;
+}
+
+// Device-pointer split multiply with Strassen's step over all M rows.
+static int split_core_s2(int M, int N, int K, double alpha, const double* A, long lda, const GenSpec& gs, double beta,
+                         double* Q, long ldq, int nmod, void* work, size_t lwork, cudaStream_t stream,
+                         unsigned* status_dev_out) {
+  if (nmod < 8 || nmod > SPL_MAX_MODULI) return PSMMA_EUNSUPPORTED;
+  if (K >= (1 << 24) || M > kSplitMaxRows || N >= (1 << 30) || !s2_fits(M, K, N)) return PSMMA_EUNSUPPORTED;
+  const SplitLayout Lo = s2_layout(M, K, N, M, nmod);
+  if (lwork < Lo.total || !work) return PSMMA_EWORKSPACE;
+  char* wk = (char*)work;
+  const SplitBuffers b = split_buffers(wk, Lo);
+  S2State st;
+  st.M = M; st.K = K; st.N = N; st.nmod = nmod; st.kp = Lo.kp; st.kr = Lo.kr;
+  st.RA = b.RA; st.RS = (__nv_bfloat16*)(wk + Lo.off_rs); st.RHL = b.RH; st.R = b.R;
+  st.status = &b.prm->status;
+  st.cc = get_consts(nmod);
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&st.sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return PSMMA_EDEVICE;
+  s2_prepare(st);
+
+  prof_begin(stream);
+  if (cudaMemsetAsync(wk, 0, Lo.off_wtab, stream) != cudaSuccess) return PSMMA_EDEVICE;
+  {
+    const int kchunk = 1024;
+    dim3 g1((M + 127) / 128, (K + kchunk - 1) / kchunk);
+    k_row_absmax<<<g1, 128, 0, stream>>>(A, lda, M, K, kchunk, b.amax, b.asq);
+  }
+  prof_mark(stream, "row_scale");
+  switch (gs.kind) {
+    case KIND_CAUCHY: k_h_pass1<KIND_CAUCHY><<<N, 256, 0, stream>>>(gs, K, Lo.kp, b.Ht, b.hmax, b.hsum, b.hsq, b.prm); break;
+    case KIND_TOEPLITZ: k_h_pass1<KIND_TOEPLITZ><<<N, 256, 0, stream>>>(gs, K, Lo.kp, b.Ht, b.hmax, b.hsum, b.hsq, b.prm); break;
+    case KIND_HANKEL: k_h_pass1<KIND_HANKEL><<<N, 256, 0, stream>>>(gs, K, Lo.kp, b.Ht, b.hmax, b.hsum, b.hsq, b.prm); break;
+    case KIND_DENSE: k_h_pass1<KIND_DENSE><<<N, 256, 0, stream>>>(gs, K, Lo.kp, b.Ht, b.hmax, b.hsum, b.hsq, b.prm); break;
+    case KIND_CAUCHY_EIG: k_h_pass1<KIND_CAUCHY_EIG><<<N, 256, 0, stream>>>(gs, K, Lo.kp, b.Ht, b.hmax, b.hsum, b.hsq, b.prm); break;
+    default: return PSMMA_EUNSUPPORTED;
+  }
+  prof_mark(stream, "h_generate");
+  k_split_params<<<PARAMS_BLOCKS, 512, 0, stream>>>(b.prm, st.cc.log2M, M, N, K, b.amax, b.asq, b.hmax, b.hsq);
+  prof_mark(stream, "params");
+  s2_h_operands(st, b.Ht, b.hmax, b.prm, stream);
+  prof_mark(stream, "residues_H");
+  const int rc = s2_pass(st, A, lda, b.amax, b.prm, 0, M, stream);
+  if (rc != PSMMA_OK) return rc;
+  dim3 gc((N + CRT_TJ - 1) / CRT_TJ, (M + CRT_TI - 1) / CRT_TI);
+  (st.cc.top32 ? k_crt_combine<false, true> : k_crt_combine<false, false>)<<<gc, dim3(32, 8), 0, stream>>>(
+      b.R, M, N, Lo.kr, st.cc, b.amax, b.hmax, b.prm, alpha, beta, Q, ldq, 0);
   prof_mark(stream, "crt_combine");
   if (cudaGetLastError() != cudaSuccess) return PSMMA_EDEVICE;
   return split_status(b.prm, stream, status_dev_out);
@@ -2864,13 +3140,18 @@ int launch_split_any(int kind, int n, int k, double alpha, const double* A, long
   const int L = block_levels(kind, k, k, block_req);
   if (L > 0 && gs.k1 == 0)
     return split_core_block(n, k, L, alpha, A, lda, gs, beta, Q, ldq, nmod, work, lwork, stream, status_dev_out);
+  if (s2_use(kind, n, k, k, block_req) && gs.k1 == 0)
+    return split_core_s2(n, k, k, alpha, A, lda, gs, beta, Q, ldq, nmod, work, lwork, stream, status_dev_out);
   return split_core(n, k, k, alpha, A, lda, gs, beta, Q, ldq, nmod, work, lwork, stream, status_dev_out);
 }
 
 int launch_split_general(int M, int N, int K, double alpha, const double* A, long lda, const GenSpec& gs,
                          double beta, double* Q, long ldq, int n_moduli, void* work, size_t lwork,
-                         cudaStream_t stream, unsigned* status_dev_out) {
+                         cudaStream_t stream, unsigned* status_dev_out, int block_req) {
   if (gs.kind == KIND_DFT) return PSMMA_EUNSUPPORTED;
+  if (s2_use(KIND_CAUCHY_EIG, M, K, N, block_req) && gs.k1 == 0)
+    return split_core_s2(M, N, K, alpha, A, lda, gs, beta, Q, ldq, resolve_nmod(n_moduli), work, lwork, stream,
+                         status_dev_out);
   return split_core(M, N, K, alpha, A, lda, gs, beta, Q, ldq, resolve_nmod(n_moduli), work, lwork, stream,
                     status_dev_out);
 }

@@ -99,14 +99,19 @@ def test_split_block_levels_rule(lib):
         assert [lib.psmma_split_block_levels(kind, 100, k) for k in ks] == [0, 0, 0, 0, 1, 0, 1, 2, 2, 2, 0]
     for kind in (_lib.KIND_CAUCHY, _lib.KIND_DFT):
         assert [lib.psmma_split_block_levels(kind, 100, k) for k in ks] == [0] * len(ks)
+    # Cauchy (and CAUCHYEIG): Strassen's step only on request, never automatically
+    assert [lib.psmma_split_block_levels(_lib.KIND_CAUCHY, k, k) for k in ks] == [0] * len(ks)
+    assert lib.psmma_split_block_levels(5, 4096, 8192) == 0
     # the workspace covers the block step's operands and the single product's, for the
     # automatic choice and for levels asked for by opts->block_levels
     from psmma_git_gb300 import workspace_size
     for k, lv in ((8192, 0), (16384, 0), (2048, 2), (1536, 3), (4096, -1)):
-        plain = workspace_size(_lib.KIND_CAUCHY, 4096, k, precision="split")
+        plain = workspace_size(_lib.KIND_TOEPLITZ, 4096, k, precision="split", block_levels=-1)
         assert workspace_size(_lib.KIND_TOEPLITZ, 4096, k, precision="split", block_levels=lv) >= plain
     assert workspace_size(_lib.KIND_HANKEL, 4096, 2048, precision="split", block_levels=2) > \
         workspace_size(_lib.KIND_HANKEL, 4096, 2048, precision="split", block_levels=-1)
+    assert workspace_size(_lib.KIND_CAUCHY, 4096, 2048, precision="split", block_levels=1) > \
+        workspace_size(_lib.KIND_CAUCHY, 4096, 2048, precision="split", block_levels=-1)
 
 
 def test_fortran_module_binds_declared_and_exported_symbols(lib):

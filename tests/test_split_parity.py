@@ -268,6 +268,46 @@ def test_split_block_step_graded_generator_keeps_column_accuracy(kind, cuda):
     assert O.col_max_rel(got, ref) < TOL
 
 
+@pytest.mark.parametrize("n,k,levels,pad", [(1000, 2048, 1, 3), (4096, 4096, 1, 0), (258, 1536, 1, 7),
+                                            (8192, 8192, 1, 0)])
+def test_split_strassen_step_same_result_as_single_product(n, k, levels, pad, cuda):
+    # Strassen's step on the residue planes (opts->block_levels = 1) computes the same integer
+    # product, so the result is the single product's bit for bit: half-row counts that are not
+    # whole tiles (500, 129), padded leading dimensions, alpha and beta
+    A = O.cfg_matrix(n, k, seed=n + 5)
+    gen = _gen("cauchy", k, seed=k + 6, clustered=0.05)
+    Q0 = O.cfg_matrix(n, k, seed=n + 7)
+    one = _split("cauchy", n, k, 0.75, A, gen, -1.5, Q0, cuda, ld_pad=pad, block_levels=-1)
+    got = _split("cauchy", n, k, 0.75, A, gen, -1.5, Q0, cuda, ld_pad=pad, block_levels=levels)
+    np.testing.assert_array_equal(got, one)
+    if n <= 1000:
+        assert O.rel_fro(got, O.dense_product("cauchy", 0.75, A, gen, -1.5, Q0, k)) < TOL
+
+
+def test_split_strassen_step_nonfinite_row_and_eig_kind(cuda):
+    # a non-finite row of A stays a NaN row (the others match the single product), and the
+    # accurate-denominator kind takes the same step
+    import psmma_git_gb300 as P
+    import torch
+    n, k = 2048, 2048
+    A = O.cfg_matrix(n, k, seed=51)
+    A[1500, 3] = np.inf
+    gen = _gen("cauchy", k, seed=52)
+    one = _split("cauchy", n, k, 1.0, A, gen, 0.0, np.zeros((n, k)), cuda, block_levels=-1)
+    got = _split("cauchy", n, k, 1.0, A, gen, 0.0, np.zeros((n, k)), cuda, block_levels=1)
+    assert np.isnan(got[1500]).all()
+    np.testing.assert_array_equal(np.delete(got, 1500, axis=0), np.delete(one, 1500, axis=0))
+    eig = [torch.from_numpy(np.ascontiguousarray(x)).to(cuda) for x in O.eig_generators(k, seed=53, tiny=k // 100)]
+    dA = _t(O.cfg_matrix(n, k, seed=54), cuda)
+    outs = []
+    for lv in (-1, 1):
+        dQ = P.fortran_empty(n, k, torch.float64, cuda)
+        P.psmma_cauchyeig(n, k, 1.0, dA, *eig, 0.0, dQ, precision="split", block_levels=lv)
+        torch.cuda.synchronize()
+        outs.append(dQ)
+    assert torch.equal(outs[0], outs[1])
+
+
 def _split_dft(n, k, alpha, B, beta, C0, cuda, n_moduli=0, variant="pzmdftl"):
     import psmma_git_gb300 as P
     import torch
