@@ -71,7 +71,7 @@ typedef struct psmma_opts {
   size_t lwork;       /* size of `work` in bytes                                               */
   int    block_levels; /* split path: Toeplitz / Hankel: levels of the block step (see
                           psmma_split_block_levels): 0 = automatic, -1 = none (one product),
-                          1..3 = that many (fewer where k is not divisible by 64 * 2^L);
+                          1..3 = that many (k padded to a multiple of 64 * 2^L);
                           Cauchy / CAUCHYEIG: 1 = Strassen's step on the residue planes
                           (n even, k divisible by 128; the same result bit for bit, seven
                           half-size modular products instead of eight), else none        */
@@ -152,9 +152,13 @@ int psmma_split_dft_radix(int n);
  * structure (Toeplitz: Y11 = Y00; Hankel: Y10 = Y01) turns the four block products into three,
  * (X1 + X2) Y00, X2 (Y10 - Y00) and X1 (Y01 - Y00) for Toeplitz; L levels give 3^L products of
  * width w = k / 2^L, (3/4)^L of the modular GEMM work, in exact modular arithmetic.  Columns j
- * and j + c w share one scaling exponent.  This returns the automatic choice
- * (opts->block_levels = 0): the largest L up to 2 with k divisible by 64 * 2^L and w >= 4096
- * (smaller leaves make the modular GEMMs' per-tile epilogue outweigh their MMAs).  The
+ * and j + c w share one scaling exponent.  Where 64 * 2^L does not divide k, the product runs
+ * on an order k' padded up to a multiple of it: H extended with the generator read as zero
+ * beyond its 2k - 1 entries (still Toeplitz / Hankel), A with zero columns, and only the first
+ * k columns of Q written.  This returns the automatic choice (opts->block_levels = 0): the L
+ * in {1, 2} with w = k' / 2^L >= 4096 that minimises the modular GEMM work (k'/k)^2 (3/4)^L,
+ * if that is at most 0.85, else 0 (smaller leaves make the modular GEMMs' per-tile epilogue
+ * outweigh their MMAs).  The
  * device-pointer calls and the server take the step; the host-pointer calls keep the single
  * product.  On the device, without a synchronisation, the call takes the single product
  * instead when an entry of H is not finite (NaN then appears in exactly the columns it does

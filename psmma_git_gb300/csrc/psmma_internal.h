@@ -30,6 +30,12 @@ struct GenSpec {
   const double *Dr = nullptr, *Ur = nullptr, *Fc = nullptr, *Vc = nullptr;
   const double* g = nullptr;
   long order = 0;
+  // glen > 0: Toeplitz / Hankel indices outside [0, glen) read zero (an H padded beyond the
+  // generator's k x k, still Toeplitz / Hankel: the split path's padded block step)
+  long glen = 0;
+  // srows > 0: only rows [0, srows) count in the column statistics (the rows of a padded H past
+  // the real ones multiply zero columns of A)
+  long srows = 0;
   const double2* wtab = nullptr;
   int n_dft = 0;
   const double* B = nullptr;

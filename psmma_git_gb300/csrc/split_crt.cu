@@ -150,7 +150,7 @@ struct SplitLayout {
   int kp, kr;
   size_t off_params, off_amax, off_hmax, off_hsum, off_asq, off_hsq, off_wtab, off_ht, off_ra, off_rh, off_r,
       total;
-  size_t off_rs = 0, off_gmax = 0;  // block-recursive products: A block sums, group column maxima
+  size_t off_rs = 0, off_gmax = 0, off_hall = 0;  // block products: A block sums, group / all-row column maxima
 };
 
 // M rows of A (and Q), K inner length, N columns of H (and Q).
@@ -233,7 +233,10 @@ static DftRadixLayout dft_radix_layout(int n, int k, int R, int nmod) {
   return D;
 }
 
-static int block_levels(int kind, int N, int K, int req);
+struct BlockChoice {  // levels of the Toeplitz / Hankel block step and the (padded) order
+  int L, Np;
+};
+static BlockChoice block_choice(int kind, int N, int K, int req);
 static SplitLayout block_layout(int M, int N, int L, int nmod);
 static bool s2_use(int kind, int M, int K, int N, int req);
 static SplitLayout s2_layout(int M, int K, int N, int rows, int nmod);
@@ -241,9 +244,9 @@ static SplitLayout s2_layout(int M, int K, int N, int rows, int nmod);
 size_t split_workspace_bytes(int kind, int n, int k, int n_moduli, int block_req) {
   if (n <= 0 || k <= 0) return 0;
   if (kind == KIND_TOEPLITZ || kind == KIND_HANKEL) {
-    const int L = block_levels(kind, k, k, block_req);
+    const BlockChoice bc = block_choice(kind, k, k, block_req);
     const size_t plain = split_layout(n, k, k, resolve_nmod(n_moduli)).total;
-    return L > 0 ? std::max(plain, block_layout(n, k, L, resolve_nmod(n_moduli)).total) : plain;
+    return bc.L > 0 ? std::max(plain, block_layout(n, bc.Np, bc.L, resolve_nmod(n_moduli)).total) : plain;
   }
   if (s2_use(kind, n, k, k, block_req))
     return std::max(split_layout(n, k, k, resolve_nmod(n_moduli)).total, s2_layout(n, k, k, n, resolve_nmod(n_moduli)).total);
@@ -359,9 +362,12 @@ __global__ void k_row_absmax(const double* __restrict__ A, long lda, int n, int 
 // H pass 1: Ht[j][kk] = H(kk, j) in FP64, column max |H| and column sum |H|, and the global
 // ratio rho = max_j sum/max over finite columns.  One block per column j.
 template <int KIND>
+// hmax_all != nullptr receives the column maximum over every generated row (with gs.srows the
+// statistics cover the first srows rows only).
 __device__ __forceinline__ void h_pass1_blk(const GenSpec& gs, int K, int kp, double* __restrict__ Ht,
                                             unsigned long long* __restrict__ hmax_bits, double* __restrict__ hsum,
-                                            double* __restrict__ hsq, SplitDevParams* prm, int j) {
+                                            double* __restrict__ hsq, SplitDevParams* prm, int j,
+                                            unsigned long long* __restrict__ hmax_all = nullptr) {
   double w = 0.0, v = 0.0, w1 = 0.0, dlj = 0.0, drj = 0.0;
   VSplit vs;
   vs.ok = false;
@@ -377,10 +383,11 @@ __device__ __forceinline__ void h_pass1_blk(const GenSpec& gs, int K, int kp, do
       drj = __ldg(gs.dr + j);  // DIFR(j)
     }
   }
-  unsigned long long mb = 0;
+  unsigned long long mb = 0, mb_all = 0;
   float s32 = 0.0f, s2_32 = 0.0f;
   int e = NO_SCALE;  // set by the thread's first nonzero entry
   bool big = false;
+  const long srows = gs.srows > 0 ? gs.srows : (long)kp;
   double* row = Ht + (long)j * kp;
   for (int kk = threadIdx.x; kk < kp; kk += blockDim.x) {
     double h = 0.0;
@@ -406,16 +413,20 @@ __device__ __forceinline__ void h_pass1_blk(const GenSpec& gs, int K, int kp, do
           h = cauchy_entry(u, v, vs, eig_den(fi, w, w1, dlj, drj, upper));
         }
       } else if (KIND == KIND_TOEPLITZ || KIND == KIND_HANKEL) {
-        if (gs.k1 > 0 && kk >= gs.k1)  // dense tail rows (the R P^T factor of a merged product)
+        if (gs.k1 > 0 && kk >= gs.k1) {  // dense tail rows (the R P^T factor of a merged product)
           h = __ldg(gs.B + (kk - gs.k1) + (long)j * gs.ldb);
-        else
-          h = KIND == KIND_TOEPLITZ ? __ldg(gs.g + (gs.order - 1) + j - kk) : __ldg(gs.g + kk + j);
+        } else {
+          const long idx = KIND == KIND_TOEPLITZ ? (gs.order - 1) + j - kk : (long)kk + j;
+          h = (gs.glen <= 0 || (idx >= 0 && idx < gs.glen)) ? __ldg(gs.g + idx) : 0.0;
+        }
       } else {  // KIND_DENSE (the split DFT generates F in k_h_pass1_dft3)
         h = __ldg(gs.B + kk + (long)j * gs.ldb);
       }
     }
     row[kk] = h;
     unsigned long long b = (unsigned long long)__double_as_longlong(h) & ABS_MASK;
+    mb_all = b > mb_all ? b : mb_all;
+    if (kk >= srows) continue;
     mb = b > mb ? b : mb;
     if (e == NO_SCALE && b) e = (int)(b >> 52) - 1023;
     if (e != NO_SCALE) {
@@ -426,7 +437,7 @@ __device__ __forceinline__ void h_pass1_blk(const GenSpec& gs, int K, int kp, do
   }
   double s = 0.0, s2 = 0.0;
   if (big) {  // entries 2^56 times the thread's first one (or Inf/NaN): FP64 sums
-    for (int kk = threadIdx.x; kk < kp; kk += blockDim.x) {
+    for (int kk = threadIdx.x; kk < srows; kk += blockDim.x) {
       const double h = row[kk];
       s += fabs(h);
       s2 = fma(h, h, s2);
@@ -435,29 +446,35 @@ __device__ __forceinline__ void h_pass1_blk(const GenSpec& gs, int K, int kp, do
     s = ldexp((double)s32, e);
     s2 = ldexp((double)s2_32, 2 * e);
   }
-  __shared__ unsigned long long smax[32];
+  __shared__ unsigned long long smax[32], smax_all[32];
   __shared__ double ssum[32], ssq[32];
   for (int o = 16; o > 0; o >>= 1) {
     unsigned long long ob = __shfl_xor_sync(0xffffffffu, mb, o);
     mb = ob > mb ? ob : mb;
+    ob = __shfl_xor_sync(0xffffffffu, mb_all, o);
+    mb_all = ob > mb_all ? ob : mb_all;
     s += __shfl_xor_sync(0xffffffffu, s, o);
     s2 += __shfl_xor_sync(0xffffffffu, s2, o);
   }
   int wid = threadIdx.x >> 5, ln = threadIdx.x & 31;
-  if (ln == 0) { smax[wid] = mb; ssum[wid] = s; ssq[wid] = s2; }
+  if (ln == 0) { smax[wid] = mb; smax_all[wid] = mb_all; ssum[wid] = s; ssq[wid] = s2; }
   __syncthreads();
   if (wid == 0) {
     int nw = blockDim.x >> 5;
     mb = ln < nw ? smax[ln] : 0ull;
+    mb_all = ln < nw ? smax_all[ln] : 0ull;
     s = ln < nw ? ssum[ln] : 0.0;
     s2 = ln < nw ? ssq[ln] : 0.0;
     for (int o = 16; o > 0; o >>= 1) {
       unsigned long long ob = __shfl_xor_sync(0xffffffffu, mb, o);
       mb = ob > mb ? ob : mb;
+      ob = __shfl_xor_sync(0xffffffffu, mb_all, o);
+      mb_all = ob > mb_all ? ob : mb_all;
       s += __shfl_xor_sync(0xffffffffu, s, o);
       s2 += __shfl_xor_sync(0xffffffffu, s2, o);
     }
     if (ln == 0) {
+      if (hmax_all) hmax_all[j] = mb_all;
       hmax_bits[j] = mb;
       hsum[j] = s;
       hsq[j] = s2;
@@ -474,6 +491,16 @@ __global__ void k_h_pass1(GenSpec gs, int K, int kp, double* __restrict__ Ht,
                           unsigned long long* __restrict__ hmax_bits, double* __restrict__ hsum,
                           double* __restrict__ hsq, SplitDevParams* prm) {
   h_pass1_blk<KIND>(gs, K, kp, Ht, hmax_bits, hsum, hsq, prm, blockIdx.x);
+}
+
+// The same, also writing the column maxima over every generated row (the block step's
+// exponents; hmax_bits then covers the first gs.srows rows).
+template <int KIND>
+__global__ void k_h_pass1_all(GenSpec gs, int K, int kp, double* __restrict__ Ht,
+                              unsigned long long* __restrict__ hmax_bits, double* __restrict__ hsum,
+                              double* __restrict__ hsq, SplitDevParams* prm,
+                              unsigned long long* __restrict__ hmax_all) {
+  h_pass1_blk<KIND>(gs, K, kp, Ht, hmax_bits, hsum, hsq, prm, blockIdx.x, hmax_all);
 }
 
 // Bits PA (rows of A) and PH (columns of H).  The integer product must satisfy
@@ -787,7 +814,8 @@ __global__ void k_guess_params(SplitDevParams* g, int PA, int PH) {
 __device__ __forceinline__ void residues_H_blk(const double* __restrict__ Ht, int ncols, int kp,
                                                const unsigned long long* __restrict__ hmax_bits,
                                                const SplitDevParams* prm, const CrtConsts& cc,
-                                               __nv_bfloat16* __restrict__ RH, int bx, int by, int ph = -1) {
+                                               __nv_bfloat16* __restrict__ RH, int bx, int by, int ph = -1,
+                                               int krows = 1 << 30) {
   const int j = by;
   const int kk = RH_PER_THREAD * (bx * blockDim.x + threadIdx.x);
   if (kk >= kp) return;  // kp is a multiple of 64: a thread's four entries are all inside
@@ -803,7 +831,7 @@ __device__ __forceinline__ void residues_H_blk(const double* __restrict__ Ht, in
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
     ng[q] = false;
-    u[q] = ok ? scaled_int(hv[q], e, &ng[q]) : 0ull;
+    u[q] = (ok && kk + q < krows) ? scaled_int(hv[q], e, &ng[q]) : 0ull;
   }
   const size_t plane = (size_t)ncols * kp;
   write_residue_quad(u, ng, cc, (uint2*)(RH + (size_t)j * kp + kk), plane / 4);
@@ -837,6 +865,7 @@ __global__ void k_residues_H_spec(const double* __restrict__ Ht, int ncols, int 
 // the non-finite columns) or when a nonzero column's maximum is more than 2^kBlockMaxSpread
 // below its group's (its entries would lose that many bits to the shared exponent).
 constexpr int kBlockMaxSpread = 4;
+// hmax_bits here: the maxima over every row of the (possibly padded) H.
 __global__ void k_group_colmax(const unsigned long long* __restrict__ hmax_bits,
                                unsigned long long* __restrict__ gmax_bits, int w, int nq, SplitDevParams* prm) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
@@ -868,13 +897,13 @@ struct BlockSums {
 
 // A residues of a block product: RA[l][r0 + qrow[q] + i][qcol[q] + kk] for every block q (as
 // k_residues_A writes them) and RS[p][l][i][kk] = the signed block sum p mod m_l, for i < rows,
-// kk < w.  Each block row keeps its own exponent (rows of different blocks are different rows of
+// kk < w; columns from kvalid on read as zero (A padded with zero columns).  Each block row keeps its own exponent (rows of different blocks are different rows of
 // A).  One CTA: 32 rows x 64 columns of each of the NQ blocks, transposed through shared memory
 // (NQ tiles of 64 x 32 doubles, the swizzle of residues_A_blk); each thread keeps the signed
 // scaled integers of its 4 columns of every block, so the sums need no second pass over A.
 template <int NQ>
 __global__ void __launch_bounds__(256) k_residues_A_blocks(const double* __restrict__ A, long lda, int M, int r0,
-                                                           int rows, int w, int kp,
+                                                           int rows, int w, int kp, int kvalid,
                                                            const unsigned long long* __restrict__ amax_bits,
                                                            const SplitDevParams* prm, CrtConsts cc,
                                                            __nv_bfloat16* __restrict__ RA,
@@ -890,7 +919,7 @@ __global__ void __launch_bounds__(256) k_residues_A_blocks(const double* __restr
       const long gi = (long)r0 + bs.qrow[q] + i0 + tx;
       const long gk = (long)bs.qcol[q] + k0 + kk;
       blk_tiles[(q * 64 + kk) * TR + ((tx + (kk >> 2)) & (TR - 1))] =
-          i0 + tx < rows ? __ldg(A + gk * lda + gi) : 0.0;
+          (i0 + tx < rows && gk < kvalid) ? __ldg(A + gk * lda + gi) : 0.0;
     }
   __syncthreads();
   const int P = prm->PA;
@@ -956,7 +985,8 @@ struct LeafTerms {
 };
 
 // RHL[y][l][j'][kk'] (pitch wk) from Ht: grid (wn columns j', kk' blocks of 512, leaves y); one
-// thread per 4 consecutive kk'.
+// thread per 4 consecutive kk'.  hmax_bits: maxima over every row of the columns read (a term of
+// an all-zero column is skipped).
 template <int NT>
 __global__ void __launch_bounds__(128) k_residues_H_leaf(const double* __restrict__ Ht, int kp, int wk, int wn,
                                                          const unsigned long long* __restrict__ hmax_bits,
@@ -1071,12 +1101,13 @@ __global__ void __launch_bounds__(128) k_residues_H_s2(const double* __restrict_
 
 // The residues of the whole H (as k_residues_H) when prm->hbad is set; columns j = blockIdx.x +
 // gridDim.x t.
-__global__ void k_residues_H_gated(const double* __restrict__ Ht, int ncols, int kp,
+// Rows from krows on (the padding of a padded H) get zero residues.
+__global__ void k_residues_H_gated(const double* __restrict__ Ht, int ncols, int kp, int krows,
                                    const unsigned long long* __restrict__ hmax_bits, const SplitDevParams* prm,
                                    CrtConsts cc, __nv_bfloat16* __restrict__ RH) {
   if (!prm->hbad) return;
   for (int j = blockIdx.x; j < ncols; j += gridDim.x)
-    residues_H_blk(Ht, ncols, kp, hmax_bits, prm, cc, RH, blockIdx.y, j);
+    residues_H_blk(Ht, ncols, kp, hmax_bits, prm, cc, RH, blockIdx.y, j, -1, krows);
 }
 
 // DFT A side: row i of the product (B^T) is column i of B, read contiguously (Bre = B as
@@ -2326,23 +2357,37 @@ static std::vector<BlkNode> block_leaves(int kind, int L) {
   return leaves;
 }
 
-// Leaves need w = N / 2^L to be a multiple of 64 (whole k blocks and 128-byte operand offsets).
-// req (psmma_opts::block_levels): 0 = automatic -- the largest L <= kBlockAutoLevels with
-// w >= kBlockMinLeaf: below that the modular GEMMs' per-tile epilogue (2 drains at k = 2048)
-// weighs about as much as their MMAs and the step stops paying; -1 = none; 1..3 = that many
-// levels, fewer where N is not divisible.
+// Leaves need w = Np / 2^L to be a multiple of 64 (whole k blocks and 128-byte operand offsets),
+// so an order N that 64 * 2^L does not divide is padded to Np: H extended by the zero-extended
+// generator (still Toeplitz / Hankel), A by zero columns, and only N columns recombined.
+// req (psmma_opts::block_levels): 0 = automatic -- the L <= kBlockAutoLevels with w >=
+// kBlockMinLeaf that minimises the GEMM work (Np / N)^2 (3/4)^L, if that is at most
+// kBlockMaxWork (below w = 4096 the modular GEMMs' per-tile epilogue, 2 drains at k = 2048,
+// weighs about as much as their MMAs and the step stops paying); -1 = none; 1..3 = that many
+// levels.
 constexpr int kBlockMinLeaf = 4096;
 constexpr int kBlockAutoLevels = 2;
-static int block_levels(int kind, int N, int K, int req) {
-  if ((kind != KIND_TOEPLITZ && kind != KIND_HANKEL) || N != K || req < 0) return 0;
-  int L = 0;
-  if (req == 0) {
-    while (L < kBlockAutoLevels && N % (64 << (L + 1)) == 0 && (N >> (L + 1)) >= kBlockMinLeaf) ++L;
-  } else {
-    while (L < std::min(req, BLK_MAX_LEVELS) && N % (64 << (L + 1)) == 0) ++L;
+constexpr double kBlockMaxWork = 0.85;
+static int round_up(int x, int m) { return (x + m - 1) / m * m; }
+static BlockChoice block_choice(int kind, int N, int K, int req) {
+  if ((kind != KIND_TOEPLITZ && kind != KIND_HANKEL) || N != K || req < 0 || N <= 0) return {0, N};
+  if (req > 0) {
+    const int L = std::min(req, BLK_MAX_LEVELS);
+    return {L, round_up(N, 64 << L)};
   }
-  return L;
+  BlockChoice best = {0, N};
+  double best_work = kBlockMaxWork;
+  for (int L = 1; L <= kBlockAutoLevels; ++L) {
+    const int Np = round_up(N, 64 << L);
+    const double work = (double)Np * Np / ((double)N * N) * std::pow(0.75, L);
+    if ((Np >> L) >= kBlockMinLeaf && work <= best_work) {
+      best = {L, Np};
+      best_work = work;
+    }
+  }
+  return best;
 }
+static int block_levels(int kind, int N, int K, int req) { return block_choice(kind, N, K, req).L; }
 
 static bool s2_use(int kind, int M, int K, int N, int req);
 
@@ -2377,6 +2422,7 @@ static SplitLayout block_layout(int M, int N, int L, int nmod) {
                 al1k((size_t)nmod * N * B.kp * 2));
   B.off_r = o;      o += al1k((size_t)nmod * M * B.kr);
   B.off_gmax = o;   o += al1k((size_t)w * 8);
+  B.off_hall = o;   o += al1k((size_t)N * 8);
   B.total = o;
   return B;
 }
@@ -2397,19 +2443,26 @@ static bool make_tmap_view(CUtensorMap* map, void* ptr, int inner, long pitch, i
 }
 
 // Q (M x N) = alpha * A (M x N) * H + beta * Q for Toeplitz / Hankel H (N x N) with L >= 1 levels
-// of the block step (block_levels).
-static int split_core_block(int M, int N, int L, double alpha, const double* A, long lda, const GenSpec& gs,
-                            double beta, double* Q, long ldq, int nmod, void* work, size_t lwork,
-                            cudaStream_t stream, unsigned* status_dev_out) {
+// of the block step on the order Np >= N (block_choice; padded when Np > N).
+static int split_core_block(int M, int N, int Np, int L, double alpha, const double* A, long lda,
+                            const GenSpec& gs_in, double beta, double* Q, long ldq, int nmod, void* work,
+                            size_t lwork, cudaStream_t stream, unsigned* status_dev_out) {
   if (nmod < 8 || nmod > SPL_MAX_MODULI) return PSMMA_EUNSUPPORTED;
-  if (N >= (1 << 24) || M > kSplitMaxRows || L < 1 || L > BLK_MAX_LEVELS) return PSMMA_EUNSUPPORTED;
-  const int w = N >> L, NQ = 1 << L;
-  const SplitLayout Lo = block_layout(M, N, L, nmod);
+  if (Np >= (1 << 24) || M > kSplitMaxRows || L < 1 || L > BLK_MAX_LEVELS || Np < N || Np % (64 << L) != 0)
+    return PSMMA_EUNSUPPORTED;
+  GenSpec gs = gs_in;
+  if (Np > N) {
+    gs.glen = 2L * N - 1;  // the padding reads the generator zero-extended
+    gs.srows = N;          // and only the real rows count in the column statistics
+  }
+  const int w = Np >> L, NQ = 1 << L;
+  const SplitLayout Lo = block_layout(M, Np, L, nmod);
   if (lwork < Lo.total || !work) return PSMMA_EWORKSPACE;
   char* wk = (char*)work;
   const SplitBuffers b = split_buffers(wk, Lo);
   __nv_bfloat16* RS = (__nv_bfloat16*)(wk + Lo.off_rs);
   unsigned long long* gmax = (unsigned long long*)(wk + Lo.off_gmax);
+  unsigned long long* hall = (unsigned long long*)(wk + Lo.off_hall);
   const CrtConsts cc = get_consts(nmod);
   const std::vector<BlkNode> leaves = block_leaves(gs.kind, L);
   const int nleaf = (int)leaves.size();
@@ -2448,12 +2501,12 @@ static int split_core_block(int M, int N, int L, double alpha, const double* A, 
   }
   prof_mark(stream, "row_scale");
   if (gs.kind == KIND_TOEPLITZ)
-    k_h_pass1<KIND_TOEPLITZ><<<N, 256, 0, stream>>>(gs, N, Lo.kp, b.Ht, b.hmax, b.hsum, b.hsq, b.prm);
+    k_h_pass1_all<KIND_TOEPLITZ><<<Np, 256, 0, stream>>>(gs, Np, Lo.kp, b.Ht, b.hmax, b.hsum, b.hsq, b.prm, hall);
   else
-    k_h_pass1<KIND_HANKEL><<<N, 256, 0, stream>>>(gs, N, Lo.kp, b.Ht, b.hmax, b.hsum, b.hsq, b.prm);
-  k_group_colmax<<<(w + 255) / 256, 256, 0, stream>>>(b.hmax, gmax, w, NQ, b.prm);
+    k_h_pass1_all<KIND_HANKEL><<<Np, 256, 0, stream>>>(gs, Np, Lo.kp, b.Ht, b.hmax, b.hsum, b.hsq, b.prm, hall);
+  k_group_colmax<<<(w + 255) / 256, 256, 0, stream>>>(hall, gmax, w, NQ, b.prm);
   prof_mark(stream, "h_generate");
-  k_split_params<<<PARAMS_BLOCKS, 512, 0, stream>>>(b.prm, cc.log2M, M, N, N, b.amax, b.asq, b.hmax, b.hsq);
+  k_split_params<<<PARAMS_BLOCKS, 512, 0, stream>>>(b.prm, cc.log2M, M, Np, Np, b.amax, b.asq, b.hmax, b.hsq);
   prof_mark(stream, "params");
   {
     const dim3 ga(w / 64, (M + 31) / 32);
@@ -2462,18 +2515,18 @@ static int split_core_block(int M, int N, int L, double alpha, const double* A, 
     if (NQ == 2) {
       e = set_smem_attr(k_residues_A_blocks<2>, smem);
       if (e == cudaSuccess)
-        k_residues_A_blocks<2><<<ga, 256, smem, stream>>>(A, lda, M, 0, M, w, Lo.kp, b.amax, b.prm, cc, b.RA, RS,
-                                                           bs);
+        k_residues_A_blocks<2><<<ga, 256, smem, stream>>>(A, lda, M, 0, M, w, Lo.kp, N, b.amax, b.prm, cc, b.RA,
+                                                           RS, bs);
     } else if (NQ == 4) {
       e = set_smem_attr(k_residues_A_blocks<4>, smem);
       if (e == cudaSuccess)
-        k_residues_A_blocks<4><<<ga, 256, smem, stream>>>(A, lda, M, 0, M, w, Lo.kp, b.amax, b.prm, cc, b.RA, RS,
-                                                           bs);
+        k_residues_A_blocks<4><<<ga, 256, smem, stream>>>(A, lda, M, 0, M, w, Lo.kp, N, b.amax, b.prm, cc, b.RA,
+                                                           RS, bs);
     } else {
       e = set_smem_attr(k_residues_A_blocks<8>, smem);
       if (e == cudaSuccess)
-        k_residues_A_blocks<8><<<ga, 256, smem, stream>>>(A, lda, M, 0, M, w, Lo.kp, b.amax, b.prm, cc, b.RA, RS,
-                                                           bs);
+        k_residues_A_blocks<8><<<ga, 256, smem, stream>>>(A, lda, M, 0, M, w, Lo.kp, N, b.amax, b.prm, cc, b.RA,
+                                                           RS, bs);
     }
     if (e != cudaSuccess) return PSMMA_EDEVICE;
   }
@@ -2481,20 +2534,18 @@ static int split_core_block(int M, int N, int L, double alpha, const double* A, 
   {
     const dim3 gh(w, rh_blocks_x(w), nleaf);
     if (NQ == 2)
-      k_residues_H_leaf<2><<<gh, 128, 0, stream>>>(b.Ht, Lo.kp, w, w, b.hmax, gmax, 1, b.prm, cc, lt, b.RH);
+      k_residues_H_leaf<2><<<gh, 128, 0, stream>>>(b.Ht, Lo.kp, w, w, hall, gmax, 1, b.prm, cc, lt, b.RH);
     else if (NQ == 4)
-      k_residues_H_leaf<4><<<gh, 128, 0, stream>>>(b.Ht, Lo.kp, w, w, b.hmax, gmax, 1, b.prm, cc, lt, b.RH);
+      k_residues_H_leaf<4><<<gh, 128, 0, stream>>>(b.Ht, Lo.kp, w, w, hall, gmax, 1, b.prm, cc, lt, b.RH);
     else
-      k_residues_H_leaf<8><<<gh, 128, 0, stream>>>(b.Ht, Lo.kp, w, w, b.hmax, gmax, 1, b.prm, cc, lt, b.RH);
-    k_residues_H_gated<<<dim3(std::min(N, 608), rh_blocks_x(Lo.kp)), 128, 0, stream>>>(b.Ht, N, Lo.kp, b.hmax,
+      k_residues_H_leaf<8><<<gh, 128, 0, stream>>>(b.Ht, Lo.kp, w, w, hall, gmax, 1, b.prm, cc, lt, b.RH);
+    k_residues_H_gated<<<dim3(std::min(Np, 608), rh_blocks_x(Lo.kp)), 128, 0, stream>>>(b.Ht, Np, Lo.kp, N, b.hmax,
                                                                                         b.prm, cc, b.RH);
   }
   prof_mark(stream, "residues_H");
 
-  constexpr int LBN = G_BN;
   using Shape = GemmShape<G_BN>;
-  using LShape = GemmShape<LBN>;
-  if (set_smem_attr(k_crt_gemm<LBN, OneGemm, true>, (int)LShape::SMEM) != cudaSuccess) return PSMMA_EDEVICE;
+  if (set_smem_attr(k_crt_gemm<G_BN, OneGemm, true>, (int)Shape::SMEM) != cudaSuccess) return PSMMA_EDEVICE;
   int dev = 0, sms = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
     return PSMMA_EDEVICE;
@@ -2510,14 +2561,14 @@ static int split_core_block(int M, int N, int L, double alpha, const double* A, 
     } else {
       ok = make_tmap_view(&og.ta, RS + (size_t)a_sum[y] * nmod * M * w, w, w, M, nmod, (long)M * w, G_BM);
     }
-    ok = ok && make_tmap_view(&og.tb, b.RH + (size_t)y * nmod * w * w, w, w, w, nmod, (long)w * w, LBN);
+    ok = ok && make_tmap_view(&og.tb, b.RH + (size_t)y * nmod * w * w, w, w, w, nmod, (long)w * w, G_BN);
     if (!ok) return PSMMA_EDEVICE;
     GemmArgs& ga = og.g;
     ga.n = M;
     ga.kr = Lo.kr;
     ga.nkb = w / G_BK;
     ga.tiles_m = (M + G_BM - 1) / G_BM;
-    ga.tiles_n = (w + LBN - 1) / LBN;
+    ga.tiles_n = (w + G_BN - 1) / G_BN;
     ga.group_m = 16;
     ga.nmod = nmod;
     ga.R = b.R;
@@ -2532,20 +2583,20 @@ static int split_core_block(int M, int N, int L, double alpha, const double* A, 
     ga.gate = &b.prm->hbad;
     ga.gate_set = 0;
     const int total_tiles = ga.tiles_m * ga.tiles_n * nmod;
-    k_crt_gemm<LBN, OneGemm, true><<<std::min(sms, total_tiles), G_THREADS, LShape::SMEM, stream>>>(og);
+    k_crt_gemm<G_BN, OneGemm, true><<<std::min(sms, total_tiles), G_THREADS, Shape::SMEM, stream>>>(og);
     prof_mark(stream, "modular_gemm");
   }
   {  // the single product, when some column of H is not finite
     OneGemm og;
     memset(&og, 0, sizeof(og));
-    if (!make_tmap(&og.ta, b.RA, Lo.kp, M, nmod, G_BM) || !make_tmap(&og.tb, b.RH, Lo.kp, N, nmod, G_BN))
+    if (!make_tmap(&og.ta, b.RA, Lo.kp, M, nmod, G_BM) || !make_tmap(&og.tb, b.RH, Lo.kp, Np, nmod, G_BN))
       return PSMMA_EDEVICE;
     GemmArgs& ga = og.g;
     ga.n = M;
     ga.kr = Lo.kr;
     ga.nkb = Lo.kp / G_BK;
     ga.tiles_m = (M + G_BM - 1) / G_BM;
-    ga.tiles_n = (N + G_BN - 1) / G_BN;
+    ga.tiles_n = (Np + G_BN - 1) / G_BN;
     ga.group_m = 16;
     ga.nmod = nmod;
     ga.R = b.R;
@@ -2661,8 +2712,8 @@ static int s2_pass(S2State& st, const double* A, long lda, const unsigned long l
   for (int q = 0; q < 4; ++q) bs.qrow[q] = (q >> 1) * h;
   const int smem = 4 * 64 * 32 * 8;
   if (set_smem_attr(k_residues_A_blocks<4>, smem) != cudaSuccess) return PSMMA_EDEVICE;
-  k_residues_A_blocks<4><<<dim3(wk / 64, (h + 31) / 32), 256, smem, stream>>>(A, lda, st.M, r0, h, wk, st.kp, amax, pk,
-                                                                               st.cc, st.RA, st.RS, bs);
+  k_residues_A_blocks<4><<<dim3(wk / 64, (h + 31) / 32), 256, smem, stream>>>(A, lda, st.M, r0, h, wk, st.kp, st.K,
+                                                                               amax, pk, st.cc, st.RA, st.RS, bs);
   prof_mark(stream, "residues_A");
   using Shape = GemmShape<G_BN>;
   if (set_smem_attr(k_crt_gemm<G_BN, OneGemm, true>, (int)Shape::SMEM) != cudaSuccess) return PSMMA_EDEVICE;
@@ -3137,9 +3188,10 @@ int launch_split_any(int kind, int n, int k, double alpha, const double* A, long
   const int nmod = resolve_nmod(n_moduli);
   if (kind == KIND_DFT) return split_core_dft3(k, n, alpha, A, lda, beta, Q, ldq, nmod, work, lwork, stream, status_dev_out);
   const GenSpec gs = reference_gens(kind, gen, ldgen, k);
-  const int L = block_levels(kind, k, k, block_req);
-  if (L > 0 && gs.k1 == 0)
-    return split_core_block(n, k, L, alpha, A, lda, gs, beta, Q, ldq, nmod, work, lwork, stream, status_dev_out);
+  const BlockChoice bc = block_choice(kind, k, k, block_req);
+  if (bc.L > 0 && gs.k1 == 0)
+    return split_core_block(n, k, bc.Np, bc.L, alpha, A, lda, gs, beta, Q, ldq, nmod, work, lwork, stream,
+                            status_dev_out);
   if (s2_use(kind, n, k, k, block_req) && gs.k1 == 0)
     return split_core_s2(n, k, k, alpha, A, lda, gs, beta, Q, ldq, nmod, work, lwork, stream, status_dev_out);
   return split_core(n, k, k, alpha, A, lda, gs, beta, Q, ldq, nmod, work, lwork, stream, status_dev_out);

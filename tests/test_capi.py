@@ -92,11 +92,15 @@ def test_workspace_size_queries(lib):
 
 
 def test_split_block_levels_rule(lib):
-    # the Toeplitz / Hankel block step chosen automatically: the largest L <= 2 with k divisible
-    # by 64 * 2^L and k / 2^L >= 4096; other kinds never take it (host logic only, no GPU work)
+    # the Toeplitz / Hankel block step chosen automatically: the L in {1, 2} with leaves of at
+    # least 4096 columns (k padded to a multiple of 64 * 2^L) that minimises (k'/k)^2 (3/4)^L,
+    # if at most 0.85; other kinds never take it (host logic only, no GPU work)
     ks = [1024, 2048, 4096, 6144, 8192, 8256, 12288, 16384, 24576, 32768, 0]
     for kind in (_lib.KIND_TOEPLITZ, _lib.KIND_HANKEL):
-        assert [lib.psmma_split_block_levels(kind, 100, k) for k in ks] == [0, 0, 0, 0, 1, 0, 1, 2, 2, 2, 0]
+        assert [lib.psmma_split_block_levels(kind, 100, k) for k in ks] == [0, 0, 0, 0, 1, 1, 1, 2, 2, 2, 0]
+        # padded: 8100 -> 8192 at L = 1; 16000 stays at L = 1 (padded to 16128, L = 2's leaves would
+        # have 4032 columns); 16129 -> 16384 at L = 2 (0.58 of the work, below L = 1's 0.76)
+        assert [lib.psmma_split_block_levels(kind, 100, k) for k in (8000, 8100, 16000, 16129)] == [0, 1, 1, 2]
     for kind in (_lib.KIND_CAUCHY, _lib.KIND_DFT):
         assert [lib.psmma_split_block_levels(kind, 100, k) for k in ks] == [0] * len(ks)
     # Cauchy (and CAUCHYEIG): Strassen's step only on request, never automatically

@@ -180,13 +180,16 @@ def test_split_wide_exponent_range_rows(cuda):
 
 @pytest.mark.parametrize("kind", ["toeplitz", "hankel"])
 @pytest.mark.parametrize("n,k,levels,pad", [(1000, 2048, 1, 3), (2048, 4096, 2, 0), (333, 6144, 2, 5),
-                                            (70, 3072, 1, 1), (130, 1536, 3, 2), (257, 8192, 0, 4)])
+                                            (70, 3072, 1, 1), (130, 1536, 3, 2), (257, 8192, 0, 4),
+                                            (300, 2000, 1, 2), (129, 3000, 2, 0), (200, 1000, 3, 1),
+                                            (65, 8100, 0, 3)])
 def test_split_block_step_matches_dense_oracle(kind, n, k, levels, pad, cuda):
     # the block step (3^L products of width k / 2^L on sums and differences of blocks), asked
-    # for by opts->block_levels (0: the automatic choice, one level at k = 8192): ragged row
-    # counts, padded leading dimensions, alpha and beta, leaves narrower than a GEMM tile
-    # (k = 1536 at L = 3: 192 columns), against the dense oracle on the whole product and
-    # column by column
+    # for by opts->block_levels (0: the automatic choice, one level at k = 8192 and at 8100,
+    # padded to 8192): ragged row counts, padded leading dimensions, alpha and beta, leaves
+    # narrower than a GEMM tile (k = 1536 or 1000 at L = 3: 192 or 128 columns), orders that
+    # 64 * 2^L does not divide (2000, 3000, 1000, 8100: the generator zero-extended, A with zero
+    # columns), against the dense oracle on the whole product and column by column
     import psmma_git_gb300 as P
     if levels == 0:
         assert P.load().psmma_split_block_levels({"toeplitz": 1, "hankel": 2}[kind], n, k) == 1
@@ -199,7 +202,7 @@ def test_split_block_step_matches_dense_oracle(kind, n, k, levels, pad, cuda):
     assert O.col_max_rel(got, ref) < 10 * TOL
 
 
-@pytest.mark.parametrize("n,levels", [(2048, 2), (4096, 3), (8192, 0)])
+@pytest.mark.parametrize("n,levels", [(2048, 2), (4096, 3), (8192, 0), (2000, 1), (3000, 2)])
 def test_split_block_step_toeplitz_known_answer_bit_exact(n, levels, cuda):
     # the reference test's generator (G(i) = N - i, G(N) = N^2) with integer A: the block
     # step's sums and differences are exact, so the closed form comes back bit for bit
@@ -235,11 +238,12 @@ def test_split_block_step_same_result_as_single_product(kind, cuda):
 
 
 @pytest.mark.parametrize("kind", ["toeplitz", "hankel"])
-def test_split_block_step_nonfinite_generator_takes_single_product(kind, cuda):
+@pytest.mark.parametrize("k", [4096, 4000])
+def test_split_block_step_nonfinite_generator_takes_single_product(kind, k, cuda):
     # a NaN and an Inf in the generator: the call falls back (on the device) to the single
     # product, which returns NaN in exactly the columns that hold them and the oracle's
-    # values elsewhere
-    n, k = 200, 4096
+    # values elsewhere (k = 4000: the padded order 4096)
+    n = 200
     A = O.cfg_matrix(n, k, seed=31)
     gen = _gen(kind, k, seed=32)
     gen[k // 3] = np.nan
