@@ -951,6 +951,34 @@ __device__ bool qr_tile(const QrTile& t, int local, double tol, unsigned* status
     __syncthreads();
     const double* vk = t.V + (long)k * M;
     bool flagged = false;
+    // The warp's columns in turn: the dot products over the rows (lanes split the rows), then
+    // the scalar tail -- F(c,k), R(k,c) and the norm downdate, some 36 FP64 instructions with
+    // two divisions and a square root -- once per 32 columns, lane j taking the warp's j-th
+    // column: GB300's FP64 pipe costs a warp instruction whatever the lanes, so a tail run by
+    // the whole warp for each column cost a third of the step at M = 2048.
+    int slot = 0, sc = -1;
+    double sd = 0.0, sf = 0.0, sr = 0.0;
+    auto tail = [&]() {
+      if (sc >= 0) {
+        const double f = tk * (sd - sf);
+        const double rkc = __ldcg(t.T + (long)sc * M + k) - sr - f;  // V(k,k) = 1
+        const double v1 = __ldcg(t.vn1 + sc), v2 = __ldcg(t.vn2 + sc);
+        double nv1 = v1;
+        if (v1 != 0.0) {
+          double temp = fabs(rkc) / v1;
+          temp = fmax(0.0, 1.0 - temp * temp);
+          const double q = v1 / v2;
+          const double temp2 = temp * q * q;
+          if (temp2 <= tol3z) flagged = true;
+          else nv1 = v1 * sqrt(temp);
+        }
+        t.F[(long)sc * cap + k] = f;
+        t.R[(long)sc * cap + k] = rkc;
+        t.vn1[sc] = nv1;
+      }
+      sc = -1;
+      slot = 0;
+    };
     for (int c = k + 1 + local * QR_WARPS + warp; c < N; c += t.ncta * QR_WARPS) {
       const double* tc = t.T + (long)c * M;
       const double* fc = t.F + (long)c * cap;
@@ -966,26 +994,16 @@ __device__ bool qr_tile(const QrTile& t, int local, double tol, unsigned* status
         fs += __shfl_xor_sync(0xffffffffu, fs, o);
         rs += __shfl_xor_sync(0xffffffffu, rs, o);
       }
-      const double f = tk * (dot - fs);
-      const double rkc = __ldcg(tc + k) - rs - f;  // V(k,k) = 1
-      const double v1 = __ldcg(t.vn1 + c), v2 = __ldcg(t.vn2 + c);
-      double nv1 = v1;
-      bool recompute = false;
-      if (v1 != 0.0) {
-        double temp = fabs(rkc) / v1;
-        temp = fmax(0.0, 1.0 - temp * temp);
-        const double q = v1 / v2;
-        const double temp2 = temp * q * q;
-        if (temp2 <= tol3z) recompute = true;
-        else nv1 = v1 * sqrt(temp);
+      if (lane == slot) {
+        sd = dot;
+        sf = fs;
+        sr = rs;
+        sc = c;
       }
-      flagged |= recompute;
-      if (lane == 0) {
-        t.F[(long)c * cap + k] = f;
-        t.R[(long)c * cap + k] = rkc;
-        t.vn1[c] = nv1;
-      }
+      if (++slot == 32) tail();
     }
+    if (slot > 0) tail();
+    flagged = __any_sync(0xffffffffu, flagged);
     if (flagged && lane == 0) atomicMax(t.flag, k + 1);
     if (!group_sync(t.bar, (++epoch) * t.ncta, status)) return false;
     if (__ldcg(t.flag) == k + 1 && k + 1 < cap) {
