@@ -769,6 +769,51 @@ __device__ __forceinline__ double lane_dot(const double* x, const double* y, int
   return (a0 + a1) + (a2 + a3);
 }
 
+// lane_dot for four columns x[0..3] against one y, each column's sum in lane_dot's order; the y
+// loads are shared.
+__device__ __forceinline__ void lane_dot4(const double* const (&x)[4], const double* y, int i0, int M,
+                                          double (&out)[4]) {
+  double a[4][4];
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) a[u][q] = 0.0;
+  int i = i0;
+  for (; i + 96 < M; i += 128) {
+    const double y0 = __ldcg(y + i), y1 = __ldcg(y + i + 32), y2 = __ldcg(y + i + 64), y3 = __ldcg(y + i + 96);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      a[u][0] = fma(__ldcg(x[u] + i), y0, a[u][0]);
+      a[u][1] = fma(__ldcg(x[u] + i + 32), y1, a[u][1]);
+      a[u][2] = fma(__ldcg(x[u] + i + 64), y2, a[u][2]);
+      a[u][3] = fma(__ldcg(x[u] + i + 96), y3, a[u][3]);
+    }
+  }
+  for (; i < M; i += 32) {
+    const double y0 = __ldcg(y + i);
+#pragma unroll
+    for (int u = 0; u < 4; ++u) a[u][0] = fma(__ldcg(x[u] + i), y0, a[u][0]);
+  }
+#pragma unroll
+  for (int u = 0; u < 4; ++u) out[u] = (a[u][0] + a[u][1]) + (a[u][2] + a[u][3]);
+}
+
+// The warp sums of four per-lane values v[0..3], reduced and scattered: lane l ends with the
+// total of v[l >> 3].  Every partial sum is one the xor butterfly forms (in commuted order),
+// so each total equals the butterfly's.
+__device__ __forceinline__ double quad_reduce(const double (&v)[4], int lane) {
+  const bool b4 = (lane & 16) != 0, b3 = (lane & 8) != 0;
+  double k0 = b4 ? v[2] : v[0], k1 = b4 ? v[3] : v[1];
+  const double s0 = b4 ? v[0] : v[2], s1 = b4 ? v[1] : v[3];
+  k0 += __shfl_xor_sync(0xffffffffu, s0, 16);
+  k1 += __shfl_xor_sync(0xffffffffu, s1, 16);
+  double kk = b3 ? k1 : k0;
+  const double ss = b3 ? k0 : k1;
+  kk += __shfl_xor_sync(0xffffffffu, ss, 8);
+  for (int o = 4; o > 0; o >>= 1) kk += __shfl_xor_sync(0xffffffffu, kk, o);
+  return kk;
+}
+
 // Step k of the leader CTA: pivot, swap, the current column a = T(k:,k) - V F(k,:)^T over the
 // reflectors p0..k-1 of the current panel (earlier ones are applied to T), its Householder
 // reflector (beta = -sign(alpha) ||a||, tau = (beta - alpha)/beta, v = a(k+1:)/(alpha - beta)),
@@ -979,28 +1024,40 @@ __device__ bool qr_tile(const QrTile& t, int local, double tol, unsigned* status
       sc = -1;
       slot = 0;
     };
-    for (int c = k + 1 + local * QR_WARPS + warp; c < N; c += t.ncta * QR_WARPS) {
-      const double* tc = t.T + (long)c * M;
-      const double* fc = t.F + (long)c * cap;
-      double dot = lane_dot(tc, vk, k + lane, M);
-      double fs = 0.0, rs = 0.0;
-      for (int j = p0 + lane; j < k; j += 32) {
-        const double fj = __ldcg(fc + j);
-        fs = fma(fj, sv[j - p0], fs);
-        rs = fma(vrow[j - p0], fj, rs);
+    // Four columns at a time: one pass over v_k for their dot products (each column's sum in
+    // lane_dot's order), then a reduce-scatter of the three sums of the four columns (levels
+    // 16 and 8 split the lanes between the columns, 4, 2, 1 finish each column in its eight
+    // lanes): 18 FP64 adds for four columns where a butterfly per column takes 60, with the
+    // same partial sums (FP64 addition commutes), so the totals are the butterfly's.
+    const int stride = t.ncta * QR_WARPS;
+    const int u_me = lane >> 3;  // the column of the quad whose totals this lane ends with
+    for (int c = k + 1 + local * QR_WARPS + warp; c < N; c += 4 * stride) {
+      double dot[4], fs[4], rs[4];
+      const double* tc[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) tc[u] = t.T + (long)min(c + u * stride, N - 1) * M;
+      lane_dot4(tc, vk, k + lane, M, dot);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const double* fc = t.F + (long)min(c + u * stride, N - 1) * cap;
+        fs[u] = 0.0;
+        rs[u] = 0.0;
+        for (int j = p0 + lane; j < k; j += 32) {
+          const double fj = __ldcg(fc + j);
+          fs[u] = fma(fj, sv[j - p0], fs[u]);
+          rs[u] = fma(vrow[j - p0], fj, rs[u]);
+        }
       }
-      for (int o = 16; o > 0; o >>= 1) {
-        dot += __shfl_xor_sync(0xffffffffu, dot, o);
-        fs += __shfl_xor_sync(0xffffffffu, fs, o);
-        rs += __shfl_xor_sync(0xffffffffu, rs, o);
+      const double td = quad_reduce(dot, lane), tf = quad_reduce(fs, lane), tr = quad_reduce(rs, lane);
+      // lane 8 u + slot holds column u's totals: stash them for the tail
+      const int cu = c + u_me * stride;
+      if ((lane & 7) == slot && cu < N) {
+        sd = td;
+        sf = tf;
+        sr = tr;
+        sc = cu;
       }
-      if (lane == slot) {
-        sd = dot;
-        sf = fs;
-        sr = rs;
-        sc = c;
-      }
-      if (++slot == 32) tail();
+      if (++slot == 8) tail();
     }
     if (slot > 0) tail();
     flagged = __any_sync(0xffffffffu, flagged);
