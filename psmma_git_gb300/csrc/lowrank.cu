@@ -865,7 +865,15 @@ __device__ void qr_leader_step(const QrTile& t, int k, int p0, double tol, bool 
   double xsq = 0.0;
   for (int i = k + threadIdx.x; i < M; i += blockDim.x) {
     double a = __ldcg(t.T + i + (long)k * M);
-    for (int j = p0; j < k; ++j) a = fma(-__ldcg(t.V + i + (long)j * M), fk[j - p0], a);
+    int j = p0;
+    for (; j + 4 <= k; j += 4) {  // four loads in flight, the same FMA order
+      double vv[4];
+#pragma unroll
+      for (int jj = 0; jj < 4; ++jj) vv[jj] = __ldcg(t.V + i + (long)(j + jj) * M);
+#pragma unroll
+      for (int jj = 0; jj < 4; ++jj) a = fma(-vv[jj], fk[j + jj - p0], a);
+    }
+    for (; j < k; ++j) a = fma(-__ldcg(t.V + i + (long)j * M), fk[j - p0], a);
     vk[i] = a;
     if (i > k) xsq = fma(a, a, xsq);
   }
@@ -918,7 +926,25 @@ __device__ void qr_restart(const QrTile& t, int p0, int k1, int r0, int c0, int 
       double a[4];
 #pragma unroll
       for (int u = 0; u < 4; ++u) a[u] = (i + 32 * u < M) ? __ldcg(tc + i + 32 * u) : 0.0;
-      for (int j = 0; j < nj; ++j) {
+      // four reflectors per pass with their 16 loads issued first (the loads of one
+      // reflector alone leave the lane waiting on L2 between FMAs); same FMA order
+      int j = 0;
+      for (; j + 4 <= nj; j += 4) {
+        double vv[4][4];
+#pragma unroll
+        for (int jj = 0; jj < 4; ++jj) {
+          const double* vj = t.V + (long)(p0 + j + jj) * M;
+#pragma unroll
+          for (int u = 0; u < 4; ++u) vv[jj][u] = (i + 32 * u < M) ? __ldcg(vj + i + 32 * u) : 0.0;
+        }
+#pragma unroll
+        for (int jj = 0; jj < 4; ++jj) {
+          const double w = fw[warp][j + jj];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) a[u] = fma(-vv[jj][u], w, a[u]);
+        }
+      }
+      for (; j < nj; ++j) {
         const double* vj = t.V + (long)(p0 + j) * M;
         const double w = fw[warp][j];
 #pragma unroll
