@@ -344,18 +344,21 @@ __global__ void k_dft_table(double2* w, int n) {
   }
 }
 
-// Splits of K that fill the SMs in whole waves when the output has few tiles: the count S
-// (1..8, at least 256 k per split) maximising the useful fraction of the last wave, with a
-// small charge per extra split for the partial traffic.
+// Splits of K that fill the SMs in whole waves when the output has few tiles (fewer than 16
+// waves; one CTA per SM): the count S (1..16, at least 128 k per split) maximising the useful
+// fraction of the last wave, with a charge of 0.2 % per extra split for the partials' traffic
+// (S M N doubles written and summed: about 10 us per split at n = 2048, 0.06 % of the product)
+// and the jobs' pipeline fill.  n = 2048: 256 tiles x 16 splits = 26.9 waves (0.998 of the
+// last wave used, against 0.963 at 4 splits); n = 4096: 1024 tiles x 4 = 26.9 waves.
 int f64_splitk_count(int M, int N, int K, int sms) {
   const long tiles = (long)((M + F64_BM - 1) / F64_BM) * ((N + F64_BN - 1) / F64_BN);
-  if (tiles >= 4L * sms || K < 512) return 1;
+  if (tiles >= 16L * sms || K < 256) return 1;
   int best = 1;
   double best_v = -1.0;
-  for (int S = 1; S <= 8 && K / S >= 256; ++S) {
+  for (int S = 1; S <= 16 && K / S >= 128; ++S) {
     const long jobs = tiles * S;
     const double eff = (double)jobs / (double)(((jobs + sms - 1) / sms) * sms);
-    const double v = eff - 0.01 * (S - 1);
+    const double v = eff - 0.002 * (S - 1);
     if (v > best_v + 1e-9) { best_v = v; best = S; }
   }
   return best;
