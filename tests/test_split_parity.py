@@ -202,6 +202,19 @@ def test_split_block_step_matches_dense_oracle(kind, n, k, levels, pad, cuda):
     assert O.col_max_rel(got, ref) < 10 * TOL
 
 
+@pytest.mark.parametrize("kind", ["toeplitz", "hankel"])
+@pytest.mark.parametrize("n,k,levels", [(1, 128, 1), (3, 256, 2), (2, 512, 3), (5, 130, 1), (1, 200, 2)])
+def test_split_block_step_tiny_shapes(kind, n, k, levels, cuda):
+    # one to five rows, leaves of 64 columns (narrower than a GEMM tile), orders padded from
+    # 130 and 200: against the dense oracle
+    A = O.cfg_matrix(n, k, seed=n * 31 + k)
+    gen = _gen(kind, k, seed=k + 9)
+    Q0 = O.cfg_matrix(n, k, seed=n + 77)
+    got = _split(kind, n, k, -0.5, A, gen, 2.0, Q0, cuda, block_levels=levels)
+    ref = O.dense_product(kind, -0.5, A, gen, 2.0, Q0, k)
+    assert O.rel_fro(got, ref) < TOL
+
+
 @pytest.mark.parametrize("n,levels", [(2048, 2), (4096, 3), (8192, 0), (2000, 1), (3000, 2)])
 def test_split_block_step_toeplitz_known_answer_bit_exact(n, levels, cuda):
     # the reference test's generator (G(i) = N - i, G(N) = N^2) with integer A: the block
