@@ -765,6 +765,28 @@ def run_cfg1(args, ws, rank, local, compact=False):
         lib.psmma_set_profiling(0)
         phases = [[names[j].decode(), round(ms[j], 3)] for j in range(max(0, m))]
         gemm_ms = sum(v for nm, v in phases if "gemm" in nm)
+        e2e = None
+        if kind in ("toeplitz", "hankel"):
+            # end to end through the host-pointer entry point (pinned host A, generator and Q;
+            # the copies inside each call, overlapped with the block step's row panels)
+            hA = torch.empty((k, n), dtype=torch.float64, pin_memory=True)
+            hA.copy_(A.t())
+            hQ = torch.empty((k, n), dtype=torch.float64, pin_memory=True)
+            hg = torch.empty(2 * k - 1, dtype=torch.float64, pin_memory=True)
+            hg.copy_(gv)
+            nA, nQ, ng = hA.numpy().T, hQ.numpy().T, hg.numpy()
+            hfn = P.psmma_toeplitz if kind == "toeplitz" else P.psmma_hankel
+            for _ in range(3):  # the first call of the shape picks the bit counts the others speculate with
+                hfn(n, k, 1.0, nA, ng, 0.0, nQ, precision="split", n_moduli=nmod)
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                hfn(n, k, 1.0, nA, ng, 0.0, nQ, precision="split", n_moduli=nmod)
+            te = (time.perf_counter() - t0) / args.steps
+            e2e = {"value": flops / te / 1e12, "unit": "TFLOP/s", "ms_per_step": te * 1e3,
+                   "h2d_bytes_per_step": n * k * 8 + (2 * k - 1) * 8, "d2h_bytes_per_step": n * k * 8,
+                   "api": f"psmma_{kind}_host (pinned host buffers)",
+                   "same_as_device_result": bool(torch.equal(torch.from_numpy(nQ.T.copy()).t().to(dev), Y))}
+            del hA, hQ, hg
         run("fp64", Y64)  # warm-up (FP64 path: one call)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -846,6 +868,8 @@ def run_cfg1(args, ws, rank, local, compact=False):
                      "cpu_baseline": cpu, "split_phases_ms": phases}
         if col_err is not None:
             out[kind]["col_max_rel_err_vs_oracle_sample"] = col_err
+        if e2e is not None:
+            out[kind]["e2e"] = e2e
         if kind in ("toeplitz", "hankel"):
             out[kind]["block_levels"] = levels
             out[kind]["executed_tflops"] = flops * 0.75 ** levels / t / 1e9

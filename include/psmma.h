@@ -159,8 +159,8 @@ int psmma_split_dft_radix(int n);
  * in {1, 2} with w = k' / 2^L >= 4096 that minimises the modular GEMM work (k'/k)^2 (3/4)^L,
  * if that is at most 0.85, else 0 (smaller leaves make the modular GEMMs' per-tile epilogue
  * outweigh their MMAs).  The
- * device-pointer calls and the server take the step; the host-pointer calls keep the single
- * product.  On the device, without a synchronisation, the call takes the single product
+ * device-pointer calls, the host-pointer calls (in their overlapped row panels) and the server
+ * take the step.  On the device, without a synchronisation, the call takes the single product
  * instead when an entry of H is not finite (NaN then appears in exactly the columns it does
  * there) or when a nonzero column's maximum is more than 2^4 below the largest of its group
  * j + c w (the shared exponent would cost that column's entries more than 4 bits).  Cauchy and

@@ -359,11 +359,11 @@ int host_real(int kind, int n, int k, double alpha, const double* A, int lda, co
     cudaEvent_t* ev;
     st = host_copy_stream(&cs, &ev);
     if (st) return st;
-    const size_t need = split_workspace_bytes(kind, n, k, o->n_moduli);
+    const size_t need = split_workspace_bytes(kind, n, k, o->n_moduli, o->block_levels);
     void* work = host_split_work(need, o, s, &st);
     if (st) return st;
     st = launch_split_host(kind, n, k, alpha, A, lda, dA, dG, (kind == KIND_CAUCHY) ? k : (int)glen, beta, Q, ldq,
-                           dQ, o->n_moduli, work, o->work ? o->lwork : need, s, cs, ev, kHostEvents);
+                           dQ, o->n_moduli, work, o->work ? o->lwork : need, s, cs, ev, kHostEvents, o->block_levels);
     if (st) {
       cudaStreamSynchronize(s);
       cudaStreamSynchronize(cs);

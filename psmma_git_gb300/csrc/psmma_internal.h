@@ -163,7 +163,7 @@ size_t split_workspace_general(int M, int N, int K, int n_moduli, int block_leve
 int launch_split_host(int kind, int n, int k, double alpha, const double* A_h, long lda_h, double* dA,
                       const double* dgen, long ldgen, double beta, double* Q_h, long ldq_h, double* dQ,
                       int n_moduli, void* work, size_t lwork, cudaStream_t s, cudaStream_t cs, cudaEvent_t* ev,
-                      int nev);
+                      int nev, int block_levels = 0);
 int launch_split_host_general(int M, int N, int K, double alpha, const double* A_h, long lda_h, double* dA,
                               const GenSpec& gs, double beta, double* Q_h, long ldq_h, double* dQ, int n_moduli,
                               void* work, size_t lwork, cudaStream_t s, cudaStream_t cs, cudaEvent_t* ev, int nev);

@@ -867,7 +867,8 @@ __global__ void k_residues_H_spec(const double* __restrict__ Ht, int ncols, int 
 constexpr int kBlockMaxSpread = 4;
 // hmax_bits here: the maxima over every row of the (possibly padded) H.
 __global__ void k_group_colmax(const unsigned long long* __restrict__ hmax_bits,
-                               unsigned long long* __restrict__ gmax_bits, int w, int nq, SplitDevParams* prm) {
+                               unsigned long long* __restrict__ gmax_bits, int w, int nq, SplitDevParams* prm,
+                               SplitDevParams* prm2) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= w) return;
   unsigned long long m = 0, mn = ~0ull;
@@ -879,7 +880,10 @@ __global__ void k_group_colmax(const unsigned long long* __restrict__ hmax_bits,
     if (b > 0 && b < mn) mn = b;
   }
   if (!bad && m > 0 && ilogb_bits(m) - ilogb_bits(mn) > kBlockMaxSpread) bad = true;
-  if (bad) prm->hbad = 1u;
+  if (bad) {
+    prm->hbad = 1u;
+    if (prm2) prm2->hbad = 1u;  // the guessed parameters of a speculative pipeline gate too
+  }
   gmax_bits[g] = m;
 }
 
@@ -896,14 +900,15 @@ struct BlockSums {
 };
 
 // A residues of a block product: RA[l][r0 + qrow[q] + i][qcol[q] + kk] for every block q (as
-// k_residues_A writes them) and RS[p][l][i][kk] = the signed block sum p mod m_l, for i < rows,
-// kk < w; columns from kvalid on read as zero (A padded with zero columns).  Each block row keeps its own exponent (rows of different blocks are different rows of
+// k_residues_A writes them) and RS[p][l][rs_r0 + i][kk] (planes of rs_rows rows) = the signed
+// block sum p mod m_l, for i < rows, kk < w; columns from kvalid on read as zero (A padded
+// with zero columns).  Each block row keeps its own exponent (rows of different blocks are different rows of
 // A).  One CTA: 32 rows x 64 columns of each of the NQ blocks, transposed through shared memory
 // (NQ tiles of 64 x 32 doubles, the swizzle of residues_A_blk); each thread keeps the signed
 // scaled integers of its 4 columns of every block, so the sums need no second pass over A.
 template <int NQ>
 __global__ void __launch_bounds__(256) k_residues_A_blocks(const double* __restrict__ A, long lda, int M, int r0,
-                                                           int rows, int w, int kp, int kvalid,
+                                                           int rows, int w, int kp, int kvalid, int rs_rows, int rs_r0,
                                                            const unsigned long long* __restrict__ amax_bits,
                                                            const SplitDevParams* prm, CrtConsts cc,
                                                            __nv_bfloat16* __restrict__ RA,
@@ -924,7 +929,7 @@ __global__ void __launch_bounds__(256) k_residues_A_blocks(const double* __restr
   __syncthreads();
   const int P = prm->PA;
   const int nsum = prm->hbad ? 0 : bs.nsum;  // the single product needs no block sums
-  const size_t plane = (size_t)M * kp, splane = (size_t)rows * w;
+  const size_t plane = (size_t)M * kp, splane = (size_t)rs_rows * w;
   const int tq = threadIdx.x & 15, tr = threadIdx.x >> 4;
   for (int r = tr; r < TR; r += 16) {
     if (i0 + r >= rows) continue;
@@ -957,7 +962,7 @@ __global__ void __launch_bounds__(256) k_residues_A_blocks(const double* __restr
         for (int q = 0; q < NQ; ++q) V += ((mk >> q) & 1) ? (((ngm >> q) & 1) ? -sv[q][v] : sv[q][v]) : 0ll;
         c4[v] = residue_chunks4(V);
       }
-      uint2* dst = (uint2*)(RS + (size_t)p * cc.nmod * splane + (size_t)(i0 + r) * w + k0 + kk);
+      uint2* dst = (uint2*)(RS + (size_t)p * cc.nmod * splane + (size_t)(rs_r0 + i0 + r) * w + k0 + kk);
 #pragma unroll
       for (int l = 0; l < SPL_MAX_MODULI; ++l) {
         if (l < cc.nmod) {
@@ -1983,9 +1988,9 @@ __global__ void __launch_bounds__(256, 3) k_crt_combine_blocks(const int8_t* __r
                                                             const unsigned long long* __restrict__ hmax_bits,
                                                             const unsigned long long* __restrict__ gmax_bits, int gw,
                                                             const SplitDevParams* prm, double alpha, double beta,
-                                                            double* __restrict__ Q, long ldq) {
+                                                            double* __restrict__ Q, long ldq, int by0) {
   crt_combine_blk<false, TOP32>(R, n, k, kr, cc, amax_bits, hmax_bits, prm, alpha, beta, Q, ldq, blockIdx.x,
-                                blockIdx.y, gmax_bits, gw);
+                                by0 + blockIdx.y, gmax_bits, gw);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -2442,151 +2447,162 @@ static bool make_tmap_view(CUtensorMap* map, void* ptr, int inner, long pitch, i
   return r == CUDA_SUCCESS;
 }
 
-// Q (M x N) = alpha * A (M x N) * H + beta * Q for Toeplitz / Hankel H (N x N) with L >= 1 levels
-// of the block step on the order Np >= N (block_choice; padded when Np > N).
-static int split_core_block(int M, int N, int Np, int L, double alpha, const double* A, long lda,
-                            const GenSpec& gs_in, double beta, double* Q, long ldq, int nmod, void* work,
-                            size_t lwork, cudaStream_t stream, unsigned* status_dev_out) {
-  if (nmod < 8 || nmod > SPL_MAX_MODULI) return PSMMA_EUNSUPPORTED;
-  if (Np >= (1 << 24) || M > kSplitMaxRows || L < 1 || L > BLK_MAX_LEVELS || Np < N || Np % (64 << L) != 0)
-    return PSMMA_EUNSUPPORTED;
-  GenSpec gs = gs_in;
-  if (Np > N) {
-    gs.glen = 2L * N - 1;  // the padding reads the generator zero-extended
-    gs.srows = N;          // and only the real rows count in the column statistics
-  }
-  const int w = Np >> L, NQ = 1 << L;
-  const SplitLayout Lo = block_layout(M, Np, L, nmod);
-  if (lwork < Lo.total || !work) return PSMMA_EWORKSPACE;
-  char* wk = (char*)work;
-  const SplitBuffers b = split_buffers(wk, Lo);
-  __nv_bfloat16* RS = (__nv_bfloat16*)(wk + Lo.off_rs);
-  unsigned long long* gmax = (unsigned long long*)(wk + Lo.off_gmax);
-  unsigned long long* hall = (unsigned long long*)(wk + Lo.off_hall);
-  const CrtConsts cc = get_consts(nmod);
-  const std::vector<BlkNode> leaves = block_leaves(gs.kind, L);
-  const int nleaf = (int)leaves.size();
-
-  // A operands: one block (a view of RA) or a sum plane (RS), numbered in leaf order
+// The launches of the block step for one call, shared by the device-pointer call (all rows at
+// once) and the host-pointer pipeline (row panels).  pk: the parameters the kernels scale with
+// and gate on (hbad) -- the call's, or the guessed ones of a speculative pipeline.
+struct BlockRun {
+  int M, N, Np, L, w, NQ, nmod, nleaf, sms;
+  GenSpec gs;
+  SplitLayout Lo;
+  SplitBuffers b;
+  __nv_bfloat16* RS;
+  unsigned long long *gmax, *hall;
+  CrtConsts cc;
+  std::vector<BlkNode> leaves;
+  std::vector<int> a_sum;
   BlockSums bs;
-  memset(&bs, 0, sizeof(bs));
-  for (int q = 0; q < NQ; ++q) bs.qcol[q] = q * w;  // column blocks of every row
-  bs.wmask = (1 << NQ) - 1;
-  std::vector<int> a_sum(nleaf, -1);
-  for (int y = 0; y < nleaf; ++y) {
-    const int mk = leaves[y].amask;
-    if ((mk & (mk - 1)) == 0) continue;
-    int p = 0;
-    while (p < bs.nsum && bs.mask[p] != mk) ++p;
-    if (p == bs.nsum) bs.mask[bs.nsum++] = mk;
-    a_sum[y] = p;
-  }
   LeafTerms lt;
-  memset(&lt, 0, sizeof(lt));
-  for (int y = 0; y < nleaf; ++y) {
-    lt.nterm[y] = leaves[y].nterm;
-    for (int t = 0; t < leaves[y].nterm; ++t) {
-      lt.sign[y][t] = (signed char)leaves[y].sign[t];
-      lt.koff[y][t] = leaves[y].r[t] * w;
-      lt.joff[y][t] = leaves[y].c[t] * w;
+
+  int init(int M_, int N_, int Np_, int L_, const GenSpec& gs_in, int nmod_, void* work, size_t lwork) {
+    M = M_; N = N_; Np = Np_; L = L_; nmod = nmod_;
+    if (nmod < 8 || nmod > SPL_MAX_MODULI) return PSMMA_EUNSUPPORTED;
+    if (Np >= (1 << 24) || M > kSplitMaxRows || L < 1 || L > BLK_MAX_LEVELS || Np < N || Np % (64 << L) != 0)
+      return PSMMA_EUNSUPPORTED;
+    gs = gs_in;
+    if (Np > N) {
+      gs.glen = 2L * N - 1;  // the padding reads the generator zero-extended
+      gs.srows = N;          // and only the real rows count in the column statistics
     }
+    w = Np >> L;
+    NQ = 1 << L;
+    Lo = block_layout(M, Np, L, nmod);
+    if (lwork < Lo.total || !work) return PSMMA_EWORKSPACE;
+    char* wk = (char*)work;
+    b = split_buffers(wk, Lo);
+    RS = (__nv_bfloat16*)(wk + Lo.off_rs);
+    gmax = (unsigned long long*)(wk + Lo.off_gmax);
+    hall = (unsigned long long*)(wk + Lo.off_hall);
+    cc = get_consts(nmod);
+    leaves = block_leaves(gs.kind, L);
+    nleaf = (int)leaves.size();
+    // A operands: one block (a view of RA) or a sum plane (RS), numbered in leaf order
+    memset(&bs, 0, sizeof(bs));
+    for (int q = 0; q < NQ; ++q) bs.qcol[q] = q * w;  // column blocks of every row
+    bs.wmask = (1 << NQ) - 1;
+    a_sum.assign(nleaf, -1);
+    for (int y = 0; y < nleaf; ++y) {
+      const int mk = leaves[y].amask;
+      if ((mk & (mk - 1)) == 0) continue;
+      int p = 0;
+      while (p < bs.nsum && bs.mask[p] != mk) ++p;
+      if (p == bs.nsum) bs.mask[bs.nsum++] = mk;
+      a_sum[y] = p;
+    }
+    memset(&lt, 0, sizeof(lt));
+    for (int y = 0; y < nleaf; ++y) {
+      lt.nterm[y] = leaves[y].nterm;
+      for (int t = 0; t < leaves[y].nterm; ++t) {
+        lt.sign[y][t] = (signed char)leaves[y].sign[t];
+        lt.koff[y][t] = leaves[y].r[t] * w;
+        lt.joff[y][t] = leaves[y].c[t] * w;
+      }
+    }
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      return PSMMA_EDEVICE;
+    using Shape = GemmShape<G_BN>;
+    if (set_smem_attr(k_crt_gemm<G_BN, OneGemm, true>, (int)Shape::SMEM) != cudaSuccess ||
+        set_smem_attr(k_crt_gemm<G_BN, OneGemm>, (int)Shape::SMEM) != cudaSuccess)
+      return PSMMA_EDEVICE;
+    const int smem = NQ * 64 * 32 * 8;
+    const cudaError_t e = NQ == 2 ? set_smem_attr(k_residues_A_blocks<2>, smem)
+                          : NQ == 4 ? set_smem_attr(k_residues_A_blocks<4>, smem)
+                                    : set_smem_attr(k_residues_A_blocks<8>, smem);
+    return e == cudaSuccess ? PSMMA_OK : PSMMA_EDEVICE;
   }
 
-  prof_begin(stream);
-  if (cudaMemsetAsync(wk, 0, Lo.off_wtab, stream) != cudaSuccess) return PSMMA_EDEVICE;
-  {
-    const int kchunk = 1024;
-    dim3 g1((M + 127) / 128, (N + kchunk - 1) / kchunk);
-    k_row_absmax<<<g1, 128, 0, stream>>>(A, lda, M, N, kchunk, b.amax, b.asq);
+  // Ht, the column statistics (real rows) and all-row maxima, the group maxima and the gate.
+  void h_side(SplitDevParams* prm2, cudaStream_t s) {
+    if (gs.kind == KIND_TOEPLITZ)
+      k_h_pass1_all<KIND_TOEPLITZ><<<Np, 256, 0, s>>>(gs, Np, Lo.kp, b.Ht, b.hmax, b.hsum, b.hsq, b.prm, hall);
+    else
+      k_h_pass1_all<KIND_HANKEL><<<Np, 256, 0, s>>>(gs, Np, Lo.kp, b.Ht, b.hmax, b.hsum, b.hsq, b.prm, hall);
+    k_group_colmax<<<(w + 255) / 256, 256, 0, s>>>(hall, gmax, w, NQ, b.prm, prm2);
   }
-  prof_mark(stream, "row_scale");
-  if (gs.kind == KIND_TOEPLITZ)
-    k_h_pass1_all<KIND_TOEPLITZ><<<Np, 256, 0, stream>>>(gs, Np, Lo.kp, b.Ht, b.hmax, b.hsum, b.hsq, b.prm, hall);
-  else
-    k_h_pass1_all<KIND_HANKEL><<<Np, 256, 0, stream>>>(gs, Np, Lo.kp, b.Ht, b.hmax, b.hsum, b.hsq, b.prm, hall);
-  k_group_colmax<<<(w + 255) / 256, 256, 0, stream>>>(hall, gmax, w, NQ, b.prm);
-  prof_mark(stream, "h_generate");
-  k_split_params<<<PARAMS_BLOCKS, 512, 0, stream>>>(b.prm, cc.log2M, M, Np, Np, b.amax, b.asq, b.hmax, b.hsq);
-  prof_mark(stream, "params");
-  {
-    const dim3 ga(w / 64, (M + 31) / 32);
-    const int smem = NQ * 64 * 32 * 8;
-    cudaError_t e = cudaSuccess;
-    if (NQ == 2) {
-      e = set_smem_attr(k_residues_A_blocks<2>, smem);
-      if (e == cudaSuccess)
-        k_residues_A_blocks<2><<<ga, 256, smem, stream>>>(A, lda, M, 0, M, w, Lo.kp, N, b.amax, b.prm, cc, b.RA,
-                                                           RS, bs);
-    } else if (NQ == 4) {
-      e = set_smem_attr(k_residues_A_blocks<4>, smem);
-      if (e == cudaSuccess)
-        k_residues_A_blocks<4><<<ga, 256, smem, stream>>>(A, lda, M, 0, M, w, Lo.kp, N, b.amax, b.prm, cc, b.RA,
-                                                           RS, bs);
-    } else {
-      e = set_smem_attr(k_residues_A_blocks<8>, smem);
-      if (e == cudaSuccess)
-        k_residues_A_blocks<8><<<ga, 256, smem, stream>>>(A, lda, M, 0, M, w, Lo.kp, N, b.amax, b.prm, cc, b.RA,
-                                                           RS, bs);
-    }
-    if (e != cudaSuccess) return PSMMA_EDEVICE;
-  }
-  prof_mark(stream, "residues_A");
-  {
+
+  // The leaves' H operands, or (gated) the whole H's residues for the single product.
+  void h_operands(const SplitDevParams* pk, cudaStream_t s) {
     const dim3 gh(w, rh_blocks_x(w), nleaf);
     if (NQ == 2)
-      k_residues_H_leaf<2><<<gh, 128, 0, stream>>>(b.Ht, Lo.kp, w, w, hall, gmax, 1, b.prm, cc, lt, b.RH);
+      k_residues_H_leaf<2><<<gh, 128, 0, s>>>(b.Ht, Lo.kp, w, w, hall, gmax, 1, pk, cc, lt, b.RH);
     else if (NQ == 4)
-      k_residues_H_leaf<4><<<gh, 128, 0, stream>>>(b.Ht, Lo.kp, w, w, hall, gmax, 1, b.prm, cc, lt, b.RH);
+      k_residues_H_leaf<4><<<gh, 128, 0, s>>>(b.Ht, Lo.kp, w, w, hall, gmax, 1, pk, cc, lt, b.RH);
     else
-      k_residues_H_leaf<8><<<gh, 128, 0, stream>>>(b.Ht, Lo.kp, w, w, hall, gmax, 1, b.prm, cc, lt, b.RH);
-    k_residues_H_gated<<<dim3(std::min(Np, 608), rh_blocks_x(Lo.kp)), 128, 0, stream>>>(b.Ht, Np, Lo.kp, N, b.hmax,
-                                                                                        b.prm, cc, b.RH);
+      k_residues_H_leaf<8><<<gh, 128, 0, s>>>(b.Ht, Lo.kp, w, w, hall, gmax, 1, pk, cc, lt, b.RH);
+    k_residues_H_gated<<<dim3(std::min(Np, 608), rh_blocks_x(Lo.kp)), 128, 0, s>>>(b.Ht, Np, Lo.kp, N, b.hmax, pk,
+                                                                                   cc, b.RH);
   }
-  prof_mark(stream, "residues_H");
 
-  using Shape = GemmShape<G_BN>;
-  if (set_smem_attr(k_crt_gemm<G_BN, OneGemm, true>, (int)Shape::SMEM) != cudaSuccess) return PSMMA_EDEVICE;
-  int dev = 0, sms = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-    return PSMMA_EDEVICE;
-  for (int y = 0; y < nleaf; ++y) {
-    const BlkNode& lf = leaves[y];
-    OneGemm og;
-    memset(&og, 0, sizeof(og));
-    bool ok;
-    if (a_sum[y] < 0) {
-      int q = 0;
-      while (!((lf.amask >> q) & 1)) ++q;
-      ok = make_tmap_view(&og.ta, b.RA + (size_t)q * w, w, Lo.kp, M, nmod, (long)M * Lo.kp, G_BM);
-    } else {
-      ok = make_tmap_view(&og.ta, RS + (size_t)a_sum[y] * nmod * M * w, w, w, M, nmod, (long)M * w, G_BM);
-    }
-    ok = ok && make_tmap_view(&og.tb, b.RH + (size_t)y * nmod * w * w, w, w, w, nmod, (long)w * w, G_BN);
-    if (!ok) return PSMMA_EDEVICE;
-    GemmArgs& ga = og.g;
-    ga.n = M;
-    ga.kr = Lo.kr;
-    ga.nkb = w / G_BK;
-    ga.tiles_m = (M + G_BM - 1) / G_BM;
-    ga.tiles_n = (w + G_BN - 1) / G_BN;
-    ga.group_m = 16;
-    ga.nmod = nmod;
-    ga.R = b.R;
-    ga.status = &b.prm->status;
-    for (int l = 0; l < nmod; ++l) { ga.m[l] = cc.m[l]; ga.inv_m[l] = cc.inv_m[l]; }
-    ga.ndst = lf.ndst;
-    for (int d = 0; d < lf.ndst; ++d) {
-      ga.dst_col[d] = lf.dst[d] * w;
-      ga.dst_op[d] = y == 0 ? 0 : 2;  // the first leaf covers every block (block_expand takes the sums first)
-    }
-    ga.ncols = w;
-    ga.gate = &b.prm->hbad;
-    ga.gate_set = 0;
-    const int total_tiles = ga.tiles_m * ga.tiles_n * nmod;
-    k_crt_gemm<G_BN, OneGemm, true><<<std::min(sms, total_tiles), G_THREADS, Shape::SMEM, stream>>>(og);
-    prof_mark(stream, "modular_gemm");
+  // Block residues and sums of rows [r0, r0 + rows) of A (leading dimension lda).
+  void a_residues(const double* A, long lda, int r0, int rows, const SplitDevParams* pk, cudaStream_t s) {
+    const dim3 ga(w / 64, (rows + 31) / 32);
+    const int smem = NQ * 64 * 32 * 8;
+    if (NQ == 2)
+      k_residues_A_blocks<2><<<ga, 256, smem, s>>>(A, lda, M, r0, rows, w, Lo.kp, N, M, r0, b.amax, pk, cc, b.RA, RS,
+                                                    bs);
+    else if (NQ == 4)
+      k_residues_A_blocks<4><<<ga, 256, smem, s>>>(A, lda, M, r0, rows, w, Lo.kp, N, M, r0, b.amax, pk, cc, b.RA, RS,
+                                                    bs);
+    else
+      k_residues_A_blocks<8><<<ga, 256, smem, s>>>(A, lda, M, r0, rows, w, Lo.kp, N, M, r0, b.amax, pk, cc, b.RA, RS,
+                                                    bs);
   }
-  {  // the single product, when some column of H is not finite
+
+  // The leaf products of rows [r0, r0 + rows) (r0 a multiple of the 128-row tile) into R, and
+  // (gated) the single product of those rows.
+  int products(int r0, int rows, const SplitDevParams* pk, cudaStream_t s) {
+    using Shape = GemmShape<G_BN>;
+    for (int y = 0; y < nleaf; ++y) {
+      const BlkNode& lf = leaves[y];
+      OneGemm og;
+      memset(&og, 0, sizeof(og));
+      bool ok;
+      if (a_sum[y] < 0) {
+        int q = 0;
+        while (!((lf.amask >> q) & 1)) ++q;
+        ok = make_tmap_view(&og.ta, b.RA + (size_t)r0 * Lo.kp + (size_t)q * w, w, Lo.kp, rows, nmod, (long)M * Lo.kp,
+                            G_BM);
+      } else {
+        ok = make_tmap_view(&og.ta, RS + (size_t)a_sum[y] * nmod * M * w + (size_t)r0 * w, w, w, rows, nmod,
+                            (long)M * w, G_BM);
+      }
+      ok = ok && make_tmap_view(&og.tb, b.RH + (size_t)y * nmod * w * w, w, w, w, nmod, (long)w * w, G_BN);
+      if (!ok) return PSMMA_EDEVICE;
+      GemmArgs& ga = og.g;
+      ga.n = rows;
+      ga.kr = Lo.kr;
+      ga.nkb = w / G_BK;
+      ga.tiles_m = (rows + G_BM - 1) / G_BM;
+      ga.tiles_n = (w + G_BN - 1) / G_BN;
+      ga.group_m = 16;
+      ga.nmod = nmod;
+      ga.R = b.R;
+      ga.status = &b.prm->status;
+      for (int l = 0; l < nmod; ++l) { ga.m[l] = cc.m[l]; ga.inv_m[l] = cc.inv_m[l]; }
+      ga.r_rows = M;
+      ga.ndst = lf.ndst;
+      for (int d = 0; d < lf.ndst; ++d) {
+        ga.dst_row[d] = r0;
+        ga.dst_col[d] = lf.dst[d] * w;
+        ga.dst_op[d] = y == 0 ? 0 : 2;  // the first leaf covers every block (block_expand takes the sums first)
+      }
+      ga.ncols = w;
+      ga.gate = &pk->hbad;
+      ga.gate_set = 0;
+      const int total_tiles = ga.tiles_m * ga.tiles_n * nmod;
+      k_crt_gemm<G_BN, OneGemm, true><<<std::min(sms, total_tiles), G_THREADS, Shape::SMEM, s>>>(og);
+    }
+    // the single product, when some column of H is not finite or spreads too far
     OneGemm og;
     memset(&og, 0, sizeof(og));
     if (!make_tmap(&og.ta, b.RA, Lo.kp, M, nmod, G_BM) || !make_tmap(&og.tb, b.RH, Lo.kp, Np, nmod, G_BN))
@@ -2595,22 +2611,58 @@ static int split_core_block(int M, int N, int Np, int L, double alpha, const dou
     ga.n = M;
     ga.kr = Lo.kr;
     ga.nkb = Lo.kp / G_BK;
-    ga.tiles_m = (M + G_BM - 1) / G_BM;
+    ga.tm0 = r0 / G_BM;
+    ga.tiles_m = (rows + G_BM - 1) / G_BM;
     ga.tiles_n = (Np + G_BN - 1) / G_BN;
     ga.group_m = 16;
     ga.nmod = nmod;
     ga.R = b.R;
     ga.status = &b.prm->status;
     for (int l = 0; l < nmod; ++l) { ga.m[l] = cc.m[l]; ga.inv_m[l] = cc.inv_m[l]; }
-    ga.gate = &b.prm->hbad;
+    ga.gate = &pk->hbad;
     ga.gate_set = 1;
-    if (set_smem_attr(k_crt_gemm<G_BN, OneGemm>, (int)Shape::SMEM) != cudaSuccess) return PSMMA_EDEVICE;
-    k_crt_gemm<G_BN, OneGemm><<<std::min(sms, ga.tiles_m * ga.tiles_n * nmod), G_THREADS, Shape::SMEM, stream>>>(og);
+    k_crt_gemm<G_BN, OneGemm><<<std::min(sms, ga.tiles_m * ga.tiles_n * nmod), G_THREADS, Shape::SMEM, s>>>(og);
+    return cudaGetLastError() == cudaSuccess ? PSMMA_OK : PSMMA_EDEVICE;
   }
 
-  dim3 gc((N + CRT_TJ - 1) / CRT_TJ, (M + CRT_TI - 1) / CRT_TI);
-  (cc.top32 ? k_crt_combine_blocks<true> : k_crt_combine_blocks<false>)<<<gc, dim3(32, 8), 0, stream>>>(
-      b.R, M, N, Lo.kr, cc, b.amax, b.hmax, gmax, w, b.prm, alpha, beta, Q, ldq);
+  // The recombination of rows [r0, r0 + rows) (r0 a multiple of CRT_TI) into Q (rows from r0).
+  void crt(int r0, int rows, double alpha, double beta, double* Q, long ldq, const SplitDevParams* pk,
+           cudaStream_t s) {
+    const dim3 gc((N + CRT_TJ - 1) / CRT_TJ, (rows + CRT_TI - 1) / CRT_TI);
+    (cc.top32 ? k_crt_combine_blocks<true> : k_crt_combine_blocks<false>)<<<gc, dim3(32, 8), 0, s>>>(
+        b.R, M, N, Lo.kr, cc, b.amax, b.hmax, gmax, w, pk, alpha, beta, Q, ldq, r0 / CRT_TI);
+  }
+};
+
+// Q (M x N) = alpha * A (M x N) * H + beta * Q for Toeplitz / Hankel H (N x N) with L >= 1 levels
+// of the block step on the order Np >= N (block_choice; padded when Np > N).
+static int split_core_block(int M, int N, int Np, int L, double alpha, const double* A, long lda,
+                            const GenSpec& gs_in, double beta, double* Q, long ldq, int nmod, void* work,
+                            size_t lwork, cudaStream_t stream, unsigned* status_dev_out) {
+  BlockRun br;
+  int st = br.init(M, N, Np, L, gs_in, nmod, work, lwork);
+  if (st != PSMMA_OK) return st;
+  const SplitBuffers& b = br.b;
+  prof_begin(stream);
+  if (cudaMemsetAsync(work, 0, br.Lo.off_wtab, stream) != cudaSuccess) return PSMMA_EDEVICE;
+  {
+    const int kchunk = 1024;
+    dim3 g1((M + 127) / 128, (N + kchunk - 1) / kchunk);
+    k_row_absmax<<<g1, 128, 0, stream>>>(A, lda, M, N, kchunk, b.amax, b.asq);
+  }
+  prof_mark(stream, "row_scale");
+  br.h_side(nullptr, stream);
+  prof_mark(stream, "h_generate");
+  k_split_params<<<PARAMS_BLOCKS, 512, 0, stream>>>(b.prm, br.cc.log2M, M, Np, Np, b.amax, b.asq, b.hmax, b.hsq);
+  prof_mark(stream, "params");
+  br.a_residues(A, lda, 0, M, b.prm, stream);
+  prof_mark(stream, "residues_A");
+  br.h_operands(b.prm, stream);
+  prof_mark(stream, "residues_H");
+  st = br.products(0, M, b.prm, stream);
+  if (st != PSMMA_OK) return st;
+  prof_mark(stream, "modular_gemm");
+  br.crt(0, M, alpha, beta, Q, ldq, b.prm, stream);
   prof_mark(stream, "crt_combine");
   if (cudaGetLastError() != cudaSuccess) return PSMMA_EDEVICE;
   return split_status(b.prm, stream, status_dev_out);
@@ -2713,7 +2765,8 @@ static int s2_pass(S2State& st, const double* A, long lda, const unsigned long l
   const int smem = 4 * 64 * 32 * 8;
   if (set_smem_attr(k_residues_A_blocks<4>, smem) != cudaSuccess) return PSMMA_EDEVICE;
   k_residues_A_blocks<4><<<dim3(wk / 64, (h + 31) / 32), 256, smem, stream>>>(A, lda, st.M, r0, h, wk, st.kp, st.K,
-                                                                               amax, pk, st.cc, st.RA, st.RS, bs);
+                                                                               h, 0, amax, pk, st.cc, st.RA, st.RS,
+                                                                               bs);
   prof_mark(stream, "residues_A");
   using Shape = GemmShape<G_BN>;
   if (set_smem_attr(k_crt_gemm<G_BN, OneGemm, true>, (int)Shape::SMEM) != cudaSuccess) return PSMMA_EDEVICE;
@@ -3026,6 +3079,150 @@ static int split_core_host(int M, int N, int K, double alpha, const double* A_h,
   return PSMMA_OK;
 }
 
+// The host-pointer pipeline of split_core_host with the Toeplitz / Hankel block step: the same
+// uploads, row panels, speculative bit counts and downloads; per panel the A block residues,
+// the leaf products and the recombination.  The H side (generation, group maxima, the leaves'
+// H operands) runs once, before the panels.
+static int split_core_host_block(int M, int N, int Np, int L, double alpha, const double* A_h, long lda_h,
+                                 double* dA, const GenSpec& gs, double beta, double* Q_h, long ldq_h, double* dQ,
+                                 int nmod, void* work, size_t lwork, cudaStream_t s, cudaStream_t cs,
+                                 cudaEvent_t* ev, int nev, int pa_guess, int ph_guess, int* pa_out, int* ph_out) {
+  constexpr int NCH = 4, NP = 12;
+  if (nev < 2 * NP + 3) return PSMMA_EUNSUPPORTED;
+  BlockRun br;
+  const int st0 = br.init(M, N, Np, L, gs, nmod, work, lwork);
+  if (st0 != PSMMA_OK) return st0;
+  const SplitBuffers& b = br.b;
+  const bool spec = pa_guess >= 8 && ph_guess >= 8 && beta == 0.0;
+  cudaEvent_t* ev_up = ev;
+  cudaEvent_t* ev_panel = ev + NP;
+  cudaEvent_t ev_start = ev[2 * NP], ev_q = ev[2 * NP + 1], ev_done = ev[2 * NP + 2];
+  bool ok = true;
+  ok &= cudaEventRecord(ev_start, s) == cudaSuccess;
+  ok &= cudaStreamWaitEvent(cs, ev_start, 0) == cudaSuccess;
+  prof_begin(s);
+  ok &= cudaMemsetAsync(work, 0, br.Lo.off_wtab, s) == cudaSuccess;
+  if (spec) k_guess_params<<<1, 1, 0, s>>>(b.prm_guess, pa_guess, ph_guess);
+  br.h_side(spec ? b.prm_guess : nullptr, s);
+  if (spec) br.h_operands(b.prm_guess, s);
+  prof_mark(s, "h_side");
+  // row panels of whole 128-row tiles, as split_core_host cuts them
+  const int tiles_m = (M + G_BM - 1) / G_BM;
+  int pb[NP + 1], npanels = 0;
+  {
+    const int tp = (tiles_m + 7) / 8;
+    pb[0] = 0;
+    if (tp >= 4 && tiles_m > tp) {
+      pb[1] = 2;
+      pb[2] = tp;
+      npanels = 2;
+    }
+    while (tiles_m - pb[npanels] > tp) { pb[npanels + 1] = pb[npanels] + tp; ++npanels; }
+    for (int rest = tiles_m - pb[npanels], cut = 0; rest > 0; ++cut) {
+      const int t = cut < 3 ? (rest + 1) / 2 : rest;
+      pb[npanels + 1] = pb[npanels] + t;
+      ++npanels;
+      rest -= t;
+    }
+  }
+  auto panel = [&](int p, const SplitDevParams* pk) {
+    const int r0 = pb[p] * G_BM, r1 = std::min(M, pb[p + 1] * G_BM);
+    ok &= br.products(r0, r1 - r0, pk, s) == PSMMA_OK;
+    br.crt(r0, r1 - r0, alpha, beta, dQ, M, pk, s);
+    prof_mark(s, "panel_gemm_crt");
+    ok &= cudaEventRecord(ev_panel[p], s) == cudaSuccess;
+    ok &= cudaStreamWaitEvent(cs, ev_panel[p], 0) == cudaSuccess;
+    ok &= cudaMemcpy2DAsync(Q_h + r0, (size_t)ldq_h * 8, dQ + r0, (size_t)M * 8, (size_t)(r1 - r0) * 8, (size_t)N,
+                            cudaMemcpyDeviceToHost, cs) == cudaSuccess;
+    prof_mark(cs, "q_panel_down");
+  };
+  static SplitDevParams* head_pinned = nullptr;  // host calls are serialised
+  if (!head_pinned && cudaHostAlloc((void**)&head_pinned, sizeof(SplitDevParams), cudaHostAllocPortable) != cudaSuccess) {
+    head_pinned = nullptr;
+    return PSMMA_ENOMEM;
+  }
+  SplitDevParams& head = *head_pinned;
+  auto finish = [&]() {
+    if (cudaGetLastError() != cudaSuccess) ok = false;
+    ok &= cudaMemcpyAsync(head_pinned, b.prm, offsetof(SplitDevParams, rho_bits), cudaMemcpyDeviceToHost, s) ==
+          cudaSuccess;
+    prof_mark(s, "params_head");
+    prof_mark(cs, "q_download_tail");
+    ok &= cudaEventRecord(ev_done, cs) == cudaSuccess;
+    ok &= cudaStreamSynchronize(s) == cudaSuccess;
+    ok &= cudaEventSynchronize(ev_done) == cudaSuccess;
+  };
+  if (spec) {
+    for (int p = 0; p < npanels; ++p) {
+      const int r0 = pb[p] * G_BM, r1 = std::min(M, pb[p + 1] * G_BM);
+      ok &= cudaMemcpy2DAsync(dA + r0, (size_t)M * 8, A_h + r0, (size_t)lda_h * 8, (size_t)(r1 - r0) * 8,
+                              (size_t)N, cudaMemcpyHostToDevice, cs) == cudaSuccess;
+      ok &= cudaEventRecord(ev_up[p], cs) == cudaSuccess;
+      prof_mark(cs, "a_panel_up");
+    }
+    for (int p = 0; p < npanels; ++p) {
+      const int r0 = pb[p] * G_BM, r1 = std::min(M, pb[p + 1] * G_BM);
+      ok &= cudaStreamWaitEvent(s, ev_up[p], 0) == cudaSuccess;
+      const int kc = 256;
+      dim3 g1((r1 - r0 + 127) / 128, (N + kc - 1) / kc);
+      k_row_absmax<<<g1, 128, 0, s>>>(dA + r0, M, r1 - r0, N, kc, b.amax + r0, b.asq + r0);
+      br.a_residues(dA, M, r0, r1 - r0, b.prm_guess, s);
+      prof_mark(s, "panel_rows");
+      panel(p, b.prm_guess);
+    }
+    k_split_params<<<PARAMS_BLOCKS, 512, 0, s>>>(b.prm, br.cc.log2M, M, Np, Np, b.amax, b.asq, b.hmax, b.hsq);
+    finish();
+    if (!ok) return PSMMA_EDEVICE;
+    if (head.status & DEV_ERR_TIMEOUT) return PSMMA_ETIMEDOUT;
+    if (pa_out) *pa_out = head.PA;
+    if (ph_out) *ph_out = head.PH;
+    if (head.PA == pa_guess && head.PH == ph_guess) return PSMMA_OK;
+    // a wrong guess: the operands and products again with the computed bit counts
+    prof_mark(s, "redo_wrong_guess");
+    br.a_residues(dA, M, 0, M, b.prm, s);
+    br.h_operands(b.prm, s);
+    ok &= cudaEventRecord(ev_start, s) == cudaSuccess;
+    ok &= cudaStreamWaitEvent(cs, ev_start, 0) == cudaSuccess;
+    for (int p = 0; p < npanels; ++p) panel(p, b.prm);
+    finish();
+    if (!ok) return PSMMA_EDEVICE;
+    return (head.status & DEV_ERR_TIMEOUT) ? PSMMA_ETIMEDOUT : PSMMA_OK;
+  }
+  // A in column chunks, its row statistics as each lands
+  const int kchunk = 1024;
+  const int cols_per = std::max(kchunk, (N + NCH * kchunk - 1) / (NCH * kchunk) * kchunk);
+  for (int ch = 0; ch < NCH; ++ch) {
+    const int c0 = ch * cols_per, c1 = std::min(N, c0 + cols_per);
+    if (c0 >= c1) break;
+    ok &= cudaMemcpy2DAsync(dA + (size_t)c0 * M, (size_t)M * 8, A_h + (size_t)c0 * lda_h, (size_t)lda_h * 8,
+                            (size_t)M * 8, (size_t)(c1 - c0), cudaMemcpyHostToDevice, cs) == cudaSuccess;
+    ok &= cudaEventRecord(ev_up[ch], cs) == cudaSuccess;
+    prof_mark(cs, "a_chunk_up");
+    ok &= cudaStreamWaitEvent(s, ev_up[ch], 0) == cudaSuccess;
+    dim3 g1((M + 127) / 128, (c1 - c0 + kchunk - 1) / kchunk);
+    k_row_absmax<<<g1, 128, 0, s>>>(dA + (size_t)c0 * M, M, M, c1 - c0, kchunk, b.amax, b.asq);
+  }
+  if (beta != 0.0) {
+    ok &= cudaMemcpy2DAsync(dQ, (size_t)M * 8, Q_h, (size_t)ldq_h * 8, (size_t)M * 8, (size_t)N,
+                            cudaMemcpyHostToDevice, cs) == cudaSuccess;
+    ok &= cudaEventRecord(ev_q, cs) == cudaSuccess;
+  }
+  if (!ok) return PSMMA_EDEVICE;
+  prof_mark(s, "a_upload_rows");
+  k_split_params<<<PARAMS_BLOCKS, 512, 0, s>>>(b.prm, br.cc.log2M, M, Np, Np, b.amax, b.asq, b.hmax, b.hsq);
+  br.a_residues(dA, M, 0, M, b.prm, s);
+  br.h_operands(b.prm, s);
+  prof_mark(s, "params_residues");
+  if (beta != 0.0 && cudaStreamWaitEvent(s, ev_q, 0) != cudaSuccess) return PSMMA_EDEVICE;
+  for (int p = 0; p < npanels; ++p) panel(p, b.prm);
+  finish();
+  if (!ok) return PSMMA_EDEVICE;
+  if (pa_out) *pa_out = head.PA;
+  if (ph_out) *ph_out = head.PH;
+  if (head.status & DEV_ERR_TIMEOUT) return PSMMA_ETIMEDOUT;
+  return PSMMA_OK;
+}
+
 struct PhKey {
   int M, N, K, kind, nmod;
   bool operator<(const PhKey& o) const {
@@ -3038,8 +3235,9 @@ static std::map<PhKey, std::pair<int, int>> g_ph;  // (PA, PH) of the last call 
 static int split_core_host_cached(int M, int N, int K, double alpha, const double* A_h, long lda_h, double* dA,
                                   const GenSpec& gs, double beta, double* Q_h, long ldq_h, double* dQ, int nmod,
                                   void* work, size_t lwork, cudaStream_t s, cudaStream_t cs, cudaEvent_t* ev,
-                                  int nev) {
-  const PhKey key{M, N, K, gs.kind, nmod};
+                                  int nev, int block_req = -1) {
+  const BlockChoice bc = gs.k1 == 0 ? block_choice(gs.kind, N, K, block_req) : BlockChoice{0, N};
+  const PhKey key{M, bc.L > 0 ? bc.Np : N, K, gs.kind * 4 + bc.L, nmod};
   int pa_guess = -1, ph_guess = -1;
   {
     std::lock_guard<std::mutex> lk(g_ph_mu);
@@ -3047,8 +3245,11 @@ static int split_core_host_cached(int M, int N, int K, double alpha, const doubl
     if (it != g_ph.end()) std::tie(pa_guess, ph_guess) = it->second;
   }
   int pa = -1, ph = -1;
-  const int st = split_core_host(M, N, K, alpha, A_h, lda_h, dA, gs, beta, Q_h, ldq_h, dQ, nmod, work, lwork, s, cs,
-                                 ev, nev, pa_guess, ph_guess, &pa, &ph);
+  const int st = bc.L > 0 ? split_core_host_block(M, N, bc.Np, bc.L, alpha, A_h, lda_h, dA, gs, beta, Q_h, ldq_h,
+                                                  dQ, nmod, work, lwork, s, cs, ev, nev, pa_guess, ph_guess, &pa,
+                                                  &ph)
+                          : split_core_host(M, N, K, alpha, A_h, lda_h, dA, gs, beta, Q_h, ldq_h, dQ, nmod, work,
+                                            lwork, s, cs, ev, nev, pa_guess, ph_guess, &pa, &ph);
   if (!st && pa >= 8 && ph >= 8) {
     std::lock_guard<std::mutex> lk(g_ph_mu);
     if (g_ph.size() > 256) g_ph.clear();
@@ -3060,10 +3261,10 @@ static int split_core_host_cached(int M, int N, int K, double alpha, const doubl
 int launch_split_host(int kind, int n, int k, double alpha, const double* A_h, long lda_h, double* dA,
                       const double* dgen, long ldgen, double beta, double* Q_h, long ldq_h, double* dQ,
                       int n_moduli, void* work, size_t lwork, cudaStream_t s, cudaStream_t cs, cudaEvent_t* ev,
-                      int nev) {
+                      int nev, int block_levels) {
   const GenSpec gs = reference_gens(kind, dgen, ldgen, k);
   return split_core_host_cached(n, k, k, alpha, A_h, lda_h, dA, gs, beta, Q_h, ldq_h, dQ, resolve_nmod(n_moduli),
-                                work, lwork, s, cs, ev, nev);
+                                work, lwork, s, cs, ev, nev, block_levels);
 }
 
 int launch_split_host_general(int M, int N, int K, double alpha, const double* A_h, long lda_h, double* dA,

@@ -203,6 +203,30 @@ def test_split_block_step_matches_dense_oracle(kind, n, k, levels, pad, cuda):
 
 
 @pytest.mark.parametrize("kind", ["toeplitz", "hankel"])
+@pytest.mark.parametrize("n,k,levels,beta", [(1000, 8192, 0, 0.0), (700, 2000, 1, 0.0), (1300, 3000, 2, -1.5),
+                                             (300, 4096, 2, 0.5)])
+def test_split_block_step_host_pointer_path(kind, n, k, levels, beta, cuda):
+    # host arrays through the overlapped host pipeline (row panels; the second call of a shape
+    # scales with the bit counts cached from the first, the speculative panels): the same
+    # result bit for bit as the device-pointer call, which the dense oracle checks
+    import psmma_git_gb300 as P
+    A = O.cfg_matrix(n, k, seed=n + 3 * k)
+    gen = _gen(kind, k, seed=k + 13)
+    Q0 = O.cfg_matrix(n, k, seed=n + 17)
+    fn = getattr(P, "psmma_" + kind)
+    outs = []
+    for _ in range(2):
+        Qh = np.asfortranarray(Q0.copy())
+        fn(n, k, 0.75, np.asfortranarray(A), gen, beta, Qh, precision="split", block_levels=levels)
+        outs.append(Qh)
+    dev = _split(kind, n, k, 0.75, A, gen, beta, Q0, cuda, block_levels=levels)
+    np.testing.assert_array_equal(outs[0], dev)
+    np.testing.assert_array_equal(outs[1], dev)
+    if k <= 4096:
+        assert O.rel_fro(dev, O.dense_product(kind, 0.75, A, gen, beta, Q0, k)) < TOL
+
+
+@pytest.mark.parametrize("kind", ["toeplitz", "hankel"])
 @pytest.mark.parametrize("n,k,levels", [(1, 128, 1), (3, 256, 2), (2, 512, 3), (5, 130, 1), (1, 200, 2)])
 def test_split_block_step_tiny_shapes(kind, n, k, levels, cuda):
     # one to five rows, leaves of 64 columns (narrower than a GEMM tile), orders padded from
