@@ -1343,7 +1343,7 @@ __global__ void k_residues_H_dft3(const double* __restrict__ Ht, int nn, int kp,
 // The modular GEMM: for modulus l and a 128 x 256 output tile, R_l = (RA_l * RH_l^T) mod m_l.
 // Warp roles (320 threads): warps 0-7 drain the accumulator (quadrant = warp % 4, column
 // half = warp / 4), warp 8 issues TMA loads, warp 9 issues tcgen05.mma.  Two 256-column FP32
-// accumulators in tensor memory alternate between 512-deep k chunks.
+// accumulators in tensor memory alternate between 1024-deep k chunks.
 // ------------------------------------------------------------------------------------------
 constexpr int G_BM = 128, G_BN = 256, G_BK = 64;
 constexpr int G_STAGES = 4;
@@ -1406,6 +1406,7 @@ struct OneGemm {
   CUtensorMap ta, tb;
   GemmArgs g;
   static constexpr bool kGlobalMaps = false;
+  static constexpr int kSub = 1;
   __device__ int total() const { return g.tiles_m * g.tiles_n * g.nmod; }
   __device__ TileInfo tile(int t) const {
     TileInfo ti;
@@ -1434,6 +1435,7 @@ struct GroupGemm {
   const GemmDesc* d;
   int count, total_tiles;
   static constexpr bool kGlobalMaps = true;
+  static constexpr int kSub = 1;
   __device__ int total() const { return total_tiles; }
   __device__ TileInfo tile(int t) const {
     int lo = 0, hi = count - 1;
@@ -1450,6 +1452,29 @@ struct GroupGemm {
     ti.n = e.n;
     ti.kr = e.kr;
     ti.nkb = e.nkb;
+    return ti;
+  }
+};
+
+// The three real products of a 3M complex product in one launch (T1 = Ar Fr, T2 = Ai Fi,
+// T3 = (Ar + Ai)(Fr + Fi); operand maps ta[p], tb[p]), each of one chunk (k <= 1024): a tile's
+// three products run back to back on the alternating accumulators and its epilogue writes
+// Re = T1 - T2 and Im = T3 - T1 - T2 (Im at +im_off bytes) once, reading no residues back.
+struct Gemm3M {
+  CUtensorMap ta[3], tb[3];
+  GemmArgs g;
+  static constexpr bool kGlobalMaps = false;
+  static constexpr int kSub = 3;
+  __device__ int total() const { return g.tiles_m * g.tiles_n * g.nmod; }
+  __device__ TileInfo tile(int t) const {
+    TileInfo ti;
+    raster_tile(g.tiles_m, g.tiles_n, g.group_m, t, ti.l, ti.tm, ti.tn);
+    ti.ta = &ta[0];
+    ti.tb = &tb[0];
+    ti.R = g.R;
+    ti.n = g.n;
+    ti.kr = g.kr;
+    ti.nkb = g.nkb;
     return ti;
   }
 };
@@ -1472,6 +1497,43 @@ __device__ __forceinline__ int mod_sym_small(int s, int m) {
   return s;
 }
 
+// v mod m in [-128, 127] for an integer v held exactly in FP32 (|v| <= 2^24) and m <= 256, on the
+// FP32 pipe, as the bits of x + 1.5 * 2^23 (the residue x is their low byte, as an int8).  Adding
+// 1.5 * 2^23 rounds to an integer and leaves it in the low mantissa bits; q = round(v * fl(1/m))
+// is within 0.5 + 1/m of v / m, so |v - q m| <= m/2 + 1 and one correction on each side
+// suffices; v - q m is exact in the FMA.  The intrinsics keep the steps apart (no contraction).
+constexpr float kRound23 = 12582912.0f;  // 1.5 * 2^23
+__device__ __forceinline__ uint32_t mod_sym_f_bits(float v, float mf, float inv_m) {
+  const float q = __fsub_rn(__fadd_rn(__fmul_rn(v, inv_m), kRound23), kRound23);
+  float x = __fmaf_rn(-q, mf, v);
+  x = x > 127.0f ? x - mf : x;
+  x = x < -128.0f ? x + mf : x;
+  return __float_as_uint(__fadd_rn(x, kRound23));
+}
+
+// (v + a) mod m likewise, for integers v (|v| <= 2^24) and a (|a| <= 256) held in FP32: the
+// quotient comes from the rounded sum (within 1 of v + a), the remainder (v - q m) + a exactly,
+// |x| <= 0.52 m.
+__device__ __forceinline__ uint32_t mod_sym_f_bits_add(float v, float a, float mf, float inv_m) {
+  const float t = __fadd_rn(v, a);
+  const float q = __fsub_rn(__fadd_rn(__fmul_rn(t, inv_m), kRound23), kRound23);
+  float x = __fadd_rn(__fmaf_rn(-q, mf, v), a);
+  x = x > 127.0f ? x - mf : x;
+  x = x < -128.0f ? x + mf : x;
+  return __float_as_uint(__fadd_rn(x, kRound23));
+}
+
+// The low bytes of four words, packed (byte j from word j).
+__device__ __forceinline__ uint32_t pack_low_bytes(uint32_t b0, uint32_t b1, uint32_t b2, uint32_t b3) {
+  return __byte_perm(__byte_perm(b0, b1, 0x0040), __byte_perm(b2, b3, 0x0040), 0x5410);
+}
+
+// Byte j of w, a residue offset by 128 (u = x + 128), back to x as a float: 0x4B4000uu is the
+// float 1.5 * 2^23 + u.
+__device__ __forceinline__ float offset_byte_f(uint32_t w, int j) {
+  return __fsub_rn(__uint_as_float(__byte_perm(w, 0x4B400000u, 0x7650 + j)), kRound23 + 128.0f);
+}
+
 // Epilogue of the 3M complex product's second and third GEMMs: combine this tile's residues x
 // (in [-128, 127]) with those already in the output plane, 16 bytes at a time.
 // mode 1: old = T1 -> store (T1 - x) mod m, and (-T1 - x) mod m at dst + im_off;
@@ -1480,11 +1542,15 @@ __device__ __forceinline__ int mod_sym_small(int s, int m) {
 template <int HALF>
 __device__ __forceinline__ void store_combined(int8_t* dst, const int (&res)[HALF], int mode, int im_off, int m,
                                                int valid = HALF) {
+  // every 16-byte load issued before the first store (the stores at dst + im_off may alias the
+  // later loads for all the compiler knows, which would serialise the round trips)
+  uint4 ov[HALF / 16];
+#pragma unroll
+  for (int v = 0; v < HALF / 16; ++v) ov[v] = v * 16 < valid ? *(const uint4*)(dst + v * 16) : make_uint4(0u, 0u, 0u, 0u);
 #pragma unroll
   for (int v = 0; v < HALF / 16; ++v) {
     if (v * 16 >= valid) break;
-    const uint4 o = *(const uint4*)(dst + v * 16);
-    const uint32_t ow[4] = {o.x, o.y, o.z, o.w};
+    const uint32_t ow[4] = {ov[v].x, ov[v].y, ov[v].z, ov[v].w};
     uint32_t w1[4], w2[4];
 #pragma unroll
     for (int t4 = 0; t4 < 4; ++t4) {
@@ -1578,17 +1644,22 @@ __global__ void __launch_bounds__(G_THREADS, 1) k_crt_gemm(const __grid_constant
             tensormap_acquire(ti.ta);
             tensormap_acquire(ti.tb);
           }
-          prefetch_tmap(ti.ta);
-          prefetch_tmap(ti.tb);
+#pragma unroll
+          for (int sub = 0; sub < TS::kSub; ++sub) {
+            prefetch_tmap(ti.ta + sub);
+            prefetch_tmap(ti.tb + sub);
+          }
           last = ti.ta;
         }
-        for (int kb = 0; kb < ti.nkb; ++kb, ++it) {
-          const int s = it % G_STAGES;
-          if (!mbar_wait(&empty[s], ((it / G_STAGES) & 1) ^ 1, g.status, abort_flag)) { ok = false; break; }
-          mbar_arrive_expect_tx(&full[s], G_A_BYTES + S::B_BYTES);
-          tma_load_3d(sA + s * G_A_BYTES, ti.ta, &full[s], kb * G_BK, ti.tm * G_BM, ti.l);
-          tma_load_3d(sB + s * S::B_BYTES, ti.tb, &full[s], kb * G_BK, ti.tn * BN, ti.l);
-          issued = it + 1;
+        for (int sub = 0; sub < TS::kSub && ok; ++sub) {
+          for (int kb = 0; kb < ti.nkb; ++kb, ++it) {
+            const int s = it % G_STAGES;
+            if (!mbar_wait(&empty[s], ((it / G_STAGES) & 1) ^ 1, g.status, abort_flag)) { ok = false; break; }
+            mbar_arrive_expect_tx(&full[s], G_A_BYTES + S::B_BYTES);
+            tma_load_3d(sA + s * G_A_BYTES, ti.ta + sub, &full[s], kb * G_BK, ti.tm * G_BM, ti.l);
+            tma_load_3d(sB + s * S::B_BYTES, ti.tb + sub, &full[s], kb * G_BK, ti.tn * BN, ti.l);
+            issued = it + 1;
+          }
         }
       }
       // every issued copy must have landed before the CTA may exit
@@ -1604,16 +1675,17 @@ __global__ void __launch_bounds__(G_THREADS, 1) k_crt_gemm(const __grid_constant
       bool ok = true;
       for (int t = blockIdx.x; t < total && ok; t += gridDim.x) {
         const int nkb = ts.tile(t).nkb;
-        const int cpt = (nkb + G_CHUNK_KB - 1) / G_CHUNK_KB;  // chunks of this tile
-        for (int cc = 0; cc < cpt && ok; ++cc, ++c) {
+        const int cpt = (nkb + G_CHUNK_KB - 1) / G_CHUNK_KB;  // chunks of each product of this tile
+        for (int cc = 0; cc < TS::kSub * cpt && ok; ++cc, ++c) {
           const int buf = c & 1;
           const uint32_t use = (uint32_t)(c >> 1);
           if (!mbar_wait(&acc_empty[buf], (use & 1) ^ 1, g.status, abort_flag)) { ok = false; break; }
           tc_fence_after();
           const uint32_t dt = tmem_base + (uint32_t)(buf * BN);
-          const int kend = min(nkb, (cc + 1) * G_CHUNK_KB);
+          const int kb0 = (cc % cpt) * G_CHUNK_KB;
+          const int kend = min(nkb, kb0 + G_CHUNK_KB);
           uint32_t acc = 0;
-          for (int kb = cc * G_CHUNK_KB; kb < kend; ++kb, ++it) {
+          for (int kb = kb0; kb < kend; ++kb, ++it) {
             const int s = it % G_STAGES;
             if (!mbar_wait(&full[s], (it / G_STAGES) & 1, g.status, abort_flag)) { ok = false; break; }
             tc_fence_after();
@@ -1644,109 +1716,167 @@ __global__ void __launch_bounds__(G_THREADS, 1) k_crt_gemm(const __grid_constant
       const int cpt = (ti.nkb + G_CHUNK_KB - 1) / G_CHUNK_KB;
       const int mi = g.m[ti.l];
       const float inv_m = g.inv_m[ti.l];
-      // int32 running sums of the chunks' exact FP32 sums (|chunk| <= 2^24), reduced to
-      // [-128, 127] every G_RED_CHUNKS chunks and at the end of the tile
-      int res[HALF];
-#pragma unroll
-      for (int e = 0; e < HALF; ++e) res[e] = 0;
-      for (int cc = 0; cc < cpt; ++cc, ++c) {
-        const int buf = c & 1;
-        const uint32_t use = (uint32_t)(c >> 1);
-        if (!mbar_wait(&acc_full[buf], use & 1, g.status, abort_flag)) { ok = false; break; }
-        tc_fence_after();
-#pragma unroll
-        for (int cb = 0; cb < HALF / 32; ++cb) {
-          uint32_t r[32];
-          tmem_ld32(tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * BN + h * HALF + cb * 32), r);
-          tmem_ld_wait();
-#pragma unroll
-          for (int e = 0; e < 32; ++e) res[cb * 32 + e] += __float2int_rn(__uint_as_float(r[e]));
-        }
-        tc_fence_before();
-        mbar_arrive(&acc_empty[buf]);
-        if ((cc % G_RED_CHUNKS) == G_RED_CHUNKS - 1 || cc == cpt - 1) {
-#pragma unroll
-          for (int e = 0; e < HALF; ++e) res[e] = mod_sym(res[e], mi, inv_m);
-        }
-      }
-      const int i = ti.tm * G_BM + q * 32 + lane;
-      if (MULTI) {
-        // per place every 16-byte load issued before the first add: one round trip per place
+      if constexpr (TS::kSub == 3) {
+        // T1 -> x1 (kept); T2 -> Re = x1 - T2 (stored) and s = -x1 - T2 (kept); T3 -> Im = s + T3
+        // (stored).  Residues on the FP32 pipe from the exact sums; kept residues are bytes
+        // offset by 128, four to a word.  The epilogue work is spread over the three drains,
+        // each within the next product's MMA time.
+        const int i = ti.tm * G_BM + q * 32 + lane;
         const int col0 = ti.tn * BN + h * HALF;
-        const int valid = g.ncols > 0 ? g.ncols - col0 : HALF;  // columns of this half in the product
-        if (ok && !*abort_flag && i < ti.n && valid > 0) {
-          // the residues packed to bytes (32 registers instead of 128); the volatile move keeps
-          // the compiler from re-deriving them from the int32 sums inside the place loop,
-          // which would keep all 128 sums live there and spill
-          uint32_t pk[HALF / 4];
+        const float mf = (float)mi;
+        int8_t* dst = ti.R + ((size_t)ti.l * ti.n + (size_t)min(i, ti.n - 1)) * ti.kr + (size_t)col0;
+        uint32_t p1[HALF / 4], ps[HALF / 4];
 #pragma unroll
-          for (int e4 = 0; e4 < HALF / 4; ++e4) {
-            const uint32_t pv = (uint32_t)(uint8_t)(int8_t)res[4 * e4] |
-                                ((uint32_t)(uint8_t)(int8_t)res[4 * e4 + 1] << 8) |
-                                ((uint32_t)(uint8_t)(int8_t)res[4 * e4 + 2] << 16) |
-                                ((uint32_t)(uint8_t)(int8_t)res[4 * e4 + 3] << 24);
-            asm volatile("mov.b32 %0, %1;" : "=r"(pk[e4]) : "r"(pv));
-          }
-          const int nd = g.ndst > 0 ? g.ndst : 1;
-          const size_t plane_rows = g.r_rows > 0 ? (size_t)g.r_rows : (size_t)ti.n;
-          for (int d = 0; d < nd; ++d) {
-            int8_t* dst = ti.R + ((size_t)ti.l * plane_rows + i + (g.ndst > 0 ? g.dst_row[d] : 0)) * ti.kr +
-                          (size_t)col0 + (g.ndst > 0 ? g.dst_col[d] : 0);
-            const int op = g.ndst > 0 ? g.dst_op[d] : g.mode;
-            if (op >= 2) {
-              uint4 o[HALF / 16];
+        for (int sub = 0; sub < 3; ++sub) {
+          const int buf = c & 1;
+          const uint32_t use = (uint32_t)(c >> 1);
+          if (!mbar_wait(&acc_full[buf], use & 1, g.status, abort_flag)) { ok = false; break; }
+          ++c;
+          tc_fence_after();
+          const bool store = sub > 0 && !*abort_flag && i < ti.n;
 #pragma unroll
-              for (int v = 0; v < HALF / 16; ++v)
-                o[v] = v * 16 < valid ? *(const uint4*)(dst + v * 16) : make_uint4(0u, 0u, 0u, 0u);
+          for (int cb = 0; cb < HALF / 32; ++cb) {
+            uint32_t r[32];
+            tmem_ld32(tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * BN + h * HALF + cb * 32), r);
+            tmem_ld_wait();
+            uint32_t wa[8], wb[8];
 #pragma unroll
-              for (int v = 0; v < HALF / 16; ++v) {
-                if (v * 16 >= valid) break;
-                const uint32_t ow[4] = {o[v].x, o[v].y, o[v].z, o[v].w};
-                uint32_t nw[4];
+            for (int e4 = 0; e4 < 8; ++e4) {
+              uint32_t ba[4], bb4[4];
 #pragma unroll
-                for (int t4 = 0; t4 < 4; ++t4) {
-                  nw[t4] = 0u;
-#pragma unroll
-                  for (int bb = 0; bb < 4; ++bb) {
-                    const int x = (int)(int8_t)(pk[4 * v + t4] >> (8 * bb));
-                    const int a = (int)(int8_t)(ow[t4] >> (8 * bb)) + (op == 3 ? -x : x);
-                    nw[t4] |= (uint32_t)(uint8_t)(int8_t)mod_sym_small(a, mi) << (8 * bb);
-                  }
+              for (int bb = 0; bb < 4; ++bb) {
+                const float v = __uint_as_float(r[4 * e4 + bb]);
+                if (sub == 0) {
+                  ba[bb] = mod_sym_f_bits(v, mf, inv_m);
+                } else if (sub == 1) {
+                  const float x1 = offset_byte_f(p1[cb * 8 + e4], bb);
+                  ba[bb] = mod_sym_f_bits_add(-v, x1, mf, inv_m);   // x1 - T2
+                  bb4[bb] = mod_sym_f_bits_add(-v, -x1, mf, inv_m);  // -x1 - T2
+                } else {
+                  ba[bb] = mod_sym_f_bits_add(v, offset_byte_f(ps[cb * 8 + e4], bb), mf, inv_m);  // s + T3
                 }
-                *(uint4*)(dst + v * 16) = make_uint4(nw[0], nw[1], nw[2], nw[3]);
               }
-            } else {
-#pragma unroll
-              for (int v = 0; v < HALF / 16; ++v)
-                if (v * 16 < valid)
-                  *(uint4*)(dst + v * 16) = make_uint4(pk[4 * v], pk[4 * v + 1], pk[4 * v + 2], pk[4 * v + 3]);
+              wa[e4] = pack_low_bytes(ba[0], ba[1], ba[2], ba[3]);
+              if (sub == 0) p1[cb * 8 + e4] = wa[e4] ^ 0x80808080u;
+              if (sub == 1) {
+                wb[e4] = pack_low_bytes(bb4[0], bb4[1], bb4[2], bb4[3]);
+                ps[cb * 8 + e4] = wb[e4] ^ 0x80808080u;
+              }
+            }
+            if (store) {
+              int8_t* o = dst + (sub == 2 ? g.im_off : 0) + cb * 32;
+              *(uint4*)o = make_uint4(wa[0], wa[1], wa[2], wa[3]);
+              *(uint4*)(o + 16) = make_uint4(wa[4], wa[5], wa[6], wa[7]);
             }
           }
+          tc_fence_before();
+          mbar_arrive(&acc_empty[buf]);
         }
-        continue;
-      }
-      const int col0 = ti.tn * BN + h * HALF;
-      const int valid = HALF;
-      const int nd = 1;
-      for (int d = 0; d < nd && ok && !*abort_flag && i < ti.n && valid > 0; ++d) {
-        int8_t* dst = ti.R + ((size_t)ti.l * ti.n + i) * ti.kr + (size_t)col0;
-        if (g.mode != 0) {
-          store_combined<HALF>(dst, res, g.mode, g.im_off, mi, valid);
+      } else {
+        // int32 running sums of the chunks' exact FP32 sums (|chunk| <= 2^24), reduced to
+        // [-128, 127] every G_RED_CHUNKS chunks and at the end of the tile
+        int res[HALF];
+#pragma unroll
+        for (int e = 0; e < HALF; ++e) res[e] = 0;
+        for (int cc = 0; cc < cpt; ++cc, ++c) {
+          const int buf = c & 1;
+          const uint32_t use = (uint32_t)(c >> 1);
+          if (!mbar_wait(&acc_full[buf], use & 1, g.status, abort_flag)) { ok = false; break; }
+          tc_fence_after();
+#pragma unroll
+          for (int cb = 0; cb < HALF / 32; ++cb) {
+            uint32_t r[32];
+            tmem_ld32(tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * BN + h * HALF + cb * 32), r);
+            tmem_ld_wait();
+#pragma unroll
+            for (int e = 0; e < 32; ++e) res[cb * 32 + e] += __float2int_rn(__uint_as_float(r[e]));
+          }
+          tc_fence_before();
+          mbar_arrive(&acc_empty[buf]);
+          if ((cc % G_RED_CHUNKS) == G_RED_CHUNKS - 1 || cc == cpt - 1) {
+#pragma unroll
+            for (int e = 0; e < HALF; ++e) res[e] = mod_sym(res[e], mi, inv_m);
+          }
+        }
+        const int i = ti.tm * G_BM + q * 32 + lane;
+        if (MULTI) {
+          // per place every 16-byte load issued before the first add: one round trip per place
+          const int col0 = ti.tn * BN + h * HALF;
+          const int valid = g.ncols > 0 ? g.ncols - col0 : HALF;  // columns of this half in the product
+          if (ok && !*abort_flag && i < ti.n && valid > 0) {
+            // the residues packed to bytes (32 registers instead of 128); the volatile move keeps
+            // the compiler from re-deriving them from the int32 sums inside the place loop,
+            // which would keep all 128 sums live there and spill
+            uint32_t pk[HALF / 4];
+#pragma unroll
+            for (int e4 = 0; e4 < HALF / 4; ++e4) {
+              const uint32_t pv = (uint32_t)(uint8_t)(int8_t)res[4 * e4] |
+                                  ((uint32_t)(uint8_t)(int8_t)res[4 * e4 + 1] << 8) |
+                                  ((uint32_t)(uint8_t)(int8_t)res[4 * e4 + 2] << 16) |
+                                  ((uint32_t)(uint8_t)(int8_t)res[4 * e4 + 3] << 24);
+              asm volatile("mov.b32 %0, %1;" : "=r"(pk[e4]) : "r"(pv));
+            }
+            const int nd = g.ndst > 0 ? g.ndst : 1;
+            const size_t plane_rows = g.r_rows > 0 ? (size_t)g.r_rows : (size_t)ti.n;
+            for (int d = 0; d < nd; ++d) {
+              int8_t* dst = ti.R + ((size_t)ti.l * plane_rows + i + (g.ndst > 0 ? g.dst_row[d] : 0)) * ti.kr +
+                            (size_t)col0 + (g.ndst > 0 ? g.dst_col[d] : 0);
+              const int op = g.ndst > 0 ? g.dst_op[d] : g.mode;
+              if (op >= 2) {
+                uint4 o[HALF / 16];
+#pragma unroll
+                for (int v = 0; v < HALF / 16; ++v)
+                  o[v] = v * 16 < valid ? *(const uint4*)(dst + v * 16) : make_uint4(0u, 0u, 0u, 0u);
+#pragma unroll
+                for (int v = 0; v < HALF / 16; ++v) {
+                  if (v * 16 >= valid) break;
+                  const uint32_t ow[4] = {o[v].x, o[v].y, o[v].z, o[v].w};
+                  uint32_t nw[4];
+#pragma unroll
+                  for (int t4 = 0; t4 < 4; ++t4) {
+                    nw[t4] = 0u;
+#pragma unroll
+                    for (int bb = 0; bb < 4; ++bb) {
+                      const int x = (int)(int8_t)(pk[4 * v + t4] >> (8 * bb));
+                      const int a = (int)(int8_t)(ow[t4] >> (8 * bb)) + (op == 3 ? -x : x);
+                      nw[t4] |= (uint32_t)(uint8_t)(int8_t)mod_sym_small(a, mi) << (8 * bb);
+                    }
+                  }
+                  *(uint4*)(dst + v * 16) = make_uint4(nw[0], nw[1], nw[2], nw[3]);
+                }
+              } else {
+#pragma unroll
+                for (int v = 0; v < HALF / 16; ++v)
+                  if (v * 16 < valid)
+                    *(uint4*)(dst + v * 16) = make_uint4(pk[4 * v], pk[4 * v + 1], pk[4 * v + 2], pk[4 * v + 3]);
+              }
+            }
+          }
           continue;
         }
-#pragma unroll
-        for (int v = 0; v < HALF / 16; ++v) {
-          if (v * 16 >= valid) break;
-          uint32_t w[4];
-#pragma unroll
-          for (int t4 = 0; t4 < 4; ++t4) {
-            uint32_t b0 = (uint32_t)(uint8_t)(int8_t)res[v * 16 + t4 * 4 + 0];
-            uint32_t b1 = (uint32_t)(uint8_t)(int8_t)res[v * 16 + t4 * 4 + 1];
-            uint32_t b2 = (uint32_t)(uint8_t)(int8_t)res[v * 16 + t4 * 4 + 2];
-            uint32_t b3 = (uint32_t)(uint8_t)(int8_t)res[v * 16 + t4 * 4 + 3];
-            w[t4] = b0 | (b1 << 8) | (b2 << 16) | (b3 << 24);
+        const int col0 = ti.tn * BN + h * HALF;
+        const int valid = HALF;
+        const int nd = 1;
+        for (int d = 0; d < nd && ok && !*abort_flag && i < ti.n && valid > 0; ++d) {
+          int8_t* dst = ti.R + ((size_t)ti.l * ti.n + i) * ti.kr + (size_t)col0;
+          if (g.mode != 0) {
+            store_combined<HALF>(dst, res, g.mode, g.im_off, mi, valid);
+            continue;
           }
-          *(uint4*)(dst + v * 16) = make_uint4(w[0], w[1], w[2], w[3]);
+#pragma unroll
+          for (int v = 0; v < HALF / 16; ++v) {
+            if (v * 16 >= valid) break;
+            uint32_t w[4];
+#pragma unroll
+            for (int t4 = 0; t4 < 4; ++t4) {
+              uint32_t b0 = (uint32_t)(uint8_t)(int8_t)res[v * 16 + t4 * 4 + 0];
+              uint32_t b1 = (uint32_t)(uint8_t)(int8_t)res[v * 16 + t4 * 4 + 1];
+              uint32_t b2 = (uint32_t)(uint8_t)(int8_t)res[v * 16 + t4 * 4 + 2];
+              uint32_t b3 = (uint32_t)(uint8_t)(int8_t)res[v * 16 + t4 * 4 + 3];
+              w[t4] = b0 | (b1 << 8) | (b2 << 16) | (b3 << 24);
+            }
+            *(uint4*)(dst + v * 16) = make_uint4(w[0], w[1], w[2], w[3]);
+          }
         }
       }
     }
@@ -3305,14 +3435,39 @@ static int dft3_enqueue(int M, int nn, double alpha, const double* B, long ldb, 
   prof_mark(stream, "residues_H");
 
   using Shape = GemmShape<G_BN>;
-  if (set_smem_attr(k_crt_gemm<G_BN, OneGemm>, (int)Shape::SMEM) != cudaSuccess)
-    return PSMMA_EDEVICE;
   int dev = 0, sms = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
     return PSMMA_EDEVICE;
-  // T1 into the Re half; T2: Re = T1 - T2, Im = -T1 - T2; T3: Im += T3
   const int kr1 = L.kr / 2;
-  for (int p = 0; p < 3; ++p) {
+  if (L.kp / G_BK <= G_CHUNK_KB) {
+    // one chunk per product: the three products in one launch, Re and Im written once
+    if (set_smem_attr(k_crt_gemm<G_BN, Gemm3M>, (int)Shape::SMEM) != cudaSuccess) return PSMMA_EDEVICE;
+    Gemm3M g3;
+    memset(&g3, 0, sizeof(g3));
+    for (int p = 0; p < 3; ++p)
+      if (!make_tmap(&g3.ta[p], b.RA + (size_t)p * nmod * M * L.kp, L.kp, M, nmod, G_BM) ||
+          !make_tmap(&g3.tb[p], b.RH + (size_t)p * nmod * nn * L.kp, L.kp, nn, nmod, G_BN))
+        return PSMMA_EDEVICE;
+    GemmArgs& ga = g3.g;
+    ga.n = M;
+    ga.kr = L.kr;
+    ga.nkb = L.kp / G_BK;
+    ga.tiles_m = (M + G_BM - 1) / G_BM;
+    ga.tiles_n = (nn + G_BN - 1) / G_BN;
+    ga.group_m = 16;
+    ga.R = b.R;
+    ga.status = &b.prm->status;
+    ga.nmod = nmod;
+    ga.im_off = kr1;
+    for (int l = 0; l < nmod; ++l) { ga.m[l] = cc.m[l]; ga.inv_m[l] = cc.inv_m[l]; }
+    const int total_tiles = ga.tiles_m * ga.tiles_n * nmod;
+    k_crt_gemm<G_BN, Gemm3M><<<std::min(sms, total_tiles), G_THREADS, Shape::SMEM, stream>>>(g3);
+    prof_mark(stream, "gemm_3m");
+  }
+  if (L.kp / G_BK > G_CHUNK_KB && set_smem_attr(k_crt_gemm<G_BN, OneGemm>, (int)Shape::SMEM) != cudaSuccess)
+    return PSMMA_EDEVICE;
+  // T1 into the Re half; T2: Re = T1 - T2, Im = -T1 - T2; T3: Im += T3
+  for (int p = 0; p < 3 && L.kp / G_BK > G_CHUNK_KB; ++p) {
     OneGemm og;
     memset(&og, 0, sizeof(og));
     __nv_bfloat16* ra = b.RA + (size_t)p * nmod * M * L.kp;
