@@ -218,17 +218,16 @@ static int dft_radix(int n) {
   return 1;
 }
 
-// Radix-R workspace: the core's (M = R k, n / R) layout, then B' and P (n x k complex each) and
-// the n-entry table w_n^t.
+// Radix-R workspace: the core's (M = R k, n / R) layout, then B' (n x k complex) and the
+// n-entry table w_n^t.
 struct DftRadixLayout {
-  size_t core, off_bp, off_p, off_w, total;
+  size_t core, off_bp, off_w, total;
 };
 static DftRadixLayout dft_radix_layout(int n, int k, int R, int nmod) {
   DftRadixLayout D;
   D.core = al1k(dft3_layout(R * k, n / R, nmod).total);
   D.off_bp = D.core;
-  D.off_p = D.off_bp + al1k((size_t)n * k * 16);
-  D.off_w = D.off_p + al1k((size_t)n * k * 16);
+  D.off_w = D.off_bp + al1k((size_t)n * k * 16);
   D.total = D.off_w + al1k((size_t)n * 16);
   return D;
 }
@@ -1166,6 +1165,92 @@ __global__ void k_row_absmax_dft(const double* __restrict__ Bre, long ldb2, int 
   }
 }
 
+// The radix step's B' (as k_dft_deinterleave: B'(m, r k + c) = B(R m + r, c), ld n/R) and, in
+// the same pass over B, the statistics k_row_absmax_dft takes of the product's rows (the
+// columns of B').  Block c takes column c of B; with 256 a multiple of R, thread t meets only
+// entries l = t mod R, i.e. row r k + c for r = t mod R, and the threads of one r are reduced
+// together (lanes xor 16 .. R, then the eight warps).
+template <int R>
+__global__ void __launch_bounds__(256) k_dft_deinterleave_stats(const double2* __restrict__ B, long ldb, int n,
+                                                                int k, double2* __restrict__ Bp,
+                                                                unsigned long long* __restrict__ amax_bits,
+                                                                double* __restrict__ asq) {
+  static_assert(256 % R == 0 && R <= 32, "a thread meets one residue class of l mod R");
+  const int nq = n / R;
+  const int r = threadIdx.x % R;
+  const int wid = threadIdx.x >> 5, ln = threadIdx.x & 31;
+  __shared__ unsigned long long smax[8][R];
+  __shared__ double ssq[8][R];
+  for (int c = blockIdx.x; c < k; c += gridDim.x) {
+    const double2* col = B + (long)c * ldb;
+    double2* dst = Bp + ((size_t)r * k + c) * nq;
+    unsigned long long mb = 0;
+    // as k_row_absmax_dft: round-up FP32 squares on the thread's power-of-two scale, FP64 for a
+    // thread whose entries reach 2^56 times its first one
+    float sq32 = 0.0f;
+    int e = NO_SCALE;
+    bool big = false;
+    for (int l = threadIdx.x; l < n; l += 256) {
+      const double2 v = __ldg(col + l);
+      dst[l / R] = v;
+      const unsigned long long b0 = (unsigned long long)__double_as_longlong(v.x) & ABS_MASK;
+      const unsigned long long b1 = (unsigned long long)__double_as_longlong(v.y) & ABS_MASK;
+      mb = b0 > mb ? b0 : mb;
+      mb = b1 > mb ? b1 : mb;
+      if (e == NO_SCALE && (b0 | b1)) e = (int)((b0 ? b0 : b1) >> 52) - 1023;
+      if (e != NO_SCALE) {
+        const float f0 = abs_scaled_up(b0, e, &big), f1 = abs_scaled_up(b1, e, &big);
+        sq32 = __fmaf_ru(f0, f0, sq32);
+        sq32 = __fmaf_ru(f1, f1, sq32);
+      }
+    }
+    double sq = 0.0;
+    if (big) {
+      for (int l = threadIdx.x; l < n; l += 256) {
+        const double2 v = __ldg(col + l);
+        sq = fma(v.x, v.x, sq);
+        sq = fma(v.y, v.y, sq);
+      }
+    } else if (e != NO_SCALE) {
+      sq = ldexp((double)sq32, 2 * e);
+    }
+    for (int o = 16; o >= R; o >>= 1) {
+      const unsigned long long ob = __shfl_xor_sync(0xffffffffu, mb, o);
+      mb = ob > mb ? ob : mb;
+      sq += __shfl_xor_sync(0xffffffffu, sq, o);
+    }
+    if (ln < R) {
+      smax[wid][ln] = mb;
+      ssq[wid][ln] = sq;
+    }
+    __syncthreads();
+    if (threadIdx.x < R) {
+      unsigned long long m2 = smax[0][threadIdx.x];
+      double s2 = ssq[0][threadIdx.x];
+      for (int w = 1; w < 8; ++w) {
+        m2 = smax[w][threadIdx.x] > m2 ? smax[w][threadIdx.x] : m2;
+        s2 += ssq[w][threadIdx.x];
+      }
+      amax_bits[(size_t)threadIdx.x * k + c] = m2;
+      asq[(size_t)threadIdx.x * k + c] = s2;
+    }
+    __syncthreads();  // the shared partials are reused for the next column
+  }
+}
+
+// The radix step around the 3M core: B (n x k complex, ldb) deinterleaved into Bp; the result
+// C (n x k complex, ldc) = alpha F_n B + beta C from the core's residues with the table wn.
+struct DftRadixSrc {
+  const double2* B;
+  long ldb;
+  int n, k, R;
+  double2* Bp;
+  const double2* wn;
+  double beta;
+  double2* C;
+  long ldc;
+};
+
 // ---- the DFT as three real products (3M form) ----------------------------------------------
 // C^T = B^T F with F(j, l) = w^(j l), w = exp(-2 pi i / n), F symmetric: Re = T1 - T2 and
 // Im = T3 - T1 - T2 for T1 = Br^T Fr, T2 = Bi^T Fi, T3 = (Br + Bi)^T (Fr + Fi).  Rows of A (columns
@@ -1952,6 +2037,82 @@ __device__ __forceinline__ int dft_col(int rc, int nn, int kr) {
   return (im >= 0 && im < nn) ? im : -1;
 }
 
+// The CRT of four neighbouring columns of one row: the residue words of the moduli at rp (a
+// 4-byte aligned address in the first plane; planes plane_w words apart), ab the row's maximum
+// (its exponent with PA), hb / fexp the columns' maxima and exponents; val = Z 2^-(s + f), NaN
+// for a non-finite row or column, 0 for a zero one.
+template <bool TOP32>
+__device__ __forceinline__ void crt_row4(const int8_t* __restrict__ rp, size_t plane_w, const CrtConsts& cc,
+                                         unsigned long long ab, int PA, const unsigned long long (&hb)[4],
+                                         const int (&fexp)[4], double (&val)[4]) {
+  const int sexp = (ab != 0 && ab < INF_BITS) ? scale_exp(ab, PA) : 0;
+  unsigned long long acc[4][4];
+  unsigned acc3[4];
+  int qi[4];
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    qi[c] = 0;
+    acc3[c] = 0;
+#pragma unroll
+    for (int t = 0; t < 4; ++t) acc[c][t] = 0;
+  }
+  const uint32_t* src = (const uint32_t*)rp;
+  // all residue words first (the loads are then in flight together), then the sums
+  uint32_t wl[SPL_MAX_MODULI];
+#pragma unroll
+  for (int l = 0; l < SPL_MAX_MODULI; ++l) wl[l] = (l < cc.nmod) ? __ldg(src + (size_t)l * plane_w) : 0u;
+#pragma unroll
+  for (int l = 0; l < SPL_MAX_MODULI; ++l) {
+    if (l >= cc.nmod) break;
+    const uint32_t w4 = wl[l];
+    const int ff = cc.ffix[l];
+    const unsigned c0 = cc.climb[l][0], c1 = cc.climb[l][1], c2 = cc.climb[l][2], c3 = cc.climb[l][3];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const int r = (int)(int8_t)(w4 >> (8 * c));
+      qi[c] += r * ff;
+      const unsigned ur = (unsigned)(r + 128);
+      acc[c][0] += (unsigned long long)ur * c0;
+      acc[c][1] += (unsigned long long)ur * c1;
+      acc[c][2] += (unsigned long long)ur * c2;
+      if (TOP32)
+        acc3[c] += ur * c3;
+      else
+        acc[c][3] += (unsigned long long)ur * c3;
+    }
+  }
+  if (TOP32) {
+#pragma unroll
+    for (int c = 0; c < 4; ++c) acc[c][3] = acc3[c];
+  }
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    if (ab >= INF_BITS || hb[c] >= INF_BITS) {
+      val[c] = __longlong_as_double(0x7FF8000000000000ll);  // NaN: non-finite input row/column
+    } else if (ab != 0 && hb[c] != 0) {
+      // Z = sum_l r_l C_l - q*M in signed 64-bit limbs (|limb terms| < 2^46), then carries
+      const long long q = (long long)((qi[c] + (1 << 18)) >> 19);
+      long long z0 = (long long)acc[c][0] - (long long)cc.biasl[0] - q * (long long)cc.Mlimb[0];
+      long long z1 = (long long)acc[c][1] - (long long)cc.biasl[1] - q * (long long)cc.Mlimb[1];
+      long long z2 = (long long)acc[c][2] - (long long)cc.biasl[2] - q * (long long)cc.Mlimb[2];
+      long long z3 = (long long)acc[c][3] - (long long)cc.biasl[3] - q * (long long)cc.Mlimb[3];
+      z1 += z0 >> 32;
+      z2 += z1 >> 32;
+      z3 += z2 >> 32;  // exact: z3 holds the sign and top bits of Z (|Z| < 2^126)
+      const unsigned long long L0 = (unsigned long long)z0 & 0xFFFFFFFFull;
+      const unsigned long long L1 = (unsigned long long)z1 & 0xFFFFFFFFull;
+      const unsigned long long L2 = (unsigned long long)z2 & 0xFFFFFFFFull;
+      unsigned long long hi = ((unsigned long long)z3 << 32) | L2, lo = (L1 << 32) | L0;
+      const bool neg = z3 < 0;
+      if (neg) {  // two's-complement negate of the 128-bit value
+        lo = ~lo + 1;
+        hi = ~hi + (lo == 0 ? 1 : 0);
+      }
+      val[c] = u128w_scaled(hi, lo, neg, sexp + fexp[c]);
+    }
+  }
+}
+
 // DFT_OUT: the product is C^T (rows = columns of C, k = n its column count) with Re in R
 // columns [0, n) and Im in [kr/2, kr/2 + n) (the 3M layout); Re / Im of element (i, j) go to
 // the interleaved complex C at 2j / 2j + 1 + i*ldq (ldq in doubles); column j's exponent is
@@ -1988,75 +2149,7 @@ __device__ __forceinline__ void crt_combine_blk(const int8_t* __restrict__ R, in
   for (int a = 0; a < CRT_TI / 8; ++a) {
     const int il = ty + 8 * a, i = i0 + il;
     double val[4] = {0.0, 0.0, 0.0, 0.0};
-    if (i < n && jb < kcols) {
-      const unsigned long long ab = amax_bits[i];
-      const int sexp = (ab != 0 && ab < INF_BITS) ? scale_exp(ab, PA) : 0;
-      unsigned long long acc[4][4];
-      unsigned acc3[4];
-      int qi[4];
-#pragma unroll
-      for (int c = 0; c < 4; ++c) {
-        qi[c] = 0;
-        acc3[c] = 0;
-#pragma unroll
-        for (int t = 0; t < 4; ++t) acc[c][t] = 0;
-      }
-      const uint32_t* src = (const uint32_t*)(R + (size_t)i * kr + jb);
-      // all residue words first (the loads are then in flight together), then the sums
-      uint32_t wl[SPL_MAX_MODULI];
-#pragma unroll
-      for (int l = 0; l < SPL_MAX_MODULI; ++l) wl[l] = (l < cc.nmod) ? __ldg(src + (size_t)l * plane_w) : 0u;
-#pragma unroll
-      for (int l = 0; l < SPL_MAX_MODULI; ++l) {
-        if (l >= cc.nmod) break;
-        const uint32_t w4 = wl[l];
-        const int ff = cc.ffix[l];
-        const unsigned c0 = cc.climb[l][0], c1 = cc.climb[l][1], c2 = cc.climb[l][2], c3 = cc.climb[l][3];
-#pragma unroll
-        for (int c = 0; c < 4; ++c) {
-          const int r = (int)(int8_t)(w4 >> (8 * c));
-          qi[c] += r * ff;
-          const unsigned ur = (unsigned)(r + 128);
-          acc[c][0] += (unsigned long long)ur * c0;
-          acc[c][1] += (unsigned long long)ur * c1;
-          acc[c][2] += (unsigned long long)ur * c2;
-          if (TOP32)
-            acc3[c] += ur * c3;
-          else
-            acc[c][3] += (unsigned long long)ur * c3;
-        }
-      }
-      if (TOP32) {
-#pragma unroll
-        for (int c = 0; c < 4; ++c) acc[c][3] = acc3[c];
-      }
-#pragma unroll
-      for (int c = 0; c < 4; ++c) {
-        if (ab >= INF_BITS || hb[c] >= INF_BITS) {
-          val[c] = __longlong_as_double(0x7FF8000000000000ll);  // NaN: non-finite input row/column
-        } else if (ab != 0 && hb[c] != 0) {
-          // Z = sum_l r_l C_l - q*M in signed 64-bit limbs (|limb terms| < 2^46), then carries
-          const long long q = (long long)((qi[c] + (1 << 18)) >> 19);
-          long long z0 = (long long)acc[c][0] - (long long)cc.biasl[0] - q * (long long)cc.Mlimb[0];
-          long long z1 = (long long)acc[c][1] - (long long)cc.biasl[1] - q * (long long)cc.Mlimb[1];
-          long long z2 = (long long)acc[c][2] - (long long)cc.biasl[2] - q * (long long)cc.Mlimb[2];
-          long long z3 = (long long)acc[c][3] - (long long)cc.biasl[3] - q * (long long)cc.Mlimb[3];
-          z1 += z0 >> 32;
-          z2 += z1 >> 32;
-          z3 += z2 >> 32;  // exact: z3 holds the sign and top bits of Z (|Z| < 2^126)
-          const unsigned long long L0 = (unsigned long long)z0 & 0xFFFFFFFFull;
-          const unsigned long long L1 = (unsigned long long)z1 & 0xFFFFFFFFull;
-          const unsigned long long L2 = (unsigned long long)z2 & 0xFFFFFFFFull;
-          unsigned long long hi = ((unsigned long long)z3 << 32) | L2, lo = (L1 << 32) | L0;
-          const bool neg = z3 < 0;
-          if (neg) {  // two's-complement negate of the 128-bit value
-            lo = ~lo + 1;
-            hi = ~hi + (lo == 0 ? 1 : 0);
-          }
-          val[c] = u128w_scaled(hi, lo, neg, sexp + fexp[c]);
-        }
-      }
-    }
+    if (i < n && jb < kcols) crt_row4<TOP32>(R + (size_t)i * kr + jb, plane_w, cc, amax_bits[i], PA, hb, fexp, val);
 #pragma unroll
     for (int c = 0; c < 4; ++c) tile[4 * tx + c][(il + tx) & 31] = val[c];
   }
@@ -2246,6 +2339,37 @@ __device__ __forceinline__ void dft4(double2 x0, double2 x1, double2 x2, double2
   y3 = make_double2(t1.x - t3.y, t1.y + t3.x);
 }
 
+// Y = DFT_R X (R = 2, 4, 8): the R-point butterflies.
+template <int R>
+__device__ __forceinline__ void radix_butterfly(const double2 (&X)[R], double2 (&Y)[R]) {
+  if (R == 2) {
+    Y[0] = cadd(X[0], X[1]);
+    Y[1] = csub(X[0], X[1]);
+  } else if (R == 4) {
+    dft4(X[0], X[1 % R], X[2 % R], X[3 % R], Y[0], Y[1 % R], Y[2 % R], Y[3 % R]);
+  } else {
+    // w_8 = (1 - i)/sqrt(2): a_r = X_r + X_(r+4) and b_r = w_8^r (X_r - X_(r+4)) give the
+    // even outputs Y_2t = DFT4(a)_t and the odd ones Y_(2t+1) = DFT4(b)_t
+    double2 a[4], b[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      a[r] = cadd(X[r % R], X[(r + 4) % R]);
+      b[r] = csub(X[r % R], X[(r + 4) % R]);
+    }
+    const double h = 0.70710678118654752440;  // 1/sqrt(2)
+    b[1] = make_double2(h * (b[1].x + b[1].y), h * (b[1].y - b[1].x));   // * (1 - i)/sqrt(2)
+    b[2] = make_double2(b[2].y, -b[2].x);                                // * -i
+    b[3] = make_double2(h * (b[3].y - b[3].x), -h * (b[3].x + b[3].y));  // * (-1 - i)/sqrt(2)
+    dft4(a[0], a[1], a[2], a[3], Y[0], Y[2 % R], Y[4 % R], Y[6 % R]);
+    dft4(b[0], b[1], b[2], b[3], Y[1 % R], Y[3 % R], Y[5 % R], Y[7 % R]);
+  }
+}
+
+// p w, complex.
+__device__ __forceinline__ double2 twiddle(double2 p, double2 w) {
+  return make_double2(fma(p.x, w.x, -p.y * w.y), fma(p.x, w.y, p.y * w.x));
+}
+
 // C(j' + nq s, c) = sum_r w_R^(s r) X_r + beta C, X_r = w_n^(j' r) P(j', r k + c) (P already
 // carries alpha).  One thread per (j', c), j' fastest: coalesced reads of P and writes of C.
 template <int R>
@@ -2260,32 +2384,11 @@ __global__ void k_dft_radix_combine(const double2* __restrict__ P, int nq, int k
         if (r == 0) {
           X[r] = p;
         } else {
-          const double2 w = __ldg(wn + j * r);
-          X[r] = make_double2(fma(p.x, w.x, -p.y * w.y), fma(p.x, w.y, p.y * w.x));
+          X[r] = twiddle(p, __ldg(wn + j * r));
         }
       }
       double2 Y[R];
-      if (R == 2) {
-        Y[0] = cadd(X[0], X[1]);
-        Y[1] = csub(X[0], X[1]);
-      } else if (R == 4) {
-        dft4(X[0], X[1 % R], X[2 % R], X[3 % R], Y[0], Y[1 % R], Y[2 % R], Y[3 % R]);
-      } else {
-        // w_8 = (1 - i)/sqrt(2): a_r = X_r + X_(r+4) and b_r = w_8^r (X_r - X_(r+4)) give the
-        // even outputs Y_2t = DFT4(a)_t and the odd ones Y_(2t+1) = DFT4(b)_t
-        double2 a[4], b[4];
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-          a[r] = cadd(X[r % R], X[(r + 4) % R]);
-          b[r] = csub(X[r % R], X[(r + 4) % R]);
-        }
-        const double h = 0.70710678118654752440;  // 1/sqrt(2)
-        b[1] = make_double2(h * (b[1].x + b[1].y), h * (b[1].y - b[1].x));   // * (1 - i)/sqrt(2)
-        b[2] = make_double2(b[2].y, -b[2].x);                                // * -i
-        b[3] = make_double2(h * (b[3].y - b[3].x), -h * (b[3].x + b[3].y));  // * (-1 - i)/sqrt(2)
-        dft4(a[0], a[1], a[2], a[3], Y[0], Y[2 % R], Y[4 % R], Y[6 % R]);
-        dft4(b[0], b[1], b[2], b[3], Y[1 % R], Y[3 % R], Y[5 % R], Y[7 % R]);
-      }
+      radix_butterfly<R>(X, Y);
       double2* out = C + (long)c * ldc + j;
 #pragma unroll
       for (int q = 0; q < R; ++q) {
@@ -2297,6 +2400,84 @@ __global__ void k_dft_radix_combine(const double2* __restrict__ P, int nq, int k
         out[(size_t)q * nq] = y;
       }
     }
+  }
+}
+
+// The radix step's CRT, twiddles and butterflies in one pass (P = alpha F_nq B' never reaches
+// HBM).  Block (bx, by) recombines the product rows r k + c (r < R, c among the block's 32 / R
+// columns of B) over the 64 columns j' = 64 bx + ..., Re and Im (residue columns j' and
+// kr/2 + j'), into shared memory, then each thread takes one (c, j') and writes
+// C(j' + nq s, c) = sum_r w_R^(s r) w_n^(j' r) alpha P(j', r k + c) + beta C(j' + nq s, c).  The
+// CRT is integer work and the butterflies FP64 work: three blocks per SM overlap the two.
+constexpr int RDX_TJ = 64;
+template <int R, bool TOP32>
+__global__ void __launch_bounds__(256, 3) k_crt_dft_radix(const int8_t* __restrict__ Rres, int M, int nq, int kr,
+                                                       CrtConsts cc, const unsigned long long* __restrict__ amax_bits,
+                                                       const unsigned long long* __restrict__ hmax_bits,
+                                                       const SplitDevParams* prm, double alpha,
+                                                       const double2* __restrict__ wn, double beta,
+                                                       double2* __restrict__ C, long ldc, int k) {
+  constexpr int CPB = 32 / R;  // columns of B per block
+  __shared__ double2 tile[32][RDX_TJ];
+  const int tx = threadIdx.x, ty = threadIdx.y, t = ty * 32 + tx;
+  const int j0 = blockIdx.x * RDX_TJ;
+  const int PA = prm->PA, PH = prm->PH;
+  // this thread's four residue columns: j' = j0 + jl0 + e, Re (tx < 16) or Im
+  const bool im = tx >= 16;
+  const int jl0 = 4 * (tx & 15);
+  const int rc = (im ? kr / 2 : 0) + j0 + jl0;
+  unsigned long long hb[4];
+  int fexp[4];
+#pragma unroll
+  for (int e = 0; e < 4; ++e) {
+    const int j = j0 + jl0 + e;
+    hb[e] = j < nq ? hmax_bits[j] : 0ull;
+    fexp[e] = (hb[e] != 0 && hb[e] < INF_BITS) ? scale_exp(hb[e], PH) : 0;
+  }
+  const size_t plane_w = (size_t)M * kr / 4;
+  const bool scale = alpha != 1.0, accumulate = beta != 0.0;
+  for (int cb = blockIdx.y * CPB; cb < k; cb += gridDim.y * CPB) {
+    for (int a = 0; a < 4; ++a) {
+      const int il = ty + 8 * a;
+      const int c = cb + il % CPB, i = (il / CPB) * k + c;
+      double val[4] = {0.0, 0.0, 0.0, 0.0};
+      if (c < k && j0 + jl0 < nq) crt_row4<TOP32>(Rres + (size_t)i * kr + rc, plane_w, cc, amax_bits[i], PA, hb, fexp, val);
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        // rotated (selects, not a dynamic index): a warp's eight-byte stores spread over the banks
+        const int er = (e + tx) & 3;
+        double v = er == 0 ? val[0] : er == 1 ? val[1] : er == 2 ? val[2] : val[3];
+        if (scale) v *= alpha;
+        double* slot = (double*)&tile[il][jl0 + er];
+        slot[im ? 1 : 0] = v;
+      }
+    }
+    __syncthreads();
+    for (int p = t; p < CPB * RDX_TJ; p += 256) {
+      const int cl = p / RDX_TJ, jl = p % RDX_TJ;
+      const int c = cb + cl, j = j0 + jl;
+      if (c < k && j < nq) {
+        double2 X[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          const double2 v = tile[r * CPB + cl][jl];
+          X[r] = r == 0 ? v : twiddle(v, __ldg(wn + j * r));
+        }
+        double2 Y[R];
+        radix_butterfly<R>(X, Y);
+        double2* out = C + (long)c * ldc + j;
+#pragma unroll
+        for (int q = 0; q < R; ++q) {
+          double2 y = Y[q];
+          if (accumulate) {
+            const double2 o = out[(size_t)q * nq];
+            y = make_double2(fma(beta, o.x, y.x), fma(beta, o.y, y.y));
+          }
+          out[(size_t)q * nq] = y;
+        }
+      }
+    }
+    __syncthreads();  // the tile is refilled for the next columns
   }
 }
 
@@ -3407,8 +3588,10 @@ int launch_split_host_general(int M, int N, int K, double alpha, const double* A
 // kind != DFT: Q (n x k) = alpha * A (n x k) * H (k x k) + beta * Q.
 // C (n x k complex, ldc) = alpha * F * B + beta * C on the split path, F(j, l) = w^(j l): the
 // rows of the product are the k columns of B (M = k), three real products per modulus (3M).
+// src != nullptr: B is src->Bp, deinterleaved from src->B here (with the row statistics).
 static int dft3_enqueue(int M, int nn, double alpha, const double* B, long ldb, double beta, double* C, long ldc,
-                        int nmod, void* work, size_t lwork, cudaStream_t stream, SplitDevParams** prm_out) {
+                        int nmod, void* work, size_t lwork, cudaStream_t stream, SplitDevParams** prm_out,
+                        const DftRadixSrc* src = nullptr) {
   if (nmod < 8 || nmod > SPL_MAX_MODULI) return PSMMA_EUNSUPPORTED;
   if (2 * nn >= (1 << 24) || M > kSplitMaxRows) return PSMMA_EUNSUPPORTED;
   const SplitLayout L = dft3_layout(M, nn, nmod);
@@ -3419,8 +3602,21 @@ static int dft3_enqueue(int M, int nn, double alpha, const double* B, long ldb, 
 
   prof_begin(stream);
   if (cudaMemsetAsync(w, 0, L.off_wtab, stream) != cudaSuccess) return PSMMA_EDEVICE;  // params, maxima, sums
-  k_row_absmax_dft<<<M, 256, 0, stream>>>(B, 2 * ldb, nn, b.amax, b.asq);
-  prof_mark(stream, "row_scale");
+  if (src) {
+    const int gx = src->k < 8192 ? src->k : 8192;
+    if (src->R == 8)
+      k_dft_deinterleave_stats<8><<<gx, 256, 0, stream>>>(src->B, src->ldb, src->n, src->k, src->Bp, b.amax, b.asq);
+    else if (src->R == 4)
+      k_dft_deinterleave_stats<4><<<gx, 256, 0, stream>>>(src->B, src->ldb, src->n, src->k, src->Bp, b.amax, b.asq);
+    else if (src->R == 2)
+      k_dft_deinterleave_stats<2><<<gx, 256, 0, stream>>>(src->B, src->ldb, src->n, src->k, src->Bp, b.amax, b.asq);
+    else
+      return PSMMA_EUNSUPPORTED;
+    prof_mark(stream, "deinterleave_row_scale");
+  } else {
+    k_row_absmax_dft<<<M, 256, 0, stream>>>(B, 2 * ldb, nn, b.amax, b.asq);
+    prof_mark(stream, "row_scale");
+  }
   int st = launch_dft_table(b.wtab, nn, stream);
   if (st) return st;
   k_h_pass1_dft3<<<nn, 256, 0, stream>>>(b.wtab, nn, L.kp, b.Ht, b.hmax, b.hsum, b.hsq, b.prm);
@@ -3491,10 +3687,28 @@ static int dft3_enqueue(int M, int nn, double alpha, const double* B, long ldb, 
     k_crt_gemm<G_BN, OneGemm><<<std::min(sms, total_tiles), G_THREADS, Shape::SMEM, stream>>>(og);
     prof_mark(stream, p == 0 ? "gemm_T1" : p == 1 ? "gemm_T2_combine" : "gemm_T3_combine");
   }
-  dim3 gc(L.kr / CRT_TJ, (M + CRT_TI - 1) / CRT_TI);
-  (cc.top32 ? k_crt_combine<true, true> : k_crt_combine<true, false>)<<<gc, dim3(32, 8), 0, stream>>>(
-      b.R, M, nn, L.kr, cc, b.amax, b.hmax, b.prm, alpha, beta, C, 2 * ldc, 0);
-  prof_mark(stream, "crt_combine");
+  if (src) {
+    const int cpb = 32 / src->R;
+    const int by = (src->k + cpb - 1) / cpb;
+    const dim3 gr((nn + RDX_TJ - 1) / RDX_TJ, by < 65535 ? by : 65535);
+#define PSMMA_CRT_RADIX(RR, T32)                                                                             \
+  k_crt_dft_radix<RR, T32><<<gr, dim3(32, 8), 0, stream>>>(b.R, M, nn, L.kr, cc, b.amax, b.hmax, b.prm, alpha, \
+                                                          src->wn, src->beta, src->C, src->ldc, src->k)
+    if (src->R == 8) {
+      if (cc.top32) PSMMA_CRT_RADIX(8, true); else PSMMA_CRT_RADIX(8, false);
+    } else if (src->R == 4) {
+      if (cc.top32) PSMMA_CRT_RADIX(4, true); else PSMMA_CRT_RADIX(4, false);
+    } else {
+      if (cc.top32) PSMMA_CRT_RADIX(2, true); else PSMMA_CRT_RADIX(2, false);
+    }
+#undef PSMMA_CRT_RADIX
+    prof_mark(stream, "crt_radix_combine");
+  } else {
+    dim3 gc(L.kr / CRT_TJ, (M + CRT_TI - 1) / CRT_TI);
+    (cc.top32 ? k_crt_combine<true, true> : k_crt_combine<true, false>)<<<gc, dim3(32, 8), 0, stream>>>(
+        b.R, M, nn, L.kr, cc, b.amax, b.hmax, b.prm, alpha, beta, C, 2 * ldc, 0);
+    prof_mark(stream, "crt_combine");
+  }
   if (cudaGetLastError() != cudaSuccess) return PSMMA_EDEVICE;
   *prm_out = b.prm;
   return PSMMA_OK;
@@ -3518,19 +3732,14 @@ static int split_core_dft3(int k, int n, double alpha, const double* B, long ldb
     if (!work || lwork < D.total) return PSMMA_EWORKSPACE;
     char* w = (char*)work;
     double2* Bp = (double2*)(w + D.off_bp);
-    double2* P = (double2*)(w + D.off_p);
     double2* wn = (double2*)(w + D.off_w);
     const int nq = n / R;
-    st = launch_dft_deinterleave((const double2*)B, ldb, n, k, R, Bp, stream);
-    if (st) return st;
     st = launch_dft_table(wn, n, stream);
     if (st) return st;
-    st = dft3_enqueue(R * k, nq, alpha, (const double*)Bp, nq, 0.0, (double*)P, nq, nmod, work, D.core, stream,
-                      &prm);
+    const DftRadixSrc src{(const double2*)B, ldb, n, k, R, Bp, wn, beta, (double2*)C, ldc};
+    st = dft3_enqueue(R * k, nq, alpha, (const double*)Bp, nq, 0.0, nullptr, 0, nmod, work, D.core, stream, &prm,
+                      &src);
     if (st) return st;
-    st = launch_dft_radix_combine(P, nq, k, wn, beta, (double2*)C, ldc, R, stream);
-    if (st) return st;
-    prof_mark(stream, "radix_combine");
   }
   if (st) return st;
   return split_status(prm, stream, status_dev_out);
