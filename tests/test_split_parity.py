@@ -437,6 +437,31 @@ def test_split_dft_radix_rows_past_the_grid_y_limit(cuda):
     torch.cuda.empty_cache()
 
 
+@pytest.mark.parametrize("n,k", [(2050, 24), (4100, 33), (8192, 40)])
+@pytest.mark.parametrize("nmod", [10, 16])
+def test_split_dft_radix_moduli_count(n, k, nmod, cuda):
+    # radix 2 / 4 (three products, inner length 1025) and 8 (the three products in one launch,
+    # inner length 1024), each through the CRT that applies the twiddles and butterflies, with
+    # the top CRT limb in 32 bits (10 moduli) and in 64 (16)
+    B = O.cfg_matrix(n, k, seed=n + 31, complex_=True)
+    C0 = O.cfg_matrix(n, k, seed=k + 32, complex_=True)
+    got = _split_dft(n, k, 0.5, B, 1.25, C0, cuda, n_moduli=nmod)
+    err = O.rel_fro(got, O.dft_product(0.5, B, 1.25, C0))
+    assert err < {10: 1e-6, 16: 1e-14}[nmod]
+
+
+@pytest.mark.parametrize("n,k", [(1000, 17), (4100, 9), (8192, 12)])
+def test_split_dft_power_of_two_scaling_is_exact(n, k, cuda):
+    # B scaled by 2^200 shifts the row exponents only: the residues, the CRT's integers, the
+    # twiddle products and the butterflies are those of the unscaled call times 2^200, bit for bit
+    B = O.cfg_matrix(n, k, seed=n + 41, complex_=True)
+    zero = np.zeros((n, k), complex)
+    base = _split_dft(n, k, 0.75, B, 0.0, zero, cuda)
+    got = _split_dft(n, k, 0.75, B * 2.0 ** 200, 0.0, zero, cuda)
+    np.testing.assert_array_equal(got, base * 2.0 ** 200)
+    assert O.rel_fro(base, O.dft_product(0.75, B, 0.0, zero)) < TOL
+
+
 def test_split_dft_ones_fixture(cuda):
     z = np.load(GOLDEN / "dft_ones_kat.npz")
     n = int(z["n"])
