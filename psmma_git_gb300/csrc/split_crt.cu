@@ -1492,6 +1492,7 @@ struct OneGemm {
   GemmArgs g;
   static constexpr bool kGlobalMaps = false;
   static constexpr int kSub = 1;
+  static constexpr int kEpiWarps = G_EPI_WARPS;
   __device__ int total() const { return g.tiles_m * g.tiles_n * g.nmod; }
   __device__ TileInfo tile(int t) const {
     TileInfo ti;
@@ -1521,6 +1522,7 @@ struct GroupGemm {
   int count, total_tiles;
   static constexpr bool kGlobalMaps = true;
   static constexpr int kSub = 1;
+  static constexpr int kEpiWarps = G_EPI_WARPS;
   __device__ int total() const { return total_tiles; }
   __device__ TileInfo tile(int t) const {
     int lo = 0, hi = count - 1;
@@ -1550,6 +1552,9 @@ struct Gemm3M {
   GemmArgs g;
   static constexpr bool kGlobalMaps = false;
   static constexpr int kSub = 3;
+  // sixteen epilogue warps (64 columns each): the drain's residue arithmetic is the limit
+  // here, and four warps per scheduler hide its latencies better than two
+  static constexpr int kEpiWarps = 16;
   __device__ int total() const { return g.tiles_m * g.tiles_n * g.nmod; }
   __device__ TileInfo tile(int t) const {
     TileInfo ti;
@@ -1673,7 +1678,8 @@ __device__ __forceinline__ void tensormap_acquire(const CUtensorMap* m) {
 // MULTI: the block-recursive products' epilogue (GemmArgs::ndst, dst_col, ncols); without it
 // every residue goes to one place and the epilogue keeps fewer registers live.
 template <int BN, class TS, bool MULTI = false>
-__global__ void __launch_bounds__(G_THREADS, 1) k_crt_gemm(const __grid_constant__ TS ts) {
+__global__ void __launch_bounds__((TS::kEpiWarps + 2) * 32, 1) k_crt_gemm(const __grid_constant__ TS ts) {
+  constexpr int EPI = TS::kEpiWarps;  // warps 0 .. EPI-1 drain, EPI issues TMA, EPI + 1 the MMAs
   using S = GemmShape<BN>;
   extern __shared__ uint8_t smem_raw[];
   uint8_t* base = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -1698,7 +1704,7 @@ __global__ void __launch_bounds__(G_THREADS, 1) k_crt_gemm(const __grid_constant
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&acc_full[b], 1);
-      mbar_init(&acc_empty[b], G_EPI_WARPS * 32);
+      mbar_init(&acc_empty[b], EPI * 32);
     }
     mbar_init(mma_done, 1);
     // a launch whose pipeline already timed out does no further work, nor one gated off
@@ -1716,7 +1722,7 @@ __global__ void __launch_bounds__(G_THREADS, 1) k_crt_gemm(const __grid_constant
   const uint32_t tmem_base = *tmem_slot;
   const int total = *abort_flag ? 0 : ts.total();
 
-  if (warp == G_EPI_WARPS) {
+  if (warp == EPI) {
     // ---------------- TMA producer ----------------
     if (lane == 0) {
       int it = 0, issued = 0;
@@ -1752,7 +1758,7 @@ __global__ void __launch_bounds__(G_THREADS, 1) k_crt_gemm(const __grid_constant
         mbar_wait_drain(&full[q % G_STAGES], (q / G_STAGES) & 1, g.status);
     }
     __syncwarp();
-  } else if (warp == G_EPI_WARPS + 1) {
+  } else if (warp == EPI + 1) {
     // ---------------- MMA issuer ----------------
     if (lane == 0) {
       const uint32_t idesc = idesc_bf16_f32(G_BM, BN);
@@ -1792,7 +1798,9 @@ __global__ void __launch_bounds__(G_THREADS, 1) k_crt_gemm(const __grid_constant
     __syncwarp();
   } else {
     // ---------------- accumulator drain (epilogue) ----------------
-    constexpr int HALF = BN / 2;  // columns per epilogue warp
+    // warp w drains TMEM lanes 32 (w mod 4) .. +31 (its quadrant's rows) and the columns
+    // [h HALF, (h + 1) HALF) of the tile, h = w / 4
+    constexpr int HALF = BN / (EPI / 4);  // columns per epilogue warp
     const int q = warp & 3, h = warp >> 2;
     int c = 0;
     bool ok = true;
@@ -3657,7 +3665,7 @@ static int dft3_enqueue(int M, int nn, double alpha, const double* B, long ldb, 
     ga.im_off = kr1;
     for (int l = 0; l < nmod; ++l) { ga.m[l] = cc.m[l]; ga.inv_m[l] = cc.inv_m[l]; }
     const int total_tiles = ga.tiles_m * ga.tiles_n * nmod;
-    k_crt_gemm<G_BN, Gemm3M><<<std::min(sms, total_tiles), G_THREADS, Shape::SMEM, stream>>>(g3);
+    k_crt_gemm<G_BN, Gemm3M><<<std::min(sms, total_tiles), (Gemm3M::kEpiWarps + 2) * 32, Shape::SMEM, stream>>>(g3);
     prof_mark(stream, "gemm_3m");
   }
   if (L.kp / G_BK > G_CHUNK_KB && set_smem_attr(k_crt_gemm<G_BN, OneGemm>, (int)Shape::SMEM) != cudaSuccess)
