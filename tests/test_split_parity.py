@@ -450,6 +450,20 @@ def test_split_dft_radix_moduli_count(n, k, nmod, cuda):
     assert err < {10: 1e-6, 16: 1e-14}[nmod]
 
 
+@pytest.mark.parametrize("n,k", [(1000, 9), (4100, 9), (8192, 6)])
+def test_split_dft_nonfinite_column_gives_nan_column(n, k, cuda):
+    # an Inf in column 3 of B: that column of C is NaN (its product row, or with the radix
+    # step one of the R rows that each output of the column combines), the others are exact
+    B = O.cfg_matrix(n, k, seed=n + 51, complex_=True)
+    B[17, 3] = np.inf
+    C0 = O.cfg_matrix(n, k, seed=k + 52, complex_=True)
+    got = _split_dft(n, k, 0.5, B, 1.5, C0, cuda)
+    assert np.isnan(got[:, 3]).all()
+    keep = [c for c in range(k) if c != 3]
+    ref = O.dft_product(0.5, B[:, keep], 1.5, C0[:, keep])
+    assert O.rel_fro(got[:, keep], ref) < TOL
+
+
 @pytest.mark.parametrize("n,k", [(1000, 17), (4100, 9), (8192, 12)])
 def test_split_dft_power_of_two_scaling_is_exact(n, k, cuda):
     # B scaled by 2^200 shifts the row exponents only: the residues, the CRT's integers, the
