@@ -418,6 +418,10 @@ def run_gpu(args, ws, rank, local):
             result["e2e"] = {"value": flops_rank / te / 1e12, "unit": "TFLOP/s",
                              "h2d_bytes_per_step": n * k * 8 + 4 * k * 8, "d2h_bytes_per_step": n * k * 8,
                              "ms_per_step": te * 1e3, "steps": e2e_steps, "call_ms": call_ms,
+                             # the mean above keeps every call; these show how much of it is
+                             # the host link's stalls (calls above 1.25x the median)
+                             "median_call_tflops": flops_rank / (statistics.median(call_ms) * 1e-3) / 1e12,
+                             "stalled_calls": sum(c > 1.25 * statistics.median(call_ms) for c in call_ms),
                              "device_span_ms": dev_ms, "redone_calls": redo, "first_call_phases_ms": first_phases,
                              "slowest_call_phases_ms": slow[1],
                              "slowest_call_timeline_ms": slow[2],
