@@ -134,3 +134,42 @@ def test_host_split_panel_cuts():
         Qh = np.full((n, k), np.nan, order="F")
         P.psmma_cauchy(n, k, 1.0, np.asfortranarray(A), gen, 0.0, Qh, precision="split")
         assert O.rel_fro(Qh, O.dense_product("cauchy", 1.0, A, gen, 0.0, None, k)) < 1e-12
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind,n,k,levels,pad", [("cauchy", 1000, 2500, 0, 3), ("toeplitz", 700, 2000, 1, 0),
+                                                 ("hankel", 300, 4096, 2, 5)])
+def test_host_split_pinned_panels_match_pageable_and_device(kind, n, k, levels, pad):
+    # pinned host buffers with padded leading dimensions through the speculative row-panel
+    # pipeline (pitched copies of whole rows, rows past n untouched).  The repeated calls agree
+    # bit for bit, and with the pageable host call and the device call (whose row statistics
+    # are summed in other partitions) to rounding
+    import torch
+    import psmma_git_gb300 as P
+    A = O.cfg_matrix(n, k, seed=n + 71)
+    gen = np.asfortranarray(_gen(kind, k, 72))
+    fn = getattr(P, "psmma_" + kind)
+    Ap = torch.zeros((k, n + pad), dtype=torch.float64, pin_memory=True)
+    Qp = torch.zeros((k, n + pad), dtype=torch.float64, pin_memory=True)
+    Ah, Qh = Ap.numpy().T[:n], Qp.numpy().T[:n]
+    Ah[:] = A
+    Qp.numpy().T[n:] = 7.0  # rows past n must stay untouched
+    pageable = np.zeros((n, k), order="F")
+    fn(n, k, 1.25, np.asfortranarray(A), gen, 0.0, pageable, precision="split", block_levels=levels)
+    first = None
+    for _ in range(3):  # speculative calls (the pageable call was the shape's first)
+        Qh[:] = np.nan
+        fn(n, k, 1.25, Ah, gen, 0.0, Qh, precision="split", block_levels=levels)
+        if first is None:
+            first = Qh.copy()
+        np.testing.assert_array_equal(Qh, first)
+    assert O.rel_fro(Qh, pageable) < 1e-13
+    assert (Qp.numpy().T[n:] == 7.0).all()
+    dev = torch.device("cuda")
+    col = lambda x: torch.from_numpy(np.ascontiguousarray(np.asarray(x).T)).to(dev).t()  # noqa: E731
+    dg = col(gen) if kind == "cauchy" else torch.from_numpy(gen).to(dev)
+    dQ = P.fortran_empty(n, k, torch.float64, dev)
+    fn(n, k, 1.25, col(A), dg, 0.0, dQ, precision="split", block_levels=levels)
+    torch.cuda.synchronize()
+    assert O.rel_fro(Qh, dQ.cpu().numpy()) < 1e-13
+    assert O.rel_fro(Qh, O.dense_product(kind, 1.25, A, gen, 0.0, None, k)) < 1e-12
