@@ -359,8 +359,10 @@ def _split_dft(n, k, alpha, B, beta, C0, cuda, n_moduli=0, variant="pzmdftl"):
     return _np(dC)
 
 
-@pytest.mark.parametrize("n,k", [(1, 1), (3, 5), (96, 40), (250, 300), (1024, 512), (2048, 2048)])
+@pytest.mark.parametrize("n,k", [(1, 1), (3, 5), (96, 40), (250, 300), (1024, 512), (2048, 2048), (1500, 37),
+                                 (2046, 20)])
 def test_split_dft_matches_fft(n, k, cuda):
+    # (1500, 37) and (2046, 20): no radix step and an inner length of two 1024-deep chunks
     B = O.cfg_matrix(n, k, seed=n + 3, complex_=True)
     C0 = O.cfg_matrix(n, k, seed=k + 4, complex_=True)
     got = _split_dft(n, k, 0.5, B, -2.0, C0, cuda)
