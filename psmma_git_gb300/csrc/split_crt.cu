@@ -1444,8 +1444,10 @@ constexpr uint32_t G_A_BYTES = G_BM * G_BK * 2;
 struct GemmArgs {
   int n, kr, nkb, tiles_m, tiles_n, group_m, nmod;  // (a grouped launch uses group_m, nmod)
   int tm0;  // one product: first row tile of this launch (row panels)
-  // The 3M complex product (Gemm3M, Gemm3MC): the Im half of the residue planes at +im_off bytes.
-  int im_off;
+  // Epilogue of the 3M complex product (T1 = Ar Fr, T2 = Ai Fi, T3 = (Ar + Ai)(Fr + Fi)):
+  // 0 stores the residues; 1 reads T1 where it stores and writes T1 - x there and -T1 - x at
+  // +im_off bytes; 2 adds x to the residues already stored.
+  int mode, im_off;
   // Block products (MULTI): each residue goes to ndst places, place d at row dst_row[d] and
   // column dst_col[d] of planes of r_rows rows, stored (dst_op 0), added (2) or subtracted (3);
   // only the product's first ncols columns are written (ncols = 0: every column of the tile).
@@ -1491,8 +1493,6 @@ struct OneGemm {
   static constexpr bool kGlobalMaps = false;
   static constexpr int kSub = 1;
   static constexpr int kEpiWarps = G_EPI_WARPS;
-  static constexpr bool kMultiChunk = false;
-  static constexpr size_t kExtraSmem = 0;
   __device__ int total() const { return g.tiles_m * g.tiles_n * g.nmod; }
   __device__ TileInfo tile(int t) const {
     TileInfo ti;
@@ -1523,8 +1523,6 @@ struct GroupGemm {
   static constexpr bool kGlobalMaps = true;
   static constexpr int kSub = 1;
   static constexpr int kEpiWarps = G_EPI_WARPS;
-  static constexpr bool kMultiChunk = false;
-  static constexpr size_t kExtraSmem = 0;
   __device__ int total() const { return total_tiles; }
   __device__ TileInfo tile(int t) const {
     int lo = 0, hi = count - 1;
@@ -1549,10 +1547,7 @@ struct GroupGemm {
 // T3 = (Ar + Ai)(Fr + Fi); operand maps ta[p], tb[p]), each of one chunk (k <= 1024): a tile's
 // three products run back to back on the alternating accumulators and its epilogue writes
 // Re = T1 - T2 and Im = T3 - T1 - T2 (Im at +im_off bytes) once, reading no residues back.
-// MC: products deeper than one 1024 chunk; each chunk before a product's last leaves its
-// residue so far in shared memory (kExtraSmem: 16 words per epilogue thread).
-template <bool MC>
-struct Gemm3MT {
+struct Gemm3M {
   CUtensorMap ta[3], tb[3];
   GemmArgs g;
   static constexpr bool kGlobalMaps = false;
@@ -1560,8 +1555,6 @@ struct Gemm3MT {
   // sixteen epilogue warps (64 columns each): the drain's residue arithmetic is the limit
   // here, and four warps per scheduler hide its latencies better than two
   static constexpr int kEpiWarps = 16;
-  static constexpr bool kMultiChunk = MC;
-  static constexpr size_t kExtraSmem = MC ? (size_t)kEpiWarps * 32 * (G_BN / (kEpiWarps / 4) / 4) * 4 : 0;
   __device__ int total() const { return g.tiles_m * g.tiles_n * g.nmod; }
   __device__ TileInfo tile(int t) const {
     TileInfo ti;
@@ -1575,8 +1568,6 @@ struct Gemm3MT {
     return ti;
   }
 };
-using Gemm3M = Gemm3MT<false>;
-using Gemm3MC = Gemm3MT<true>;
 
 // s mod m in [-128, 127] for |s| <= 2^28 + 128 and m <= 256: the float quotient estimate is
 // within 0.3 of s / m, so q is off by at most one and one correction on each side suffices.
@@ -1633,49 +1624,39 @@ __device__ __forceinline__ float offset_byte_f(uint32_t w, int j) {
   return __fsub_rn(__uint_as_float(__byte_perm(w, 0x4B400000u, 0x7650 + j)), kRound23 + 128.0f);
 }
 
-// One chunk's drain in the epilogue of the multi-chunk 3M products (Gemm3MC), 32 columns per
-// TMEM load, residues on the FP32 pipe from the chunk's exact sums v.  ADD: the residue of the
-// product's earlier chunks (word w of this thread's carry at cy[w * CS]) is added.  KIND 0:
-// the residue so far to the carry (a chunk before the last); 1: p1 = T1; 2: Re = x1 - T2
-// stored, ps = -x1 - T2; 3: Im = s + T3 stored.  Kept residues are bytes offset by 128.
-template <int KIND, bool ADD, int HALF, int CS>
-__device__ __forceinline__ void drain3m(uint32_t taddr, uint32_t (&p1)[HALF / 4], uint32_t (&ps)[HALF / 4],
-                                        uint32_t* cy, float mf, float inv_m, int8_t* out, bool store) {
+// Epilogue of the 3M complex product's second and third GEMMs: combine this tile's residues x
+// (in [-128, 127]) with those already in the output plane, 16 bytes at a time.
+// mode 1: old = T1 -> store (T1 - x) mod m, and (-T1 - x) mod m at dst + im_off;
+// mode 2: old = -T1 - T2 -> store (old + x) mod m.
+// Only the first `valid` columns (a multiple of 16) are touched.
+template <int HALF>
+__device__ __forceinline__ void store_combined(int8_t* dst, const int (&res)[HALF], int mode, int im_off, int m,
+                                               int valid = HALF) {
+  // every 16-byte load issued before the first store (the stores at dst + im_off may alias the
+  // later loads for all the compiler knows, which would serialise the round trips)
+  uint4 ov[HALF / 16];
 #pragma unroll
-  for (int cb = 0; cb < HALF / 32; ++cb) {
-    uint32_t r[32];
-    tmem_ld32(taddr + (uint32_t)(cb * 32), r);
-    tmem_ld_wait();
-    uint32_t wa[8];
+  for (int v = 0; v < HALF / 16; ++v) ov[v] = v * 16 < valid ? *(const uint4*)(dst + v * 16) : make_uint4(0u, 0u, 0u, 0u);
 #pragma unroll
-    for (int e4 = 0; e4 < 8; ++e4) {
-      const int w = cb * 8 + e4;
-      const uint32_t pw = ADD ? cy[w * CS] : 0u;
-      uint32_t ba[4], bs[4];
+  for (int v = 0; v < HALF / 16; ++v) {
+    if (v * 16 >= valid) break;
+    const uint32_t ow[4] = {ov[v].x, ov[v].y, ov[v].z, ov[v].w};
+    uint32_t w1[4], w2[4];
+#pragma unroll
+    for (int t4 = 0; t4 < 4; ++t4) {
+      w1[t4] = 0u;
+      w2[t4] = 0u;
 #pragma unroll
       for (int bb = 0; bb < 4; ++bb) {
-        const float v = __uint_as_float(r[4 * e4 + bb]);
-        const float part = ADD ? offset_byte_f(pw, bb) : 0.0f;  // the earlier chunks
-        if (KIND <= 1) {
-          ba[bb] = ADD ? mod_sym_f_bits_add(v, part, mf, inv_m) : mod_sym_f_bits(v, mf, inv_m);
-        } else if (KIND == 2) {
-          const float x1 = offset_byte_f(p1[w], bb);
-          ba[bb] = mod_sym_f_bits_add(-v, ADD ? x1 - part : x1, mf, inv_m);    // x1 - T2
-          bs[bb] = mod_sym_f_bits_add(-v, ADD ? -x1 - part : -x1, mf, inv_m);  // -x1 - T2
-        } else {
-          const float sv = offset_byte_f(ps[w], bb);
-          ba[bb] = mod_sym_f_bits_add(v, ADD ? sv + part : sv, mf, inv_m);  // s + T3
-        }
+        const int old = (int)(int8_t)(ow[t4] >> (8 * bb));
+        const int x = res[v * 16 + t4 * 4 + bb];
+        const int a = mod_sym_small(mode == 1 ? old - x : old + x, m);
+        w1[t4] |= (uint32_t)(uint8_t)(int8_t)a << (8 * bb);
+        if (mode == 1) w2[t4] |= (uint32_t)(uint8_t)(int8_t)mod_sym_small(-old - x, m) << (8 * bb);
       }
-      wa[e4] = pack_low_bytes(ba[0], ba[1], ba[2], ba[3]);
-      if (KIND == 0) cy[w * CS] = wa[e4] ^ 0x80808080u;
-      if (KIND == 1) p1[w] = wa[e4] ^ 0x80808080u;
-      if (KIND == 2) ps[w] = pack_low_bytes(bs[0], bs[1], bs[2], bs[3]) ^ 0x80808080u;
     }
-    if (KIND >= 2 && store) {
-      *(uint4*)(out + cb * 32) = make_uint4(wa[0], wa[1], wa[2], wa[3]);
-      *(uint4*)(out + cb * 32 + 16) = make_uint4(wa[4], wa[5], wa[6], wa[7]);
-    }
+    *(uint4*)(dst + v * 16) = make_uint4(w1[0], w1[1], w1[2], w1[3]);
+    if (mode == 1) *(uint4*)(dst + im_off + v * 16) = make_uint4(w2[0], w2[1], w2[2], w2[3]);
   }
 }
 
@@ -1712,7 +1693,6 @@ __global__ void __launch_bounds__((TS::kEpiWarps + 2) * 32, 1) k_crt_gemm(const 
   uint64_t* mma_done = acc_empty + 2;
   uint32_t* tmem_slot = (uint32_t*)(mma_done + 1);
   volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
-  uint32_t* carry = (uint32_t*)((uint8_t*)bars + 256);  // TS::kExtraSmem bytes (Gemm3MC)
   const GemmArgs& g = ts.g;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1829,48 +1809,7 @@ __global__ void __launch_bounds__((TS::kEpiWarps + 2) * 32, 1) k_crt_gemm(const 
       const int cpt = (ti.nkb + G_CHUNK_KB - 1) / G_CHUNK_KB;
       const int mi = g.m[ti.l];
       const float inv_m = g.inv_m[ti.l];
-      if constexpr (TS::kSub == 3 && TS::kMultiChunk) {
-        // as the one-chunk form below, the chunks before each product's last carrying its
-        // residue so far in shared memory (a loop of their own; the last chunk's drain, which
-        // also uses T1's and s's kept residues, outside it)
-        const int i = ti.tm * G_BM + q * 32 + lane;
-        const int col0 = ti.tn * BN + h * HALF;
-        const float mf = (float)mi;
-        int8_t* dst = ti.R + ((size_t)ti.l * ti.n + (size_t)min(i, ti.n - 1)) * ti.kr + (size_t)col0;
-        constexpr int CS = EPI * 32;  // the carry's word stride
-        uint32_t* cy = carry + threadIdx.x;
-        uint32_t p1[HALF / 4], ps[HALF / 4];
-        // one chunk: wait for its accumulator, drain it (the arguments), hand the accumulator back
-#define PSMMA_3M_CHUNK(...)                                                                                \
-  {                                                                                                        \
-    const int buf = c & 1;                                                                                 \
-    const uint32_t use = (uint32_t)(c >> 1);                                                               \
-    if (!mbar_wait(&acc_full[buf], use & 1, g.status, abort_flag)) {                                       \
-      ok = false;                                                                                          \
-    } else {                                                                                               \
-      ++c;                                                                                                 \
-      tc_fence_after();                                                                                    \
-      const uint32_t taddr = tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(buf * BN + h * HALF);     \
-      __VA_ARGS__;                                                                                         \
-      tc_fence_before();                                                                                   \
-      mbar_arrive(&acc_empty[buf]);                                                                        \
-    }                                                                                                      \
-  }
-#define PSMMA_3M_PRODUCT(FIN)                                                                              \
-  for (int cc = 0; cc < cpt - 1 && ok; ++cc)                                                               \
-    PSMMA_3M_CHUNK(if (cc == 0) drain3m<0, false, HALF, CS>(taddr, p1, ps, cy, mf, inv_m, dst, false);     \
-                   else drain3m<0, true, HALF, CS>(taddr, p1, ps, cy, mf, inv_m, dst, false))              \
-  if (ok)                                                                                                  \
-    PSMMA_3M_CHUNK(const bool store = !*abort_flag && i < ti.n;                                            \
-                   int8_t* out = dst + (FIN == 3 ? g.im_off : 0);                                          \
-                   if (cpt == 1) drain3m<FIN, false, HALF, CS>(taddr, p1, ps, cy, mf, inv_m, out, store);  \
-                   else drain3m<FIN, true, HALF, CS>(taddr, p1, ps, cy, mf, inv_m, out, store))
-        PSMMA_3M_PRODUCT(1)
-        if (ok) { PSMMA_3M_PRODUCT(2) }
-        if (ok) { PSMMA_3M_PRODUCT(3) }
-#undef PSMMA_3M_PRODUCT
-#undef PSMMA_3M_CHUNK
-      } else if constexpr (TS::kSub == 3) {
+      if constexpr (TS::kSub == 3) {
         // T1 -> x1 (kept); T2 -> Re = x1 - T2 (stored) and s = -x1 - T2 (kept); T3 -> Im = s + T3
         // (stored).  Residues on the FP32 pipe from the exact sums; kept residues are bytes
         // offset by 128, four to a word.  The epilogue work is spread over the three drains,
@@ -1975,7 +1914,7 @@ __global__ void __launch_bounds__((TS::kEpiWarps + 2) * 32, 1) k_crt_gemm(const 
             for (int d = 0; d < nd; ++d) {
               int8_t* dst = ti.R + ((size_t)ti.l * plane_rows + i + (g.ndst > 0 ? g.dst_row[d] : 0)) * ti.kr +
                             (size_t)col0 + (g.ndst > 0 ? g.dst_col[d] : 0);
-              const int op = g.ndst > 0 ? g.dst_op[d] : 0;
+              const int op = g.ndst > 0 ? g.dst_op[d] : g.mode;
               if (op >= 2) {
                 uint4 o[HALF / 16];
 #pragma unroll
@@ -2013,6 +1952,10 @@ __global__ void __launch_bounds__((TS::kEpiWarps + 2) * 32, 1) k_crt_gemm(const 
         const int nd = 1;
         for (int d = 0; d < nd && ok && !*abort_flag && i < ti.n && valid > 0; ++d) {
           int8_t* dst = ti.R + ((size_t)ti.l * ti.n + i) * ti.kr + (size_t)col0;
+          if (g.mode != 0) {
+            store_combined<HALF>(dst, res, g.mode, g.im_off, mi, valid);
+            continue;
+          }
 #pragma unroll
           for (int v = 0; v < HALF / 16; ++v) {
             if (v * 16 >= valid) break;
@@ -3701,12 +3644,10 @@ static int dft3_enqueue(int M, int nn, double alpha, const double* B, long ldb, 
   if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
     return PSMMA_EDEVICE;
   const int kr1 = L.kr / 2;
-  // the three products in one launch, Re and Im written once (Gemm3MC when a product spans
-  // more than one 1024-deep chunk)
-  auto launch_3m = [&](auto g3) -> int {
-    using T3 = decltype(g3);
-    const int smem = (int)(Shape::SMEM + T3::kExtraSmem);
-    if (set_smem_attr(k_crt_gemm<G_BN, T3>, smem) != cudaSuccess) return PSMMA_EDEVICE;
+  if (L.kp / G_BK <= G_CHUNK_KB) {
+    // one chunk per product: the three products in one launch, Re and Im written once
+    if (set_smem_attr(k_crt_gemm<G_BN, Gemm3M>, (int)Shape::SMEM) != cudaSuccess) return PSMMA_EDEVICE;
+    Gemm3M g3;
     memset(&g3, 0, sizeof(g3));
     for (int p = 0; p < 3; ++p)
       if (!make_tmap(&g3.ta[p], b.RA + (size_t)p * nmod * M * L.kp, L.kp, M, nmod, G_BM) ||
@@ -3725,12 +3666,36 @@ static int dft3_enqueue(int M, int nn, double alpha, const double* B, long ldb, 
     ga.im_off = kr1;
     for (int l = 0; l < nmod; ++l) { ga.m[l] = cc.m[l]; ga.inv_m[l] = cc.inv_m[l]; }
     const int total_tiles = ga.tiles_m * ga.tiles_n * nmod;
-    k_crt_gemm<G_BN, T3><<<std::min(sms, total_tiles), (T3::kEpiWarps + 2) * 32, smem, stream>>>(g3);
+    k_crt_gemm<G_BN, Gemm3M><<<std::min(sms, total_tiles), (Gemm3M::kEpiWarps + 2) * 32, Shape::SMEM, stream>>>(g3);
     prof_mark(stream, "gemm_3m");
-    return PSMMA_OK;
-  };
-  const int st3 = L.kp / G_BK <= G_CHUNK_KB ? launch_3m(Gemm3M{}) : launch_3m(Gemm3MC{});
-  if (st3) return st3;
+  }
+  if (L.kp / G_BK > G_CHUNK_KB && set_smem_attr(k_crt_gemm<G_BN, OneGemm>, (int)Shape::SMEM) != cudaSuccess)
+    return PSMMA_EDEVICE;
+  // T1 into the Re half; T2: Re = T1 - T2, Im = -T1 - T2; T3: Im += T3
+  for (int p = 0; p < 3 && L.kp / G_BK > G_CHUNK_KB; ++p) {
+    OneGemm og;
+    memset(&og, 0, sizeof(og));
+    __nv_bfloat16* ra = b.RA + (size_t)p * nmod * M * L.kp;
+    __nv_bfloat16* rh = b.RH + (size_t)p * nmod * nn * L.kp;
+    if (!make_tmap(&og.ta, ra, L.kp, M, nmod, G_BM) || !make_tmap(&og.tb, rh, L.kp, nn, nmod, G_BN))
+      return PSMMA_EDEVICE;
+    GemmArgs& ga = og.g;
+    ga.n = M;
+    ga.kr = L.kr;
+    ga.nkb = L.kp / G_BK;
+    ga.tiles_m = (M + G_BM - 1) / G_BM;
+    ga.tiles_n = (nn + G_BN - 1) / G_BN;
+    ga.group_m = 16;
+    ga.R = b.R + (p == 2 ? kr1 : 0);
+    ga.status = &b.prm->status;
+    ga.nmod = nmod;
+    ga.mode = p;
+    ga.im_off = kr1;
+    for (int l = 0; l < nmod; ++l) { ga.m[l] = cc.m[l]; ga.inv_m[l] = cc.inv_m[l]; }
+    const int total_tiles = ga.tiles_m * ga.tiles_n * nmod;
+    k_crt_gemm<G_BN, OneGemm><<<std::min(sms, total_tiles), G_THREADS, Shape::SMEM, stream>>>(og);
+    prof_mark(stream, p == 0 ? "gemm_T1" : p == 1 ? "gemm_T2_combine" : "gemm_T3_combine");
+  }
   if (src) {
     const int cpb = 32 / src->R;
     const int by = (src->k + cpb - 1) / cpb;
