@@ -2414,7 +2414,7 @@ __global__ void k_dft_radix_combine(const double2* __restrict__ P, int nq, int k
 // The radix step's CRT, twiddles and butterflies in one pass (P = alpha F_nq B' never reaches
 // HBM).  Block (bx, by) recombines the product rows r k + c (r < R, c among the block's 32 / R
 // columns of B) over the 64 columns j' = 64 bx + ..., Re and Im (residue columns j' and
-// kr/2 + j'), into shared memory, then each thread takes one (c, j') and writes
+// kr/2 + j'), into shared memory, then each thread takes (c, j') pairs in turn and writes
 // C(j' + nq s, c) = sum_r w_R^(s r) w_n^(j' r) alpha P(j', r k + c) + beta C(j' + nq s, c).  The
 // CRT is integer work and the butterflies FP64 work: four blocks per SM (64 registers, a few
 // spilled) overlap the two better than three at 74 registers (n = 8192: 2.23 -> 1.98 ms).
